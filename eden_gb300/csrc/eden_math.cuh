@@ -1,0 +1,48 @@
+// Device-side arithmetic of the simulation step, shared by the per-step and
+// the windowed kernels.  Every expression keeps the operation order of the
+// reference's generated C so single-precision results stay within rounding
+// of it (the reference compiles with -Ofast, so bit equality is not defined).
+#pragma once
+#include <cstdint>
+
+#include "../../include/eden_gpu.h"
+
+namespace eden {
+
+// Thomas Wang's 64-bit integer hash (eden/Eden.cpp:3199-3213).
+__device__ __forceinline__ uint64_t hash64shift(uint64_t key) {
+    key = (~key) + (key << 21);
+    key = key ^ (key >> 24);
+    key = (key + (key << 3)) + (key << 8);
+    key = key ^ (key >> 14);
+    key = (key + (key << 2)) + (key << 4);
+    key = key ^ (key >> 28);
+    key = key + (key << 31);
+    return key;
+}
+
+// randof(x, work_item, instance, step, invocation) (eden/Eden.cpp:3216-3233):
+// 24 bits of instance, 40 bits of step, hashed 128 -> 64 bits, 23-bit mantissa.
+__device__ __forceinline__ float randof(float x, int64_t work_item, int64_t instance, int64_t step,
+                                        int invocation_id) {
+    uint64_t hi = ((uint64_t)work_item << 24) | ((uint64_t)instance & ((1ULL << 24) - 1));
+    uint64_t lo = ((uint64_t)(int64_t)invocation_id << 40) | ((uint64_t)step & ((1ULL << 40) - 1));
+    uint64_t sample = hash64shift(hash64shift(lo) ^ hi);
+    const int scale = 1 << 23;
+    float r = (float)(uint32_t)(sample & (uint64_t)(scale - 1)) / (float)scale;
+    return x * r;
+}
+
+// HH rate forms (eden/Eden.cpp:5164-5181).
+__device__ __forceinline__ float rate_value(int kind, float r, float mid, float s, float v) {
+    if (kind == EDEN_RATE_EXP) return r * expf((v - mid) / s);
+    if (kind == EDEN_RATE_EXPLINEAR)
+        return r * ((v == mid) ? 1.0f : (((v - mid) / s) / (1.0f - expf(-(v - mid) / s))));
+    return r / (1.0f + expf((mid - v) / s));
+}
+
+// Channel type table in constant memory (a handful of ionChannelHH types).
+constexpr int kMaxChanTypes = 32;
+constexpr int kMaxSynTypes = 32;
+
+}  // namespace eden

@@ -1,0 +1,462 @@
+"""Lower a NetworkSpec into the engine-unit arrays of `EdenGpuModel`.
+
+This mirrors what the reference's GenerateModel() computes for the
+mechanisms of this path (eden/Eden.cpp:677-10378), with single precision
+where the reference stores `Real` (float):
+
+* units: quantities are converted as ScaleEntry::ConvertTo does
+  (eden/NeuroML.h:530-532): value * 10^(pow_from - pow_native) in double,
+  then stored as float.  Engine units are us, mV, nA, pF, uS, Mohm, um
+  (eden/NeuroML.cpp:307-400);
+* compartments: one per segment, in segment order; area of a cylinder
+  pi*d*L, of a zero-length segment pi*d^2 (GeomHelp::Area,
+  eden/Eden.cpp:242-252); capacitance = Cm * area
+  (eden/Eden.cpp:4222-4226); axial resistance between a compartment and its
+  parent = proximal half of the child + distal half of the parent, each
+  Ra*(4/pi)*len/(d_from*d_to) (eden/Eden.cpp:4228-4241, 4256-4308,
+  4340-4347); the fixed diagonal sum of 1/(R*C) over neighbours
+  (eden/Eden.cpp:4488-4501);
+* per-cell RNG seed reverse_bits(seed) ^ gid (eden/Eden.cpp:7672-7691);
+* expTwoSynapse's derived peakTime / waveformFactor evaluated in float
+  the way the generated code does (LEMS_CoreComponents.inc.xml:152-153).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .network import (Izhikevich2007Cell, NetworkSpec, PhysicalCell,
+                      SYN_EXPONE, SYN_EXPTWO)
+
+F32 = np.float32
+MAX_GATES = 4
+
+
+def _to_f32(x) -> np.float32:
+    return F32(float(x))
+
+
+def ms_to_us(x):
+    return np.asarray(x, dtype=np.float64) * 1000.0
+
+
+def reverse_bits32(x: int) -> int:
+    x &= 0xFFFFFFFF
+    x = ((x & 0xFFFF0000) >> 16) | ((x & 0x0000FFFF) << 16)
+    x = ((x & 0xFF00FF00) >> 8) | ((x & 0x00FF00FF) << 8)
+    x = ((x & 0xF0F0F0F0) >> 4) | ((x & 0x0F0F0F0F) << 4)
+    x = ((x & 0xCCCCCCCC) >> 2) | ((x & 0x33333333) << 2)
+    x = ((x & 0xAAAAAAAA) >> 1) | ((x & 0x55555555) << 1)
+    return x & 0xFFFFFFFF
+
+
+def cell_seeds(seed: int, n: int) -> np.ndarray:
+    r = reverse_bits32(int(seed) & 0xFFFFFFFF)
+    s = (np.uint32(r) ^ np.arange(n, dtype=np.uint32)).astype(np.uint32)
+    return s.view(np.int32)
+
+
+def exptwo_waveform_factor(tau_rise_us: float, tau_decay_us: float) -> np.float32:
+    """peakTime and waveformFactor in float, as the generated kernel
+    evaluates LEMS_CoreComponents.inc.xml:152-153."""
+    tr, td = F32(tau_rise_us), F32(tau_decay_us)
+    with np.errstate(all="ignore"):
+        tp = F32(F32(F32(np.log(F32(td / tr))) * F32(F32(tr * td) * F32(1e-12))) / F32(td - tr)) * F32(1e12)
+        tp = F32(tp)
+        wf = F32(1.0) / F32(-np.exp(F32(-tp / tr)) + np.exp(F32(-tp / td)))
+    return F32(wf)
+
+
+# ---------------------------------------------------------------------------
+@dataclass
+class LoweredModel:
+    dt: np.float32
+    seed: int
+    n_steps: int
+    # physical
+    phys_comp_off: np.ndarray
+    comp_parent: np.ndarray
+    comp_c: np.ndarray
+    comp_r_axial: np.ndarray
+    comp_area: np.ndarray
+    comp_inv_rc: np.ndarray
+    comp_v0: np.ndarray
+    chan_types: np.ndarray        # structured, see CHAN_DTYPE
+    comp_chan_off: np.ndarray
+    chan_type: np.ndarray
+    chan_gbase: np.ndarray
+    chan_erev: np.ndarray
+    # point neurons
+    izh_params: np.ndarray        # [n_izh, 10]
+    # spike sources (one per gid)
+    src_target: np.ndarray
+    src_threshold: np.ndarray
+    src_cell_seed: np.ndarray
+    # synapses
+    syn_types: np.ndarray         # structured, see SYN_DTYPE
+    syn_target: np.ndarray
+    syn_type: np.ndarray
+    syn_src: np.ndarray
+    syn_weight: np.ndarray
+    syn_delay: np.ndarray
+    # poisson
+    pois_target: np.ndarray
+    pois_type: np.ndarray
+    pois_rate: np.ndarray
+    pois_weight: np.ndarray
+    pois_src: np.ndarray
+    pois_instance: np.ndarray
+    # pulses
+    pulse_target: np.ndarray
+    pulse_start: np.ndarray
+    pulse_duration: np.ndarray
+    pulse_amplitude: np.ndarray
+    pulse_weight: np.ndarray
+    # recording
+    trace_target: np.ndarray
+    event_src: np.ndarray         # spike source recorded by each EventSelection
+    # bookkeeping
+    gid_target_base: np.ndarray = field(default=None)  # first target of each gid
+
+    @property
+    def n_comp(self) -> int:
+        return int(len(self.comp_c))
+
+    @property
+    def n_izh(self) -> int:
+        return int(len(self.izh_params))
+
+    @property
+    def n_target(self) -> int:
+        return self.n_comp + self.n_izh
+
+    @property
+    def n_phys(self) -> int:
+        return int(len(self.phys_comp_off) - 1)
+
+
+CHAN_DTYPE = np.dtype([
+    ("n_gates", np.int32), ("gate_instances", np.int32, MAX_GATES),
+    ("fwd_kind", np.int32, MAX_GATES), ("fwd_rate", np.float32, MAX_GATES),
+    ("fwd_mid", np.float32, MAX_GATES), ("fwd_scale", np.float32, MAX_GATES),
+    ("rev_kind", np.int32, MAX_GATES), ("rev_rate", np.float32, MAX_GATES),
+    ("rev_mid", np.float32, MAX_GATES), ("rev_scale", np.float32, MAX_GATES),
+    ("q10", np.float32, MAX_GATES),
+], align=True)
+
+SYN_DTYPE = np.dtype([
+    ("kind", np.int32), ("gbase", np.float32), ("erev", np.float32),
+    ("tau_decay", np.float32), ("tau_rise", np.float32),
+    ("waveform_factor", np.float32), ("weight_prop", np.float32),
+], align=True)
+
+
+def _cable_geometry(cell: PhysicalCell):
+    """Per-compartment C (pF), R to parent (Mohm), area (um2), sum 1/(RC)."""
+    n = cell.n_seg
+    L = np.asarray(cell.seg_len, np.float64)
+    d = np.asarray(cell.seg_diam, np.float64)
+    # floats of the XML coordinates, as the reference parses them
+    area = np.where(L == 0, np.pi * d * d, (np.pi / 2.0) * (d + d) * np.sqrt(L * L)).astype(F32)
+    cm_native = _to_f32(cell.cm)                      # uF/cm2, native
+    c = (area.astype(np.float64) * float(cm_native) * 1e-2).astype(F32)
+    ra_native = _to_f32(cell.ra * 1e-3)               # ohm*cm -> kohm*cm
+    half = np.where(L == 0, d / 2.0, L / 2.0)
+    r_half = (float(ra_native) * (4.0 / np.pi) * half / (d * d) * 10.0).astype(F32)
+    r_prox, r_dist = r_half, r_half
+    parent = np.asarray(cell.seg_parent, np.int64)
+    r_axial = np.full(n, np.nan, dtype=F32)
+    for i in range(n):
+        p = parent[i]
+        if p >= 0:
+            r_axial[i] = F32(r_prox[i] + r_dist[p])
+    inv_rc = np.zeros(n, dtype=F32)
+    for i in range(n):
+        p = parent[i]
+        if p >= 0:
+            # edge (i, p) contributes to both ends; index by the child
+            inv_rc[i] = F32(inv_rc[i] + F32(1.0 / (float(r_axial[i]) * float(c[i]))))
+            inv_rc[p] = F32(inv_rc[p] + F32(1.0 / (float(r_axial[i]) * float(c[p]))))
+    return c, r_axial, area, inv_rc
+
+
+def lower(spec: NetworkSpec) -> LoweredModel:
+    dt = _to_f32(spec.dt * 1000.0)
+    gid_off = spec.pop_offsets()
+    n_cells = spec.n_cells
+
+    # ---- channel types ------------------------------------------------------
+    chan_types = np.zeros(len(spec.channels), dtype=CHAN_DTYPE)
+    for k, ch in enumerate(spec.channels):
+        ct = chan_types[k]
+        if len(ch.gates) > MAX_GATES:
+            raise ValueError(f"channel {ch.name}: more than {MAX_GATES} gates")
+        ct["n_gates"] = len(ch.gates)
+        for g, gate in enumerate(ch.gates):
+            ct["gate_instances"][g] = gate.instances
+            ct["fwd_kind"][g] = gate.forward.kind
+            ct["fwd_rate"][g] = _to_f32(gate.forward.rate * 1e-3)   # per_ms -> per_us
+            ct["fwd_mid"][g] = _to_f32(gate.forward.midpoint)
+            ct["fwd_scale"][g] = _to_f32(gate.forward.scale)
+            ct["rev_kind"][g] = gate.reverse.kind
+            ct["rev_rate"][g] = _to_f32(gate.reverse.rate * 1e-3)
+            ct["rev_mid"][g] = _to_f32(gate.reverse.midpoint)
+            ct["rev_scale"][g] = _to_f32(gate.reverse.scale)
+            ct["q10"][g] = 1.0
+
+    # ---- cells, in gid order ------------------------------------------------
+    phys_off = [0]
+    comp_parent, comp_c, comp_r, comp_area, comp_inv, comp_v0 = [], [], [], [], [], []
+    chan_off = [0]
+    chan_type, chan_g, chan_e = [], [], []
+    izh = []
+    src_target = np.zeros(n_cells, np.int32)
+    src_thr = np.full(n_cells, np.nan, np.float32)
+    gid_base = np.zeros(n_cells, np.int64)
+    gid_is_izh = np.zeros(n_cells, bool)
+    izh_index = np.full(n_cells, -1, np.int64)
+    geom_cache = {}
+    gid = 0
+    for pop in spec.populations:
+        ct = spec.cell_type(pop.cell_type)
+        for _ in range(pop.size):
+            if isinstance(ct, PhysicalCell):
+                if ct.name not in geom_cache:
+                    geom_cache[ct.name] = _cable_geometry(ct)
+                c, r, a, inv = geom_cache[ct.name]
+                base = phys_off[-1]
+                gid_base[gid] = base
+                comp_parent.append(np.asarray(ct.seg_parent, np.int32))
+                comp_c.append(c)
+                comp_r.append(r)
+                comp_area.append(a)
+                comp_inv.append(inv)
+                comp_v0.append(np.full(ct.n_seg, _to_f32(ct.v0), np.float32))
+                for s in range(ct.n_seg):
+                    for dens in ct.densities:
+                        if dens.seg_mask[s]:
+                            chan_type.append(dens.channel)
+                            chan_g.append(dens.cond)
+                            chan_e.append(dens.erev)
+                    chan_off.append(len(chan_type))
+                phys_off.append(base + ct.n_seg)
+                src_target[gid] = base  # segment 0 detects spikes
+                src_thr[gid] = _to_f32(ct.spike_thresh)
+            elif isinstance(ct, Izhikevich2007Cell):
+                gid_is_izh[gid] = True
+                izh_index[gid] = len(izh)
+                izh.append([ct.C, ct.v0, ct.k, ct.vr, ct.vt, ct.vpeak,
+                            ct.a * 1e-3, ct.b * 1e-3, ct.c, ct.d * 1e-3])
+            else:
+                raise ValueError(f"unsupported cell type {type(ct).__name__}")
+            gid += 1
+    n_comp = phys_off[-1]
+    for g in np.nonzero(gid_is_izh)[0]:
+        gid_base[g] = n_comp + izh_index[g]
+        src_target[g] = n_comp + izh_index[g]
+
+    def target_of(gids, segs):
+        gids = np.asarray(gids, np.int64)
+        segs = np.asarray(segs, np.int64)
+        t = gid_base[gids] + np.where(gid_is_izh[gids], 0, segs)
+        return t.astype(np.int32)
+
+    # ---- synapse types --------------------------------------------------------
+    syn_types = np.zeros(len(spec.synapses), dtype=SYN_DTYPE)
+    syn_index = {}
+    for k, s in enumerate(spec.synapses):
+        syn_index[s.name] = k
+        st = syn_types[k]
+        st["kind"] = s.kind
+        st["gbase"] = _to_f32(s.gbase * 1e-3)     # nS -> uS
+        st["erev"] = _to_f32(s.erev)
+        st["tau_decay"] = _to_f32(s.tau_decay * 1000.0)
+        st["tau_rise"] = _to_f32(s.tau_rise * 1000.0) if s.kind == SYN_EXPTWO else 0.0
+        st["waveform_factor"] = (exptwo_waveform_factor(st["tau_rise"], st["tau_decay"])
+                                 if s.kind == SYN_EXPTWO else 1.0)
+        st["weight_prop"] = 1.0
+
+    # ---- connection synapses: grouped per target, type order, then connection order
+    tgt, typ, src, wgt, dly, order_key = [], [], [], [], [], []
+    seq = 0
+    for pr in spec.projections:
+        k = syn_index[pr.synapse]
+        n = len(pr.pre_cell)
+        tgt.append(target_of(pr.post_cell, pr.post_seg))
+        typ.append(np.full(n, k, np.int32))
+        src.append(np.asarray(pr.pre_cell, np.int32))
+        wgt.append(np.asarray(pr.weight, np.float64).astype(F32))
+        dly.append(ms_to_us(pr.delay).astype(F32))
+        order_key.append(np.arange(seq, seq + n, dtype=np.int64))
+        seq += n
+    if tgt:
+        tgt = np.concatenate(tgt); typ = np.concatenate(typ); src = np.concatenate(src)
+        wgt = np.concatenate(wgt); dly = np.concatenate(dly); order_key = np.concatenate(order_key)
+        perm = np.lexsort((order_key, typ, tgt))
+        tgt, typ, src, wgt, dly = tgt[perm], typ[perm], src[perm], wgt[perm], dly[perm]
+    else:
+        tgt = np.zeros(0, np.int32); typ = np.zeros(0, np.int32); src = np.zeros(0, np.int32)
+        wgt = np.zeros(0, F32); dly = np.zeros(0, F32)
+
+    # ---- poisson inputs -----------------------------------------------------
+    pt, pty, pr_, pw, ps, pinst = [], [], [], [], [], []
+    for po in spec.poissons:
+        k = syn_index[po.synapse]
+        cells = np.asarray(po.cell, np.int64)
+        segs = np.asarray(po.seg, np.int64)
+        t = target_of(cells, segs)
+        # instance number within each (cell, compartment) table, in input order
+        inst = np.zeros(len(cells), np.int32)
+        counter = {}
+        for i in range(len(cells)):
+            key = int(t[i])
+            inst[i] = counter.get(key, 0)
+            counter[key] = inst[i] + 1
+        pt.append(t); pty.append(np.full(len(cells), k, np.int32))
+        pr_.append(np.full(len(cells), _to_f32(po.rate * 1e-6), F32))
+        pw.append(np.ones(len(cells), F32)); ps.append(cells.astype(np.int32)); pinst.append(inst)
+    cat = lambda xs, dt_: (np.concatenate(xs) if xs else np.zeros(0, dt_))
+    pt, pty, pr_, pw, ps, pinst = (cat(pt, np.int32), cat(pty, np.int32), cat(pr_, F32),
+                                   cat(pw, F32), cat(ps, np.int32), cat(pinst, np.int32))
+    if len(pt):
+        perm = np.argsort(pt, kind="stable")
+        pt, pty, pr_, pw, ps, pinst = pt[perm], pty[perm], pr_[perm], pw[perm], ps[perm], pinst[perm]
+
+    # ---- pulses ---------------------------------------------------------------
+    qt, qs, qd, qa = [], [], [], []
+    for pu in spec.pulses:
+        qt.append(target_of(pu.cell, pu.seg))
+        qs.append(ms_to_us(pu.delay).astype(F32))
+        qd.append(ms_to_us(pu.duration).astype(F32))
+        qa.append(np.asarray(pu.amplitude, np.float64).astype(F32))
+    qt, qs, qd, qa = cat(qt, np.int32), cat(qs, F32), cat(qd, F32), cat(qa, F32)
+    if len(qt):
+        perm = np.argsort(qt, kind="stable")
+        qt, qs, qd, qa = qt[perm], qs[perm], qd[perm], qa[perm]
+
+    trace_target = np.array([target_of([gid_off[c.pop] + c.cell], [c.seg])[0]
+                             for c in spec.trace_columns], dtype=np.int32)
+    event_src = np.array([gid_off[e.pop] + e.cell for e in spec.event_selections], dtype=np.int32)
+
+    izh_arr = np.asarray(izh, np.float64).astype(F32).reshape(-1, 10)
+
+    return LoweredModel(
+        dt=dt, seed=int(spec.seed), n_steps=spec.n_steps(),
+        phys_comp_off=np.asarray(phys_off, np.int32),
+        comp_parent=cat(comp_parent, np.int32), comp_c=cat(comp_c, F32),
+        comp_r_axial=cat(comp_r, F32), comp_area=cat(comp_area, F32),
+        comp_inv_rc=cat(comp_inv, F32), comp_v0=cat(comp_v0, F32),
+        chan_types=chan_types, comp_chan_off=np.asarray(chan_off, np.int32),
+        chan_type=np.asarray(chan_type, np.int32),
+        chan_gbase=np.asarray(chan_g, np.float64).astype(F32),
+        chan_erev=np.asarray(chan_e, np.float64).astype(F32),
+        izh_params=izh_arr,
+        src_target=src_target, src_threshold=src_thr,
+        src_cell_seed=cell_seeds(spec.seed, n_cells),
+        syn_types=syn_types, syn_target=tgt.astype(np.int32), syn_type=typ.astype(np.int32),
+        syn_src=src.astype(np.int32), syn_weight=wgt.astype(F32), syn_delay=dly.astype(F32),
+        pois_target=pt, pois_type=pty, pois_rate=pr_, pois_weight=pw, pois_src=ps,
+        pois_instance=pinst,
+        pulse_target=qt, pulse_start=qs, pulse_duration=qd, pulse_amplitude=qa,
+        pulse_weight=np.ones(len(qt), F32),
+        trace_target=trace_target, event_src=event_src, gid_target_base=gid_base,
+    )
+
+
+# ---------------------------------------------------------------------------
+# ctypes mirror of include/eden_gpu.h
+# ---------------------------------------------------------------------------
+ABI_VERSION = 1
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+class CModel(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_int32), ("dt", ctypes.c_float), ("seed", ctypes.c_int64),
+        ("n_phys", ctypes.c_int32), ("phys_comp_off", _i32p),
+        ("n_comp", ctypes.c_int32), ("comp_parent", _i32p), ("comp_c", _f32p),
+        ("comp_r_axial", _f32p), ("comp_area", _f32p), ("comp_inv_rc", _f32p), ("comp_v0", _f32p),
+        ("n_chan_types", ctypes.c_int32), ("chan_types", ctypes.c_void_p),
+        ("comp_chan_off", _i32p), ("chan_type", _i32p), ("chan_gbase", _f32p), ("chan_erev", _f32p),
+        ("n_izh", ctypes.c_int32), ("izh_params", _f32p),
+        ("n_src", ctypes.c_int32), ("src_target", _i32p), ("src_threshold", _f32p),
+        ("src_cell_seed", _i32p),
+        ("n_syn_types", ctypes.c_int32), ("syn_types", ctypes.c_void_p),
+        ("n_syn", ctypes.c_int64), ("syn_target", _i32p), ("syn_type", _i32p),
+        ("syn_src", _i32p), ("syn_weight", _f32p), ("syn_delay", _f32p),
+        ("n_pois", ctypes.c_int64), ("pois_target", _i32p), ("pois_type", _i32p),
+        ("pois_rate", _f32p), ("pois_weight", _f32p), ("pois_src", _i32p), ("pois_instance", _i32p),
+        ("n_pulse", ctypes.c_int64), ("pulse_target", _i32p), ("pulse_start", _f32p),
+        ("pulse_duration", _f32p), ("pulse_amplitude", _f32p), ("pulse_weight", _f32p),
+    ]
+
+
+def to_cmodel(m: LoweredModel):
+    """Build the C struct; returns (struct, keepalive list of arrays)."""
+    keep = []
+
+    def p(arr, dtype, ptype):
+        a = np.ascontiguousarray(arr, dtype=dtype)
+        if a.size == 0:
+            a = np.zeros(1, dtype=dtype)
+        keep.append(a)
+        return a.ctypes.data_as(ptype)
+
+    def pv(arr):
+        a = np.ascontiguousarray(arr)
+        if a.size == 0:
+            a = np.zeros(1, dtype=arr.dtype)
+        keep.append(a)
+        return ctypes.c_void_p(a.ctypes.data)
+
+    cm = CModel()
+    cm.abi_version = ABI_VERSION
+    cm.dt = float(m.dt)
+    cm.seed = int(m.seed)
+    cm.n_phys = m.n_phys
+    cm.phys_comp_off = p(m.phys_comp_off, np.int32, _i32p)
+    cm.n_comp = m.n_comp
+    cm.comp_parent = p(m.comp_parent, np.int32, _i32p)
+    cm.comp_c = p(m.comp_c, F32, _f32p)
+    cm.comp_r_axial = p(m.comp_r_axial, F32, _f32p)
+    cm.comp_area = p(m.comp_area, F32, _f32p)
+    cm.comp_inv_rc = p(m.comp_inv_rc, F32, _f32p)
+    cm.comp_v0 = p(m.comp_v0, F32, _f32p)
+    cm.n_chan_types = len(m.chan_types)
+    cm.chan_types = pv(m.chan_types)
+    cm.comp_chan_off = p(m.comp_chan_off, np.int32, _i32p)
+    cm.chan_type = p(m.chan_type, np.int32, _i32p)
+    cm.chan_gbase = p(m.chan_gbase, F32, _f32p)
+    cm.chan_erev = p(m.chan_erev, F32, _f32p)
+    cm.n_izh = m.n_izh
+    cm.izh_params = p(m.izh_params.reshape(-1), F32, _f32p)
+    cm.n_src = len(m.src_target)
+    cm.src_target = p(m.src_target, np.int32, _i32p)
+    cm.src_threshold = p(m.src_threshold, F32, _f32p)
+    cm.src_cell_seed = p(m.src_cell_seed, np.int32, _i32p)
+    cm.n_syn_types = len(m.syn_types)
+    cm.syn_types = pv(m.syn_types)
+    cm.n_syn = len(m.syn_target)
+    cm.syn_target = p(m.syn_target, np.int32, _i32p)
+    cm.syn_type = p(m.syn_type, np.int32, _i32p)
+    cm.syn_src = p(m.syn_src, np.int32, _i32p)
+    cm.syn_weight = p(m.syn_weight, F32, _f32p)
+    cm.syn_delay = p(m.syn_delay, F32, _f32p)
+    cm.n_pois = len(m.pois_target)
+    cm.pois_target = p(m.pois_target, np.int32, _i32p)
+    cm.pois_type = p(m.pois_type, np.int32, _i32p)
+    cm.pois_rate = p(m.pois_rate, F32, _f32p)
+    cm.pois_weight = p(m.pois_weight, F32, _f32p)
+    cm.pois_src = p(m.pois_src, np.int32, _i32p)
+    cm.pois_instance = p(m.pois_instance, np.int32, _i32p)
+    cm.n_pulse = len(m.pulse_target)
+    cm.pulse_target = p(m.pulse_target, np.int32, _i32p)
+    cm.pulse_start = p(m.pulse_start, F32, _f32p)
+    cm.pulse_duration = p(m.pulse_duration, F32, _f32p)
+    cm.pulse_amplitude = p(m.pulse_amplitude, F32, _f32p)
+    cm.pulse_weight = p(m.pulse_weight, F32, _f32p)
+    return cm, keep

@@ -1,0 +1,282 @@
+"""Neutral description of the NeuroML networks this path simulates.
+
+A `NetworkSpec` holds, in numpy arrays, exactly the NeuroML content the
+GPU path supports: physical (multi-compartment) cells with ionChannelHH
+channels, izhikevich2007Cell point neurons, expOneSynapse / expTwoSynapse
+synapses reached through `connectionWD` projections, pulseGenerator and
+poissonFiringSynapse inputs, and the LEMS `<Simulation>` with its
+`OutputFile` / `EventOutputFile` recorders.
+
+Three producers/consumers share it:
+  * workloads.py builds it from a seed (the synthetic configurations);
+  * neuroml_io.py writes it as LEMS/NeuroML and reads it back from such files
+    (the reference's input format, so the reference simulator can run the
+    same model);
+  * lowering.py turns it into the device-side structure-of-arrays model.
+
+Quantities are stored in NeuroML's physiological units as written in the
+XML (mV, ms, um, nS, nA, pF, mS/cm2, uF/cm2, ohm*cm, Hz) so that writing
+and re-reading a spec is lossless; the conversion to engine units
+(us, mV, nA, pF, uS, Mohm, um — eden/NeuroML.cpp:307-400) happens in
+lowering.py.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+
+# ---------------------------------------------------------------------------
+# Channel kinetics (ionChannelHH with gateHHrates, eden/NeuroML.cpp:4030-4110)
+# ---------------------------------------------------------------------------
+RATE_EXP = 0        # HHExpRate:        r * exp((v - mid) / s)
+RATE_EXPLINEAR = 1  # HHExpLinearRate:  r * x / (1 - exp(-x)), x = (v - mid) / s
+RATE_SIGMOID = 2    # HHSigmoidRate:    r / (1 + exp((mid - v) / s))
+
+RATE_TYPE_NAMES = {RATE_EXP: "HHExpRate", RATE_EXPLINEAR: "HHExpLinearRate",
+                   RATE_SIGMOID: "HHSigmoidRate"}
+
+
+@dataclass
+class Rate:
+    kind: int
+    rate: float      # per_ms
+    midpoint: float  # mV
+    scale: float     # mV
+
+
+@dataclass
+class Gate:
+    name: str
+    instances: int
+    forward: Rate
+    reverse: Rate
+
+
+@dataclass
+class Channel:
+    name: str
+    gates: List[Gate] = field(default_factory=list)
+    species: Optional[str] = None
+
+
+def hh_channels() -> List[Channel]:
+    """The classic squid-axon HH set (leak, Na m3h, K n4), with the rate
+    constants of the reference example examples/NML2_SingleCompHHCell.nml."""
+    leak = Channel("passiveChan")
+    na = Channel("naChan", [
+        Gate("m", 3, Rate(RATE_EXPLINEAR, 1.0, -40.0, 10.0), Rate(RATE_EXP, 4.0, -65.0, -18.0)),
+        Gate("h", 1, Rate(RATE_EXP, 0.07, -65.0, -20.0), Rate(RATE_SIGMOID, 1.0, -35.0, 10.0)),
+    ], species="na")
+    k = Channel("kChan", [
+        Gate("n", 4, Rate(RATE_EXPLINEAR, 0.1, -55.0, 10.0), Rate(RATE_EXP, 0.125, -65.0, -80.0)),
+    ], species="k")
+    return [leak, na, k]
+
+
+# ---------------------------------------------------------------------------
+# Cell types
+# ---------------------------------------------------------------------------
+@dataclass
+class ChannelDensity:
+    """channelDensity: `channel` (index into NetworkSpec.channels) on the
+    segments whose mask is set, conductivity `cond` mS/cm2, reversal mV."""
+    channel: int
+    cond: float
+    erev: float
+    seg_mask: np.ndarray  # bool per segment
+
+
+@dataclass
+class PhysicalCell:
+    """A NeuroML <cell>: an unbranched-or-branched tree of cylindrical
+    segments, one compartment per segment.
+
+    seg_parent[i] < i (root = segment 0 with parent -1).  Segment i runs from
+    its parent's distal point along +x by seg_len[i] um with constant
+    diameter seg_diam[i] um; a zero-length root is a sphere of that diameter.
+    """
+    name: str
+    seg_parent: np.ndarray
+    seg_len: np.ndarray
+    seg_diam: np.ndarray
+    densities: List[ChannelDensity]
+    cm: float = 1.0            # uF/cm2
+    ra: float = 30.0           # ohm*cm
+    v0: float = -65.0          # mV
+    spike_thresh: float = -20.0  # mV
+    seg_groups: dict = field(default_factory=dict)  # name -> bool mask (for writing)
+
+    @property
+    def n_seg(self) -> int:
+        return int(len(self.seg_parent))
+
+
+@dataclass
+class Izhikevich2007Cell:
+    name: str
+    C: float = 100.0      # pF
+    k: float = 0.7        # nS/mV
+    vr: float = -60.0     # mV
+    vt: float = -40.0     # mV
+    vpeak: float = 35.0   # mV
+    a: float = 0.03       # per_ms
+    b: float = -2.0       # nS
+    c: float = -50.0      # mV
+    d: float = 100.0      # pA
+    v0: float = -60.0     # mV
+
+
+# ---------------------------------------------------------------------------
+# Synapses and inputs
+# ---------------------------------------------------------------------------
+SYN_EXPONE = 0
+SYN_EXPTWO = 1
+
+
+@dataclass
+class SynapseType:
+    name: str
+    kind: int
+    gbase: float          # nS
+    erev: float           # mV
+    tau_decay: float      # ms
+    tau_rise: float = 0.0  # ms (expTwo only)
+
+
+@dataclass
+class Population:
+    name: str
+    cell_type: str        # name of a PhysicalCell or Izhikevich2007Cell
+    size: int
+
+
+@dataclass
+class Projection:
+    """connectionWD list with one synapse type.  Cells are global cell ids
+    (gids: population declaration order, then index); the NeuroML writer
+    splits a projection per (pre population, post population) pair."""
+    name: str
+    pre_pop: str
+    post_pop: str
+    synapse: str
+    pre_cell: np.ndarray     # int index within pre_pop
+    post_cell: np.ndarray    # int index within post_pop
+    post_seg: np.ndarray     # int segment id on the post cell
+    weight: np.ndarray       # float, dimensionless
+    delay: np.ndarray        # float, ms
+
+
+@dataclass
+class PulseInputs:
+    """One pulseGenerator per entry (delay/duration ms, amplitude nA) on
+    cell gid `cell`, segment `seg`."""
+    pop: str
+    cell: np.ndarray
+    seg: np.ndarray
+    delay: np.ndarray
+    duration: np.ndarray
+    amplitude: np.ndarray
+
+
+@dataclass
+class PoissonInputs:
+    """poissonFiringSynapse instances (`rate` Hz, each driving its own
+    instance of `synapse`) on cell gid `cell`, segment `seg`."""
+    pop: str
+    synapse: str
+    rate: float
+    cell: np.ndarray
+    seg: np.ndarray
+
+
+@dataclass
+class OutputColumn:
+    pop: str
+    cell: int
+    seg: int
+    quantity: str = "v"   # only membrane potential is recorded
+
+
+@dataclass
+class EventSelection:
+    pop: str
+    cell: int
+    seg: int = 0
+
+
+@dataclass
+class NetworkSpec:
+    name: str
+    dt: float               # ms
+    length: float           # ms
+    seed: int
+    channels: List[Channel] = field(default_factory=list)
+    cells: list = field(default_factory=list)           # PhysicalCell | Izhikevich2007Cell
+    synapses: List[SynapseType] = field(default_factory=list)
+    populations: List[Population] = field(default_factory=list)
+    projections: List[Projection] = field(default_factory=list)
+    pulses: List[PulseInputs] = field(default_factory=list)
+    poissons: List[PoissonInputs] = field(default_factory=list)
+    trace_columns: List[OutputColumn] = field(default_factory=list)
+    trace_file: str = "trajectory.txt"
+    event_selections: List[EventSelection] = field(default_factory=list)
+    event_file: str = "spikes.txt"
+    event_format: str = "TIME_ID"
+
+    # -- lookups ---------------------------------------------------------
+    def cell_type(self, name: str):
+        for c in self.cells:
+            if c.name == name:
+                return c
+        raise KeyError(name)
+
+    def synapse(self, name: str) -> SynapseType:
+        for s in self.synapses:
+            if s.name == name:
+                return s
+        raise KeyError(name)
+
+    def population(self, name: str) -> Population:
+        for p in self.populations:
+            if p.name == name:
+                return p
+        raise KeyError(name)
+
+    def pop_offsets(self) -> dict:
+        """Global cell id (gid) of each population's first cell, in
+        declaration order (the reference's work-item order)."""
+        off, out = 0, {}
+        for p in self.populations:
+            out[p.name] = off
+            off += p.size
+        return out
+
+    @property
+    def n_cells(self) -> int:
+        return sum(p.size for p in self.populations)
+
+    def n_compartments(self) -> int:
+        total = 0
+        for p in self.populations:
+            ct = self.cell_type(p.cell_type)
+            total += p.size * (ct.n_seg if isinstance(ct, PhysicalCell) else 1)
+        return total
+
+    def n_synapses(self) -> int:
+        return int(sum(len(pr.pre_cell) for pr in self.projections))
+
+    def n_poisson(self) -> int:
+        return int(sum(len(pi.cell) for pi in self.poissons))
+
+    def n_steps(self) -> int:
+        """Non-initialisation steps: t = 0, dt, ... while t <= length
+        (eden/Eden.cpp:11488)."""
+        dt_us = np.float32(self.dt * 1000.0)
+        t_final = self.length * 1000.0
+        n, t = 0, 0.0
+        # times are exact multiples of dt in the configurations used here
+        n = int(np.floor(t_final / float(dt_us) + 1e-9)) + 1
+        return n

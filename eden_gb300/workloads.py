@@ -1,0 +1,250 @@
+"""Seeded synthetic networks: the workloads this path is measured and tested on.
+
+No public dataset exists for these runs; each generator draws a NeuroML
+network of a stated shape from numpy's `default_rng(seed)`:
+
+  single_comp_hh   1,000 single-compartment HH cells, one DC pulse each
+                   (uniform 0-0.3 nA), no synapses, dt 0.025 ms, 1,000 ms.
+  multicomp_net    10,000 cells with random branching trees (segment count
+                   log-uniform in [1, 500], segment length 5-50 um, diameter
+                   0.5-4 um, Ra 150 ohm*cm), HH soma + passive dendrites,
+                   expTwoSynapse (0.5 / 5 ms, 1 nS, 0 mV) at fixed in-degree
+                   100 with delays 0.5-5 ms, plus one 5 Hz poissonFiringSynapse
+                   per synapse slot; dt 0.025 ms, 1,000 ms.
+  izh_net          100,000 izhikevich2007Cell (80 % RS, 20 % FS), expOneSynapse
+                   at in-degree 100 (lognormal weights, delays 1-20 ms in whole
+                   steps), one DC pulse per cell; dt 0.1 ms, 1,000 ms.
+  ball_and_stick   256 soma + 50-compartment HH cables with lognormal
+                   per-instance parameters, 0.5 nA step for 150 ms;
+                   dt 0.025 ms, 200 ms.
+  mixed_scale      the multicomp and izhikevich populations together.
+
+Every generator takes scale arguments (cell count, in-degree, length) so the
+same distributions produce the small cases the CPU reference can finish.
+Delays are rounded to whole microseconds so that delivery times are exact
+in single precision.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .network import (ChannelDensity, EventSelection, Izhikevich2007Cell,
+                      NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
+                      Population, Projection, PulseInputs, SynapseType,
+                      SYN_EXPONE, SYN_EXPTWO, hh_channels)
+
+# conductivities (mS/cm2) and reversal potentials (mV) of the HH cells
+G_NA, G_K, G_L = 120.0, 36.0, 0.3
+E_NA, E_K, E_L = 50.0, -77.0, -54.387
+
+
+def _hh_densities(n_seg: int, hh_mask: np.ndarray) -> list:
+    allseg = np.ones(n_seg, dtype=bool)
+    return [
+        ChannelDensity(0, G_L, E_L, allseg),
+        ChannelDensity(1, G_NA, E_NA, hh_mask.copy()),
+        ChannelDensity(2, G_K, E_K, hh_mask.copy()),
+    ]
+
+
+def _round_us(delay_ms: np.ndarray) -> np.ndarray:
+    return np.round(np.asarray(delay_ms) * 1000.0) / 1000.0
+
+
+# ---------------------------------------------------------------------------
+def single_comp_hh(n_cells: int = 1000, length_ms: float = 1000.0,
+                   dt_ms: float = 0.025, seed: int = 1234,
+                   n_recorded: int = 10) -> NetworkSpec:
+    rng = np.random.default_rng(seed)
+    cell = PhysicalCell(
+        name="hhcell",
+        seg_parent=np.array([-1]), seg_len=np.array([0.0]), seg_diam=np.array([17.8]),
+        densities=_hh_densities(1, np.ones(1, dtype=bool)),
+        cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0,
+    )
+    spec = NetworkSpec("single_comp_hh", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.cells.append(cell)
+    spec.populations.append(Population("hhpop", "hhcell", n_cells))
+    amp = np.round(rng.uniform(0.0, 0.3, n_cells), 6)
+    spec.pulses.append(PulseInputs("*", np.arange(n_cells), np.zeros(n_cells, int),
+                                   np.zeros(n_cells), np.full(n_cells, length_ms), amp))
+    rec = np.sort(rng.choice(n_cells, size=min(n_recorded, n_cells), replace=False))
+    spec.trace_columns = [OutputColumn("hhpop", int(c), 0) for c in rec]
+    spec.event_selections = [EventSelection("hhpop", c, 0) for c in range(n_cells)]
+    return spec
+
+
+# ---------------------------------------------------------------------------
+def random_tree(rng, n_seg: int, soma_len=20.0, soma_diam=20.0):
+    """Random recursive tree: each new segment attaches to a uniformly chosen
+    earlier one.  Segment 0 is a fixed-size cylindrical soma."""
+    parent = np.empty(n_seg, dtype=np.int64)
+    parent[0] = -1
+    if n_seg > 1:
+        parent[1:] = np.floor(rng.uniform(0, 1, n_seg - 1) * np.arange(1, n_seg)).astype(np.int64)
+    length = np.round(rng.uniform(5.0, 50.0, n_seg), 3)
+    diam = np.round(rng.uniform(0.5, 4.0, n_seg), 3)
+    length[0], diam[0] = soma_len, soma_diam
+    return parent, length, diam
+
+
+def multicomp_net(n_cells: int = 10000, in_degree: int = 100, length_ms: float = 1000.0,
+                  dt_ms: float = 0.025, seed: int = 1234, max_seg: int = 500,
+                  poisson_rate_hz: float = 5.0, n_recorded: int = 10,
+                  weight: float = 1.0, soma_diam: float = 20.0) -> NetworkSpec:
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("multicomp_net", dt_ms, length_ms, seed, channels=hh_channels())
+    syn = SynapseType("syn_e2", SYN_EXPTWO, gbase=1.0, erev=0.0, tau_decay=5.0, tau_rise=0.5)
+    spec.synapses.append(syn)
+    nseg = np.round(np.exp(rng.uniform(0.0, np.log(max_seg), n_cells))).astype(int)
+    nseg = np.clip(nseg, 1, max_seg)
+    for c in range(n_cells):
+        parent, length, diam = random_tree(rng, int(nseg[c]), soma_diam=soma_diam, soma_len=soma_diam)
+        soma = np.zeros(len(parent), dtype=bool)
+        soma[0] = True
+        cell = PhysicalCell(f"mc{c}", parent, length, diam, _hh_densities(len(parent), soma),
+                            cm=1.0, ra=150.0, v0=-65.0, spike_thresh=-20.0,
+                            seg_groups={"soma_group": soma, "dend_group": ~soma})
+        spec.cells.append(cell)
+        spec.populations.append(Population(f"pop{c}", f"mc{c}", 1))
+    # recurrent expTwo connections, fixed in-degree, presyn uniform over cells
+    pre = rng.integers(0, n_cells, size=(n_cells, in_degree))
+    delay = _round_us(rng.uniform(0.5, 5.0, size=(n_cells, in_degree)))
+    post = np.repeat(np.arange(n_cells), in_degree)
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre.ravel(), post, "syn_e2",
+                                             np.full(post.size, weight), delay.ravel()))
+    # one Poisson source per synapse slot, onto the soma
+    if poisson_rate_hz > 0:
+        spec.poissons.append(PoissonInputs("*", "syn_e2", poisson_rate_hz,
+                                           np.repeat(np.arange(n_cells), in_degree),
+                                           np.zeros(n_cells * in_degree, dtype=int)))
+    rec = np.sort(rng.choice(n_cells, size=min(n_recorded, n_cells), replace=False))
+    spec.trace_columns = [OutputColumn(f"pop{c}", 0, 0) for c in rec]
+    spec.event_selections = [EventSelection(f"pop{c}", 0, 0) for c in range(n_cells)]
+    return spec
+
+
+def _flat_projection(spec, name, pre_gid, post_gid, synapse, weight, delay, post_seg=None):
+    """A projection expressed on global cell ids; neuroml_io splits it per
+    (pre, post) population pair when writing XML."""
+    if post_seg is None:
+        post_seg = np.zeros(len(post_gid), dtype=np.int64)
+    return Projection(name, "*", "*", synapse, np.asarray(pre_gid, np.int64),
+                      np.asarray(post_gid, np.int64), np.asarray(post_seg, np.int64),
+                      np.asarray(weight, np.float64), np.asarray(delay, np.float64))
+
+
+# ---------------------------------------------------------------------------
+def izh_net(n_cells: int = 100000, in_degree: int = 100, length_ms: float = 1000.0,
+            dt_ms: float = 0.1, seed: int = 1234, n_recorded: int = 10,
+            pulse_max_na: float = 0.5) -> NetworkSpec:
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("izh_net", dt_ms, length_ms, seed)
+    n_exc = int(round(0.8 * n_cells))
+    n_inh = n_cells - n_exc
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.cells.append(Izhikevich2007Cell("izFS", a=0.1, d=0.0, c=-55.0))
+    spec.populations.append(Population("exc", "izRS", n_exc))
+    if n_inh:
+        spec.populations.append(Population("inh", "izFS", n_inh))
+    spec.synapses.append(SynapseType("syn_exc", SYN_EXPONE, gbase=1.0, erev=0.0, tau_decay=2.0))
+    spec.synapses.append(SynapseType("syn_inh", SYN_EXPONE, gbase=1.0, erev=-80.0, tau_decay=5.0))
+    pre = rng.integers(0, n_cells, size=(n_cells, in_degree)).ravel()
+    post = np.repeat(np.arange(n_cells), in_degree)
+    w = np.round(rng.lognormal(-1.0, 0.5, size=pre.size), 6)
+    steps = rng.integers(10, 201, size=pre.size)
+    delay = np.round(steps * dt_ms, 6)
+    exc = pre < n_exc
+    spec.projections.append(_flat_projection(spec, "proj_exc", pre[exc], post[exc], "syn_exc", w[exc], delay[exc]))
+    spec.projections.append(_flat_projection(spec, "proj_inh", pre[~exc], post[~exc], "syn_inh", w[~exc], delay[~exc]))
+    amp = np.round(rng.uniform(0.0, pulse_max_na, n_cells), 6)
+    gids = np.arange(n_cells)
+    spec.pulses.append(PulseInputs("*", gids, np.zeros(n_cells, int), np.zeros(n_cells),
+                                   np.full(n_cells, length_ms), amp))
+    rec = np.sort(rng.choice(n_cells, size=min(n_recorded, n_cells), replace=False))
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, int(g)), 0) for g in rec]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n_cells)]
+    return spec
+
+
+def _gid_to_pop(spec, gid):
+    for p in spec.populations:
+        if gid < p.size:
+            return p.name, gid
+        gid -= p.size
+    raise IndexError(gid)
+
+
+# ---------------------------------------------------------------------------
+def ball_and_stick(n_inst: int = 256, n_dend: int = 50, length_ms: float = 200.0,
+                   dt_ms: float = 0.025, seed: int = 1234, sigma: float = 0.3,
+                   amp_na: float = 0.5, pulse_ms: float = 150.0,
+                   params: np.ndarray | None = None) -> NetworkSpec:
+    """Per-instance parameters (7): soma gNa, gK, gL, dendrite gNa, gK, gL
+    (mS/cm2) and Ra (ohm*cm), lognormal around the HH defaults."""
+    rng = np.random.default_rng(seed)
+    base = np.array([G_NA, G_K, G_L, G_NA, G_K, G_L, 150.0])
+    if params is None:
+        params = np.round(base * rng.lognormal(0.0, sigma, size=(n_inst, 7)), 6)
+    spec = NetworkSpec("ball_and_stick", dt_ms, length_ms, seed, channels=hh_channels())
+    n_seg = 1 + n_dend
+    parent = np.arange(-1, n_seg - 1, dtype=np.int64)
+    seg_len = np.full(n_seg, 500.0 / n_dend)
+    seg_diam = np.full(n_seg, 2.0)
+    seg_len[0], seg_diam[0] = 20.0, 20.0
+    soma = np.zeros(n_seg, dtype=bool)
+    soma[0] = True
+    for i in range(n_inst):
+        p = params[i]
+        dens = [
+            ChannelDensity(0, p[2], E_L, soma.copy()), ChannelDensity(1, p[0], E_NA, soma.copy()),
+            ChannelDensity(2, p[1], E_K, soma.copy()),
+            ChannelDensity(0, p[5], E_L, ~soma), ChannelDensity(1, p[3], E_NA, ~soma),
+            ChannelDensity(2, p[4], E_K, ~soma),
+        ]
+        spec.cells.append(PhysicalCell(f"bs{i}", parent.copy(), seg_len.copy(), seg_diam.copy(), dens,
+                                       cm=1.0, ra=float(p[6]), v0=-65.0, spike_thresh=-20.0,
+                                       seg_groups={"soma_group": soma, "dend_group": ~soma}))
+        spec.populations.append(Population(f"pop{i}", f"bs{i}", 1))
+    spec.pulses.append(PulseInputs("*", np.arange(n_inst), np.zeros(n_inst, int), np.zeros(n_inst),
+                                   np.full(n_inst, pulse_ms), np.full(n_inst, amp_na)))
+    spec.trace_columns = [OutputColumn(f"pop{i}", 0, 0) for i in range(min(n_inst, 10))]
+    spec.event_selections = [EventSelection(f"pop{i}", 0, 0) for i in range(n_inst)]
+    spec.params = params
+    return spec
+
+
+# ---------------------------------------------------------------------------
+def mixed_scale(n_izh: int = 160000, n_mc: int = 40000, in_degree: int = 100,
+                length_ms: float = 1000.0, dt_ms: float = 0.025, seed: int = 1234,
+                poisson_rate_hz: float = 2.0, n_seg: int = 100) -> NetworkSpec:
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("mixed_scale", dt_ms, length_ms, seed, channels=hh_channels())
+    syn = SynapseType("syn_e2", SYN_EXPTWO, gbase=1.0, erev=0.0, tau_decay=5.0, tau_rise=0.5)
+    spec.synapses.append(syn)
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("izh", "izRS", n_izh))
+    for c in range(n_mc):
+        parent, length, diam = random_tree(rng, n_seg)
+        soma = np.zeros(n_seg, dtype=bool)
+        soma[0] = True
+        spec.cells.append(PhysicalCell(f"mc{c}", parent, length, diam, _hh_densities(n_seg, soma),
+                                       cm=1.0, ra=150.0, seg_groups={"soma_group": soma, "dend_group": ~soma}))
+        spec.populations.append(Population(f"pop{c}", f"mc{c}", 1))
+    n = n_izh + n_mc
+    pre = rng.integers(0, n, size=(n, in_degree)).ravel()
+    post = np.repeat(np.arange(n), in_degree)
+    delay = _round_us(rng.uniform(0.5, 10.0, size=pre.size))
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre, post, "syn_e2", np.full(pre.size, 0.2), delay))
+    spec.poissons.append(PoissonInputs("*", "syn_e2", poisson_rate_hz, post.copy(), np.zeros(post.size, dtype=int)))
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
+CONFIGS = {
+    "single_comp_hh": single_comp_hh,
+    "multicomp_net": multicomp_net,
+    "izh_net": izh_net,
+    "ball_and_stick": ball_and_stick,
+    "mixed_scale": mixed_scale,
+}

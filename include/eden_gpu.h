@@ -1,0 +1,212 @@
+/*
+ * eden_gpu.h — C ABI of libeden_gpu.so, the GB300 (sm_103a) implementation of
+ * EDEN's per-timestep simulation loop.
+ *
+ * The reference runs its step loop in eden/Eden.cpp:11488-11938: each step an
+ * OpenMP loop calls one generated `doit()` per cell through the
+ * `IterationCallback` C ABI (eden/Eden.cpp:64-76, called at 11856-11865), then
+ * swaps the now/next state buffers (11935-11937).  This library replaces that
+ * loop.  The host lowers the parsed model once into the plain
+ * structure-of-arrays `EdenGpuModel` below (engine units of
+ * eden/NeuroML.cpp:307-400: us, mV, nA, pF, uS, Mohm, um) and then advances
+ * the network any number of steps per call.
+ *
+ * All entry points return 0 on success and a negative EDEN_GPU_E* code on
+ * failure; `edenGpuLastError` gives the message.  Nothing here calls exit(),
+ * abort() or traps; device-side faults (a bounded wait that ran out, a
+ * non-finite recorded value) are reported through the same codes after the
+ * call that saw them.
+ */
+#ifndef EDEN_GPU_H
+#define EDEN_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EDEN_GPU_ABI_VERSION 1
+
+enum {
+    EDEN_GPU_OK = 0,
+    EDEN_GPU_E_INVALID = -1,   /* malformed model or argument */
+    EDEN_GPU_E_CUDA = -2,      /* a CUDA runtime call failed */
+    EDEN_GPU_E_NOMEM = -3,     /* device allocation refused */
+    EDEN_GPU_E_NONFINITE = -4, /* NaN/Inf in a recorded value */
+    EDEN_GPU_E_RANGE = -5,     /* record buffer too small / index out of range */
+    EDEN_GPU_E_NODEVICE = -6   /* no CUDA device visible */
+};
+
+/* Gate rate forms of ionChannelHH/gateHHrates (eden/Eden.cpp:5164-5181). */
+enum {
+    EDEN_RATE_EXP = 0,        /* r * exp((V - mid) / s)                     */
+    EDEN_RATE_EXPLINEAR = 1,  /* r * x / (1 - exp(-x)), x = (V - mid) / s; r at V == mid */
+    EDEN_RATE_SIGMOID = 2     /* r / (1 + exp((mid - V) / s))               */
+};
+
+#define EDEN_MAX_GATES 4
+
+/* One ionChannelHH type: up to EDEN_MAX_GATES gateHHrates, each contributing
+ * q^instances to the open fraction (eden/Eden.cpp:5678-5717). Rates in 1/us. */
+typedef struct EdenGpuChannelType {
+    int32_t n_gates;
+    int32_t gate_instances[EDEN_MAX_GATES];
+    int32_t fwd_kind[EDEN_MAX_GATES];
+    float fwd_rate[EDEN_MAX_GATES], fwd_mid[EDEN_MAX_GATES], fwd_scale[EDEN_MAX_GATES];
+    int32_t rev_kind[EDEN_MAX_GATES];
+    float rev_rate[EDEN_MAX_GATES], rev_mid[EDEN_MAX_GATES], rev_scale[EDEN_MAX_GATES];
+    float q10[EDEN_MAX_GATES];
+} EdenGpuChannelType;
+
+enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1 };
+
+/* expOneSynapse (native, eden/Eden.cpp:3424-3466) or expTwoSynapse (LEMS,
+ * LEMS_CoreComponents.inc.xml:145-180).  gbase uS, erev mV, taus us.
+ * `waveform_factor` is expTwo's derived 1/(-exp(-tp/tr)+exp(-tp/td)) and
+ * `weight_prop` its LEMS `weight` property (default 1). */
+typedef struct EdenGpuSynapseType {
+    int32_t kind;
+    float gbase, erev, tau_decay, tau_rise, waveform_factor, weight_prop;
+} EdenGpuSynapseType;
+
+/*
+ * The lowered network.  "Targets" are the places a membrane potential lives:
+ * targets [0, n_comp) are the compartments of physical cells (cell by cell,
+ * each cell's compartments in the reference's compartment order), targets
+ * [n_comp, n_comp + n_izh) are izhikevich2007Cell point neurons.
+ * Every array is host memory, read during edenGpuCreate only.
+ */
+typedef struct EdenGpuModel {
+    int32_t abi_version;      /* EDEN_GPU_ABI_VERSION */
+    float dt;                 /* us */
+    int64_t seed;             /* simulation RNG seed */
+
+    /* physical cells and their compartments */
+    int32_t n_phys;
+    const int32_t *phys_comp_off;   /* [n_phys + 1] */
+    int32_t n_comp;
+    const int32_t *comp_parent;     /* [n_comp] parent within the cell, -1 at the root */
+    const float *comp_c;            /* [n_comp] capacitance, pF */
+    const float *comp_r_axial;      /* [n_comp] axial resistance to the parent, Mohm (root: unused) */
+    const float *comp_area;         /* [n_comp] membrane area, um2 */
+    const float *comp_inv_rc;       /* [n_comp] sum over neighbours of 1/(R*C), 1/us */
+    const float *comp_v0;           /* [n_comp] initial V, mV */
+
+    /* channel instances (channelDensity on a compartment), grouped by compartment */
+    int32_t n_chan_types;
+    const EdenGpuChannelType *chan_types;
+    const int32_t *comp_chan_off;   /* [n_comp + 1] */
+    const int32_t *chan_type;       /* [n_chan] */
+    const float *chan_gbase;        /* [n_chan] conductivity, mS/cm2 */
+    const float *chan_erev;         /* [n_chan] mV */
+
+    /* izhikevich2007Cell point neurons, engine units (eden/Eden.cpp:6821-6914):
+     * params[10*i + k], k = C pF, v0 mV, k nS/mV, vr, vt, vpeak mV,
+     *                        a 1/us, b uS, c mV, d nA */
+    int32_t n_izh;
+    const float *izh_params;
+
+    /* spike sources: one per cell (gid order); `src_target` is the target
+     * whose threshold crossing (physical: V < thr < V_next, eden/Eden.cpp:6248)
+     * or izhikevich v > vpeak (LEMS OnCondition) emits the spike */
+    int32_t n_src;
+    const int32_t *src_target;      /* [n_src] */
+    const float *src_threshold;     /* [n_src] mV, physical sources only */
+    const int32_t *src_cell_seed;   /* [n_src] reverse_bits(seed) ^ gid (eden/Eden.cpp:7679-7691) */
+
+    /* synapse types and connection synapses (connectionWD instances) */
+    int32_t n_syn_types;
+    const EdenGpuSynapseType *syn_types;
+    int64_t n_syn;
+    const int32_t *syn_target;      /* [n_syn] */
+    const int32_t *syn_type;        /* [n_syn] */
+    const int32_t *syn_src;         /* [n_syn] presynaptic source */
+    const float *syn_weight;        /* [n_syn] connection weight */
+    const float *syn_delay;         /* [n_syn] us */
+
+    /* poissonFiringSynapse inputs, each with its own synapse instance */
+    int64_t n_pois;
+    const int32_t *pois_target;
+    const int32_t *pois_type;       /* synapse type it drives */
+    const float *pois_rate;         /* 1/us */
+    const float *pois_weight;
+    const int32_t *pois_src;        /* cell (spike source index) whose RNG seed it uses */
+    const int32_t *pois_instance;   /* instance number in the reference's per-cell input table */
+
+    /* pulseGenerator inputs */
+    int64_t n_pulse;
+    const int32_t *pulse_target;
+    const float *pulse_start, *pulse_duration, *pulse_amplitude, *pulse_weight; /* us, us, nA, - */
+
+    /* per-target input order: within each target the reference sums channel,
+     * then input (pulse, Poisson), then synapse currents (eden/Eden.cpp:6057-6060) */
+} EdenGpuModel;
+
+/* Execution options. */
+enum { EDEN_MODE_PLAIN = 0, EDEN_MODE_BATCHED = 1 };
+typedef struct EdenGpuOptions {
+    int32_t mode;             /* EDEN_MODE_PLAIN: one set of launches per step;
+                                 EDEN_MODE_BATCHED: multi-step windows, graph-captured */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t steps_per_launch; /* batched window length; 0 = autotune (bounded by the minimum delay) */
+    int32_t cells_per_block;  /* 0 = autotune */
+    int32_t record_capacity_steps; /* trace samples buffered on the device between fetches */
+    int32_t spike_capacity;   /* spike events buffered on the device between fetches */
+    int32_t n_trace;          /* recorded targets (membrane potential) */
+    const int32_t *trace_target;
+    int32_t reserved[8];
+} EdenGpuOptions;
+
+/* Records produced since the previous fetch, in step order. */
+typedef struct EdenGpuRecords {
+    /* caller-provided host buffers and their capacities */
+    float *trace;             /* [trace_capacity * n_trace], sample-major */
+    int64_t *trace_step;      /* [trace_capacity] step index of each sample */
+    int64_t trace_capacity;
+    int32_t *spike_src;       /* [spike_capacity] */
+    int64_t *spike_step;      /* [spike_capacity] step at which the spike is logged */
+    int64_t spike_capacity;
+    /* filled in */
+    int64_t n_trace_samples;
+    int64_t n_spikes;
+} EdenGpuRecords;
+
+typedef struct EdenGpuCtx EdenGpuCtx;
+
+/* Build a context: validate the model, upload it to device memory in the
+ * GPU layout, build the spike fan-out table.  Replaces the reference's
+ * GenerateModel() output tables (eden/Eden.cpp:677, RawTables 446-532)
+ * and the now/next buffer allocation (11095-11150). */
+int edenGpuCreate(const EdenGpuModel *model, const EdenGpuOptions *opt, EdenGpuCtx **out);
+
+/* Advance `n_steps` steps starting at step index `first_step`.  Step indices
+ * follow the reference loop (eden/Eden.cpp:11488-11510): steps <= 0 are the
+ * initialisation passes at t = 0, step k >= 1 runs at t = (k - 1) * dt.
+ * Records the state at the start of every non-initialisation step (the
+ * reference's output phase, 11555-11635). */
+int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
+
+/* Copy records accumulated since the last fetch into caller buffers. */
+int edenGpuFetchRecords(EdenGpuCtx *ctx, EdenGpuRecords *rec);
+
+/* Read / write membrane potentials of all targets (n_comp + n_izh floats). */
+int edenGpuReadV(EdenGpuCtx *ctx, float *v_host, int64_t n);
+int edenGpuWriteV(EdenGpuCtx *ctx, const float *v_host, int64_t n);
+
+/* Per-synapse pending spike times (us) and synapse state, for routing checks. */
+int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *state_a, float *state_b, int64_t n);
+
+/* Device time of the last edenGpuRun in milliseconds and the number of
+ * kernel launches it issued. */
+int edenGpuLastRunStats(EdenGpuCtx *ctx, double *device_ms, int64_t *launches);
+
+const char *edenGpuLastError(EdenGpuCtx *ctx);
+void edenGpuDestroy(EdenGpuCtx *ctx);
+int edenGpuAbiVersion(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,512 @@
+/*
+ * eden_port.c — CPU restatement of EDEN's per-timestep simulation loop.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the GPU path is checked
+ * against and the CPU baseline `bench.py` times beside it; the product never
+ * links or calls it.  It runs on the same lowered model (include/eden_gpu.h)
+ * the GPU library takes, and restates, in plain C with IEEE single precision,
+ * what the reference's generated per-cell kernels compute:
+ *
+ *   step loop, 4 init passes, now/next swap   eden/Eden.cpp:11488-11938
+ *   HH gates (exp-Euler, clamp) + currents    eden/Eden.cpp:5126-5259, 5678-5717, 5805-5898
+ *   voltage pre-update                        eden/Eden.cpp:6057-6107
+ *   Hines backward-Euler tree solve           eden/Eden.cpp:6114-6225 (order 4416-4473)
+ *   synapse trigger + single pending spike    eden/Eden.cpp:3646-3686
+ *   expOneSynapse                             eden/Eden.cpp:3424-3466
+ *   expTwoSynapse (LEMS, forward Euler)       LEMS_CoreComponents.inc.xml:145-180, eden/Eden.cpp:2832-2994
+ *   poissonFiringSynapse + randof hash RNG    LEMS_CoreComponents.inc.xml:623-672, eden/Eden.cpp:3199-3233, 3873-3912
+ *   pulseGenerator                            eden/Eden.cpp:3798-3826
+ *   izhikevich2007Cell (LEMS)                 LEMS_CoreComponents.inc.xml:1140-1185, eden/Eden.cpp:6821-6914
+ *   threshold crossing + spike send           eden/Eden.cpp:6247-6252, 3946-3995
+ *   trajectory / event loggers                eden/Eden.cpp:11555-11635
+ *
+ * Its parity with the reference itself is pinned by tests/test_oracle_vs_reference.py
+ * against fixtures produced by the reference simulator built from its own sources.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../../include/eden_gpu.h"
+
+/* ---- RNG: Thomas Wang's 64-bit integer hash, as used by randof ---------- */
+static uint64_t hash64shift(uint64_t key) {
+    key = (~key) + (key << 21);
+    key = key ^ (key >> 24);
+    key = (key + (key << 3)) + (key << 8);
+    key = key ^ (key >> 14);
+    key = (key + (key << 2)) + (key << 4);
+    key = key ^ (key >> 28);
+    key = key + (key << 31);
+    return key;
+}
+
+static float randof(float x, int64_t work_item, int64_t instance, int64_t step, int invocation_id) {
+    uint64_t hi = ((uint64_t)work_item << 24) | ((uint64_t)instance & ((1ULL << 24) - 1));
+    uint64_t lo = ((uint64_t)(int64_t)invocation_id << 40) | ((uint64_t)step & ((1ULL << 40) - 1));
+    uint64_t sample = hash64shift(hash64shift(lo) ^ hi);
+    const int scale = 1 << 23;
+    float r = (float)(sample % (uint64_t)scale) / (float)scale;
+    return x * r;
+}
+
+static float rate_value(int kind, float r, float mid, float s, float v) {
+    switch (kind) {
+        case EDEN_RATE_EXP: return r * expf((v - mid) / s);
+        case EDEN_RATE_EXPLINEAR:
+            return r * ((v == mid) ? 1.0f : (((v - mid) / s) / (1.0f - expf(-(v - mid) / s))));
+        default: return r / (1.0f + expf((mid - v) / s));
+    }
+}
+
+typedef struct {
+    const EdenGpuModel *m;
+    int64_t n_target;
+    /* double-buffered state */
+    float *v[2], *gate[2], *izh_u[2];
+    float *syn_a[2], *syn_b[2], *syn_pend[2];
+    unsigned char *trig[2];
+    float *pois_ts[2], *pois_isi[2], *pois_a[2], *pois_b[2];
+    unsigned char *spiked[2];           /* event-logger slot per source */
+    float *diag;
+    int64_t *gate_off;                  /* [n_chan + 1] */
+    int64_t *syn_off, *pois_off, *pulse_off; /* [n_target + 1] */
+    int64_t *fan_off, *fan_syn;         /* CSR source -> synapses */
+    int32_t *order;                     /* per-cell DFS post-order, local ids */
+    int32_t *src_of_target;             /* source id detecting at a target, or -1 */
+    int64_t *syn_fire_count;
+} Port;
+
+static int64_t *csr_by_key(const int32_t *key, int64_t n, int64_t nkeys) {
+    int64_t *off = (int64_t *)calloc((size_t)nkeys + 1, sizeof(int64_t));
+    for (int64_t i = 0; i < n; i++) off[key[i] + 1]++;
+    for (int64_t k = 0; k < nkeys; k++) off[k + 1] += off[k];
+    return off;
+}
+
+/* Depth-first post-order from the root, children in increasing index order
+ * (BackwardEuler::GetOrderLists, eden/Eden.cpp:4411-4473). */
+static void dfs_postorder(const int32_t *parent, int n, int32_t *order) {
+    int *child_off = (int *)calloc((size_t)n + 1, sizeof(int));
+    int *children = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 1; i < n; i++) child_off[parent[i] + 1]++;
+    for (int i = 0; i < n; i++) child_off[i + 1] += child_off[i];
+    int *fill = (int *)calloc((size_t)n + 1, sizeof(int));
+    for (int i = 1; i < n; i++) children[child_off[parent[i]] + fill[parent[i]]++] = i;
+    int *stack = (int *)malloc(sizeof(int) * (size_t)(n + 1));
+    int *next = (int *)calloc((size_t)n + 1, sizeof(int));
+    int sp = 0, k = 0;
+    if (n > 0) stack[sp++] = 0;
+    while (sp > 0) {
+        int u = stack[sp - 1];
+        if (next[u] < child_off[u + 1] - child_off[u]) {
+            stack[sp++] = children[child_off[u] + next[u]++];
+        } else {
+            order[k++] = u;
+            sp--;
+        }
+    }
+    free(child_off); free(children); free(fill); free(stack); free(next);
+}
+
+/* One synapse instance: trigger/pending logic, exposure, state update.
+ * Returns the weighted current and conductance through *iw, *gw. */
+static inline void synapse_step(const EdenGpuSynapseType *st, int init, float t, float dt,
+                                int spike_in_raw, float delay, float pend, float *pend_next,
+                                float a, float b, float *a_next, float *b_next, float v, float w,
+                                float *iw, float *gw, int *fired) {
+    int spike_now = 0;
+    float next_next = pend;
+    if (!init) {
+        if (t <= pend && pend < t + dt) spike_now = 1;
+        if (spike_in_raw) {
+            float fresh = t + delay;
+            if (t <= fresh && fresh < t + dt) spike_now = 1;
+            if (next_next < t + dt && next_next < fresh) next_next = fresh;
+        }
+    }
+    *pend_next = next_next;
+    *fired = spike_now;
+    if (st->kind == EDEN_SYN_EXPONE) {
+        float g = a;
+        float i = g * (st->erev - v);
+        float gn;
+        if (!init) {
+            gn = a - dt * (a / st->tau_decay);
+            if (spike_now) gn = a + st->gbase;
+        } else {
+            gn = a;
+        }
+        *a_next = gn;
+        *b_next = b;
+        *iw = i * w;
+        *gw = g * w;
+    } else {
+        float g = st->gbase * (b - a);
+        float i = g * (st->erev - v);
+        float an, bn;
+        if (init) {
+            an = 0.0f; bn = 0.0f;
+        } else {
+            an = a + dt * (-a / st->tau_rise);
+            bn = b + dt * (-b / st->tau_decay);
+            if (spike_now) {
+                an = a + st->weight_prop * st->waveform_factor;
+                bn = b + st->weight_prop * st->waveform_factor;
+            }
+        }
+        *a_next = an;
+        *b_next = bn;
+        *iw = i * w;
+        *gw = g * w;
+    }
+}
+
+/* Poisson-driven synapse: the spiker fires its own synapse in the same step. */
+static inline void poisson_step(const Port *P, int cur, int64_t k, int init, float dt, int64_t step,
+                                float v, float *iw, float *gw) {
+    const EdenGpuModel *m = P->m;
+    int nxt = cur ^ 1;
+    float rate = m->pois_rate[k];
+    float avg_isi = 1.0f / rate;
+    int64_t work_item = (int64_t)m->src_cell_seed[m->pois_src[k]];
+    int64_t inst = m->pois_instance[k];
+    float ts = P->pois_ts[cur][k], isi = P->pois_isi[cur][k];
+    int fired = 0;
+    if (init) {
+        P->pois_ts[nxt][k] = 0.0f;
+        P->pois_isi[nxt][k] = (-avg_isi) * logf(1.0f - randof(1.0f, work_item, inst, step, 0));
+    } else {
+        P->pois_ts[nxt][k] = ts + dt * 1.0f;
+        P->pois_isi[nxt][k] = isi;
+        if (ts > isi) {
+            P->pois_ts[nxt][k] = 0.0f;
+            P->pois_isi[nxt][k] = (-avg_isi) * logf(1.0f - randof(1.0f, work_item, inst, step, 1));
+            fired = 1;
+        }
+    }
+    const EdenGpuSynapseType *st = &m->syn_types[m->pois_type[k]];
+    float a = P->pois_a[cur][k], b = P->pois_b[cur][k];
+    float g = st->gbase * (b - a);
+    float i = g * (st->erev - v);
+    float an, bn;
+    if (st->kind == EDEN_SYN_EXPONE) {
+        g = a;
+        i = g * (st->erev - v);
+        if (!init) {
+            an = a - dt * (a / st->tau_decay);
+            if (fired) an = a + st->gbase;
+        } else {
+            an = a;
+        }
+        bn = b;
+    } else if (init) {
+        an = 0.0f; bn = 0.0f;
+    } else {
+        an = a + dt * (-a / st->tau_rise);
+        bn = b + dt * (-b / st->tau_decay);
+        if (fired) {
+            an = a + st->weight_prop * st->waveform_factor;
+            bn = b + st->weight_prop * st->waveform_factor;
+        }
+    }
+    P->pois_a[nxt][k] = an;
+    P->pois_b[nxt][k] = bn;
+    *iw = i * m->pois_weight[k];
+    *gw = g * m->pois_weight[k];
+}
+
+/* Synapse + input currents into one target (in the reference's order:
+ * inputs then synapses are separate totals, each synapse type a block). */
+static void target_currents(Port *P, int cur, int64_t tgt, int init, float t, float dt, int64_t step,
+                            float v, float *I_in, float *G_in, float *I_syn, float *G_syn) {
+    const EdenGpuModel *m = P->m;
+    int nxt = cur ^ 1;
+    float Iin = 0.0f, Gin = 0.0f, Isyn = 0.0f, Gsyn = 0.0f;
+    /* pulses */
+    if (P->pulse_off[tgt + 1] > P->pulse_off[tgt]) {
+        float Ip = 0.0f;
+        for (int64_t k = P->pulse_off[tgt]; k < P->pulse_off[tgt + 1]; k++) {
+            float s = m->pulse_start[k];
+            if (s <= t && t <= s + m->pulse_duration[k]) Ip += m->pulse_amplitude[k] * m->pulse_weight[k];
+        }
+        Iin += Ip;
+    }
+    /* Poisson inputs, one block per synapse type run */
+    int64_t k = P->pois_off[tgt];
+    while (k < P->pois_off[tgt + 1]) {
+        int type = m->pois_type[k];
+        float Ia = 0.0f, Ga = 0.0f;
+        for (; k < P->pois_off[tgt + 1] && m->pois_type[k] == type; k++) {
+            float iw, gw;
+            poisson_step(P, cur, k, init, dt, step, v, &iw, &gw);
+            Ia += iw; Ga += gw;
+        }
+        Iin += Ia; Gin += Ga;
+    }
+    /* connection synapses, one block per synapse type */
+    int64_t s = P->syn_off[tgt];
+    while (s < P->syn_off[tgt + 1]) {
+        int type = m->syn_type[s];
+        const EdenGpuSynapseType *st = &m->syn_types[type];
+        float Ia = 0.0f, Ga = 0.0f;
+        for (; s < P->syn_off[tgt + 1] && m->syn_type[s] == type; s++) {
+            int in = 0;
+            if (!init) {
+                in = P->trig[cur][s] != 0;
+                P->trig[cur][s] = 0;
+            }
+            float iw, gw;
+            int fired;
+            synapse_step(st, init, t, dt, in, m->syn_delay[s], P->syn_pend[cur][s], &P->syn_pend[nxt][s],
+                         P->syn_a[cur][s], P->syn_b[cur][s], &P->syn_a[nxt][s], &P->syn_b[nxt][s],
+                         v, m->syn_weight[s], &iw, &gw, &fired);
+            if (fired) P->syn_fire_count[s]++;
+            Ia += iw; Ga += gw;
+        }
+        Isyn += Ia; Gsyn += Ga;
+    }
+    *I_in = Iin; *G_in = Gin; *I_syn = Isyn; *G_syn = Gsyn;
+}
+
+static void send_spike(Port *P, int nxt, int32_t src) {
+    for (int64_t e = P->fan_off[src]; e < P->fan_off[src + 1]; e++)
+        __atomic_store_n(&P->trig[nxt][P->fan_syn[e]], (unsigned char)1, __ATOMIC_RELAXED);
+    P->spiked[nxt][src] = 1;
+}
+
+static void phys_cell_step(Port *P, int cur, int32_t cell, int init, float t, float dt, int64_t step) {
+    const EdenGpuModel *m = P->m;
+    int nxt = cur ^ 1;
+    int32_t c0 = m->phys_comp_off[cell], c1 = m->phys_comp_off[cell + 1];
+    const float *V = P->v[cur];
+    float *Vn = P->v[nxt];
+    for (int32_t c = c0; c < c1; c++) {
+        float A = m->comp_area[c], Vc = V[c];
+        float Ich = 0.0f, Gch = 0.0f;
+        for (int32_t ch = m->comp_chan_off[c]; ch < m->comp_chan_off[c + 1]; ch++) {
+            const EdenGpuChannelType *ct = &m->chan_types[m->chan_type[ch]];
+            float fopen = 1.0f;
+            int64_t go = P->gate_off[ch];
+            for (int g = 0; g < ct->n_gates; g++) {
+                float q = P->gate[cur][go + g];
+                float alpha = rate_value(ct->fwd_kind[g], ct->fwd_rate[g], ct->fwd_mid[g], ct->fwd_scale[g], Vc);
+                float beta = rate_value(ct->rev_kind[g], ct->rev_rate[g], ct->rev_mid[g], ct->rev_scale[g], Vc);
+                float tau = 1.0f / (alpha + beta);
+                float inf = alpha / (alpha + beta);
+                float qn;
+                if (init) {
+                    qn = inf;
+                } else {
+                    float tau_factor = (dt * ct->q10[g]) / tau;
+                    float blend = expf(-tau_factor);
+                    qn = blend * q + (1.0f - blend) * inf;
+                    if (!(qn > 1e-6f)) qn = 1e-6f;
+                    if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
+                }
+                P->gate[nxt][go + g] = qn;
+                for (int r = 0; r < ct->gate_instances[g]; r++) fopen = fopen * q;
+            }
+            float Gscaled = m->chan_gbase[ch] * fopen;
+            float iD = Gscaled * (m->chan_erev[ch] - Vc) * 1e-5f;
+            float gD = Gscaled * 1e-5f;
+            Ich += iD * A;
+            Gch += gD * A;
+        }
+        float Iin, Gin, Isyn, Gsyn;
+        target_currents(P, cur, c, init, t, dt, step, Vc, &Iin, &Gin, &Isyn, &Gsyn);
+        float I = Ich + Iin + Isyn;
+        float G = Gch + Gin + Gsyn;
+        P->diag[c] = 1.0f * (G / m->comp_c[c]) + m->comp_inv_rc[c];
+        Vn[c] = init ? Vc : Vc + (dt * (I + (Vc * G))) / m->comp_c[c];
+    }
+    if (!init) {
+        int32_t n = c1 - c0;
+        const int32_t *ord = P->order + c0;
+        const int32_t *par = m->comp_parent + c0;
+        const float *R = m->comp_r_axial + c0, *C = m->comp_c + c0;
+        float *D = P->diag + c0, *X = Vn + c0;
+        for (int32_t k = 0; k < n; k++) D[k] = 1.0f + D[k] * dt;
+        for (int32_t k = 0; k < n - 1; k++) {
+            int32_t i = ord[k], j = par[i];
+            int32_t idx = i > j ? i : j;
+            float Rr = R[idx];
+            float Ui = -dt / (Rr * C[i]);
+            float Uj = -dt / (Rr * C[j]);
+            float ratio = Uj / D[i];
+            D[j] -= ratio * Ui;
+            X[j] -= ratio * X[i];
+        }
+        int32_t r = ord[n - 1];
+        X[r] = X[r] / D[r];
+        for (int32_t k = n - 2; k >= 0; k--) {
+            int32_t i = ord[k], j = par[i];
+            int32_t idx = i > j ? i : j;
+            float Rr = R[idx];
+            float Ui = -dt / (Rr * C[i]);
+            X[i] = (X[i] - Ui * X[j]) / D[i];
+        }
+    }
+    for (int32_t c = c0; c < c1; c++) {
+        int32_t src = P->src_of_target[c];
+        if (src < 0) continue;
+        float thr = m->src_threshold[src];
+        if (V[c] < thr && thr < Vn[c]) send_spike(P, nxt, src);
+    }
+}
+
+static void izh_step(Port *P, int cur, int32_t k, int init, float t, float dt, int64_t step) {
+    const EdenGpuModel *m = P->m;
+    int nxt = cur ^ 1;
+    int64_t tgt = (int64_t)m->n_comp + k;
+    const float *p = m->izh_params + 10 * (int64_t)k;
+    float C = p[0], v0 = p[1], kk = p[2], vr = p[3], vt = p[4], vpeak = p[5];
+    float a = p[6], b = p[7], c = p[8], d = p[9];
+    float v = P->v[cur][tgt], u = P->izh_u[cur][k];
+    float Iin, Gin, Isyn, Gsyn;
+    target_currents(P, cur, tgt, init, t, dt, step, v, &Iin, &Gin, &Isyn, &Gsyn);
+    float iext = Isyn + Iin;
+    float iMemb = ((kk * (v - vr)) * 1e-3f) * (v - vt) + iext - u;
+    float vn, un;
+    int spike = 0;
+    if (init) {
+        vn = v0;
+        un = 0.0f;
+    } else {
+        float dv = iMemb / C;
+        vn = v + dt * dv;
+        float du = (a * ((b * (v - vr)) - u)) * 1e-3f;
+        un = u + dt * du * 1e3f;
+        if (v > vpeak) {
+            vn = c;
+            un = u + d;
+            spike = 1;
+        }
+    }
+    P->v[nxt][tgt] = vn;
+    P->izh_u[nxt][k] = un;
+    int32_t src = P->src_of_target[tgt];
+    if (spike && src >= 0) send_spike(P, nxt, src);
+}
+
+/*
+ * Run the model for `n_steps` non-initialisation steps (after the 4
+ * initialisation passes), recording V of `trace_target` at every step's
+ * output phase into trace[step][col] and every logged spike as
+ * (source, logging step).  Returns 0 or a negative code.
+ */
+int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const int32_t *trace_target,
+                  float *trace, int64_t spike_cap, int32_t *spike_src, int64_t *spike_step,
+                  int64_t *n_spikes, int64_t *syn_fire_count, float *syn_final_pending, int32_t n_threads) {
+    if (!m || m->abi_version != EDEN_GPU_ABI_VERSION) return EDEN_GPU_E_INVALID;
+    Port P;
+    memset(&P, 0, sizeof(P));
+    P.m = m;
+    int64_t nt = (int64_t)m->n_comp + m->n_izh;
+    P.n_target = nt;
+    int64_t n_chan = m->comp_chan_off[m->n_comp];
+    P.gate_off = (int64_t *)calloc((size_t)n_chan + 1, sizeof(int64_t));
+    for (int64_t ch = 0; ch < n_chan; ch++)
+        P.gate_off[ch + 1] = P.gate_off[ch] + m->chan_types[m->chan_type[ch]].n_gates;
+    int64_t n_gate = P.gate_off[n_chan];
+    int64_t ns = m->n_syn, np = m->n_pois;
+    for (int b = 0; b < 2; b++) {
+        P.v[b] = (float *)calloc((size_t)nt + 1, sizeof(float));
+        P.gate[b] = (float *)calloc((size_t)n_gate + 1, sizeof(float));
+        P.izh_u[b] = (float *)calloc((size_t)m->n_izh + 1, sizeof(float));
+        P.syn_a[b] = (float *)calloc((size_t)ns + 1, sizeof(float));
+        P.syn_b[b] = (float *)calloc((size_t)ns + 1, sizeof(float));
+        P.syn_pend[b] = (float *)calloc((size_t)ns + 1, sizeof(float));
+        P.trig[b] = (unsigned char *)calloc((size_t)ns + 1, 1);
+        P.pois_ts[b] = (float *)calloc((size_t)np + 1, sizeof(float));
+        P.pois_isi[b] = (float *)calloc((size_t)np + 1, sizeof(float));
+        P.pois_a[b] = (float *)calloc((size_t)np + 1, sizeof(float));
+        P.pois_b[b] = (float *)calloc((size_t)np + 1, sizeof(float));
+        P.spiked[b] = (unsigned char *)calloc((size_t)m->n_src + 1, 1);
+    }
+    P.diag = (float *)calloc((size_t)m->n_comp + 1, sizeof(float));
+    P.syn_fire_count = (int64_t *)calloc((size_t)ns + 1, sizeof(int64_t));
+    /* initial state: V0, izhikevich v0, pending spikes at -inf (eden/Eden.cpp:9081-9094) */
+    for (int b = 0; b < 2; b++) {
+        for (int32_t c = 0; c < m->n_comp; c++) P.v[b][c] = m->comp_v0[c];
+        for (int32_t k = 0; k < m->n_izh; k++) P.v[b][m->n_comp + k] = m->izh_params[10 * (int64_t)k + 1];
+        for (int64_t s = 0; s < ns; s++) P.syn_pend[b][s] = -INFINITY;
+    }
+    P.syn_off = csr_by_key(m->syn_target, ns, nt);
+    P.pois_off = csr_by_key(m->pois_target, np, nt);
+    P.pulse_off = csr_by_key(m->pulse_target, m->n_pulse, nt);
+    P.fan_off = csr_by_key(m->syn_src, ns, m->n_src);
+    P.fan_syn = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ns + 1));
+    {
+        int64_t *fill = (int64_t *)calloc((size_t)m->n_src + 1, sizeof(int64_t));
+        for (int64_t s = 0; s < ns; s++) {  /* connection order = synapse order */
+            int32_t src = m->syn_src[s];
+            P.fan_syn[P.fan_off[src] + fill[src]++] = s;
+        }
+        free(fill);
+    }
+    P.order = (int32_t *)malloc(sizeof(int32_t) * (size_t)(m->n_comp + 1));
+    for (int32_t cell = 0; cell < m->n_phys; cell++) {
+        int32_t c0 = m->phys_comp_off[cell], c1 = m->phys_comp_off[cell + 1];
+        dfs_postorder(m->comp_parent + c0, c1 - c0, P.order + c0);
+    }
+    P.src_of_target = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nt + 1));
+    for (int64_t t = 0; t < nt; t++) P.src_of_target[t] = -1;
+    for (int32_t s = 0; s < m->n_src; s++) P.src_of_target[m->src_target[s]] = s;
+
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+    int cur = 0;
+    double time = 0.0;
+    const float dt = m->dt;
+    int64_t nsp = 0;
+    int rc = 0;
+    int64_t last_step = n_steps;  /* steps 1..n_steps are the non-init ones */
+    for (int64_t step = -3; step <= last_step; step++) {
+        int init = step <= 0;
+        if (!init) {
+            /* output phase: trajectory columns, then event slots read & clear */
+            for (int32_t j = 0; j < n_trace; j++)
+                trace[(step - 1) * n_trace + j] = P.v[cur][trace_target[j]];
+            for (int32_t s = 0; s < m->n_src; s++) {
+                if (P.spiked[cur][s]) {
+                    if (nsp < spike_cap) {
+                        spike_src[nsp] = s;
+                        spike_step[nsp] = step;
+                    } else {
+                        rc = EDEN_GPU_E_RANGE;
+                    }
+                    nsp++;
+                }
+                P.spiked[cur][s] = 0;
+            }
+        }
+        float t = (float)time;
+        int32_t n_items = m->n_phys + m->n_izh;
+#pragma omp parallel for schedule(static)
+        for (int32_t item = 0; item < n_items; item++) {
+            if (item < m->n_phys)
+                phys_cell_step(&P, cur, item, init, t, dt, step);
+            else
+                izh_step(&P, cur, item - m->n_phys, init, t, dt, step);
+        }
+        if (!init) time += dt;
+        cur ^= 1;
+    }
+    *n_spikes = nsp;
+    if (syn_fire_count) memcpy(syn_fire_count, P.syn_fire_count, sizeof(int64_t) * (size_t)ns);
+    if (syn_final_pending) memcpy(syn_final_pending, P.syn_pend[cur], sizeof(float) * (size_t)ns);
+    for (int b = 0; b < 2; b++) {
+        free(P.v[b]); free(P.gate[b]); free(P.izh_u[b]); free(P.syn_a[b]); free(P.syn_b[b]);
+        free(P.syn_pend[b]); free(P.trig[b]); free(P.pois_ts[b]); free(P.pois_isi[b]);
+        free(P.pois_a[b]); free(P.pois_b[b]); free(P.spiked[b]);
+    }
+    free(P.diag); free(P.syn_fire_count); free(P.gate_off); free(P.syn_off); free(P.pois_off);
+    free(P.pulse_off); free(P.fan_off); free(P.fan_syn); free(P.order); free(P.src_of_target);
+    return rc;
+}

@@ -1,0 +1,66 @@
+"""GPU path vs the oracle (the C restatement of the reference loop) on the
+same seeded inputs, through the C ABI, in both execution modes.
+
+Tolerances (the reference validation harness's own criteria, restated in
+tests/criteria.py): spike trains samecount with every spike within 0.1 ms;
+membrane potential inside box(0.1 ms, 0.5 mV) of the oracle's trace.  The
+two differ only by single-precision rounding (CUDA's expf/logf against
+glibc's, and the order of the synaptic current sums), which can move a spike
+by one 25 us step; the recurrent multicompartment case is chaotic, so it is
+compared over its first 15 ms only."""
+import numpy as np
+import pytest
+
+import eden_port
+from eden_gb300 import lowering, workloads
+from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
+from criteria import box_violations, samecount
+from helpers import spike_trains
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "single_comp_hh": dict(n_cells=64, length_ms=100.0),
+    "izh_net": dict(n_cells=300, in_degree=20, length_ms=100.0),
+    "multicomp_poisson": ("multicomp_net", dict(n_cells=24, in_degree=20, length_ms=60.0, max_seg=80, weight=0.0)),
+    "multicomp_recurrent": ("multicomp_net", dict(n_cells=24, in_degree=20, length_ms=15.0, max_seg=80)),
+    "ball_and_stick": dict(n_inst=8, length_ms=40.0),
+}
+
+
+def _spec(name):
+    case = CASES[name]
+    if isinstance(case, tuple):
+        return workloads.CONFIGS[case[0]](**case[1])
+    return workloads.CONFIGS[name](**case)
+
+
+@pytest.fixture(scope="module")
+def oracle_runs():
+    cache = {}
+
+    def get(name):
+        if name not in cache:
+            low = lowering.lower(_spec(name))
+            cache[name] = (low, eden_port.run(low))
+        return cache[name]
+    return get
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+@pytest.mark.parametrize("name", list(CASES))
+def test_gpu_matches_oracle(name, mode, oracle_runs):
+    low, ref = oracle_runs(name)
+    sim = Simulation(low, mode=mode)
+    rec = sim.run()
+    sim.close()
+    assert rec.trace.shape == ref["trace"].shape
+    dt_ms = float(low.dt) * 1e-3
+    shift = int(round(0.1 / dt_ms))
+    wrong, far = samecount(spike_trains(ref["spike_src"], ref["spike_step"]),
+                           spike_trains(rec.spike_src, rec.spike_step), shift)
+    assert not wrong, f"spike counts differ for cells {wrong[:10]}"
+    assert not far, f"spikes more than 0.1 ms apart for cells {far[:10]}"
+    assert np.isfinite(rec.trace).all()
+    nbad, worst = box_violations(ref["trace"], rec.trace, dt_ms, 0.1, 0.5)
+    assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst by {worst} mV"
