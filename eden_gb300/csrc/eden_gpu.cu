@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -26,6 +27,9 @@ using namespace eden;
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kCellThreads = 128;   // k_cells_t: four warps
+constexpr int kHinesThreads = 128;  // k_hines_t: four warps, each staging one forest
+constexpr int kForestNodes = 512;   // largest forest (a larger cell gets a forest of its own)
 constexpr int kGraphWindows = 16;  // windows per captured graph
 
 struct Window {
@@ -68,9 +72,11 @@ struct EdenGpuCtx {
     int grid_inputs = 0, grid_targets = 0, grid_hines = 0, grid_deliver = 0, grid_window = 0;
     int n_sm_unused = 0;
     int smem_per_sm = 0, smem_optin = 0;   // bytes
-    int gcap = 0, forest_cap = 0;          // targets per group / compartments per forest
+    int gcap = 0, forest_cap = 0;           // largest cell / compartments per staged forest
     bool smem_window = false;              // groups fit shared memory
-    size_t smem_hines = 0, smem_win = 0;
+    size_t smem_hines = 0;
+    struct CellClass { int cta_begin, cta_end; size_t smem; };
+    std::vector<CellClass> classes;        // k_cells_t launches of one window
     double last_ms = 0.0;
     int64_t last_launches = 0;
     int sticky_status = 0;
@@ -100,21 +106,24 @@ struct EdenGpuCtx {
 // ---------------------------------------------------------------------------
 namespace eden {
 
-// Per-step path, phase 1: one warp per target with inputs.
-__global__ void __launch_bounds__(256) k_inputs_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
+// Phase 1 of both paths: input blocks over the window, one warp per target
+// with inputs (the per-step path runs it with K = 1).
+__global__ void __launch_bounds__(256, 3) k_inputs_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
+    __shared__ float tiles[8][32 * kAccStride];
+    __shared__ float tk[32];
     const WindowArgs w = tab[*base + idx];
-    const float *vin = m.v[w.par];
-    const float t = (float)w.t0;
+    if (threadIdx.x < 32) {
+        // single-precision time of each step of the window, accumulated in
+        // double from the window start as the reference accumulates it
+        double t = w.t0;
+        for (int j = 0; j < (int)threadIdx.x && w.step0 + j > 0; j++) t += (double)m.dt;
+        tk[threadIdx.x] = (float)t;
+    }
+    __syncthreads();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int ii = warp; ii < m.n_in; ii += nwarps) {
-        int tg = m.in_tgt[ii];
-        float Iin, Gin, Isyn, Gsyn;
-        inputs_warp(m, tg, w, w.step0, t, true, vin[tg], Iin, Gin, Isyn, Gsyn);
-        if ((threadIdx.x & 31) == 0) {
-            m.in_I[tg] = Iin; m.in_G[tg] = Gin; m.syn_I[tg] = Isyn; m.syn_G[tg] = Gsyn;
-        }
-    }
+    float *tile = tiles[threadIdx.x >> 5];
+    for (int c = warp; c < m.n_chunk; c += nwarps) chunk_window(m, c, w, tile, tk);
 }
 
 // Per-step path, phase 2: one thread per target.
@@ -125,14 +134,19 @@ __global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs 
     float *vout = m.v[w.par ^ 1];
     const int n = m.n_target;
     const int nround = (n + 31) & ~31;  // whole warps stay converged for the spike ballot
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += gridDim.x * blockDim.x)
-        if (i < n) target_step(m, i, init, w.step0, vin[i], m.in_I[i], m.in_G[i], m.syn_I[i], m.syn_G[i],
-                               &vout[i], &m.diag[i], w.wpar);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += gridDim.x * blockDim.x) {
+        if (i < n) {
+            float v = vin[i], Iin, Gin, Isyn, Gsyn;
+            block_currents(m.Gp, m.t_blk0[i], m.t_blk0[i + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
+                           Gsyn);
+            target_step(m, i, init, w.step0, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar);
+        }
+    }
 }
 
-// Per-step path, phase 3: one warp per forest, staged in shared memory when
-// the forest fits its warp's slice (cap floats per array), else in place.
-__global__ void __launch_bounds__(256) k_hines_t(DevModel m, const WindowArgs *tab, const int *base, int idx, int cap) {
+// Per-step path, phase 3: one warp per forest, staged in the warp's slice of
+// shared memory when the forest has at most `cap` compartments.
+__global__ void __launch_bounds__(kHinesThreads) k_hines_t(DevModel m, const WindowArgs *tab, const int *base, int idx, int cap) {
     extern __shared__ float sm[];
     const WindowArgs w = tab[*base + idx];
     const bool init = w.step0 <= 0;
@@ -140,23 +154,28 @@ __global__ void __launch_bounds__(256) k_hines_t(DevModel m, const WindowArgs *t
     float *x = m.v[w.par ^ 1];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    float *sD = sm + (size_t)wib * 5 * cap, *sX = sD + cap, *sU = sX + cap, *sL = sU + cap, *sV = sL + cap;
+    // per-warp slice: D, X, U, L, V, child ends, parents, depth boundaries (cap each)
+    float *sD = sm + (size_t)wib * 8 * cap, *sX = sD + cap, *sU = sX + cap, *sL = sU + cap, *sV = sL + cap;
+    int32_t *sCE = (int32_t *)(sV + cap), *sP = sCE + cap, *sLV = sP + cap;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int f = warp; f < m.n_forest; f += nwarps) {
-        const int c0 = m.fo_t0[f], n = m.fo_t1[f] - c0;
-        if (n <= cap) {
+        const int c0 = m.fo_t0[f], n = m.fo_t1[f] - c0, nlev = m.fo_nlev[f];
+        const int32_t *lv = m.lvl + m.fo_l0[f];
+        if (n <= cap && nlev < cap) {
             for (int i = lane; i < n; i += 32) {
                 sD[i] = m.diag[c0 + i]; sX[i] = x[c0 + i]; sU[i] = m.c_u[c0 + i];
                 sL[i] = m.c_l[c0 + i]; sV[i] = vin[c0 + i];
+                sCE[i] = m.c_cend[c0 + i] - c0; sP[i] = m.c_parent[c0 + i] - c0;
             }
+            for (int i = lane; i <= nlev; i += 32) sLV[i] = lv[i] - c0;
             __syncwarp();
-            hines_forest(m, f, init, w.step0, sD, sX, sU, sL, sV, c0, w.wpar);
+            hines_forest(m, init, w.step0, sD, sX, sU, sL, sCE, sP, sLV, nlev, sV, c0, w.wpar, true);
             __syncwarp();
             for (int i = lane; i < n; i += 32) x[c0 + i] = sX[i];
             __syncwarp();
         } else {
-            hines_forest(m, f, init, w.step0, m.diag, x, m.c_u, m.c_l, vin, 0, w.wpar);
+            hines_forest(m, init, w.step0, m.diag, x, m.c_u, m.c_l, m.c_cend, m.c_parent, lv, nlev, vin, 0, w.wpar, true);
         }
     }
 }
@@ -198,70 +217,189 @@ __global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs 
 // emitted inside the window cannot fire a synapse before the window ends.
 // Its trigger bits are delivered after the window (k_deliver_t) and replayed
 // in order at the start of the next one (replay_mask), which reproduces the
-// step-by-step pending-spike decisions exactly.  The group's membrane
-// potentials, Hines diagonal and off-diagonals and per-target input currents
-// live in shared memory for the whole window (gcap targets per group).
-template <bool SMEM>
-__global__ void __launch_bounds__(256) k_window_t(DevModel m, const WindowArgs *tab, const int *base, int idx, int gcap) {
+// step-by-step pending-spike decisions exactly.  Synaptic conductances do not
+// depend on V, so k_inputs_t has already produced them for all K steps.
+// Everything else a step touches -- membrane potentials, compartment
+// constants, channels and gates, the tree and its depth boundaries, input
+// block kinds -- is staged in shared memory for the whole window.
+// Windowed path: every warp advances one unit (a forest of physical cells or
+// a batch of izhikevich neurons) K steps on its own, synchronising only within
+// the warp.  Within a window no cell reads another cell's state: the only
+// coupling is through synaptic triggers, and every connection delay is
+// >= K * dt, so a spike emitted inside the window cannot fire a synapse before
+// the window ends.  Its trigger bits are delivered after the window
+// (k_deliver_t) and replayed in order at the start of the next one
+// (replay_mask), which reproduces the step-by-step pending-spike decisions
+// exactly.  Synaptic conductances do not depend on V, so k_inputs_t has
+// already produced them for all K steps.  Everything else a step reads is
+// staged in the warp's shared-memory slice for the whole window.
+// This launch runs CTAs [cta_begin, cta_end).
+__global__ void __launch_bounds__(kCellThreads) k_cells_t(DevModel m, const WindowArgs *tab, const int *base, int idx,
+                                                          int cta_begin, int cta_end) {
     extern __shared__ float sm[];
     const WindowArgs w = tab[*base + idx];
+    const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int nwarps = blockDim.x >> 5;
-    for (int g = blockIdx.x; g < m.n_group; g += gridDim.x) {
-        const int t0 = m.g_t0[g], n = m.g_t1[g] - t0;
-        float *V[2], *D, *U, *L, *sIin, *sGin, *sIsyn, *sGsyn;
-        int b0;
-        if (SMEM) {
-            V[0] = sm; V[1] = sm + gcap; D = sm + 2 * gcap; U = sm + 3 * gcap; L = sm + 4 * gcap;
-            sIin = sm + 5 * gcap; sGin = sm + 6 * gcap; sIsyn = sm + 7 * gcap; sGsyn = sm + 8 * gcap;
-            b0 = t0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                V[w.par][i] = m.v[w.par][t0 + i];
-                U[i] = m.c_u[t0 + i];
-                L[i] = m.c_l[t0 + i];
-                sIin[i] = 0.f; sGin[i] = 0.f; sIsyn[i] = 0.f; sGsyn[i] = 0.f;
+    for (int cta = cta_begin + blockIdx.x; cta < cta_end; cta += gridDim.x) {
+        const int u = m.cta_u0[cta] + warp;
+        if (u >= m.cta_u0[cta + 1]) continue;
+        const int t0 = m.un_t0[u], n = m.un_t1[u] - t0, fi = m.un_f[u];
+        const int ngt = m.un_ngt[u], gt0 = m.un_gt0[u];
+        const int s0 = m.un_s0[u], ns = m.un_s1[u] - s0;
+        const int r0 = m.un_r0[u], r1 = m.un_r1[u];
+        const int nlev = fi >= 0 ? m.fo_nlev[fi] : 0;
+        const int l0 = fi >= 0 ? m.fo_l0[fi] : 0;
+        float *S = sm + m.un_off[u];
+        float *V[2] = {S, S + n};
+        float *D = S + 2 * n, *U = S + 3 * n, *L = S + 4 * n;
+        int32_t *CE = (int32_t *)(S + 5 * n), *P = CE + n;
+        float *FG = S + 7 * n, *FE = S + 8 * n, *FGC = S + 9 * n, *FD0 = S + 10 * n, *FA = S + 11 * n, *FC = S + 12 * n;
+        float *GT = S + 13 * n;
+        int32_t *GI_T = (int32_t *)(GT + ngt), *GI_TG = GI_T + ngt;
+        int32_t *LV = GI_TG + ngt;
+        int32_t *ST = LV + nlev + 1, *SSRC = ST + ns;
+        float *STHR = (float *)(SSRC + ns);
+        // izhikevich batches keep their parameters and u in the compartment slots
+        float *IZ[11] = {D, U, L, (float *)CE, (float *)P, FG, FE, FGC, FD0, FA, FC};
+        const int izh0 = fi < 0 ? m.t_izh[t0] : 0;
+        // ---- stage the unit
+        for (int i = lane; i < n; i += 32) {
+            const int t = t0 + i;
+            V[w.par][i] = m.v[w.par][t];
+            if (fi >= 0) {
+                U[i] = m.c_u[t]; L[i] = m.c_l[t];
+                CE[i] = m.c_cend[t] - t0; P[i] = m.c_parent[t] - t0;
+                FG[i] = m.flat_g[t]; FE[i] = m.flat_e[t]; FGC[i] = m.flat_gc[t]; FD0[i] = m.flat_d0[t];
+                FA[i] = m.c_area[t]; FC[i] = m.c_cm[t];
+            } else {
+                const int iz = izh0 + i;
+                IZ[0][i] = m.iz_C[iz]; IZ[1][i] = m.iz_v0[iz]; IZ[2][i] = m.iz_k[iz]; IZ[3][i] = m.iz_vr[iz];
+                IZ[4][i] = m.iz_vt[iz]; IZ[5][i] = m.iz_vpeak[iz]; IZ[6][i] = m.iz_a[iz]; IZ[7][i] = m.iz_b[iz];
+                IZ[8][i] = m.iz_c[iz]; IZ[9][i] = m.iz_d[iz]; IZ[10][i] = m.iz_u[iz];
             }
-            __syncthreads();
-        } else {
-            V[0] = m.v[0]; V[1] = m.v[1]; D = m.diag; U = const_cast<float *>(m.c_u); L = const_cast<float *>(m.c_l);
-            sIin = m.in_I; sGin = m.in_G; sIsyn = m.syn_I; sGsyn = m.syn_G;
-            b0 = 0;
         }
+        for (int i = lane; i < ngt; i += 32) GT[i] = m.gate[gt0 + i];
+        if (fi >= 0) {
+            // gate update items: (target, gate number | channel type << 8)
+            for (int i = lane; i < n; i += 32) {
+                for (int ch = m.c_chan0[t0 + i]; ch < m.c_chan0[t0 + i + 1]; ch++) {
+                    const int q0 = m.ch_gate0[ch] - gt0, q1 = m.ch_gate0[ch + 1] - gt0;
+                    for (int q = q0; q < q1; q++) { GI_T[q] = i; GI_TG[q] = (q - q0) | (m.ch_type[ch] << 8); }
+                }
+            }
+            for (int i = lane; i <= nlev; i += 32) LV[i] = m.lvl[l0 + i] - t0;
+        }
+        for (int i = lane; i < ns; i += 32) { ST[i] = m.gs_t[s0 + i]; SSRC[i] = m.gs_src[s0 + i]; STHR[i] = m.gs_thr[s0 + i]; }
+        __syncwarp();
         int par = w.par;
-        double time = w.t0;
         for (int k = 0; k < w.K; k++) {
             const int64_t step = w.step0 + k;
             const bool init = step <= 0;
-            const float t = (float)time;
-            float *vin = V[par], *vout = V[par ^ 1];
-            for (int ii = m.g_i0[g] + warp; ii < m.g_i1[g]; ii += nwarps) {
-                int tg = m.in_tgt[ii];
-                float Iin, Gin, Isyn, Gsyn;
-                inputs_warp(m, tg, w, step, t, k == 0, vin[tg - b0], Iin, Gin, Isyn, Gsyn);
-                if ((threadIdx.x & 31) == 0) {
-                    sIin[tg - b0] = Iin; sGin[tg - b0] = Gin; sIsyn[tg - b0] = Isyn; sGsyn[tg - b0] = Gsyn;
-                }
-            }
-            __syncthreads();
-            const int nround = (n + 31) & ~31;
-            for (int i = threadIdx.x; i < nround; i += blockDim.x) {
+            const float *vin = V[par];
+            float *vout = V[par ^ 1];
+            const float *Gpk = m.Gp + (size_t)k * m.n_chunk;
+            const float dt = m.dt;
+            for (int i0 = 0; i0 < n; i0 += 32) {
+                const int i = i0 + lane;
+                bool spike = false;
+                int src = -1;
                 if (i < n) {
-                    int tl = t0 + i - b0;
-                    target_step(m, t0 + i, init, step, vin[tl], sIin[tl], sGin[tl], sIsyn[tl], sGsyn[tl], &vout[tl],
-                                &D[tl], w.wpar);
+                    const int t = t0 + i;
+                    const float v = vin[i];
+                    if (fi >= 0 && FG[i] >= 0.0f) {
+                        // one gateless channel, no inputs (eden/Eden.cpp:5805-5898, 6057-6107)
+                        const float I = (FG[i] * (FE[i] - v) * 1e-5f) * FA[i];
+                        D[i] = FD0[i];
+                        vout[i] = init ? v : v + (dt * ((I + 0.0f + 0.0f) + (v * FGC[i]))) / FC[i];
+                    } else {
+                        float Iin, Gin, Isyn, Gsyn;
+                        block_currents(Gpk, m.t_blk0[t], m.t_blk0[t + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin,
+                                       Gin, Isyn, Gsyn);
+                        if (fi >= 0) {
+                            // channels + voltage pre-update (eden/Eden.cpp:5013-6107)
+                            const float A = FA[i];
+                            float Ich = 0.f, Gch = 0.f;
+                            for (int ch = m.c_chan0[t]; ch < m.c_chan0[t + 1]; ch++) {
+                                const ChanTypeDev &ct = c_chan_types[m.ch_type[ch]];
+                                float fopen = 1.0f;
+                                const float *q = GT + (m.ch_gate0[ch] - gt0);
+                                for (int gi = 0; gi < ct.n_gates; gi++) {
+                                    const float qo = q[gi];
+                                    for (int rr = 0; rr < ct.inst[gi]; rr++) fopen = fopen * qo;
+                                }
+                                const float gs = m.ch_gbase[ch] * fopen;
+                                Ich += (gs * (m.ch_erev[ch] - v) * 1e-5f) * A;
+                                Gch += (gs * 1e-5f) * A;
+                            }
+                            const float I = Ich + Iin + Isyn;
+                            const float G = Gch + Gin + Gsyn;
+                            const float C = FC[i];
+                            D[i] = 1.0f * (G / C) + m.c_inv_rc[t];
+                            vout[i] = init ? v : v + (dt * (I + (v * G))) / C;
+                        } else {
+                            // izhikevich2007Cell (LEMS_CoreComponents.inc.xml:1140-1185)
+                            const float u = IZ[10][i];
+                            const float vr = IZ[3][i];
+                            const float imemb = ((IZ[2][i] * (v - vr)) * 1e-3f) * (v - IZ[4][i]) + (Isyn + Iin) - u;
+                            float vn, un;
+                            if (init) {
+                                vn = IZ[1][i];
+                                un = 0.0f;
+                            } else {
+                                vn = v + dt * (imemb / IZ[0][i]);
+                                const float du = (IZ[6][i] * ((IZ[7][i] * (v - vr)) - u)) * 1e-3f;
+                                un = u + dt * du * 1e3f;
+                                if (v > IZ[5][i]) {
+                                    vn = IZ[8][i];
+                                    un = u + IZ[9][i];
+                                    spike = true;
+                                }
+                            }
+                            vout[i] = vn;
+                            IZ[10][i] = un;
+                            src = m.t_src[t];
+                        }
+                    }
                 }
+                if (fi < 0) push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar);
             }
-            __syncthreads();
-            for (int f = m.g_f0[g] + warp; f < m.g_f1[g]; f += nwarps)
-                hines_forest(m, f, init, step, D, vout, U, L, vin, b0, w.wpar);
-            __syncthreads();
+            if (!init) {
+                // trajectory samples of this step's starting state
+                const int64_t row = (step - 1) % m.trace_cap;
+                for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = vin[m.gr_t[q]];
+            }
+            __syncwarp();
+            if (fi >= 0) {
+                hines_forest(m, init, step, D, vout, U, L, CE, P, LV, nlev, vin, t0, w.wpar, false);
+                __syncwarp();
+                // gate updates from this step's V and gate values (the currents
+                // above used the values before the update, as the reference does)
+                for (int q = lane; q < ngt; q += 32) {
+                    const int tg = GI_TG[q];
+                    GT[q] = gate_next(c_chan_types[tg >> 8], tg & 0xff, init, dt, vin[GI_T[q]], GT[q]);
+                }
+                // threshold crossings of the unit's spike sources (eden/Eden.cpp:6247-6252)
+                for (int q0 = 0; q0 < ns; q0 += 32) {
+                    const int q = q0 + lane;
+                    bool spk = false;
+                    int src2 = -1;
+                    if (q < ns) {
+                        const int tl = ST[q];
+                        src2 = SSRC[q];
+                        spk = vin[tl] < STHR[q] && STHR[q] < vout[tl];
+                    }
+                    push_spike(m, spk, src2, (int32_t)(step + 1), w.wpar);
+                }
+                __syncwarp();
+            }
             par ^= 1;
-            if (!init) time += (double)m.dt;
         }
-        if (SMEM) {
-            for (int i = threadIdx.x; i < n; i += blockDim.x) m.v[par][t0 + i] = V[par][i];
-            __syncthreads();
+        // ---- write the unit back
+        for (int i = lane; i < n; i += 32) {
+            m.v[par][t0 + i] = V[par][i];
+            if (fi < 0) m.iz_u[izh0 + i] = IZ[10][i];
         }
+        for (int i = lane; i < ngt; i += 32) m.gate[gt0 + i] = GT[i];
     }
 }
 
@@ -457,138 +595,141 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         total += c;
     }
 
-    // ---- groups: contiguous cells, balanced work, at most gcap targets
-    // gcap is sized so that four CTAs fit an SM's shared memory
-    const int smem_per_sm = ctx->smem_per_sm;
-    int gcap = std::max(256, std::min(4096, (smem_per_sm / 4) / (9 * (int)sizeof(float))));
-    gcap = std::max(gcap, max_cell);
-    ctx->smem_window = (size_t)gcap * 9 * sizeof(float) <= (size_t)ctx->smem_optin;
-    int cells_per_block = opt ? opt->cells_per_block : 0;
-    int want_groups = std::max(1, ctx->n_sm * 4 * 2);
-    std::vector<std::pair<int, int>> groups;  // [cell0, cell1)
-    {
-        double target = total / want_groups;
-        int g = 0;
-        while (g < n_cells) {
-            int start = g, ntg = 0;
-            double acc = 0;
-            if (cells_per_block > 0) {
-                while (g < n_cells && g - start < cells_per_block && (ntg + cell_n[g] <= gcap || g == start))
-                    ntg += cell_n[g++];
-            } else {
-                while (g < n_cells && (acc < target || g == start) && (ntg + cell_n[g] <= gcap || g == start)) {
-                    acc += cost[g];
-                    ntg += cell_n[g++];
-                }
-            }
-            groups.push_back({start, g});
+    // ---- schedule order: physical cells by tree depth (then size), then point
+    // neurons, so that a CTA's warps finish their cable solves together
+    std::vector<int32_t> cell_levels(n_cells, 0);
+    std::vector<std::vector<int>> cell_width(n_cells);
+    for (int g = 0; g < n_cells; g++) {
+        if (cell_phys[g] < 0) continue;
+        int a = m->phys_comp_off[cell_phys[g]], b = m->phys_comp_off[cell_phys[g] + 1];
+        std::vector<int> dep(b - a, 0);
+        int mx = 0;
+        for (int i = 1; i < b - a; i++) {
+            dep[i] = dep[m->comp_parent[a + i]] + 1;
+            mx = std::max(mx, dep[i]);
         }
+        cell_levels[g] = mx + 1;
+        cell_width[g].assign(mx + 1, 0);
+        for (int i = 0; i < b - a; i++) cell_width[g][dep[i]]++;
     }
+    std::vector<int32_t> order(n_cells);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        bool ix = cell_phys[x] < 0, iy = cell_phys[y] < 0;
+        if (ix != iy) return iy;  // physical cells first
+        if (cell_levels[x] != cell_levels[y]) return cell_levels[x] < cell_levels[y];
+        return cell_n[x] < cell_n[y];
+    });
 
-    // ---- internal order: per group, per forest a joint breadth-first order
+    // ---- units: each warp of the windowed kernel owns one unit for the whole
+    // window -- a forest of physical cells (joint breadth-first numbering,
+    // at most 32 nodes per depth level, at most kForestNodes nodes) or a batch
+    // of up to 32 izhikevich neurons.  Targets are numbered unit by unit.
+    const int forest_node_cap = kForestNodes;
     std::vector<int32_t> u2i(nt, -1), i2u(nt, -1);
     std::vector<int32_t> c_parent(nt, -1), c_child0(nt, 0), c_nchild(nt, 0), t_izh(nt, -1);
     std::vector<float> c_u(nt, 0.f), c_l(nt, 0.f);
-    std::vector<int32_t> fo_t0, fo_t1, fo_l0, fo_nlev, lvl;
-    std::vector<int32_t> g_t0, g_t1, g_f0, g_f1;
-    const int warps_per_block = kThreads / 32;
+    std::vector<int32_t> fo_t0, fo_t1, fo_l0, fo_nlev, lvl;     // forests (also the per-step path's)
+    std::vector<int32_t> un_t0, un_t1, un_f;                    // units: targets, forest or -1
     int next = 0;
     int max_forest = 1;
+    int izh_slot = 0;
+    std::vector<int32_t> izh_user_of_slot;
     std::vector<int> coff, kids, fill;
-    for (auto &gr : groups) {
-        g_t0.push_back(next);
-        g_f0.push_back((int)fo_t0.size());
-        std::vector<int> phys;
-        for (int g = gr.first; g < gr.second; g++)
-            if (cell_phys[g] >= 0) phys.push_back(g);
-        // split the group's physical cells into up to warps_per_block forests of similar size
-        int64_t comps = 0;
-        for (int g : phys) comps += cell_n[g];
-        int nf = std::min<int>(warps_per_block, (int)phys.size());
+    {
+        std::vector<int> phys, izhs;
+        for (int k = 0; k < n_cells; k++) (cell_phys[order[k]] >= 0 ? phys : izhs).push_back(order[k]);
         size_t pi = 0;
-        int64_t acc = 0;
-        for (int f = 0; f < nf; f++) {
-            int64_t want = (comps * (f + 1)) / nf;
-            const size_t later = (size_t)(nf - 1 - f);
+        while (pi < phys.size()) {
             std::vector<int> fc;
+            std::vector<int> fw;  // the forest's node count per depth
+            int nodes = 0;
             while (pi < phys.size()) {
-                if (!fc.empty() && phys.size() - pi <= later) break;          // leave a cell per later forest
-                if (!fc.empty() && f < nf - 1 && acc + cell_n[phys[pi]] > want) break;
-                acc += cell_n[phys[pi]];
-                fc.push_back(phys[pi++]);
+                const int c = phys[pi];
+                const std::vector<int> &cw = cell_width[c];
+                bool fits = fc.empty() || nodes + cell_n[c] <= forest_node_cap;
+                for (size_t d = 0; fits && d < cw.size(); d++)
+                    if ((d < fw.size() ? fw[d] : 0) + cw[d] > 32) fits = false;
+                if (!fits && !fc.empty()) break;
+                if (fw.size() < cw.size()) fw.resize(cw.size(), 0);
+                for (size_t d = 0; d < cw.size(); d++) fw[d] += cw[d];
+                fc.push_back(c);
+                nodes += cell_n[c];
+                pi++;
             }
-            if (fc.empty()) continue;
             // joint BFS over the forest's cells
             struct Node { int cell_base; int local; int depth; };
             std::vector<Node> q;
             for (int g : fc) q.push_back({m->phys_comp_off[cell_phys[g]], 0, 0});
-            int f_t0 = next;
+            const int f_t0 = next;
+            un_t0.push_back(f_t0);
+            un_f.push_back((int)fo_t0.size());
             fo_t0.push_back(f_t0);
             fo_l0.push_back((int)lvl.size());
             lvl.push_back(f_t0);
             int depth = 0;
-            // children lists of each cell, built on first visit
             std::vector<std::vector<int>> cell_kids(fc.size());
-            std::vector<int> cell_of_base;
             for (size_t ci = 0; ci < fc.size(); ci++) {
-                int pcell = cell_phys[fc[ci]];
-                int a = m->phys_comp_off[pcell], b = m->phys_comp_off[pcell + 1], n = b - a;
-                coff.assign(n + 1, 0);
-                for (int i = 1; i < n; i++) coff[m->comp_parent[a + i] + 1]++;
-                for (int i = 0; i < n; i++) coff[i + 1] += coff[i];
-                kids.assign(n > 1 ? n - 1 : 1, 0);
-                fill.assign(n, 0);
-                for (int i = 1; i < n; i++) {
-                    int p = m->comp_parent[a + i];
-                    kids[coff[p] + fill[p]++] = i;
+                const int pcell = cell_phys[fc[ci]];
+                const int a0 = m->phys_comp_off[pcell], n0 = m->phys_comp_off[pcell + 1] - a0;
+                coff.assign(n0 + 1, 0);
+                for (int i = 1; i < n0; i++) coff[m->comp_parent[a0 + i] + 1]++;
+                for (int i = 0; i < n0; i++) coff[i + 1] += coff[i];
+                kids.assign(n0 > 1 ? n0 - 1 : 1, 0);
+                fill.assign(n0, 0);
+                for (int i = 1; i < n0; i++) {
+                    const int pp = m->comp_parent[a0 + i];
+                    kids[coff[pp] + fill[pp]++] = i;
                 }
-                // store as flattened: [coff (n+1)] [kids (n-1)]
-                std::vector<int> &ck = cell_kids[ci];
+                std::vector<int> &ck = cell_kids[ci];  // [coff (n0+1)] [kids (n0-1)]
                 ck.assign(coff.begin(), coff.end());
-                ck.insert(ck.end(), kids.begin(), kids.begin() + std::max(0, n - 1));
+                ck.insert(ck.end(), kids.begin(), kids.begin() + std::max(0, n0 - 1));
             }
-            std::vector<int> node_cell;  // forest cell index of each queued node
+            std::vector<int> node_cell;
             for (size_t ci = 0; ci < fc.size(); ci++) node_cell.push_back((int)ci);
             for (size_t h = 0; h < q.size(); h++) {
-                Node u = q[h];
-                int ci = node_cell[h];
+                const Node u = q[h];
+                const int ci = node_cell[h];
                 if (u.depth != depth) {
                     depth = u.depth;
                     lvl.push_back(f_t0 + (int)h);
                 }
-                int it = f_t0 + (int)h;
-                int ut = u.cell_base + u.local;
+                const int it = f_t0 + (int)h;
+                const int ut = u.cell_base + u.local;
                 u2i[ut] = it;
                 i2u[it] = ut;
                 const std::vector<int> &ck = cell_kids[ci];
-                int pcell = cell_phys[fc[ci]];
-                int n = m->phys_comp_off[pcell + 1] - m->phys_comp_off[pcell];
-                int k0 = ck[u.local], k1 = ck[u.local + 1];
+                const int pcell = cell_phys[fc[ci]];
+                const int n0 = m->phys_comp_off[pcell + 1] - m->phys_comp_off[pcell];
+                const int k0 = ck[u.local], k1 = ck[u.local + 1];
                 c_nchild[it] = k1 - k0;
                 c_child0[it] = k1 > k0 ? f_t0 + (int)q.size() : 0;
                 for (int k = k0; k < k1; k++) {
-                    q.push_back({u.cell_base, ck[n + 1 + k], u.depth + 1});
+                    q.push_back({u.cell_base, ck[n0 + 1 + k], u.depth + 1});
                     node_cell.push_back(ci);
                 }
             }
-            int fn = (int)q.size();
+            const int fn = (int)q.size();
             lvl.push_back(f_t0 + fn);
             fo_nlev.push_back(depth + 1);
             fo_t1.push_back(f_t0 + fn);
             max_forest = std::max(max_forest, fn);
             next += fn;
+            un_t1.push_back(next);
         }
-        // the group's izhikevich neurons follow its forests
-        for (int g = gr.first; g < gr.second; g++) {
-            if (cell_izh[g] < 0) continue;
-            int ut = n_comp + cell_izh[g];
-            u2i[ut] = next;
-            i2u[next] = ut;
-            t_izh[next] = cell_izh[g];
-            next++;
+        for (size_t k = 0; k < izhs.size(); k += 32) {
+            un_t0.push_back(next);
+            un_f.push_back(-1);
+            for (size_t j = k; j < std::min(izhs.size(), k + 32); j++) {
+                const int ut = n_comp + cell_izh[izhs[j]];
+                u2i[ut] = next;
+                i2u[next] = ut;
+                t_izh[next] = izh_slot++;
+                izh_user_of_slot.push_back(cell_izh[izhs[j]]);
+                next++;
+            }
+            un_t1.push_back(next);
         }
-        g_t1.push_back(next);
-        g_f1.push_back((int)fo_t0.size());
     }
     if (next != nt) return ctx->fail(EDEN_GPU_E_INVALID, "cells not covered by spike sources");
     // parents and off-diagonals in internal numbering
@@ -605,8 +746,20 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             c_l[it] = -dt / (R * m->comp_c[a + p]);
         }
     }
+    // end of each node's child range (children of consecutive nodes are consecutive)
+    std::vector<int32_t> c_cend(nt, 0);
+    for (int it = 0; it < nt; it++) c_cend[it] = c_child0[it] + c_nchild[it];
+    for (size_t f = 0; f < fo_t0.size(); f++) {
+        // nodes without children still need the running end for their successor
+        int run = lvl[fo_l0[f] + 1 < (int)lvl.size() ? fo_l0[f] + 1 : fo_l0[f]];
+        if (fo_nlev[f] == 1) run = fo_t1[f];
+        for (int it = fo_t0[f]; it < fo_t1[f]; it++) {
+            if (c_nchild[it] > 0) run = c_child0[it] + c_nchild[it];
+            c_cend[it] = run;
+        }
+    }
     ctx->user_to_internal = u2i;
-    ctx->gcap = gcap;
+    ctx->gcap = max_cell;
     ctx->forest_cap = max_forest;
     // ---- per-target constants in internal order
     std::vector<float> c_cm(nt, 1.f), c_inv(nt, 0.f), c_area(nt, 0.f), v0(nt, 0.f);
@@ -640,11 +793,36 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (int ch = 0; ch < n_chan; ch++) ch_gate0[ch + 1] = ch_gate0[ch] + m->chan_types[ch_type[ch]].n_gates;
     int n_gate = ch_gate0[n_chan];
 
-    // izhikevich structure of arrays
+    // flat parameters of compartments with one gateless channel and no inputs
+    std::vector<float> flat_g(nt, -1.0f), flat_e(nt, 0.f), flat_gc(nt, 0.f), flat_d0(nt, 0.f);
+    {
+        std::vector<char> has_input(nt, 0);
+        for (int64_t k = 0; k < m->n_pulse; k++) has_input[u2i[m->pulse_target[k]]] = 1;
+        for (int64_t k = 0; k < m->n_pois; k++) has_input[u2i[m->pois_target[k]]] = 1;
+        for (int64_t k = 0; k < m->n_syn; k++) has_input[u2i[m->syn_target[k]]] = 1;
+        for (int it = 0; it < nt; it++) {
+            if (t_izh[it] >= 0 || has_input[it]) continue;
+            if (c_chan0[it + 1] - c_chan0[it] != 1) continue;
+            const int ch = c_chan0[it];
+            if (m->chan_types[ch_type[ch]].n_gates != 0) continue;
+            const float g = ch_g[ch];
+            if (!(g >= 0.0f)) continue;
+            // the same operations as the general path with fopen = 1 and no inputs
+            const float gs = g * 1.0f;
+            const float Gc = (gs * 1e-5f) * c_area[it];
+            const float G = Gc + 0.0f + 0.0f;
+            flat_g[it] = gs;
+            flat_e[it] = ch_e[ch];
+            flat_gc[it] = G;
+            flat_d0[it] = 1.0f * (G / c_cm[it]) + c_inv[it];
+        }
+    }
+
+    // izhikevich structure of arrays, in slot (internal) order
     std::vector<float> iz[10];
     for (int f = 0; f < 10; f++) {
         iz[f].resize(n_izh);
-        for (int k = 0; k < n_izh; k++) iz[f][k] = m->izh_params[10 * (int64_t)k + f];
+        for (int k = 0; k < n_izh; k++) iz[f][k] = m->izh_params[10 * (int64_t)izh_user_of_slot[k] + f];
     }
 
     // ---- inputs sorted by internal target (then type, then input order)
@@ -671,11 +849,6 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     std::vector<int64_t> qoff = offsets(qord, m->pulse_target);
     std::vector<int64_t> poff = offsets(pord, m->pois_target);
     std::vector<int64_t> soff = offsets(sord, m->syn_target);
-    std::vector<int32_t> t_pulse0(nt + 1), t_pois0(nt + 1);
-    for (int t = 0; t <= nt; t++) {
-        t_pulse0[t] = (int32_t)qoff[t];
-        t_pois0[t] = (int32_t)poff[t];
-    }
     std::vector<float> pu_s(m->n_pulse), pu_d(m->n_pulse), pu_a(m->n_pulse), pu_w(m->n_pulse);
     for (int64_t k = 0; k < m->n_pulse; k++) {
         int64_t o = qord[k];
@@ -683,7 +856,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         pu_a[k] = m->pulse_amplitude[o]; pu_w[k] = m->pulse_weight[o];
     }
     std::vector<float> po_rate(m->n_pois), po_w(m->n_pois);
-    std::vector<int32_t> po_seed(m->n_pois), po_inst(m->n_pois), po_tgt(m->n_pois);
+    std::vector<int32_t> po_seed(m->n_pois), po_inst(m->n_pois);
     std::vector<uint8_t> po_type(m->n_pois);
     for (int64_t k = 0; k < m->n_pois; k++) {
         int64_t o = pord[k];
@@ -691,20 +864,17 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         po_seed[k] = m->src_cell_seed[m->pois_src[o]];
         po_inst[k] = m->pois_instance[o];
         po_type[k] = (uint8_t)m->pois_type[o];
-        po_tgt[k] = u2i[m->pois_target[o]];
     }
     const int64_t ns = m->n_syn;
     ctx->n_syn = ns;
     std::vector<float> sy_w(ns), sy_d(ns), sy_pend(ns, -INFINITY);
     std::vector<uint8_t> sy_type(ns);
-    std::vector<int32_t> sy_tgt(ns);
     ctx->syn_internal_of_user.assign(ns, 0);
     float min_delay = INFINITY;
     for (int64_t k = 0; k < ns; k++) {
         int64_t o = sord[k];
         sy_w[k] = m->syn_weight[o]; sy_d[k] = m->syn_delay[o];
         sy_type[k] = (uint8_t)m->syn_type[o];
-        sy_tgt[k] = u2i[m->syn_target[o]];
         ctx->syn_internal_of_user[o] = k;
         min_delay = std::min(min_delay, m->syn_delay[o]);
     }
@@ -726,12 +896,56 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         t_src[u2i[m->src_target[s]]] = s;
         src_thr[s] = m->src_threshold[s];
     }
+    // input blocks per target: pulses, then Poisson runs, then synapse runs of one type
+    std::vector<int32_t> t_blk0(nt + 1, 0);
+    std::vector<int32_t> bk_kind;
+    std::vector<uint8_t> bk_type;
+    std::vector<float> bk_erev;
+    std::vector<int64_t> bk_i0, bk_i1;
+    std::vector<int32_t> in_tgt;
+    for (int t = 0; t < nt; t++) {
+        t_blk0[t] = (int32_t)bk_kind.size();
+        if (qoff[t + 1] > qoff[t]) {
+            bk_kind.push_back(BK_PULSE); bk_erev.push_back(0.f); bk_type.push_back(0);
+            bk_i0.push_back(qoff[t]); bk_i1.push_back(qoff[t + 1]);
+        }
+        for (int64_t k = poff[t]; k < poff[t + 1];) {
+            int64_t k1 = k;
+            while (k1 < poff[t + 1] && po_type[k1] == po_type[k]) k1++;
+            bk_kind.push_back(BK_POIS); bk_erev.push_back(m->syn_types[po_type[k]].erev); bk_type.push_back(po_type[k]);
+            bk_i0.push_back(k); bk_i1.push_back(k1);
+            k = k1;
+        }
+        for (int64_t k = soff[t]; k < soff[t + 1];) {
+            int64_t k1 = k;
+            while (k1 < soff[t + 1] && sy_type[k1] == sy_type[k]) k1++;
+            bk_kind.push_back(BK_SYN); bk_erev.push_back(m->syn_types[sy_type[k]].erev); bk_type.push_back(sy_type[k]);
+            bk_i0.push_back(k); bk_i1.push_back(k1);
+            k = k1;
+        }
+        if ((int)bk_kind.size() > t_blk0[t]) in_tgt.push_back(t);
+    }
+    t_blk0[nt] = (int32_t)bk_kind.size();
+    const int n_block = (int)bk_kind.size();
+    // chunks of at most 32 items per block
+    std::vector<int32_t> bk_c0(n_block + 1, 0), ck_blk, ck_n;
+    std::vector<int64_t> ck_i0;
+    for (int b = 0; b < n_block; b++) {
+        bk_c0[b] = (int32_t)ck_blk.size();
+        for (int64_t i = bk_i0[b]; i < bk_i1[b]; i += 32) {
+            ck_blk.push_back(b);
+            ck_i0.push_back(i);
+            ck_n.push_back((int32_t)std::min<int64_t>(32, bk_i1[b] - i));
+        }
+    }
+    bk_c0[n_block] = (int32_t)ck_blk.size();
+    const int n_chunk = (int)ck_blk.size();
 
     // ---- window length: every delay must cover the window (see k_window)
-    int kmax = 31;
+    int kmax = kMaxWindow;
     if (ns > 0) {
         double dsteps = std::floor((double)min_delay / (double)dt);
-        kmax = (int)std::max(1.0, std::min(31.0, dsteps));
+        kmax = (int)std::max(1.0, std::min((double)kMaxWindow, dsteps));
     }
     ctx->mode = opt ? opt->mode : EDEN_MODE_PLAIN;
     int kreq = (opt && opt->steps_per_launch > 0) ? opt->steps_per_launch : kmax;
@@ -755,46 +969,118 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     ctx->trace_cap = (opt && opt->record_capacity_steps > 0) ? opt->record_capacity_steps : 4096;
     int64_t log_cap = (opt && opt->spike_capacity > 0) ? opt->spike_capacity : (int64_t)1 << 22;
 
-    // ---- upload
-    DevModel &d = ctx->d;
-    // targets with any input, in internal order; each group's are contiguous
-    std::vector<int32_t> in_tgt, g_i0, g_i1;
+    // ---- per-unit lists of the windowed kernel: spike sources and recorded
+    // targets (unit-local indices), gates, and each unit's shared-memory words
+    const int n_unit = (int)un_t0.size();
+    std::vector<int32_t> un_gt0(n_unit), un_ngt(n_unit), un_s0(n_unit), un_s1(n_unit), un_r0(n_unit), un_r1(n_unit);
+    std::vector<int32_t> gs_t, gs_src, gr_t, gr_col;
+    std::vector<float> gs_thr;
+    std::vector<int> un_words(n_unit);
+    for (int u = 0; u < n_unit; u++) {
+        const int a = un_t0[u], b = un_t1[u];
+        un_s0[u] = (int)gs_t.size();
+        if (un_f[u] >= 0)
+            for (int t = a; t < b; t++)
+                if (t_src[t] >= 0) { gs_t.push_back(t - a); gs_src.push_back(t_src[t]); gs_thr.push_back(src_thr[t_src[t]]); }
+        un_s1[u] = (int)gs_t.size();
+        un_r0[u] = (int)gr_t.size();
+        for (int t = a; t < b; t++)
+            for (int k = t_trace0[t]; k < t_trace0[t + 1]; k++) { gr_t.push_back(t - a); gr_col.push_back(trace_col[k]); }
+        un_r1[u] = (int)gr_t.size();
+        un_gt0[u] = ch_gate0[c_chan0[a]];
+        un_ngt[u] = ch_gate0[c_chan0[b]] - un_gt0[u];
+        const int nlev = un_f[u] >= 0 ? fo_nlev[un_f[u]] : 0;
+        un_words[u] = unit_words(b - a, un_ngt[u], nlev, un_s1[u] - un_s0[u]);
+    }
+    // CTAs of up to four units, packed longest-first onto the CTA with the
+    // fewest words so that every CTA needs about the same shared memory
+    const int upc = kCellThreads / 32;
+    const int n_cta = (n_unit + upc - 1) / upc;
+    std::vector<int> uorder(n_unit);
+    std::iota(uorder.begin(), uorder.end(), 0);
+    std::stable_sort(uorder.begin(), uorder.end(), [&](int x, int y) { return un_words[x] > un_words[y]; });
+    std::vector<std::vector<int>> cta_units(n_cta);
+    std::vector<int> cta_words(n_cta, 0);
     {
-        size_t gi = 0;
-        for (size_t gg = 0; gg < g_t0.size(); gg++) {
-            g_i0.push_back((int)in_tgt.size());
-            for (int t = g_t0[gg]; t < g_t1[gg]; t++)
-                if (t_pulse0[t + 1] > t_pulse0[t] || t_pois0[t + 1] > t_pois0[t] || soff[t + 1] > soff[t])
-                    in_tgt.push_back(t);
-            g_i1.push_back((int)in_tgt.size());
-            gi++;
+        // min-heap of (words, cta) over CTAs that still have room
+        std::vector<std::pair<int, int>> heap;
+        for (int c = 0; c < n_cta; c++) heap.push_back({0, c});
+        auto cmp = [](const std::pair<int, int> &x, const std::pair<int, int> &y) { return x > y; };
+        std::make_heap(heap.begin(), heap.end(), cmp);
+        for (int uu : uorder) {
+            std::pop_heap(heap.begin(), heap.end(), cmp);
+            auto top = heap.back();
+            heap.pop_back();
+            cta_units[top.second].push_back(uu);
+            cta_words[top.second] += un_words[uu];
+            if ((int)cta_units[top.second].size() < upc) {
+                heap.push_back({cta_words[top.second], top.second});
+                std::push_heap(heap.begin(), heap.end(), cmp);
+            }
         }
     }
-    d.n_target = nt; d.n_src = m->n_src; d.n_group = (int)g_t0.size(); d.n_forest = (int)fo_t0.size();
+    std::vector<int32_t> cta_u0, un_off(n_unit, 0), unit_of_slot;
+    for (int c = 0; c < n_cta; c++) {
+        cta_u0.push_back((int)unit_of_slot.size());
+        for (int uu : cta_units[c]) unit_of_slot.push_back(uu);
+    }
+    cta_u0.push_back((int)unit_of_slot.size());
+    // units are referenced through their CTA slot: renumber the unit tables in slot order
+    auto perm = [&](std::vector<int32_t> &v) {
+        std::vector<int32_t> o(v.size());
+        for (size_t j = 0; j < unit_of_slot.size(); j++) o[j] = v[unit_of_slot[j]];
+        v.swap(o);
+    };
+    for (auto *v : {&un_t0, &un_t1, &un_f, &un_gt0, &un_ngt, &un_s0, &un_s1, &un_r0, &un_r1}) perm(*v);
+    {
+        std::vector<int> w2(n_unit);
+        for (int j = 0; j < n_unit; j++) w2[j] = un_words[unit_of_slot[j]];
+        un_words.swap(w2);
+    }
+    for (size_t c = 0; c + 1 < cta_u0.size(); c++) {
+        int off = 0;
+        for (int j = cta_u0[c]; j < cta_u0[c + 1]; j++) { un_off[j] = off; off += un_words[j]; }
+    }
+    // one launch over all CTAs, sized by the largest
+    ctx->classes.clear();
+    {
+        int mx = 1;
+        for (int c = 0; c < n_cta; c++) mx = std::max(mx, cta_words[c]);
+        ctx->classes.push_back({0, n_cta, (size_t)mx * sizeof(float)});
+    }
+    size_t max_smem_class = 0;
+    for (auto &cl : ctx->classes) max_smem_class = std::max(max_smem_class, cl.smem);
+    ctx->smem_window = max_smem_class <= (size_t)ctx->smem_optin;
+
+    // ---- upload
+    DevModel &d = ctx->d;
+    d.n_target = nt; d.n_src = m->n_src; d.n_unit = n_unit; d.n_forest = (int)fo_t0.size();
     d.n_in = (int)in_tgt.size();
+    d.n_block = n_block;
+    d.n_chunk = n_chunk;
     d.n_syn = ns; d.n_pois = m->n_pois; d.dt = dt;
     TRY(upload_vec(ctx, &d.v[0], v0));
     TRY(upload_vec(ctx, &d.v[1], v0));
     TRY(upload(ctx, &d.diag, (const float *)nullptr, nt));
     TRY(upload_c(ctx, &d.c_cm, c_cm)); TRY(upload_c(ctx, &d.c_inv_rc, c_inv)); TRY(upload_c(ctx, &d.c_area, c_area));
     TRY(upload_c(ctx, &d.c_u, c_u)); TRY(upload_c(ctx, &d.c_l, c_l));
-    TRY(upload_c(ctx, &d.c_nchild, c_nchild)); TRY(upload_c(ctx, &d.c_child0, c_child0));
-    TRY(upload_c(ctx, &d.c_parent, c_parent)); TRY(upload_c(ctx, &d.t_izh, t_izh));
+    TRY(upload_c(ctx, &d.c_cend, c_cend)); TRY(upload_c(ctx, &d.c_parent, c_parent));
+    TRY(upload_c(ctx, &d.flat_g, flat_g)); TRY(upload_c(ctx, &d.flat_e, flat_e));
+    TRY(upload_c(ctx, &d.flat_gc, flat_gc)); TRY(upload_c(ctx, &d.flat_d0, flat_d0)); TRY(upload_c(ctx, &d.t_izh, t_izh));
     TRY(upload_c(ctx, &d.fo_t0, fo_t0)); TRY(upload_c(ctx, &d.fo_t1, fo_t1)); TRY(upload_c(ctx, &d.fo_l0, fo_l0));
     TRY(upload_c(ctx, &d.fo_nlev, fo_nlev)); TRY(upload_c(ctx, &d.lvl, lvl));
     TRY(upload_c(ctx, &d.in_tgt, in_tgt));
-    TRY(upload(ctx, &d.in_I, (const float *)nullptr, (size_t)nt));
-    TRY(upload(ctx, &d.in_G, (const float *)nullptr, (size_t)nt));
-    TRY(upload(ctx, &d.syn_I, (const float *)nullptr, (size_t)nt));
-    TRY(upload(ctx, &d.syn_G, (const float *)nullptr, (size_t)nt));
+    TRY(upload_c(ctx, &d.t_blk0, t_blk0)); TRY(upload_c(ctx, &d.bk_kind, bk_kind));
+    TRY(upload_c(ctx, &d.bk_type, bk_type)); TRY(upload_c(ctx, &d.bk_erev, bk_erev));
+    TRY(upload_c(ctx, &d.bk_c0, bk_c0)); TRY(upload_c(ctx, &d.ck_blk, ck_blk));
+    TRY(upload_c(ctx, &d.ck_i0, ck_i0)); TRY(upload_c(ctx, &d.ck_n, ck_n));
+    TRY(upload(ctx, &d.Gp, (const float *)nullptr, (size_t)32 * (size_t)std::max(n_chunk, 1)));
     TRY(upload_c(ctx, &d.c_chan0, c_chan0)); TRY(upload_c(ctx, &d.ch_type, ch_type));
     TRY(upload_c(ctx, &d.ch_gate0, ch_gate0)); TRY(upload_c(ctx, &d.ch_gbase, ch_g)); TRY(upload_c(ctx, &d.ch_erev, ch_e));
     TRY(upload(ctx, &d.gate, (const float *)nullptr, (size_t)n_gate));
     const float **izp[10] = {&d.iz_C, &d.iz_v0, &d.iz_k, &d.iz_vr, &d.iz_vt, &d.iz_vpeak, &d.iz_a, &d.iz_b, &d.iz_c, &d.iz_d};
     for (int f = 0; f < 10; f++) TRY(upload_c(ctx, izp[f], iz[f]));
     TRY(upload(ctx, &d.iz_u, (const float *)nullptr, (size_t)n_izh));
-    TRY(upload_c(ctx, &d.t_pulse0, t_pulse0)); TRY(upload_c(ctx, &d.t_pois0, t_pois0));
-    TRY(upload_c(ctx, &d.t_syn0, soff));
     TRY(upload_c(ctx, &d.pu_start, pu_s)); TRY(upload_c(ctx, &d.pu_dur, pu_d));
     TRY(upload_c(ctx, &d.pu_amp, pu_a)); TRY(upload_c(ctx, &d.pu_w, pu_w));
     TRY(upload(ctx, &d.po_ts, (const float *)nullptr, (size_t)m->n_pois));
@@ -827,9 +1113,12 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     d.n_trace = n_trace;
     TRY(upload(ctx, &d.trace_buf, (const float *)nullptr, (size_t)ctx->trace_cap * (size_t)std::max(n_trace, 1)));
     d.trace_cap = ctx->trace_cap;
-    TRY(upload_c(ctx, &d.g_t0, g_t0)); TRY(upload_c(ctx, &d.g_t1, g_t1));
-    TRY(upload_c(ctx, &d.g_f0, g_f0)); TRY(upload_c(ctx, &d.g_f1, g_f1));
-    TRY(upload_c(ctx, &d.g_i0, g_i0)); TRY(upload_c(ctx, &d.g_i1, g_i1));
+    TRY(upload_c(ctx, &d.un_t0, un_t0)); TRY(upload_c(ctx, &d.un_t1, un_t1)); TRY(upload_c(ctx, &d.un_f, un_f));
+    TRY(upload_c(ctx, &d.un_off, un_off)); TRY(upload_c(ctx, &d.un_gt0, un_gt0)); TRY(upload_c(ctx, &d.un_ngt, un_ngt));
+    TRY(upload_c(ctx, &d.un_s0, un_s0)); TRY(upload_c(ctx, &d.un_s1, un_s1));
+    TRY(upload_c(ctx, &d.un_r0, un_r0)); TRY(upload_c(ctx, &d.un_r1, un_r1)); TRY(upload_c(ctx, &d.cta_u0, cta_u0));
+    TRY(upload_c(ctx, &d.gs_t, gs_t)); TRY(upload_c(ctx, &d.gs_src, gs_src)); TRY(upload_c(ctx, &d.gs_thr, gs_thr));
+    TRY(upload_c(ctx, &d.gr_t, gr_t)); TRY(upload_c(ctx, &d.gr_col, gr_col));
     TRY(upload(ctx, &d.status, (const int32_t *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_base, (const int *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_zero, (const int *)nullptr, 1));
@@ -854,6 +1143,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         st[k].kind = s.kind; st[k].gbase = s.gbase; st[k].erev = s.erev;
         st[k].tau_decay = s.tau_decay; st[k].tau_rise = s.tau_rise;
         st[k].wf_w = s.weight_prop * s.waveform_factor;
+        st[k].r_decay = 1.0f / s.tau_decay;
+        st[k].r_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f / s.tau_rise : 1.0f;
     }
     CUDA_TRY(ctx, cudaMemcpyToSymbol(c_chan_types, ct, sizeof(ct)));
     CUDA_TRY(ctx, cudaMemcpyToSymbol(c_syn_types, st, sizeof(st)));
@@ -863,22 +1154,46 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         int64_t b = (n + kThreads - 1) / kThreads;
         return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)ctx->n_sm * 32));
     };
-    ctx->grid_inputs = blocks_for((int64_t)d.n_in * 32);
+    ctx->grid_inputs = blocks_for((int64_t)n_chunk * 32);
     ctx->grid_targets = blocks_for(nt);
-    ctx->grid_hines = blocks_for((int64_t)d.n_forest * 32);
+    ctx->grid_hines = (int)std::max<int64_t>(1, ((int64_t)d.n_forest * 32 + kHinesThreads - 1) / kHinesThreads);
     ctx->grid_deliver = ctx->n_sm * 4;
-    ctx->grid_window = d.n_group;
-    // per-step Hines: each warp stages a forest of up to forest_cap compartments (5 arrays)
-    ctx->smem_hines = (size_t)warps_per_block * 5 * ctx->forest_cap * sizeof(float);
+    ctx->grid_window = 0;
+    // per-step Hines: each warp stages a forest of up to forest_cap compartments
+    // (7 arrays plus depth boundaries); larger forests are solved in place
+    const int hines_warps = kHinesThreads / 32;
+    ctx->forest_cap = std::min(ctx->forest_cap + 1, kForestNodes + 1);
+    ctx->smem_hines = (size_t)hines_warps * 8 * ctx->forest_cap * sizeof(float);
     if (ctx->smem_hines > (size_t)ctx->smem_optin) {
-        ctx->forest_cap = (int)(ctx->smem_optin / (warps_per_block * 5 * sizeof(float)));
-        ctx->smem_hines = (size_t)warps_per_block * 5 * ctx->forest_cap * sizeof(float);
+        ctx->forest_cap = (int)(ctx->smem_optin / (hines_warps * 8 * sizeof(float)));
+        ctx->smem_hines = (size_t)hines_warps * 8 * ctx->forest_cap * sizeof(float);
     }
-    ctx->smem_win = ctx->smem_window ? (size_t)ctx->gcap * 9 * sizeof(float) : 0;
+    // windowed path: the group staging of k_cells_t; when the largest group
+    // does not fit, the batched mode runs the per-step kernels instead
+    // the windowed path needs every class to fit one CTA's shared memory; if
+    // not, the batched mode runs the per-step kernels instead
+    if (!ctx->smem_window) ctx->K = 1;
     CUDA_TRY(ctx, cudaFuncSetAttribute(k_hines_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_hines));
     if (ctx->smem_window)
-        CUDA_TRY(ctx, cudaFuncSetAttribute(k_window_t<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)ctx->smem_win));
+        CUDA_TRY(ctx, cudaFuncSetAttribute(k_cells_t, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)std::min<size_t>(max_smem_class, (size_t)ctx->smem_optin)));
+    if (getenv("EDEN_GPU_VERBOSE")) {
+        int occ_cells = 0, occ_inputs = 0;
+        if (ctx->smem_window)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cells, k_cells_t, kCellThreads, max_smem_class);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_inputs, k_inputs_t, kThreads, 0);
+        int64_t fnodes = 0, flev = 0;
+        for (size_t f = 0; f < fo_t0.size(); f++) { fnodes += fo_t1[f] - fo_t0[f]; flev += fo_nlev[f]; }
+        fprintf(stderr,
+                "libeden_gpu: %d targets, %d cells, %lld synapses, %lld poisson, %d blocks, %d input targets\n"
+                "libeden_gpu: K=%d, %d CTAs (%d thr, up to %zu B smem, %d/SM at the largest), %zu forests "
+                "(%.1f nodes, %.1f levels avg)\n"
+                "libeden_gpu: %d units, %zu size classes; inputs grid %d (%d/SM)\n",
+                nt, m->n_src, (long long)ns, (long long)m->n_pois, n_block, (int)in_tgt.size(), ctx->K,
+                (int)cta_words.size(), kCellThreads, max_smem_class, occ_cells, fo_t0.size(),
+                fo_t0.empty() ? 0.0 : (double)fnodes / fo_t0.size(), fo_t0.empty() ? 0.0 : (double)flev / fo_t0.size(),
+                n_unit, ctx->classes.size(), ctx->grid_inputs, occ_inputs);
+    }
     return 0;
 }
 
@@ -931,18 +1246,21 @@ static int ensure_wtab(EdenGpuCtx *ctx, int64_t n) {
 static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     DevModel &d = ctx->d;
     cudaStream_t s = ctx->stream;
-    if (ctx->mode == EDEN_MODE_BATCHED) {
-        if (ctx->smem_window)
-            k_window_t<true><<<ctx->grid_window, kThreads, ctx->smem_win, s>>>(d, ctx->d_wtab, base, idx, ctx->gcap);
-        else
-            k_window_t<false><<<ctx->grid_window, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx, ctx->gcap);
+    if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
+        k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+        int n = 1;
+        for (const auto &cl : ctx->classes) {
+            const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
+            k_cells_t<<<nb, kCellThreads, cl.smem, s>>>(d, ctx->d_wtab, base, idx, cl.cta_begin, cl.cta_end);
+            n++;
+        }
         k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
-        return 2;
+        return n + 1;
     }
     (void)K;
     k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
-    k_hines_t<<<ctx->grid_hines, kThreads, ctx->smem_hines, s>>>(d, ctx->d_wtab, base, idx, ctx->forest_cap);
+    k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(d, ctx->d_wtab, base, idx, ctx->forest_cap);
     k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
     return 4;
 }
@@ -1019,7 +1337,7 @@ extern "C" int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) 
                 cudaGraphDestroy(g);
             }
             CUDA_TRY(ctx, cudaGraphLaunch(ctx->graph, ctx->stream));
-            launches += kGraphWindows * 2 + 1;
+            launches += kGraphWindows * (2 + (int64_t)ctx->classes.size()) + 1;
             i += kGraphWindows;
         }
     }

@@ -38,12 +38,28 @@ struct ChanTypeDev {
 struct SynTypeDev {
     int kind;
     float gbase, erev, tau_decay, tau_rise, wf_w;  // wf_w = weight_prop * waveform_factor
+    float r_decay, r_rise;                          // correctly rounded 1 / tau
 };
+
+// x / tau, correctly rounded, from r = RN(1/tau): q = RN(x*r) is within an
+// ulp of the quotient, the residual x - tau*q is exact in one FMA, and
+// RN(q + r*residual) is the correctly rounded quotient (Markstein's
+// theorem, the basis of software division on FMA machines).  The guard sends
+// operands near the underflow range, where the residual is not exact, to
+// the hardware division.
+__device__ __forceinline__ float div_by_tau(float x, float tau, float r) {
+    if (fabsf(x) < 0x1p-100f) return x / tau;
+    const float q = x * r;
+    const float e = fmaf(-q, tau, x);
+    return fmaf(e, r, q);
+}
 
 __constant__ ChanTypeDev c_chan_types[kMaxChanTypes];
 __constant__ SynTypeDev c_syn_types[kMaxSynTypes];
 
 enum : int { ST_OK = 0, ST_LOG_OVERFLOW = 1 };
+enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2 };
+constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
 
 struct DevModel {
     int32_t n_target, n_src, n_group, n_forest, n_in;
@@ -53,8 +69,13 @@ struct DevModel {
     float *v[2];
     float *diag;
     const float *c_cm, *c_inv_rc, *c_area, *c_u, *c_l;  // U = -dt/(R C_i), L = -dt/(R C_parent)
-    const int32_t *c_nchild, *c_child0, *c_parent;   // internal target indices; parent -1 at roots
+    const int32_t *c_cend, *c_parent;  // end of each node's child range; parent (internal, -1 at roots)
     const int32_t *t_izh;                            // izhikevich index or -1
+    // flat per-target parameters of the common compartment: one channel
+    // without gates and no inputs.  flat_g < 0 marks every other target.
+    // Its diagonal flat_d0 = G/C + inv_rc and conductance flat_gc = (g*1e-5)*A
+    // are step-invariant and precomputed with the same float operations.
+    const float *flat_g, *flat_e, *flat_gc, *flat_d0;
     // forests: physical compartments [fo_t0, fo_t1), depth boundaries lvl[fo_l0 .. fo_l0 + fo_nlev]
     const int32_t *fo_t0, *fo_t1, *fo_l0, *fo_nlev, *lvl;
     // channels
@@ -64,10 +85,24 @@ struct DevModel {
     // izhikevich, structure of arrays
     const float *iz_C, *iz_v0, *iz_k, *iz_vr, *iz_vt, *iz_vpeak, *iz_a, *iz_b, *iz_c, *iz_d;
     float *iz_u;
-    // per-target input ranges and the list of targets with inputs
-    const int32_t *t_pulse0, *t_pois0;
-    const int64_t *t_syn0;
-    const int32_t *in_tgt;
+    // input blocks: each target's pulses, then Poisson inputs and connection
+    // synapses in runs of one synapse type; a block's conductance (or, for
+    // pulses, current) for step k of the window is G[k * n_block + block]
+    int32_t n_block;
+    const int32_t *t_blk0;            // [n_target + 1]
+    const int32_t *bk_kind;           // BK_PULSE, BK_POIS, BK_SYN
+    const uint8_t *bk_type;           // synapse type of a Poisson / synapse block
+    const float *bk_erev;
+    const int32_t *in_tgt;            // targets with any block
+    // blocks are cut into chunks of at most 32 items, one warp each; step k's
+    // partial sum of chunk c is Gp[k * n_chunk + c] and a block's value is the
+    // sum of its chunks' partials in chunk order
+    int32_t n_chunk;
+    const int32_t *bk_c0;             // [n_block + 1] chunk range of each block
+    const int32_t *ck_blk;            // block of each chunk
+    const int64_t *ck_i0;             // first item of each chunk
+    const int32_t *ck_n;              // items in the chunk
+    float *Gp;                        // [32 * n_chunk]
     const float *pu_start, *pu_dur, *pu_amp, *pu_w;
     // Poisson inputs
     float *po_ts, *po_isi, *po_a, *po_b;
@@ -79,8 +114,6 @@ struct DevModel {
     uint32_t *sy_mask;
     const float *sy_w, *sy_delay;
     const uint8_t *sy_type;
-    // per-target input currents of the current step (per-step path)
-    float *in_I, *in_G, *syn_I, *syn_G;
     // spike sources and fan-out (source -> synapses, connection order)
     const int32_t *t_src;
     const float *src_thr;
@@ -99,10 +132,27 @@ struct DevModel {
     int32_t n_trace;
     float *trace_buf;
     int64_t trace_cap;
-    // groups for k_window
-    const int32_t *g_t0, *g_t1, *g_f0, *g_f1, *g_i0, *g_i1;
+    // units of the windowed kernel, one warp each: targets [un_t0, un_t1),
+    // forest un_f (-1: a batch of izhikevich neurons), shared-memory slice at
+    // word un_off of its CTA, gates [un_gt0, un_gt0 + un_ngt), spike sources
+    // gs_*[un_s0 .. un_s1) and recorded targets gr_*[un_r0 .. un_r1)
+    // (target indices local to the unit); CTA c runs units [cta_u0[c], cta_u0[c+1])
+    int32_t n_unit;
+    const int32_t *un_t0, *un_t1, *un_f, *un_off, *un_gt0, *un_ngt, *un_s0, *un_s1, *un_r0, *un_r1;
+    const int32_t *cta_u0;
+    const int32_t *gs_t, *gs_src, *gr_t, *gr_col;
+    const float *gs_thr;
     int32_t *status;
 };
+
+// Shared-memory words of a unit's slice in the windowed kernel: 13 per
+// target (V twice, D, U, L, child-range end, parent and the flat
+// parameters; an izhikevich batch keeps its 10 parameters and u in the same
+// slots), 3 per gate (value and update item), the forest's depth boundaries
+// and 3 per spike source.
+__host__ __device__ inline int unit_words(int n, int ngt, int nlev, int ns) {
+    return 13 * n + 3 * ngt + (nlev + 1) + 3 * ns;
+}
 
 // Per-window arguments: the window covers steps [step0, step0 + K); steps
 // <= 0 are initialisation passes.  The previous window began at step
@@ -147,27 +197,28 @@ __device__ __forceinline__ void push_spike(const DevModel &m, bool spiked, int32
 // ---------------------------------------------------------------------------
 // State update + exposure of expOne (native, eden/Eden.cpp:3424-3466) or
 // expTwo (LEMS forward Euler; OnEvent replaces the decay on that step).
-__device__ __forceinline__ void synapse_dyn(const SynTypeDev &st, bool init, float dt, bool fire, float v,
-                                            float w, float &a, float &b, float &iw, float &gw) {
-    if (st.kind == EDEN_SYN_EXPONE) {
+// The decay keeps the reference's correctly rounded quotient -x / tau (a
+// plain product with 1 / tau differs by an ulp, enough to move a spike of a
+// recurrent network); div_by_tau computes it without a hardware division.
+template <int KIND>
+__device__ __forceinline__ float synapse_dyn_k(const SynTypeDev &st, bool init, float dt, bool fire, float w,
+                                               float &a, float &b) {
+    if (KIND == EDEN_SYN_EXPONE) {
         float g = a;
-        float i = g * (st.erev - v);
         if (!init) {
-            float an = a - dt * (a / st.tau_decay);
+            float an = a - dt * div_by_tau(a, st.tau_decay, st.r_decay);
             if (fire) an = a + st.gbase;
             a = an;
         }
-        iw = i * w;
-        gw = g * w;
+        return g * w;
     } else {
         float g = st.gbase * (b - a);
-        float i = g * (st.erev - v);
         if (init) {
             a = 0.0f;
             b = 0.0f;
         } else {
-            float an = a + dt * (-a / st.tau_rise);
-            float bn = b + dt * (-b / st.tau_decay);
+            float an = a + dt * div_by_tau(-a, st.tau_rise, st.r_rise);
+            float bn = b + dt * div_by_tau(-b, st.tau_decay, st.r_decay);
             if (fire) {
                 an = a + st.wf_w;
                 bn = b + st.wf_w;
@@ -175,8 +226,7 @@ __device__ __forceinline__ void synapse_dyn(const SynTypeDev &st, bool init, flo
             a = an;
             b = bn;
         }
-        iw = i * w;
-        gw = g * w;
+        return g * w;
     }
 }
 
@@ -203,101 +253,161 @@ __device__ __forceinline__ bool replay_mask(uint32_t mask, const WindowArgs &w, 
     return (mask >> w.Kprev) & 1u;
 }
 
-// One poissonFiringSynapse for one step (LEMS_CoreComponents.inc.xml:623-672):
-// the spiker fires its own synapse instance on the step its OnCondition holds.
-__device__ __forceinline__ void pois_step(const DevModel &m, int64_t k, bool init, int64_t step, float v,
-                                          float &iw, float &gw) {
-    float ts = m.po_ts[k], isi = m.po_isi[k], a = m.po_a[k], b = m.po_b[k];
-    float avg_isi = 1.0f / m.po_rate[k];
-    bool fired = false;
-    if (init) {
-        ts = 0.0f;
-        isi = (-avg_isi) * logf(1.0f - randof(1.0f, (int64_t)m.po_seed[k], m.po_inst[k], step, 0));
-    } else if (ts > isi) {
-        ts = 0.0f;
-        isi = (-avg_isi) * logf(1.0f - randof(1.0f, (int64_t)m.po_seed[k], m.po_inst[k], step, 1));
-        fired = true;
-    } else {
-        ts = ts + m.dt * 1.0f;
-    }
-    synapse_dyn(c_syn_types[m.po_type[k]], init, m.dt, fired, v, m.po_w[k], a, b, iw, gw);
-    m.po_ts[k] = ts;
-    m.po_isi[k] = isi;
-    m.po_a[k] = a;
-    m.po_b[k] = b;
-}
+// Per-warp accumulation tile: row `lane` (stride kAccStride, padded so that
+// both a row write and a column read are free of bank conflicts) holds the
+// lane's partial sum for each step of the window.
+constexpr int kAccStride = 33;
 
-// One connection synapse for one step; `first` = first step of a window,
-// where the previous window's triggers are read (and the mask cleared).
-__device__ __forceinline__ void syn_step(const DevModel &m, int64_t s, const WindowArgs &w, bool init, bool first,
-                                         float t, float v, float &iw, float &gw) {
-    float pend = m.sy_pend[s], a = m.sy_a[s], b = m.sy_b[s];
-    bool fire = false;
-    if (!init) {
-        if (first) {
-            uint32_t mask = m.sy_mask[s];
-            if (mask) {
-                m.sy_mask[s] = 0;
-                float delay = m.sy_delay[s];
-                bool trig = replay_mask(mask, w, m.dt, delay, pend);
-                if (t <= pend && pend < t + m.dt) fire = true;
-                if (trig && trigger_arrival(t, m.dt, delay, pend)) fire = true;
-            } else if (t <= pend && pend < t + m.dt) {
-                fire = true;
+// Poisson input `it` over the K steps of a window; row[j] = its step-j term.
+template <int KIND>
+__device__ __forceinline__ void pois_steps(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
+                                           float *row) {
+    const float dt = m.dt;
+    float ts = m.po_ts[it], isi = m.po_isi[it], a = m.po_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.po_b[it] : 0.0f;
+    const float wt = m.po_w[it];
+    if (w.step0 <= 0) {
+        for (int j = 0; j < w.K; j++) {
+            ts = 0.0f;
+            isi = (-(1.0f / m.po_rate[it])) *
+                  logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], w.step0 + j, 0));
+            row[j] = synapse_dyn_k<KIND>(st, true, dt, false, wt, a, b);
+        }
+    } else {
+        for (int j = 0; j < w.K; j++) {
+            const bool fired = ts > isi;
+            if (fired) {
+                ts = 0.0f;
+                isi = (-(1.0f / m.po_rate[it])) *
+                      logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], w.step0 + j, 1));
+            } else {
+                ts = ts + dt * 1.0f;
             }
-        } else if (t <= pend && pend < t + m.dt) {
-            fire = true;
+            row[j] = synapse_dyn_k<KIND>(st, false, dt, fired, wt, a, b);
         }
     }
-    synapse_dyn(c_syn_types[m.sy_type[s]], init, m.dt, fire, v, m.sy_w[s], a, b, iw, gw);
-    m.sy_pend[s] = pend;
-    m.sy_a[s] = a;
-    m.sy_b[s] = b;
+    m.po_ts[it] = ts; m.po_isi[it] = isi; m.po_a[it] = a;
+    if (KIND == EDEN_SYN_EXPTWO) m.po_b[it] = b;
 }
 
-// Input and synapse currents into target t, computed by a whole warp: each
-// lane updates every 32nd item and the partial sums are combined by a
-// butterfly reduction, so every lane returns the same totals.
-// (The reference sums the same terms sequentially, eden/Eden.cpp:5927-5945.)
-__device__ __forceinline__ void inputs_warp(const DevModel &m, int t, const WindowArgs &w, int64_t step, float time,
-                                            bool first, float v, float &Iin, float &Gin, float &Isyn, float &Gsyn) {
+// One chunk (at most 32 items of one input block) over the K steps of a
+// window, one item per lane with its state in registers.  Lane l writes its
+// item's step-j term to row l of the warp's tile; lane j then sums column j
+// over the chunk's rows in a fixed order into Gp[j][chunk].  Terms are g*w
+// (the conductance before the step's update, as the reference exposes it)
+// for Poisson inputs and synapses, and the current for pulses.
+__device__ __forceinline__ void chunk_window(const DevModel &m, int c, const WindowArgs &w, float *tile,
+                                             const float *tk) {
     const int lane = threadIdx.x & 31;
-    const bool init = step <= 0;
-    float ip = 0.0f;
-    const int q0 = m.t_pulse0[t], q1 = m.t_pulse0[t + 1];
-    for (int q = q0 + lane; q < q1; q += 32) {
-        float s = m.pu_start[q];
-        if (s <= time && time <= s + m.pu_dur[q]) ip += m.pu_amp[q] * m.pu_w[q];
+    const int bk = m.ck_blk[c];
+    const int kind = m.bk_kind[bk];
+    const int n = m.ck_n[c];
+    const int64_t it = m.ck_i0[c] + lane;
+    float *row = tile + lane * kAccStride;
+    const float dt = m.dt;
+    const bool init = w.step0 <= 0;
+    if (lane < n) {
+        if (kind == BK_PULSE) {
+            const float st = m.pu_start[it], du = m.pu_dur[it], aw = m.pu_amp[it] * m.pu_w[it];
+            for (int j = 0; j < w.K; j++) {
+                const float tf = tk[j];
+                row[j] = (st <= tf && tf <= st + du) ? aw : 0.0f;
+            }
+        } else if (kind == BK_POIS) {
+            // poissonFiringSynapse (LEMS_CoreComponents.inc.xml:623-672): the
+            // spiker fires its own synapse instance on the step its OnCondition holds
+            const SynTypeDev st = c_syn_types[m.bk_type[bk]];
+            if (st.kind == EDEN_SYN_EXPTWO) pois_steps<EDEN_SYN_EXPTWO>(m, it, w, st, row);
+            else pois_steps<EDEN_SYN_EXPONE>(m, it, w, st, row);
+        } else {
+            // connection synapse: replay the previous window's triggers, then each
+            // step fires the pending spike when it falls due (eden/Eden.cpp:3646-3686)
+            const SynTypeDev st = c_syn_types[m.bk_type[bk]];
+            float pend = m.sy_pend[it], a = m.sy_a[it], b = st.kind == EDEN_SYN_EXPTWO ? m.sy_b[it] : 0.0f;
+            const float wt = m.sy_w[it];
+            const float pend0 = pend;
+            bool trig = false;
+            if (!init) {
+                const uint32_t mask = m.sy_mask[it];
+                if (mask) {
+                    m.sy_mask[it] = 0;
+                    trig = replay_mask(mask, w, dt, m.sy_delay[it], pend);
+                }
+            }
+            if (st.kind == EDEN_SYN_EXPTWO) {
+                for (int j = 0; j < w.K; j++) {
+                    const float t = tk[j];
+                    bool fire = false;
+                    if (!init) {
+                        // the pending spike falls due before a trigger of this step may replace it
+                        fire = (t <= pend && pend < t + dt);
+                        if (j == 0 && trig && trigger_arrival(t, dt, m.sy_delay[it], pend)) fire = true;
+                    }
+                    row[j] = synapse_dyn_k<EDEN_SYN_EXPTWO>(st, init, dt, fire, wt, a, b);
+                }
+                m.sy_b[it] = b;
+            } else {
+                for (int j = 0; j < w.K; j++) {
+                    const float t = tk[j];
+                    bool fire = false;
+                    if (!init) {
+                        fire = (t <= pend && pend < t + dt);
+                        if (j == 0 && trig && trigger_arrival(t, dt, m.sy_delay[it], pend)) fire = true;
+                    }
+                    row[j] = synapse_dyn_k<EDEN_SYN_EXPONE>(st, init, dt, fire, wt, a, b);
+                }
+            }
+            if (pend != pend0) m.sy_pend[it] = pend;
+            m.sy_a[it] = a;
+        }
     }
-    float pi = 0.0f, pg = 0.0f;
-    const int p0 = m.t_pois0[t], p1 = m.t_pois0[t + 1];
-    for (int p = p0 + lane; p < p1; p += 32) {
-        float iw, gw;
-        pois_step(m, p, init, step, v, iw, gw);
-        pi += iw;
-        pg += gw;
+    __syncwarp();
+    if (lane < w.K) {
+        float tot = 0.0f;
+        for (int r = 0; r < n; r++) tot += tile[r * kAccStride + lane];
+        m.Gp[(size_t)lane * m.n_chunk + c] = tot;
     }
-    float si = 0.0f, sg = 0.0f;
-    const int64_t s0 = m.t_syn0[t], s1 = m.t_syn0[t + 1];
-    for (int64_t s = s0 + lane; s < s1; s += 32) {
-        float iw, gw;
-        syn_step(m, s, w, init, first, time, v, iw, gw);
-        si += iw;
-        sg += gw;
+    __syncwarp();
+}
+
+// Currents into target t at step j of the window from its input blocks:
+// pulses add current; conductance blocks add g*(erev - v) and g, inputs
+// first, then synapses, as eden/Eden.cpp:6057-6060 orders them.  BK_K and
+// BK_E are the blocks' kinds and reversal potentials, BC0 their chunk ranges
+// (indexed from blk0 and chk0, which may point into shared memory).
+__device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1, const int32_t *BK_K,
+                                               const float *BK_E, const int32_t *BC0, int chk0, float v, float &Iin,
+                                               float &Gin, float &Isyn, float &Gsyn) {
+    Iin = 0.0f; Gin = 0.0f; Isyn = 0.0f; Gsyn = 0.0f;
+    for (int bk = b0; bk < b1; bk++) {
+        float g = 0.0f;
+        for (int c = BC0[bk]; c < BC0[bk + 1]; c++) g += Gpk[c + chk0];
+        const int kind = BK_K[bk];
+        if (kind == BK_PULSE) {
+            Iin += g;
+        } else if (kind == BK_POIS) {
+            Iin += g * (BK_E[bk] - v);
+            Gin += g;
+        } else {
+            Isyn += g * (BK_E[bk] - v);
+            Gsyn += g;
+        }
     }
-    if (q1 > q0) ip = warp_sum(ip);
-    if (p1 > p0) {
-        pi = warp_sum(pi);
-        pg = warp_sum(pg);
-    }
-    if (s1 > s0) {
-        si = warp_sum(si);
-        sg = warp_sum(sg);
-    }
-    Iin = ip + pi;
-    Gin = pg;
-    Isyn = si;
-    Gsyn = sg;
+}
+
+// One HH gate for one step (eden/Eden.cpp:5126-5259): exponential-Euler
+// relaxation towards inf(V) with time constant tau(V), clamped to
+// [1e-6, 1 - 1e-6]; initialisation sets it to inf(V).
+__device__ __forceinline__ float gate_next(const ChanTypeDev &ct, int gi, bool init, float dt, float v, float qo) {
+    const float alpha = rate_value(ct.fk[gi], ct.fr[gi], ct.fm[gi], ct.fs[gi], v);
+    const float beta = rate_value(ct.rk[gi], ct.rr[gi], ct.rm[gi], ct.rs[gi], v);
+    const float tau = 1.0f / (alpha + beta);
+    const float inf = alpha / (alpha + beta);
+    if (init) return inf;
+    const float blend = expf(-((dt * ct.q10[gi]) / tau));
+    float qn = blend * qo + (1.0f - blend) * inf;
+    if (!(qn > 1e-6f)) qn = 1e-6f;
+    if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
+    return qn;
 }
 
 // ---------------------------------------------------------------------------
@@ -324,21 +434,8 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
             float fopen = 1.0f;
             float *q = m.gate + m.ch_gate0[ch];
             for (int g = 0; g < ct.n_gates; g++) {
-                float qo = q[g];
-                float alpha = rate_value(ct.fk[g], ct.fr[g], ct.fm[g], ct.fs[g], v);
-                float beta = rate_value(ct.rk[g], ct.rr[g], ct.rm[g], ct.rs[g], v);
-                float tau = 1.0f / (alpha + beta);
-                float inf = alpha / (alpha + beta);
-                float qn;
-                if (init) {
-                    qn = inf;
-                } else {
-                    float blend = expf(-((m.dt * ct.q10[g]) / tau));
-                    qn = blend * qo + (1.0f - blend) * inf;
-                    if (!(qn > 1e-6f)) qn = 1e-6f;
-                    if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
-                }
-                q[g] = qn;
+                const float qo = q[g];
+                q[g] = gate_next(ct, g, init, m.dt, v, qo);
                 for (int r = 0; r < ct.inst[g]; r++) fopen = fopen * qo;
             }
             float gs = m.ch_gbase[ch] * fopen;
@@ -380,58 +477,64 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
 // ---------------------------------------------------------------------------
 // cable solve
 // ---------------------------------------------------------------------------
-// Backward-Euler Hines solve of one forest by one warp (eden/Eden.cpp:6114-6225),
-// on arrays indexed by (internal target - base): D (diagonal, in), X (the
-// pre-updated V, solved in place), U, L (off-diagonals).  Depths are processed
-// deepest first; each node pulls its children's elimination terms in
-// increasing child order, the same sequence of operations as the reference's
-// depth-first post-order.  Back-substitution then runs root-first.  Ends with
-// the threshold test V < thr < V_next of the forest's spike sources
-// (eden/Eden.cpp:6247-6252).
-__device__ __forceinline__ void hines_forest(const DevModel &m, int f, bool init, int64_t step, float *D, float *X,
-                                             const float *U, const float *L, const float *Vin, int base,
-                                             int wpar) {
+// Backward-Euler Hines solve of one forest by one warp (eden/Eden.cpp:6114-6225).
+// Arrays may live in shared or global memory and share one index space:
+// D (diagonal, in), X (the pre-updated V, solved in place), U, L
+// (off-diagonals), CE (end of each node's child range), P (parent), and LV
+// (the forest's depth boundaries, nlev + 1 entries); `base` maps that index
+// space back to internal target ids for the spike check.  Depths are
+// processed deepest first; each node pulls its children's elimination terms
+// in increasing child order, the same sequence of operations as the
+// reference's depth-first post-order, and keeps the reciprocal of its final
+// pivot.  Back-substitution then runs root-first.  When check_spikes is set
+// it ends with the threshold test V < thr < V_next of the forest's spike
+// sources (eden/Eden.cpp:6247-6252).
+__device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64_t step, float *D, float *X,
+                                             const float *U, const float *L, const int32_t *CE, const int32_t *P,
+                                             const int32_t *LV, int nlev, const float *Vin, int base, int wpar,
+                                             bool check_spikes) {
     const int lane = threadIdx.x & 31;
-    const int c0 = m.fo_t0[f], c1 = m.fo_t1[f];
+    const int c0 = LV[0], c1 = LV[nlev];
     if (!init && c1 > c0) {
         const float dt = m.dt;
-        for (int c = c0 + lane; c < c1; c += 32) D[c - base] = 1.0f + D[c - base] * dt;
+        for (int c = c0 + lane; c < c1; c += 32) D[c] = 1.0f + D[c] * dt;
         __syncwarp();
-        const int32_t *lv = m.lvl + m.fo_l0[f];
-        const int nlev = m.fo_nlev[f];
-        for (int lev = nlev - 2; lev >= 0; lev--) {
-            for (int j = lv[lev] + lane; j < lv[lev + 1]; j += 32) {
-                int n = m.c_nchild[j];
-                if (n == 0) continue;
-                int ch = m.c_child0[j] - base;
-                float dj = D[j - base], xj = X[j - base];
-                for (int k = 0; k < n; k++) {
-                    float ratio = L[ch + k] / D[ch + k];
-                    dj -= ratio * U[ch + k];
-                    xj -= ratio * X[ch + k];
+        for (int lev = nlev - 1; lev >= 0; lev--) {
+            const int j0 = LV[lev], j1 = LV[lev + 1];
+            for (int j = j0 + lane; j < j1; j += 32) {
+                const int kb = (j == j0) ? j1 : CE[j - 1];
+                const int ke = CE[j];
+                float dj = D[j];
+                if (ke > kb) {
+                    float xj = X[j];
+                    for (int i = kb; i < ke; i++) {
+                        const float ratio = L[i] * D[i];  // D[i] holds the child's reciprocal pivot
+                        dj -= ratio * U[i];
+                        xj -= ratio * X[i];
+                    }
+                    X[j] = xj;
                 }
-                D[j - base] = dj;
-                X[j - base] = xj;
+                D[j] = __fdividef(1.0f, dj);
             }
             __syncwarp();
         }
-        for (int r = lv[0] + lane; r < lv[1]; r += 32) X[r - base] = X[r - base] / D[r - base];
+        for (int r = LV[0] + lane; r < LV[1]; r += 32) X[r] = X[r] * D[r];
         __syncwarp();
         for (int lev = 1; lev < nlev; lev++) {
-            for (int i = lv[lev] + lane; i < lv[lev + 1]; i += 32)
-                X[i - base] = (X[i - base] - U[i - base] * X[m.c_parent[i] - base]) / D[i - base];
+            for (int i = LV[lev] + lane; i < LV[lev + 1]; i += 32) X[i] = (X[i] - U[i] * X[P[i]]) * D[i];
             __syncwarp();
         }
     }
+    if (!check_spikes) return;
     for (int c0w = c0; c0w < c1; c0w += 32) {
-        int c = c0w + lane;
+        const int c = c0w + lane;
         bool spk = false;
         int src = -1;
         if (c < c1) {
-            src = m.t_src[c];
+            src = m.t_src[c + base];
             if (src >= 0) {
-                float thr = m.src_thr[src];
-                spk = (Vin[c - base] < thr && thr < X[c - base]);
+                const float thr = m.src_thr[src];
+                spk = (Vin[c] < thr && thr < X[c]);
             }
         }
         push_spike(m, spk, src, (int32_t)(step + 1), wpar);
