@@ -1,0 +1,321 @@
+"""Benchmark of the GB300 simulation step on the batched multicompartment network.
+
+Workload (one GPU): 10,000 cells with seeded random branching trees (segment
+count log-uniform in [1, 500], 0.80 M compartments), HH soma + passive
+dendrites, 1 M expTwoSynapse connections at fixed in-degree 100 with
+0.5-5 ms delays, 1 M 5 Hz poissonFiringSynapse inputs; dt 0.025 ms.  A bench
+"step" is one pass of the simulation loop over STEPS_PER_ITER simulation
+steps; `value` is compartment-steps/s (compartments x simulation steps /
+device time) with the network resident in HBM; `e2e` runs the whole thing
+through the C ABI from host buffers (model upload, stepping, record fetch).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun each rank advances an independent replica (its own seed):
+the path does not shard, so `scaling` is weak and no collective is used.
+`--impl reference` times the CPU restatement of the reference loop (the
+reference's own build needs its source tree, absent where this runs) with
+all host threads on the same workload and prints the same line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "compartment-steps/s, batched vs plain GPU, at ≤0.1 ms spike-time error"
+UNIT = "compartment-steps/s"
+STEPS_PER_ITER = 320          # simulation steps per bench step (16 windows of 20)
+L2_FLUSH_BYTES = 256 << 20    # written between timed iterations (> 129 MB L2)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cells", type=int, default=10000)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--profile", action="store_true",
+                    help="only advance the batched path (init + warmup + steps bench steps) for ncu")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per simulation step (each SoA array streamed once, FP32):
+# passive compartment 24 B, HH compartment 48 B, izhikevich 16 B, expTwo
+# synapse 33 B, expOne 25 B, Poisson source 16 B + its synapse, pulse 12 B,
+# delivered event 5 B
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(low, events_per_step: float) -> dict:
+    n_comp = low.n_comp
+    chan_gated = (low.chan_types["n_gates"][low.chan_type] > 0).astype(np.int64)
+    per_comp = np.add.reduceat(np.concatenate([chan_gated, [0]]), low.comp_chan_off[:-1]) if n_comp else np.zeros(0)
+    per_comp[low.comp_chan_off[:-1] == low.comp_chan_off[1:]] = 0
+    n_hh = int((per_comp > 0).sum())
+    kinds = low.syn_types["kind"]
+    syn_b = float(np.where(kinds[low.syn_type] == 1, 33, 25).sum()) if len(low.syn_type) else 0.0
+    pois_b = float(np.where(kinds[low.pois_type] == 1, 33 + 16, 25 + 16).sum()) if len(low.pois_type) else 0.0
+    cells_b = 48.0 * n_hh + 24.0 * (n_comp - n_hh) + 16.0 * low.n_izh
+    inputs_b = syn_b + pois_b + 12.0 * len(low.pulse_target)
+    return {"cells": cells_b, "inputs": inputs_b, "deliver": 5.0 * events_per_step,
+            "total": cells_b + inputs_b + 5.0 * events_per_step}
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() in ("active", "0x1") or flag == "1":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def flush_l2(buf):
+    import torch
+    buf.fill_(1.0)
+    torch.cuda.synchronize()
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(low, threads: int, budget_s: float = 15.0):
+    """Time the CPU restatement on a bounded number of simulation steps of the
+    same workload; returns (compartment-steps/s, steps timed)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
+    import eden_port
+    t0 = time.perf_counter()
+    eden_port.run(low, n_steps=4, trace_target=np.zeros(0, np.int32), threads=threads, spike_cap=1 << 20)
+    per = (time.perf_counter() - t0) / 8.0  # 4 init + 4 steps
+    n = int(max(8, min(2000, budget_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    eden_port.run(low, n_steps=n, trace_target=np.zeros(0, np.int32), threads=threads, spike_cap=1 << 22)
+    dt = time.perf_counter() - t0
+    # the timed call also runs the 4 initialisation passes
+    return low.n_target * n / (dt * n / (n + 4)), n
+
+
+def load_profile_traffic():
+    """DRAM bytes per k_cells_t launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "k_cells_t_multicomp_net.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch_scaled")
+    return None
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from eden_gb300 import lowering, workloads
+
+    spec = workloads.multicomp_net(n_cells=args.cells, seed=args.seed + rank)
+    low = lowering.lower(spec)
+    config = {"workload": f"multicomp_net: {args.cells} cells, {low.n_comp} compartments, "
+                          f"{len(low.syn_target)} expTwo synapses (in-degree 100, delay 0.5-5 ms), "
+                          f"{len(low.pois_target)} Poisson inputs at 5 Hz, dt 0.025 ms",
+              "cells": args.cells, "compartments": low.n_comp, "synapses": int(len(low.syn_target)),
+              "poisson_inputs": int(len(low.pois_target)), "sim_steps_per_bench_step": STEPS_PER_ITER,
+              "l2": "flushed (256 MB write) between timed bench steps", "replicas": world, "seed": args.seed}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        val, n = cpu_sample(low, threads, budget_s=20.0)
+        ms = low.n_target * STEPS_PER_ITER / val * 1e3
+        line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+                "config": config,
+                "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"{n} simulation steps of the full workload (after 4 init passes), "
+                                           f"C restatement of the reference loop, OpenMP {threads} threads"},
+                "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
+    torch.cuda.set_device(0)
+    if args.profile:
+        sim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=STEPS_PER_ITER * 2)
+        sim.initialize()
+        for _ in range(args.warmup + args.steps):
+            sim.run_steps(STEPS_PER_ITER)
+            sim.fetch()
+        sim.close()
+        print("profile run done")
+        return
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # ---- device-timed batched run (kernel timing on: CUDA events around each launch)
+    sim = Simulation(low, mode=MODE_BATCHED, kernel_timing=True, record_capacity_steps=STEPS_PER_ITER * 2)
+    sim.initialize()
+    for _ in range(max(3, args.warmup)):
+        sim.run_steps(STEPS_PER_ITER)
+        sim.fetch()
+    base_stats = sim.kernel_stats()
+    launches0 = sum(n for _, n in base_stats.values())
+    clocks = ClockSampler()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    total_ms, spikes = 0.0, 0
+    for _ in range(args.steps):
+        flush_l2(flush)
+        total_ms += sim.run_steps(STEPS_PER_ITER)
+        rec = sim.fetch()
+        spikes += len(rec.spike_src)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    stats = sim.kernel_stats()
+    sim.close()
+    gpu_launches = sum(n for _, n in stats.values()) - launches0
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    sim_steps = STEPS_PER_ITER * args.steps
+    value = world * low.n_target * sim_steps / (total_ms * 1e-3)
+
+    # ---- roofline of the dominant kernel (k_cells_t), bytes per launch
+    events_per_step = spikes * (len(low.syn_target) / max(1, len(low.src_target))) / sim_steps
+    ab = algorithmic_bytes(low, events_per_step)
+    k_ms = {k: (stats[k][0] - base_stats[k][0], stats[k][1] - base_stats[k][1]) for k in stats}
+    dom = max(k_ms, key=lambda k: k_ms[k][0])
+    steps_per_launch = sim_steps / max(1, k_ms[dom][1])
+    bytes_per_launch = {"k_cells_t": ab["cells"], "k_inputs_t": ab["inputs"],
+                        "k_deliver_t": ab["deliver"]}.get(dom, ab["total"]) * steps_per_launch
+    avg_ms = k_ms[dom][0] / max(1, k_ms[dom][1])
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    # ---- plain (per-step) GPU path on the same network, for the batched/plain ratio
+    psim = Simulation(low, mode=MODE_PLAIN, record_capacity_steps=STEPS_PER_ITER * 2)
+    psim.initialize()
+    psim.run_steps(STEPS_PER_ITER)
+    psim.fetch()
+    plain_ms = 0.0
+    for _ in range(2):
+        flush_l2(flush)
+        plain_ms += psim.run_steps(STEPS_PER_ITER)
+        psim.fetch()
+    psim.close()
+    plain_value = low.n_target * 2 * STEPS_PER_ITER / (plain_ms * 1e-3)
+
+    # ---- end to end through the C ABI: model upload, stepping, record fetch
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    esim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=STEPS_PER_ITER * 2)
+    rec_bytes = 0
+    esim.initialize()
+    for _ in range(args.steps):
+        esim.run_steps(STEPS_PER_ITER)
+        r = esim.fetch()
+        rec_bytes += r.trace.nbytes + r.trace_step.nbytes + r.spike_src.nbytes + r.spike_step.nbytes
+    esim.close()
+    e2e_s = time.perf_counter() - t0
+    model_bytes = sum(a.nbytes for a in esim._keep)
+    e2e_value = world * low.n_target * sim_steps / e2e_s
+
+    # ---- CPU baseline (rank 0 only)
+    cpu = None
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        cval, n = cpu_sample(low, threads, budget_s=15.0)
+        cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} simulation steps of the same network (after 4 init passes), C restatement of "
+                         f"the reference loop, OpenMP {threads} threads"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+                "config": config,
+                "plain_gpu": {"value": plain_value, "unit": UNIT, "ratio_batched_over_plain": value / world / plain_value},
+                "e2e": {"value": e2e_value, "unit": UNIT,
+                        "h2d_bytes_per_step": model_bytes / (sim_steps + 4) / 1.0,
+                        "d2h_bytes_per_step": rec_bytes / sim_steps},
+                "gpu_launches": int(gpu_launches),
+                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                             "traffic": load_profile_traffic(), "bytes_per_launch": bytes_per_launch,
+                             "avg_launch_ms": avg_ms, "step_bytes": ab["total"],
+                             "step_achieved_gbs": ab["total"] * sim_steps / (total_ms * 1e-3) / 1e9 / world * world},
+                "kernels_ms": {k: round(v[0], 3) for k, v in k_ms.items()},
+                "clocks": clk,
+                "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

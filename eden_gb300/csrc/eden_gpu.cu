@@ -79,6 +79,13 @@ struct EdenGpuCtx {
     std::vector<CellClass> classes;        // k_cells_t launches of one window
     double last_ms = 0.0;
     int64_t last_launches = 0;
+    // kernel timing: an event pair per launch of the current run
+    bool kernel_timing = false;
+    std::vector<cudaEvent_t> tev;
+    std::vector<int> tev_kind;
+    size_t tev_used = 0;
+    double k_ms[EDEN_KERNEL_KINDS] = {0};
+    int64_t k_n[EDEN_KERNEL_KINDS] = {0};
     int sticky_status = 0;
 
     int fail(int code, const char *fmt, ...) {
@@ -534,6 +541,7 @@ extern "C" void edenGpuDestroy(EdenGpuCtx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     for (void *p : ctx->allocs) cudaFree(p);
+    for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);
     if (ctx->h_wtab) cudaFreeHost(ctx->h_wtab);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -948,6 +956,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         kmax = (int)std::max(1.0, std::min((double)kMaxWindow, dsteps));
     }
     ctx->mode = opt ? opt->mode : EDEN_MODE_PLAIN;
+    ctx->kernel_timing = opt && opt->kernel_timing;
     int kreq = (opt && opt->steps_per_launch > 0) ? opt->steps_per_launch : kmax;
     ctx->K = ctx->mode == EDEN_MODE_BATCHED ? std::max(1, std::min(kreq, kmax)) : 1;
 
@@ -1242,26 +1251,60 @@ static int ensure_wtab(EdenGpuCtx *ctx, int64_t n) {
     return 0;
 }
 
+// Event pair around a launch when kernel timing is on.
+static void tmark(EdenGpuCtx *ctx, int kind, bool before) {
+    if (!ctx->kernel_timing) return;
+    if (before) {
+        if (ctx->tev_used + 2 > ctx->tev.size()) {
+            for (int k = 0; k < 64; k++) {
+                cudaEvent_t e;
+                cudaEventCreate(&e);
+                ctx->tev.push_back(e);
+                ctx->tev_kind.push_back(0);
+            }
+        }
+        ctx->tev_kind[ctx->tev_used] = kind;
+        cudaEventRecord(ctx->tev[ctx->tev_used], ctx->stream);
+    } else {
+        cudaEventRecord(ctx->tev[ctx->tev_used + 1], ctx->stream);
+        ctx->tev_used += 2;
+    }
+}
+
 // Launch the kernels of window `idx` of the current table; returns launches.
 static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     DevModel &d = ctx->d;
     cudaStream_t s = ctx->stream;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
+        tmark(ctx, EDEN_KERNEL_INPUTS, true);
         k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+        tmark(ctx, EDEN_KERNEL_INPUTS, false);
         int n = 1;
+        tmark(ctx, EDEN_KERNEL_CELLS, true);
         for (const auto &cl : ctx->classes) {
             const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
             k_cells_t<<<nb, kCellThreads, cl.smem, s>>>(d, ctx->d_wtab, base, idx, cl.cta_begin, cl.cta_end);
             n++;
         }
+        tmark(ctx, EDEN_KERNEL_CELLS, false);
+        tmark(ctx, EDEN_KERNEL_DELIVER, true);
         k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+        tmark(ctx, EDEN_KERNEL_DELIVER, false);
         return n + 1;
     }
     (void)K;
+    tmark(ctx, EDEN_KERNEL_INPUTS, true);
     k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+    tmark(ctx, EDEN_KERNEL_INPUTS, false);
+    tmark(ctx, EDEN_KERNEL_TARGETS, true);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+    tmark(ctx, EDEN_KERNEL_TARGETS, false);
+    tmark(ctx, EDEN_KERNEL_HINES, true);
     k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(d, ctx->d_wtab, base, idx, ctx->forest_cap);
+    tmark(ctx, EDEN_KERNEL_HINES, false);
+    tmark(ctx, EDEN_KERNEL_DELIVER, true);
     k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+    tmark(ctx, EDEN_KERNEL_DELIVER, false);
     return 4;
 }
 
@@ -1312,8 +1355,9 @@ extern "C" int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) 
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     int64_t launches = 0;
     size_t i = 0;
+    ctx->tev_used = 0;
     // graph replay for full chunks of regular windows (batched mode)
-    if (ctx->mode == EDEN_MODE_BATCHED) {
+    if (ctx->mode == EDEN_MODE_BATCHED && !ctx->kernel_timing) {
         while (i < wins.size() && wins[i].step0 <= 0) {
             launches += launch_window(ctx, ctx->d_zero, (int)i, wins[i].K);
             i++;
@@ -1349,11 +1393,25 @@ extern "C" int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) 
     CUDA_TRY(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     ctx->last_ms = ms;
     ctx->last_launches = launches;
+    for (size_t e = 0; e < ctx->tev_used; e += 2) {
+        float kms = 0;
+        CUDA_TRY(ctx, cudaEventElapsedTime(&kms, ctx->tev[e], ctx->tev[e + 1]));
+        ctx->k_ms[ctx->tev_kind[e]] += kms;
+        ctx->k_n[ctx->tev_kind[e]]++;
+    }
     ctx->next_step = last + 1;
     int status = 0;
     CUDA_TRY(ctx, cudaMemcpy(&status, ctx->d.status, sizeof(int), cudaMemcpyDeviceToHost));
     ctx->sticky_status |= status;
     if (status & ST_LOG_OVERFLOW) return ctx->fail(EDEN_GPU_E_RANGE, "spike log overflow; fetch records more often");
+    return 0;
+}
+
+extern "C" int edenGpuKernelStats(EdenGpuCtx *ctx, int32_t kind, double *total_ms, int64_t *launches) {
+    if (!ctx) return EDEN_GPU_E_INVALID;
+    if (kind < 0 || kind >= EDEN_KERNEL_KINDS) return ctx->fail(EDEN_GPU_E_RANGE, "kernel kind %d", kind);
+    if (total_ms) *total_ms = ctx->k_ms[kind];
+    if (launches) *launches = ctx->k_n[kind];
     return 0;
 }
 

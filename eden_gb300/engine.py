@@ -35,7 +35,7 @@ class COptions(ctypes.Structure):
                 ("steps_per_launch", ctypes.c_int32), ("cells_per_block", ctypes.c_int32),
                 ("record_capacity_steps", ctypes.c_int32), ("spike_capacity", ctypes.c_int32),
                 ("n_trace", ctypes.c_int32), ("trace_target", ctypes.POINTER(ctypes.c_int32)),
-                ("reserved", ctypes.c_int32 * 8)]
+                ("kernel_timing", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
 
 
 class CRecords(ctypes.Structure):
@@ -46,8 +46,9 @@ class CRecords(ctypes.Structure):
 
 
 EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuFetchRecords", "edenGpuReadV", "edenGpuWriteV",
-            "edenGpuReadSynapses", "edenGpuLastRunStats", "edenGpuLastError", "edenGpuDestroy",
-            "edenGpuAbiVersion"]
+            "edenGpuReadSynapses", "edenGpuLastRunStats", "edenGpuKernelStats", "edenGpuLastError",
+            "edenGpuDestroy", "edenGpuAbiVersion"]
+KERNEL_NAMES = ["k_inputs_t", "k_cells_t", "k_targets_t", "k_hines_t", "k_deliver_t"]
 
 
 def load_library(path: str | None = None, build_if_missing: bool = True):
@@ -76,6 +77,9 @@ def load_library(path: str | None = None, build_if_missing: bool = True):
     lib.edenGpuReadSynapses.restype = ctypes.c_int
     lib.edenGpuLastRunStats.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
     lib.edenGpuLastRunStats.restype = ctypes.c_int
+    lib.edenGpuKernelStats.argtypes = [P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_int64)]
+    lib.edenGpuKernelStats.restype = ctypes.c_int
     lib.edenGpuLastError.argtypes = [P]
     lib.edenGpuLastError.restype = ctypes.c_char_p
     lib.edenGpuDestroy.argtypes = [P]
@@ -108,7 +112,8 @@ class Simulation:
 
     def __init__(self, lowered: LoweredModel, mode: int = MODE_BATCHED, device: int = 0,
                  steps_per_launch: int = 0, cells_per_block: int = 0, trace_target=None,
-                 record_capacity_steps: int = 4096, spike_capacity: int = 1 << 22):
+                 record_capacity_steps: int = 4096, spike_capacity: int = 1 << 22,
+                 kernel_timing: bool = False):
         self.lib = load_library()
         self.lowered = lowered
         self._cm, self._keep = to_cmodel(lowered)
@@ -121,6 +126,7 @@ class Simulation:
         opt.cells_per_block = cells_per_block
         opt.record_capacity_steps = record_capacity_steps
         opt.spike_capacity = spike_capacity
+        opt.kernel_timing = 1 if kernel_timing else 0
         opt.n_trace = len(self.trace_target)
         opt.trace_target = self.trace_target.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if len(self.trace_target) else None
         self._opt = opt
@@ -219,6 +225,16 @@ class Simulation:
         keep = rec.spike_step <= self.next_step - 1
         rec.spike_src, rec.spike_step = rec.spike_src[keep], rec.spike_step[keep]
         return rec
+
+    def kernel_stats(self) -> dict:
+        """{kernel name: (total device ms, launches)} accumulated with kernel_timing."""
+        out = {}
+        for k, name in enumerate(KERNEL_NAMES):
+            ms = ctypes.c_double()
+            n = ctypes.c_int64()
+            self._check(self.lib.edenGpuKernelStats(self.ctx, k, ctypes.byref(ms), ctypes.byref(n)))
+            out[name] = (float(ms.value), int(n.value))
+        return out
 
     # -- state access ----------------------------------------------------------
     def read_v(self) -> np.ndarray:

@@ -156,8 +156,20 @@ typedef struct EdenGpuOptions {
     int32_t spike_capacity;   /* spike events buffered on the device between fetches */
     int32_t n_trace;          /* recorded targets (membrane potential) */
     const int32_t *trace_target;
-    int32_t reserved[8];
+    int32_t kernel_timing;    /* 1: bracket every kernel launch with CUDA events (no graph
+                                 replay) and accumulate per-kernel device time */
+    int32_t reserved[7];
 } EdenGpuOptions;
+
+/* Kernels whose device time kernel_timing accumulates. */
+enum {
+    EDEN_KERNEL_INPUTS = 0,   /* synapse / Poisson / pulse input blocks */
+    EDEN_KERNEL_CELLS = 1,    /* windowed cell kernel (batched mode) */
+    EDEN_KERNEL_TARGETS = 2,  /* per-step target kernel (plain mode) */
+    EDEN_KERNEL_HINES = 3,    /* per-step cable solve (plain mode) */
+    EDEN_KERNEL_DELIVER = 4,  /* spike fan-out */
+    EDEN_KERNEL_KINDS = 5
+};
 
 /* Records produced since the previous fetch, in step order. */
 typedef struct EdenGpuRecords {
@@ -201,6 +213,11 @@ int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *state_a, floa
 /* Device time of the last edenGpuRun in milliseconds and the number of
  * kernel launches it issued. */
 int edenGpuLastRunStats(EdenGpuCtx *ctx, double *device_ms, int64_t *launches);
+
+/* Per-kernel device time accumulated since creation when kernel_timing is
+ * set (the reference's only timing is its Config/Setup/Run wall-clock line,
+ * eden/Eden.cpp:11951; this is the GPU-side breakdown of Run). */
+int edenGpuKernelStats(EdenGpuCtx *ctx, int32_t kind, double *total_ms, int64_t *launches);
 
 const char *edenGpuLastError(EdenGpuCtx *ctx);
 void edenGpuDestroy(EdenGpuCtx *ctx);
