@@ -1,0 +1,183 @@
+"""`eden nml <LEMS file>` on the GPU, and the runEden() wrapper.
+
+Drop-in for the reference's command line (eden/Eden.cpp:10379-10546) and its
+Python wrapper (testing/python_package/eden_simulator/run_sim.py:22-107):
+the same LEMS/NeuroML input, the same output files -- OutputFile trajectories
+as "%+16.8g" columns (time in seconds, then each quantity in SI units,
+eden/Eden.cpp:10856-10871) and EventOutputFile spikes in TIME_ID / ID_TIME
+form (10897-10927) -- and the same `Config: .. Setup: .. Run: ..` timing line
+(11951).  Command-line tokens the reference accepts are accepted; `gcc`,
+`icc` and the CPU-only debugging tokens are ignored.
+
+    python -m eden_gb300 nml LEMS_file.xml [rng_seed N] [verbose] [plain]
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+from collections import OrderedDict
+
+import numpy as np
+
+from . import lowering, neuroml_io
+
+
+def _fmt(x: float) -> str:
+    return "%+16.8g" % x
+
+
+def _step_times(dt_us: float, last_step: int) -> np.ndarray:
+    """Simulation time in seconds of steps 0..last_step: the reference starts at
+    0, runs the initialisation steps at t = 0 and then adds the float dt to a
+    double accumulator once per step (eden/Eden.cpp:11486, 11931), so step
+    k >= 1 runs at the double sum of k - 1 dts."""
+    n = max(int(last_step), 1)
+    acc = np.concatenate([[0.0], np.add.accumulate(np.full(n - 1, float(np.float32(dt_us))))])
+    return np.concatenate([[0.0], acc]) * 1e-6
+
+
+def write_outputs(spec, low, rec, base_dir: str, n_steps: int) -> list:
+    """Write every OutputFile / EventOutputFile of the simulation."""
+    written = []
+    last = max([int(rec.trace_step.max()) if len(rec.trace_step) else 1,
+                int(rec.spike_step.max()) if len(rec.spike_step) else 1, n_steps])
+    times = _step_times(float(low.dt), last)
+    col0 = 0
+    for _id, fname, cols in getattr(spec, "output_files", []):
+        path = os.path.join(base_dir, fname)
+        ncol = len(cols)
+        block = rec.trace[:, col0:col0 + ncol].astype(np.float64) * 1e-3  # mV -> V
+        with open(path, "w") as f:
+            for r in range(block.shape[0]):
+                k = int(rec.trace_step[r])
+                f.write(_fmt(times[k]) + "".join(" " + _fmt(v) for v in block[r]) + "\n")
+        col0 += ncol
+        written.append(path)
+    # spikes: per logging step, in EventSelection order
+    for _id, fname, fmt, sels in getattr(spec, "event_files", []):
+        path = os.path.join(base_dir, fname)
+        off = spec.pop_offsets()
+        col_of_src = {}
+        for j, (_sid, _sel, (pop, idx)) in enumerate(sels):
+            col_of_src.setdefault(off[pop] + idx, []).append(j)
+        rows = []
+        for s, k in zip(rec.spike_src, rec.spike_step):
+            for j in col_of_src.get(int(s), []):
+                rows.append((int(k), j))
+        rows.sort()
+        with open(path, "w") as f:
+            for k, j in rows:
+                t = _fmt(times[k])
+                sid = sels[j][0]
+                if fmt == "ID_TIME":
+                    f.write(f"{sid} {t.strip()}\n")
+                else:
+                    f.write(f"{t} {sid}\n")
+        written.append(path)
+    return written
+
+
+def run_lems(lems_file: str, seed: int | None = None, mode: str = "batched", verbose: bool = False,
+             out_dir: str | None = None) -> dict:
+    """Simulate a LEMS file on the GPU and write its output files next to it
+    (or in out_dir).  Returns timing in seconds: config, setup, run."""
+    from .engine import MODE_BATCHED, MODE_PLAIN, Simulation
+    t0 = time.perf_counter()
+    spec = neuroml_io.read_lems(lems_file)
+    if seed is not None:
+        spec.seed = seed
+    t1 = time.perf_counter()
+    low = lowering.lower(spec)
+    sim = Simulation(low, mode=MODE_PLAIN if mode == "plain" else MODE_BATCHED)
+    t2 = time.perf_counter()
+    rec = sim.run()
+    t3 = time.perf_counter()
+    sim.close()
+    base = out_dir or os.path.dirname(os.path.abspath(lems_file))
+    files = write_outputs(spec, low, rec, base, low.n_steps)
+    if verbose:
+        print(f"{low.n_target} targets, {len(low.syn_target)} synapses, {low.n_steps} steps; wrote {files}")
+    return {"config": t1 - t0, "setup": t2 - t1, "run": t3 - t2, "files": files}
+
+
+def main(argv=None) -> int:
+    argv = list(sys.argv[1:] if argv is None else argv)
+    lems, seed, verbose, mode = None, None, False, "batched"
+    i = 0
+    while i < len(argv):
+        tok = argv[i]
+        if tok == "nml":
+            lems = argv[i + 1]
+            i += 2
+            continue
+        if tok == "rng_seed":
+            seed = int(argv[i + 1])
+            i += 2
+            continue
+        if tok == "cable_solver":
+            if argv[i + 1] not in ("auto", "bwd_euler"):
+                print(f"cable_solver {argv[i + 1]} is not available on the GPU path (backward Euler only)")
+                return 2
+            i += 2
+            continue
+        if tok == "verbose":
+            verbose = True
+        elif tok == "plain":
+            mode = "plain"
+        elif tok in ("gcc", "icc", "-S", "debug", "debug_netcode", "full_dump", "dump_state_scalar",
+                     "dump_raw_layout"):
+            pass
+        else:
+            print(f"unknown command line token {tok}")
+            return 2
+        i += 1
+    if lems is None:
+        print("usage: eden nml <LEMS file> [rng_seed N] [verbose] [plain]")
+        return 2
+    print("--- Extensible Dynamics Engine for Networks (GB300 step loop) ---")
+    try:
+        t = run_lems(lems, seed=seed, mode=mode, verbose=verbose)
+    except (ValueError, OSError) as e:
+        print(f"cmdline: could not make sense of NeuroML file: {e}")
+        return 1
+    print("Config: %.3f Setup: %.3f Run: %.3f " % (t["config"], t["setup"], t["run"]))
+    return 0
+
+
+def runEden(example_lems_file, reload_events=False, threads=None, extra_cmdline_args=None, executable_path=None,
+            verbose=False, full_cmdline=None):
+    """Run a LEMS/NeuroML2 file on the GPU; same signature and return value as
+    the reference wrapper: an OrderedDict of trajectories ('t' and one key per
+    OutputColumn quantity) and, with reload_events, one of spike times per
+    EventSelection select path.  `threads`, `executable_path` and
+    `full_cmdline` concern the CPU executable and are accepted and ignored."""
+    args = ["nml", example_lems_file] + list(extra_cmdline_args or [])
+    rc = main(args)
+    if rc != 0:
+        raise RuntimeError("Could not run simulation")
+    return reload_saved_data(example_lems_file, reload_events=reload_events)
+
+
+def reload_saved_data(lems_file_name, reload_events=False):
+    """Read back the output files a run wrote (run_sim.py:110-252)."""
+    spec = neuroml_io.read_lems(lems_file_name)
+    base = os.path.dirname(os.path.abspath(lems_file_name))
+    traces, events = OrderedDict(), OrderedDict()
+    for _id, fname, cols in spec.output_files:
+        data = np.loadtxt(os.path.join(base, fname), ndmin=2)
+        traces["t"] = data[:, 0]
+        for j, (_cid, quantity, _t) in enumerate(cols):
+            traces[quantity] = data[:, j + 1]
+    if reload_events:
+        for _id, fname, fmt, sels in spec.event_files:
+            sel_of = {sid: select for sid, select, _ in sels}
+            for _sid, select, _ in sels:
+                events[select] = []
+            with open(os.path.join(base, fname)) as f:
+                for line in f:
+                    a, b = line.split()
+                    t, sid = (float(a), int(b)) if fmt == "TIME_ID" else (float(b), int(a))
+                    events[sel_of[sid]].append(t)
+        return OrderedDict(sorted(traces.items())), OrderedDict(sorted(events.items()))
+    return OrderedDict(sorted(traces.items()))

@@ -97,10 +97,16 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
         w(f' <population id="{p.name}" component="{p.cell_type}" size="{p.size}"/>\n')
     pop_of, local_of = _gid_maps(spec)
     for pr in spec.projections:
-        groups = defaultdict(list)
+        # consecutive runs of one (pre, post) population pair, so the file's
+        # connection order -- the reference's instantiation order -- is the
+        # projection's own
+        groups = []
         for i in range(len(pr.pre_cell)):
-            groups[(pop_of[pr.pre_cell[i]], pop_of[pr.post_cell[i]])].append(i)
-        for gi, ((pa, pb), idx) in enumerate(groups.items()):
+            key = (pop_of[pr.pre_cell[i]], pop_of[pr.post_cell[i]])
+            if not groups or groups[-1][0] != key:
+                groups.append((key, []))
+            groups[-1][1].append(i)
+        for gi, ((pa, pb), idx) in enumerate(groups):
             w(f' <projection id="{pr.name}_{gi}" presynapticPopulation="{pa}" '
               f'postsynapticPopulation="{pb}" synapse="{pr.synapse}">\n')
             for n, i in enumerate(idx):
@@ -218,3 +224,324 @@ def _write_cell(w, spec: NetworkSpec, c: PhysicalCell) -> None:
     w('  </membraneProperties>\n  <intracellularProperties>\n')
     w(f'   <resistivity value="{_f(c.ra)} ohm_cm"/>\n')
     w('  </intracellularProperties>\n </biophysicalProperties>\n</cell>\n')
+
+
+# ---------------------------------------------------------------------------
+# reading
+# ---------------------------------------------------------------------------
+# unit name -> factor to the NetworkSpec unit of its dimension (mV, ms, nS,
+# nA, pF, mS/cm2, uF/cm2, ohm*cm, Hz, per_ms, nS/mV), following the scales
+# the reference accepts (eden/NeuroML.cpp:307-400)
+_UNITS = {
+    "voltage": {"V": 1e3, "mV": 1.0},
+    "time": {"s": 1e3, "sec": 1e3, "second": 1e3, "seconds": 1e3, "ms": 1.0, "msec": 1.0, "us": 1e-3,
+             "usec": 1e-3},
+    "conductance": {"S": 1e9, "mS": 1e6, "uS": 1e3, "nS": 1.0, "pS": 1e-3},
+    "current": {"A": 1e9, "mA": 1e6, "uA": 1e3, "nA": 1.0, "pA": 1e-3},
+    "capacitance": {"F": 1e12, "mF": 1e9, "uF": 1e6, "nF": 1e3, "pF": 1.0},
+    "conductivity": {"S_per_m2": 0.1, "mS_per_cm2": 1.0, "S_per_cm2": 1e3, "S_per_mm2": 1e5},
+    "spec_capacitance": {"uF_per_cm2": 1.0, "F_per_m2": 100.0, "uF_per_mm2": 100.0},
+    "resistivity": {"ohm_cm": 1.0, "kohm_cm": 1e3, "ohm_m": 100.0},
+    "frequency_hz": {"Hz": 1.0, "per_s": 1.0, "per_ms": 1e3, "kHz": 1e3, "per_us": 1e6, "MHz": 1e6},
+    "rate_per_ms": {"per_ms": 1.0, "kHz": 1.0, "per_s": 1e-3, "Hz": 1e-3, "per_us": 1e3, "MHz": 1e3},
+    "cond_per_voltage": {"nS_per_mV": 1.0, "S_per_V": 1e9 / 1e3, "uS_per_mV": 1e3, "pS_per_mV": 1e-3},
+}
+_QTY = re.compile(r"^\s*([-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?)\s*([A-Za-z_0-9]*)\s*$")
+
+
+def _qty(el, attr, dim, default=None):
+    text = el.get(attr)
+    if text is None:
+        if default is not None:
+            return default
+        raise ValueError(f"<{_tag(el)}> lacks required attribute {attr}")
+    m = _QTY.match(text)
+    if not m:
+        raise ValueError(f"<{_tag(el)}> {attr}={text!r} is not a number with a unit")
+    value, unit = float(m.group(1)), m.group(2)
+    if dim is None:
+        if unit:
+            raise ValueError(f"<{_tag(el)}> {attr}={text!r} should be dimensionless")
+        return value
+    table = _UNITS[dim]
+    if unit not in table:
+        raise ValueError(f"<{_tag(el)}> {attr}: unit {unit!r} not supported for {dim} (known: {sorted(table)})")
+    return value * table[unit]
+
+
+def _tag(el):
+    return el.tag.split("}")[-1]
+
+
+def _children(el, tag):
+    return [c for c in el if _tag(c) == tag]
+
+
+_RATE_KIND = {v: k for k, v in RATE_TYPE_NAMES.items()}
+
+
+def _parse_rate(el):
+    kind = el.get("type")
+    if kind not in _RATE_KIND:
+        raise ValueError(f"gate rate type {kind!r} not supported (HHExpRate, HHExpLinearRate, HHSigmoidRate)")
+    return Rate(_RATE_KIND[kind], _qty(el, "rate", "rate_per_ms"), _qty(el, "midpoint", "voltage"),
+                _qty(el, "scale", "voltage"))
+
+
+def _parse_cell(el, channels_by_name):
+    name = el.get("id")
+    morph = _children(el, "morphology")
+    if len(morph) != 1:
+        raise ValueError(f"cell {name}: exactly one inline <morphology> is supported")
+    segs = _children(morph[0], "segment")
+    ids = [int(s.get("id")) for s in segs]
+    index = {sid: i for i, sid in enumerate(ids)}
+    n = len(segs)
+    parent = np.full(n, -1, np.int64)
+    length = np.zeros(n)
+    dprox = np.zeros(n)
+    ddist = np.zeros(n)
+    dist_pt = [None] * n
+    for i, s in enumerate(segs):
+        par = _children(s, "parent")
+        if par:
+            if par[0].get("fractionAlong", "1") not in ("1", "1.0"):
+                raise ValueError(f"cell {name}: segment {ids[i]} attaches with fractionAlong != 1")
+            parent[i] = index[int(par[0].get("segment"))]
+            if parent[i] >= i:
+                raise ValueError(f"cell {name}: segment {ids[i]} must follow its parent")
+        d = _children(s, "distal")[0]
+        pr = _children(s, "proximal")
+        p_el = pr[0] if pr else None
+        dp = np.array([float(d.get(k)) for k in "xyz"])
+        if p_el is not None:
+            pp = np.array([float(p_el.get(k)) for k in "xyz"])
+            dprox[i] = float(p_el.get("diameter"))
+        else:
+            if parent[i] < 0:
+                raise ValueError(f"cell {name}: root segment needs a proximal point")
+            pp = dist_pt[parent[i]]
+            dprox[i] = ddist[parent[i]]
+        ddist[i] = float(d.get("diameter"))
+        dist_pt[i] = dp
+        length[i] = float(np.sqrt(((dp - pp) ** 2).sum()))
+    if ids != sorted(ids) or ids[0] != 0:
+        raise ValueError(f"cell {name}: segments must be numbered 0.. in order")
+    groups = {}
+    for g in _children(morph[0], "segmentGroup"):
+        mask = np.zeros(n, bool)
+        for mbr in _children(g, "member"):
+            mask[index[int(mbr.get("segment"))]] = True
+        for inc in _children(g, "include"):
+            mask |= groups[inc.get("segmentGroup")]
+        if _children(g, "property"):
+            raise ValueError(f"cell {name}: segment group properties (cable subdivision) are not supported")
+        groups[g.get("id")] = mask
+    groups.setdefault("all", np.ones(n, bool))
+    bio = _children(el, "biophysicalProperties")[0]
+    mem = _children(bio, "membraneProperties")[0]
+    intra = _children(bio, "intracellularProperties")[0]
+    dens = []
+    cm = v0 = thr = None
+    for c in mem:
+        t = _tag(c)
+        if t == "channelDensity":
+            ch = c.get("ionChannel")
+            if ch not in channels_by_name:
+                raise ValueError(f"cell {name}: unknown ionChannel {ch}")
+            mask = groups[c.get("segmentGroup", "all")]
+            dens.append(ChannelDensity(channels_by_name[ch], _qty(c, "condDensity", "conductivity"),
+                                       _qty(c, "erev", "voltage"), mask.copy()))
+        elif t == "specificCapacitance":
+            cm = _qty(c, "value", "spec_capacitance")
+        elif t == "initMembPotential":
+            v0 = _qty(c, "value", "voltage")
+        elif t == "spikeThresh":
+            thr = _qty(c, "value", "voltage")
+        else:
+            raise ValueError(f"cell {name}: <{t}> is not supported")
+    ra = _qty(_children(intra, "resistivity")[0], "value", "resistivity")
+    cell = PhysicalCell(name, parent, length, ddist.copy(), dens, cm=cm, ra=ra, v0=v0,
+                        spike_thresh=thr if thr is not None else 0.0, seg_groups=groups)
+    cell.seg_dprox = dprox
+    return cell
+
+
+def _cell_ref(text, pops):
+    """'../pop[3]', '../pop/3/celltype', 'pop[3]' or 'pop/3' -> (population, index)."""
+    t = text.strip()
+    while t.startswith("../"):
+        t = t[3:]
+    m = re.match(r"^([^/\[\]]+)\[(\d+)\]", t)
+    if m:
+        return m.group(1), int(m.group(2))
+    parts = t.split("/")
+    if len(parts) >= 2 and parts[0] in pops:
+        return parts[0], int(parts[1])
+    raise ValueError(f"cell reference {text!r} not understood")
+
+
+def read_lems(path: str) -> NetworkSpec:
+    """Read a LEMS simulation file (and the NeuroML it includes) into a
+    NetworkSpec.  Raises ValueError on anything outside the supported subset."""
+    base = os.path.dirname(os.path.abspath(path))
+    root = ET.parse(path).getroot()
+    elems = list(root)
+    for inc in _children(root, "Include"):
+        f = inc.get("file")
+        if f in ("Cells.xml", "Networks.xml", "Simulation.xml", "Synapses.xml", "Inputs.xml",
+                 "NeuroMLCoreDimensions.xml", "NeuroMLCoreCompTypes.xml", "Channels.xml", "PyNN.xml"):
+            continue
+        fp = os.path.join(base, f)
+        elems.extend(list(ET.parse(fp).getroot()))
+    target = _children(root, "Target")[0].get("component")
+    sims = [e for e in elems if _tag(e) == "Simulation" and e.get("id") == target]
+    if not sims:
+        raise ValueError(f"simulation {target} not found")
+    sim = sims[0]
+    seed = int(sim.get("seed", "0"))
+    spec = NetworkSpec(os.path.splitext(os.path.basename(path))[0], _qty(sim, "step", "time"),
+                       _qty(sim, "length", "time"), seed)
+    # components
+    channels_by_name, synapses, pulses_def, pois_def, cells = {}, {}, {}, {}, {}
+    net = None
+    for e in elems:
+        t = _tag(e)
+        if t == "ionChannelHH" or t == "ionChannel":
+            gates = []
+            for g in e:
+                gt = _tag(g)
+                if gt in ("notes", "annotation"):
+                    continue
+                if gt != "gateHHrates":
+                    raise ValueError(f"ionChannel {e.get('id')}: <{gt}> not supported (gateHHrates only)")
+                fwd = _parse_rate(_children(g, "forwardRate")[0])
+                rev = _parse_rate(_children(g, "reverseRate")[0])
+                gates.append(Gate(g.get("id"), int(g.get("instances", "1")), fwd, rev))
+            channels_by_name[e.get("id")] = len(spec.channels)
+            spec.channels.append(Channel(e.get("id"), gates, e.get("species")))
+        elif t == "expOneSynapse":
+            synapses[e.get("id")] = SynapseType(e.get("id"), SYN_EXPONE, _qty(e, "gbase", "conductance"),
+                                                _qty(e, "erev", "voltage"), _qty(e, "tauDecay", "time"))
+        elif t == "expTwoSynapse":
+            synapses[e.get("id")] = SynapseType(e.get("id"), SYN_EXPTWO, _qty(e, "gbase", "conductance"),
+                                                _qty(e, "erev", "voltage"), _qty(e, "tauDecay", "time"),
+                                                _qty(e, "tauRise", "time"))
+        elif t == "pulseGenerator":
+            pulses_def[e.get("id")] = (_qty(e, "delay", "time"), _qty(e, "duration", "time"),
+                                       _qty(e, "amplitude", "current"))
+        elif t == "poissonFiringSynapse":
+            pois_def[e.get("id")] = (_qty(e, "averageRate", "frequency_hz"), e.get("synapse"))
+        elif t == "izhikevich2007Cell":
+            cells[e.get("id")] = Izhikevich2007Cell(
+                e.get("id"), C=_qty(e, "C", "capacitance"), k=_qty(e, "k", "cond_per_voltage"),
+                vr=_qty(e, "vr", "voltage"), vt=_qty(e, "vt", "voltage"), vpeak=_qty(e, "vpeak", "voltage"),
+                a=_qty(e, "a", "rate_per_ms"), b=_qty(e, "b", "conductance"), c=_qty(e, "c", "voltage"),
+                d=_qty(e, "d", "current") * 1e3, v0=_qty(e, "v0", "voltage"))  # d in pA
+        elif t == "network" and e.get("id") == sim.get("target"):
+            net = e
+    for e in elems:
+        if _tag(e) == "cell":
+            cells[e.get("id")] = _parse_cell(e, channels_by_name)
+    if net is None:
+        raise ValueError(f"network {sim.get('target')} not found")
+    spec.synapses = list(synapses.values())
+    syn_names = list(synapses)
+    # populations (declaration order = gid order)
+    pops = {}
+    for p in _children(net, "population"):
+        comp = p.get("component")
+        if comp not in cells:
+            raise ValueError(f"population {p.get('id')}: component {comp} not supported")
+        size = int(p.get("size")) if p.get("size") else len(_children(p, "instance"))
+        pops[p.get("id")] = Population(p.get("id"), comp, size)
+        spec.populations.append(pops[p.get("id")])
+    used = {p.cell_type for p in spec.populations}
+    spec.cells = [c for n_, c in cells.items() if n_ in used]
+    off = spec.pop_offsets()
+    gid = lambda pop_idx: off[pop_idx[0]] + pop_idx[1]
+    # projections
+    by_syn = {}
+    for pr in _children(net, "projection"):
+        syn = pr.get("synapse")
+        if syn not in synapses:
+            raise ValueError(f"projection {pr.get('id')}: synapse {syn} not supported")
+        rows = by_syn.setdefault(syn, [[], [], [], [], []])
+        for c in pr:
+            if _tag(c) not in ("connectionWD", "connection"):
+                continue
+            rows[0].append(gid(_cell_ref(c.get("preCellId"), pops)))
+            rows[1].append(gid(_cell_ref(c.get("postCellId"), pops)))
+            rows[2].append(int(c.get("postSegmentId", "0")))
+            rows[3].append(float(c.get("weight", "1")))
+            rows[4].append(_qty(c, "delay", "time", 0.0) if c.get("delay") else 0.0)
+    for syn, rows in by_syn.items():
+        spec.projections.append(Projection(f"proj_{syn}", "*", "*", syn, np.array(rows[0], np.int64),
+                                           np.array(rows[1], np.int64), np.array(rows[2], np.int64),
+                                           np.array(rows[3]), np.array(rows[4])))
+    # inputs
+    pcell, pseg, pdel, pdur, pamp = [], [], [], [], []
+    pois_rows = {}
+    for il in _children(net, "inputList"):
+        comp = il.get("component")
+        for inp in _children(il, "input"):
+            g = gid(_cell_ref(inp.get("target"), pops))
+            seg = int(inp.get("segmentId", "0"))
+            if comp in pulses_def:
+                d, du, a = pulses_def[comp]
+                pcell.append(g); pseg.append(seg); pdel.append(d); pdur.append(du); pamp.append(a)
+            elif comp in pois_def:
+                pois_rows.setdefault(comp, []).append((g, seg))
+            else:
+                raise ValueError(f"inputList component {comp} not supported")
+    for ei in _children(net, "explicitInput"):
+        comp = ei.get("input")
+        g = gid(_cell_ref(ei.get("target"), pops))
+        if comp not in pulses_def:
+            raise ValueError(f"explicitInput {comp} not supported")
+        d, du, a = pulses_def[comp]
+        pcell.append(g); pseg.append(0); pdel.append(d); pdur.append(du); pamp.append(a)
+    if pcell:
+        spec.pulses.append(PulseInputs("*", np.array(pcell), np.array(pseg), np.array(pdel), np.array(pdur),
+                                       np.array(pamp)))
+    for comp, rows in pois_rows.items():
+        rate, syn = pois_def[comp]
+        if syn not in synapses:
+            raise ValueError(f"poissonFiringSynapse {comp}: synapse {syn} not supported")
+        spec.poissons.append(PoissonInputs("*", syn, rate, np.array([r[0] for r in rows]),
+                                           np.array([r[1] for r in rows])))
+    # recorders
+    spec.trace_columns, spec.event_selections = [], []
+    spec.output_files, spec.event_files = [], []
+    for of in _children(sim, "OutputFile"):
+        cols = []
+        for col in _children(of, "OutputColumn"):
+            cols.append((col.get("id"), col.get("quantity"), _quantity_target(col.get("quantity"), pops, cells)))
+        spec.output_files.append((of.get("id"), of.get("fileName"), cols))
+        spec.trace_columns.extend(OutputColumn(*c[2]) for c in cols)
+    for ef in _children(sim, "EventOutputFile"):
+        sels = []
+        for sel in _children(ef, "EventSelection"):
+            pop, idx = _cell_ref(sel.get("select"), pops)
+            sels.append((int(sel.get("id")), sel.get("select"), (pop, idx)))
+        spec.event_files.append((ef.get("id"), ef.get("fileName"), ef.get("format", "TIME_ID"), sels))
+        spec.event_selections.extend(EventSelection(s[2][0], s[2][1], 0) for s in sels)
+    return spec
+
+
+def _quantity_target(q, pops, cells):
+    """'pop/3/celltype/seg/v', 'pop/3/celltype/v' or 'pop[3]/v' -> (pop, cell, seg)."""
+    parts = q.strip().split("/")
+    if parts[-1] != "v":
+        raise ValueError(f"recorded quantity {q!r}: only membrane potential v is supported")
+    m = re.match(r"^([^/\[\]]+)\[(\d+)\]$", parts[0])
+    if m:
+        pop, idx, rest = m.group(1), int(m.group(2)), parts[1:-1]
+    else:
+        pop, idx, rest = parts[0], int(parts[1]), parts[2:-1]
+        if rest and rest[0] in cells:
+            rest = rest[1:]
+    seg = int(rest[0]) if rest else 0
+    if pop not in pops:
+        raise ValueError(f"recorded quantity {q!r}: unknown population")
+    return (pop, idx, seg)

@@ -1,0 +1,46 @@
+"""Regenerate the golden fixtures from the reference simulator.
+
+Writes each case of cases.py as LEMS/NeuroML, runs the reference EDEN built
+from its own sources (oracle/_ref/eden, see oracle/Makefile) in a scratch
+directory, and stores its OutputFile trajectory and EventOutputFile spikes in
+tests/golden/<case>.npz.  Needs the reference source tree (to build the
+oracle binary); the fixtures it writes are what the tests read.
+
+    python tests/golden/make_golden.py [case ...]
+"""
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, HERE)
+
+import reference_runner  # noqa: E402
+from cases import CASES, spec_of  # noqa: E402
+from eden_gb300 import neuroml_io  # noqa: E402
+
+
+def make(name):
+    spec = spec_of(name)
+    with tempfile.TemporaryDirectory() as d:
+        lems = neuroml_io.write_lems(spec, d)
+        out = reference_runner.run(lems, threads=4)
+    traj = out["trajectory"].astype(np.float64)
+    ev = np.array(out.get("events", []), dtype=np.float64).reshape(-1, 2)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), time_s=traj[:, 0], values_si=traj[:, 1:].astype(np.float32),
+                        event_time_s=ev[:, 0], event_id=ev[:, 1].astype(np.int32),
+                        trajectory_head=out["trajectory_text"].splitlines()[:3],
+                        events_head=out.get("events_text", "").splitlines()[:3])
+    print(f"{name}: {traj.shape[0]} samples x {traj.shape[1] - 1} columns, {len(ev)} spikes")
+
+
+if __name__ == "__main__":
+    if not reference_runner.available():
+        sys.exit("oracle/_ref/eden is not built (make -C oracle ref)")
+    for name in (sys.argv[1:] or list(CASES)):
+        make(name)

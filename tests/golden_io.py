@@ -1,0 +1,18 @@
+"""Loading the reference's golden outputs in the oracle's terms."""
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def load(name, lowered):
+    """Returns (trace_mV [samples, columns], spike_src, spike_log_step)."""
+    z = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    trace = z["values_si"].astype(np.float64) * 1e3
+    dt_s = float(lowered.dt) * 1e-6
+    ids = z["event_id"]
+    src = lowered.event_src[ids] if len(ids) else np.zeros(0, np.int32)
+    # an event stamped t_n was emitted in step n and is logged at step n + 1
+    step = np.rint(z["event_time_s"] / dt_s).astype(np.int64) + 1
+    return trace, src, step

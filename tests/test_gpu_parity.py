@@ -15,24 +15,16 @@ import eden_port
 from eden_gb300 import lowering, workloads
 from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
 from criteria import box_violations, samecount
+from golden.cases import CASES, spec_of
+from golden_io import load
 from helpers import spike_trains
 
 pytestmark = pytest.mark.gpu
 
-CASES = {
-    "single_comp_hh": dict(n_cells=64, length_ms=100.0),
-    "izh_net": dict(n_cells=300, in_degree=20, length_ms=100.0),
-    "multicomp_poisson": ("multicomp_net", dict(n_cells=24, in_degree=20, length_ms=60.0, max_seg=80, weight=0.0)),
-    "multicomp_recurrent": ("multicomp_net", dict(n_cells=24, in_degree=20, length_ms=15.0, max_seg=80)),
-    "ball_and_stick": dict(n_inst=8, length_ms=40.0),
-}
 
 
 def _spec(name):
-    case = CASES[name]
-    if isinstance(case, tuple):
-        return workloads.CONFIGS[case[0]](**case[1])
-    return workloads.CONFIGS[name](**case)
+    return spec_of(name)
 
 
 @pytest.fixture(scope="module")
@@ -64,3 +56,19 @@ def test_gpu_matches_oracle(name, mode, oracle_runs):
     assert np.isfinite(rec.trace).all()
     nbad, worst = box_violations(ref["trace"], rec.trace, dt_ms, 0.1, 0.5)
     assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst by {worst} mV"
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_gpu_matches_reference_outputs(name, oracle_runs):
+    """The GPU path against the reference simulator's own fixture outputs."""
+    low, _ = oracle_runs(name)
+    ref_trace, ref_src, ref_step = load(name, low)
+    sim = Simulation(low, mode=MODE_BATCHED)
+    rec = sim.run()
+    sim.close()
+    dt_ms = float(low.dt) * 1e-3
+    wrong, far = samecount(spike_trains(ref_src, ref_step), spike_trains(rec.spike_src, rec.spike_step),
+                           int(round(0.1 / dt_ms)))
+    assert not wrong and not far, f"spike trains differ: counts {wrong[:5]}, timing {far[:5]}"
+    nbad, worst = box_violations(ref_trace, rec.trace, dt_ms, 0.1, CASES[name][2])
+    assert nbad == 0, f"{nbad} samples outside box, worst {worst} mV"
