@@ -44,14 +44,20 @@ struct SynTypeDev {
 // x / tau, correctly rounded, from r = RN(1/tau): q = RN(x*r) is within an
 // ulp of the quotient, the residual x - tau*q is exact in one FMA, and
 // RN(q + r*residual) is the correctly rounded quotient (Markstein's
-// theorem, the basis of software division on FMA machines).  The guard sends
-// operands near the underflow range, where the residual is not exact, to
-// the hardware division.
+// theorem, the basis of software division on FMA machines).  The residual
+// is exact only away from the underflow range, so an operand below 2^-100
+// is scaled by 2^64 first (exact) and the quotient scaled back (exact unless
+// the quotient itself is subnormal, where it may differ from the correctly
+// rounded one by one subnormal ulp, 2^-149).  Branch-free: synapse states
+// that have decayed to tiny values or zero are common, and a divergent
+// branch to a hardware division there cost more than the division saves.
 __device__ __forceinline__ float div_by_tau(float x, float tau, float r) {
-    if (fabsf(x) < 0x1p-100f) return x / tau;
-    const float q = x * r;
-    const float e = fmaf(-q, tau, x);
-    return fmaf(e, r, q);
+    const bool tiny = fabsf(x) < 0x1p-100f;
+    const float xs = tiny ? x * 0x1p64f : x;
+    const float q = xs * r;
+    const float e = fmaf(-q, tau, xs);
+    const float qs = fmaf(e, r, q);
+    return tiny ? qs * 0x1p-64f : qs;
 }
 
 __constant__ ChanTypeDev c_chan_types[kMaxChanTypes];
