@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -1500,5 +1501,160 @@ extern "C" int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *st
         CUDA_TRY(ctx, cudaMemcpy(tmp.data(), srcs[k], sizeof(float) * n, cudaMemcpyDeviceToHost));
         for (int64_t u = 0; u < n; u++) outs[k][u] = tmp[ctx->syn_internal_of_user[u]];
     }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// edenGpuRunStaticScratch: edenGpuRun without any allocation.
+//
+// edenGpuRun can allocate while it runs: it grows the window table (device
+// memory and pinned host memory) when one call spans more windows than the
+// table holds, and the first batched call instantiates a CUDA graph.  A
+// caller that has handed the simulator a fixed device-memory budget up front
+// (a co-simulation beside other GPU code that owns the rest of HBM), or a
+// host loop that must not stall on cudaMalloc/cudaFree (both can synchronise
+// the whole device), cannot accept that.  This entry point runs the same
+// kernels in the same order as edenGpuRun, with
+//   - the input kernel's per-window conductance scratch (32 rows of n_chunk
+//     floats) in the file-scope array g_static_gp instead of the context's
+//     buffer, which limits it to models of at most kStaticGpChunks input
+//     chunks (16 MiB of scratch); larger models get EDEN_GPU_E_RANGE;
+//   - the window arguments in the file-scope table g_static_wtab, filled
+//     from a stack buffer at most kStaticWindows windows at a time;
+//   - plain launches: no graph, no kernel-timing events.
+// The first call on a device looks up both arrays' device addresses with
+// cudaGetSymbolAddress, with that device current.  That set-up should happen
+// before any stream capture begins: a call with n_steps = 0 does only it.
+// Nothing in either array has to start at zero: every window writes rows
+// 0..K-1 of every chunk before the cell kernels read them, and each launch
+// reads only table entries written by the copy before it.
+// The arrays exist once per device, not per context: calls that overlap in
+// time on one device (two threads, or two contexts on different streams)
+// race on them, so the caller must serialise such calls.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kStaticGpChunks = 131072;  // input chunks the static scratch holds
+constexpr int kStaticWindows = 128;      // window arguments copied per batch
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+float *g_static_gp_ptr[kStaticMaxDevices];
+WindowArgs *g_static_wtab_ptr[kStaticMaxDevices];
+}  // namespace
+
+static __device__ __align__(256) float g_static_gp[32 * kStaticGpChunks];
+static __device__ __align__(256) WindowArgs g_static_wtab[kStaticWindows];
+
+// Device addresses of the static arrays on ctx's device (which is current).
+static int static_scratch(EdenGpuCtx *ctx, float **gp, WindowArgs **tab) {
+    const int dev = ctx->device;
+    if (dev < 0 || dev >= kStaticMaxDevices)
+        return ctx->fail(EDEN_GPU_E_RANGE, "edenGpuRunStaticScratch: device %d beyond the %d supported", dev,
+                         kStaticMaxDevices);
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_gp_ptr[dev]) {
+        void *p = nullptr, *q = nullptr;
+        CUDA_TRY(ctx, cudaGetSymbolAddress(&p, g_static_gp));
+        CUDA_TRY(ctx, cudaGetSymbolAddress(&q, g_static_wtab));
+        g_static_gp_ptr[dev] = (float *)p;
+        g_static_wtab_ptr[dev] = (WindowArgs *)q;
+    }
+    *gp = g_static_gp_ptr[dev];
+    *tab = g_static_wtab_ptr[dev];
+    return 0;
+}
+
+// The launches of launch_window for window `idx` of `tab`, with the model
+// `dm` (the context's, scratch pointer replaced) and without timing marks.
+static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const WindowArgs *tab, int idx) {
+    cudaStream_t s = ctx->stream;
+    const int *zero = ctx->d_zero;
+    if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
+        k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(dm, tab, zero, idx);
+        int n = 1;
+        for (const auto &cl : ctx->classes) {
+            const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
+            k_cells_t<<<nb, kCellThreads, cl.smem, s>>>(dm, tab, zero, idx, cl.cta_begin, cl.cta_end);
+            n++;
+        }
+        k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);
+        return n + 1;
+    }
+    k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(dm, tab, zero, idx);
+    k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(dm, tab, zero, idx);
+    k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(dm, tab, zero, idx, ctx->forest_cap);
+    k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);
+    return 4;
+}
+
+extern "C" int edenGpuRunStaticScratch(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) {
+    if (!ctx) return EDEN_GPU_E_INVALID;
+    if (n_steps < 0) return ctx->fail(EDEN_GPU_E_INVALID, "negative step count");
+    if (first_step != ctx->next_step)
+        return ctx->fail(EDEN_GPU_E_INVALID, "steps must be contiguous: expected first_step %lld",
+                         (long long)ctx->next_step);
+    if (ctx->d.n_chunk > kStaticGpChunks)
+        return ctx->fail(EDEN_GPU_E_RANGE,
+                         "edenGpuRunStaticScratch: the model has %d input chunks but the static scratch holds %d "
+                         "(%d MiB); run it with edenGpuRun",
+                         ctx->d.n_chunk, kStaticGpChunks, (int)(sizeof(float) * 32 * kStaticGpChunks >> 20));
+    const int64_t last = first_step + n_steps - 1;
+    const int64_t rec_first = std::max<int64_t>(first_step, 1);
+    if (last >= rec_first && last - ctx->trace_first_unfetched + 1 > ctx->trace_cap)
+        return ctx->fail(EDEN_GPU_E_RANGE, "trajectory buffer holds %lld steps; fetch records first",
+                         (long long)ctx->trace_cap);
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    float *gp = nullptr;
+    WindowArgs *tab = nullptr;
+    TRY(static_scratch(ctx, &gp, &tab));
+    if (n_steps == 0) return 0;
+    DevModel dm = ctx->d;
+    dm.Gp = gp;
+    WindowArgs batch[kStaticWindows];
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    int64_t launches = 0;
+    int64_t s = first_step;
+    while (s <= last) {
+        // the same window schedule and bookkeeping as edenGpuRun
+        int nb = 0;
+        while (nb < kStaticWindows && s <= last) {
+            int K;
+            if (ctx->mode != EDEN_MODE_BATCHED) K = 1;
+            else if (s <= 0) K = (int)std::min<int64_t>(-s + 1, last - s + 1);
+            else K = (int)std::min<int64_t>(ctx->K, last - s + 1);
+            WindowArgs &w = batch[nb++];
+            w.step0 = s;
+            w.K = K;
+            w.Kprev = ctx->Kprev;
+            w.t0 = ctx->time;
+            w.t_prev0 = ctx->t_prev0;
+            w.par = ctx->par;
+            w.wpar = ctx->wpar;
+            if (s > 0) {
+                ctx->t_prev0 = ctx->time;
+                ctx->Kprev = K;
+                for (int k = 0; k < K; k++) ctx->time += (double)ctx->d.dt;
+            }
+            ctx->par ^= (K & 1);
+            ctx->wpar ^= 1;
+            s += K;
+        }
+        // stream-ordered after the previous batch's launches, so the table is
+        // not overwritten while they read it; the stack buffer is free for
+        // reuse once the copy call returns
+        CUDA_TRY(ctx, cudaMemcpyAsync(tab, batch, sizeof(WindowArgs) * nb, cudaMemcpyHostToDevice, ctx->stream));
+        for (int i = 0; i < nb; i++) launches += launch_window_static(ctx, dm, tab, i);
+        CUDA_TRY(ctx, cudaGetLastError());
+    }
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    CUDA_TRY(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->last_ms = ms;
+    ctx->last_launches = launches;
+    ctx->next_step = last + 1;
+    int status = 0;
+    CUDA_TRY(ctx, cudaMemcpy(&status, ctx->d.status, sizeof(int), cudaMemcpyDeviceToHost));
+    ctx->sticky_status |= status;
+    if (status & ST_LOG_OVERFLOW) return ctx->fail(EDEN_GPU_E_RANGE, "spike log overflow; fetch records more often");
     return 0;
 }

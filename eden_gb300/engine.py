@@ -45,7 +45,7 @@ class CRecords(ctypes.Structure):
                 ("n_trace_samples", ctypes.c_int64), ("n_spikes", ctypes.c_int64)]
 
 
-EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuFetchRecords", "edenGpuReadV", "edenGpuWriteV",
+EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuRunStaticScratch", "edenGpuFetchRecords", "edenGpuReadV", "edenGpuWriteV",
             "edenGpuReadSynapses", "edenGpuLastRunStats", "edenGpuKernelStats", "edenGpuLastError",
             "edenGpuDestroy", "edenGpuAbiVersion"]
 KERNEL_NAMES = ["k_inputs_t", "k_cells_t", "k_targets_t", "k_hines_t", "k_deliver_t"]

@@ -200,6 +200,25 @@ int edenGpuCreate(const EdenGpuModel *model, const EdenGpuOptions *opt, EdenGpuC
  * reference's output phase, 11555-11635). */
 int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
 
+/* edenGpuRun for callers that cannot allocate while the simulation runs (no
+ * counterpart in the reference, whose loop runs on the host).  edenGpuRun may
+ * allocate during a call -- it grows its window table when a call spans more
+ * windows than the table holds, and its first batched call instantiates a
+ * CUDA graph -- which a caller holding a fixed device-memory budget, or one
+ * that cannot let cudaMalloc/cudaFree synchronise the device mid-run, must
+ * avoid.  This entry point runs the same kernels in the same order and
+ * allocates nothing: the input scratch lives in a static device array of
+ * 16 MiB (models of at most 131072 input chunks of 32 inputs; larger models
+ * get EDEN_GPU_E_RANGE), window arguments in a static device table, and the
+ * launches are direct (no graph, no kernel timing).  Results equal
+ * edenGpuRun's; the two may be interleaved on one context.
+ * The first call on a device performs a one-time set-up (looking up the
+ * static arrays' device addresses); n_steps = 0 does only that, and it should
+ * come before any stream capture starts.  The static arrays are shared by all
+ * contexts on a device: calls that overlap in time on one device race on
+ * them, so serialise them. */
+int edenGpuRunStaticScratch(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
+
 /* Copy records accumulated since the last fetch into caller buffers. */
 int edenGpuFetchRecords(EdenGpuCtx *ctx, EdenGpuRecords *rec);
 
