@@ -14,7 +14,7 @@ LIB = os.path.join(HERE, "libeden_gpu.so")
 SOURCES = [os.path.join(HERE, "csrc", f) for f in ("eden_gpu.cu", "eden_kernels.cuh", "eden_math.cuh")]
 HEADER = os.path.join(ROOT, "include", "eden_gpu.h")
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-shared"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared"]
 
 
 def nvcc() -> str:

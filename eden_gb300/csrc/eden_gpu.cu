@@ -219,17 +219,6 @@ __global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs 
     }
 }
 
-// Windowed path: one CTA advances one group of cells K steps.  Within a
-// window no cell reads another cell's state: the only coupling is through
-// synaptic triggers, and every connection delay is >= K * dt, so a spike
-// emitted inside the window cannot fire a synapse before the window ends.
-// Its trigger bits are delivered after the window (k_deliver_t) and replayed
-// in order at the start of the next one (replay_mask), which reproduces the
-// step-by-step pending-spike decisions exactly.  Synaptic conductances do not
-// depend on V, so k_inputs_t has already produced them for all K steps.
-// Everything else a step touches -- membrane potentials, compartment
-// constants, channels and gates, the tree and its depth boundaries, input
-// block kinds -- is staged in shared memory for the whole window.
 // Windowed path: every warp advances one unit (a forest of physical cells or
 // a batch of izhikevich neurons) K steps on its own, synchronising only within
 // the warp.  Within a window no cell reads another cell's state: the only
@@ -241,173 +230,201 @@ __global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs 
 // exactly.  Synaptic conductances do not depend on V, so k_inputs_t has
 // already produced them for all K steps.  Everything else a step reads is
 // staged in the warp's shared-memory slice for the whole window.
-// This launch runs CTAs [cta_begin, cta_end).
+
+// A forest unit over the window.  Per step: trajectory samples of the step's
+// starting V; the flat compartments' pre-update V += c_kc (the same value
+// for every step, because their currents are linear in V with constant
+// conductance); the non-flat compartments' currents (inputs, channels with
+// the gate values before this step's update), diagonal and pre-update; the
+// cable solve; gate updates from the starting V; threshold crossings.
+__device__ __forceinline__ void forest_window(const DevModel &m, const WindowArgs &w, int u, float *S) {
+    const int lane = threadIdx.x & 31;
+    const int t0 = m.un_t0[u], n = m.un_t1[u] - t0, fi = m.un_f[u];
+    const int ngt = m.un_ngt[u], gt0 = m.un_gt0[u];
+    const int s0 = m.un_s0[u], ns = m.un_s1[u] - s0;
+    const int r0 = m.un_r0[u], r1 = m.un_r1[u];
+    const int nf0 = m.un_nf0[u], nf = m.un_nf1[u] - nf0;
+    const int nlev = m.fo_nlev[fi], l0 = m.fo_l0[fi];
+    float *X = S, *KC = S + n, *L = S + 2 * n, *PV = S + 3 * n, *RT = S + 4 * n, *U = S + 5 * n;
+    uint32_t *CEP = (uint32_t *)(S + 6 * n);
+    int32_t *NT = (int32_t *)(S + 7 * n);
+    float *VO = (float *)(NT + nf), *NA = VO + nf, *NC = NA + nf, *NIR = NC + nf;
+    float *GT = NIR + nf;
+    int32_t *GI_S = (int32_t *)(GT + ngt), *GI_TG = GI_S + ngt;
+    int32_t *LV = GI_TG + ngt;
+    int32_t *ST = LV + nlev + 1, *SSRC = ST + ns;
+    float *STHR = (float *)(SSRC + ns);
+    // ---- stage the unit
+    const float *vsrc = m.v[w.par];
+    for (int i = lane; i < n; i += 32) {
+        const int t = t0 + i;
+        X[i] = vsrc[t]; KC[i] = m.c_kc[t]; L[i] = m.c_l[t]; PV[i] = m.c_pv0[t];
+        RT[i] = m.c_rt0[t]; U[i] = m.c_u[t]; CEP[i] = m.c_cep[t];
+    }
+    for (int j = lane; j < nf; j += 32) {
+        const int ti = m.nf_t[nf0 + j], t = t0 + ti;
+        NT[j] = ti; NA[j] = m.c_area[t]; NC[j] = m.c_cm[t]; NIR[j] = m.c_inv_rc[t];
+        // gate update items: (non-flat slot, gate number | channel type << 8)
+        for (int ch = m.c_chan0[t]; ch < m.c_chan0[t + 1]; ch++) {
+            const int q0 = m.ch_gate0[ch] - gt0, q1 = m.ch_gate0[ch + 1] - gt0;
+            for (int q = q0; q < q1; q++) { GI_S[q] = j; GI_TG[q] = (q - q0) | (m.ch_type[ch] << 8); }
+        }
+    }
+    for (int i = lane; i < ngt; i += 32) GT[i] = m.gate[gt0 + i];
+    for (int i = lane; i <= nlev; i += 32) LV[i] = m.lvl[l0 + i] - t0;
+    for (int i = lane; i < ns; i += 32) { ST[i] = m.gs_t[s0 + i]; SSRC[i] = m.gs_src[s0 + i]; STHR[i] = m.gs_thr[s0 + i]; }
+    __syncwarp();
+    const float dt = m.dt;
+    for (int k = 0; k < w.K; k++) {
+        const int64_t step = w.step0 + k;
+        const bool init = step <= 0;
+        const float *Gpk = m.Gp + (size_t)k * m.n_chunk;
+        if (!init) {
+            // trajectory samples of this step's starting state
+            const int64_t row = (step - 1) % m.trace_cap;
+            for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = X[m.gr_t[q]];
+            __syncwarp();
+            // flat compartments (c_kc is 0 for the others, which the next loop sets)
+            for (int i = lane; i < n; i += 32) X[i] = X[i] + KC[i];
+        }
+        __syncwarp();
+        for (int j = lane; j < nf; j += 32) {
+            // channels + voltage pre-update (eden/Eden.cpp:5013-6107)
+            const int ti = NT[j], t = t0 + ti;
+            const float v = X[ti];
+            VO[j] = v;
+            float Iin, Gin, Isyn, Gsyn;
+            block_currents(Gpk, m.t_blk0[t], m.t_blk0[t + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
+                           Gsyn);
+            const float A = NA[j];
+            float Ich = 0.f, Gch = 0.f;
+            for (int ch = m.c_chan0[t]; ch < m.c_chan0[t + 1]; ch++) {
+                const ChanTypeDev &ct = c_chan_types[m.ch_type[ch]];
+                float fopen = 1.0f;
+                const float *q = GT + (m.ch_gate0[ch] - gt0);
+                for (int gi = 0; gi < ct.n_gates; gi++) {
+                    const float qo = q[gi];
+                    for (int rr = 0; rr < ct.inst[gi]; rr++) fopen = fopen * qo;
+                }
+                const float gs = m.ch_gbase[ch] * fopen;
+                Ich += (gs * (m.ch_erev[ch] - v) * 1e-5f) * A;
+                Gch += (gs * 1e-5f) * A;
+            }
+            const float I = Ich + Iin + Isyn;
+            const float G = Gch + Gin + Gsyn;
+            const float C = NC[j];
+            PV[ti] = 1.0f * (G / C) + NIR[j];
+            X[ti] = init ? v : v + (dt * (I + (v * G))) / C;
+        }
+        __syncwarp();
+        if (!init) hines_window(dt, X, L, PV, RT, U, CEP, LV, nlev);
+        // gate updates from this step's starting V and gate values (the
+        // currents above used the values before the update, as the reference does)
+        for (int q = lane; q < ngt; q += 32) {
+            const int tg = GI_TG[q];
+            GT[q] = gate_next(c_chan_types[tg >> 8], tg & 0xff, init, dt, VO[GI_S[q]], GT[q]);
+        }
+        // threshold crossings of the unit's spike sources (eden/Eden.cpp:6247-6252)
+        for (int q0 = 0; q0 < ns; q0 += 32) {
+            const int q = q0 + lane;
+            bool spk = false;
+            int src = -1;
+            if (q < ns) {
+                const int sl = ST[q];
+                src = SSRC[q];
+                spk = VO[sl] < STHR[q] && STHR[q] < X[NT[sl]];
+            }
+            push_spike(m, spk, src, (int32_t)(step + 1), w.wpar);
+        }
+        __syncwarp();
+    }
+    // ---- write the unit back into the buffer that holds the window's final state
+    float *vdst = m.v[w.par ^ (w.K & 1)];
+    for (int i = lane; i < n; i += 32) vdst[t0 + i] = X[i];
+    for (int i = lane; i < ngt; i += 32) m.gate[gt0 + i] = GT[i];
+}
+
+// A batch of up to 32 izhikevich2007Cell neurons over the window
+// (LEMS_CoreComponents.inc.xml:1140-1185), one lane each.
+__device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &w, int u, float *S) {
+    const int lane = threadIdx.x & 31;
+    const int t0 = m.un_t0[u], n = m.un_t1[u] - t0;
+    const int r0 = m.un_r0[u], r1 = m.un_r1[u];
+    // slice: V (two buffers), then C, v0, k, vr, vt, vpeak, a, b, c, d, u
+#define IZ(f, i) S[(2 + (f)) * n + (i)]
+    const int izh0 = m.t_izh[t0];
+    for (int i = lane; i < n; i += 32) {
+        const int iz = izh0 + i;
+        S[w.par * n + i] = m.v[w.par][t0 + i];
+        IZ(0, i) = m.iz_C[iz]; IZ(1, i) = m.iz_v0[iz]; IZ(2, i) = m.iz_k[iz]; IZ(3, i) = m.iz_vr[iz];
+        IZ(4, i) = m.iz_vt[iz]; IZ(5, i) = m.iz_vpeak[iz]; IZ(6, i) = m.iz_a[iz]; IZ(7, i) = m.iz_b[iz];
+        IZ(8, i) = m.iz_c[iz]; IZ(9, i) = m.iz_d[iz]; IZ(10, i) = m.iz_u[iz];
+    }
+    __syncwarp();
+    int par = w.par;
+    const float dt = m.dt;
+    for (int k = 0; k < w.K; k++) {
+        const int64_t step = w.step0 + k;
+        const bool init = step <= 0;
+        const float *vin = S + par * n;
+        float *vout = S + (par ^ 1) * n;
+        const float *Gpk = m.Gp + (size_t)k * m.n_chunk;
+        const int i = lane;
+        bool spike = false;
+        int src = -1;
+        if (i < n) {
+            const int t = t0 + i;
+            const float v = vin[i];
+            float Iin, Gin, Isyn, Gsyn;
+            block_currents(Gpk, m.t_blk0[t], m.t_blk0[t + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
+                           Gsyn);
+            const float uu = IZ(10, i);
+            const float vr = IZ(3, i);
+            const float imemb = ((IZ(2, i) * (v - vr)) * 1e-3f) * (v - IZ(4, i)) + (Isyn + Iin) - uu;
+            float vn, un;
+            if (init) {
+                vn = IZ(1, i);
+                un = 0.0f;
+            } else {
+                vn = v + dt * (imemb / IZ(0, i));
+                const float du = (IZ(6, i) * ((IZ(7, i) * (v - vr)) - uu)) * 1e-3f;
+                un = uu + dt * du * 1e3f;
+                if (v > IZ(5, i)) {
+                    vn = IZ(8, i);
+                    un = uu + IZ(9, i);
+                    spike = true;
+                }
+            }
+            vout[i] = vn;
+            IZ(10, i) = un;
+            src = m.t_src[t];
+        }
+        push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar);
+        if (!init) {
+            const int64_t row = (step - 1) % m.trace_cap;
+            for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = vin[m.gr_t[q]];
+        }
+        __syncwarp();
+        par ^= 1;
+    }
+    for (int i = lane; i < n; i += 32) {
+        m.v[par][t0 + i] = S[par * n + i];
+        m.iz_u[izh0 + i] = IZ(10, i);
+    }
+}
+#undef IZ
+
+// This launch runs CTAs [cta_begin, cta_end), each a few units, one per warp.
 __global__ void __launch_bounds__(kCellThreads) k_cells_t(DevModel m, const WindowArgs *tab, const int *base, int idx,
                                                           int cta_begin, int cta_end) {
     extern __shared__ float sm[];
     const WindowArgs w = tab[*base + idx];
-    const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     for (int cta = cta_begin + blockIdx.x; cta < cta_end; cta += gridDim.x) {
         const int u = m.cta_u0[cta] + warp;
         if (u >= m.cta_u0[cta + 1]) continue;
-        const int t0 = m.un_t0[u], n = m.un_t1[u] - t0, fi = m.un_f[u];
-        const int ngt = m.un_ngt[u], gt0 = m.un_gt0[u];
-        const int s0 = m.un_s0[u], ns = m.un_s1[u] - s0;
-        const int r0 = m.un_r0[u], r1 = m.un_r1[u];
-        const int nlev = fi >= 0 ? m.fo_nlev[fi] : 0;
-        const int l0 = fi >= 0 ? m.fo_l0[fi] : 0;
-        float *S = sm + m.un_off[u];
-        float *V[2] = {S, S + n};
-        float *D = S + 2 * n, *U = S + 3 * n, *L = S + 4 * n;
-        int32_t *CE = (int32_t *)(S + 5 * n), *P = CE + n;
-        float *FG = S + 7 * n, *FE = S + 8 * n, *FGC = S + 9 * n, *FD0 = S + 10 * n, *FA = S + 11 * n, *FC = S + 12 * n;
-        float *GT = S + 13 * n;
-        int32_t *GI_T = (int32_t *)(GT + ngt), *GI_TG = GI_T + ngt;
-        int32_t *LV = GI_TG + ngt;
-        int32_t *ST = LV + nlev + 1, *SSRC = ST + ns;
-        float *STHR = (float *)(SSRC + ns);
-        // izhikevich batches keep their parameters and u in the compartment slots
-        float *IZ[11] = {D, U, L, (float *)CE, (float *)P, FG, FE, FGC, FD0, FA, FC};
-        const int izh0 = fi < 0 ? m.t_izh[t0] : 0;
-        // ---- stage the unit
-        for (int i = lane; i < n; i += 32) {
-            const int t = t0 + i;
-            V[w.par][i] = m.v[w.par][t];
-            if (fi >= 0) {
-                U[i] = m.c_u[t]; L[i] = m.c_l[t];
-                CE[i] = m.c_cend[t] - t0; P[i] = m.c_parent[t] - t0;
-                FG[i] = m.flat_g[t]; FE[i] = m.flat_e[t]; FGC[i] = m.flat_gc[t]; FD0[i] = m.flat_d0[t];
-                FA[i] = m.c_area[t]; FC[i] = m.c_cm[t];
-            } else {
-                const int iz = izh0 + i;
-                IZ[0][i] = m.iz_C[iz]; IZ[1][i] = m.iz_v0[iz]; IZ[2][i] = m.iz_k[iz]; IZ[3][i] = m.iz_vr[iz];
-                IZ[4][i] = m.iz_vt[iz]; IZ[5][i] = m.iz_vpeak[iz]; IZ[6][i] = m.iz_a[iz]; IZ[7][i] = m.iz_b[iz];
-                IZ[8][i] = m.iz_c[iz]; IZ[9][i] = m.iz_d[iz]; IZ[10][i] = m.iz_u[iz];
-            }
-        }
-        for (int i = lane; i < ngt; i += 32) GT[i] = m.gate[gt0 + i];
-        if (fi >= 0) {
-            // gate update items: (target, gate number | channel type << 8)
-            for (int i = lane; i < n; i += 32) {
-                for (int ch = m.c_chan0[t0 + i]; ch < m.c_chan0[t0 + i + 1]; ch++) {
-                    const int q0 = m.ch_gate0[ch] - gt0, q1 = m.ch_gate0[ch + 1] - gt0;
-                    for (int q = q0; q < q1; q++) { GI_T[q] = i; GI_TG[q] = (q - q0) | (m.ch_type[ch] << 8); }
-                }
-            }
-            for (int i = lane; i <= nlev; i += 32) LV[i] = m.lvl[l0 + i] - t0;
-        }
-        for (int i = lane; i < ns; i += 32) { ST[i] = m.gs_t[s0 + i]; SSRC[i] = m.gs_src[s0 + i]; STHR[i] = m.gs_thr[s0 + i]; }
-        __syncwarp();
-        int par = w.par;
-        for (int k = 0; k < w.K; k++) {
-            const int64_t step = w.step0 + k;
-            const bool init = step <= 0;
-            const float *vin = V[par];
-            float *vout = V[par ^ 1];
-            const float *Gpk = m.Gp + (size_t)k * m.n_chunk;
-            const float dt = m.dt;
-            for (int i0 = 0; i0 < n; i0 += 32) {
-                const int i = i0 + lane;
-                bool spike = false;
-                int src = -1;
-                if (i < n) {
-                    const int t = t0 + i;
-                    const float v = vin[i];
-                    if (fi >= 0 && FG[i] >= 0.0f) {
-                        // one gateless channel, no inputs (eden/Eden.cpp:5805-5898, 6057-6107)
-                        const float I = (FG[i] * (FE[i] - v) * 1e-5f) * FA[i];
-                        D[i] = FD0[i];
-                        vout[i] = init ? v : v + (dt * ((I + 0.0f + 0.0f) + (v * FGC[i]))) / FC[i];
-                    } else {
-                        float Iin, Gin, Isyn, Gsyn;
-                        block_currents(Gpk, m.t_blk0[t], m.t_blk0[t + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin,
-                                       Gin, Isyn, Gsyn);
-                        if (fi >= 0) {
-                            // channels + voltage pre-update (eden/Eden.cpp:5013-6107)
-                            const float A = FA[i];
-                            float Ich = 0.f, Gch = 0.f;
-                            for (int ch = m.c_chan0[t]; ch < m.c_chan0[t + 1]; ch++) {
-                                const ChanTypeDev &ct = c_chan_types[m.ch_type[ch]];
-                                float fopen = 1.0f;
-                                const float *q = GT + (m.ch_gate0[ch] - gt0);
-                                for (int gi = 0; gi < ct.n_gates; gi++) {
-                                    const float qo = q[gi];
-                                    for (int rr = 0; rr < ct.inst[gi]; rr++) fopen = fopen * qo;
-                                }
-                                const float gs = m.ch_gbase[ch] * fopen;
-                                Ich += (gs * (m.ch_erev[ch] - v) * 1e-5f) * A;
-                                Gch += (gs * 1e-5f) * A;
-                            }
-                            const float I = Ich + Iin + Isyn;
-                            const float G = Gch + Gin + Gsyn;
-                            const float C = FC[i];
-                            D[i] = 1.0f * (G / C) + m.c_inv_rc[t];
-                            vout[i] = init ? v : v + (dt * (I + (v * G))) / C;
-                        } else {
-                            // izhikevich2007Cell (LEMS_CoreComponents.inc.xml:1140-1185)
-                            const float u = IZ[10][i];
-                            const float vr = IZ[3][i];
-                            const float imemb = ((IZ[2][i] * (v - vr)) * 1e-3f) * (v - IZ[4][i]) + (Isyn + Iin) - u;
-                            float vn, un;
-                            if (init) {
-                                vn = IZ[1][i];
-                                un = 0.0f;
-                            } else {
-                                vn = v + dt * (imemb / IZ[0][i]);
-                                const float du = (IZ[6][i] * ((IZ[7][i] * (v - vr)) - u)) * 1e-3f;
-                                un = u + dt * du * 1e3f;
-                                if (v > IZ[5][i]) {
-                                    vn = IZ[8][i];
-                                    un = u + IZ[9][i];
-                                    spike = true;
-                                }
-                            }
-                            vout[i] = vn;
-                            IZ[10][i] = un;
-                            src = m.t_src[t];
-                        }
-                    }
-                }
-                if (fi < 0) push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar);
-            }
-            if (!init) {
-                // trajectory samples of this step's starting state
-                const int64_t row = (step - 1) % m.trace_cap;
-                for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = vin[m.gr_t[q]];
-            }
-            __syncwarp();
-            if (fi >= 0) {
-                hines_forest(m, init, step, D, vout, U, L, CE, P, LV, nlev, vin, t0, w.wpar, false);
-                __syncwarp();
-                // gate updates from this step's V and gate values (the currents
-                // above used the values before the update, as the reference does)
-                for (int q = lane; q < ngt; q += 32) {
-                    const int tg = GI_TG[q];
-                    GT[q] = gate_next(c_chan_types[tg >> 8], tg & 0xff, init, dt, vin[GI_T[q]], GT[q]);
-                }
-                // threshold crossings of the unit's spike sources (eden/Eden.cpp:6247-6252)
-                for (int q0 = 0; q0 < ns; q0 += 32) {
-                    const int q = q0 + lane;
-                    bool spk = false;
-                    int src2 = -1;
-                    if (q < ns) {
-                        const int tl = ST[q];
-                        src2 = SSRC[q];
-                        spk = vin[tl] < STHR[q] && STHR[q] < vout[tl];
-                    }
-                    push_spike(m, spk, src2, (int32_t)(step + 1), w.wpar);
-                }
-                __syncwarp();
-            }
-            par ^= 1;
-        }
-        // ---- write the unit back
-        for (int i = lane; i < n; i += 32) {
-            m.v[par][t0 + i] = V[par][i];
-            if (fi < 0) m.iz_u[izh0 + i] = IZ[10][i];
-        }
-        for (int i = lane; i < ngt; i += 32) m.gate[gt0 + i] = GT[i];
+        if (m.un_f[u] >= 0) forest_window(m, w, u, sm + m.un_off[u]);
+        else izh_window(m, w, u, sm + m.un_off[u]);
     }
 }
 
@@ -827,6 +844,38 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         }
     }
 
+    // windowed-path constants (see DevModel::c_kc): a compartment is flat when
+    // it has one gateless channel and no inputs, is no spike source, and every
+    // compartment below it is flat; its pivot and elimination factor are then
+    // the same every step and are computed here once, deepest first
+    std::vector<char> nonflat(nt, 1);
+    std::vector<float> c_kc(nt, 0.f), c_pv0(nt, 0.f), c_rt0(nt, 0.f);
+    std::vector<uint32_t> c_cep(nt, 0);
+    {
+        std::vector<char> is_src(nt, 0);
+        for (int s = 0; s < m->n_src; s++) is_src[u2i[m->src_target[s]]] = 1;
+        for (size_t f = 0; f < fo_t0.size(); f++) {
+            const int a = fo_t0[f], b = fo_t1[f];
+            for (int it = b - 1; it >= a; it--) {
+                const int k0 = c_child0[it], k1 = c_child0[it] + c_nchild[it];
+                bool flat = flat_g[it] >= 0.0f && !is_src[it];
+                for (int c = k0; flat && c < k1; c++) flat = !nonflat[c];
+                nonflat[it] = flat ? 0 : 1;
+                if (flat) {
+                    c_kc[it] = (dt * (flat_gc[it] * flat_e[it])) / c_cm[it];
+                    float dj = 1.0f + flat_d0[it] * dt;
+                    for (int c = k0; c < k1; c++) dj -= c_rt0[c] * c_u[c];
+                    const float inv = 1.0f / dj;
+                    c_pv0[it] = inv;
+                    c_rt0[it] = c_l[it] * inv;
+                }
+                const uint32_t ce = (uint32_t)(c_cend[it] - a);
+                const uint32_t pp = c_parent[it] >= 0 ? (uint32_t)(c_parent[it] - a + 1) : 0u;
+                c_cep[it] = ce | (pp << kCepParentShift) | (nonflat[it] ? kCepNonFlat : 0u);
+            }
+        }
+    }
+
     // izhikevich structure of arrays, in slot (internal) order
     std::vector<float> iz[10];
     for (int f = 0; f < 10; f++) {
@@ -985,22 +1034,38 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     std::vector<int32_t> un_gt0(n_unit), un_ngt(n_unit), un_s0(n_unit), un_s1(n_unit), un_r0(n_unit), un_r1(n_unit);
     std::vector<int32_t> gs_t, gs_src, gr_t, gr_col;
     std::vector<float> gs_thr;
+    std::vector<int32_t> un_nf0(n_unit), un_nf1(n_unit), nf_t;
     std::vector<int> un_words(n_unit);
+    {
+        std::vector<int32_t> slot_of(nt, -1);
+        for (int u = 0; u < n_unit; u++) {
+            const int a = un_t0[u], b = un_t1[u];
+            un_nf0[u] = (int)nf_t.size();
+            if (un_f[u] >= 0)
+                for (int t = a; t < b; t++)
+                    if (nonflat[t]) { slot_of[t] = (int)nf_t.size() - un_nf0[u]; nf_t.push_back(t - a); }
+            un_nf1[u] = (int)nf_t.size();
+        }
+        for (int u = 0; u < n_unit; u++) {
+            const int a = un_t0[u], b = un_t1[u];
+            un_s0[u] = (int)gs_t.size();
+            if (un_f[u] >= 0)
+                for (int t = a; t < b; t++)
+                    if (t_src[t] >= 0) { gs_t.push_back(slot_of[t]); gs_src.push_back(t_src[t]); gs_thr.push_back(src_thr[t_src[t]]); }
+            un_s1[u] = (int)gs_t.size();
+        }
+    }
     for (int u = 0; u < n_unit; u++) {
         const int a = un_t0[u], b = un_t1[u];
-        un_s0[u] = (int)gs_t.size();
-        if (un_f[u] >= 0)
-            for (int t = a; t < b; t++)
-                if (t_src[t] >= 0) { gs_t.push_back(t - a); gs_src.push_back(t_src[t]); gs_thr.push_back(src_thr[t_src[t]]); }
-        un_s1[u] = (int)gs_t.size();
         un_r0[u] = (int)gr_t.size();
         for (int t = a; t < b; t++)
             for (int k = t_trace0[t]; k < t_trace0[t + 1]; k++) { gr_t.push_back(t - a); gr_col.push_back(trace_col[k]); }
         un_r1[u] = (int)gr_t.size();
         un_gt0[u] = ch_gate0[c_chan0[a]];
         un_ngt[u] = ch_gate0[c_chan0[b]] - un_gt0[u];
-        const int nlev = un_f[u] >= 0 ? fo_nlev[un_f[u]] : 0;
-        un_words[u] = unit_words(b - a, un_ngt[u], nlev, un_s1[u] - un_s0[u]);
+        un_words[u] = un_f[u] >= 0 ? forest_words(b - a, un_nf1[u] - un_nf0[u], un_ngt[u], fo_nlev[un_f[u]],
+                                                  un_s1[u] - un_s0[u])
+                                   : izh_words(b - a);
     }
     // CTAs of up to four units, packed longest-first onto the CTA with the
     // fewest words so that every CTA needs about the same shared memory
@@ -1041,7 +1106,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (size_t j = 0; j < unit_of_slot.size(); j++) o[j] = v[unit_of_slot[j]];
         v.swap(o);
     };
-    for (auto *v : {&un_t0, &un_t1, &un_f, &un_gt0, &un_ngt, &un_s0, &un_s1, &un_r0, &un_r1}) perm(*v);
+    for (auto *v : {&un_t0, &un_t1, &un_f, &un_gt0, &un_ngt, &un_s0, &un_s1, &un_r0, &un_r1, &un_nf0, &un_nf1}) perm(*v);
     {
         std::vector<int> w2(n_unit);
         for (int j = 0; j < n_unit; j++) w2[j] = un_words[unit_of_slot[j]];
@@ -1075,8 +1140,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.c_cm, c_cm)); TRY(upload_c(ctx, &d.c_inv_rc, c_inv)); TRY(upload_c(ctx, &d.c_area, c_area));
     TRY(upload_c(ctx, &d.c_u, c_u)); TRY(upload_c(ctx, &d.c_l, c_l));
     TRY(upload_c(ctx, &d.c_cend, c_cend)); TRY(upload_c(ctx, &d.c_parent, c_parent));
-    TRY(upload_c(ctx, &d.flat_g, flat_g)); TRY(upload_c(ctx, &d.flat_e, flat_e));
-    TRY(upload_c(ctx, &d.flat_gc, flat_gc)); TRY(upload_c(ctx, &d.flat_d0, flat_d0)); TRY(upload_c(ctx, &d.t_izh, t_izh));
+    TRY(upload_c(ctx, &d.c_kc, c_kc)); TRY(upload_c(ctx, &d.c_pv0, c_pv0));
+    TRY(upload_c(ctx, &d.c_rt0, c_rt0)); TRY(upload_c(ctx, &d.c_cep, c_cep)); TRY(upload_c(ctx, &d.t_izh, t_izh));
     TRY(upload_c(ctx, &d.fo_t0, fo_t0)); TRY(upload_c(ctx, &d.fo_t1, fo_t1)); TRY(upload_c(ctx, &d.fo_l0, fo_l0));
     TRY(upload_c(ctx, &d.fo_nlev, fo_nlev)); TRY(upload_c(ctx, &d.lvl, lvl));
     TRY(upload_c(ctx, &d.in_tgt, in_tgt));
@@ -1129,6 +1194,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.un_r0, un_r0)); TRY(upload_c(ctx, &d.un_r1, un_r1)); TRY(upload_c(ctx, &d.cta_u0, cta_u0));
     TRY(upload_c(ctx, &d.gs_t, gs_t)); TRY(upload_c(ctx, &d.gs_src, gs_src)); TRY(upload_c(ctx, &d.gs_thr, gs_thr));
     TRY(upload_c(ctx, &d.gr_t, gr_t)); TRY(upload_c(ctx, &d.gr_col, gr_col));
+    TRY(upload_c(ctx, &d.un_nf0, un_nf0)); TRY(upload_c(ctx, &d.un_nf1, un_nf1)); TRY(upload_c(ctx, &d.nf_t, nf_t));
     TRY(upload(ctx, &d.status, (const int32_t *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_base, (const int *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_zero, (const int *)nullptr, 1));

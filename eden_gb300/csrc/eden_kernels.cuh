@@ -77,11 +77,18 @@ struct DevModel {
     const float *c_cm, *c_inv_rc, *c_area, *c_u, *c_l;  // U = -dt/(R C_i), L = -dt/(R C_parent)
     const int32_t *c_cend, *c_parent;  // end of each node's child range; parent (internal, -1 at roots)
     const int32_t *t_izh;                            // izhikevich index or -1
-    // flat per-target parameters of the common compartment: one channel
-    // without gates and no inputs.  flat_g < 0 marks every other target.
-    // Its diagonal flat_d0 = G/C + inv_rc and conductance flat_gc = (g*1e-5)*A
-    // are step-invariant and precomputed with the same float operations.
-    const float *flat_g, *flat_e, *flat_gc, *flat_d0;
+    // windowed-path constants of each physical compartment.  A "flat"
+    // compartment has one gateless channel, no inputs, is no spike source and
+    // has only flat compartments below it; everything else is "non-flat".
+    //   c_kc   flat: the pre-update increment dt*(G*E)/C (V' = V + c_kc, the
+    //          reference's V + dt*(I + V*G)/C with I = G*(E - V)); non-flat: 0
+    //   c_pv0  flat: reciprocal of its Hines pivot, which is the same every
+    //          step because nothing below it changes; non-flat: unused
+    //   c_rt0  flat: L / pivot, its elimination factor into its parent
+    //   c_cep  child-range end | (parent + 1) << 10 | non-flat << 20, all
+    //          local to the compartment's forest
+    const float *c_kc, *c_pv0, *c_rt0;
+    const uint32_t *c_cep;
     // forests: physical compartments [fo_t0, fo_t1), depth boundaries lvl[fo_l0 .. fo_l0 + fo_nlev]
     const int32_t *fo_t0, *fo_t1, *fo_l0, *fo_nlev, *lvl;
     // channels
@@ -148,17 +155,26 @@ struct DevModel {
     const int32_t *cta_u0;
     const int32_t *gs_t, *gs_src, *gr_t, *gr_col;
     const float *gs_thr;
+    // non-flat compartments of forest units: nf_t[un_nf0[u] .. un_nf1[u]) are
+    // unit-local indices; spike sources (gs_t) and gates refer to these slots
+    const int32_t *un_nf0, *un_nf1, *nf_t;
     int32_t *status;
 };
 
-// Shared-memory words of a unit's slice in the windowed kernel: 13 per
-// target (V twice, D, U, L, child-range end, parent and the flat
-// parameters; an izhikevich batch keeps its 10 parameters and u in the same
-// slots), 3 per gate (value and update item), the forest's depth boundaries
-// and 3 per spike source.
-__host__ __device__ inline int unit_words(int n, int ngt, int nlev, int ns) {
-    return 13 * n + 3 * ngt + (nlev + 1) + 3 * ns;
+constexpr uint32_t kCepMask = 0x3ffu;
+constexpr int kCepParentShift = 10;
+constexpr uint32_t kCepNonFlat = 1u << 20;
+
+// Shared-memory words of a unit's slice in the windowed kernel.  A forest:
+// 7 per compartment (V, c_kc, L, pivot, elimination factor, U, packed
+// child-end/parent/flag), 5 per non-flat compartment (local index, V at the
+// step start, area, C, sum of 1/(R C)), 3 per gate (value and update item),
+// the depth boundaries and 3 per spike source.  A batch of izhikevich
+// neurons: V twice and 11 parameter / state words per neuron.
+__host__ __device__ inline int forest_words(int n, int nf, int ngt, int nlev, int ns) {
+    return 7 * n + 5 * nf + 3 * ngt + (nlev + 1) + 3 * ns;
 }
+__host__ __device__ inline int izh_words(int n) { return 13 * n + 1; }
 
 // Per-window arguments: the window covers steps [step0, step0 + K); steps
 // <= 0 are initialisation passes.  The previous window began at step
@@ -544,6 +560,57 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
             }
         }
         push_spike(m, spk, src, (int32_t)(step + 1), wpar);
+    }
+}
+
+// Backward-Euler Hines solve of one forest by one warp for the windowed path,
+// on the unit's shared-memory slice (eden/Eden.cpp:6114-6225).  Flat
+// compartments keep the reciprocal pivot PV and the elimination factor RT
+// = L / pivot computed once, because their diagonals never change; a
+// non-flat compartment's pivot is rebuilt every step from its diagonal
+// (PV holds G/C + sum 1/(RC) on entry) and its children's factors, in
+// increasing child order as the reference's post-order visits them.  Depths
+// hold at most 32 compartments, one per lane.  Back-substitution runs
+// root-first.  X holds the pre-updated V on entry and V_next on return.
+__device__ __forceinline__ void hines_window(float dt, float *X, const float *L, float *PV, float *RT,
+                                             const float *U, const uint32_t *CEP, const int32_t *LV, int nlev) {
+    const int lane = threadIdx.x & 31;
+    for (int lev = nlev - 1; lev >= 0; lev--) {
+        const int j0 = LV[lev], j1 = LV[lev + 1];
+        const int j = j0 + lane;
+        if (j < j1) {
+            const uint32_t cep = CEP[j];
+            const int ke = (int)(cep & kCepMask);
+            const int kb = lane == 0 ? j1 : (int)(CEP[j - 1] & kCepMask);
+            if (cep & kCepNonFlat) {
+                float dj = 1.0f + PV[j] * dt;
+                float xj = X[j];
+                for (int i = kb; i < ke; i++) {
+                    const float r = RT[i];
+                    dj -= r * U[i];
+                    xj -= r * X[i];
+                }
+                const float inv = __fdividef(1.0f, dj);
+                PV[j] = inv;
+                RT[j] = L[j] * inv;
+                X[j] = xj;
+            } else if (ke > kb) {
+                float xj = X[j];
+                for (int i = kb; i < ke; i++) xj -= RT[i] * X[i];
+                X[j] = xj;
+            }
+        }
+        __syncwarp();
+    }
+    for (int r = LV[0] + lane; r < LV[1]; r += 32) X[r] = X[r] * PV[r];
+    __syncwarp();
+    for (int lev = 1; lev < nlev; lev++) {
+        const int i = LV[lev] + lane;
+        if (i < LV[lev + 1]) {
+            const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
+            X[i] = (X[i] - U[i] * X[p]) * PV[i];
+        }
+        __syncwarp();
     }
 }
 
