@@ -231,12 +231,15 @@ __global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs 
 // already produced them for all K steps.  Everything else a step reads is
 // staged in the warp's shared-memory slice for the whole window.
 
-// A forest unit over the window.  Per step: trajectory samples of the step's
-// starting V; the flat compartments' pre-update V += c_kc (the same value
-// for every step, because their currents are linear in V with constant
-// conductance); the non-flat compartments' currents (inputs, channels with
-// the gate values before this step's update), diagonal and pre-update; the
-// cable solve; gate updates from the starting V; threshold crossings.
+// A forest unit over the window.  At the window start the unit stages its
+// compartments, its non-flat compartments' descriptors, its gates with their
+// parameter records, and the conductance series of its input chunks for all
+// K steps (written by k_inputs_t), so that a step reads shared memory only.
+// Per step: trajectory samples of the step's starting V; the non-flat
+// compartments' currents (inputs, channels with the gate values before this
+// step's update), diagonal and pre-update; the cable solve, which also
+// applies the flat compartments' constant pre-update; gate updates from the
+// starting V; threshold crossings.
 __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArgs &w, int u, float *S) {
     const int lane = threadIdx.x & 31;
     const int t0 = m.un_t0[u], n = m.un_t1[u] - t0, fi = m.un_f[u];
@@ -245,15 +248,23 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     const int r0 = m.un_r0[u], r1 = m.un_r1[u];
     const int nf0 = m.un_nf0[u], nf = m.un_nf1[u] - nf0;
     const int nlev = m.fo_nlev[fi], l0 = m.fo_l0[fi];
+    const int ub0 = m.t_blk0[t0], nblk = m.t_blk0[t0 + n] - ub0;
+    const int uc0 = m.bk_c0[ub0], nck = m.bk_c0[ub0 + nblk] - uc0;
     float *X = S, *KC = S + n, *L = S + 2 * n, *PV = S + 3 * n, *RT = S + 4 * n, *U = S + 5 * n;
     uint32_t *CEP = (uint32_t *)(S + 6 * n);
     int32_t *NT = (int32_t *)(S + 7 * n);
     float *VO = (float *)(NT + nf), *NA = VO + nf, *NC = NA + nf, *NIR = NC + nf;
-    float *GT = NIR + nf;
-    int32_t *GI_S = (int32_t *)(GT + ngt), *GI_TG = GI_S + ngt;
-    int32_t *LV = GI_TG + ngt;
+    int32_t *NB0 = (int32_t *)(NIR + nf), *NB1 = NB0 + nf, *NCH0 = NB1 + nf, *NCH1 = NCH0 + nf;
+    float *GT = (float *)(NCH1 + nf);
+    int32_t *GI_S = (int32_t *)(GT + ngt);
+    float *GP = (float *)(GI_S + ngt);
+    int32_t *LV = (int32_t *)(GP + kGateWords * ngt);
     int32_t *ST = LV + nlev + 1, *SSRC = ST + ns;
     float *STHR = (float *)(SSRC + ns);
+    int32_t *BKK = (int32_t *)(STHR + ns);
+    float *BKE = (float *)(BKK + nblk);
+    int32_t *BKC = (int32_t *)(BKE + nblk);
+    float *GS = (float *)(BKC + nblk + 1);
     // ---- stage the unit
     const float *vsrc = m.v[w.par];
     for (int i = lane; i < n; i += 32) {
@@ -264,41 +275,50 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     for (int j = lane; j < nf; j += 32) {
         const int ti = m.nf_t[nf0 + j], t = t0 + ti;
         NT[j] = ti; NA[j] = m.c_area[t]; NC[j] = m.c_cm[t]; NIR[j] = m.c_inv_rc[t];
-        // gate update items: (non-flat slot, gate number | channel type << 8)
-        for (int ch = m.c_chan0[t]; ch < m.c_chan0[t + 1]; ch++) {
+        NB0[j] = m.t_blk0[t] - ub0; NB1[j] = m.t_blk0[t + 1] - ub0;
+        const int ch0 = m.c_chan0[t], ch1 = m.c_chan0[t + 1];
+        NCH0[j] = ch0; NCH1[j] = ch1;
+        // gate update items: the non-flat slot and the gate's parameter record
+        for (int ch = ch0; ch < ch1; ch++) {
             const int q0 = m.ch_gate0[ch] - gt0, q1 = m.ch_gate0[ch + 1] - gt0;
-            for (int q = q0; q < q1; q++) { GI_S[q] = j; GI_TG[q] = (q - q0) | (m.ch_type[ch] << 8); }
+            const float *src = m.gate_par + (size_t)m.ch_type[ch] * EDEN_MAX_GATES * kGateWords;
+            for (int q = q0; q < q1; q++) {
+                GI_S[q] = j;
+                for (int k = 0; k < kGateWords; k++) GP[q * kGateWords + k] = src[(q - q0) * kGateWords + k];
+            }
         }
     }
     for (int i = lane; i < ngt; i += 32) GT[i] = m.gate[gt0 + i];
-    for (int i = lane; i <= nlev; i += 32) LV[i] = m.lvl[l0 + i] - t0;
+    for (int i = lane; i <= nlev; i += 32) LV[i] = (m.lvl[l0 + i] - t0) | (m.lvl_nf[l0 + i] ? kLvNonFlat : 0);
     for (int i = lane; i < ns; i += 32) { ST[i] = m.gs_t[s0 + i]; SSRC[i] = m.gs_src[s0 + i]; STHR[i] = m.gs_thr[s0 + i]; }
+    for (int b = lane; b <= nblk; b += 32) {
+        BKC[b] = m.bk_c0[ub0 + b] - uc0;
+        if (b < nblk) { BKK[b] = m.bk_kind[ub0 + b]; BKE[b] = m.bk_erev[ub0 + b]; }
+    }
+    for (int k = 0; k < w.K; k++)
+        for (int c = lane; c < nck; c += 32) GS[k * nck + c] = m.Gp[(size_t)k * m.n_chunk + uc0 + c];
     __syncwarp();
     const float dt = m.dt;
     for (int k = 0; k < w.K; k++) {
         const int64_t step = w.step0 + k;
         const bool init = step <= 0;
-        const float *Gpk = m.Gp + (size_t)k * m.n_chunk;
         if (!init) {
             // trajectory samples of this step's starting state
             const int64_t row = (step - 1) % m.trace_cap;
             for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = X[m.gr_t[q]];
-            __syncwarp();
-            // flat compartments (c_kc is 0 for the others, which the next loop sets)
-            for (int i = lane; i < n; i += 32) X[i] = X[i] + KC[i];
         }
         __syncwarp();
+        const float *Gk = GS + k * nck;
         for (int j = lane; j < nf; j += 32) {
             // channels + voltage pre-update (eden/Eden.cpp:5013-6107)
-            const int ti = NT[j], t = t0 + ti;
+            const int ti = NT[j];
             const float v = X[ti];
             VO[j] = v;
             float Iin, Gin, Isyn, Gsyn;
-            block_currents(Gpk, m.t_blk0[t], m.t_blk0[t + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
-                           Gsyn);
+            block_currents(Gk, NB0[j], NB1[j], BKK, BKE, BKC, 0, v, Iin, Gin, Isyn, Gsyn);
             const float A = NA[j];
             float Ich = 0.f, Gch = 0.f;
-            for (int ch = m.c_chan0[t]; ch < m.c_chan0[t + 1]; ch++) {
+            for (int ch = NCH0[j]; ch < NCH1[j]; ch++) {
                 const ChanTypeDev &ct = c_chan_types[m.ch_type[ch]];
                 float fopen = 1.0f;
                 const float *q = GT + (m.ch_gate0[ch] - gt0);
@@ -317,13 +337,11 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             X[ti] = init ? v : v + (dt * (I + (v * G))) / C;
         }
         __syncwarp();
-        if (!init) hines_window(dt, X, L, PV, RT, U, CEP, LV, nlev);
+        if (!init) hines_window(dt, X, KC, L, PV, RT, U, CEP, LV, nlev);
         // gate updates from this step's starting V and gate values (the
         // currents above used the values before the update, as the reference does)
-        for (int q = lane; q < ngt; q += 32) {
-            const int tg = GI_TG[q];
-            GT[q] = gate_next(c_chan_types[tg >> 8], tg & 0xff, init, dt, VO[GI_S[q]], GT[q]);
-        }
+        for (int q = lane; q < ngt; q += 32)
+            GT[q] = gate_next_p(GP + q * kGateWords, init, dt, VO[GI_S[q]], GT[q]);
         // threshold crossings of the unit's spike sources (eden/Eden.cpp:6247-6252)
         for (int q0 = 0; q0 < ns; q0 += 32) {
             const int q = q0 + lane;
@@ -415,7 +433,7 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
 #undef IZ
 
 // This launch runs CTAs [cta_begin, cta_end), each a few units, one per warp.
-__global__ void __launch_bounds__(kCellThreads) k_cells_t(DevModel m, const WindowArgs *tab, const int *base, int idx,
+__global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const WindowArgs *tab, const int *base, int idx,
                                                           int cta_begin, int cta_end) {
     extern __shared__ float sm[];
     const WindowArgs w = tab[*base + idx];
@@ -876,6 +894,25 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         }
     }
 
+    // depths of each forest that hold a non-flat compartment (parallel to lvl)
+    std::vector<uint8_t> lvl_nf(lvl.size(), 0);
+    for (size_t f = 0; f < fo_t0.size(); f++)
+        for (int l = 0; l < fo_nlev[f]; l++)
+            for (int it = lvl[fo_l0[f] + l]; it < lvl[fo_l0[f] + l + 1]; it++)
+                if (nonflat[it]) lvl_nf[fo_l0[f] + l] = 1;
+    // gate parameter records per channel type and gate (gate_next_p)
+    std::vector<float> gate_par((size_t)std::max(m->n_chan_types, 1) * EDEN_MAX_GATES * kGateWords, 0.f);
+    for (int k = 0; k < m->n_chan_types; k++) {
+        const EdenGpuChannelType &ty = m->chan_types[k];
+        for (int g = 0; g < ty.n_gates; g++) {
+            float *r = &gate_par[((size_t)k * EDEN_MAX_GATES + g) * kGateWords];
+            int32_t fk = ty.fwd_kind[g], rk = ty.rev_kind[g];
+            memcpy(&r[0], &fk, 4); r[1] = ty.fwd_rate[g]; r[2] = ty.fwd_mid[g]; r[3] = ty.fwd_scale[g];
+            memcpy(&r[4], &rk, 4); r[5] = ty.rev_rate[g]; r[6] = ty.rev_mid[g]; r[7] = ty.rev_scale[g];
+            r[8] = ty.q10[g];
+        }
+    }
+
     // izhikevich structure of arrays, in slot (internal) order
     std::vector<float> iz[10];
     for (int f = 0; f < 10; f++) {
@@ -985,15 +1022,15 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     }
     t_blk0[nt] = (int32_t)bk_kind.size();
     const int n_block = (int)bk_kind.size();
-    // chunks of at most 32 items per block
+    // chunks of at most kChunkItems items per block
     std::vector<int32_t> bk_c0(n_block + 1, 0), ck_blk, ck_n;
     std::vector<int64_t> ck_i0;
     for (int b = 0; b < n_block; b++) {
         bk_c0[b] = (int32_t)ck_blk.size();
-        for (int64_t i = bk_i0[b]; i < bk_i1[b]; i += 32) {
+        for (int64_t i = bk_i0[b]; i < bk_i1[b]; i += kChunkItems) {
             ck_blk.push_back(b);
             ck_i0.push_back(i);
-            ck_n.push_back((int32_t)std::min<int64_t>(32, bk_i1[b] - i));
+            ck_n.push_back((int32_t)std::min<int64_t>(kChunkItems, bk_i1[b] - i));
         }
     }
     bk_c0[n_block] = (int32_t)ck_blk.size();
@@ -1063,9 +1100,14 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         un_r1[u] = (int)gr_t.size();
         un_gt0[u] = ch_gate0[c_chan0[a]];
         un_ngt[u] = ch_gate0[c_chan0[b]] - un_gt0[u];
-        un_words[u] = un_f[u] >= 0 ? forest_words(b - a, un_nf1[u] - un_nf0[u], un_ngt[u], fo_nlev[un_f[u]],
-                                                  un_s1[u] - un_s0[u])
-                                   : izh_words(b - a);
+        if (un_f[u] >= 0) {
+            const int nblk = t_blk0[b] - t_blk0[a];
+            const int nck = bk_c0[t_blk0[b]] - bk_c0[t_blk0[a]];
+            un_words[u] = forest_words(b - a, un_nf1[u] - un_nf0[u], un_ngt[u], fo_nlev[un_f[u]], un_s1[u] - un_s0[u],
+                                       nblk, nck, std::max(ctx->K, 4));
+        } else {
+            un_words[u] = izh_words(b - a);
+        }
     }
     // CTAs of up to four units, packed longest-first onto the CTA with the
     // fewest words so that every CTA needs about the same shared memory
@@ -1195,6 +1237,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.gs_t, gs_t)); TRY(upload_c(ctx, &d.gs_src, gs_src)); TRY(upload_c(ctx, &d.gs_thr, gs_thr));
     TRY(upload_c(ctx, &d.gr_t, gr_t)); TRY(upload_c(ctx, &d.gr_col, gr_col));
     TRY(upload_c(ctx, &d.un_nf0, un_nf0)); TRY(upload_c(ctx, &d.un_nf1, un_nf1)); TRY(upload_c(ctx, &d.nf_t, nf_t));
+    TRY(upload_c(ctx, &d.lvl_nf, lvl_nf)); TRY(upload_c(ctx, &d.gate_par, gate_par));
     TRY(upload(ctx, &d.status, (const int32_t *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_base, (const int *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_zero, (const int *)nullptr, 1));

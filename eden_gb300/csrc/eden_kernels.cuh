@@ -66,6 +66,7 @@ __constant__ SynTypeDev c_syn_types[kMaxSynTypes];
 enum : int { ST_OK = 0, ST_LOG_OVERFLOW = 1 };
 enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2 };
 constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
+constexpr int kChunkItems = 128; // input items per chunk (one warp, up to four per lane)
 
 struct DevModel {
     int32_t n_target, n_src, n_group, n_forest, n_in;
@@ -107,7 +108,7 @@ struct DevModel {
     const uint8_t *bk_type;           // synapse type of a Poisson / synapse block
     const float *bk_erev;
     const int32_t *in_tgt;            // targets with any block
-    // blocks are cut into chunks of at most 32 items, one warp each; step k's
+    // blocks are cut into chunks of at most kChunkItems items, one warp each; step k's
     // partial sum of chunk c is Gp[k * n_chunk + c] and a block's value is the
     // sum of its chunks' partials in chunk order
     int32_t n_chunk;
@@ -158,21 +159,29 @@ struct DevModel {
     // non-flat compartments of forest units: nf_t[un_nf0[u] .. un_nf1[u]) are
     // unit-local indices; spike sources (gs_t) and gates refer to these slots
     const int32_t *un_nf0, *un_nf1, *nf_t;
+    // per forest depth boundary (parallel to lvl): the depth holds a non-flat compartment
+    const uint8_t *lvl_nf;
+    // per channel type and gate, the 9-word gate parameter record (gate_next_p)
+    const float *gate_par;
     int32_t *status;
 };
 
 constexpr uint32_t kCepMask = 0x3ffu;
 constexpr int kCepParentShift = 10;
 constexpr uint32_t kCepNonFlat = 1u << 20;
+constexpr int kGateWords = 9;  // gate parameter record (gate_next_p)
 
 // Shared-memory words of a unit's slice in the windowed kernel.  A forest:
 // 7 per compartment (V, c_kc, L, pivot, elimination factor, U, packed
-// child-end/parent/flag), 5 per non-flat compartment (local index, V at the
-// step start, area, C, sum of 1/(R C)), 3 per gate (value and update item),
-// the depth boundaries and 3 per spike source.  A batch of izhikevich
-// neurons: V twice and 11 parameter / state words per neuron.
-__host__ __device__ inline int forest_words(int n, int nf, int ngt, int nlev, int ns) {
-    return 7 * n + 5 * nf + 3 * ngt + (nlev + 1) + 3 * ns;
+// child-end/parent/flag), 9 per non-flat compartment (local index, V at the
+// step start, area, C, sum of 1/(R C), input-block range, channel range),
+// 11 per gate (value, non-flat slot, parameter record), the depth
+// boundaries, 3 per spike source, 3 per input block (kind, reversal
+// potential, chunk start) plus one, and the window's conductance series of
+// the unit's input chunks (kcap steps).  A batch of izhikevich neurons: V
+// twice and 11 parameter / state words per neuron.
+__host__ __device__ inline int forest_words(int n, int nf, int ngt, int nlev, int ns, int nblk, int nck, int kcap) {
+    return 7 * n + 9 * nf + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck;
 }
 __host__ __device__ inline int izh_words(int n) { return 13 * n + 1; }
 
@@ -280,10 +289,16 @@ __device__ __forceinline__ bool replay_mask(uint32_t mask, const WindowArgs &w, 
 // lane's partial sum for each step of the window.
 constexpr int kAccStride = 33;
 
-// Poisson input `it` over the K steps of a window; row[j] = its step-j term.
+// Row update of the accumulation tile: the lane's first item of a chunk
+// writes its term, later items add theirs.
+__device__ __forceinline__ void row_put(float *row, int j, float term, bool acc) {
+    row[j] = acc ? row[j] + term : term;
+}
+
+// Poisson input `it` over the K steps of a window; adds its step-j term to row[j].
 template <int KIND>
 __device__ __forceinline__ void pois_steps(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
-                                           float *row) {
+                                           float *row, bool acc) {
     const float dt = m.dt;
     float ts = m.po_ts[it], isi = m.po_isi[it], a = m.po_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.po_b[it] : 0.0f;
     const float wt = m.po_w[it];
@@ -292,7 +307,7 @@ __device__ __forceinline__ void pois_steps(const DevModel &m, int64_t it, const 
             ts = 0.0f;
             isi = (-(1.0f / m.po_rate[it])) *
                   logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], w.step0 + j, 0));
-            row[j] = synapse_dyn_k<KIND>(st, true, dt, false, wt, a, b);
+            row_put(row, j, synapse_dyn_k<KIND>(st, true, dt, false, wt, a, b), acc);
         }
     } else {
         for (int j = 0; j < w.K; j++) {
@@ -304,88 +319,87 @@ __device__ __forceinline__ void pois_steps(const DevModel &m, int64_t it, const 
             } else {
                 ts = ts + dt * 1.0f;
             }
-            row[j] = synapse_dyn_k<KIND>(st, false, dt, fired, wt, a, b);
+            row_put(row, j, synapse_dyn_k<KIND>(st, false, dt, fired, wt, a, b), acc);
         }
     }
     m.po_ts[it] = ts; m.po_isi[it] = isi; m.po_a[it] = a;
     if (KIND == EDEN_SYN_EXPTWO) m.po_b[it] = b;
 }
 
-// One chunk (at most 32 items of one input block) over the K steps of a
-// window, one item per lane with its state in registers.  Lane l writes its
-// item's step-j term to row l of the warp's tile; lane j then sums column j
-// over the chunk's rows in a fixed order into Gp[j][chunk].  Terms are g*w
-// (the conductance before the step's update, as the reference exposes it)
-// for Poisson inputs and synapses, and the current for pulses.
+// Connection synapse `it` over the K steps of a window: replay the previous
+// window's triggers, then each step fires the pending spike when it falls
+// due (eden/Eden.cpp:3646-3686); adds its step-j term to row[j].
+template <int KIND>
+__device__ __forceinline__ void synapse_steps(const DevModel &m, int64_t it, const WindowArgs &w,
+                                              const SynTypeDev &st, const float *tk, float *row, bool acc) {
+    const float dt = m.dt;
+    const bool init = w.step0 <= 0;
+    float pend = m.sy_pend[it], a = m.sy_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.sy_b[it] : 0.0f;
+    const float wt = m.sy_w[it];
+    const float pend0 = pend;
+    bool trig = false;
+    if (!init) {
+        const uint32_t mask = m.sy_mask[it];
+        if (mask) {
+            m.sy_mask[it] = 0;
+            trig = replay_mask(mask, w, dt, m.sy_delay[it], pend);
+        }
+    }
+    for (int j = 0; j < w.K; j++) {
+        const float t = tk[j];
+        bool fire = false;
+        if (!init) {
+            // the pending spike falls due before a trigger of this step may replace it
+            fire = (t <= pend && pend < t + dt);
+            if (j == 0 && trig && trigger_arrival(t, dt, m.sy_delay[it], pend)) fire = true;
+        }
+        row_put(row, j, synapse_dyn_k<KIND>(st, init, dt, fire, wt, a, b), acc);
+    }
+    if (pend != pend0) m.sy_pend[it] = pend;
+    m.sy_a[it] = a;
+    if (KIND == EDEN_SYN_EXPTWO) m.sy_b[it] = b;
+}
+
+// One chunk (at most kChunkItems items of one input block) over the K steps
+// of a window.  Lane l handles items l, l + 32, ... with their state in
+// registers and accumulates their step-j terms in row l of the warp's tile;
+// lane j then sums column j over the rows in a fixed order into
+// Gp[j][chunk].  Terms are g*w (the conductance before the step's update, as
+// the reference exposes it) for Poisson inputs and synapses, and the current
+// for pulses.
 __device__ __forceinline__ void chunk_window(const DevModel &m, int c, const WindowArgs &w, float *tile,
                                              const float *tk) {
     const int lane = threadIdx.x & 31;
     const int bk = m.ck_blk[c];
     const int kind = m.bk_kind[bk];
     const int n = m.ck_n[c];
-    const int64_t it = m.ck_i0[c] + lane;
     float *row = tile + lane * kAccStride;
-    const float dt = m.dt;
-    const bool init = w.step0 <= 0;
-    if (lane < n) {
+    for (int r = 0; lane + 32 * r < n; r++) {
+        const int64_t it = m.ck_i0[c] + lane + 32 * r;
+        const bool acc = r > 0;
         if (kind == BK_PULSE) {
             const float st = m.pu_start[it], du = m.pu_dur[it], aw = m.pu_amp[it] * m.pu_w[it];
             for (int j = 0; j < w.K; j++) {
                 const float tf = tk[j];
-                row[j] = (st <= tf && tf <= st + du) ? aw : 0.0f;
+                row_put(row, j, (st <= tf && tf <= st + du) ? aw : 0.0f, acc);
             }
         } else if (kind == BK_POIS) {
             // poissonFiringSynapse (LEMS_CoreComponents.inc.xml:623-672): the
             // spiker fires its own synapse instance on the step its OnCondition holds
             const SynTypeDev st = c_syn_types[m.bk_type[bk]];
-            if (st.kind == EDEN_SYN_EXPTWO) pois_steps<EDEN_SYN_EXPTWO>(m, it, w, st, row);
-            else pois_steps<EDEN_SYN_EXPONE>(m, it, w, st, row);
+            if (st.kind == EDEN_SYN_EXPTWO) pois_steps<EDEN_SYN_EXPTWO>(m, it, w, st, row, acc);
+            else pois_steps<EDEN_SYN_EXPONE>(m, it, w, st, row, acc);
         } else {
-            // connection synapse: replay the previous window's triggers, then each
-            // step fires the pending spike when it falls due (eden/Eden.cpp:3646-3686)
             const SynTypeDev st = c_syn_types[m.bk_type[bk]];
-            float pend = m.sy_pend[it], a = m.sy_a[it], b = st.kind == EDEN_SYN_EXPTWO ? m.sy_b[it] : 0.0f;
-            const float wt = m.sy_w[it];
-            const float pend0 = pend;
-            bool trig = false;
-            if (!init) {
-                const uint32_t mask = m.sy_mask[it];
-                if (mask) {
-                    m.sy_mask[it] = 0;
-                    trig = replay_mask(mask, w, dt, m.sy_delay[it], pend);
-                }
-            }
-            if (st.kind == EDEN_SYN_EXPTWO) {
-                for (int j = 0; j < w.K; j++) {
-                    const float t = tk[j];
-                    bool fire = false;
-                    if (!init) {
-                        // the pending spike falls due before a trigger of this step may replace it
-                        fire = (t <= pend && pend < t + dt);
-                        if (j == 0 && trig && trigger_arrival(t, dt, m.sy_delay[it], pend)) fire = true;
-                    }
-                    row[j] = synapse_dyn_k<EDEN_SYN_EXPTWO>(st, init, dt, fire, wt, a, b);
-                }
-                m.sy_b[it] = b;
-            } else {
-                for (int j = 0; j < w.K; j++) {
-                    const float t = tk[j];
-                    bool fire = false;
-                    if (!init) {
-                        fire = (t <= pend && pend < t + dt);
-                        if (j == 0 && trig && trigger_arrival(t, dt, m.sy_delay[it], pend)) fire = true;
-                    }
-                    row[j] = synapse_dyn_k<EDEN_SYN_EXPONE>(st, init, dt, fire, wt, a, b);
-                }
-            }
-            if (pend != pend0) m.sy_pend[it] = pend;
-            m.sy_a[it] = a;
+            if (st.kind == EDEN_SYN_EXPTWO) synapse_steps<EDEN_SYN_EXPTWO>(m, it, w, st, tk, row, acc);
+            else synapse_steps<EDEN_SYN_EXPONE>(m, it, w, st, tk, row, acc);
         }
     }
     __syncwarp();
     if (lane < w.K) {
+        const int rows = n < 32 ? n : 32;
         float tot = 0.0f;
-        for (int r = 0; r < n; r++) tot += tile[r * kAccStride + lane];
+        for (int r = 0; r < rows; r++) tot += tile[r * kAccStride + lane];
         m.Gp[(size_t)lane * m.n_chunk + c] = tot;
     }
     __syncwarp();
@@ -419,17 +433,30 @@ __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1,
 // One HH gate for one step (eden/Eden.cpp:5126-5259): exponential-Euler
 // relaxation towards inf(V) with time constant tau(V), clamped to
 // [1e-6, 1 - 1e-6]; initialisation sets it to inf(V).
-__device__ __forceinline__ float gate_next(const ChanTypeDev &ct, int gi, bool init, float dt, float v, float qo) {
-    const float alpha = rate_value(ct.fk[gi], ct.fr[gi], ct.fm[gi], ct.fs[gi], v);
-    const float beta = rate_value(ct.rk[gi], ct.rr[gi], ct.rm[gi], ct.rs[gi], v);
+__device__ __forceinline__ float gate_relax(float alpha, float beta, float q10, bool init, float dt, float qo) {
     const float tau = 1.0f / (alpha + beta);
     const float inf = alpha / (alpha + beta);
     if (init) return inf;
-    const float blend = expf(-((dt * ct.q10[gi]) / tau));
+    const float blend = expf(-((dt * q10) / tau));
     float qn = blend * qo + (1.0f - blend) * inf;
     if (!(qn > 1e-6f)) qn = 1e-6f;
     if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
     return qn;
+}
+
+__device__ __forceinline__ float gate_next(const ChanTypeDev &ct, int gi, bool init, float dt, float v, float qo) {
+    const float alpha = rate_value(ct.fk[gi], ct.fr[gi], ct.fm[gi], ct.fs[gi], v);
+    const float beta = rate_value(ct.rk[gi], ct.rr[gi], ct.rm[gi], ct.rs[gi], v);
+    return gate_relax(alpha, beta, ct.q10[gi], init, dt, qo);
+}
+
+// The same from a gate's 9-word parameter record (forward form, rate,
+// midpoint, scale; reverse form, rate, midpoint, scale; q10 factor), kept
+// in shared memory by the windowed kernel.
+__device__ __forceinline__ float gate_next_p(const float *P, bool init, float dt, float v, float qo) {
+    const float alpha = rate_value(__float_as_int(P[0]), P[1], P[2], P[3], v);
+    const float beta = rate_value(__float_as_int(P[4]), P[5], P[6], P[7], v);
+    return gate_relax(alpha, beta, P[8], init, dt, qo);
 }
 
 // ---------------------------------------------------------------------------
@@ -566,25 +593,31 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
 // Backward-Euler Hines solve of one forest by one warp for the windowed path,
 // on the unit's shared-memory slice (eden/Eden.cpp:6114-6225).  Flat
 // compartments keep the reciprocal pivot PV and the elimination factor RT
-// = L / pivot computed once, because their diagonals never change; a
-// non-flat compartment's pivot is rebuilt every step from its diagonal
-// (PV holds G/C + sum 1/(RC) on entry) and its children's factors, in
-// increasing child order as the reference's post-order visits them.  Depths
-// hold at most 32 compartments, one per lane.  Back-substitution runs
-// root-first.  X holds the pre-updated V on entry and V_next on return.
-__device__ __forceinline__ void hines_window(float dt, float *X, const float *L, float *PV, float *RT,
-                                             const float *U, const uint32_t *CEP, const int32_t *LV, int nlev) {
+// = L / pivot computed once, because their diagonals never change, and
+// their pre-update (V += KC) is folded into the elimination; a non-flat
+// compartment's pivot is rebuilt every step from its diagonal (PV holds
+// G/C + sum 1/(RC) on entry, X its pre-updated V) and its children's
+// factors, in increasing child order as the reference's post-order visits
+// them.  Depths hold at most 32 compartments, one per lane; LV marks the
+// depths that hold a non-flat compartment.  Back-substitution runs
+// root-first.  X holds V_next on return.
+constexpr int32_t kLvMask = 0xffff;
+constexpr int32_t kLvNonFlat = 1 << 16;
+__device__ __forceinline__ void hines_window(float dt, float *X, const float *KC, const float *L, float *PV,
+                                             float *RT, const float *U, const uint32_t *CEP, const int32_t *LV,
+                                             int nlev) {
     const int lane = threadIdx.x & 31;
     for (int lev = nlev - 1; lev >= 0; lev--) {
-        const int j0 = LV[lev], j1 = LV[lev + 1];
+        const int32_t lw = LV[lev];
+        const int j0 = lw & kLvMask, j1 = LV[lev + 1] & kLvMask;
         const int j = j0 + lane;
         if (j < j1) {
             const uint32_t cep = CEP[j];
             const int ke = (int)(cep & kCepMask);
             const int kb = lane == 0 ? j1 : (int)(CEP[j - 1] & kCepMask);
-            if (cep & kCepNonFlat) {
+            float xj = X[j] + KC[j];
+            if ((lw & kLvNonFlat) && (cep & kCepNonFlat)) {
                 float dj = 1.0f + PV[j] * dt;
-                float xj = X[j];
                 for (int i = kb; i < ke; i++) {
                     const float r = RT[i];
                     dj -= r * U[i];
@@ -593,20 +626,18 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *L,
                 const float inv = __fdividef(1.0f, dj);
                 PV[j] = inv;
                 RT[j] = L[j] * inv;
-                X[j] = xj;
-            } else if (ke > kb) {
-                float xj = X[j];
+            } else {
                 for (int i = kb; i < ke; i++) xj -= RT[i] * X[i];
-                X[j] = xj;
             }
+            X[j] = xj;
         }
         __syncwarp();
     }
-    for (int r = LV[0] + lane; r < LV[1]; r += 32) X[r] = X[r] * PV[r];
+    for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) X[r] = X[r] * PV[r];
     __syncwarp();
     for (int lev = 1; lev < nlev; lev++) {
-        const int i = LV[lev] + lane;
-        if (i < LV[lev + 1]) {
+        const int i = (LV[lev] & kLvMask) + lane;
+        if (i < (LV[lev + 1] & kLvMask)) {
             const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
             X[i] = (X[i] - U[i] * X[p]) * PV[i];
         }

@@ -33,12 +33,19 @@ __device__ __forceinline__ float randof(float x, int64_t work_item, int64_t inst
     return x * r;
 }
 
-// HH rate forms (eden/Eden.cpp:5164-5181).
+// HH rate forms (eden/Eden.cpp:5164-5181), evaluated without branching on
+// the form so that the gates of a warp with different forms do not diverge;
+// each form keeps its own operations: EXP r * exp(x), EXPLINEAR
+// r * (x / (1 - exp(-x))) (r where V == mid), SIGMOID r / (1 + exp(-x)),
+// with x = (V - mid) / s (mid - V is exactly -(V - mid)).
 __device__ __forceinline__ float rate_value(int kind, float r, float mid, float s, float v) {
-    if (kind == EDEN_RATE_EXP) return r * expf((v - mid) / s);
-    if (kind == EDEN_RATE_EXPLINEAR)
-        return r * ((v == mid) ? 1.0f : (((v - mid) / s) / (1.0f - expf(-(v - mid) / s))));
-    return r / (1.0f + expf((mid - v) / s));
+    const float x = (v - mid) / s;
+    const float e = expf(kind == EDEN_RATE_EXP ? x : -x);
+    const bool sig = kind == EDEN_RATE_SIGMOID;
+    const float q = (sig ? r : x) / (sig ? 1.0f + e : 1.0f - e);
+    if (kind == EDEN_RATE_EXP) return r * e;
+    if (sig) return q;
+    return r * ((v == mid) ? 1.0f : q);
 }
 
 // Channel type table in constant memory (a handful of ionChannelHH types).

@@ -208,8 +208,8 @@ int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
  * that cannot let cudaMalloc/cudaFree synchronise the device mid-run, must
  * avoid.  This entry point runs the same kernels in the same order and
  * allocates nothing: the input scratch lives in a static device array of
- * 16 MiB (models of at most 131072 input chunks of 32 inputs; larger models
- * get EDEN_GPU_E_RANGE), window arguments in a static device table, and the
+ * 16 MiB (models of at most 131072 input chunks; a chunk is up to 128
+ * inputs of one type on one compartment; larger models get EDEN_GPU_E_RANGE), window arguments in a static device table, and the
  * launches are direct (no graph, no kernel timing).  Results equal
  * edenGpuRun's; the two may be interleaved on one context.
  * The first call on a device performs a one-time set-up (looking up the

@@ -86,9 +86,10 @@ def test_static_scratch_interleaves_with_run():
 
 
 def test_static_scratch_rejects_models_beyond_its_size():
-    # 30000 point cells x 100 synapses: about 150000 input chunks of 32,
-    # more than the 131072 the static scratch holds
-    low = lowering.lower(workloads.izh_net(n_cells=30000, in_degree=100, length_ms=1.0, n_recorded=1))
+    # 80000 point neurons, each with a pulse and excitatory and inhibitory
+    # synapses: about 231000 input chunks, more than the 131072 the static
+    # scratch holds
+    low = lowering.lower(workloads.izh_net(n_cells=80000, in_degree=10, length_ms=1.0, n_recorded=1))
     sim = engine.Simulation(low)
     try:
         with pytest.raises(engine.EdenGpuError) as e:
