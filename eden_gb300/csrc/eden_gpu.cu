@@ -255,7 +255,10 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     int32_t *NT = (int32_t *)(S + 7 * n);
     float *VO = (float *)(NT + nf), *NA = VO + nf, *NC = NA + nf, *NIR = NC + nf;
     int32_t *NB0 = (int32_t *)(NIR + nf), *NB1 = NB0 + nf, *NCH0 = NB1 + nf, *NCH1 = NCH0 + nf;
-    float *GT = (float *)(NCH1 + nf);
+    const int uch0 = nf > 0 ? m.nf_c0[nf0] : 0, nch = nf > 0 ? m.nf_c1[nf0 + nf - 1] - uch0 : 0;
+    float *CHG = (float *)(NCH1 + nf), *CHE = CHG + nch;
+    int32_t *CHQ = (int32_t *)(CHE + nch), *CHI = CHQ + nch;
+    float *GT = (float *)(CHI + nch);
     int32_t *GI_S = (int32_t *)(GT + ngt);
     float *GP = (float *)(GI_S + ngt);
     int32_t *LV = (int32_t *)(GP + kGateWords * ngt);
@@ -277,7 +280,7 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
         NT[j] = ti; NA[j] = m.c_area[t]; NC[j] = m.c_cm[t]; NIR[j] = m.c_inv_rc[t];
         NB0[j] = m.t_blk0[t] - ub0; NB1[j] = m.t_blk0[t + 1] - ub0;
         const int ch0 = m.c_chan0[t], ch1 = m.c_chan0[t + 1];
-        NCH0[j] = ch0; NCH1[j] = ch1;
+        NCH0[j] = m.nf_c0[nf0 + j] - uch0; NCH1[j] = m.nf_c1[nf0 + j] - uch0;
         // gate update items: the non-flat slot and the gate's parameter record
         for (int ch = ch0; ch < ch1; ch++) {
             const int q0 = m.ch_gate0[ch] - gt0, q1 = m.ch_gate0[ch + 1] - gt0;
@@ -288,8 +291,14 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             }
         }
     }
+    for (int c = lane; c < nch; c += 32) {
+        CHG[c] = m.nfc_g[uch0 + c]; CHE[c] = m.nfc_e[uch0 + c]; CHQ[c] = m.nfc_q[uch0 + c]; CHI[c] = m.nfc_i[uch0 + c];
+    }
     for (int i = lane; i < ngt; i += 32) GT[i] = m.gate[gt0 + i];
-    for (int i = lane; i <= nlev; i += 32) LV[i] = (m.lvl[l0 + i] - t0) | (m.lvl_nf[l0 + i] ? kLvNonFlat : 0);
+    for (int i = lane; i <= nlev; i += 32) {
+        const int info = m.lvl_info[l0 + i];
+        LV[i] = (m.lvl[l0 + i] - t0) | ((info & 0x80) ? kLvNonFlat : 0);
+    }
     for (int i = lane; i < ns; i += 32) { ST[i] = m.gs_t[s0 + i]; SSRC[i] = m.gs_src[s0 + i]; STHR[i] = m.gs_thr[s0 + i]; }
     for (int b = lane; b <= nblk; b += 32) {
         BKC[b] = m.bk_c0[ub0 + b] - uc0;
@@ -318,16 +327,17 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             block_currents(Gk, NB0[j], NB1[j], BKK, BKE, BKC, 0, v, Iin, Gin, Isyn, Gsyn);
             const float A = NA[j];
             float Ich = 0.f, Gch = 0.f;
-            for (int ch = NCH0[j]; ch < NCH1[j]; ch++) {
-                const ChanTypeDev &ct = c_chan_types[m.ch_type[ch]];
+            for (int c = NCH0[j]; c < NCH1[j]; c++) {
+                const int gi_pack = CHI[c];
+                const float *q = GT + CHQ[c];
                 float fopen = 1.0f;
-                const float *q = GT + (m.ch_gate0[ch] - gt0);
-                for (int gi = 0; gi < ct.n_gates; gi++) {
+                for (int gi = 0; gi < (gi_pack & 7); gi++) {
                     const float qo = q[gi];
-                    for (int rr = 0; rr < ct.inst[gi]; rr++) fopen = fopen * qo;
+                    const int inst = (gi_pack >> (3 + 5 * gi)) & 31;
+                    for (int rr = 0; rr < inst; rr++) fopen = fopen * qo;
                 }
-                const float gs = m.ch_gbase[ch] * fopen;
-                Ich += (gs * (m.ch_erev[ch] - v) * 1e-5f) * A;
+                const float gs = CHG[c] * fopen;
+                Ich += (gs * (CHE[c] - v) * 1e-5f) * A;
                 Gch += (gs * 1e-5f) * A;
             }
             const float I = Ich + Iin + Isyn;
@@ -887,19 +897,19 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
                     c_pv0[it] = inv;
                     c_rt0[it] = c_l[it] * inv;
                 }
-                const uint32_t ce = (uint32_t)(c_cend[it] - a);
+                const uint32_t cb = k1 > k0 ? (uint32_t)(k0 - a) : 0u, ce = k1 > k0 ? (uint32_t)(k1 - a) : 0u;
                 const uint32_t pp = c_parent[it] >= 0 ? (uint32_t)(c_parent[it] - a + 1) : 0u;
-                c_cep[it] = ce | (pp << kCepParentShift) | (nonflat[it] ? kCepNonFlat : 0u);
+                c_cep[it] = ce | (cb << kCepBeginShift) | (pp << kCepParentShift) | (nonflat[it] ? kCepNonFlat : 0u);
             }
         }
     }
 
-    // depths of each forest that hold a non-flat compartment (parallel to lvl)
-    std::vector<uint8_t> lvl_nf(lvl.size(), 0);
+    // per forest depth (parallel to lvl): non-flat flag
+    std::vector<uint8_t> lvl_info(lvl.size(), 0);
     for (size_t f = 0; f < fo_t0.size(); f++)
         for (int l = 0; l < fo_nlev[f]; l++)
             for (int it = lvl[fo_l0[f] + l]; it < lvl[fo_l0[f] + l + 1]; it++)
-                if (nonflat[it]) lvl_nf[fo_l0[f] + l] = 1;
+                if (nonflat[it]) lvl_info[fo_l0[f] + l] = 0x80;
     // gate parameter records per channel type and gate (gate_next_p)
     std::vector<float> gate_par((size_t)std::max(m->n_chan_types, 1) * EDEN_MAX_GATES * kGateWords, 0.f);
     for (int k = 0; k < m->n_chan_types; k++) {
@@ -1092,6 +1102,25 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             un_s1[u] = (int)gs_t.size();
         }
     }
+    // channels of each unit's non-flat compartments, in slot order
+    std::vector<int32_t> nf_c0(nf_t.size()), nf_c1(nf_t.size()), nfc_q, nfc_i;
+    std::vector<float> nfc_g, nfc_e;
+    for (int u = 0; u < n_unit; u++) {
+        const int a = un_t0[u];
+        const int gbase = ch_gate0[c_chan0[a]];
+        for (int k = un_nf0[u]; k < un_nf1[u]; k++) {
+            const int t = a + nf_t[k];
+            nf_c0[k] = (int)nfc_g.size();
+            for (int ch = c_chan0[t]; ch < c_chan0[t + 1]; ch++) {
+                const EdenGpuChannelType &ty = m->chan_types[ch_type[ch]];
+                int32_t pack = ty.n_gates;
+                for (int g = 0; g < ty.n_gates; g++) pack |= ty.gate_instances[g] << (3 + 5 * g);
+                nfc_g.push_back(ch_g[ch]); nfc_e.push_back(ch_e[ch]);
+                nfc_q.push_back(ch_gate0[ch] - gbase); nfc_i.push_back(pack);
+            }
+            nf_c1[k] = (int)nfc_g.size();
+        }
+    }
     for (int u = 0; u < n_unit; u++) {
         const int a = un_t0[u], b = un_t1[u];
         un_r0[u] = (int)gr_t.size();
@@ -1103,8 +1132,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         if (un_f[u] >= 0) {
             const int nblk = t_blk0[b] - t_blk0[a];
             const int nck = bk_c0[t_blk0[b]] - bk_c0[t_blk0[a]];
-            un_words[u] = forest_words(b - a, un_nf1[u] - un_nf0[u], un_ngt[u], fo_nlev[un_f[u]], un_s1[u] - un_s0[u],
-                                       nblk, nck, std::max(ctx->K, 4));
+            const int nfch = un_nf1[u] > un_nf0[u] ? nf_c1[un_nf1[u] - 1] - nf_c0[un_nf0[u]] : 0;
+            un_words[u] = forest_words(b - a, un_nf1[u] - un_nf0[u], nfch, un_ngt[u], fo_nlev[un_f[u]],
+                                       un_s1[u] - un_s0[u], nblk, nck, std::max(ctx->K, 4));
         } else {
             un_words[u] = izh_words(b - a);
         }
@@ -1237,7 +1267,10 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.gs_t, gs_t)); TRY(upload_c(ctx, &d.gs_src, gs_src)); TRY(upload_c(ctx, &d.gs_thr, gs_thr));
     TRY(upload_c(ctx, &d.gr_t, gr_t)); TRY(upload_c(ctx, &d.gr_col, gr_col));
     TRY(upload_c(ctx, &d.un_nf0, un_nf0)); TRY(upload_c(ctx, &d.un_nf1, un_nf1)); TRY(upload_c(ctx, &d.nf_t, nf_t));
-    TRY(upload_c(ctx, &d.lvl_nf, lvl_nf)); TRY(upload_c(ctx, &d.gate_par, gate_par));
+    TRY(upload_c(ctx, &d.lvl_info, lvl_info)); TRY(upload_c(ctx, &d.gate_par, gate_par));
+    TRY(upload_c(ctx, &d.nf_c0, nf_c0)); TRY(upload_c(ctx, &d.nf_c1, nf_c1));
+    TRY(upload_c(ctx, &d.nfc_g, nfc_g)); TRY(upload_c(ctx, &d.nfc_e, nfc_e));
+    TRY(upload_c(ctx, &d.nfc_q, nfc_q)); TRY(upload_c(ctx, &d.nfc_i, nfc_i));
     TRY(upload(ctx, &d.status, (const int32_t *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_base, (const int *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_zero, (const int *)nullptr, 1));

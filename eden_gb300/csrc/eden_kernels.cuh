@@ -86,8 +86,8 @@ struct DevModel {
     //   c_pv0  flat: reciprocal of its Hines pivot, which is the same every
     //          step because nothing below it changes; non-flat: unused
     //   c_rt0  flat: L / pivot, its elimination factor into its parent
-    //   c_cep  child-range end | (parent + 1) << 10 | non-flat << 20, all
-    //          local to the compartment's forest
+    //   c_cep  child-range end | child-range begin << 10 | (parent + 1) << 20
+    //          | non-flat << 30, all local to the compartment's forest
     const float *c_kc, *c_pv0, *c_rt0;
     const uint32_t *c_cep;
     // forests: physical compartments [fo_t0, fo_t1), depth boundaries lvl[fo_l0 .. fo_l0 + fo_nlev]
@@ -159,29 +159,38 @@ struct DevModel {
     // non-flat compartments of forest units: nf_t[un_nf0[u] .. un_nf1[u]) are
     // unit-local indices; spike sources (gs_t) and gates refer to these slots
     const int32_t *un_nf0, *un_nf1, *nf_t;
-    // per forest depth boundary (parallel to lvl): the depth holds a non-flat compartment
-    const uint8_t *lvl_nf;
+    // per forest depth (parallel to lvl): 0x80 if it holds a non-flat compartment
+    const uint8_t *lvl_info;
+    // channels of the non-flat compartments, per non-flat compartment
+    // [nf_c0, nf_c1): conductivity, reversal potential, first gate (index in
+    // the unit's gates) and gate count | instances << (3 + 5 * gate)
+    const int32_t *nf_c0, *nf_c1;
+    const float *nfc_g, *nfc_e;
+    const int32_t *nfc_q, *nfc_i;
     // per channel type and gate, the 9-word gate parameter record (gate_next_p)
     const float *gate_par;
     int32_t *status;
 };
 
 constexpr uint32_t kCepMask = 0x3ffu;
-constexpr int kCepParentShift = 10;
-constexpr uint32_t kCepNonFlat = 1u << 20;
+constexpr int kCepBeginShift = 10;
+constexpr int kCepParentShift = 20;
+constexpr uint32_t kCepNonFlat = 1u << 30;
 constexpr int kGateWords = 9;  // gate parameter record (gate_next_p)
 
 // Shared-memory words of a unit's slice in the windowed kernel.  A forest:
 // 7 per compartment (V, c_kc, L, pivot, elimination factor, U, packed
-// child-end/parent/flag), 9 per non-flat compartment (local index, V at the
-// step start, area, C, sum of 1/(R C), input-block range, channel range),
-// 11 per gate (value, non-flat slot, parameter record), the depth
-// boundaries, 3 per spike source, 3 per input block (kind, reversal
-// potential, chunk start) plus one, and the window's conductance series of
-// the unit's input chunks (kcap steps).  A batch of izhikevich neurons: V
+// child range/parent/flag), 9 per non-flat compartment (local index, V at
+// the step start, area, C, sum of 1/(R C), input-block range, channel
+// range), 4 per channel of a non-flat compartment, 11 per gate (value,
+// non-flat slot, parameter record), the depth boundaries, 3 per spike
+// source, 3 per input block (kind, reversal potential, chunk start) plus
+// one, and the window's conductance series of the unit's input chunks
+// (kcap steps).  A batch of izhikevich neurons: V
 // twice and 11 parameter / state words per neuron.
-__host__ __device__ inline int forest_words(int n, int nf, int ngt, int nlev, int ns, int nblk, int nck, int kcap) {
-    return 7 * n + 9 * nf + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck;
+__host__ __device__ inline int forest_words(int n, int nf, int nfch, int ngt, int nlev, int ns, int nblk, int nck,
+                                            int kcap) {
+    return 7 * n + 9 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck;
 }
 __host__ __device__ inline int izh_words(int n) { return 13 * n + 1; }
 
@@ -598,23 +607,22 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
 // compartment's pivot is rebuilt every step from its diagonal (PV holds
 // G/C + sum 1/(RC) on entry, X its pre-updated V) and its children's
 // factors, in increasing child order as the reference's post-order visits
-// them.  Depths hold at most 32 compartments, one per lane; LV marks the
-// depths that hold a non-flat compartment.  Back-substitution runs
-// root-first.  X holds V_next on return.
+// them.  Depths hold at most 32 compartments, one per lane; LV packs each
+// depth's first compartment and whether it holds a non-flat one.
+// Back-substitution runs root-first.  X holds V_next on return.
 constexpr int32_t kLvMask = 0xffff;
 constexpr int32_t kLvNonFlat = 1 << 16;
 __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC, const float *L, float *PV,
                                              float *RT, const float *U, const uint32_t *CEP, const int32_t *LV,
                                              int nlev) {
     const int lane = threadIdx.x & 31;
+    int end = LV[nlev] & kLvMask;
     for (int lev = nlev - 1; lev >= 0; lev--) {
         const int32_t lw = LV[lev];
-        const int j0 = lw & kLvMask, j1 = LV[lev + 1] & kLvMask;
-        const int j = j0 + lane;
-        if (j < j1) {
+        const int j = (lw & kLvMask) + lane;
+        if (j < end) {
             const uint32_t cep = CEP[j];
-            const int ke = (int)(cep & kCepMask);
-            const int kb = lane == 0 ? j1 : (int)(CEP[j - 1] & kCepMask);
+            const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
             float xj = X[j] + KC[j];
             if ((lw & kLvNonFlat) && (cep & kCepNonFlat)) {
                 float dj = 1.0f + PV[j] * dt;
@@ -627,10 +635,16 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
                 PV[j] = inv;
                 RT[j] = L[j] * inv;
             } else {
-                for (int i = kb; i < ke; i++) xj -= RT[i] * X[i];
+                // most compartments have at most two children: take those
+                // without a loop, in order
+                int i = kb;
+                if (i < ke) xj -= RT[i] * X[i];
+                if (i + 1 < ke) xj -= RT[i + 1] * X[i + 1];
+                for (i = kb + 2; i < ke; i++) xj -= RT[i] * X[i];
             }
             X[j] = xj;
         }
+        end = lw & kLvMask;
         __syncwarp();
     }
     for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) X[r] = X[r] * PV[r];
