@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -598,6 +599,18 @@ extern "C" void edenGpuDestroy(EdenGpuCtx *ctx) {
 static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGpuOptions *opt) {
     const int n_comp = m->n_comp, n_izh = m->n_izh, n_phys = m->n_phys;
     const int nt = n_comp + n_izh;
+    // set-up phase timing, printed with EDEN_GPU_VERBOSE
+    const bool verbose = getenv("EDEN_GPU_VERBOSE") != nullptr;
+    auto t_last = std::chrono::steady_clock::now();
+    std::string timing;
+    auto phase = [&](const char *next) {
+        const auto now = std::chrono::steady_clock::now();
+        char b[64];
+        snprintf(b, sizeof(b), " %.1f ms, then %s:", std::chrono::duration<double, std::milli>(now - t_last).count(), next);
+        timing += b;
+        t_last = now;
+    };
+    timing = "cells:";
     const int n_cells = m->n_src;
     const float dt = m->dt;
     ctx->n_target = nt;
@@ -649,6 +662,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         total += c;
     }
 
+    phase("order");
     // ---- schedule order: physical cells by tree depth (then size), then point
     // neurons, so that a CTA's warps finish their cable solves together
     std::vector<int32_t> cell_levels(n_cells, 0);
@@ -675,6 +689,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         return cell_n[x] < cell_n[y];
     });
 
+    phase("units");
     // ---- units: each warp of the windowed kernel owns one unit for the whole
     // window -- a forest of physical cells (joint breadth-first numbering,
     // at most 32 nodes per depth level, at most kForestNodes nodes) or a batch
@@ -815,6 +830,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     ctx->user_to_internal = u2i;
     ctx->gcap = max_cell;
     ctx->forest_cap = max_forest;
+    phase("constants");
     // ---- per-target constants in internal order
     std::vector<float> c_cm(nt, 1.f), c_inv(nt, 0.f), c_area(nt, 0.f), v0(nt, 0.f);
     std::vector<int32_t> c_chan0(nt + 1, 0);
@@ -930,16 +946,21 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int k = 0; k < n_izh; k++) iz[f][k] = m->izh_params[10 * (int64_t)izh_user_of_slot[k] + f];
     }
 
+    phase("inputs-sort");
     // ---- inputs sorted by internal target (then type, then input order)
+    // (two stable counting passes: by type, then by internal target)
     auto sort_items = [&](int64_t n, const int32_t *tgt, const int32_t *type) {
-        std::vector<int64_t> idx(n);
+        std::vector<int64_t> idx(n), tmp(n);
         std::iota(idx.begin(), idx.end(), 0);
-        std::stable_sort(idx.begin(), idx.end(), [&](int64_t x, int64_t y) {
-            int tx = u2i[tgt[x]], ty = u2i[tgt[y]];
-            if (tx != ty) return tx < ty;
-            if (type) return type[x] < type[y];
-            return false;
-        });
+        auto pass = [&](int nkeys, auto key) {
+            std::vector<int64_t> cnt((size_t)nkeys + 1, 0);
+            for (int64_t k = 0; k < n; k++) cnt[key(idx[k]) + 1]++;
+            for (int b = 0; b < nkeys; b++) cnt[b + 1] += cnt[b];
+            for (int64_t k = 0; k < n; k++) tmp[cnt[key(idx[k])]++] = idx[k];
+            idx.swap(tmp);
+        };
+        if (type) pass(kMaxSynTypes, [&](int64_t x) { return (int)type[x]; });
+        pass(nt, [&](int64_t x) { return (int)u2i[tgt[x]]; });
         return idx;
     };
     auto offsets = [&](const std::vector<int64_t> &order, const int32_t *tgt) {
@@ -983,6 +1004,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         ctx->syn_internal_of_user[o] = k;
         min_delay = std::min(min_delay, m->syn_delay[o]);
     }
+    phase("fanout");
     // source fan-out in connection (user) order
     std::vector<int64_t> fan0(m->n_src + 1, 0);
     for (int64_t o = 0; o < ns; o++) fan0[m->syn_src[o] + 1]++;
@@ -1001,6 +1023,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         t_src[u2i[m->src_target[s]]] = s;
         src_thr[s] = m->src_threshold[s];
     }
+    phase("blocks");
     // input blocks per target: pulses, then Poisson runs, then synapse runs of one type
     std::vector<int32_t> t_blk0(nt + 1, 0);
     std::vector<int32_t> bk_kind;
@@ -1075,6 +1098,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     ctx->trace_cap = (opt && opt->record_capacity_steps > 0) ? opt->record_capacity_steps : 4096;
     int64_t log_cap = (opt && opt->spike_capacity > 0) ? opt->spike_capacity : (int64_t)1 << 22;
 
+    phase("unit-lists");
     // ---- per-unit lists of the windowed kernel: spike sources and recorded
     // targets (unit-local indices), gates, and each unit's shared-memory words
     const int n_unit = (int)un_t0.size();
@@ -1139,6 +1163,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             un_words[u] = izh_words(b - a);
         }
     }
+    phase("packing");
     // CTAs of up to four units, packed longest-first onto the CTA with the
     // fewest words so that every CTA needs about the same shared memory
     const int upc = kCellThreads / 32;
@@ -1199,6 +1224,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (auto &cl : ctx->classes) max_smem_class = std::max(max_smem_class, cl.smem);
     ctx->smem_window = max_smem_class <= (size_t)ctx->smem_optin;
 
+    phase("upload");
     // ---- upload
     DevModel &d = ctx->d;
     d.n_target = nt; d.n_src = m->n_src; d.n_unit = n_unit; d.n_forest = (int)fo_t0.size();
@@ -1275,6 +1301,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload(ctx, &ctx->d_base, (const int *)nullptr, 1));
     TRY(upload(ctx, &ctx->d_zero, (const int *)nullptr, 1));
 
+    phase("tables");
     // ---- constant tables
     ChanTypeDev ct[kMaxChanTypes];
     memset(ct, 0, sizeof(ct));
@@ -1329,7 +1356,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     if (ctx->smem_window)
         CUDA_TRY(ctx, cudaFuncSetAttribute(k_cells_t, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)std::min<size_t>(max_smem_class, (size_t)ctx->smem_optin)));
-    if (getenv("EDEN_GPU_VERBOSE")) {
+    phase("done");
+    if (verbose) {
+        fprintf(stderr, "libeden_gpu: set-up %s\n", timing.c_str());
         int occ_cells = 0, occ_inputs = 0;
         if (ctx->smem_window)
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cells, k_cells_t, kCellThreads, max_smem_class);
