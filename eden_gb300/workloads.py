@@ -91,8 +91,14 @@ def random_tree(rng, n_seg: int, soma_len=20.0, soma_diam=20.0):
 def multicomp_net(n_cells: int = 10000, in_degree: int = 100, length_ms: float = 1000.0,
                   dt_ms: float = 0.025, seed: int = 1234, max_seg: int = 500,
                   poisson_rate_hz: float = 5.0, n_recorded: int = 10,
-                  weight: float = 1.0, soma_diam: float = 20.0) -> NetworkSpec:
+                  weight: float = 1.0, soma_diam: float = 20.0, hh_dend_frac: float = 0.0,
+                  syn_on_dendrites: bool = False) -> NetworkSpec:
+    """hh_dend_frac > 0 puts HH channels on that fraction of dendritic
+    segments as well; syn_on_dendrites places each connection on a random
+    segment of the target cell instead of the soma (both drawn from a second
+    generator, so the default network is unchanged)."""
     rng = np.random.default_rng(seed)
+    rng2 = np.random.default_rng(seed + 1)
     spec = NetworkSpec("multicomp_net", dt_ms, length_ms, seed, channels=hh_channels())
     syn = SynapseType("syn_e2", SYN_EXPTWO, gbase=1.0, erev=0.0, tau_decay=5.0, tau_rise=0.5)
     spec.synapses.append(syn)
@@ -102,7 +108,8 @@ def multicomp_net(n_cells: int = 10000, in_degree: int = 100, length_ms: float =
         parent, length, diam = random_tree(rng, int(nseg[c]), soma_diam=soma_diam, soma_len=soma_diam)
         soma = np.zeros(len(parent), dtype=bool)
         soma[0] = True
-        cell = PhysicalCell(f"mc{c}", parent, length, diam, _hh_densities(len(parent), soma),
+        hh = soma | (rng2.random(len(parent)) < hh_dend_frac) if hh_dend_frac > 0 else soma
+        cell = PhysicalCell(f"mc{c}", parent, length, diam, _hh_densities(len(parent), hh),
                             cm=1.0, ra=150.0, v0=-65.0, spike_thresh=-20.0,
                             seg_groups={"soma_group": soma, "dend_group": ~soma})
         spec.cells.append(cell)
@@ -111,8 +118,12 @@ def multicomp_net(n_cells: int = 10000, in_degree: int = 100, length_ms: float =
     pre = rng.integers(0, n_cells, size=(n_cells, in_degree))
     delay = _round_us(rng.uniform(0.5, 5.0, size=(n_cells, in_degree)))
     post = np.repeat(np.arange(n_cells), in_degree)
+    post_seg = None
+    if syn_on_dendrites:
+        nsegs = np.array([len(spec.cells[c].seg_parent) for c in range(n_cells)])
+        post_seg = (rng2.random(post.size) * nsegs[post]).astype(int)
     spec.projections.append(_flat_projection(spec, "proj_e2", pre.ravel(), post, "syn_e2",
-                                             np.full(post.size, weight), delay.ravel()))
+                                             np.full(post.size, weight), delay.ravel(), post_seg=post_seg))
     # one Poisson source per synapse slot, onto the soma
     if poisson_rate_hz > 0:
         spec.poissons.append(PoissonInputs("*", "syn_e2", poisson_rate_hz,

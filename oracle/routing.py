@@ -83,3 +83,30 @@ def route(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step):
         pend[s] = p
         fires[s] = len(fired)
     return pend, fires
+
+
+def route_pending(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step):
+    """The pending slot of every synapse after all triggers read at steps
+    <= last_step, as route() computes it, vectorised over each spike's
+    fan-out (in step order; spikes of one step reach disjoint synapses) so
+    that it runs at full network sizes."""
+    syn_src = np.asarray(syn_src)
+    syn_delay = np.asarray(syn_delay, F32)
+    n_src = int(syn_src.max()) + 1 if len(syn_src) else 0
+    order = np.argsort(syn_src, kind="stable")
+    fan0 = np.zeros(n_src + 1, np.int64)
+    np.add.at(fan0, syn_src + 1, 1)
+    fan0 = np.cumsum(fan0)
+    times = step_times(dt_us, last_step + 1)
+    dt = F32(dt_us)
+    pend = np.full(len(syn_src), -np.inf, F32)
+    spike_src = np.asarray(spike_src)
+    spike_step = np.asarray(spike_step)
+    keep = (spike_step >= 1) & (spike_step <= last_step) & (spike_src < n_src)
+    for k, s in sorted(zip(spike_step[keep].tolist(), spike_src[keep].tolist())):
+        syn = order[fan0[s]:fan0[s + 1]]
+        t = times[k]
+        fresh = (t + syn_delay[syn]).astype(F32)
+        p = pend[syn]
+        pend[syn] = np.where((p < F32(t + dt)) & (p < fresh), fresh, p)
+    return pend

@@ -23,8 +23,20 @@ pytestmark = pytest.mark.gpu
 
 
 
+# networks checked against the oracle only (no reference fixtures): HH
+# channels and synapses on dendrites, so that non-flat compartments sit
+# inside the trees with flat ones above and below them; and the mixed
+# point-neuron / multicompartment network
+EXTRA = {
+    "multicomp_active_dendrites": lambda: workloads.multicomp_net(
+        n_cells=24, in_degree=20, length_ms=40.0, max_seg=80, n_recorded=6, hh_dend_frac=0.2,
+        syn_on_dendrites=True),
+    "mixed_small": lambda: workloads.mixed_scale(n_izh=400, n_mc=100, in_degree=20, length_ms=30.0, n_seg=30),
+}
+
+
 def _spec(name):
-    return spec_of(name)
+    return EXTRA[name]() if name in EXTRA else spec_of(name)
 
 
 @pytest.fixture(scope="module")
@@ -40,7 +52,7 @@ def oracle_runs():
 
 
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
-@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("name", list(CASES) + list(EXTRA))
 def test_gpu_matches_oracle(name, mode, oracle_runs):
     low, ref = oracle_runs(name)
     sim = Simulation(low, mode=mode)
@@ -54,8 +66,10 @@ def test_gpu_matches_oracle(name, mode, oracle_runs):
     assert not wrong, f"spike counts differ for cells {wrong[:10]}"
     assert not far, f"spikes more than 0.1 ms apart for cells {far[:10]}"
     assert np.isfinite(rec.trace).all()
-    nbad, worst = box_violations(ref["trace"], rec.trace, dt_ms, 0.1, 0.5)
-    assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst by {worst} mV"
+    assert len(ref["spike_src"]) > 0
+    if rec.trace.shape[1]:
+        nbad, worst = box_violations(ref["trace"], rec.trace, dt_ms, 0.1, 0.5)
+        assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst by {worst} mV"
 
 
 @pytest.mark.parametrize("name", list(CASES))

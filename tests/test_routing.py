@@ -22,6 +22,9 @@ def test_oracle_routing_matches_restatement(name):
     assert np.array_equal(pend.view(np.uint32), out["syn_final_pending"].view(np.uint32))
     assert np.array_equal(fires, out["syn_fire_count"])
     assert fires.sum() > 0
+    fast = routing.route_pending(low.syn_src, low.syn_delay, out["spike_src"], out["spike_step"], float(low.dt),
+                                 low.n_steps)
+    assert np.array_equal(fast.view(np.uint32), pend.view(np.uint32))
 
 
 def test_single_pending_slot_drops_closely_spaced_spikes():
