@@ -27,53 +27,104 @@ def _fmt(x: float) -> str:
     return "%+16.8g" % x
 
 
-def _step_times(dt_us: float, last_step: int) -> np.ndarray:
-    """Simulation time in seconds of steps 0..last_step: the reference starts at
+def _step_times_us(dt_us: float, last_step: int) -> np.ndarray:
+    """Simulation time in us of steps 0..last_step: the reference starts at
     0, runs the initialisation steps at t = 0 and then adds the float dt to a
     double accumulator once per step (eden/Eden.cpp:11486, 11931), so step
     k >= 1 runs at the double sum of k - 1 dts."""
     n = max(int(last_step), 1)
     acc = np.concatenate([[0.0], np.add.accumulate(np.full(n - 1, float(np.float32(dt_us))))])
-    return np.concatenate([[0.0], acc]) * 1e-6
+    return np.concatenate([[0.0], acc])
+
+
+def _step_times(dt_us: float, last_step: int) -> np.ndarray:
+    """The same in seconds, as the output files print it."""
+    return _step_times_us(dt_us, last_step) * 1e-6
+
+
+def trajectory_frames(of: dict, times_us: np.ndarray, steps: np.ndarray):
+    """(timestamp in us, sample row) of every frame a trajectory logger emits,
+    given the step of each recorded sample (eden/Eden.cpp:11565-11599):
+    explicit sample points take the first step at or after each point and
+    are stamped with the point; otherwise a step inside [start, end) is
+    sampled when the sampling interval has passed since the last frame."""
+    frames = []
+    if of.get("points"):
+        pts, nxt = of["points"], 0
+        for r, k in enumerate(steps):
+            t = times_us[k]
+            while nxt < len(pts) and pts[nxt] <= t:
+                frames.append((pts[nxt], r))
+                nxt += 1
+        return frames
+    last = -np.inf
+    for r, k in enumerate(steps):
+        t = times_us[k]
+        if of["start"] <= t < of["end"] and last + of["interval"] <= t:
+            frames.append((t, r))
+            last = t
+    return frames
+
+
+def event_frames(ef: dict, times_us: np.ndarray, first_step: int, last_step: int, cols_at_step: dict):
+    """(timestamp in us, [column indices]) of every frame an event logger
+    emits (eden/Eden.cpp:11600-11633): a step inside [start, end) with events,
+    or any such step once maximum_interval has passed since the last frame."""
+    frames = []
+    last = -np.inf
+    for k in range(first_step, last_step + 1):
+        t = times_us[k]
+        if not (ef["start"] <= t < ef["end"]):
+            continue
+        inst = cols_at_step.get(k, [])
+        if inst or last + ef["max_interval"] <= t:
+            frames.append((t, inst))
+            last = t
+    return frames
 
 
 def write_outputs(spec, low, rec, base_dir: str, n_steps: int) -> list:
-    """Write every OutputFile / EventOutputFile of the simulation."""
+    """Write every trajectory and event logger of the simulation in the
+    reference's formats (eden/Eden.cpp:10843-10940)."""
     written = []
     last = max([int(rec.trace_step.max()) if len(rec.trace_step) else 1,
                 int(rec.spike_step.max()) if len(rec.spike_step) else 1, n_steps])
-    times = _step_times(float(low.dt), last)
+    times_us = _step_times_us(float(low.dt), last)
     col0 = 0
-    for _id, fname, cols in getattr(spec, "output_files", []):
-        path = os.path.join(base_dir, fname)
-        ncol = len(cols)
-        block = rec.trace[:, col0:col0 + ncol].astype(np.float64) * 1e-3  # mV -> V
+    for of in getattr(spec, "output_files", []):
+        path = os.path.join(base_dir, of["path"])
+        ncol = len(of["cols"])
+        scale = np.array([c[3] for c in of["cols"]], np.float64)  # engine mV -> the column's units
+        block = rec.trace[:, col0:col0 + ncol].astype(np.float64) * scale
         with open(path, "w") as f:
-            for r in range(block.shape[0]):
-                k = int(rec.trace_step[r])
-                f.write(_fmt(times[k]) + "".join(" " + _fmt(v) for v in block[r]) + "\n")
+            for t, r in trajectory_frames(of, times_us, rec.trace_step):
+                f.write(_fmt(t * 1e-6) + "".join(" " + _fmt(v) for v in block[r]) + "\n")
         col0 += ncol
         written.append(path)
-    # spikes: per logging step, in EventSelection order
-    for _id, fname, fmt, sels in getattr(spec, "event_files", []):
-        path = os.path.join(base_dir, fname)
-        off = spec.pop_offsets()
+    off = spec.pop_offsets()
+    for ef in getattr(spec, "event_files", []):
+        path = os.path.join(base_dir, ef["path"])
+        sels = ef["sels"]
         col_of_src = {}
         for j, (_sid, _sel, (pop, idx)) in enumerate(sels):
             col_of_src.setdefault(off[pop] + idx, []).append(j)
-        rows = []
+        cols_at_step = {}
         for s, k in zip(rec.spike_src, rec.spike_step):
             for j in col_of_src.get(int(s), []):
-                rows.append((int(k), j))
-        rows.sort()
+                cols_at_step.setdefault(int(k), []).append(j)
+        for k in cols_at_step:
+            cols_at_step[k].sort()
         with open(path, "w") as f:
-            for k, j in rows:
-                t = _fmt(times[k])
-                sid = sels[j][0]
-                if fmt == "ID_TIME":
-                    f.write(f"{sid} {t.strip()}\n")
+            for t, inst in event_frames(ef, times_us, 1, n_steps, cols_at_step):
+                ts = _fmt(t * 1e-6)
+                if ef["format"] == "ascii_v0":
+                    f.write(ts + "".join(f" {sels[j][0]}" for j in inst) + "\n")
+                elif ef["format"] == "ID_TIME":
+                    for j in inst:
+                        f.write(f"{sels[j][0]} {ts.strip()}\n")
                 else:
-                    f.write(f"{t} {sid}\n")
+                    for j in inst:
+                        f.write(f"{ts} {sels[j][0]}\n")
         written.append(path)
     return written
 
@@ -164,20 +215,28 @@ def reload_saved_data(lems_file_name, reload_events=False):
     spec = neuroml_io.read_lems(lems_file_name)
     base = os.path.dirname(os.path.abspath(lems_file_name))
     traces, events = OrderedDict(), OrderedDict()
-    for _id, fname, cols in spec.output_files:
-        data = np.loadtxt(os.path.join(base, fname), ndmin=2)
+    for of in spec.output_files:
+        data = np.loadtxt(os.path.join(base, of["path"]), ndmin=2)
         traces["t"] = data[:, 0]
-        for j, (_cid, quantity, _t) in enumerate(cols):
+        for j, (_cid, quantity, _t, _scale) in enumerate(of["cols"]):
             traces[quantity] = data[:, j + 1]
     if reload_events:
-        for _id, fname, fmt, sels in spec.event_files:
-            sel_of = {sid: select for sid, select, _ in sels}
-            for _sid, select, _ in sels:
+        for ef in spec.event_files:
+            sel_of = {sid: select for sid, select, _ in ef["sels"]}
+            for _sid, select, _ in ef["sels"]:
                 events[select] = []
-            with open(os.path.join(base, fname)) as f:
+            with open(os.path.join(base, ef["path"])) as f:
                 for line in f:
-                    a, b = line.split()
-                    t, sid = (float(a), int(b)) if fmt == "TIME_ID" else (float(b), int(a))
-                    events[sel_of[sid]].append(t)
+                    parts = line.split()
+                    if not parts:
+                        continue
+                    if ef["format"] == "ascii_v0":
+                        t = float(parts[0])
+                        for sid in parts[1:]:
+                            events[sel_of[int(sid)]].append(t)
+                    elif ef["format"] == "TIME_ID":
+                        events[sel_of[int(parts[1])]].append(float(parts[0]))
+                    else:
+                        events[sel_of[int(parts[0])]].append(float(parts[1]))
         return OrderedDict(sorted(traces.items())), OrderedDict(sorted(events.items()))
     return OrderedDict(sorted(traces.items()))

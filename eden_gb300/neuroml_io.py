@@ -510,21 +510,55 @@ def read_lems(path: str) -> NetworkSpec:
             raise ValueError(f"poissonFiringSynapse {comp}: synapse {syn} not supported")
         spec.poissons.append(PoissonInputs("*", syn, rate, np.array([r[0] for r in rows]),
                                            np.array([r[1] for r in rows])))
-    # recorders
+    # recorders: OutputFile / EventOutputFile and EDEN's EdenOutputFile /
+    # EdenEventOutputFile with their time window, sampling interval or explicit
+    # sample points, and heartbeat interval (eden/NeuroML.cpp:8037-8290);
+    # times are kept in us
     spec.trace_columns, spec.event_selections = [], []
     spec.output_files, spec.event_files = [], []
-    for of in _children(sim, "OutputFile"):
+    inf = float("inf")
+
+    def _path(e):
+        if e.get("fileName") is not None:
+            return e.get("fileName")
+        href = e.get("href") or ""
+        if not href.startswith("file://"):
+            raise ValueError(f"<{_tag(e)} id={e.get('id')}>: only file:// outputs are supported")
+        return href[len("file://"):]
+
+    def _us(e, attr, default):
+        return _qty(e, attr, "time") * 1e3 if e.get(attr) is not None else default
+
+    # recorded membrane potentials leave the engine in mV: classic OutputFile
+    # columns are written in SI units, EdenOutputFile columns in their
+    # output_units (eden/NeuroML.cpp:8170-8183)
+    volt_out = {"V": 1e-3, "mV": 1.0, "uV": 1e3}
+    for of in [c for c in sim if _tag(c) in ("OutputFile", "EdenOutputFile")]:
         cols = []
         for col in _children(of, "OutputColumn"):
-            cols.append((col.get("id"), col.get("quantity"), _quantity_target(col.get("quantity"), pops, cells)))
-        spec.output_files.append((of.get("id"), of.get("fileName"), cols))
+            units = col.get("output_units") if _tag(of) == "EdenOutputFile" else "V"
+            if units not in volt_out:
+                raise ValueError(f"OutputColumn {col.get('id')}: output_units {units!r} not supported")
+            cols.append((col.get("id"), col.get("quantity"), _quantity_target(col.get("quantity"), pops, cells),
+                         volt_out[units]))
+        points = None
+        for sp in _children(of, "SamplePoints"):
+            points = [_qty(x, "t", "time") * 1e3 for x in _children(sp, "s")]
+        spec.output_files.append({"id": of.get("id"), "path": _path(of), "cols": cols,
+                                  "start": _us(of, "starting_from", -inf), "end": _us(of, "up_to_excluding", inf),
+                                  "interval": _us(of, "sampling_interval", 0.0), "points": points})
         spec.trace_columns.extend(OutputColumn(*c[2]) for c in cols)
-    for ef in _children(sim, "EventOutputFile"):
+    for ef in [c for c in sim if _tag(c) in ("EventOutputFile", "EdenEventOutputFile")]:
         sels = []
         for sel in _children(ef, "EventSelection"):
             pop, idx = _cell_ref(sel.get("select"), pops)
             sels.append((int(sel.get("id")), sel.get("select"), (pop, idx)))
-        spec.event_files.append((ef.get("id"), ef.get("fileName"), ef.get("format", "TIME_ID"), sels))
+        fmt = ef.get("format", "TIME_ID")
+        if fmt not in ("TIME_ID", "ID_TIME", "ascii_v0"):
+            raise ValueError(f"<{_tag(ef)} id={ef.get('id')}>: unknown format {fmt}")
+        spec.event_files.append({"id": ef.get("id"), "path": _path(ef), "format": fmt, "sels": sels,
+                                 "start": _us(ef, "starting_from", -inf), "end": _us(ef, "up_to_excluding", inf),
+                                 "max_interval": _us(ef, "maximum_interval", inf)})
         spec.event_selections.extend(EventSelection(s[2][0], s[2][1], 0) for s in sels)
     return spec
 

@@ -20,3 +20,31 @@ def spec_of(name):
     from eden_gb300 import workloads
     gen, kw, _, _ = CASES[name]
     return workloads.CONFIGS[gen](**kw)
+
+
+# EDEN's extended loggers, added to the izh_net case's LEMS file: a trajectory
+# window sampled every 1 ms, explicit sample points, and an ascii_v0 event
+# file with a time window and a 10 ms heartbeat.  Their reference outputs are
+# in tests/golden/loggers.npz.
+LOGGER_FILES = ("sub.txt", "pts.txt", "ev.txt", "ev_id_time.txt")
+
+
+def add_eden_loggers(lems_path):
+    import re
+    txt = open(lems_path).read()
+    cols = re.findall(r'  <OutputColumn [^>]*/>\n', txt)[:3]
+    # extended columns name their output units
+    cols = [c.replace('/>', ' output_units="%s"/>' % u) for c, u in zip(cols, ("V", "mV", "mV"))]
+    sels = re.findall(r'  <EventSelection [^>]*/>\n', txt)
+    extra = (
+        ' <EdenOutputFile id="sub" href="file://sub.txt" format="ascii_v0" starting_from="10ms" '
+        'up_to_excluding="60.05ms" sampling_interval="1ms">\n' + "".join(cols) + ' </EdenOutputFile>\n'
+        ' <EdenOutputFile id="pts" href="file://pts.txt" format="ascii_v0">\n'
+        '  <SamplePoints><s t="0ms"/><s t="0.5ms"/><s t="12.34ms"/><s t="50ms"/><s t="99.95ms"/></SamplePoints>\n'
+        + "".join(cols) + ' </EdenOutputFile>\n'
+        ' <EdenEventOutputFile id="ev" href="file://ev.txt" format="ascii_v0" starting_from="5ms" '
+        'up_to_excluding="80ms" maximum_interval="10ms">\n' + "".join(sels[:120]) + ' </EdenEventOutputFile>\n'
+        ' <EdenEventOutputFile id="evi" href="file://ev_id_time.txt" format="ID_TIME">\n'
+        + "".join(sels[100:160]) + ' </EdenEventOutputFile>\n')
+    txt = txt.replace('</Simulation>', extra + '</Simulation>')
+    open(lems_path, "w").write(txt)

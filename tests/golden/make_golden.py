@@ -21,7 +21,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, HERE)
 
 import reference_runner  # noqa: E402
-from cases import CASES, spec_of  # noqa: E402
+from cases import CASES, LOGGER_FILES, add_eden_loggers, spec_of  # noqa: E402
 from eden_gb300 import neuroml_io  # noqa: E402
 
 
@@ -39,8 +39,22 @@ def make(name):
     print(f"{name}: {traj.shape[0]} samples x {traj.shape[1] - 1} columns, {len(ev)} spikes")
 
 
+def make_loggers():
+    """The izh_net case with EDEN's extended loggers (cases.add_eden_loggers)."""
+    with tempfile.TemporaryDirectory() as d:
+        lems = neuroml_io.write_lems(spec_of("izh_net"), d)
+        add_eden_loggers(lems)
+        keep = os.path.join(d, "run")
+        os.makedirs(keep)
+        reference_runner.run(lems, threads=4, keep_dir=keep)
+        texts = {os.path.splitext(f)[0]: open(os.path.join(keep, f)).read() for f in LOGGER_FILES}
+    np.savez_compressed(os.path.join(HERE, "loggers.npz"), **texts)
+    print("loggers:", {k: len(v.splitlines()) for k, v in texts.items()})
+
+
 if __name__ == "__main__":
     if not reference_runner.available():
         sys.exit("oracle/_ref/eden is not built (make -C oracle ref)")
-    for name in (sys.argv[1:] or list(CASES)):
-        make(name)
+    names = sys.argv[1:] or list(CASES) + ["loggers"]
+    for name in names:
+        make_loggers() if name == "loggers" else make(name)

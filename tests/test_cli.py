@@ -14,13 +14,15 @@ import pytest
 import eden_port
 from eden_gb300 import cli, lowering, neuroml_io
 from eden_gb300.engine import Records
-from golden.cases import CASES, spec_of
+from golden.cases import CASES, LOGGER_FILES, add_eden_loggers, spec_of
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def _write_from_oracle(name, tmp_path):
+def _write_from_oracle(name, tmp_path, extended=False):
     lems = neuroml_io.write_lems(spec_of(name), str(tmp_path))
+    if extended:
+        add_eden_loggers(lems)
     spec = neuroml_io.read_lems(lems)
     low = lowering.lower(spec)
     out = eden_port.run(low)
@@ -65,10 +67,10 @@ def test_output_files_match_reference_layout(name, tmp_path):
 def test_reload_saved_data(tmp_path):
     lems, spec, files = _write_from_oracle("izh_net", tmp_path)
     traces, events = cli.reload_saved_data(lems, reload_events=True)
-    quantities = [c[1] for _id, _f, cols in spec.output_files for c in cols]
+    quantities = [c[1] for of in spec.output_files for c in of["cols"]]
     assert set(traces) == {"t", *quantities}
     assert np.all(np.diff(traces["t"]) > 0)
-    sels = [s[1] for _id, _f, _fmt, ss in spec.event_files for s in ss]
+    sels = [s[1] for ef in spec.event_files for s in ef["sels"]]
     assert set(events) == set(sels)
     assert sum(len(v) for v in events.values()) == len(open(files[1]).read().splitlines())
 
@@ -90,3 +92,38 @@ def test_command_line_rejects_unknown_tokens(capsys):
     assert cli.main(["nml", "x.xml", "bogus_token"]) == 2
     assert cli.main([]) == 2
     assert cli.main(["nml", "x.xml", "cable_solver", "fwd_euler"]) == 2
+
+
+def test_extended_loggers_match_reference(tmp_path):
+    """EdenOutputFile (time window and sampling interval; explicit sample
+    points; output_units) and EdenEventOutputFile (ascii_v0 with a time window
+    and heartbeat frames; ID_TIME) written from the oracle's records against
+    the reference's own files for the same LEMS input: events line for line,
+    timestamps character for character, values within 1e-3 of their units."""
+    lems, spec, files = _write_from_oracle("izh_net", tmp_path, extended=True)
+    z = np.load(os.path.join(HERE, "golden", "loggers.npz"))
+    for f in LOGGER_FILES:
+        mine = open(os.path.join(str(tmp_path), f)).read().splitlines()
+        ref = str(z[os.path.splitext(f)[0]]).splitlines()
+        assert len(mine) == len(ref), f
+        if f.startswith("ev"):
+            assert mine == ref, f
+        else:
+            assert [l[:16] for l in mine] == [l[:16] for l in ref], f
+            a = np.array([[float(x) for x in l.split()] for l in mine])
+            b = np.array([[float(x) for x in l.split()] for l in ref])
+            np.testing.assert_allclose(a, b, rtol=0, atol=1e-3)
+    traces, events = cli.reload_saved_data(lems, reload_events=True)
+    assert sum(len(v) for v in events.values()) > 0
+
+
+def test_logger_sampling_rules():
+    times = np.arange(0, 101) * 100.0  # us of steps 0..100 (synthetic: step k at 100 k)
+    steps = np.arange(1, 101)          # the step of each recorded row
+    of = {"points": None, "start": 1000.0, "end": 3000.0, "interval": 500.0}
+    assert [t for t, _ in cli.trajectory_frames(of, times, steps)] == [1000.0, 1500.0, 2000.0, 2500.0]
+    of = {"points": [0.0, 250.0, 250.0, 9999.0]}
+    assert cli.trajectory_frames(of, times, steps) == [(0.0, 0), (250.0, 2), (250.0, 2), (9999.0, 99)]
+    ef = {"start": 0.0, "end": 1000.0, "max_interval": 300.0}
+    fr = cli.event_frames(ef, times, 1, 100, {4: [2, 5]})
+    assert fr == [(100.0, []), (400.0, [2, 5]), (700.0, [])]
