@@ -29,6 +29,7 @@ using namespace eden;
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kInputThreads = 128;  // k_inputs_t: four warps, each with two event tiles
 constexpr int kCellThreads = 128;   // k_cells_t: four warps
 constexpr int kHinesThreads = 128;  // k_hines_t: four warps, each staging one forest
 constexpr int kForestNodes = 512;   // largest forest (a larger cell gets a forest of its own)
@@ -55,6 +56,8 @@ struct EdenGpuCtx {
     int n_target = 0, n_comp_user = 0, n_izh = 0;
     std::vector<int32_t> user_to_internal;   // user target -> internal target
     std::vector<int64_t> syn_internal_of_user;  // user synapse -> internal synapse
+    std::vector<uint8_t> h_sy_type;             // internal synapse -> synapse type
+    std::vector<SynTypeDev> h_syn_types;
     int64_t n_syn = 0;
     // run state
     int64_t next_step = -3;
@@ -117,8 +120,8 @@ namespace eden {
 
 // Phase 1 of both paths: input blocks over the window, one warp per target
 // with inputs (the per-step path runs it with K = 1).
-__global__ void __launch_bounds__(256, 3) k_inputs_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
-    __shared__ float tiles[8][32 * kAccStride];
+__global__ void __launch_bounds__(kInputThreads) k_inputs_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
+    __shared__ float tiles[kInputThreads / 32][2][32 * kAccStride];
     __shared__ float tk[32];
     const WindowArgs w = tab[*base + idx];
     if (threadIdx.x < 32) {
@@ -131,8 +134,8 @@ __global__ void __launch_bounds__(256, 3) k_inputs_t(DevModel m, const WindowArg
     __syncthreads();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    float *tile = tiles[threadIdx.x >> 5];
-    for (int c = warp; c < m.n_chunk; c += nwarps) chunk_window(m, c, w, tile, tk);
+    float *tileA = tiles[threadIdx.x >> 5][0], *tileB = tiles[threadIdx.x >> 5][1];
+    for (int c = warp; c < m.n_chunk; c += nwarps) chunk_window(m, c, w, tileA, tileB, tk);
 }
 
 // Per-step path, phase 2: one thread per target.
@@ -1248,6 +1251,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.bk_c0, bk_c0)); TRY(upload_c(ctx, &d.ck_blk, ck_blk));
     TRY(upload_c(ctx, &d.ck_i0, ck_i0)); TRY(upload_c(ctx, &d.ck_n, ck_n));
     TRY(upload(ctx, &d.Gp, (const float *)nullptr, (size_t)32 * (size_t)std::max(n_chunk, 1)));
+    TRY(upload(ctx, &d.ck_a, (const float *)nullptr, (size_t)std::max(n_chunk, 1)));
+    TRY(upload(ctx, &d.ck_b, (const float *)nullptr, (size_t)std::max(n_chunk, 1)));
     TRY(upload_c(ctx, &d.c_chan0, c_chan0)); TRY(upload_c(ctx, &d.ch_type, ch_type));
     TRY(upload_c(ctx, &d.ch_gate0, ch_gate0)); TRY(upload_c(ctx, &d.ch_gbase, ch_g)); TRY(upload_c(ctx, &d.ch_erev, ch_e));
     TRY(upload(ctx, &d.gate, (const float *)nullptr, (size_t)n_gate));
@@ -1260,15 +1265,18 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload(ctx, &d.po_isi, (const float *)nullptr, (size_t)m->n_pois));
     TRY(upload(ctx, &d.po_a, (const float *)nullptr, (size_t)m->n_pois));
     TRY(upload(ctx, &d.po_b, (const float *)nullptr, (size_t)m->n_pois));
+    TRY(upload(ctx, &d.po_last, (const int32_t *)nullptr, (size_t)m->n_pois));
     TRY(upload_c(ctx, &d.po_rate, po_rate)); TRY(upload_c(ctx, &d.po_w, po_w));
     TRY(upload_c(ctx, &d.po_seed, po_seed)); TRY(upload_c(ctx, &d.po_inst, po_inst));
     TRY(upload_c(ctx, &d.po_type, po_type));
     TRY(upload(ctx, &d.sy_a, (const float *)nullptr, (size_t)ns));
     TRY(upload(ctx, &d.sy_b, (const float *)nullptr, (size_t)ns));
+    TRY(upload(ctx, &d.sy_last, (const int32_t *)nullptr, (size_t)ns));
     TRY(upload_vec(ctx, &d.sy_pend, sy_pend));
     TRY(upload(ctx, &d.sy_mask, (const uint32_t *)nullptr, (size_t)ns));
     TRY(upload_c(ctx, &d.sy_w, sy_w)); TRY(upload_c(ctx, &d.sy_delay, sy_d));
     TRY(upload_c(ctx, &d.sy_type, sy_type));
+    ctx->h_sy_type = sy_type;
     TRY(upload_c(ctx, &d.t_src, t_src)); TRY(upload_c(ctx, &d.src_thr, src_thr));
     TRY(upload_c(ctx, &d.fan0, fan0)); TRY(upload_c(ctx, &d.fan_syn, fan_syn));
     // a source spikes at most once per step: a window list never exceeds n_src * K
@@ -1324,16 +1332,20 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         st[k].wf_w = s.weight_prop * s.waveform_factor;
         st[k].r_decay = 1.0f / s.tau_decay;
         st[k].r_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f / s.tau_rise : 1.0f;
+        st[k].f_decay = 1.0f - dt / s.tau_decay;
+        st[k].f_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f - dt / s.tau_rise : 1.0f;
     }
     CUDA_TRY(ctx, cudaMemcpyToSymbol(c_chan_types, ct, sizeof(ct)));
     CUDA_TRY(ctx, cudaMemcpyToSymbol(c_syn_types, st, sizeof(st)));
+    ctx->h_syn_types.assign(st, st + kMaxSynTypes);
 
     // ---- launch shapes
     auto blocks_for = [&](int64_t n) {
         int64_t b = (n + kThreads - 1) / kThreads;
         return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)ctx->n_sm * 32));
     };
-    ctx->grid_inputs = blocks_for((int64_t)n_chunk * 32);
+    ctx->grid_inputs = (int)std::max<int64_t>(
+        1, std::min<int64_t>(((int64_t)n_chunk * 32 + kInputThreads - 1) / kInputThreads, (int64_t)ctx->n_sm * 64));
     ctx->grid_targets = blocks_for(nt);
     ctx->grid_hines = (int)std::max<int64_t>(1, ((int64_t)d.n_forest * 32 + kHinesThreads - 1) / kHinesThreads);
     ctx->grid_deliver = ctx->n_sm * 4;
@@ -1449,7 +1461,7 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     cudaStream_t s = ctx->stream;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
         tmark(ctx, EDEN_KERNEL_INPUTS, true);
-        k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
         tmark(ctx, EDEN_KERNEL_INPUTS, false);
         int n = 1;
         tmark(ctx, EDEN_KERNEL_CELLS, true);
@@ -1466,7 +1478,7 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     }
     (void)K;
     tmark(ctx, EDEN_KERNEL_INPUTS, true);
-    k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
     tmark(ctx, EDEN_KERNEL_INPUTS, false);
     tmark(ctx, EDEN_KERNEL_TARGETS, true);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
@@ -1664,13 +1676,23 @@ extern "C" int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *st
     if (n != ctx->n_syn) return ctx->fail(EDEN_GPU_E_RANGE, "expected %lld synapses", (long long)ctx->n_syn);
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    std::vector<float> tmp(std::max<int64_t>(n, 1));
-    float *outs[3] = {pending_us, state_a, state_b};
-    float *srcs[3] = {ctx->d.sy_pend, ctx->d.sy_a, ctx->d.sy_b};
-    for (int k = 0; k < 3; k++) {
-        if (!outs[k] || n == 0) continue;
-        CUDA_TRY(ctx, cudaMemcpy(tmp.data(), srcs[k], sizeof(float) * n, cudaMemcpyDeviceToHost));
-        for (int64_t u = 0; u < n; u++) outs[k][u] = tmp[ctx->syn_internal_of_user[u]];
+    if (n == 0) return 0;
+    std::vector<float> pend(n), a(n), b(n);
+    std::vector<int32_t> last(n);
+    CUDA_TRY(ctx, cudaMemcpy(pend.data(), ctx->d.sy_pend, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(ctx, cudaMemcpy(a.data(), ctx->d.sy_a, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(ctx, cudaMemcpy(b.data(), ctx->d.sy_b, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(ctx, cudaMemcpy(last.data(), ctx->d.sy_last, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    // each synapse keeps its state as of its last event; decay it to the
+    // start of the next step the way the kernel does for its next event
+    for (int64_t u = 0; u < n; u++) {
+        const int64_t k = ctx->syn_internal_of_user[u];
+        const SynTypeDev &st = ctx->h_syn_types[ctx->h_sy_type[k]];
+        const int64_t steps = std::max<int64_t>(0, ctx->next_step - (int64_t)last[k] - 1);
+        const bool two = st.kind == EDEN_SYN_EXPTWO;
+        if (pending_us) pending_us[u] = pend[k];
+        if (state_a) state_a[u] = steps > 0 ? a[k] * powf(two ? st.f_rise : st.f_decay, (float)steps) : a[k];
+        if (state_b) state_b[u] = two ? (steps > 0 ? b[k] * powf(st.f_decay, (float)steps) : b[k]) : 0.0f;
     }
     return 0;
 }
@@ -1740,7 +1762,7 @@ static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const Windo
     cudaStream_t s = ctx->stream;
     const int *zero = ctx->d_zero;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
-        k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(dm, tab, zero, idx);
+        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, zero, idx);
         int n = 1;
         for (const auto &cl : ctx->classes) {
             const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
@@ -1750,7 +1772,7 @@ static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const Windo
         k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);
         return n + 1;
     }
-    k_inputs_t<<<ctx->grid_inputs, kThreads, 0, s>>>(dm, tab, zero, idx);
+    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, zero, idx);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(dm, tab, zero, idx);
     k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(dm, tab, zero, idx, ctx->forest_cap);
     k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);

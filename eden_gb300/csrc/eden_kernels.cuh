@@ -39,6 +39,7 @@ struct SynTypeDev {
     int kind;
     float gbase, erev, tau_decay, tau_rise, wf_w;  // wf_w = weight_prop * waveform_factor
     float r_decay, r_rise;                          // correctly rounded 1 / tau
+    float f_decay, f_rise;                          // 1 - dt / tau, one step's decay factor
 };
 
 // x / tau, correctly rounded, from r = RN(1/tau): q = RN(x*r) is within an
@@ -117,14 +118,17 @@ struct DevModel {
     const int64_t *ck_i0;             // first item of each chunk
     const int32_t *ck_n;              // items in the chunk
     float *Gp;                        // [32 * n_chunk]
+    float *ck_a, *ck_b;               // aggregate synapse state of each chunk (weighted sums)
     const float *pu_start, *pu_dur, *pu_amp, *pu_w;
     // Poisson inputs
-    float *po_ts, *po_isi, *po_a, *po_b;
+    float *po_ts, *po_isi, *po_a, *po_b;  // po_a/po_b: own synapse state just after its last event
+    int32_t *po_last;                      // step of that event
     const float *po_rate, *po_w;
     const int32_t *po_seed, *po_inst;
     const uint8_t *po_type;
     // connection synapses
-    float *sy_a, *sy_b, *sy_pend;
+    float *sy_a, *sy_b, *sy_pend;     // sy_a/sy_b: state just after the synapse's last event
+    int32_t *sy_last;                 // step of that event
     uint32_t *sy_mask;
     const float *sy_w, *sy_delay;
     const uint8_t *sy_type;
@@ -235,41 +239,6 @@ __device__ __forceinline__ void push_spike(const DevModel &m, bool spiked, int32
 // ---------------------------------------------------------------------------
 // synapses and inputs
 // ---------------------------------------------------------------------------
-// State update + exposure of expOne (native, eden/Eden.cpp:3424-3466) or
-// expTwo (LEMS forward Euler; OnEvent replaces the decay on that step).
-// The decay keeps the reference's correctly rounded quotient -x / tau (a
-// plain product with 1 / tau differs by an ulp, enough to move a spike of a
-// recurrent network); div_by_tau computes it without a hardware division.
-template <int KIND>
-__device__ __forceinline__ float synapse_dyn_k(const SynTypeDev &st, bool init, float dt, bool fire, float w,
-                                               float &a, float &b) {
-    if (KIND == EDEN_SYN_EXPONE) {
-        float g = a;
-        if (!init) {
-            float an = a - dt * div_by_tau(a, st.tau_decay, st.r_decay);
-            if (fire) an = a + st.gbase;
-            a = an;
-        }
-        return g * w;
-    } else {
-        float g = st.gbase * (b - a);
-        if (init) {
-            a = 0.0f;
-            b = 0.0f;
-        } else {
-            float an = a + dt * div_by_tau(-a, st.tau_rise, st.r_rise);
-            float bn = b + dt * div_by_tau(-b, st.tau_decay, st.r_decay);
-            if (fire) {
-                an = a + st.wf_w;
-                bn = b + st.wf_w;
-            }
-            a = an;
-            b = bn;
-        }
-        return g * w;
-    }
-}
-
 // Pending-spike rule for a trigger read at time t (eden/Eden.cpp:3646-3686):
 // fire now if t <= t+delay < t+dt; keep it as the single pending spike only if
 // the old one is already due (pend < t+dt) and earlier than the new one.
@@ -293,124 +262,224 @@ __device__ __forceinline__ bool replay_mask(uint32_t mask, const WindowArgs &w, 
     return (mask >> w.Kprev) & 1u;
 }
 
-// Per-warp accumulation tile: row `lane` (stride kAccStride, padded so that
-// both a row write and a column read are free of bank conflicts) holds the
-// lane's partial sum for each step of the window.
-constexpr int kAccStride = 33;
+// ---------------------------------------------------------------------------
+// input chunks: event-driven synapses with an aggregate state per chunk
+// ---------------------------------------------------------------------------
+// expOne and expTwo synapses are linear between events, so the weighted sum
+// of a chunk's synapse states obeys the same update as one synapse (expOne
+// G' = G - dt*G/tau, eden/Eden.cpp:3424-3466; expTwo A' = A - dt*A/tau_rise,
+// B' = B - dt*B/tau_decay, LEMS_CoreComponents.inc.xml:145-180) and the
+// chunk's conductance is its exposure (G, or gbase*(B - A)).  A synapse only
+// costs work when it fires.  On that step the reference replaces the
+// synapse's decay by the jump (G += gbase; A, B += weight_prop*wf), so the
+// aggregate gets back the decay it applied to that synapse plus the jump,
+// both times its weight.  For that the synapse keeps its own state as of its
+// last event and the step of that event.
 
-// Row update of the accumulation tile: the lane's first item of a chunk
-// writes its term, later items add theirs.
-__device__ __forceinline__ void row_put(float *row, int j, float term, bool acc) {
-    row[j] = acc ? row[j] + term : term;
+// A synapse's own state at the start of step s from its value just after its
+// event at step `last`: the reference's per-step a - dt*(a/tau), in closed
+// form a * f^n with f = 1 - dt/tau (used only for the decay its event replaces).
+__device__ __forceinline__ float decayed(float a, float f, int n) {
+    return n > 0 ? a * powf(f, (float)n) : a;
 }
 
-// Poisson input `it` over the K steps of a window; adds its step-j term to row[j].
+// The contribution (dA, dB) of one synapse's event at step s to its chunk's
+// aggregate, and the synapse's own state after it.
 template <int KIND>
-__device__ __forceinline__ void pois_steps(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
-                                           float *row, bool acc) {
+__device__ __forceinline__ void input_event(const SynTypeDev &st, float dt, float w, int64_t s, float &a, float &b,
+                                            int32_t &last, float &dA, float &dB) {
+    const int n = (int)(s - (int64_t)last) - 1;
+    if (KIND == EDEN_SYN_EXPTWO) {
+        const float ai = decayed(a, st.f_rise, n), bi = decayed(b, st.f_decay, n);
+        dA = w * (dt * div_by_tau(ai, st.tau_rise, st.r_rise) + st.wf_w);
+        dB = w * (dt * div_by_tau(bi, st.tau_decay, st.r_decay) + st.wf_w);
+        a = ai + st.wf_w;
+        b = bi + st.wf_w;
+    } else {
+        const float gi = decayed(a, st.f_decay, n);
+        dA = w * (dt * div_by_tau(gi, st.tau_decay, st.r_decay) + st.gbase);
+        dB = 0.0f;
+        a = gi + st.gbase;
+    }
+    last = (int32_t)s;
+}
+
+// Adds an event at window step j to the lane's rows of the event tiles,
+// clearing the rows on the lane's first event of the window.
+__device__ __forceinline__ void put_event(float *rowA, float *rowB, bool &used, int K, int j, float dA, float dB) {
+    if (!used) {
+        for (int q = 0; q < K; q++) { rowA[q] = 0.0f; rowB[q] = 0.0f; }
+        used = true;
+    }
+    rowA[j] += dA;
+    rowB[j] += dB;
+}
+
+// Poisson input `it` over the K steps of a window (poissonFiringSynapse,
+// LEMS_CoreComponents.inc.xml:623-672): initialisation draws the first
+// interval at each init step; afterwards the input fires its own synapse on
+// the step its time since the last spike exceeds the interval, and draws the
+// next interval.
+template <int KIND>
+__device__ __forceinline__ void pois_window(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
+                                            float *rowA, float *rowB, bool &used) {
     const float dt = m.dt;
-    float ts = m.po_ts[it], isi = m.po_isi[it], a = m.po_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.po_b[it] : 0.0f;
-    const float wt = m.po_w[it];
+    float ts = m.po_ts[it], isi = m.po_isi[it];
     if (w.step0 <= 0) {
         for (int j = 0; j < w.K; j++) {
             ts = 0.0f;
             isi = (-(1.0f / m.po_rate[it])) *
                   logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], w.step0 + j, 0));
-            row_put(row, j, synapse_dyn_k<KIND>(st, true, dt, false, wt, a, b), acc);
         }
     } else {
         for (int j = 0; j < w.K; j++) {
-            const bool fired = ts > isi;
-            if (fired) {
+            if (ts > isi) {
                 ts = 0.0f;
                 isi = (-(1.0f / m.po_rate[it])) *
                       logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], w.step0 + j, 1));
+                float a = m.po_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.po_b[it] : 0.0f;
+                int32_t last = m.po_last[it];
+                float dA, dB;
+                input_event<KIND>(st, dt, m.po_w[it], w.step0 + j, a, b, last, dA, dB);
+                m.po_a[it] = a;
+                if (KIND == EDEN_SYN_EXPTWO) m.po_b[it] = b;
+                m.po_last[it] = last;
+                put_event(rowA, rowB, used, w.K, j, dA, dB);
             } else {
                 ts = ts + dt * 1.0f;
             }
-            row_put(row, j, synapse_dyn_k<KIND>(st, false, dt, fired, wt, a, b), acc);
         }
     }
-    m.po_ts[it] = ts; m.po_isi[it] = isi; m.po_a[it] = a;
-    if (KIND == EDEN_SYN_EXPTWO) m.po_b[it] = b;
+    m.po_ts[it] = ts;
+    m.po_isi[it] = isi;
 }
 
-// Connection synapse `it` over the K steps of a window: replay the previous
-// window's triggers, then each step fires the pending spike when it falls
-// due (eden/Eden.cpp:3646-3686); adds its step-j term to row[j].
+// Connection synapse `it` over the window: replay the previous window's
+// triggers (replay_mask), then fire the single pending spike on the step
+// whose interval holds it (eden/Eden.cpp:3646-3686).  That step is in this
+// window for at most one pending spike: a trigger replaces the pending
+// spike only once it is due, and a spike read at the first step lands at
+// least K steps later.  The first step's trigger fires at once only for a
+// delay below dt.
 template <int KIND>
-__device__ __forceinline__ void synapse_steps(const DevModel &m, int64_t it, const WindowArgs &w,
-                                              const SynTypeDev &st, const float *tk, float *row, bool acc) {
+__device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
+                                           const float *tk, float *rowA, float *rowB, bool &used) {
+    if (w.step0 <= 0) return;  // no spikes reach a synapse during initialisation
     const float dt = m.dt;
-    const bool init = w.step0 <= 0;
-    float pend = m.sy_pend[it], a = m.sy_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.sy_b[it] : 0.0f;
-    const float wt = m.sy_w[it];
+    float pend = m.sy_pend[it];
     const float pend0 = pend;
     bool trig = false;
-    if (!init) {
-        const uint32_t mask = m.sy_mask[it];
-        if (mask) {
-            m.sy_mask[it] = 0;
-            trig = replay_mask(mask, w, dt, m.sy_delay[it], pend);
-        }
+    float delay = 0.0f;
+    const uint32_t mask = m.sy_mask[it];
+    if (mask) {
+        m.sy_mask[it] = 0;
+        delay = m.sy_delay[it];
+        trig = replay_mask(mask, w, dt, delay, pend);
     }
-    for (int j = 0; j < w.K; j++) {
-        const float t = tk[j];
-        bool fire = false;
-        if (!init) {
-            // the pending spike falls due before a trigger of this step may replace it
-            fire = (t <= pend && pend < t + dt);
-            if (j == 0 && trig && trigger_arrival(t, dt, m.sy_delay[it], pend)) fire = true;
-        }
-        row_put(row, j, synapse_dyn_k<KIND>(st, init, dt, fire, wt, a, b), acc);
-    }
+    int jf = -1;
+    if (pend >= tk[0] && pend < tk[w.K - 1] + dt)
+        for (int j = 0; j < w.K; j++)
+            if (tk[j] <= pend && pend < tk[j] + dt) { jf = j; break; }
+    bool now = false;
+    if (trig) now = trigger_arrival(tk[0], dt, delay, pend);
     if (pend != pend0) m.sy_pend[it] = pend;
+    if (jf < 0 && !now) return;
+    float a = m.sy_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.sy_b[it] : 0.0f;
+    int32_t last = m.sy_last[it];
+    const float wt = m.sy_w[it];
+    float dA, dB;
+    if (now && jf != 0) {
+        input_event<KIND>(st, dt, wt, w.step0, a, b, last, dA, dB);
+        put_event(rowA, rowB, used, w.K, 0, dA, dB);
+    }
+    if (jf >= 0) {
+        input_event<KIND>(st, dt, wt, w.step0 + jf, a, b, last, dA, dB);
+        put_event(rowA, rowB, used, w.K, jf, dA, dB);
+    }
     m.sy_a[it] = a;
     if (KIND == EDEN_SYN_EXPTWO) m.sy_b[it] = b;
+    m.sy_last[it] = last;
 }
 
+// Per-warp accumulation tiles: row `lane` (stride kAccStride, padded so that
+// both a row write and a column read are free of bank conflicts) holds the
+// lane's terms for each step of the window.
+constexpr int kAccStride = 33;
+
 // One chunk (at most kChunkItems items of one input block) over the K steps
-// of a window.  Lane l handles items l, l + 32, ... with their state in
-// registers and accumulates their step-j terms in row l of the warp's tile;
-// lane j then sums column j over the rows in a fixed order into
-// Gp[j][chunk].  Terms are g*w (the conductance before the step's update, as
-// the reference exposes it) for Poisson inputs and synapses, and the current
-// for pulses.
-__device__ __forceinline__ void chunk_window(const DevModel &m, int c, const WindowArgs &w, float *tile,
-                                             const float *tk) {
+// of a window, lane l handling items l, l + 32, ...  Pulses add their
+// current to row l of tile A, and lane j sums column j in row order into
+// Gp[j][chunk].  Synapses and Poisson inputs add their events to the tiles;
+// lane j sums step j's events over the rows in row order, and every lane then
+// steps the chunk's aggregate state through the window, lane j keeping the
+// exposure of step j (the conductance before the step's update, as the
+// reference exposes it) for Gp[j][chunk].
+__device__ __forceinline__ void chunk_window(const DevModel &m, int c, const WindowArgs &w, float *tileA,
+                                             float *tileB, const float *tk) {
     const int lane = threadIdx.x & 31;
     const int bk = m.ck_blk[c];
     const int kind = m.bk_kind[bk];
     const int n = m.ck_n[c];
-    float *row = tile + lane * kAccStride;
-    for (int r = 0; lane + 32 * r < n; r++) {
-        const int64_t it = m.ck_i0[c] + lane + 32 * r;
-        const bool acc = r > 0;
-        if (kind == BK_PULSE) {
+    float *rowA = tileA + lane * kAccStride, *rowB = tileB + lane * kAccStride;
+    if (kind == BK_PULSE) {
+        for (int r = 0; lane + 32 * r < n; r++) {
+            const int64_t it = m.ck_i0[c] + lane + 32 * r;
             const float st = m.pu_start[it], du = m.pu_dur[it], aw = m.pu_amp[it] * m.pu_w[it];
             for (int j = 0; j < w.K; j++) {
                 const float tf = tk[j];
-                row_put(row, j, (st <= tf && tf <= st + du) ? aw : 0.0f, acc);
+                const float term = (st <= tf && tf <= st + du) ? aw : 0.0f;
+                rowA[j] = r > 0 ? rowA[j] + term : term;
             }
-        } else if (kind == BK_POIS) {
-            // poissonFiringSynapse (LEMS_CoreComponents.inc.xml:623-672): the
-            // spiker fires its own synapse instance on the step its OnCondition holds
-            const SynTypeDev st = c_syn_types[m.bk_type[bk]];
-            if (st.kind == EDEN_SYN_EXPTWO) pois_steps<EDEN_SYN_EXPTWO>(m, it, w, st, row, acc);
-            else pois_steps<EDEN_SYN_EXPONE>(m, it, w, st, row, acc);
+        }
+        __syncwarp();
+        if (lane < w.K) {
+            const int rows = n < 32 ? n : 32;
+            float tot = 0.0f;
+            for (int r = 0; r < rows; r++) tot += tileA[r * kAccStride + lane];
+            m.Gp[(size_t)lane * m.n_chunk + c] = tot;
+        }
+        __syncwarp();
+        return;
+    }
+    const SynTypeDev st = c_syn_types[m.bk_type[bk]];
+    const bool two = st.kind == EDEN_SYN_EXPTWO;
+    bool used = false;
+    for (int r = 0; lane + 32 * r < n; r++) {
+        const int64_t it = m.ck_i0[c] + lane + 32 * r;
+        if (kind == BK_POIS) {
+            if (two) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, rowA, rowB, used);
+            else pois_window<EDEN_SYN_EXPONE>(m, it, w, st, rowA, rowB, used);
         } else {
-            const SynTypeDev st = c_syn_types[m.bk_type[bk]];
-            if (st.kind == EDEN_SYN_EXPTWO) synapse_steps<EDEN_SYN_EXPTWO>(m, it, w, st, tk, row, acc);
-            else synapse_steps<EDEN_SYN_EXPONE>(m, it, w, st, tk, row, acc);
+            if (two) syn_window<EDEN_SYN_EXPTWO>(m, it, w, st, tk, rowA, rowB, used);
+            else syn_window<EDEN_SYN_EXPONE>(m, it, w, st, tk, rowA, rowB, used);
         }
     }
+    const unsigned rows = __ballot_sync(0xffffffffu, used);
     __syncwarp();
-    if (lane < w.K) {
-        const int rows = n < 32 ? n : 32;
-        float tot = 0.0f;
-        for (int r = 0; r < rows; r++) tot += tile[r * kAccStride + lane];
-        m.Gp[(size_t)lane * m.n_chunk + c] = tot;
+    float ea = 0.0f, eb = 0.0f;  // lane j: the chunk's events of step j
+    if (lane < w.K)
+        for (unsigned r = rows; r; r &= r - 1) {
+            const int q = __ffs(r) - 1;
+            ea += tileA[q * kAccStride + lane];
+            eb += tileB[q * kAccStride + lane];
+        }
+    const float dt = m.dt;
+    float A = m.ck_a[c], B = m.ck_b[c], gj = 0.0f;
+    for (int j = 0; j < w.K; j++) {
+        const float eaj = __shfl_sync(0xffffffffu, ea, j), ebj = __shfl_sync(0xffffffffu, eb, j);
+        const float g = two ? st.gbase * (B - A) : A;
+        if (lane == j) gj = g;
+        if (w.step0 + j <= 0) {
+            if (two) { A = 0.0f; B = 0.0f; }
+        } else if (two) {
+            A = A - dt * div_by_tau(A, st.tau_rise, st.r_rise) + eaj;
+            B = B - dt * div_by_tau(B, st.tau_decay, st.r_decay) + ebj;
+        } else {
+            A = A - dt * div_by_tau(A, st.tau_decay, st.r_decay) + eaj;
+        }
     }
+    if (lane < w.K) m.Gp[(size_t)lane * m.n_chunk + c] = gj;
+    if (lane == 0) { m.ck_a[c] = A; m.ck_b[c] = B; }
     __syncwarp();
 }
 
