@@ -1235,6 +1235,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     d.n_block = n_block;
     d.n_chunk = n_chunk;
     d.n_syn = ns; d.n_pois = m->n_pois; d.dt = dt;
+    d.pois_exact = (dt == std::floor(dt) && dt <= 1048576.0f) ? 1 : 0;
     TRY(upload_vec(ctx, &d.v[0], v0));
     TRY(upload_vec(ctx, &d.v[1], v0));
     TRY(upload(ctx, &d.diag, (const float *)nullptr, nt));
@@ -1338,6 +1339,16 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     CUDA_TRY(ctx, cudaMemcpyToSymbol(c_chan_types, ct, sizeof(ct)));
     CUDA_TRY(ctx, cudaMemcpyToSymbol(c_syn_types, st, sizeof(st)));
     ctx->h_syn_types.assign(st, st + kMaxSynTypes);
+    // powers of each decay factor for windows without events
+    {
+        std::vector<float> pw((size_t)kMaxSynTypes * 2 * kPowLen, 0.0f);
+        for (int k = 0; k < kMaxSynTypes; k++)
+            for (int j = 0; j < kPowLen; j++) {
+                pw[((size_t)k * 2 + 0) * kPowLen + j] = (float)std::pow((double)st[k].f_rise, j);
+                pw[((size_t)k * 2 + 1) * kPowLen + j] = (float)std::pow((double)st[k].f_decay, j);
+            }
+        TRY(upload_c(ctx, &ctx->d.syn_pow, pw));
+    }
 
     // ---- launch shapes
     auto blocks_for = [&](int64_t n) {

@@ -68,6 +68,7 @@ enum : int { ST_OK = 0, ST_LOG_OVERFLOW = 1 };
 enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2 };
 constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
 constexpr int kChunkItems = 128; // input items per chunk (one warp, up to four per lane)
+constexpr int kPowLen = 33;      // powers 0..32 of a synapse decay factor
 
 struct DevModel {
     int32_t n_target, n_src, n_group, n_forest, n_in;
@@ -118,6 +119,8 @@ struct DevModel {
     const int64_t *ck_i0;             // first item of each chunk
     const int32_t *ck_n;              // items in the chunk
     float *Gp;                        // [32 * n_chunk]
+    const float *syn_pow;             // per synapse type: f_rise^j, then f_decay^j, j < kPowLen
+    int32_t pois_exact;               // dt is a whole number of us: Poisson clocks advance exactly
     float *ck_a, *ck_b;               // aggregate synapse state of each chunk (weighted sums)
     const float *pu_start, *pu_dur, *pu_amp, *pu_w;
     // Poisson inputs
@@ -318,33 +321,63 @@ __device__ __forceinline__ void put_event(float *rowA, float *rowB, bool &used, 
 // Poisson input `it` over the K steps of a window (poissonFiringSynapse,
 // LEMS_CoreComponents.inc.xml:623-672): initialisation draws the first
 // interval at each init step; afterwards the input fires its own synapse on
-// the step its time since the last spike exceeds the interval, and draws the
-// next interval.
+// the step its time since the last spike exceeds the interval (then restarts
+// that time at 0 and draws the next interval), else adds dt to it.  When dt
+// is a whole number of us and the times stay below 2^24 us, every such sum
+// is exact, so the firing step is found directly instead of step by step.
+__device__ __forceinline__ float pois_draw(const DevModel &m, int64_t it, int64_t step, int invocation) {
+    return (-(1.0f / m.po_rate[it])) * logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], step, invocation));
+}
+
+template <int KIND>
+__device__ __forceinline__ void pois_fire(const DevModel &m, int64_t it, const SynTypeDev &st, int64_t s, int j, int K,
+                                          float *rowA, float *rowB, bool &used) {
+    float a = m.po_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.po_b[it] : 0.0f;
+    int32_t last = m.po_last[it];
+    float dA, dB;
+    input_event<KIND>(st, m.dt, m.po_w[it], s, a, b, last, dA, dB);
+    m.po_a[it] = a;
+    if (KIND == EDEN_SYN_EXPTWO) m.po_b[it] = b;
+    m.po_last[it] = last;
+    put_event(rowA, rowB, used, K, j, dA, dB);
+}
+
 template <int KIND>
 __device__ __forceinline__ void pois_window(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
-                                            float *rowA, float *rowB, bool &used) {
+                                            float ts, float isi, float *rowA, float *rowB, bool &used) {
     const float dt = m.dt;
-    float ts = m.po_ts[it], isi = m.po_isi[it];
     if (w.step0 <= 0) {
         for (int j = 0; j < w.K; j++) {
             ts = 0.0f;
-            isi = (-(1.0f / m.po_rate[it])) *
-                  logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], w.step0 + j, 0));
+            isi = pois_draw(m, it, w.step0 + j, 0);
+        }
+    } else if (m.pois_exact && isi < 0x1p23f) {
+        int j = 0;
+        while (true) {
+            // first step from j on whose time since the last spike exceeds isi
+            int jn = 0;
+            if (!(ts > isi)) {
+                jn = (int)floorf((isi - ts) / dt) + 1;
+                while (jn > 1 && ts + (float)(jn - 1) * dt > isi) jn--;
+                while (!(ts + (float)jn * dt > isi)) jn++;
+            }
+            if (j + jn >= w.K) {
+                ts = ts + (float)(w.K - j) * dt;
+                break;
+            }
+            j += jn;
+            isi = pois_draw(m, it, w.step0 + j, 1);
+            pois_fire<KIND>(m, it, st, w.step0 + j, j, w.K, rowA, rowB, used);
+            ts = 0.0f;
+            j += 1;
+            if (j >= w.K) break;
         }
     } else {
         for (int j = 0; j < w.K; j++) {
             if (ts > isi) {
                 ts = 0.0f;
-                isi = (-(1.0f / m.po_rate[it])) *
-                      logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], w.step0 + j, 1));
-                float a = m.po_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.po_b[it] : 0.0f;
-                int32_t last = m.po_last[it];
-                float dA, dB;
-                input_event<KIND>(st, dt, m.po_w[it], w.step0 + j, a, b, last, dA, dB);
-                m.po_a[it] = a;
-                if (KIND == EDEN_SYN_EXPTWO) m.po_b[it] = b;
-                m.po_last[it] = last;
-                put_event(rowA, rowB, used, w.K, j, dA, dB);
+                isi = pois_draw(m, it, w.step0 + j, 1);
+                pois_fire<KIND>(m, it, st, w.step0 + j, j, w.K, rowA, rowB, used);
             } else {
                 ts = ts + dt * 1.0f;
             }
@@ -363,14 +396,13 @@ __device__ __forceinline__ void pois_window(const DevModel &m, int64_t it, const
 // delay below dt.
 template <int KIND>
 __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
-                                           const float *tk, float *rowA, float *rowB, bool &used) {
+                                           const float *tk, float pend, uint32_t mask, float *rowA, float *rowB,
+                                           bool &used) {
     if (w.step0 <= 0) return;  // no spikes reach a synapse during initialisation
     const float dt = m.dt;
-    float pend = m.sy_pend[it];
     const float pend0 = pend;
     bool trig = false;
     float delay = 0.0f;
-    const uint32_t mask = m.sy_mask[it];
     if (mask) {
         m.sy_mask[it] = 0;
         delay = m.sy_delay[it];
@@ -441,21 +473,53 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, const Win
         __syncwarp();
         return;
     }
-    const SynTypeDev st = c_syn_types[m.bk_type[bk]];
+    const int type = m.bk_type[bk];
+    const SynTypeDev st = c_syn_types[type];
     const bool two = st.kind == EDEN_SYN_EXPTWO;
     bool used = false;
-    for (int r = 0; lane + 32 * r < n; r++) {
-        const int64_t it = m.ck_i0[c] + lane + 32 * r;
+    // the items' per-window state, loaded up front so the loads overlap
+    const int64_t i0 = m.ck_i0[c] + lane;
+    float s0v[kChunkItems / 32], s1v[kChunkItems / 32];
+#pragma unroll
+    for (int r = 0; r < kChunkItems / 32; r++) {
+        s0v[r] = 0.0f; s1v[r] = 0.0f;
+        if (lane + 32 * r < n) {
+            const int64_t it = i0 + 32 * r;
+            if (kind == BK_POIS) { s0v[r] = m.po_ts[it]; s1v[r] = m.po_isi[it]; }
+            else { s0v[r] = m.sy_pend[it]; s1v[r] = __uint_as_float(m.sy_mask[it]); }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kChunkItems / 32; r++) {
+        if (lane + 32 * r >= n) break;
+        const int64_t it = i0 + 32 * r;
         if (kind == BK_POIS) {
-            if (two) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, rowA, rowB, used);
-            else pois_window<EDEN_SYN_EXPONE>(m, it, w, st, rowA, rowB, used);
+            if (two) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
+            else pois_window<EDEN_SYN_EXPONE>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
         } else {
-            if (two) syn_window<EDEN_SYN_EXPTWO>(m, it, w, st, tk, rowA, rowB, used);
-            else syn_window<EDEN_SYN_EXPONE>(m, it, w, st, tk, rowA, rowB, used);
+            const uint32_t mask = __float_as_uint(s1v[r]);
+            if (two) syn_window<EDEN_SYN_EXPTWO>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
+            else syn_window<EDEN_SYN_EXPONE>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
         }
     }
     const unsigned rows = __ballot_sync(0xffffffffu, used);
     __syncwarp();
+    const float dt = m.dt;
+    float A = m.ck_a[c], B = m.ck_b[c], gj = 0.0f;
+    if (rows == 0) {
+        // no event in the window: the aggregate decays in closed form,
+        // A f^j, from the factors' powers (syn_pow)
+        const float *pr = m.syn_pow + (size_t)type * 2 * kPowLen, *pd = pr + kPowLen;
+        if (lane < w.K) gj = two ? st.gbase * (B * pd[lane] - A * pr[lane]) : A * pd[lane];
+        if (w.step0 > 0) {
+            A = A * (two ? pr[w.K] : pd[w.K]);
+            B = two ? B * pd[w.K] : B;
+        }
+        if (lane < w.K) m.Gp[(size_t)lane * m.n_chunk + c] = gj;
+        if (lane == 0) { m.ck_a[c] = A; m.ck_b[c] = B; }
+        __syncwarp();
+        return;
+    }
     float ea = 0.0f, eb = 0.0f;  // lane j: the chunk's events of step j
     if (lane < w.K)
         for (unsigned r = rows; r; r &= r - 1) {
@@ -463,8 +527,6 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, const Win
             ea += tileA[q * kAccStride + lane];
             eb += tileB[q * kAccStride + lane];
         }
-    const float dt = m.dt;
-    float A = m.ck_a[c], B = m.ck_b[c], gj = 0.0f;
     for (int j = 0; j < w.K; j++) {
         const float eaj = __shfl_sync(0xffffffffu, ea, j), ebj = __shfl_sync(0xffffffffu, eb, j);
         const float g = two ? st.gbase * (B - A) : A;
