@@ -143,6 +143,38 @@ def cpu_sample(low, threads: int, budget_s: float = 15.0):
     return low.n_target * n / (dt * n / (n + 4)), n
 
 
+def precision_sample(low, threads: int, n_steps: int = 400):
+    """Spike-time and voltage error of the batched GPU path against the
+    double-precision oracle over the first n_steps of the same network (a
+    bounded sample: the oracle runs on the host cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
+    import eden_port
+    from eden_gb300.engine import MODE_BATCHED, Simulation
+    f64 = eden_port.run(low, n_steps=n_steps, threads=threads, spike_cap=1 << 22, double=True)
+    sim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=n_steps + 8)
+    rec = sim.run(n_steps)
+    sim.close()
+    keep = f64["spike_step"] <= n_steps
+    a = {}
+    for s_, k in zip(f64["spike_src"][keep], f64["spike_step"][keep]):
+        a.setdefault(int(s_), []).append(int(k))
+    b = {}
+    for s_, k in zip(rec.spike_src, rec.spike_step):
+        b.setdefault(int(s_), []).append(int(k))
+    mismatch, worst = 0, 0
+    for c in set(a) | set(b):
+        x, y = sorted(a.get(c, [])), sorted(b.get(c, []))
+        if len(x) != len(y):
+            mismatch += 1
+        elif x:
+            worst = max(worst, max(abs(p - q) for p, q in zip(x, y)))
+    dv = float(np.abs(rec.trace.astype(np.float64) - f64["trace"]).max()) if rec.trace.size else 0.0
+    dt_ms = float(low.dt) * 1e-3
+    return {"reference": "double-precision oracle (oracle/port, EDEN_PORT_DOUBLE)", "steps": n_steps,
+            "spikes": int(keep.sum()), "cells_count_mismatch": mismatch, "max_spike_shift_ms": worst * dt_ms,
+            "max_abs_dv_mV": dv}
+
+
 def load_profile_traffic():
     """DRAM bytes per k_cells_t launch from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "k_cells_t_multicomp_net.json")
@@ -287,12 +319,14 @@ def main():
 
     # ---- CPU baseline (rank 0 only)
     cpu = None
+    precision = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
         cval, n = cpu_sample(low, threads, budget_s=15.0)
         cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} simulation steps of the same network (after 4 init passes), C restatement of "
                          f"the reference loop, OpenMP {threads} threads"}
+        precision = precision_sample(low, threads)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -311,7 +345,8 @@ def main():
                              "step_achieved_gbs": ab["total"] * sim_steps / (total_ms * 1e-3) / 1e9 / world * world},
                 "kernels_ms": {k: round(v[0], 3) for k, v in k_ms.items()},
                 "clocks": clk,
-                "cpu_baseline": cpu}
+                "cpu_baseline": cpu,
+                "spike_time_error": precision}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -70,6 +70,9 @@ struct EdenGpuCtx {
     // window table (device + pinned host)
     WindowArgs *d_wtab = nullptr;
     WindowArgs *h_wtab = nullptr;
+    WindowTimes *d_wtimes = nullptr;
+    WindowTimes *h_wtimes = nullptr;
+    float prev_tk[32] = {0};    // step times of the last window run
     int64_t wtab_cap = 0;
     int *d_base = nullptr;      // chunk base read by graph-launched kernels
     int *d_zero = nullptr;      // always 0, for direct launches
@@ -120,17 +123,13 @@ namespace eden {
 
 // Phase 1 of both paths: input blocks over the window, one warp per target
 // with inputs (the per-step path runs it with K = 1).
-__global__ void __launch_bounds__(kInputThreads) k_inputs_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
+__global__ void __launch_bounds__(kInputThreads) k_inputs_t(DevModel m, const WindowArgs *tab,
+                                                             const WindowTimes *ttab, const int *base, int idx) {
     __shared__ float tiles[kInputThreads / 32][2][32 * kAccStride];
-    __shared__ float tk[32];
-    const WindowArgs w = tab[*base + idx];
-    if (threadIdx.x < 32) {
-        // single-precision time of each step of the window, accumulated in
-        // double from the window start as the reference accumulates it
-        double t = w.t0;
-        for (int j = 0; j < (int)threadIdx.x && w.step0 + j > 0; j++) t += (double)m.dt;
-        tk[threadIdx.x] = (float)t;
-    }
+    __shared__ float tk[64];  // the window's step times, then the previous window's
+    const int wi = *base + idx;
+    const WindowArgs w = tab[wi];
+    if (threadIdx.x < 64) tk[threadIdx.x] = threadIdx.x < 32 ? ttab[wi].tk[threadIdx.x] : ttab[wi].tprev[threadIdx.x - 32];
     __syncthreads();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -593,6 +592,7 @@ extern "C" void edenGpuDestroy(EdenGpuCtx *ctx) {
     for (void *p : ctx->allocs) cudaFree(p);
     for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);
     if (ctx->h_wtab) cudaFreeHost(ctx->h_wtab);
+    if (ctx->h_wtimes) cudaFreeHost(ctx->h_wtimes);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1432,18 +1432,58 @@ extern "C" int edenGpuCreate(const EdenGpuModel *model, const EdenGpuOptions *op
 static int ensure_wtab(EdenGpuCtx *ctx, int64_t n) {
     if (n <= ctx->wtab_cap) return 0;
     int64_t cap = std::max<int64_t>(n, 1024);
+    // the captured graph refers to the old tables: capture it again
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
     if (ctx->h_wtab) cudaFreeHost(ctx->h_wtab);
-    if (ctx->d_wtab) {
-        cudaFree(ctx->d_wtab);
-        ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), (void *)ctx->d_wtab), ctx->allocs.end());
+    if (ctx->h_wtimes) cudaFreeHost(ctx->h_wtimes);
+    ctx->h_wtab = nullptr;
+    ctx->h_wtimes = nullptr;
+    for (void *old : {(void *)ctx->d_wtab, (void *)ctx->d_wtimes}) {
+        if (!old) continue;
+        cudaFree(old);
+        ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), old), ctx->allocs.end());
     }
     CUDA_TRY(ctx, cudaMallocHost(&ctx->h_wtab, sizeof(WindowArgs) * cap));
-    void *p = nullptr;
+    CUDA_TRY(ctx, cudaMallocHost(&ctx->h_wtimes, sizeof(WindowTimes) * cap));
+    void *p = nullptr, *q = nullptr;
     CUDA_TRY(ctx, cudaMalloc(&p, sizeof(WindowArgs) * cap));
     ctx->allocs.push_back(p);
+    CUDA_TRY(ctx, cudaMalloc(&q, sizeof(WindowTimes) * cap));
+    ctx->allocs.push_back(q);
     ctx->d_wtab = (WindowArgs *)p;
+    ctx->d_wtimes = (WindowTimes *)q;
     ctx->wtab_cap = cap;
     return 0;
+}
+
+// The next window's arguments and step times (in double from the host
+// clock, as the reference accumulates time, eden/Eden.cpp:11486, 11931), and
+// the host clock advanced past it; the previous window's times are kept for
+// the trigger replay.
+static void fill_window(EdenGpuCtx *ctx, WindowArgs &w, WindowTimes &tt, int64_t s, int K) {
+    w.step0 = s;
+    w.K = K;
+    w.Kprev = ctx->Kprev;
+    w.par = ctx->par;
+    w.wpar = ctx->wpar;
+    double t = ctx->time;
+    for (int j = 0; j < 32; j++) {
+        tt.tk[j] = (float)t;
+        tt.tprev[j] = ctx->prev_tk[j];
+        if (s + j > 0) t += (double)ctx->d.dt;
+    }
+    if (s > 0) {
+        ctx->t_prev0 = ctx->time;
+        ctx->Kprev = K;
+        for (int k = 0; k < K; k++) ctx->time += (double)ctx->d.dt;
+        for (int j = 0; j < 32; j++) ctx->prev_tk[j] = tt.tk[j];
+    }
+    ctx->par ^= (K & 1);
+    ctx->wpar ^= 1;
 }
 
 // Event pair around a launch when kernel timing is on.
@@ -1472,7 +1512,7 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     cudaStream_t s = ctx->stream;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
         tmark(ctx, EDEN_KERNEL_INPUTS, true);
-        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, ctx->d_wtimes, base, idx);
         tmark(ctx, EDEN_KERNEL_INPUTS, false);
         int n = 1;
         tmark(ctx, EDEN_KERNEL_CELLS, true);
@@ -1489,7 +1529,7 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     }
     (void)K;
     tmark(ctx, EDEN_KERNEL_INPUTS, true);
-    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, ctx->d_wtimes, base, idx);
     tmark(ctx, EDEN_KERNEL_INPUTS, false);
     tmark(ctx, EDEN_KERNEL_TARGETS, true);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
@@ -1527,25 +1567,11 @@ extern "C" int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) 
         s += K;
     }
     TRY(ensure_wtab(ctx, (int64_t)wins.size() + kGraphWindows));
-    for (size_t i = 0; i < wins.size(); i++) {
-        WindowArgs &w = ctx->h_wtab[i];
-        w.step0 = wins[i].step0;
-        w.K = wins[i].K;
-        w.Kprev = ctx->Kprev;
-        w.t0 = ctx->time;
-        w.t_prev0 = ctx->t_prev0;
-        w.par = ctx->par;
-        w.wpar = ctx->wpar;
-        if (w.step0 > 0) {
-            ctx->t_prev0 = ctx->time;
-            ctx->Kprev = w.K;
-            for (int k = 0; k < w.K; k++) ctx->time += (double)ctx->d.dt;
-        }
-        ctx->par ^= (w.K & 1);
-        ctx->wpar ^= 1;
-    }
+    for (size_t i = 0; i < wins.size(); i++) fill_window(ctx, ctx->h_wtab[i], ctx->h_wtimes[i], wins[i].step0, wins[i].K);
     CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_wtab, ctx->h_wtab, sizeof(WindowArgs) * wins.size(), cudaMemcpyHostToDevice,
                                   ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_wtimes, ctx->h_wtimes, sizeof(WindowTimes) * wins.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
     CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_base, 0, sizeof(int), ctx->stream));
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     int64_t launches = 0;
@@ -1723,8 +1749,9 @@ extern "C" int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *st
 //     floats) in the file-scope array g_static_gp instead of the context's
 //     buffer, which limits it to models of at most kStaticGpChunks input
 //     chunks (16 MiB of scratch); larger models get EDEN_GPU_E_RANGE;
-//   - the window arguments in the file-scope table g_static_wtab, filled
-//     from a stack buffer at most kStaticWindows windows at a time;
+//   - the window arguments and step times in the file-scope tables
+//     g_static_wtab and g_static_wtimes, filled from stack buffers at most
+//     kStaticWindows windows at a time;
 //   - plain launches: no graph, no kernel-timing events.
 // The first call on a device looks up both arrays' device addresses with
 // cudaGetSymbolAddress, with that device current.  That set-up should happen
@@ -1738,18 +1765,20 @@ extern "C" int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *st
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int kStaticGpChunks = 131072;  // input chunks the static scratch holds
-constexpr int kStaticWindows = 128;      // window arguments copied per batch
+constexpr int kStaticWindows = 64;       // window arguments copied per batch
 constexpr int kStaticMaxDevices = 64;
 std::mutex g_static_mu;
 float *g_static_gp_ptr[kStaticMaxDevices];
 WindowArgs *g_static_wtab_ptr[kStaticMaxDevices];
+WindowTimes *g_static_wtimes_ptr[kStaticMaxDevices];
 }  // namespace
 
 static __device__ __align__(256) float g_static_gp[32 * kStaticGpChunks];
 static __device__ __align__(256) WindowArgs g_static_wtab[kStaticWindows];
+static __device__ __align__(256) WindowTimes g_static_wtimes[kStaticWindows];
 
 // Device addresses of the static arrays on ctx's device (which is current).
-static int static_scratch(EdenGpuCtx *ctx, float **gp, WindowArgs **tab) {
+static int static_scratch(EdenGpuCtx *ctx, float **gp, WindowArgs **tab, WindowTimes **times) {
     const int dev = ctx->device;
     if (dev < 0 || dev >= kStaticMaxDevices)
         return ctx->fail(EDEN_GPU_E_RANGE, "edenGpuRunStaticScratch: device %d beyond the %d supported", dev,
@@ -1759,21 +1788,26 @@ static int static_scratch(EdenGpuCtx *ctx, float **gp, WindowArgs **tab) {
         void *p = nullptr, *q = nullptr;
         CUDA_TRY(ctx, cudaGetSymbolAddress(&p, g_static_gp));
         CUDA_TRY(ctx, cudaGetSymbolAddress(&q, g_static_wtab));
+        void *r = nullptr;
+        CUDA_TRY(ctx, cudaGetSymbolAddress(&r, g_static_wtimes));
+        g_static_wtimes_ptr[dev] = (WindowTimes *)r;
         g_static_gp_ptr[dev] = (float *)p;
         g_static_wtab_ptr[dev] = (WindowArgs *)q;
     }
     *gp = g_static_gp_ptr[dev];
     *tab = g_static_wtab_ptr[dev];
+    *times = g_static_wtimes_ptr[dev];
     return 0;
 }
 
 // The launches of launch_window for window `idx` of `tab`, with the model
 // `dm` (the context's, scratch pointer replaced) and without timing marks.
-static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const WindowArgs *tab, int idx) {
+static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const WindowArgs *tab, const WindowTimes *times,
+                                int idx) {
     cudaStream_t s = ctx->stream;
     const int *zero = ctx->d_zero;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
-        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, zero, idx);
+        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, times, zero, idx);
         int n = 1;
         for (const auto &cl : ctx->classes) {
             const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
@@ -1783,7 +1817,7 @@ static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const Windo
         k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);
         return n + 1;
     }
-    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, zero, idx);
+    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, times, zero, idx);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(dm, tab, zero, idx);
     k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(dm, tab, zero, idx, ctx->forest_cap);
     k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);
@@ -1809,11 +1843,13 @@ extern "C" int edenGpuRunStaticScratch(EdenGpuCtx *ctx, int64_t first_step, int6
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     float *gp = nullptr;
     WindowArgs *tab = nullptr;
-    TRY(static_scratch(ctx, &gp, &tab));
+    WindowTimes *times = nullptr;
+    TRY(static_scratch(ctx, &gp, &tab, &times));
     if (n_steps == 0) return 0;
     DevModel dm = ctx->d;
     dm.Gp = gp;
     WindowArgs batch[kStaticWindows];
+    WindowTimes tbatch[kStaticWindows];
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     int64_t launches = 0;
     int64_t s = first_step;
@@ -1825,28 +1861,16 @@ extern "C" int edenGpuRunStaticScratch(EdenGpuCtx *ctx, int64_t first_step, int6
             if (ctx->mode != EDEN_MODE_BATCHED) K = 1;
             else if (s <= 0) K = (int)std::min<int64_t>(-s + 1, last - s + 1);
             else K = (int)std::min<int64_t>(ctx->K, last - s + 1);
-            WindowArgs &w = batch[nb++];
-            w.step0 = s;
-            w.K = K;
-            w.Kprev = ctx->Kprev;
-            w.t0 = ctx->time;
-            w.t_prev0 = ctx->t_prev0;
-            w.par = ctx->par;
-            w.wpar = ctx->wpar;
-            if (s > 0) {
-                ctx->t_prev0 = ctx->time;
-                ctx->Kprev = K;
-                for (int k = 0; k < K; k++) ctx->time += (double)ctx->d.dt;
-            }
-            ctx->par ^= (K & 1);
-            ctx->wpar ^= 1;
+            fill_window(ctx, batch[nb], tbatch[nb], s, K);
+            nb++;
             s += K;
         }
         // stream-ordered after the previous batch's launches, so the table is
         // not overwritten while they read it; the stack buffer is free for
         // reuse once the copy call returns
         CUDA_TRY(ctx, cudaMemcpyAsync(tab, batch, sizeof(WindowArgs) * nb, cudaMemcpyHostToDevice, ctx->stream));
-        for (int i = 0; i < nb; i++) launches += launch_window_static(ctx, dm, tab, i);
+        CUDA_TRY(ctx, cudaMemcpyAsync(times, tbatch, sizeof(WindowTimes) * nb, cudaMemcpyHostToDevice, ctx->stream));
+        for (int i = 0; i < nb; i++) launches += launch_window_static(ctx, dm, tab, times, i);
         CUDA_TRY(ctx, cudaGetLastError());
     }
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));

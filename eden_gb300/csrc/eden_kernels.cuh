@@ -203,14 +203,21 @@ __host__ __device__ inline int izh_words(int n) { return 13 * n + 1; }
 
 // Per-window arguments: the window covers steps [step0, step0 + K); steps
 // <= 0 are initialisation passes.  The previous window began at step
-// step0 - Kprev at time t_prev0; its triggers are the mask bits 1..Kprev-1
-// (replayed before step0) and bit Kprev (the trigger of step0 itself).
+// step0 - Kprev; its triggers are the mask bits 1..Kprev-1 (replayed before
+// step0) and bit Kprev (the trigger of step0 itself).
 struct WindowArgs {
     int64_t step0;
     int32_t K, Kprev;
-    double t0, t_prev0;
     int32_t par;   // which V buffer holds the state at step0
     int32_t wpar;  // window parity: which spike list this window fills
+};
+
+// Single-precision times (us) of the window's steps and of the previous
+// window's, accumulated on the host in double from 0 as the reference
+// accumulates its time (eden/Eden.cpp:11486, 11931).
+struct WindowTimes {
+    float tk[32];
+    float tprev[32];
 };
 
 __device__ __forceinline__ float warp_sum(float x) {
@@ -255,13 +262,10 @@ __device__ __forceinline__ bool trigger_arrival(float t, float dt, float delay, 
 // Replay triggers of the previous window (bits 1..Kprev-1) and return the
 // trigger of the window's first step (bit Kprev).  Exact because every delay
 // is at least Kprev * dt, so none of these spikes can fall due before step0.
-__device__ __forceinline__ bool replay_mask(uint32_t mask, const WindowArgs &w, float dt, float delay,
-                                            float &pend) {
-    double t = w.t_prev0;
-    for (int b = 1; b < w.Kprev; b++) {
-        t += (double)dt;
-        if ((mask >> b) & 1u) trigger_arrival((float)t, dt, delay, pend);
-    }
+__device__ __forceinline__ bool replay_mask(uint32_t mask, const WindowArgs &w, const float *tprev, float dt,
+                                            float delay, float &pend) {
+    for (int b = 1; b < w.Kprev; b++)
+        if ((mask >> b) & 1u) trigger_arrival(tprev[b], dt, delay, pend);
     return (mask >> w.Kprev) & 1u;
 }
 
@@ -406,7 +410,7 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
     if (mask) {
         m.sy_mask[it] = 0;
         delay = m.sy_delay[it];
-        trig = replay_mask(mask, w, dt, delay, pend);
+        trig = replay_mask(mask, w, tk + 32, dt, delay, pend);
     }
     int jf = -1;
     if (pend >= tk[0] && pend < tk[w.K - 1] + dt)
@@ -491,15 +495,16 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, const Win
     }
 #pragma unroll
     for (int r = 0; r < kChunkItems / 32; r++) {
-        if (lane + 32 * r >= n) break;
-        const int64_t it = i0 + 32 * r;
-        if (kind == BK_POIS) {
-            if (two) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
-            else pois_window<EDEN_SYN_EXPONE>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
-        } else {
-            const uint32_t mask = __float_as_uint(s1v[r]);
-            if (two) syn_window<EDEN_SYN_EXPTWO>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
-            else syn_window<EDEN_SYN_EXPONE>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
+        if (lane + 32 * r < n) {
+            const int64_t it = i0 + 32 * r;
+            if (kind == BK_POIS) {
+                if (two) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
+                else pois_window<EDEN_SYN_EXPONE>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
+            } else {
+                const uint32_t mask = __float_as_uint(s1v[r]);
+                if (two) syn_window<EDEN_SYN_EXPTWO>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
+                else syn_window<EDEN_SYN_EXPONE>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
+            }
         }
     }
     const unsigned rows = __ballot_sync(0xffffffffu, used);
@@ -738,8 +743,9 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
 // compartment's pivot is rebuilt every step from its diagonal (PV holds
 // G/C + sum 1/(RC) on entry, X its pre-updated V) and its children's
 // factors, in increasing child order as the reference's post-order visits
-// them.  Depths hold at most 32 compartments, one per lane; LV packs each
-// depth's first compartment and whether it holds a non-flat one.
+// them.  A depth's compartments are spread over the lanes (at most 32 per
+// depth unless a single cell is wider); LV packs each depth's first
+// compartment and whether it holds a non-flat one.
 // Back-substitution runs root-first.  X holds V_next on return.
 constexpr int32_t kLvMask = 0xffff;
 constexpr int32_t kLvNonFlat = 1 << 16;
@@ -750,8 +756,8 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
     int end = LV[nlev] & kLvMask;
     for (int lev = nlev - 1; lev >= 0; lev--) {
         const int32_t lw = LV[lev];
-        const int j = (lw & kLvMask) + lane;
-        if (j < end) {
+        // a depth holds at most 32 compartments unless one cell alone is wider
+        for (int j = (lw & kLvMask) + lane; j < end; j += 32) {
             const uint32_t cep = CEP[j];
             const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
             float xj = X[j] + KC[j];
@@ -781,8 +787,8 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
     for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) X[r] = X[r] * PV[r];
     __syncwarp();
     for (int lev = 1; lev < nlev; lev++) {
-        const int i = (LV[lev] & kLvMask) + lane;
-        if (i < (LV[lev + 1] & kLvMask)) {
+        const int i1 = LV[lev + 1] & kLvMask;
+        for (int i = (LV[lev] & kLvMask) + lane; i < i1; i += 32) {
             const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
             X[i] = (X[i] - U[i] * X[p]) * PV[i];
         }

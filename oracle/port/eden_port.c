@@ -24,6 +24,22 @@
  * against fixtures produced by the reference simulator built from its own sources.
  */
 #include <math.h>
+/* The arithmetic type: IEEE single precision, as the reference's generated
+ * kernels compute; building with -DEDEN_PORT_DOUBLE gives the same loop in
+ * double precision (eden_port_run then still takes and returns the float
+ * model and records), the FP64 reference the single-precision results'
+ * errors are stated against. */
+#ifdef EDEN_PORT_DOUBLE
+typedef double real;
+#define R(x) x
+#define EXP exp
+#define LOG log
+#else
+typedef float real;
+#define R(x) x##f
+#define EXP expf
+#define LOG logf
+#endif
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -45,21 +61,21 @@ static uint64_t hash64shift(uint64_t key) {
     return key;
 }
 
-static float randof(float x, int64_t work_item, int64_t instance, int64_t step, int invocation_id) {
+static real randof(real x, int64_t work_item, int64_t instance, int64_t step, int invocation_id) {
     uint64_t hi = ((uint64_t)work_item << 24) | ((uint64_t)instance & ((1ULL << 24) - 1));
     uint64_t lo = ((uint64_t)(int64_t)invocation_id << 40) | ((uint64_t)step & ((1ULL << 40) - 1));
     uint64_t sample = hash64shift(hash64shift(lo) ^ hi);
     const int scale = 1 << 23;
-    float r = (float)(sample % (uint64_t)scale) / (float)scale;
+    real r = (real)(sample % (uint64_t)scale) / (real)scale;
     return x * r;
 }
 
-static float rate_value(int kind, float r, float mid, float s, float v) {
+static real rate_value(int kind, real r, real mid, real s, real v) {
     switch (kind) {
-        case EDEN_RATE_EXP: return r * expf((v - mid) / s);
+        case EDEN_RATE_EXP: return r * EXP((v - mid) / s);
         case EDEN_RATE_EXPLINEAR:
-            return r * ((v == mid) ? 1.0f : (((v - mid) / s) / (1.0f - expf(-(v - mid) / s))));
-        default: return r / (1.0f + expf((mid - v) / s));
+            return r * ((v == mid) ? R(1.0) : (((v - mid) / s) / (R(1.0) - EXP(-(v - mid) / s))));
+        default: return r / (R(1.0) + EXP((mid - v) / s));
     }
 }
 
@@ -67,12 +83,12 @@ typedef struct {
     const EdenGpuModel *m;
     int64_t n_target;
     /* double-buffered state */
-    float *v[2], *gate[2], *izh_u[2];
-    float *syn_a[2], *syn_b[2], *syn_pend[2];
+    real *v[2], *gate[2], *izh_u[2];
+    real *syn_a[2], *syn_b[2], *syn_pend[2];
     unsigned char *trig[2];
-    float *pois_ts[2], *pois_isi[2], *pois_a[2], *pois_b[2];
+    real *pois_ts[2], *pois_isi[2], *pois_a[2], *pois_b[2];
     unsigned char *spiked[2];           /* event-logger slot per source */
-    float *diag;
+    real *diag;
     int64_t *gate_off;                  /* [n_chan + 1] */
     int64_t *syn_off, *pois_off, *pulse_off; /* [n_target + 1] */
     int64_t *fan_off, *fan_syn;         /* CSR source -> synapses */
@@ -115,16 +131,16 @@ static void dfs_postorder(const int32_t *parent, int n, int32_t *order) {
 
 /* One synapse instance: trigger/pending logic, exposure, state update.
  * Returns the weighted current and conductance through *iw, *gw. */
-static inline void synapse_step(const EdenGpuSynapseType *st, int init, float t, float dt,
-                                int spike_in_raw, float delay, float pend, float *pend_next,
-                                float a, float b, float *a_next, float *b_next, float v, float w,
-                                float *iw, float *gw, int *fired) {
+static inline void synapse_step(const EdenGpuSynapseType *st, int init, real t, real dt,
+                                int spike_in_raw, real delay, real pend, real *pend_next,
+                                real a, real b, real *a_next, real *b_next, real v, real w,
+                                real *iw, real *gw, int *fired) {
     int spike_now = 0;
-    float next_next = pend;
+    real next_next = pend;
     if (!init) {
         if (t <= pend && pend < t + dt) spike_now = 1;
         if (spike_in_raw) {
-            float fresh = t + delay;
+            real fresh = t + delay;
             if (t <= fresh && fresh < t + dt) spike_now = 1;
             if (next_next < t + dt && next_next < fresh) next_next = fresh;
         }
@@ -132,9 +148,9 @@ static inline void synapse_step(const EdenGpuSynapseType *st, int init, float t,
     *pend_next = next_next;
     *fired = spike_now;
     if (st->kind == EDEN_SYN_EXPONE) {
-        float g = a;
-        float i = g * (st->erev - v);
-        float gn;
+        real g = a;
+        real i = g * (st->erev - v);
+        real gn;
         if (!init) {
             gn = a - dt * (a / st->tau_decay);
             if (spike_now) gn = a + st->gbase;
@@ -146,11 +162,11 @@ static inline void synapse_step(const EdenGpuSynapseType *st, int init, float t,
         *iw = i * w;
         *gw = g * w;
     } else {
-        float g = st->gbase * (b - a);
-        float i = g * (st->erev - v);
-        float an, bn;
+        real g = st->gbase * (b - a);
+        real i = g * (st->erev - v);
+        real an, bn;
         if (init) {
-            an = 0.0f; bn = 0.0f;
+            an = R(0.0); bn = R(0.0);
         } else {
             an = a + dt * (-a / st->tau_rise);
             bn = b + dt * (-b / st->tau_decay);
@@ -167,33 +183,33 @@ static inline void synapse_step(const EdenGpuSynapseType *st, int init, float t,
 }
 
 /* Poisson-driven synapse: the spiker fires its own synapse in the same step. */
-static inline void poisson_step(const Port *P, int cur, int64_t k, int init, float dt, int64_t step,
-                                float v, float *iw, float *gw) {
+static inline void poisson_step(const Port *P, int cur, int64_t k, int init, real dt, int64_t step,
+                                real v, real *iw, real *gw) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
-    float rate = m->pois_rate[k];
-    float avg_isi = 1.0f / rate;
+    real rate = m->pois_rate[k];
+    real avg_isi = R(1.0) / rate;
     int64_t work_item = (int64_t)m->src_cell_seed[m->pois_src[k]];
     int64_t inst = m->pois_instance[k];
-    float ts = P->pois_ts[cur][k], isi = P->pois_isi[cur][k];
+    real ts = P->pois_ts[cur][k], isi = P->pois_isi[cur][k];
     int fired = 0;
     if (init) {
-        P->pois_ts[nxt][k] = 0.0f;
-        P->pois_isi[nxt][k] = (-avg_isi) * logf(1.0f - randof(1.0f, work_item, inst, step, 0));
+        P->pois_ts[nxt][k] = R(0.0);
+        P->pois_isi[nxt][k] = (-avg_isi) * LOG(R(1.0) - randof(R(1.0), work_item, inst, step, 0));
     } else {
-        P->pois_ts[nxt][k] = ts + dt * 1.0f;
+        P->pois_ts[nxt][k] = ts + dt * R(1.0);
         P->pois_isi[nxt][k] = isi;
         if (ts > isi) {
-            P->pois_ts[nxt][k] = 0.0f;
-            P->pois_isi[nxt][k] = (-avg_isi) * logf(1.0f - randof(1.0f, work_item, inst, step, 1));
+            P->pois_ts[nxt][k] = R(0.0);
+            P->pois_isi[nxt][k] = (-avg_isi) * LOG(R(1.0) - randof(R(1.0), work_item, inst, step, 1));
             fired = 1;
         }
     }
     const EdenGpuSynapseType *st = &m->syn_types[m->pois_type[k]];
-    float a = P->pois_a[cur][k], b = P->pois_b[cur][k];
-    float g = st->gbase * (b - a);
-    float i = g * (st->erev - v);
-    float an, bn;
+    real a = P->pois_a[cur][k], b = P->pois_b[cur][k];
+    real g = st->gbase * (b - a);
+    real i = g * (st->erev - v);
+    real an, bn;
     if (st->kind == EDEN_SYN_EXPONE) {
         g = a;
         i = g * (st->erev - v);
@@ -205,7 +221,7 @@ static inline void poisson_step(const Port *P, int cur, int64_t k, int init, flo
         }
         bn = b;
     } else if (init) {
-        an = 0.0f; bn = 0.0f;
+        an = R(0.0); bn = R(0.0);
     } else {
         an = a + dt * (-a / st->tau_rise);
         bn = b + dt * (-b / st->tau_decay);
@@ -222,16 +238,16 @@ static inline void poisson_step(const Port *P, int cur, int64_t k, int init, flo
 
 /* Synapse + input currents into one target (in the reference's order:
  * inputs then synapses are separate totals, each synapse type a block). */
-static void target_currents(Port *P, int cur, int64_t tgt, int init, float t, float dt, int64_t step,
-                            float v, float *I_in, float *G_in, float *I_syn, float *G_syn) {
+static void target_currents(Port *P, int cur, int64_t tgt, int init, real t, real dt, int64_t step,
+                            real v, real *I_in, real *G_in, real *I_syn, real *G_syn) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
-    float Iin = 0.0f, Gin = 0.0f, Isyn = 0.0f, Gsyn = 0.0f;
+    real Iin = R(0.0), Gin = R(0.0), Isyn = R(0.0), Gsyn = R(0.0);
     /* pulses */
     if (P->pulse_off[tgt + 1] > P->pulse_off[tgt]) {
-        float Ip = 0.0f;
+        real Ip = R(0.0);
         for (int64_t k = P->pulse_off[tgt]; k < P->pulse_off[tgt + 1]; k++) {
-            float s = m->pulse_start[k];
+            real s = m->pulse_start[k];
             if (s <= t && t <= s + m->pulse_duration[k]) Ip += m->pulse_amplitude[k] * m->pulse_weight[k];
         }
         Iin += Ip;
@@ -240,9 +256,9 @@ static void target_currents(Port *P, int cur, int64_t tgt, int init, float t, fl
     int64_t k = P->pois_off[tgt];
     while (k < P->pois_off[tgt + 1]) {
         int type = m->pois_type[k];
-        float Ia = 0.0f, Ga = 0.0f;
+        real Ia = R(0.0), Ga = R(0.0);
         for (; k < P->pois_off[tgt + 1] && m->pois_type[k] == type; k++) {
-            float iw, gw;
+            real iw, gw;
             poisson_step(P, cur, k, init, dt, step, v, &iw, &gw);
             Ia += iw; Ga += gw;
         }
@@ -253,14 +269,14 @@ static void target_currents(Port *P, int cur, int64_t tgt, int init, float t, fl
     while (s < P->syn_off[tgt + 1]) {
         int type = m->syn_type[s];
         const EdenGpuSynapseType *st = &m->syn_types[type];
-        float Ia = 0.0f, Ga = 0.0f;
+        real Ia = R(0.0), Ga = R(0.0);
         for (; s < P->syn_off[tgt + 1] && m->syn_type[s] == type; s++) {
             int in = 0;
             if (!init) {
                 in = P->trig[cur][s] != 0;
                 P->trig[cur][s] = 0;
             }
-            float iw, gw;
+            real iw, gw;
             int fired;
             synapse_step(st, init, t, dt, in, m->syn_delay[s], P->syn_pend[cur][s], &P->syn_pend[nxt][s],
                          P->syn_a[cur][s], P->syn_b[cur][s], &P->syn_a[nxt][s], &P->syn_b[nxt][s],
@@ -279,49 +295,49 @@ static void send_spike(Port *P, int nxt, int32_t src) {
     P->spiked[nxt][src] = 1;
 }
 
-static void phys_cell_step(Port *P, int cur, int32_t cell, int init, float t, float dt, int64_t step) {
+static void phys_cell_step(Port *P, int cur, int32_t cell, int init, real t, real dt, int64_t step) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
     int32_t c0 = m->phys_comp_off[cell], c1 = m->phys_comp_off[cell + 1];
-    const float *V = P->v[cur];
-    float *Vn = P->v[nxt];
+    const real *V = P->v[cur];
+    real *Vn = P->v[nxt];
     for (int32_t c = c0; c < c1; c++) {
-        float A = m->comp_area[c], Vc = V[c];
-        float Ich = 0.0f, Gch = 0.0f;
+        real A = m->comp_area[c], Vc = V[c];
+        real Ich = R(0.0), Gch = R(0.0);
         for (int32_t ch = m->comp_chan_off[c]; ch < m->comp_chan_off[c + 1]; ch++) {
             const EdenGpuChannelType *ct = &m->chan_types[m->chan_type[ch]];
-            float fopen = 1.0f;
+            real fopen = R(1.0);
             int64_t go = P->gate_off[ch];
             for (int g = 0; g < ct->n_gates; g++) {
-                float q = P->gate[cur][go + g];
-                float alpha = rate_value(ct->fwd_kind[g], ct->fwd_rate[g], ct->fwd_mid[g], ct->fwd_scale[g], Vc);
-                float beta = rate_value(ct->rev_kind[g], ct->rev_rate[g], ct->rev_mid[g], ct->rev_scale[g], Vc);
-                float tau = 1.0f / (alpha + beta);
-                float inf = alpha / (alpha + beta);
-                float qn;
+                real q = P->gate[cur][go + g];
+                real alpha = rate_value(ct->fwd_kind[g], ct->fwd_rate[g], ct->fwd_mid[g], ct->fwd_scale[g], Vc);
+                real beta = rate_value(ct->rev_kind[g], ct->rev_rate[g], ct->rev_mid[g], ct->rev_scale[g], Vc);
+                real tau = R(1.0) / (alpha + beta);
+                real inf = alpha / (alpha + beta);
+                real qn;
                 if (init) {
                     qn = inf;
                 } else {
-                    float tau_factor = (dt * ct->q10[g]) / tau;
-                    float blend = expf(-tau_factor);
-                    qn = blend * q + (1.0f - blend) * inf;
-                    if (!(qn > 1e-6f)) qn = 1e-6f;
-                    if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
+                    real tau_factor = (dt * ct->q10[g]) / tau;
+                    real blend = EXP(-tau_factor);
+                    qn = blend * q + (R(1.0) - blend) * inf;
+                    if (!(qn > R(1e-6))) qn = R(1e-6);
+                    if (!(qn < (real)(1 - 1e-6))) qn = (real)(1 - 1e-6);
                 }
                 P->gate[nxt][go + g] = qn;
                 for (int r = 0; r < ct->gate_instances[g]; r++) fopen = fopen * q;
             }
-            float Gscaled = m->chan_gbase[ch] * fopen;
-            float iD = Gscaled * (m->chan_erev[ch] - Vc) * 1e-5f;
-            float gD = Gscaled * 1e-5f;
+            real Gscaled = m->chan_gbase[ch] * fopen;
+            real iD = Gscaled * (m->chan_erev[ch] - Vc) * R(1e-5);
+            real gD = Gscaled * R(1e-5);
             Ich += iD * A;
             Gch += gD * A;
         }
-        float Iin, Gin, Isyn, Gsyn;
+        real Iin, Gin, Isyn, Gsyn;
         target_currents(P, cur, c, init, t, dt, step, Vc, &Iin, &Gin, &Isyn, &Gsyn);
-        float I = Ich + Iin + Isyn;
-        float G = Gch + Gin + Gsyn;
-        P->diag[c] = 1.0f * (G / m->comp_c[c]) + m->comp_inv_rc[c];
+        real I = Ich + Iin + Isyn;
+        real G = Gch + Gin + Gsyn;
+        P->diag[c] = R(1.0) * (G / m->comp_c[c]) + m->comp_inv_rc[c];
         Vn[c] = init ? Vc : Vc + (dt * (I + (Vc * G))) / m->comp_c[c];
     }
     if (!init) {
@@ -329,15 +345,15 @@ static void phys_cell_step(Port *P, int cur, int32_t cell, int init, float t, fl
         const int32_t *ord = P->order + c0;
         const int32_t *par = m->comp_parent + c0;
         const float *R = m->comp_r_axial + c0, *C = m->comp_c + c0;
-        float *D = P->diag + c0, *X = Vn + c0;
-        for (int32_t k = 0; k < n; k++) D[k] = 1.0f + D[k] * dt;
+        real *D = P->diag + c0, *X = Vn + c0;
+        for (int32_t k = 0; k < n; k++) D[k] = R(1.0) + D[k] * dt;
         for (int32_t k = 0; k < n - 1; k++) {
             int32_t i = ord[k], j = par[i];
             int32_t idx = i > j ? i : j;
-            float Rr = R[idx];
-            float Ui = -dt / (Rr * C[i]);
-            float Uj = -dt / (Rr * C[j]);
-            float ratio = Uj / D[i];
+            real Rr = R[idx];
+            real Ui = -dt / (Rr * C[i]);
+            real Uj = -dt / (Rr * C[j]);
+            real ratio = Uj / D[i];
             D[j] -= ratio * Ui;
             X[j] -= ratio * X[i];
         }
@@ -346,41 +362,41 @@ static void phys_cell_step(Port *P, int cur, int32_t cell, int init, float t, fl
         for (int32_t k = n - 2; k >= 0; k--) {
             int32_t i = ord[k], j = par[i];
             int32_t idx = i > j ? i : j;
-            float Rr = R[idx];
-            float Ui = -dt / (Rr * C[i]);
+            real Rr = R[idx];
+            real Ui = -dt / (Rr * C[i]);
             X[i] = (X[i] - Ui * X[j]) / D[i];
         }
     }
     for (int32_t c = c0; c < c1; c++) {
         int32_t src = P->src_of_target[c];
         if (src < 0) continue;
-        float thr = m->src_threshold[src];
+        real thr = m->src_threshold[src];
         if (V[c] < thr && thr < Vn[c]) send_spike(P, nxt, src);
     }
 }
 
-static void izh_step(Port *P, int cur, int32_t k, int init, float t, float dt, int64_t step) {
+static void izh_step(Port *P, int cur, int32_t k, int init, real t, real dt, int64_t step) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
     int64_t tgt = (int64_t)m->n_comp + k;
     const float *p = m->izh_params + 10 * (int64_t)k;
-    float C = p[0], v0 = p[1], kk = p[2], vr = p[3], vt = p[4], vpeak = p[5];
-    float a = p[6], b = p[7], c = p[8], d = p[9];
-    float v = P->v[cur][tgt], u = P->izh_u[cur][k];
-    float Iin, Gin, Isyn, Gsyn;
+    real C = p[0], v0 = p[1], kk = p[2], vr = p[3], vt = p[4], vpeak = p[5];
+    real a = p[6], b = p[7], c = p[8], d = p[9];
+    real v = P->v[cur][tgt], u = P->izh_u[cur][k];
+    real Iin, Gin, Isyn, Gsyn;
     target_currents(P, cur, tgt, init, t, dt, step, v, &Iin, &Gin, &Isyn, &Gsyn);
-    float iext = Isyn + Iin;
-    float iMemb = ((kk * (v - vr)) * 1e-3f) * (v - vt) + iext - u;
-    float vn, un;
+    real iext = Isyn + Iin;
+    real iMemb = ((kk * (v - vr)) * R(1e-3)) * (v - vt) + iext - u;
+    real vn, un;
     int spike = 0;
     if (init) {
         vn = v0;
-        un = 0.0f;
+        un = R(0.0);
     } else {
-        float dv = iMemb / C;
+        real dv = iMemb / C;
         vn = v + dt * dv;
-        float du = (a * ((b * (v - vr)) - u)) * 1e-3f;
-        un = u + dt * du * 1e3f;
+        real du = (a * ((b * (v - vr)) - u)) * R(1e-3);
+        un = u + dt * du * R(1e3);
         if (v > vpeak) {
             vn = c;
             un = u + d;
@@ -415,20 +431,20 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
     int64_t n_gate = P.gate_off[n_chan];
     int64_t ns = m->n_syn, np = m->n_pois;
     for (int b = 0; b < 2; b++) {
-        P.v[b] = (float *)calloc((size_t)nt + 1, sizeof(float));
-        P.gate[b] = (float *)calloc((size_t)n_gate + 1, sizeof(float));
-        P.izh_u[b] = (float *)calloc((size_t)m->n_izh + 1, sizeof(float));
-        P.syn_a[b] = (float *)calloc((size_t)ns + 1, sizeof(float));
-        P.syn_b[b] = (float *)calloc((size_t)ns + 1, sizeof(float));
-        P.syn_pend[b] = (float *)calloc((size_t)ns + 1, sizeof(float));
+        P.v[b] = (real *)calloc((size_t)nt + 1, sizeof(real));
+        P.gate[b] = (real *)calloc((size_t)n_gate + 1, sizeof(real));
+        P.izh_u[b] = (real *)calloc((size_t)m->n_izh + 1, sizeof(real));
+        P.syn_a[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
+        P.syn_b[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
+        P.syn_pend[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
         P.trig[b] = (unsigned char *)calloc((size_t)ns + 1, 1);
-        P.pois_ts[b] = (float *)calloc((size_t)np + 1, sizeof(float));
-        P.pois_isi[b] = (float *)calloc((size_t)np + 1, sizeof(float));
-        P.pois_a[b] = (float *)calloc((size_t)np + 1, sizeof(float));
-        P.pois_b[b] = (float *)calloc((size_t)np + 1, sizeof(float));
+        P.pois_ts[b] = (real *)calloc((size_t)np + 1, sizeof(real));
+        P.pois_isi[b] = (real *)calloc((size_t)np + 1, sizeof(real));
+        P.pois_a[b] = (real *)calloc((size_t)np + 1, sizeof(real));
+        P.pois_b[b] = (real *)calloc((size_t)np + 1, sizeof(real));
         P.spiked[b] = (unsigned char *)calloc((size_t)m->n_src + 1, 1);
     }
-    P.diag = (float *)calloc((size_t)m->n_comp + 1, sizeof(float));
+    P.diag = (real *)calloc((size_t)m->n_comp + 1, sizeof(real));
     P.syn_fire_count = (int64_t *)calloc((size_t)ns + 1, sizeof(int64_t));
     /* initial state: V0, izhikevich v0, pending spikes at -inf (eden/Eden.cpp:9081-9094) */
     for (int b = 0; b < 2; b++) {
@@ -463,7 +479,7 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
 #endif
     int cur = 0;
     double time = 0.0;
-    const float dt = m->dt;
+    const real dt = m->dt;
     int64_t nsp = 0;
     int rc = 0;
     int64_t last_step = n_steps;  /* steps 1..n_steps are the non-init ones */
@@ -486,7 +502,7 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
                 P.spiked[cur][s] = 0;
             }
         }
-        float t = (float)time;
+        real t = (real)time;
         int32_t n_items = m->n_phys + m->n_izh;
 #pragma omp parallel for schedule(static)
         for (int32_t item = 0; item < n_items; item++) {
@@ -500,7 +516,8 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
     }
     *n_spikes = nsp;
     if (syn_fire_count) memcpy(syn_fire_count, P.syn_fire_count, sizeof(int64_t) * (size_t)ns);
-    if (syn_final_pending) memcpy(syn_final_pending, P.syn_pend[cur], sizeof(float) * (size_t)ns);
+    if (syn_final_pending)
+        for (int64_t s = 0; s < ns; s++) syn_final_pending[s] = (float)P.syn_pend[cur][s];
     for (int b = 0; b < 2; b++) {
         free(P.v[b]); free(P.gate[b]); free(P.izh_u[b]); free(P.syn_a[b]); free(P.syn_b[b]);
         free(P.syn_pend[b]); free(P.trig[b]); free(P.pois_ts[b]); free(P.pois_isi[b]);

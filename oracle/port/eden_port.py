@@ -1,4 +1,5 @@
-"""ctypes wrapper of the C restatement (libeden_port.so).
+"""ctypes wrapper of the C restatement (libeden_port.so, and libeden_port64.so:
+the same loop in double precision).
 
 Test infrastructure only: imported by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg, never by the product package.
@@ -11,6 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libeden_port.so")
+LIB64 = os.path.join(HERE, "libeden_port64.so")
 
 
 def build() -> str:
@@ -18,24 +20,25 @@ def build() -> str:
     return LIB
 
 
-_lib = None
+_libs = {}
 
 
-def _load():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def _load(double=False):
+    path = LIB64 if double else LIB
+    if path not in _libs:
+        if not os.path.exists(path):
             build()
-        _lib = ctypes.CDLL(LIB)
-        _lib.eden_port_run.restype = ctypes.c_int
-    return _lib
+        lib = ctypes.CDLL(path)
+        lib.eden_port_run.restype = ctypes.c_int
+        _libs[path] = lib
+    return _libs[path]
 
 
-def run(lowered, n_steps=None, trace_target=None, threads=0, spike_cap=None):
+def run(lowered, n_steps=None, trace_target=None, threads=0, spike_cap=None, double=False):
     """Run the port; returns dict(trace [n_steps, n_trace] f32, spike_src,
     spike_step, syn_fire_count, syn_final_pending, rc)."""
     from eden_gb300.lowering import to_cmodel
-    lib = _load()
+    lib = _load(double)
     cm, keep = to_cmodel(lowered)
     if n_steps is None:
         n_steps = lowered.n_steps

@@ -4,6 +4,9 @@ at any size, where the oracle would take too long:
 * routing: every synapse's pending-spike slot equals the reference's
   delivery and single-pending-spike rule replayed from the GPU's own spike
   log (oracle/routing.py), bit for bit;
+* parity at full size over the first 400 steps (10 ms) of multicomp_net
+  against the oracle: the parity tests' samecount(0.1 ms) and
+  box(0.1 ms, 0.5 mV), in both modes;
 * bounds: every membrane potential finite (inside [-100, +70] mV for the
   cable cells; an izhikevich v may overshoot vpeak by one step before its
   reset), every spike logged at most once per cell and step.
@@ -14,9 +17,12 @@ multicomp_net: 10,000 cells, 797,757 compartments, 1 M expTwo synapses and
 import numpy as np
 import pytest
 
+import eden_port
 import routing
+from criteria import box_violations, samecount
+from helpers import spike_trains
 from eden_gb300 import lowering, workloads
-from eden_gb300.engine import MODE_BATCHED, Simulation
+from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
 
 pytestmark = pytest.mark.gpu
 
@@ -45,3 +51,26 @@ def test_full_size_routing_and_bounds(name, length_ms):
         assert np.isfinite(rec.trace).all()
     finally:
         sim.close()
+
+
+@pytest.fixture(scope="module")
+def full_multicomp():
+    low = lowering.lower(workloads.multicomp_net(length_ms=10.0))
+    return low, eden_port.run(low, n_steps=400)
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+def test_full_size_parity_first_10ms(full_multicomp, mode):
+    low, ref = full_multicomp
+    sim = Simulation(low, mode=mode, record_capacity_steps=408)
+    try:
+        rec = sim.run(400)
+    finally:
+        sim.close()
+    shift = int(round(0.1 / (float(low.dt) * 1e-3)))
+    wrong, far = samecount(spike_trains(ref["spike_src"], ref["spike_step"]),
+                           spike_trains(rec.spike_src, rec.spike_step), shift)
+    assert not wrong, f"{len(wrong)} cells with a different spike count, e.g. {wrong[:5]}"
+    assert not far, f"{len(far)} cells with a spike more than 0.1 ms off, e.g. {far[:5]}"
+    nbad, worst = box_violations(ref["trace"], rec.trace, float(low.dt) * 1e-3, 0.1, 0.5)
+    assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst {worst} mV"

@@ -25,13 +25,17 @@ pytestmark = pytest.mark.gpu
 
 # networks checked against the oracle only (no reference fixtures): HH
 # channels and synapses on dendrites, so that non-flat compartments sit
-# inside the trees with flat ones above and below them; and the mixed
-# point-neuron / multicompartment network
+# inside the trees with flat ones above and below them; the mixed
+# point-neuron / multicompartment network; and large cells whose trees are
+# wider than a warp at some depth
 EXTRA = {
     "multicomp_active_dendrites": lambda: workloads.multicomp_net(
         n_cells=24, in_degree=20, length_ms=40.0, max_seg=80, n_recorded=6, hh_dend_frac=0.2,
         syn_on_dendrites=True),
     "mixed_small": lambda: workloads.mixed_scale(n_izh=400, n_mc=100, in_degree=20, length_ms=30.0, n_seg=30),
+    # cells of up to 500 compartments, one with 83 compartments at one depth
+    "multicomp_large_cells": lambda: workloads.multicomp_net(n_cells=12, in_degree=20, length_ms=30.0, max_seg=500,
+                                                             n_recorded=6),
 }
 
 
