@@ -134,7 +134,19 @@ __global__ void __launch_bounds__(kInputThreads) k_inputs_t(DevModel m, const Wi
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     float *tileA = tiles[threadIdx.x >> 5][0], *tileB = tiles[threadIdx.x >> 5][1];
-    for (int c = warp; c < m.n_chunk; c += nwarps) chunk_window(m, c, w, tileA, tileB, tk);
+    // each warp walks its chunks with the next chunk's descriptor in flight
+    int c = warp;
+    int32_t info = 0;
+    int64_t i0 = 0;
+    if (c < m.n_chunk) { info = m.ck_info[c]; i0 = m.ck_i0[c]; }
+    while (c < m.n_chunk) {
+        const int cn = c + nwarps;
+        int32_t info_n = 0;
+        int64_t i0_n = 0;
+        if (cn < m.n_chunk) { info_n = m.ck_info[cn]; i0_n = m.ck_i0[cn]; }
+        chunk_window(m, c, info, i0, w, tileA, tileB, tk);
+        c = cn; info = info_n; i0 = i0_n;
+    }
 }
 
 // Per-step path, phase 2: one thread per target.
@@ -1071,6 +1083,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     }
     bk_c0[n_block] = (int32_t)ck_blk.size();
     const int n_chunk = (int)ck_blk.size();
+    std::vector<int32_t> ck_info(n_chunk);
+    for (int c = 0; c < n_chunk; c++)
+        ck_info[c] = bk_kind[ck_blk[c]] | ((int32_t)bk_type[ck_blk[c]] << 2) | (ck_n[c] << 8);
 
     // ---- window length: every delay must cover the window (see k_window)
     int kmax = kMaxWindow;
@@ -1251,6 +1266,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.bk_type, bk_type)); TRY(upload_c(ctx, &d.bk_erev, bk_erev));
     TRY(upload_c(ctx, &d.bk_c0, bk_c0)); TRY(upload_c(ctx, &d.ck_blk, ck_blk));
     TRY(upload_c(ctx, &d.ck_i0, ck_i0)); TRY(upload_c(ctx, &d.ck_n, ck_n));
+    TRY(upload_c(ctx, &d.ck_info, ck_info));
     TRY(upload(ctx, &d.Gp, (const float *)nullptr, (size_t)32 * (size_t)std::max(n_chunk, 1)));
     TRY(upload(ctx, &d.ck_a, (const float *)nullptr, (size_t)std::max(n_chunk, 1)));
     TRY(upload(ctx, &d.ck_b, (const float *)nullptr, (size_t)std::max(n_chunk, 1)));
@@ -1355,8 +1371,14 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         int64_t b = (n + kThreads - 1) / kThreads;
         return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)ctx->n_sm * 32));
     };
-    ctx->grid_inputs = (int)std::max<int64_t>(
-        1, std::min<int64_t>(((int64_t)n_chunk * 32 + kInputThreads - 1) / kInputThreads, (int64_t)ctx->n_sm * 64));
+    {
+        // resident blocks only: each warp then walks several chunks
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_inputs_t, kInputThreads, 0);
+        ctx->grid_inputs = (int)std::max<int64_t>(
+            1, std::min<int64_t>(((int64_t)n_chunk * 32 + kInputThreads - 1) / kInputThreads,
+                                 (int64_t)ctx->n_sm * std::max(per_sm, 1)));
+    }
     ctx->grid_targets = blocks_for(nt);
     ctx->grid_hines = (int)std::max<int64_t>(1, ((int64_t)d.n_forest * 32 + kHinesThreads - 1) / kHinesThreads);
     ctx->grid_deliver = ctx->n_sm * 4;

@@ -116,6 +116,7 @@ struct DevModel {
     int32_t n_chunk;
     const int32_t *bk_c0;             // [n_block + 1] chunk range of each block
     const int32_t *ck_blk;            // block of each chunk
+    const int32_t *ck_info;           // kind | synapse type << 2 | items << 8
     const int64_t *ck_i0;             // first item of each chunk
     const int32_t *ck_n;              // items in the chunk
     float *Gp;                        // [32 * n_chunk]
@@ -286,24 +287,25 @@ __device__ __forceinline__ bool replay_mask(uint32_t mask, const WindowArgs &w, 
 // A synapse's own state at the start of step s from its value just after its
 // event at step `last`: the reference's per-step a - dt*(a/tau), in closed
 // form a * f^n with f = 1 - dt/tau (used only for the decay its event replaces).
-__device__ __forceinline__ float decayed(float a, float f, int n) {
-    return n > 0 ? a * powf(f, (float)n) : a;
+__device__ __forceinline__ float decayed(float a, float f, const float *fpow, int n) {
+    if (n <= 0) return a;
+    return a * (n < kPowLen ? fpow[n] : powf(f, (float)n));
 }
 
 // The contribution (dA, dB) of one synapse's event at step s to its chunk's
 // aggregate, and the synapse's own state after it.
 template <int KIND>
-__device__ __forceinline__ void input_event(const SynTypeDev &st, float dt, float w, int64_t s, float &a, float &b,
-                                            int32_t &last, float &dA, float &dB) {
+__device__ __forceinline__ void input_event(const SynTypeDev &st, const float *pw, float dt, float w, int64_t s,
+                                            float &a, float &b, int32_t &last, float &dA, float &dB) {
     const int n = (int)(s - (int64_t)last) - 1;
     if (KIND == EDEN_SYN_EXPTWO) {
-        const float ai = decayed(a, st.f_rise, n), bi = decayed(b, st.f_decay, n);
+        const float ai = decayed(a, st.f_rise, pw, n), bi = decayed(b, st.f_decay, pw + kPowLen, n);
         dA = w * (dt * div_by_tau(ai, st.tau_rise, st.r_rise) + st.wf_w);
         dB = w * (dt * div_by_tau(bi, st.tau_decay, st.r_decay) + st.wf_w);
         a = ai + st.wf_w;
         b = bi + st.wf_w;
     } else {
-        const float gi = decayed(a, st.f_decay, n);
+        const float gi = decayed(a, st.f_decay, pw + kPowLen, n);
         dA = w * (dt * div_by_tau(gi, st.tau_decay, st.r_decay) + st.gbase);
         dB = 0.0f;
         a = gi + st.gbase;
@@ -339,7 +341,7 @@ __device__ __forceinline__ void pois_fire(const DevModel &m, int64_t it, const S
     float a = m.po_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.po_b[it] : 0.0f;
     int32_t last = m.po_last[it];
     float dA, dB;
-    input_event<KIND>(st, m.dt, m.po_w[it], s, a, b, last, dA, dB);
+    input_event<KIND>(st, m.syn_pow + (size_t)m.po_type[it] * 2 * kPowLen, m.dt, m.po_w[it], s, a, b, last, dA, dB);
     m.po_a[it] = a;
     if (KIND == EDEN_SYN_EXPTWO) m.po_b[it] = b;
     m.po_last[it] = last;
@@ -424,12 +426,13 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
     int32_t last = m.sy_last[it];
     const float wt = m.sy_w[it];
     float dA, dB;
+    const float *pw = m.syn_pow + (size_t)m.sy_type[it] * 2 * kPowLen;
     if (now && jf != 0) {
-        input_event<KIND>(st, dt, wt, w.step0, a, b, last, dA, dB);
+        input_event<KIND>(st, pw, dt, wt, w.step0, a, b, last, dA, dB);
         put_event(rowA, rowB, used, w.K, 0, dA, dB);
     }
     if (jf >= 0) {
-        input_event<KIND>(st, dt, wt, w.step0 + jf, a, b, last, dA, dB);
+        input_event<KIND>(st, pw, dt, wt, w.step0 + jf, a, b, last, dA, dB);
         put_event(rowA, rowB, used, w.K, jf, dA, dB);
     }
     m.sy_a[it] = a;
@@ -450,16 +453,15 @@ constexpr int kAccStride = 33;
 // steps the chunk's aggregate state through the window, lane j keeping the
 // exposure of step j (the conductance before the step's update, as the
 // reference exposes it) for Gp[j][chunk].
-__device__ __forceinline__ void chunk_window(const DevModel &m, int c, const WindowArgs &w, float *tileA,
-                                             float *tileB, const float *tk) {
+__device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t info, int64_t ck_i0,
+                                             const WindowArgs &w, float *tileA, float *tileB, const float *tk) {
     const int lane = threadIdx.x & 31;
-    const int bk = m.ck_blk[c];
-    const int kind = m.bk_kind[bk];
-    const int n = m.ck_n[c];
+    const int kind = info & 3;
+    const int n = info >> 8;
     float *rowA = tileA + lane * kAccStride, *rowB = tileB + lane * kAccStride;
     if (kind == BK_PULSE) {
         for (int r = 0; lane + 32 * r < n; r++) {
-            const int64_t it = m.ck_i0[c] + lane + 32 * r;
+            const int64_t it = ck_i0 + lane + 32 * r;
             const float st = m.pu_start[it], du = m.pu_dur[it], aw = m.pu_amp[it] * m.pu_w[it];
             for (int j = 0; j < w.K; j++) {
                 const float tf = tk[j];
@@ -477,12 +479,14 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, const Win
         __syncwarp();
         return;
     }
-    const int type = m.bk_type[bk];
+    const int type = (info >> 2) & 63;
     const SynTypeDev st = c_syn_types[type];
     const bool two = st.kind == EDEN_SYN_EXPTWO;
     bool used = false;
-    // the items' per-window state, loaded up front so the loads overlap
-    const int64_t i0 = m.ck_i0[c] + lane;
+    // the chunk's aggregate and its items' per-window state, loaded up front
+    // so the loads overlap
+    float A = m.ck_a[c], B = m.ck_b[c];
+    const int64_t i0 = ck_i0 + lane;
     float s0v[kChunkItems / 32], s1v[kChunkItems / 32];
 #pragma unroll
     for (int r = 0; r < kChunkItems / 32; r++) {
@@ -510,7 +514,7 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, const Win
     const unsigned rows = __ballot_sync(0xffffffffu, used);
     __syncwarp();
     const float dt = m.dt;
-    float A = m.ck_a[c], B = m.ck_b[c], gj = 0.0f;
+    float gj = 0.0f;
     if (rows == 0) {
         // no event in the window: the aggregate decays in closed form,
         // A f^j, from the factors' powers (syn_pow)
@@ -532,19 +536,29 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, const Win
             ea += tileA[q * kAccStride + lane];
             eb += tileB[q * kAccStride + lane];
         }
-    for (int j = 0; j < w.K; j++) {
-        const float eaj = __shfl_sync(0xffffffffu, ea, j), ebj = __shfl_sync(0xffffffffu, eb, j);
-        const float g = two ? st.gbase * (B - A) : A;
-        if (lane == j) gj = g;
-        if (w.step0 + j <= 0) {
-            if (two) { A = 0.0f; B = 0.0f; }
-        } else if (two) {
-            A = A - dt * div_by_tau(A, st.tau_rise, st.r_rise) + eaj;
-            B = B - dt * div_by_tau(B, st.tau_decay, st.r_decay) + ebj;
-        } else {
-            A = A - dt * div_by_tau(A, st.tau_decay, st.r_decay) + eaj;
+    // the aggregate over the window: with one step's decay factor f,
+    // X_j = f^j X_0 + sum_{i<j} f^(j-1-i) e_i, the sums by a scan over the lanes
+    const float *pr = m.syn_pow + (size_t)type * 2 * kPowLen, *pd = pr + kPowLen;
+    const float *pa = two ? pr : pd;
+    float va = lane < w.K ? ea : 0.0f, vb = lane < w.K ? eb : 0.0f;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float ua = __shfl_up_sync(0xffffffffu, va, d), ub = __shfl_up_sync(0xffffffffu, vb, d);
+        if (lane >= d) {
+            va = fmaf(pa[d], ua, va);
+            vb = fmaf(pd[d], ub, vb);
         }
     }
+    // lane j: sums of the events before step j
+    float sa = __shfl_up_sync(0xffffffffu, va, 1), sb = __shfl_up_sync(0xffffffffu, vb, 1);
+    if (lane == 0) { sa = 0.0f; sb = 0.0f; }
+    if (lane < w.K) {
+        const float Aj = A * pa[lane] + sa, Bj = B * pd[lane] + sb;
+        gj = two ? st.gbase * (Bj - Aj) : Aj;
+    }
+    const float ta = __shfl_sync(0xffffffffu, va, w.K - 1), tb = __shfl_sync(0xffffffffu, vb, w.K - 1);
+    A = A * pa[w.K] + ta;
+    B = two ? B * pd[w.K] + tb : B;
     if (lane < w.K) m.Gp[(size_t)lane * m.n_chunk + c] = gj;
     if (lane == 0) { m.ck_a[c] = A; m.ck_b[c] = B; }
     __syncwarp();
