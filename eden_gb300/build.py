@@ -11,10 +11,15 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libeden_gpu.so")
-SOURCES = [os.path.join(HERE, "csrc", f) for f in ("eden_gpu.cu", "eden_kernels.cuh", "eden_math.cuh")]
 HEADER = os.path.join(ROOT, "include", "eden_gpu.h")
+SOURCES = [os.path.join(HERE, "csrc", f) for f in ("eden_gpu.cu", "eden_codegen.cuh", "eden_window.cuh",
+                                                   "eden_kernels.cuh", "eden_math.cuh")]
+# the kernel sources the library compiles again at run time (NVRTC), in
+# dependency order; build() embeds them as csrc/_rtc_src.inc
+RTC_SOURCES = [HEADER] + [os.path.join(HERE, "csrc", f) for f in ("eden_math.cuh", "eden_kernels.cuh",
+                                                                 "eden_window.cuh")]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared", "-ldl"]
 
 
 def nvcc() -> str:
@@ -31,8 +36,36 @@ def needs_build() -> bool:
     return any(os.path.getmtime(s) > t for s in SOURCES + [HEADER])
 
 
+def embed_rtc_sources() -> str:
+    """Writes csrc/_rtc_src.inc: the kernel headers as string literals, with
+    their local #include lines and #pragma once removed (they are joined in
+    dependency order)."""
+    parts = []
+    for path in RTC_SOURCES:
+        text = []
+        for line in open(path).read().splitlines():
+            if line.startswith('#include "') or line.strip() == "#pragma once":
+                continue
+            text.append(line)
+        body = "\n".join(text) + "\n"
+        # raw-string chunks below the compilers' literal limits
+        for k in range(0, len(body), 30000):
+            parts.append(body[k:k + 30000])
+    out = os.path.join(HERE, "csrc", "_rtc_src.inc")
+    with open(out + ".tmp", "w") as f:
+        f.write("// generated by eden_gb300/build.py from " + ", ".join(os.path.basename(p) for p in RTC_SOURCES) + "\n")
+        f.write("static const char *const kRtcSourceParts[] = {\n")
+        for chunk in parts:
+            assert ")EDENRTC" not in chunk
+            f.write('R"EDENRTC(' + chunk + ')EDENRTC",\n')
+        f.write("};\n")
+    os.replace(out + ".tmp", out)
+    return out
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     if force or needs_build():
+        embed_rtc_sources()
         cmd = [nvcc(), *NVCC_FLAGS, os.path.join(HERE, "csrc", "eden_gpu.cu"), "-o", LIB + ".tmp"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -28,10 +29,6 @@ using namespace eden;
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kInputThreads = 128;  // k_inputs_t: four warps, each with two event tiles
-constexpr int kCellThreads = 128;   // k_cells_t: four warps
-constexpr int kHinesThreads = 128;  // k_hines_t: four warps, each staging one forest
 constexpr int kForestNodes = 512;   // largest forest (a larger cell gets a forest of its own)
 constexpr int kGraphWindows = 16;  // windows per captured graph
 
@@ -95,6 +92,12 @@ struct EdenGpuCtx {
     double k_ms[EDEN_KERNEL_KINDS] = {0};
     int64_t k_n[EDEN_KERNEL_KINDS] = {0};
     int sticky_status = 0;
+    // the windowed kernels launched: the built-in ones or those compiled for
+    // this model at creation (eden_codegen.cuh)
+    const void *fn_inputs = nullptr, *fn_cells = nullptr, *fn_deliver = nullptr;
+    bool codegen_used = false;
+    std::string codegen_source, codegen_note;
+    double codegen_ms = 0.0;
 
     int fail(int code, const char *fmt, ...) {
         char buf[1024];
@@ -115,365 +118,18 @@ struct EdenGpuCtx {
                                "%s failed: %s", #call, cudaGetErrorString(e_));                     \
     } while (0)
 
-// ---------------------------------------------------------------------------
-// kernels; each reads its WindowArgs from a device table so that a captured
-// graph can be replayed over many windows
-// ---------------------------------------------------------------------------
-namespace eden {
+#include "eden_window.cuh"
+#include "eden_codegen.cuh"
 
-// Phase 1 of both paths: input blocks over the window, one warp per target
-// with inputs (the per-step path runs it with K = 1).
-__global__ void __launch_bounds__(kInputThreads) k_inputs_t(DevModel m, const WindowArgs *tab,
-                                                             const WindowTimes *ttab, const int *base, int idx) {
-    __shared__ float tiles[kInputThreads / 32][2][32 * kAccStride];
-    __shared__ float tk[64];  // the window's step times, then the previous window's
-    const int wi = *base + idx;
-    const WindowArgs w = tab[wi];
-    if (threadIdx.x < 64) tk[threadIdx.x] = threadIdx.x < 32 ? ttab[wi].tk[threadIdx.x] : ttab[wi].tprev[threadIdx.x - 32];
-    __syncthreads();
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    float *tileA = tiles[threadIdx.x >> 5][0], *tileB = tiles[threadIdx.x >> 5][1];
-    // each warp walks its chunks with the next chunk's descriptor in flight
-    int c = warp;
-    int32_t info = 0;
-    int64_t i0 = 0;
-    if (c < m.n_chunk) { info = m.ck_info[c]; i0 = m.ck_i0[c]; }
-    while (c < m.n_chunk) {
-        const int cn = c + nwarps;
-        int32_t info_n = 0;
-        int64_t i0_n = 0;
-        if (cn < m.n_chunk) { info_n = m.ck_info[cn]; i0_n = m.ck_i0[cn]; }
-        chunk_window(m, c, info, i0, w, tileA, tileB, tk);
-        c = cn; info = info_n; i0 = i0_n;
-    }
+namespace {
+// Launch of a kernel given by handle (a built-in __global__ function or a
+// kernel loaded from the model's compiled library).
+template <typename... A>
+cudaError_t launch_k(const void *fn, int grid, int block, size_t smem, cudaStream_t s, A... args) {
+    void *argv[] = {(void *)&args...};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), argv, smem, s);
 }
-
-// Per-step path, phase 2: one thread per target.
-__global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
-    const WindowArgs w = tab[*base + idx];
-    const bool init = w.step0 <= 0;
-    const float *vin = m.v[w.par];
-    float *vout = m.v[w.par ^ 1];
-    const int n = m.n_target;
-    const int nround = (n + 31) & ~31;  // whole warps stay converged for the spike ballot
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += gridDim.x * blockDim.x) {
-        if (i < n) {
-            float v = vin[i], Iin, Gin, Isyn, Gsyn;
-            block_currents(m.Gp, m.t_blk0[i], m.t_blk0[i + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
-                           Gsyn);
-            target_step(m, i, init, w.step0, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar);
-        }
-    }
-}
-
-// Per-step path, phase 3: one warp per forest, staged in the warp's slice of
-// shared memory when the forest has at most `cap` compartments.
-__global__ void __launch_bounds__(kHinesThreads) k_hines_t(DevModel m, const WindowArgs *tab, const int *base, int idx, int cap) {
-    extern __shared__ float sm[];
-    const WindowArgs w = tab[*base + idx];
-    const bool init = w.step0 <= 0;
-    const float *vin = m.v[w.par];
-    float *x = m.v[w.par ^ 1];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    // per-warp slice: D, X, U, L, V, child ends, parents, depth boundaries (cap each)
-    float *sD = sm + (size_t)wib * 8 * cap, *sX = sD + cap, *sU = sX + cap, *sL = sU + cap, *sV = sL + cap;
-    int32_t *sCE = (int32_t *)(sV + cap), *sP = sCE + cap, *sLV = sP + cap;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int f = warp; f < m.n_forest; f += nwarps) {
-        const int c0 = m.fo_t0[f], n = m.fo_t1[f] - c0, nlev = m.fo_nlev[f];
-        const int32_t *lv = m.lvl + m.fo_l0[f];
-        if (n <= cap && nlev < cap) {
-            for (int i = lane; i < n; i += 32) {
-                sD[i] = m.diag[c0 + i]; sX[i] = x[c0 + i]; sU[i] = m.c_u[c0 + i];
-                sL[i] = m.c_l[c0 + i]; sV[i] = vin[c0 + i];
-                sCE[i] = m.c_cend[c0 + i] - c0; sP[i] = m.c_parent[c0 + i] - c0;
-            }
-            for (int i = lane; i <= nlev; i += 32) sLV[i] = lv[i] - c0;
-            __syncwarp();
-            hines_forest(m, init, w.step0, sD, sX, sU, sL, sCE, sP, sLV, nlev, sV, c0, w.wpar, true);
-            __syncwarp();
-            for (int i = lane; i < n; i += 32) x[c0 + i] = sX[i];
-            __syncwarp();
-        } else {
-            hines_forest(m, init, w.step0, m.diag, x, m.c_u, m.c_l, m.c_cend, m.c_parent, lv, nlev, vin, 0, w.wpar, true);
-        }
-    }
-}
-
-// Fan the spikes of window `w` out to their synapses' trigger masks
-// (bit = logging step - window start = the step at which the reference reads
-// the trigger, eden/Eden.cpp:3964-3992) and append them to the spike log.
-__global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
-    const WindowArgs w = tab[*base + idx];
-    const int wp = w.wpar;
-    const int n = m.wspk_count[wp];
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    // the other parity's list was consumed by the previous window's delivery
-    // and is refilled only by the next window: clear it for that window
-    if (blockIdx.x == 0 && threadIdx.x == 0) m.wspk_count[wp ^ 1] = 0;
-    for (int e = warp; e < n; e += nwarps) {
-        int src = m.wspk_src[wp][e];
-        int log_step = m.wspk_step[wp][e];
-        uint32_t bit = 1u << (uint32_t)(log_step - w.step0);
-        int64_t f0 = m.fan0[src], f1 = m.fan0[src + 1];
-        for (int64_t f = f0 + lane; f < f1; f += 32) atomicOr(&m.sy_mask[m.fan_syn[f]], bit);
-        if (lane == 0) {
-            unsigned long long slot = atomicAdd(m.log_count, 1ull);
-            if ((int64_t)slot < m.log_cap) {
-                m.log_src[slot] = src;
-                m.log_step[slot] = log_step;
-            } else {
-                atomicOr(m.status, ST_LOG_OVERFLOW);
-            }
-        }
-    }
-}
-
-// Windowed path: every warp advances one unit (a forest of physical cells or
-// a batch of izhikevich neurons) K steps on its own, synchronising only within
-// the warp.  Within a window no cell reads another cell's state: the only
-// coupling is through synaptic triggers, and every connection delay is
-// >= K * dt, so a spike emitted inside the window cannot fire a synapse before
-// the window ends.  Its trigger bits are delivered after the window
-// (k_deliver_t) and replayed in order at the start of the next one
-// (replay_mask), which reproduces the step-by-step pending-spike decisions
-// exactly.  Synaptic conductances do not depend on V, so k_inputs_t has
-// already produced them for all K steps.  Everything else a step reads is
-// staged in the warp's shared-memory slice for the whole window.
-
-// A forest unit over the window.  At the window start the unit stages its
-// compartments, its non-flat compartments' descriptors, its gates with their
-// parameter records, and the conductance series of its input chunks for all
-// K steps (written by k_inputs_t), so that a step reads shared memory only.
-// Per step: trajectory samples of the step's starting V; the non-flat
-// compartments' currents (inputs, channels with the gate values before this
-// step's update), diagonal and pre-update; the cable solve, which also
-// applies the flat compartments' constant pre-update; gate updates from the
-// starting V; threshold crossings.
-__device__ __forceinline__ void forest_window(const DevModel &m, const WindowArgs &w, int u, float *S) {
-    const int lane = threadIdx.x & 31;
-    const int t0 = m.un_t0[u], n = m.un_t1[u] - t0, fi = m.un_f[u];
-    const int ngt = m.un_ngt[u], gt0 = m.un_gt0[u];
-    const int s0 = m.un_s0[u], ns = m.un_s1[u] - s0;
-    const int r0 = m.un_r0[u], r1 = m.un_r1[u];
-    const int nf0 = m.un_nf0[u], nf = m.un_nf1[u] - nf0;
-    const int nlev = m.fo_nlev[fi], l0 = m.fo_l0[fi];
-    const int ub0 = m.t_blk0[t0], nblk = m.t_blk0[t0 + n] - ub0;
-    const int uc0 = m.bk_c0[ub0], nck = m.bk_c0[ub0 + nblk] - uc0;
-    float *X = S, *KC = S + n, *L = S + 2 * n, *PV = S + 3 * n, *RT = S + 4 * n, *U = S + 5 * n;
-    uint32_t *CEP = (uint32_t *)(S + 6 * n);
-    int32_t *NT = (int32_t *)(S + 7 * n);
-    float *VO = (float *)(NT + nf), *NA = VO + nf, *NC = NA + nf, *NIR = NC + nf;
-    int32_t *NB0 = (int32_t *)(NIR + nf), *NB1 = NB0 + nf, *NCH0 = NB1 + nf, *NCH1 = NCH0 + nf;
-    const int uch0 = nf > 0 ? m.nf_c0[nf0] : 0, nch = nf > 0 ? m.nf_c1[nf0 + nf - 1] - uch0 : 0;
-    float *CHG = (float *)(NCH1 + nf), *CHE = CHG + nch;
-    int32_t *CHQ = (int32_t *)(CHE + nch), *CHI = CHQ + nch;
-    float *GT = (float *)(CHI + nch);
-    int32_t *GI_S = (int32_t *)(GT + ngt);
-    float *GP = (float *)(GI_S + ngt);
-    int32_t *LV = (int32_t *)(GP + kGateWords * ngt);
-    int32_t *ST = LV + nlev + 1, *SSRC = ST + ns;
-    float *STHR = (float *)(SSRC + ns);
-    int32_t *BKK = (int32_t *)(STHR + ns);
-    float *BKE = (float *)(BKK + nblk);
-    int32_t *BKC = (int32_t *)(BKE + nblk);
-    float *GS = (float *)(BKC + nblk + 1);
-    // ---- stage the unit
-    const float *vsrc = m.v[w.par];
-    for (int i = lane; i < n; i += 32) {
-        const int t = t0 + i;
-        X[i] = vsrc[t]; KC[i] = m.c_kc[t]; L[i] = m.c_l[t]; PV[i] = m.c_pv0[t];
-        RT[i] = m.c_rt0[t]; U[i] = m.c_u[t]; CEP[i] = m.c_cep[t];
-    }
-    for (int j = lane; j < nf; j += 32) {
-        const int ti = m.nf_t[nf0 + j], t = t0 + ti;
-        NT[j] = ti; NA[j] = m.c_area[t]; NC[j] = m.c_cm[t]; NIR[j] = m.c_inv_rc[t];
-        NB0[j] = m.t_blk0[t] - ub0; NB1[j] = m.t_blk0[t + 1] - ub0;
-        const int ch0 = m.c_chan0[t], ch1 = m.c_chan0[t + 1];
-        NCH0[j] = m.nf_c0[nf0 + j] - uch0; NCH1[j] = m.nf_c1[nf0 + j] - uch0;
-        // gate update items: the non-flat slot and the gate's parameter record
-        for (int ch = ch0; ch < ch1; ch++) {
-            const int q0 = m.ch_gate0[ch] - gt0, q1 = m.ch_gate0[ch + 1] - gt0;
-            const float *src = m.gate_par + (size_t)m.ch_type[ch] * EDEN_MAX_GATES * kGateWords;
-            for (int q = q0; q < q1; q++) {
-                GI_S[q] = j;
-                for (int k = 0; k < kGateWords; k++) GP[q * kGateWords + k] = src[(q - q0) * kGateWords + k];
-            }
-        }
-    }
-    for (int c = lane; c < nch; c += 32) {
-        CHG[c] = m.nfc_g[uch0 + c]; CHE[c] = m.nfc_e[uch0 + c]; CHQ[c] = m.nfc_q[uch0 + c]; CHI[c] = m.nfc_i[uch0 + c];
-    }
-    for (int i = lane; i < ngt; i += 32) GT[i] = m.gate[gt0 + i];
-    for (int i = lane; i <= nlev; i += 32) {
-        const int info = m.lvl_info[l0 + i];
-        LV[i] = (m.lvl[l0 + i] - t0) | ((info & 0x80) ? kLvNonFlat : 0);
-    }
-    for (int i = lane; i < ns; i += 32) { ST[i] = m.gs_t[s0 + i]; SSRC[i] = m.gs_src[s0 + i]; STHR[i] = m.gs_thr[s0 + i]; }
-    for (int b = lane; b <= nblk; b += 32) {
-        BKC[b] = m.bk_c0[ub0 + b] - uc0;
-        if (b < nblk) { BKK[b] = m.bk_kind[ub0 + b]; BKE[b] = m.bk_erev[ub0 + b]; }
-    }
-    for (int k = 0; k < w.K; k++)
-        for (int c = lane; c < nck; c += 32) GS[k * nck + c] = m.Gp[(size_t)k * m.n_chunk + uc0 + c];
-    __syncwarp();
-    const float dt = m.dt;
-    for (int k = 0; k < w.K; k++) {
-        const int64_t step = w.step0 + k;
-        const bool init = step <= 0;
-        if (!init) {
-            // trajectory samples of this step's starting state
-            const int64_t row = (step - 1) % m.trace_cap;
-            for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = X[m.gr_t[q]];
-        }
-        __syncwarp();
-        const float *Gk = GS + k * nck;
-        for (int j = lane; j < nf; j += 32) {
-            // channels + voltage pre-update (eden/Eden.cpp:5013-6107)
-            const int ti = NT[j];
-            const float v = X[ti];
-            VO[j] = v;
-            float Iin, Gin, Isyn, Gsyn;
-            block_currents(Gk, NB0[j], NB1[j], BKK, BKE, BKC, 0, v, Iin, Gin, Isyn, Gsyn);
-            const float A = NA[j];
-            float Ich = 0.f, Gch = 0.f;
-            for (int c = NCH0[j]; c < NCH1[j]; c++) {
-                const int gi_pack = CHI[c];
-                const float *q = GT + CHQ[c];
-                float fopen = 1.0f;
-                for (int gi = 0; gi < (gi_pack & 7); gi++) {
-                    const float qo = q[gi];
-                    const int inst = (gi_pack >> (3 + 5 * gi)) & 31;
-                    for (int rr = 0; rr < inst; rr++) fopen = fopen * qo;
-                }
-                const float gs = CHG[c] * fopen;
-                Ich += (gs * (CHE[c] - v) * 1e-5f) * A;
-                Gch += (gs * 1e-5f) * A;
-            }
-            const float I = Ich + Iin + Isyn;
-            const float G = Gch + Gin + Gsyn;
-            const float C = NC[j];
-            PV[ti] = 1.0f * (G / C) + NIR[j];
-            X[ti] = init ? v : v + (dt * (I + (v * G))) / C;
-        }
-        __syncwarp();
-        if (!init) hines_window(dt, X, KC, L, PV, RT, U, CEP, LV, nlev);
-        // gate updates from this step's starting V and gate values (the
-        // currents above used the values before the update, as the reference does)
-        for (int q = lane; q < ngt; q += 32)
-            GT[q] = gate_next_p(GP + q * kGateWords, init, dt, VO[GI_S[q]], GT[q]);
-        // threshold crossings of the unit's spike sources (eden/Eden.cpp:6247-6252)
-        for (int q0 = 0; q0 < ns; q0 += 32) {
-            const int q = q0 + lane;
-            bool spk = false;
-            int src = -1;
-            if (q < ns) {
-                const int sl = ST[q];
-                src = SSRC[q];
-                spk = VO[sl] < STHR[q] && STHR[q] < X[NT[sl]];
-            }
-            push_spike(m, spk, src, (int32_t)(step + 1), w.wpar);
-        }
-        __syncwarp();
-    }
-    // ---- write the unit back into the buffer that holds the window's final state
-    float *vdst = m.v[w.par ^ (w.K & 1)];
-    for (int i = lane; i < n; i += 32) vdst[t0 + i] = X[i];
-    for (int i = lane; i < ngt; i += 32) m.gate[gt0 + i] = GT[i];
-}
-
-// A batch of up to 32 izhikevich2007Cell neurons over the window
-// (LEMS_CoreComponents.inc.xml:1140-1185), one lane each.
-__device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &w, int u, float *S) {
-    const int lane = threadIdx.x & 31;
-    const int t0 = m.un_t0[u], n = m.un_t1[u] - t0;
-    const int r0 = m.un_r0[u], r1 = m.un_r1[u];
-    // slice: V (two buffers), then C, v0, k, vr, vt, vpeak, a, b, c, d, u
-#define IZ(f, i) S[(2 + (f)) * n + (i)]
-    const int izh0 = m.t_izh[t0];
-    for (int i = lane; i < n; i += 32) {
-        const int iz = izh0 + i;
-        S[w.par * n + i] = m.v[w.par][t0 + i];
-        IZ(0, i) = m.iz_C[iz]; IZ(1, i) = m.iz_v0[iz]; IZ(2, i) = m.iz_k[iz]; IZ(3, i) = m.iz_vr[iz];
-        IZ(4, i) = m.iz_vt[iz]; IZ(5, i) = m.iz_vpeak[iz]; IZ(6, i) = m.iz_a[iz]; IZ(7, i) = m.iz_b[iz];
-        IZ(8, i) = m.iz_c[iz]; IZ(9, i) = m.iz_d[iz]; IZ(10, i) = m.iz_u[iz];
-    }
-    __syncwarp();
-    int par = w.par;
-    const float dt = m.dt;
-    for (int k = 0; k < w.K; k++) {
-        const int64_t step = w.step0 + k;
-        const bool init = step <= 0;
-        const float *vin = S + par * n;
-        float *vout = S + (par ^ 1) * n;
-        const float *Gpk = m.Gp + (size_t)k * m.n_chunk;
-        const int i = lane;
-        bool spike = false;
-        int src = -1;
-        if (i < n) {
-            const int t = t0 + i;
-            const float v = vin[i];
-            float Iin, Gin, Isyn, Gsyn;
-            block_currents(Gpk, m.t_blk0[t], m.t_blk0[t + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
-                           Gsyn);
-            const float uu = IZ(10, i);
-            const float vr = IZ(3, i);
-            const float imemb = ((IZ(2, i) * (v - vr)) * 1e-3f) * (v - IZ(4, i)) + (Isyn + Iin) - uu;
-            float vn, un;
-            if (init) {
-                vn = IZ(1, i);
-                un = 0.0f;
-            } else {
-                vn = v + dt * (imemb / IZ(0, i));
-                const float du = (IZ(6, i) * ((IZ(7, i) * (v - vr)) - uu)) * 1e-3f;
-                un = uu + dt * du * 1e3f;
-                if (v > IZ(5, i)) {
-                    vn = IZ(8, i);
-                    un = uu + IZ(9, i);
-                    spike = true;
-                }
-            }
-            vout[i] = vn;
-            IZ(10, i) = un;
-            src = m.t_src[t];
-        }
-        push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar);
-        if (!init) {
-            const int64_t row = (step - 1) % m.trace_cap;
-            for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = vin[m.gr_t[q]];
-        }
-        __syncwarp();
-        par ^= 1;
-    }
-    for (int i = lane; i < n; i += 32) {
-        m.v[par][t0 + i] = S[par * n + i];
-        m.iz_u[izh0 + i] = IZ(10, i);
-    }
-}
-#undef IZ
-
-// This launch runs CTAs [cta_begin, cta_end), each a few units, one per warp.
-__global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const WindowArgs *tab, const int *base, int idx,
-                                                          int cta_begin, int cta_end) {
-    extern __shared__ float sm[];
-    const WindowArgs w = tab[*base + idx];
-    const int warp = threadIdx.x >> 5;
-    for (int cta = cta_begin + blockIdx.x; cta < cta_end; cta += gridDim.x) {
-        const int u = m.cta_u0[cta] + warp;
-        if (u >= m.cta_u0[cta + 1]) continue;
-        if (m.un_f[u] >= 0) forest_window(m, w, u, sm + m.un_off[u]);
-        else izh_window(m, w, u, sm + m.un_off[u]);
-    }
-}
-
-__global__ void k_bump(int *base, int by) { *base += by; }
-
-}  // namespace eden
+}  // namespace
 
 // ---------------------------------------------------------------------------
 namespace {
@@ -595,6 +251,18 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
 extern "C" int edenGpuAbiVersion(void) { return EDEN_GPU_ABI_VERSION; }
 
 extern "C" const char *edenGpuLastError(EdenGpuCtx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+extern "C" int64_t edenGpuGeneratedSource(EdenGpuCtx *ctx, char *buf, int64_t cap) {
+    if (!ctx) return EDEN_GPU_E_INVALID;
+    if (!ctx->codegen_used) return 0;
+    const std::string &src = ctx->codegen_source;
+    if (buf && cap > 0) {
+        const size_t k = std::min<size_t>(src.size(), (size_t)(cap - 1));
+        memcpy(buf, src.data(), k);
+        buf[k] = '\0';
+    }
+    return (int64_t)src.size();
+}
 
 extern "C" void edenGpuDestroy(EdenGpuCtx *ctx) {
     if (!ctx) return;
@@ -1144,8 +812,11 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             un_s1[u] = (int)gs_t.size();
         }
     }
-    // channels of each unit's non-flat compartments, in slot order
-    std::vector<int32_t> nf_c0(nf_t.size()), nf_c1(nf_t.size()), nfc_q, nfc_i;
+    // channels of each unit's non-flat compartments, in slot order, and the
+    // channel set of each (the generated code has one routine per set)
+    std::vector<int32_t> nf_c0(nf_t.size()), nf_c1(nf_t.size()), nfc_q, nfc_i, nf_sig(nf_t.size(), -1);
+    std::map<std::vector<int>, int> set_id;
+    std::vector<std::vector<int>> chan_sets;
     std::vector<float> nfc_g, nfc_e;
     for (int u = 0; u < n_unit; u++) {
         const int a = un_t0[u];
@@ -1153,6 +824,16 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int k = un_nf0[u]; k < un_nf1[u]; k++) {
             const int t = a + nf_t[k];
             nf_c0[k] = (int)nfc_g.size();
+            std::vector<int> set;
+            for (int ch = c_chan0[t]; ch < c_chan0[t + 1]; ch++) set.push_back(ch_type[ch]);
+            auto found = set_id.find(set);
+            if (found != set_id.end()) {
+                nf_sig[k] = found->second;
+            } else if (chan_sets.size() < 64) {
+                nf_sig[k] = (int)chan_sets.size();
+                set_id[set] = nf_sig[k];
+                chan_sets.push_back(set);
+            }
             for (int ch = c_chan0[t]; ch < c_chan0[t + 1]; ch++) {
                 const EdenGpuChannelType &ty = m->chan_types[ch_type[ch]];
                 int32_t pack = ty.n_gates;
@@ -1319,7 +1000,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.gr_t, gr_t)); TRY(upload_c(ctx, &d.gr_col, gr_col));
     TRY(upload_c(ctx, &d.un_nf0, un_nf0)); TRY(upload_c(ctx, &d.un_nf1, un_nf1)); TRY(upload_c(ctx, &d.nf_t, nf_t));
     TRY(upload_c(ctx, &d.lvl_info, lvl_info)); TRY(upload_c(ctx, &d.gate_par, gate_par));
-    TRY(upload_c(ctx, &d.nf_c0, nf_c0)); TRY(upload_c(ctx, &d.nf_c1, nf_c1));
+    TRY(upload_c(ctx, &d.nf_c0, nf_c0)); TRY(upload_c(ctx, &d.nf_c1, nf_c1)); TRY(upload_c(ctx, &d.nf_sig, nf_sig));
     TRY(upload_c(ctx, &d.nfc_g, nfc_g)); TRY(upload_c(ctx, &d.nfc_e, nfc_e));
     TRY(upload_c(ctx, &d.nfc_q, nfc_q)); TRY(upload_c(ctx, &d.nfc_i, nfc_i));
     TRY(upload(ctx, &d.status, (const int32_t *)nullptr, 1));
@@ -1352,8 +1033,14 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         st[k].f_decay = 1.0f - dt / s.tau_decay;
         st[k].f_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f - dt / s.tau_rise : 1.0f;
     }
-    CUDA_TRY(ctx, cudaMemcpyToSymbol(c_chan_types, ct, sizeof(ct)));
-    CUDA_TRY(ctx, cudaMemcpyToSymbol(c_syn_types, st, sizeof(st)));
+    {
+        const ChanTypeDev *pc = nullptr;
+        const SynTypeDev *ps = nullptr;
+        TRY(upload(ctx, (ChanTypeDev **)&pc, ct, kMaxChanTypes));
+        TRY(upload(ctx, (SynTypeDev **)&ps, st, kMaxSynTypes));
+        d.chan_types = pc;
+        d.syn_types = ps;
+    }
     ctx->h_syn_types.assign(st, st + kMaxSynTypes);
     // powers of each decay factor for windows without events
     {
@@ -1371,14 +1058,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         int64_t b = (n + kThreads - 1) / kThreads;
         return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)ctx->n_sm * 32));
     };
-    {
-        // resident blocks only: each warp then walks several chunks
-        int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_inputs_t, kInputThreads, 0);
-        ctx->grid_inputs = (int)std::max<int64_t>(
-            1, std::min<int64_t>(((int64_t)n_chunk * 32 + kInputThreads - 1) / kInputThreads,
-                                 (int64_t)ctx->n_sm * std::max(per_sm, 1)));
-    }
+    ctx->grid_inputs = 1;  // set below, once the kernels are chosen
     ctx->grid_targets = blocks_for(nt);
     ctx->grid_hines = (int)std::max<int64_t>(1, ((int64_t)d.n_forest * 32 + kHinesThreads - 1) / kHinesThreads);
     ctx->grid_deliver = ctx->n_sm * 4;
@@ -1397,17 +1077,50 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     // the windowed path needs every class to fit one CTA's shared memory; if
     // not, the batched mode runs the per-step kernels instead
     if (!ctx->smem_window) ctx->K = 1;
+    // the windowed kernels: compiled for this model's channel sets when the
+    // batched mode uses them (codegen >= 0) and NVRTC is available, else the
+    // built-in ones (codegen = 1 makes a failed compile an error)
+    ctx->fn_inputs = (const void *)k_inputs_t;
+    ctx->fn_cells = (const void *)k_cells_t;
+    ctx->fn_deliver = (const void *)k_deliver_t;
+    const int codegen = opt ? opt->codegen : 0;
+    if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window && codegen >= 0) {
+        phase("codegen");
+        ctx->codegen_source = eden_codegen::program_source(eden_codegen::channel_routines(m->chan_types, chan_sets));
+        eden_codegen::Kernels kk;
+        std::string why;
+        if (eden_codegen::compile(ctx->codegen_source, ctx->device, kk, why, ctx->codegen_ms)) {
+            ctx->fn_inputs = kk.inputs;
+            ctx->fn_cells = kk.cells;
+            ctx->fn_deliver = kk.deliver;
+            ctx->codegen_used = true;
+        } else {
+            ctx->codegen_note = why;
+            if (codegen == 1) return ctx->fail(EDEN_GPU_E_CUDA, "code generation failed: %s", why.c_str());
+        }
+    }
     CUDA_TRY(ctx, cudaFuncSetAttribute(k_hines_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_hines));
     if (ctx->smem_window)
-        CUDA_TRY(ctx, cudaFuncSetAttribute(k_cells_t, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CUDA_TRY(ctx, cudaFuncSetAttribute(ctx->fn_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)std::min<size_t>(max_smem_class, (size_t)ctx->smem_optin)));
+    {
+        // resident input blocks only: each warp then walks several chunks
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ctx->fn_inputs, kInputThreads, 0);
+        ctx->grid_inputs = (int)std::max<int64_t>(
+            1, std::min<int64_t>(((int64_t)ctx->d.n_chunk * 32 + kInputThreads - 1) / kInputThreads,
+                                 (int64_t)ctx->n_sm * std::max(per_sm, 1)));
+    }
     phase("done");
     if (verbose) {
         fprintf(stderr, "libeden_gpu: set-up %s\n", timing.c_str());
         int occ_cells = 0, occ_inputs = 0;
         if (ctx->smem_window)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cells, k_cells_t, kCellThreads, max_smem_class);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_inputs, k_inputs_t, kThreads, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cells, ctx->fn_cells, kCellThreads, max_smem_class);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_inputs, ctx->fn_inputs, kInputThreads, 0);
+        fprintf(stderr, "libeden_gpu: kernels %s%s%s (%.0f ms)\n",
+                ctx->codegen_used ? "compiled for this model" : "built in",
+                ctx->codegen_note.empty() ? "" : ": ", ctx->codegen_note.c_str(), ctx->codegen_ms);
         int64_t fnodes = 0, flev = 0;
         for (size_t f = 0; f < fo_t0.size(); f++) { fnodes += fo_t1[f] - fo_t0[f]; flev += fo_nlev[f]; }
         fprintf(stderr,
@@ -1534,24 +1247,27 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     cudaStream_t s = ctx->stream;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
         tmark(ctx, EDEN_KERNEL_INPUTS, true);
-        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, ctx->d_wtimes, base, idx);
+        launch_k(ctx->fn_inputs, ctx->grid_inputs, kInputThreads, 0, s, d, (const WindowArgs *)ctx->d_wtab,
+                 (const WindowTimes *)ctx->d_wtimes, base, idx);
         tmark(ctx, EDEN_KERNEL_INPUTS, false);
         int n = 1;
         tmark(ctx, EDEN_KERNEL_CELLS, true);
         for (const auto &cl : ctx->classes) {
             const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
-            k_cells_t<<<nb, kCellThreads, cl.smem, s>>>(d, ctx->d_wtab, base, idx, cl.cta_begin, cl.cta_end);
+            launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, d, (const WindowArgs *)ctx->d_wtab, base, idx,
+                     cl.cta_begin, cl.cta_end);
             n++;
         }
         tmark(ctx, EDEN_KERNEL_CELLS, false);
         tmark(ctx, EDEN_KERNEL_DELIVER, true);
-        k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+        launch_k(ctx->fn_deliver, ctx->grid_deliver, kThreads, 0, s, d, (const WindowArgs *)ctx->d_wtab, base, idx);
         tmark(ctx, EDEN_KERNEL_DELIVER, false);
         return n + 1;
     }
     (void)K;
     tmark(ctx, EDEN_KERNEL_INPUTS, true);
-    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(d, ctx->d_wtab, ctx->d_wtimes, base, idx);
+    launch_k(ctx->fn_inputs, ctx->grid_inputs, kInputThreads, 0, s, d, (const WindowArgs *)ctx->d_wtab,
+             (const WindowTimes *)ctx->d_wtimes, base, idx);
     tmark(ctx, EDEN_KERNEL_INPUTS, false);
     tmark(ctx, EDEN_KERNEL_TARGETS, true);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
@@ -1560,7 +1276,7 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(d, ctx->d_wtab, base, idx, ctx->forest_cap);
     tmark(ctx, EDEN_KERNEL_HINES, false);
     tmark(ctx, EDEN_KERNEL_DELIVER, true);
-    k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+    launch_k(ctx->fn_deliver, ctx->grid_deliver, kThreads, 0, s, d, (const WindowArgs *)ctx->d_wtab, base, idx);
     tmark(ctx, EDEN_KERNEL_DELIVER, false);
     return 4;
 }
@@ -1829,20 +1545,20 @@ static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const Windo
     cudaStream_t s = ctx->stream;
     const int *zero = ctx->d_zero;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
-        k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, times, zero, idx);
+        launch_k(ctx->fn_inputs, ctx->grid_inputs, kInputThreads, 0, s, dm, tab, times, zero, idx);
         int n = 1;
         for (const auto &cl : ctx->classes) {
             const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
-            k_cells_t<<<nb, kCellThreads, cl.smem, s>>>(dm, tab, zero, idx, cl.cta_begin, cl.cta_end);
+            launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, dm, tab, zero, idx, cl.cta_begin, cl.cta_end);
             n++;
         }
-        k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);
+        launch_k(ctx->fn_deliver, ctx->grid_deliver, kThreads, 0, s, dm, tab, zero, idx);
         return n + 1;
     }
-    k_inputs_t<<<ctx->grid_inputs, kInputThreads, 0, s>>>(dm, tab, times, zero, idx);
+    launch_k(ctx->fn_inputs, ctx->grid_inputs, kInputThreads, 0, s, dm, tab, times, zero, idx);
     k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(dm, tab, zero, idx);
     k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(dm, tab, zero, idx, ctx->forest_cap);
-    k_deliver_t<<<ctx->grid_deliver, kThreads, 0, s>>>(dm, tab, zero, idx);
+    launch_k(ctx->fn_deliver, ctx->grid_deliver, kThreads, 0, s, dm, tab, zero, idx);
     return 4;
 }
 

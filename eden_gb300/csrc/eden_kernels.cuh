@@ -20,7 +20,9 @@
 //   inputs    connection synapses, Poisson inputs and pulses sorted by target;
 //             targets with any input are listed in `in_tgt` (one warp each).
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cstdint>
+#endif
 
 #include "eden_math.cuh"
 
@@ -61,8 +63,6 @@ __device__ __forceinline__ float div_by_tau(float x, float tau, float r) {
     return tiny ? qs * 0x1p-64f : qs;
 }
 
-__constant__ ChanTypeDev c_chan_types[kMaxChanTypes];
-__constant__ SynTypeDev c_syn_types[kMaxSynTypes];
 
 enum : int { ST_OK = 0, ST_LOG_OVERFLOW = 1 };
 enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2 };
@@ -72,6 +72,10 @@ constexpr int kPowLen = 33;      // powers 0..32 of a synapse decay factor
 
 struct DevModel {
     int32_t n_target, n_src, n_group, n_forest, n_in;
+    // channel and synapse type tables (per context, so that contexts of
+    // different models can run side by side)
+    const ChanTypeDev *chan_types;
+    const SynTypeDev *syn_types;
     int64_t n_syn, n_pois;
     float dt;
     // targets
@@ -173,6 +177,7 @@ struct DevModel {
     // [nf_c0, nf_c1): conductivity, reversal potential, first gate (index in
     // the unit's gates) and gate count | instances << (3 + 5 * gate)
     const int32_t *nf_c0, *nf_c1;
+    const int32_t *nf_sig;            // channel set of each non-flat compartment (generated code), -1: none
     const float *nfc_g, *nfc_e;
     const int32_t *nfc_q, *nfc_i;
     // per channel type and gate, the 9-word gate parameter record (gate_next_p)
@@ -188,9 +193,9 @@ constexpr int kGateWords = 9;  // gate parameter record (gate_next_p)
 
 // Shared-memory words of a unit's slice in the windowed kernel.  A forest:
 // 7 per compartment (V, c_kc, L, pivot, elimination factor, U, packed
-// child range/parent/flag), 9 per non-flat compartment (local index, V at
+// child range/parent/flag), 10 per non-flat compartment (local index, V at
 // the step start, area, C, sum of 1/(R C), input-block range, channel
-// range), 4 per channel of a non-flat compartment, 11 per gate (value,
+// range, channel set), 4 per channel of a non-flat compartment, 11 per gate (value,
 // non-flat slot, parameter record), the depth boundaries, 3 per spike
 // source, 3 per input block (kind, reversal potential, chunk start) plus
 // one, and the window's conductance series of the unit's input chunks
@@ -198,7 +203,7 @@ constexpr int kGateWords = 9;  // gate parameter record (gate_next_p)
 // twice and 11 parameter / state words per neuron.
 __host__ __device__ inline int forest_words(int n, int nf, int nfch, int ngt, int nlev, int ns, int nblk, int nck,
                                             int kcap) {
-    return 7 * n + 9 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck;
+    return 7 * n + 10 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck;
 }
 __host__ __device__ inline int izh_words(int n) { return 13 * n + 1; }
 
@@ -480,7 +485,7 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
         return;
     }
     const int type = (info >> 2) & 63;
-    const SynTypeDev st = c_syn_types[type];
+    const SynTypeDev st = m.syn_types[type];
     const bool two = st.kind == EDEN_SYN_EXPTWO;
     bool used = false;
     // the chunk's aggregate and its items' per-window state, loaded up front
@@ -513,7 +518,6 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     }
     const unsigned rows = __ballot_sync(0xffffffffu, used);
     __syncwarp();
-    const float dt = m.dt;
     float gj = 0.0f;
     if (rows == 0) {
         // no event in the window: the aggregate decays in closed form,
@@ -638,7 +642,7 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
         float A = m.c_area[t];
         float Ich = 0.0f, Gch = 0.0f;
         for (int ch = m.c_chan0[t]; ch < m.c_chan0[t + 1]; ch++) {
-            const ChanTypeDev &ct = c_chan_types[m.ch_type[ch]];
+            const ChanTypeDev &ct = m.chan_types[m.ch_type[ch]];
             float fopen = 1.0f;
             float *q = m.gate + m.ch_gate0[ch];
             for (int g = 0; g < ct.n_gates; g++) {

@@ -3,7 +3,9 @@
 // reference's generated C so single-precision results stay within rounding
 // of it (the reference compiles with -Ofast, so bit equality is not defined).
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cstdint>
+#endif
 
 #include "../../include/eden_gpu.h"
 

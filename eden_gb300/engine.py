@@ -35,7 +35,7 @@ class COptions(ctypes.Structure):
                 ("steps_per_launch", ctypes.c_int32), ("cells_per_block", ctypes.c_int32),
                 ("record_capacity_steps", ctypes.c_int32), ("spike_capacity", ctypes.c_int32),
                 ("n_trace", ctypes.c_int32), ("trace_target", ctypes.POINTER(ctypes.c_int32)),
-                ("kernel_timing", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("kernel_timing", ctypes.c_int32), ("codegen", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
 
 
 class CRecords(ctypes.Structure):
@@ -45,7 +45,7 @@ class CRecords(ctypes.Structure):
                 ("n_trace_samples", ctypes.c_int64), ("n_spikes", ctypes.c_int64)]
 
 
-EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuRunStaticScratch", "edenGpuFetchRecords", "edenGpuReadV", "edenGpuWriteV",
+EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuRunStaticScratch", "edenGpuFetchRecords", "edenGpuGeneratedSource", "edenGpuReadV", "edenGpuWriteV",
             "edenGpuReadSynapses", "edenGpuLastRunStats", "edenGpuKernelStats", "edenGpuLastError",
             "edenGpuDestroy", "edenGpuAbiVersion"]
 KERNEL_NAMES = ["k_inputs_t", "k_cells_t", "k_targets_t", "k_hines_t", "k_deliver_t"]
@@ -80,6 +80,8 @@ def load_library(path: str | None = None, build_if_missing: bool = True):
     lib.edenGpuKernelStats.argtypes = [P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_int64)]
     lib.edenGpuKernelStats.restype = ctypes.c_int
+    lib.edenGpuGeneratedSource.argtypes = [P, ctypes.c_char_p, ctypes.c_int64]
+    lib.edenGpuGeneratedSource.restype = ctypes.c_int64
     lib.edenGpuLastError.argtypes = [P]
     lib.edenGpuLastError.restype = ctypes.c_char_p
     lib.edenGpuDestroy.argtypes = [P]
@@ -113,7 +115,7 @@ class Simulation:
     def __init__(self, lowered: LoweredModel, mode: int = MODE_BATCHED, device: int = 0,
                  steps_per_launch: int = 0, cells_per_block: int = 0, trace_target=None,
                  record_capacity_steps: int = 4096, spike_capacity: int = 1 << 22,
-                 kernel_timing: bool = False):
+                 kernel_timing: bool = False, codegen: int = 0):
         self.lib = load_library()
         self.lowered = lowered
         self._cm, self._keep = to_cmodel(lowered)
@@ -127,6 +129,7 @@ class Simulation:
         opt.record_capacity_steps = record_capacity_steps
         opt.spike_capacity = spike_capacity
         opt.kernel_timing = 1 if kernel_timing else 0
+        opt.codegen = codegen
         opt.n_trace = len(self.trace_target)
         opt.trace_target = self.trace_target.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if len(self.trace_target) else None
         self._opt = opt
@@ -235,6 +238,18 @@ class Simulation:
             self._check(self.lib.edenGpuKernelStats(self.ctx, k, ctypes.byref(ms), ctypes.byref(n)))
             out[name] = (float(ms.value), int(n.value))
         return out
+
+    def generated_source(self) -> str:
+        """The CUDA source compiled for this model ('' when the built-in
+        kernels run)."""
+        n = self.lib.edenGpuGeneratedSource(self.ctx, None, 0)
+        if n < 0:
+            raise EdenGpuError(int(n), self._err())
+        if n == 0:
+            return ""
+        buf = ctypes.create_string_buffer(int(n) + 1)
+        self.lib.edenGpuGeneratedSource(self.ctx, buf, n + 1)
+        return buf.value.decode()
 
     # -- state access ----------------------------------------------------------
     def read_v(self) -> np.ndarray:

@@ -20,8 +20,10 @@
 #ifndef EDEN_GPU_H
 #define EDEN_GPU_H
 
+#ifndef __CUDACC_RTC__
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -158,7 +160,10 @@ typedef struct EdenGpuOptions {
     const int32_t *trace_target;
     int32_t kernel_timing;    /* 1: bracket every kernel launch with CUDA events (no graph
                                  replay) and accumulate per-kernel device time */
-    int32_t reserved[7];
+    int32_t codegen;          /* batched mode: 0 = compile the windowed kernels for the
+                                 model's channel sets with NVRTC when available (else use
+                                 the built-in ones), 1 = require it, -1 = built-in kernels */
+    int32_t reserved[6];
 } EdenGpuOptions;
 
 /* Kernels whose device time kernel_timing accumulates. */
@@ -186,6 +191,10 @@ typedef struct EdenGpuRecords {
 } EdenGpuRecords;
 
 typedef struct EdenGpuCtx EdenGpuCtx;
+
+/* (the entry points are host functions; the types above are also compiled
+ * into the library's run-time generated kernels, which see no declarations) */
+#ifndef __CUDACC_RTC__
 
 /* Build a context: validate the model, upload it to device memory in the
  * GPU layout, build the spike fan-out table.  Replaces the reference's
@@ -238,9 +247,18 @@ int edenGpuLastRunStats(EdenGpuCtx *ctx, double *device_ms, int64_t *launches);
  * eden/Eden.cpp:11951; this is the GPU-side breakdown of Run). */
 int edenGpuKernelStats(EdenGpuCtx *ctx, int32_t kind, double *total_ms, int64_t *launches);
 
+/* The CUDA source compiled at creation for this model's windowed kernels
+ * (batched mode with codegen >= 0: the library's kernels plus one routine
+ * per channel set, the counterpart of the C the reference generates per cell
+ * type, eden/Eden.cpp:7017-7180).  Copies at most cap - 1 bytes and a NUL
+ * into buf when buf is not null; returns the source length, 0 when the
+ * built-in kernels run, or a negative error code. */
+int64_t edenGpuGeneratedSource(EdenGpuCtx *ctx, char *buf, int64_t cap);
+
 const char *edenGpuLastError(EdenGpuCtx *ctx);
 void edenGpuDestroy(EdenGpuCtx *ctx);
 int edenGpuAbiVersion(void);
+#endif /* __CUDACC_RTC__ */
 
 #ifdef __cplusplus
 }
