@@ -29,7 +29,8 @@ using namespace eden;
 
 namespace {
 
-constexpr int kForestNodes = 512;   // largest forest (a larger cell gets a forest of its own)
+constexpr int kForestNodes = 768;   // largest forest (a larger cell gets a forest of its own)
+constexpr int kForestWidth = 64;    // most compartments of a forest at one depth (two per lane)
 constexpr int kGraphWindows = 16;  // windows per captured graph
 
 struct Window {
@@ -375,7 +376,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     phase("units");
     // ---- units: each warp of the windowed kernel owns one unit for the whole
     // window -- a forest of physical cells (joint breadth-first numbering,
-    // at most 32 nodes per depth level, at most kForestNodes nodes) or a batch
+    // at most kForestWidth nodes per depth level, at most kForestNodes nodes) or a batch
     // of up to 32 izhikevich neurons.  Targets are numbered unit by unit.
     const int forest_node_cap = kForestNodes;
     std::vector<int32_t> u2i(nt, -1), i2u(nt, -1);
@@ -401,7 +402,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
                 const std::vector<int> &cw = cell_width[c];
                 bool fits = fc.empty() || nodes + cell_n[c] <= forest_node_cap;
                 for (size_t d = 0; fits && d < cw.size(); d++)
-                    if ((d < fw.size() ? fw[d] : 0) + cw[d] > 32) fits = false;
+                    if ((d < fw.size() ? fw[d] : 0) + cw[d] > kForestWidth) fits = false;
                 if (!fits && !fc.empty()) break;
                 if (fw.size() < cw.size()) fw.resize(cw.size(), 0);
                 for (size_t d = 0; d < cw.size(); d++) fw[d] += cw[d];
@@ -921,7 +922,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     }
     size_t max_smem_class = 0;
     for (auto &cl : ctx->classes) max_smem_class = std::max(max_smem_class, cl.smem);
-    ctx->smem_window = max_smem_class <= (size_t)ctx->smem_optin;
+    // (the windowed kernel packs forest-local indices in 10 bits: a single
+    // cell of more than 1023 compartments runs the per-step kernels)
+    ctx->smem_window = max_smem_class <= (size_t)ctx->smem_optin && max_forest <= 1023;
 
     phase("upload");
     // ---- upload

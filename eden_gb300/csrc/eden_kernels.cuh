@@ -761,8 +761,8 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
 // compartment's pivot is rebuilt every step from its diagonal (PV holds
 // G/C + sum 1/(RC) on entry, X its pre-updated V) and its children's
 // factors, in increasing child order as the reference's post-order visits
-// them.  A depth's compartments are spread over the lanes (at most 32 per
-// depth unless a single cell is wider); LV packs each depth's first
+// them.  A depth's compartments are spread over the lanes (at most 64 per
+// depth, two per lane, unless a single cell is wider); LV packs each depth's first
 // compartment and whether it holds a non-flat one.
 // Back-substitution runs root-first.  X holds V_next on return.
 constexpr int32_t kLvMask = 0xffff;
@@ -774,7 +774,7 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
     int end = LV[nlev] & kLvMask;
     for (int lev = nlev - 1; lev >= 0; lev--) {
         const int32_t lw = LV[lev];
-        // a depth holds at most 32 compartments unless one cell alone is wider
+        // a depth holds at most 64 compartments unless one cell alone is wider
         for (int j = (lw & kLvMask) + lane; j < end; j += 32) {
             const uint32_t cep = CEP[j];
             const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
