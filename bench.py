@@ -6,8 +6,9 @@ dendrites, 1 M expTwoSynapse connections at fixed in-degree 100 with
 0.5-5 ms delays, 1 M 5 Hz poissonFiringSynapse inputs; dt 0.025 ms.  A bench
 "step" is one pass of the simulation loop over STEPS_PER_ITER simulation
 steps; `value` is compartment-steps/s (compartments x simulation steps /
-device time) with the network resident in HBM; `e2e` runs the whole thing
-through the C ABI from host buffers (model upload, stepping, record fetch).
+device time) with the network resident in HBM; `e2e` runs the whole
+configured simulation (1 s, 40,001 steps) through the C ABI from host buffers
+(model upload and device layout, stepping, record fetches) on the wall clock.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -300,22 +301,27 @@ def main():
     psim.close()
     plain_value = low.n_target * 2 * STEPS_PER_ITER / (plain_ms * 1e-3)
 
-    # ---- end to end through the C ABI: model upload, stepping, record fetch
+    # ---- end to end through the C ABI, the whole configured run (1 s of
+    # simulated time): model upload and layout, stepping, record fetches
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    e2e_steps = int(low.n_steps)
     t0 = time.perf_counter()
-    esim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=STEPS_PER_ITER * 2)
+    esim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=4096)
     rec_bytes = 0
     esim.initialize()
-    for _ in range(args.steps):
-        esim.run_steps(STEPS_PER_ITER)
+    done = 0
+    while done < e2e_steps:
+        k = min(4096, e2e_steps - done)
+        esim.run_steps(k)
         r = esim.fetch()
         rec_bytes += r.trace.nbytes + r.trace_step.nbytes + r.spike_src.nbytes + r.spike_step.nbytes
+        done += k
     esim.close()
     e2e_s = time.perf_counter() - t0
     model_bytes = sum(a.nbytes for a in esim._keep)
-    e2e_value = world * low.n_target * sim_steps / e2e_s
+    e2e_value = world * low.n_target * e2e_steps / e2e_s
 
     # ---- CPU baseline (rank 0 only)
     cpu = None
@@ -335,8 +341,11 @@ def main():
                 "config": config,
                 "plain_gpu": {"value": plain_value, "unit": UNIT, "ratio_batched_over_plain": value / world / plain_value},
                 "e2e": {"value": e2e_value, "unit": UNIT,
-                        "h2d_bytes_per_step": model_bytes / (sim_steps + 4) / 1.0,
-                        "d2h_bytes_per_step": rec_bytes / sim_steps},
+                        "h2d_bytes_per_step": model_bytes / (e2e_steps + 4),
+                        "d2h_bytes_per_step": rec_bytes / e2e_steps, "steps": e2e_steps,
+                        "seconds": e2e_s,
+                        "covers": "create (upload, device layout, kernels compiled for the model or "
+                                  "taken from the process cache), the whole configured run, record fetches"},
                 "gpu_launches": int(gpu_launches),
                 "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
