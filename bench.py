@@ -195,17 +195,33 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def replica_seed(base: int, rank: int) -> int:
+    """Each rank simulates its own replica of the network."""
+    return base + rank
+
+
+def max_over_ranks(x: float, dist) -> float:
+    """The slowest rank's figure (timings are taken as the max over ranks)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
     from eden_gb300 import lowering, workloads
 
-    spec = workloads.multicomp_net(n_cells=args.cells, seed=args.seed + rank)
+    spec = workloads.multicomp_net(n_cells=args.cells, seed=replica_seed(args.seed, rank))
     low = lowering.lower(spec)
     config = {"workload": f"multicomp_net: {args.cells} cells, {low.n_comp} compartments, "
                           f"{len(low.syn_target)} expTwo synapses (in-degree 100, delay 0.5-5 ms), "
@@ -233,9 +249,9 @@ def main():
 
     import torch
     from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
-    torch.cuda.set_device(0)
+    torch.cuda.set_device(dev)
     if args.profile:
-        sim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=STEPS_PER_ITER * 2)
+        sim = Simulation(low, mode=MODE_BATCHED, device=dev, record_capacity_steps=STEPS_PER_ITER * 2)
         sim.initialize()
         for _ in range(args.warmup + args.steps):
             sim.run_steps(STEPS_PER_ITER)
@@ -246,7 +262,7 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     # ---- device-timed batched run (kernel timing on: CUDA events around each launch)
-    sim = Simulation(low, mode=MODE_BATCHED, kernel_timing=True, record_capacity_steps=STEPS_PER_ITER * 2)
+    sim = Simulation(low, mode=MODE_BATCHED, device=dev, kernel_timing=True, record_capacity_steps=STEPS_PER_ITER * 2)
     sim.initialize()
     for _ in range(max(3, args.warmup)):
         sim.run_steps(STEPS_PER_ITER)
@@ -269,10 +285,7 @@ def main():
     stats = sim.kernel_stats()
     sim.close()
     gpu_launches = sum(n for _, n in stats.values()) - launches0
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist)
     sim_steps = STEPS_PER_ITER * args.steps
     value = world * low.n_target * sim_steps / (total_ms * 1e-3)
 
@@ -289,7 +302,7 @@ def main():
     peak, peak_kind = peaks()
 
     # ---- plain (per-step) GPU path on the same network, for the batched/plain ratio
-    psim = Simulation(low, mode=MODE_PLAIN, record_capacity_steps=STEPS_PER_ITER * 2)
+    psim = Simulation(low, mode=MODE_PLAIN, device=dev, record_capacity_steps=STEPS_PER_ITER * 2)
     psim.initialize()
     psim.run_steps(STEPS_PER_ITER)
     psim.fetch()
@@ -299,6 +312,7 @@ def main():
         plain_ms += psim.run_steps(STEPS_PER_ITER)
         psim.fetch()
     psim.close()
+    plain_ms = max_over_ranks(plain_ms, dist)
     plain_value = low.n_target * 2 * STEPS_PER_ITER / (plain_ms * 1e-3)
 
     # ---- end to end through the C ABI, the whole configured run (1 s of
@@ -308,7 +322,7 @@ def main():
     torch.cuda.synchronize()
     e2e_steps = int(low.n_steps)
     t0 = time.perf_counter()
-    esim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=4096)
+    esim = Simulation(low, mode=MODE_BATCHED, device=dev, record_capacity_steps=4096)
     rec_bytes = 0
     esim.initialize()
     done = 0
@@ -319,7 +333,7 @@ def main():
         rec_bytes += r.trace.nbytes + r.trace_step.nbytes + r.spike_src.nbytes + r.spike_step.nbytes
         done += k
     esim.close()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     model_bytes = sum(a.nbytes for a in esim._keep)
     e2e_value = world * low.n_target * e2e_steps / e2e_s
 
