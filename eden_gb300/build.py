@@ -12,14 +12,17 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libeden_gpu.so")
 HEADER = os.path.join(ROOT, "include", "eden_gpu.h")
-SOURCES = [os.path.join(HERE, "csrc", f) for f in ("eden_gpu.cu", "eden_codegen.cuh", "eden_window.cuh",
+SOURCES = [os.path.join(HERE, "csrc", f) for f in ("eden_gpu.cu", "eden_grad.cu", "eden_codegen.cuh", "eden_window.cuh",
                                                    "eden_kernels.cuh", "eden_math.cuh")]
+# translation units, compiled in parallel and linked into one library
+UNITS = ["eden_gpu.cu", "eden_grad.cu"]
 # the kernel sources the library compiles again at run time (NVRTC), in
 # dependency order; build() embeds them as csrc/_rtc_src.inc
 RTC_SOURCES = [HEADER] + [os.path.join(HERE, "csrc", f) for f in ("eden_math.cuh", "eden_kernels.cuh",
                                                                  "eden_window.cuh")]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared", "-ldl"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+LINK_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-ldl"]
 
 
 def nvcc() -> str:
@@ -66,7 +69,18 @@ def embed_rtc_sources() -> str:
 def build(force: bool = False, verbose: bool = False) -> str:
     if force or needs_build():
         embed_rtc_sources()
-        cmd = [nvcc(), *NVCC_FLAGS, os.path.join(HERE, "csrc", "eden_gpu.cu"), "-o", LIB + ".tmp"]
+        objs, procs = [], []
+        for unit in UNITS:
+            obj = os.path.join(HERE, "csrc", "_" + unit.replace(".cu", ".o"))
+            cmd = [nvcc(), *NVCC_FLAGS, "-c", os.path.join(HERE, "csrc", unit), "-o", obj]
+            if verbose:
+                print(" ".join(cmd), file=sys.stderr)
+            procs.append((cmd, subprocess.Popen(cmd)))
+            objs.append(obj)
+        for cmd, p in procs:
+            if p.wait() != 0:
+                raise subprocess.CalledProcessError(p.returncode, cmd)
+        cmd = [nvcc(), *LINK_FLAGS, *objs, "-o", LIB + ".tmp"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         subprocess.check_call(cmd)

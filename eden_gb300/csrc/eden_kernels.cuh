@@ -593,20 +593,6 @@ __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1,
     }
 }
 
-// One HH gate for one step (eden/Eden.cpp:5126-5259): exponential-Euler
-// relaxation towards inf(V) with time constant tau(V), clamped to
-// [1e-6, 1 - 1e-6]; initialisation sets it to inf(V).
-__device__ __forceinline__ float gate_relax(float alpha, float beta, float q10, bool init, float dt, float qo) {
-    const float tau = 1.0f / (alpha + beta);
-    const float inf = alpha / (alpha + beta);
-    if (init) return inf;
-    const float blend = expf(-((dt * q10) / tau));
-    float qn = blend * qo + (1.0f - blend) * inf;
-    if (!(qn > 1e-6f)) qn = 1e-6f;
-    if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
-    return qn;
-}
-
 __device__ __forceinline__ float gate_next(const ChanTypeDev &ct, int gi, bool init, float dt, float v, float qo) {
     const float alpha = rate_value(ct.fk[gi], ct.fr[gi], ct.fm[gi], ct.fs[gi], v);
     const float beta = rate_value(ct.rk[gi], ct.rr[gi], ct.rm[gi], ct.rs[gi], v);

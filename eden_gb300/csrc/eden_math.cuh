@@ -50,6 +50,20 @@ __device__ __forceinline__ float rate_value(int kind, float r, float mid, float 
     return r * ((v == mid) ? 1.0f : q);
 }
 
+// One HH gate for one step (eden/Eden.cpp:5126-5259): exponential-Euler
+// relaxation towards inf(V) with time constant tau(V), clamped to
+// [1e-6, 1 - 1e-6]; initialisation sets it to inf(V).
+__device__ __forceinline__ float gate_relax(float alpha, float beta, float q10, bool init, float dt, float qo) {
+    const float tau = 1.0f / (alpha + beta);
+    const float inf = alpha / (alpha + beta);
+    if (init) return inf;
+    const float blend = expf(-((dt * q10) / tau));
+    float qn = blend * qo + (1.0f - blend) * inf;
+    if (!(qn > 1e-6f)) qn = 1e-6f;
+    if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
+    return qn;
+}
+
 // Channel type table in constant memory (a handful of ionChannelHH types).
 constexpr int kMaxChanTypes = 32;
 constexpr int kMaxSynTypes = 32;

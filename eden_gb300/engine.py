@@ -47,7 +47,8 @@ class CRecords(ctypes.Structure):
 
 EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuRunStaticScratch", "edenGpuFetchRecords", "edenGpuGeneratedSource", "edenGpuReadV", "edenGpuWriteV",
             "edenGpuReadSynapses", "edenGpuLastRunStats", "edenGpuKernelStats", "edenGpuLastError",
-            "edenGpuDestroy", "edenGpuAbiVersion"]
+            "edenGpuDestroy", "edenGpuAbiVersion", "edenGpuGradCreate", "edenGpuGradForward",
+            "edenGpuGradBackward", "edenGpuGradTiming", "edenGpuGradLastError", "edenGpuGradDestroy"]
 KERNEL_NAMES = ["k_inputs_t", "k_cells_t", "k_targets_t", "k_hines_t", "k_deliver_t"]
 
 

@@ -119,6 +119,8 @@ class LoweredModel:
     event_src: np.ndarray         # spike source recorded by each EventSelection
     # bookkeeping
     gid_target_base: np.ndarray = field(default=None)  # first target of each gid
+    chan_density: np.ndarray = field(default=None)     # channel -> index of its channelDensity in the cell type
+    phys_ra: np.ndarray = field(default=None)          # physical cell -> axial resistivity, ohm*cm
 
     @property
     def n_comp(self) -> int:
@@ -211,6 +213,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     comp_parent, comp_c, comp_r, comp_area, comp_inv, comp_v0 = [], [], [], [], [], []
     chan_off = [0]
     chan_type, chan_g, chan_e = [], [], []
+    chan_dens, phys_ra = [], []
     izh = []
     src_target = np.zeros(n_cells, np.int32)
     src_thr = np.full(n_cells, np.nan, np.float32)
@@ -235,13 +238,15 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                 comp_inv.append(inv)
                 comp_v0.append(np.full(ct.n_seg, _to_f32(ct.v0), np.float32))
                 for s in range(ct.n_seg):
-                    for dens in ct.densities:
+                    for kd, dens in enumerate(ct.densities):
                         if dens.seg_mask[s]:
+                            chan_dens.append(kd)
                             chan_type.append(dens.channel)
                             chan_g.append(dens.cond)
                             chan_e.append(dens.erev)
                     chan_off.append(len(chan_type))
                 phys_off.append(base + ct.n_seg)
+                phys_ra.append(float(ct.ra))
                 src_target[gid] = base  # segment 0 detects spikes
                 src_thr[gid] = _to_f32(ct.spike_thresh)
             elif isinstance(ct, Izhikevich2007Cell):
@@ -362,6 +367,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         pulse_target=qt, pulse_start=qs, pulse_duration=qd, pulse_amplitude=qa,
         pulse_weight=np.ones(len(qt), F32),
         trace_target=trace_target, event_src=event_src, gid_target_base=gid_base,
+        chan_density=np.asarray(chan_dens, np.int32), phys_ra=np.asarray(phys_ra, np.float64),
     )
 
 

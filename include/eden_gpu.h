@@ -258,6 +258,63 @@ int64_t edenGpuGeneratedSource(EdenGpuCtx *ctx, char *buf, int64_t cap);
 const char *edenGpuLastError(EdenGpuCtx *ctx);
 void edenGpuDestroy(EdenGpuCtx *ctx);
 int edenGpuAbiVersion(void);
+
+/*
+ * Gradients (no counterpart in the reference, which has no gradient path).
+ *
+ * For models of independent physical cells -- HH channels
+ * (ionChannelHH/gateHHrates) and pulse inputs; no synapses, Poisson inputs
+ * or point neurons -- the library runs the same step as edenGpuRun's plain
+ * path (gates eden/Eden.cpp:5126-5259, channel currents 5805-5898, V
+ * pre-update 6057-6107, Hines solve 6114-6225) with chosen channel
+ * conductivities and cell axial resistivities taken from a parameter vector,
+ * records the membrane potential of chosen compartments at the start of
+ * steps 1..n_steps, and returns the gradient of any scalar function of that
+ * trace with respect to the parameters, given the function's gradient with
+ * respect to the trace: the discrete adjoint of the step, run backward in
+ * time over segments recomputed from forward states stored every
+ * `checkpoint_every` steps.
+ *
+ * Pointers to parameters, traces and gradients may be host or device
+ * memory.  Calls are synchronous.
+ */
+typedef struct EdenGpuGradSpec {
+    int32_t n_params;
+    const int32_t *chan_param;     /* [n_chan] parameter that is the channel's conductivity
+                                      (mS/cm2), or -1 to keep chan_gbase; may be null */
+    const int32_t *cell_ra_param;  /* [n_phys] parameter that is the cell's axial resistivity
+                                      (ohm cm), or -1; may be null */
+    const float *cell_ra;          /* [n_phys] the resistivity (ohm cm) that comp_r_axial and
+                                      comp_inv_rc were computed with; needed with cell_ra_param */
+    int32_t n_rec;
+    const int32_t *rec_comp;       /* [n_rec] compartments recorded as trace columns */
+    int64_t n_steps;               /* trace rows: steps 1..n_steps */
+    int32_t checkpoint_every;      /* steps per recomputed segment; 0 = 100 */
+    int32_t device;
+    int32_t reserved[4];
+} EdenGpuGradSpec;
+
+typedef struct EdenGpuGrad EdenGpuGrad;
+
+/* Validate and upload; *out is set even on failure (read the message with
+ * edenGpuGradLastError, then destroy it). */
+int edenGpuGradCreate(const EdenGpuModel *model, const EdenGpuGradSpec *spec, EdenGpuGrad **out);
+
+/* Run the initialisation passes and steps 1..n_steps with `params`
+ * ([n_params]); write the trace ([n_steps * n_rec], step-major) and keep the
+ * checkpoints for the next edenGpuGradBackward. */
+int edenGpuGradForward(EdenGpuGrad *g, const float *params, float *trace);
+
+/* Gradient ([n_params]) of a scalar function of the last forward's trace,
+ * given that function's gradient with respect to the trace
+ * ([n_steps * n_rec]).  Parameters that no channel or cell uses get 0. */
+int edenGpuGradBackward(EdenGpuGrad *g, const float *trace_grad, float *param_grad);
+
+/* Device time in milliseconds of the last forward and backward calls. */
+int edenGpuGradTiming(EdenGpuGrad *g, double *forward_ms, double *backward_ms);
+
+const char *edenGpuGradLastError(EdenGpuGrad *g);
+void edenGpuGradDestroy(EdenGpuGrad *g);
 #endif /* __CUDACC_RTC__ */
 
 #ifdef __cplusplus

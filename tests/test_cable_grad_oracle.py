@@ -1,0 +1,96 @@
+"""The double-precision cable oracle that checks the GPU adjoint: its
+forward run against the double-precision C restatement of the reference
+(libeden_port64), and its forward-mode sensitivities against central
+finite differences of its own forward run.  CPU only."""
+import numpy as np
+import pytest
+
+from eden_gb300 import lowering, workloads
+from eden_gb300.gradient import per_cell_density_map
+from oracle.cable_grad import Cable, loss_and_trace_grad
+from oracle.port import eden_port
+
+# the seven per-instance parameters of the ball-and-stick workload: soma gNa,
+# gK, gL, dendrite gNa, gK, gL (their channelDensity indices), then Ra
+BS_DENSITIES = [1, 2, 0, 4, 5, 3]
+K = 7
+
+
+def small_ball_and_stick(n_inst=3, n_dend=8, length_ms=20.0, amp_na=0.5):
+    spec = workloads.ball_and_stick(n_inst=n_inst, n_dend=n_dend, length_ms=length_ms, amp_na=amp_na)
+    low = lowering.lower(spec)
+    return spec, low, per_cell_density_map(low, BS_DENSITIES)
+
+
+def per_cell_directions(n_params):
+    d = np.zeros((K, n_params))
+    for j in range(K):
+        d[j, j::K] = 1.0
+    return d
+
+
+def fd_grad(cab, low, pm, rec, target, h):
+    """Per-cell central differences of the MSE with relative step h."""
+    g = np.zeros((len(rec), K))
+    n = target.size
+    for j in range(K):
+        up = pm.values.astype(np.float64).copy()
+        dn = up.copy()
+        up[j::K] *= 1 + h
+        dn[j::K] *= 1 - h
+        tu, _ = cab.run(up, low.n_steps, rec)
+        td, _ = cab.run(dn, low.n_steps, rec)
+        g[:, j] = (((tu - target) ** 2).sum(0) - ((td - target) ** 2).sum(0)) / n / (2 * h * pm.values[j::K])
+    return g
+
+
+def fd_grad_linear(cab, low, pm, rec, w, h):
+    """Per-cell central differences of sum(w * trace) with relative step h."""
+    g = np.zeros((len(rec), K))
+    for j in range(K):
+        up = pm.values.astype(np.float64).copy()
+        dn = up.copy()
+        up[j::K] *= 1 + h
+        dn[j::K] *= 1 - h
+        tu, _ = cab.run(up, low.n_steps, rec)
+        td, _ = cab.run(dn, low.n_steps, rec)
+        g[:, j] = ((tu - td) * w).sum(0) / (2 * h * pm.values[j::K])
+    return g
+
+
+def test_param_map_reproduces_the_workload_parameters():
+    spec, low, pm = small_ball_and_stick()
+    np.testing.assert_allclose(pm.values.reshape(-1, K), spec.params, rtol=1e-6)
+
+
+def test_forward_matches_double_precision_port():
+    _, low, pm = small_ball_and_stick()
+    rec = low.phys_comp_off[:-1]
+    cab = Cable(low, pm.chan_param, pm.cell_ra_param, low.phys_ra)
+    tr, _ = cab.run(pm.values, low.n_steps, rec)
+    ref = eden_port.run(low, trace_target=rec, double=True)["trace"]
+    assert tr.max() > 0.0          # the cells spike
+    # the port returns its double trace rounded to float
+    np.testing.assert_allclose(tr, ref, rtol=0, atol=2e-5)
+
+
+def test_sensitivities_match_finite_differences():
+    _, low, pm = small_ball_and_stick()
+    rec = low.phys_comp_off[:-1]
+    cab = Cable(low, pm.chan_param, pm.cell_ra_param, low.phys_ra)
+    tr, dtr = cab.run(pm.values, low.n_steps, rec, per_cell_directions(pm.n_params))
+    target = tr + 0.5 * np.sin(np.arange(len(tr)))[:, None]
+    _, tg = loss_and_trace_grad(tr, target)
+    g_tl = np.einsum("nc,jnc->cj", tg, dtr)
+    # a small step isolates the derivative ...
+    g_fd = fd_grad(cab, low, pm, rec, target, 1e-6)
+    np.testing.assert_allclose(g_tl, g_fd, rtol=1e-4, atol=1e-6 * np.abs(g_fd).max())
+    # ... and the 1e-4 relative step agrees to its truncation error
+    g_fd4 = fd_grad(cab, low, pm, rec, target, 1e-4)
+    assert np.abs(g_tl - g_fd4).max() <= 1e-3 * np.abs(g_fd4).max()
+
+
+def test_oracle_refuses_networks_with_synapses():
+    low = lowering.lower(workloads.multicomp_net(n_cells=4, in_degree=2, length_ms=1.0))
+    with pytest.raises(ValueError):
+        Cable(low, None)
