@@ -378,7 +378,22 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     // window -- a forest of physical cells (joint breadth-first numbering,
     // at most kForestWidth nodes per depth level, at most kForestNodes nodes) or a batch
     // of up to 32 izhikevich neurons.  Targets are numbered unit by unit.
-    const int forest_node_cap = kForestNodes;
+    // Small networks get smaller forests, so that at least about four units
+    // per SM run (a window's time is that of its slowest warp); large ones
+    // fill forests up to kForestNodes.
+    int forest_node_cap = kForestNodes;
+    {
+        int64_t n_phys_comp = 0;
+        int largest = 1;
+        for (int k = 0; k < n_cells; k++)
+            if (cell_phys[k] >= 0) {
+                n_phys_comp += cell_n[k];
+                largest = std::max(largest, cell_n[k]);
+            }
+        const int64_t units = 4 * (int64_t)std::max(ctx->n_sm, 1);
+        const int64_t even = (n_phys_comp + units - 1) / units;
+        forest_node_cap = (int)std::min<int64_t>(kForestNodes, std::max<int64_t>({even, (int64_t)largest, 32}));
+    }
     std::vector<int32_t> u2i(nt, -1), i2u(nt, -1);
     std::vector<int32_t> c_parent(nt, -1), c_child0(nt, 0), c_nchild(nt, 0), t_izh(nt, -1);
     std::vector<float> c_u(nt, 0.f), c_l(nt, 0.f);
