@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--profile", action="store_true",
                     help="only advance the batched path (init + warmup + steps bench steps) for ncu")
+    ap.add_argument("--profile-adjoint", type=float, default=0.0, metavar="MS",
+                    help="only run one gradient forward and backward of the ball-and-stick "
+                         "configuration over MS ms, for ncu")
     return ap.parse_args()
 
 
@@ -176,6 +179,74 @@ def precision_sample(low, threads: int, n_steps: int = 400):
             "max_abs_dv_mV": dv}
 
 
+def adjoint_sample():
+    """The adjoint parameter-fitting configuration: 256 ball-and-stick cells
+    (soma + 50-compartment cable, HH everywhere), 7 parameters per cell
+    (soma and dendrite gNa, gK, gL; Ra) drawn lognormal, a 0.5 nA step for
+    150 ms, dt 0.025 ms for 200 ms (8001 steps); loss = MSE of the somatic V
+    against the trace of a second seeded parameter draw.  Times one forward
+    (trace + checkpoints every 100 steps) and one backward (recomputed
+    segments + adjoint) through edenGpuGrad*, the batched simulation of the
+    same network, and checks the gradient of the first 8 cells over the first
+    50 ms against the double-precision forward sensitivities (oracle/cable_grad.py)
+    contracted with the same trace gradient."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from cable_grad import Cable, loss_and_trace_grad
+    from eden_gb300 import lowering, workloads
+    from eden_gb300.engine import MODE_BATCHED, Simulation
+    from eden_gb300.gradient import CableGradient, per_cell_density_map
+    dens = [1, 2, 0, 4, 5, 3]
+    spec = workloads.ball_and_stick(seed=1234)
+    tspec = workloads.ball_and_stick(seed=4321)
+    low = lowering.lower(spec)
+    rec = np.ascontiguousarray(low.phys_comp_off[:-1], np.int32)
+    pm = per_cell_density_map(low, dens)
+    tpm = per_cell_density_map(lowering.lower(tspec), dens)
+    g = CableGradient(low, pm, rec_comp=rec, checkpoint_every=100)
+    target = g.forward(tpm.values).astype(np.float64)
+    fwd, bwd = [], []
+    for _ in range(3):
+        tr = g.forward(pm.values)
+        loss, tg = loss_and_trace_grad(tr.astype(np.float64), target)
+        grad = g.backward(tg)
+        f, b = g.timing()
+        fwd.append(f)
+        bwd.append(b)
+    g.close()
+    sim = Simulation(low, mode=MODE_BATCHED, trace_target=rec)
+    sim.run()
+    sim_ms = sim.device_ms
+    sim.close()
+    # accuracy on a bounded sample
+    n_sub, sub_ms = 8, 50.0
+    sub = workloads.ball_and_stick(n_inst=n_sub, length_ms=sub_ms, params=spec.params[:n_sub])
+    slow = lowering.lower(sub)
+    spm = per_cell_density_map(slow, dens)
+    srec = np.ascontiguousarray(slow.phys_comp_off[:-1], np.int32)
+    gs = CableGradient(slow, spm, rec_comp=srec)
+    tr_s = gs.forward(spm.values).astype(np.float64)
+    _, tg_s = loss_and_trace_grad(tr_s, target[:slow.n_steps, :n_sub])
+    grad_s = gs.backward(tg_s).reshape(-1, 7)
+    gs.close()
+    cab = Cable(slow, spm.chan_param, spm.cell_ra_param, slow.phys_ra)
+    dirs = np.zeros((7, spm.n_params))
+    for j in range(7):
+        dirs[j, j::7] = 1.0
+    _, dtr = cab.run(spm.values, slow.n_steps, srec, dirs)
+    g64 = np.einsum("nc,jnc->cj", tg_s, dtr)
+    rel = float((np.abs(grad_s - g64).max(0) / np.abs(g64).max(0)).max())
+    f_ms, b_ms = min(fwd), min(bwd)
+    return {"config": "ball_and_stick: 256 cells x 51 compartments, 7 parameters each (1792), "
+                      "dt 0.025 ms, 200 ms (8001 steps), checkpoints every 100 steps",
+            "loss": loss, "grad_norm": float(np.linalg.norm(grad)),
+            "forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
+            "batched_simulation_ms": sim_ms, "backward_over_batched_simulation": b_ms / sim_ms,
+            "grad_max_rel_err_vs_fp64": rel,
+            "grad_check": f"first {n_sub} cells, first {sub_ms:g} ms: GPU adjoint vs double-precision forward "
+                          "sensitivities contracted with the same trace gradient, per parameter, relative "
+                          "to that parameter's largest gradient"}
+
+
 def load_profile_traffic():
     """DRAM bytes per k_cells_t launch from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "k_cells_t_multicomp_net.json")
@@ -210,8 +281,23 @@ def max_over_ranks(x: float, dist) -> float:
     return float(t.item())
 
 
+def profile_adjoint(length_ms: float):
+    from eden_gb300 import lowering, workloads
+    from eden_gb300.gradient import CableGradient, per_cell_density_map
+    low = lowering.lower(workloads.ball_and_stick(length_ms=length_ms))
+    pm = per_cell_density_map(low, [1, 2, 0, 4, 5, 3])
+    g = CableGradient(low, pm, rec_comp=np.ascontiguousarray(low.phys_comp_off[:-1], np.int32))
+    tr = g.forward(pm.values)
+    g.backward(np.ones_like(tr) / tr.size)
+    print(json.dumps({"forward_ms": g.timing()[0], "backward_ms": g.timing()[1], "steps": low.n_steps}))
+    g.close()
+
+
 def main():
     args = parse()
+    if args.profile_adjoint > 0:
+        profile_adjoint(args.profile_adjoint)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -340,6 +426,7 @@ def main():
     # ---- CPU baseline (rank 0 only)
     cpu = None
     precision = None
+    adjoint = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
         cval, n = cpu_sample(low, threads, budget_s=15.0)
@@ -347,6 +434,7 @@ def main():
                "sample": f"{n} simulation steps of the same network (after 4 init passes), C restatement of "
                          f"the reference loop, OpenMP {threads} threads"}
         precision = precision_sample(low, threads)
+        adjoint = adjoint_sample()
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -369,7 +457,8 @@ def main():
                 "kernels_ms": {k: round(v[0], 3) for k, v in k_ms.items()},
                 "clocks": clk,
                 "cpu_baseline": cpu,
-                "spike_time_error": precision}
+                "spike_time_error": precision,
+                "adjoint": adjoint}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
