@@ -247,6 +247,51 @@ def adjoint_sample():
                           "to that parameter's largest gradient"}
 
 
+def scale_sample(dev: int):
+    """The scale configuration: 160,000 izhikevich2007 cells + 40,000
+    100-compartment HH-dendrite trees (4.16 M compartments), 20 M expTwo
+    synapses (in-degree 100, delays 0.5-10 ms), 20 M Poisson inputs at 2 Hz,
+    dt 0.025 ms.  Device memory the context holds, and batched and plain
+    throughput over 640 simulation steps after 320 warm-up steps (inputs
+    resident; the network is 1.2 GB, far above L2)."""
+    import torch
+    from eden_gb300 import lowering, workloads
+    from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
+    t0 = time.perf_counter()
+    low = lowering.lower(workloads.mixed_scale())
+    t_lower = time.perf_counter() - t0
+    out = {"workload": f"mixed_scale: {low.n_izh} izhikevich2007 + {low.n_phys} trees, {low.n_comp} compartments, "
+                       f"{len(low.syn_target)} expTwo synapses, {len(low.pois_target)} Poisson inputs at 2 Hz",
+           "targets": low.n_target, "host_lowering_s": t_lower}
+    for mode, key in ((MODE_BATCHED, "batched"), (MODE_PLAIN, "plain")):
+        torch.cuda.synchronize(dev)
+        free0 = torch.cuda.mem_get_info(dev)[0]
+        t0 = time.perf_counter()
+        sim = Simulation(low, mode=mode, device=dev, record_capacity_steps=STEPS_PER_ITER * 2,
+                         spike_capacity=1 << 24)
+        t_create = time.perf_counter() - t0
+        free1 = torch.cuda.mem_get_info(dev)[0]
+        sim.initialize()
+        sim.run_steps(STEPS_PER_ITER)
+        sim.fetch()
+        ms, spikes = 0.0, 0
+        for _ in range(2):
+            ms += sim.run_steps(STEPS_PER_ITER)
+            spikes += len(sim.fetch().spike_src)
+        sim.close()
+        steps = 2 * STEPS_PER_ITER
+        fan = len(low.syn_target) / max(len(low.src_target), 1)
+        ab = algorithmic_bytes(low, spikes * fan / steps)
+        out[key] = {"value": low.n_target * steps / (ms * 1e-3), "unit": UNIT, "ms_per_sim_step": ms / steps,
+                    "device_bytes": int(free0 - free1), "create_s": t_create,
+                    "step_algorithmic_bytes": ab["total"],
+                    "step_achieved_gbs": ab["total"] / (ms / steps * 1e-3) / 1e9,
+                    "spikes_per_sim_step": spikes / steps}
+    out["ratio_batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    out["fits_180_gb"] = max(out["batched"]["device_bytes"], out["plain"]["device_bytes"]) < 180e9
+    return out
+
+
 def load_profile_traffic():
     """DRAM bytes per k_cells_t launch from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "k_cells_t_multicomp_net.json")
@@ -427,6 +472,7 @@ def main():
     cpu = None
     precision = None
     adjoint = None
+    scale = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
         cval, n = cpu_sample(low, threads, budget_s=15.0)
@@ -435,6 +481,7 @@ def main():
                          f"the reference loop, OpenMP {threads} threads"}
         precision = precision_sample(low, threads)
         adjoint = adjoint_sample()
+        scale = scale_sample(dev)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -458,7 +505,8 @@ def main():
                 "clocks": clk,
                 "cpu_baseline": cpu,
                 "spike_time_error": precision,
-                "adjoint": adjoint}
+                "adjoint": adjoint,
+                "scale": scale}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

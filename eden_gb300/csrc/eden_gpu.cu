@@ -80,6 +80,7 @@ struct EdenGpuCtx {
     int smem_per_sm = 0, smem_optin = 0;   // bytes
     int gcap = 0, forest_cap = 0;           // largest cell / compartments per staged forest
     bool smem_window = false;              // groups fit shared memory
+    int max_cell_blocks = 0;               // most blocks of a k_cells_t launch
     size_t smem_hines = 0;
     struct CellClass { int cta_begin, cta_end; size_t smem; };
     std::vector<CellClass> classes;        // k_cells_t launches of one window
@@ -1080,6 +1081,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     ctx->grid_targets = blocks_for(nt);
     ctx->grid_hines = (int)std::max<int64_t>(1, ((int64_t)d.n_forest * 32 + kHinesThreads - 1) / kHinesThreads);
     ctx->grid_deliver = ctx->n_sm * 4;
+    ctx->max_cell_blocks = (opt && opt->max_cell_blocks > 0) ? opt->max_cell_blocks : ctx->n_sm * 32;
     ctx->grid_window = 0;
     // per-step Hines: each warp stages a forest of up to forest_cap compartments
     // (7 arrays plus depth boundaries); larger forests are solved in place
@@ -1271,7 +1273,7 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
         int n = 1;
         tmark(ctx, EDEN_KERNEL_CELLS, true);
         for (const auto &cl : ctx->classes) {
-            const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
+            const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->max_cell_blocks);
             launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, d, (const WindowArgs *)ctx->d_wtab, base, idx,
                      cl.cta_begin, cl.cta_end);
             n++;
@@ -1566,7 +1568,7 @@ static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const Windo
         launch_k(ctx->fn_inputs, ctx->grid_inputs, kInputThreads, 0, s, dm, tab, times, zero, idx);
         int n = 1;
         for (const auto &cl : ctx->classes) {
-            const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->n_sm * 32);
+            const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->max_cell_blocks);
             launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, dm, tab, zero, idx, cl.cta_begin, cl.cta_end);
             n++;
         }

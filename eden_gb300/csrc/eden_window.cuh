@@ -364,6 +364,9 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
 #undef IZ
 
 // This launch runs CTAs [cta_begin, cta_end), each a few units, one per warp.
+// A block runs several CTAs in turn when there are more CTAs than blocks;
+// their units are laid out differently in shared memory, so every warp of
+// the block finishes its unit before any starts on the next CTA.
 __global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const WindowArgs *tab, const int *base, int idx,
                                                           int cta_begin, int cta_end) {
     extern __shared__ float sm[];
@@ -371,9 +374,11 @@ __global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const W
     const int warp = threadIdx.x >> 5;
     for (int cta = cta_begin + blockIdx.x; cta < cta_end; cta += gridDim.x) {
         const int u = m.cta_u0[cta] + warp;
-        if (u >= m.cta_u0[cta + 1]) continue;
-        if (m.un_f[u] >= 0) forest_window(m, w, u, sm + m.un_off[u]);
-        else izh_window(m, w, u, sm + m.un_off[u]);
+        if (u < m.cta_u0[cta + 1]) {
+            if (m.un_f[u] >= 0) forest_window(m, w, u, sm + m.un_off[u]);
+            else izh_window(m, w, u, sm + m.un_off[u]);
+        }
+        __syncthreads();
     }
 }
 

@@ -170,18 +170,21 @@ def _cable_geometry(cell: PhysicalCell):
     r_prox, r_dist = r_half, r_half
     parent = np.asarray(cell.seg_parent, np.int64)
     r_axial = np.full(n, np.nan, dtype=F32)
-    for i in range(n):
-        p = parent[i]
-        if p >= 0:
-            r_axial[i] = F32(r_prox[i] + r_dist[p])
     inv_rc = np.zeros(n, dtype=F32)
-    for i in range(n):
-        p = parent[i]
-        if p >= 0:
-            # edge (i, p) contributes to both ends; index by the child
-            inv_rc[i] = F32(inv_rc[i] + F32(1.0 / (float(r_axial[i]) * float(c[i]))))
-            inv_rc[p] = F32(inv_rc[p] + F32(1.0 / (float(r_axial[i]) * float(c[p]))))
+    ci = np.nonzero(parent >= 0)[0]
+    if len(ci):
+        pi = parent[ci]
+        r_axial[ci] = (r_prox[ci] + r_dist[pi]).astype(F32)
+        r64 = r_axial[ci].astype(np.float64)
+        # edge (i, p) contributes to both ends; a node's own edge comes first,
+        # then its children's in increasing order (the order of a loop over i)
+        inv_rc[ci] = (1.0 / (r64 * c[ci].astype(np.float64))).astype(F32)
+        np.add.at(inv_rc, pi, (1.0 / (r64 * c[pi].astype(np.float64))).astype(F32))
     return c, r_axial, area, inv_rc
+
+
+def joined(parts, dtype) -> np.ndarray:
+    return np.concatenate(parts).astype(dtype) if parts else np.zeros(0, dtype)
 
 
 def lower(spec: NetworkSpec) -> LoweredModel:
@@ -211,9 +214,10 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     # ---- cells, in gid order ------------------------------------------------
     phys_off = [0]
     comp_parent, comp_c, comp_r, comp_area, comp_inv, comp_v0 = [], [], [], [], [], []
-    chan_off = [0]
+    chan_off = [np.zeros(1, np.int64)]     # per cell: arrays, joined at the end
     chan_type, chan_g, chan_e = [], [], []
     chan_dens, phys_ra = [], []
+    chan_cache, chan_count = {}, [0]
     izh = []
     src_target = np.zeros(n_cells, np.int32)
     src_thr = np.full(n_cells, np.nan, np.float32)
@@ -237,14 +241,28 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                 comp_area.append(a)
                 comp_inv.append(inv)
                 comp_v0.append(np.full(ct.n_seg, _to_f32(ct.v0), np.float32))
-                for s in range(ct.n_seg):
-                    for kd, dens in enumerate(ct.densities):
-                        if dens.seg_mask[s]:
-                            chan_dens.append(kd)
-                            chan_type.append(dens.channel)
-                            chan_g.append(dens.cond)
-                            chan_e.append(dens.erev)
-                    chan_off.append(len(chan_type))
+                if ct.name not in chan_cache:
+                    # channels segment by segment, densities in declaration order
+                    if ct.densities:
+                        mask = np.stack([np.asarray(d.seg_mask, bool) for d in ct.densities])  # [D, n_seg]
+                        seg_i, kd = np.nonzero(mask.T)
+                    else:
+                        seg_i = kd = np.zeros(0, np.int64)
+                    per_seg = np.bincount(seg_i, minlength=ct.n_seg)
+                    dd = ct.densities
+                    chan_cache[ct.name] = (kd.astype(np.int32),
+                                           np.array([dd[k].channel for k in range(len(dd))], np.int32)[kd],
+                                           np.array([dd[k].cond for k in range(len(dd))], np.float64)[kd],
+                                           np.array([dd[k].erev for k in range(len(dd))], np.float64)[kd],
+                                           np.cumsum(per_seg))
+                kd_c, ty_c, g_c, e_c, ends = chan_cache[ct.name]
+                n_before = chan_count[0]
+                chan_dens.append(kd_c)
+                chan_type.append(ty_c)
+                chan_g.append(g_c)
+                chan_e.append(e_c)
+                chan_off.append(n_before + ends)
+                chan_count[0] += len(kd_c)
                 phys_off.append(base + ct.n_seg)
                 phys_ra.append(float(ct.ra))
                 src_target[gid] = base  # segment 0 detects spikes
@@ -353,10 +371,10 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         comp_parent=cat(comp_parent, np.int32), comp_c=cat(comp_c, F32),
         comp_r_axial=cat(comp_r, F32), comp_area=cat(comp_area, F32),
         comp_inv_rc=cat(comp_inv, F32), comp_v0=cat(comp_v0, F32),
-        chan_types=chan_types, comp_chan_off=np.asarray(chan_off, np.int32),
-        chan_type=np.asarray(chan_type, np.int32),
-        chan_gbase=np.asarray(chan_g, np.float64).astype(F32),
-        chan_erev=np.asarray(chan_e, np.float64).astype(F32),
+        chan_types=chan_types, comp_chan_off=np.concatenate(chan_off).astype(np.int32),
+        chan_type=joined(chan_type, np.int32),
+        chan_gbase=joined(chan_g, np.float64).astype(F32),
+        chan_erev=joined(chan_e, np.float64).astype(F32),
         izh_params=izh_arr,
         src_target=src_target, src_threshold=src_thr,
         src_cell_seed=cell_seeds(spec.seed, n_cells),
@@ -367,7 +385,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         pulse_target=qt, pulse_start=qs, pulse_duration=qd, pulse_amplitude=qa,
         pulse_weight=np.ones(len(qt), F32),
         trace_target=trace_target, event_src=event_src, gid_target_base=gid_base,
-        chan_density=np.asarray(chan_dens, np.int32), phys_ra=np.asarray(phys_ra, np.float64),
+        chan_density=joined(chan_dens, np.int32), phys_ra=np.asarray(phys_ra, np.float64),
     )
 
 

@@ -227,23 +227,32 @@ class NetworkSpec:
     event_format: str = "TIME_ID"
 
     # -- lookups ---------------------------------------------------------
+    def _index(self, attr: str, items) -> dict:
+        # name -> item, rebuilt when the list changed length
+        cache = self.__dict__.setdefault("_lookup", {})
+        hit = cache.get(attr)
+        if hit is None or hit[0] != len(items):
+            hit = (len(items), {x.name: x for x in reversed(items)})
+            cache[attr] = hit
+        return hit[1]
+
     def cell_type(self, name: str):
-        for c in self.cells:
-            if c.name == name:
-                return c
-        raise KeyError(name)
+        try:
+            return self._index("cells", self.cells)[name]
+        except KeyError:
+            raise KeyError(name) from None
 
     def synapse(self, name: str) -> SynapseType:
-        for s in self.synapses:
-            if s.name == name:
-                return s
-        raise KeyError(name)
+        try:
+            return self._index("synapses", self.synapses)[name]
+        except KeyError:
+            raise KeyError(name) from None
 
     def population(self, name: str) -> Population:
-        for p in self.populations:
-            if p.name == name:
-                return p
-        raise KeyError(name)
+        try:
+            return self._index("populations", self.populations)[name]
+        except KeyError:
+            raise KeyError(name) from None
 
     def pop_offsets(self) -> dict:
         """Global cell id (gid) of each population's first cell, in

@@ -179,11 +179,18 @@ def izh_net(n_cells: int = 100000, in_degree: int = 100, length_ms: float = 1000
 
 
 def _gid_to_pop(spec, gid):
-    for p in spec.populations:
-        if gid < p.size:
-            return p.name, gid
-        gid -= p.size
-    raise IndexError(gid)
+    """(population, index) of a global cell id."""
+    n_pops = len(spec.populations)
+    cache = spec.__dict__.setdefault("_gid_starts", {})
+    starts = cache.get(n_pops)
+    if starts is None:
+        starts = np.concatenate([[0], np.cumsum([p.size for p in spec.populations])])
+        cache.clear()
+        cache[n_pops] = starts
+    k = int(np.searchsorted(starts, gid, side="right")) - 1
+    if gid < 0 or k >= n_pops:
+        raise IndexError(gid)
+    return spec.populations[k].name, int(gid - starts[k])
 
 
 # ---------------------------------------------------------------------------

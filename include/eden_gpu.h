@@ -163,7 +163,10 @@ typedef struct EdenGpuOptions {
     int32_t codegen;          /* batched mode: 0 = compile the windowed kernels for the
                                  model's channel sets with NVRTC when available (else use
                                  the built-in ones), 1 = require it, -1 = built-in kernels */
-    int32_t reserved[6];
+    int32_t max_cell_blocks;  /* batched mode: most blocks of one windowed cell-kernel launch
+                                 (0 = 32 per SM); with fewer blocks than CTAs each block runs
+                                 several CTAs in turn */
+    int32_t reserved[5];
 } EdenGpuOptions;
 
 /* Kernels whose device time kernel_timing accumulates. */

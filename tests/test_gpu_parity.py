@@ -90,3 +90,24 @@ def test_gpu_matches_reference_outputs(name, oracle_runs):
     assert not wrong and not far, f"spike trains differ: counts {wrong[:5]}, timing {far[:5]}"
     nbad, worst = box_violations(ref_trace, rec.trace, dt_ms, 0.1, CASES[name][2])
     assert nbad == 0, f"{nbad} samples outside box, worst {worst} mV"
+
+
+@pytest.mark.parametrize("blocks", [1, 3])
+def test_blocks_running_several_ctas_in_turn(blocks):
+    """With fewer cell-kernel blocks than CTAs (networks of more than 32
+    CTAs per SM, forced here on a small one), every block runs several CTAs
+    one after another in its shared memory; the records equal those of one
+    CTA per block bit for bit."""
+    low = lowering.lower(EXTRA["mixed_small"]())
+    out = []
+    for cap in (0, blocks):
+        sim = Simulation(low, mode=MODE_BATCHED, max_cell_blocks=cap)
+        try:
+            out.append(sim.run())
+        finally:
+            sim.close()
+    a, b = out
+    assert len(a.spike_src) > 0
+    np.testing.assert_array_equal(a.trace, b.trace)
+    np.testing.assert_array_equal(a.spike_src, b.spike_src)
+    np.testing.assert_array_equal(a.spike_step, b.spike_step)
