@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--profile", action="store_true",
                     help="only advance the batched path (init + warmup + steps bench steps) for ncu")
+    ap.add_argument("--shape", type=str, default="",
+                    help="batched launch shape steps_per_launch,segments_per_warp,segments_per_depth "
+                         "(0 = built-in) instead of the autotuner's")
     ap.add_argument("--profile-adjoint", type=float, default=0.0, metavar="MS",
                     help="only run one gradient forward and backward of the ball-and-stick "
                          "configuration over MS ms, for ncu")
@@ -379,10 +382,22 @@ def main():
         return
 
     import torch
+    from eden_gb300 import autotune
     from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
     torch.cuda.set_device(dev)
+    # ---- launch shape: the autotuner's choice (searched once per network
+    # and device, outside every timed region), or the one given
+    if args.shape:
+        k, spw, spd = (int(x) for x in args.shape.split(","))
+        shape = {"steps_per_launch": k, "segments_per_warp": spw, "segments_per_depth": spd}
+        config["launch_shape"] = dict(shape, source="--shape")
+    else:
+        tuned = autotune.tune(low, dev)
+        shape = autotune.options(tuned)
+        config["launch_shape"] = dict(shape, source="autotuner", search_s=round(tuned["search_s"], 2),
+                                      candidates_timed=len(tuned["tried"]), cached=tuned["cached"])
     if args.profile:
-        sim = Simulation(low, mode=MODE_BATCHED, device=dev, record_capacity_steps=STEPS_PER_ITER * 2)
+        sim = Simulation(low, mode=MODE_BATCHED, device=dev, record_capacity_steps=STEPS_PER_ITER * 2, **shape)
         sim.initialize()
         for _ in range(args.warmup + args.steps):
             sim.run_steps(STEPS_PER_ITER)
@@ -393,7 +408,8 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     # ---- device-timed batched run (kernel timing on: CUDA events around each launch)
-    sim = Simulation(low, mode=MODE_BATCHED, device=dev, kernel_timing=True, record_capacity_steps=STEPS_PER_ITER * 2)
+    sim = Simulation(low, mode=MODE_BATCHED, device=dev, kernel_timing=True, record_capacity_steps=STEPS_PER_ITER * 2,
+                     **shape)
     sim.initialize()
     for _ in range(max(3, args.warmup)):
         sim.run_steps(STEPS_PER_ITER)
@@ -453,7 +469,7 @@ def main():
     torch.cuda.synchronize()
     e2e_steps = int(low.n_steps)
     t0 = time.perf_counter()
-    esim = Simulation(low, mode=MODE_BATCHED, device=dev, record_capacity_steps=4096)
+    esim = Simulation(low, mode=MODE_BATCHED, device=dev, record_capacity_steps=4096, **shape)
     rec_bytes = 0
     esim.initialize()
     done = 0

@@ -383,7 +383,10 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     // per SM run (a window's time is that of its slowest warp); large ones
     // fill forests up to kForestNodes.
     int forest_node_cap = kForestNodes;
-    {
+    const int forest_width = (opt && opt->segments_per_depth > 0) ? std::min(opt->segments_per_depth, 1023) : kForestWidth;
+    if (opt && opt->segments_per_warp > 0) {
+        forest_node_cap = std::min(opt->segments_per_warp, 1023);
+    } else {
         int64_t n_phys_comp = 0;
         int largest = 1;
         for (int k = 0; k < n_cells; k++)
@@ -418,7 +421,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
                 const std::vector<int> &cw = cell_width[c];
                 bool fits = fc.empty() || nodes + cell_n[c] <= forest_node_cap;
                 for (size_t d = 0; fits && d < cw.size(); d++)
-                    if ((d < fw.size() ? fw[d] : 0) + cw[d] > kForestWidth) fits = false;
+                    if ((d < fw.size() ? fw[d] : 0) + cw[d] > forest_width) fits = false;
                 if (!fits && !fc.empty()) break;
                 if (fw.size() < cw.size()) fw.resize(cw.size(), 0);
                 for (size_t d = 0; d < cw.size(); d++) fw[d] += cw[d];
@@ -1086,7 +1089,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     // per-step Hines: each warp stages a forest of up to forest_cap compartments
     // (7 arrays plus depth boundaries); larger forests are solved in place
     const int hines_warps = kHinesThreads / 32;
-    ctx->forest_cap = std::min(ctx->forest_cap + 1, kForestNodes + 1);
+    ctx->forest_cap = std::min(ctx->forest_cap + 1, std::max(kForestNodes, max_forest) + 1);
     ctx->smem_hines = (size_t)hines_warps * 8 * ctx->forest_cap * sizeof(float);
     if (ctx->smem_hines > (size_t)ctx->smem_optin) {
         ctx->forest_cap = (int)(ctx->smem_optin / (hines_warps * 8 * sizeof(float)));

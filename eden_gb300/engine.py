@@ -36,7 +36,8 @@ class COptions(ctypes.Structure):
                 ("record_capacity_steps", ctypes.c_int32), ("spike_capacity", ctypes.c_int32),
                 ("n_trace", ctypes.c_int32), ("trace_target", ctypes.POINTER(ctypes.c_int32)),
                 ("kernel_timing", ctypes.c_int32), ("codegen", ctypes.c_int32),
-                ("max_cell_blocks", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("max_cell_blocks", ctypes.c_int32), ("segments_per_warp", ctypes.c_int32),
+                ("segments_per_depth", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class CRecords(ctypes.Structure):
@@ -117,7 +118,8 @@ class Simulation:
     def __init__(self, lowered: LoweredModel, mode: int = MODE_BATCHED, device: int = 0,
                  steps_per_launch: int = 0, cells_per_block: int = 0, trace_target=None,
                  record_capacity_steps: int = 4096, spike_capacity: int = 1 << 22,
-                 kernel_timing: bool = False, codegen: int = 0, max_cell_blocks: int = 0):
+                 kernel_timing: bool = False, codegen: int = 0, max_cell_blocks: int = 0,
+                 segments_per_warp: int = 0, segments_per_depth: int = 0):
         self.lib = load_library()
         self.lowered = lowered
         self._cm, self._keep = to_cmodel(lowered)
@@ -133,6 +135,8 @@ class Simulation:
         opt.kernel_timing = 1 if kernel_timing else 0
         opt.codegen = codegen
         opt.max_cell_blocks = max_cell_blocks
+        opt.segments_per_warp = segments_per_warp
+        opt.segments_per_depth = segments_per_depth
         opt.n_trace = len(self.trace_target)
         opt.trace_target = self.trace_target.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if len(self.trace_target) else None
         self._opt = opt

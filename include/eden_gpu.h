@@ -166,7 +166,11 @@ typedef struct EdenGpuOptions {
     int32_t max_cell_blocks;  /* batched mode: most blocks of one windowed cell-kernel launch
                                  (0 = 32 per SM); with fewer blocks than CTAs each block runs
                                  several CTAs in turn */
-    int32_t reserved[5];
+    int32_t segments_per_warp;  /* most compartments of one warp's forest of cells (0 = sized
+                                   to the network, at most 768; at most 1023); a larger cell
+                                   gets a warp of its own */
+    int32_t segments_per_depth; /* most compartments of a forest at one depth (0 = 64) */
+    int32_t reserved[3];
 } EdenGpuOptions;
 
 /* Kernels whose device time kernel_timing accumulates. */
