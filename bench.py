@@ -150,15 +150,17 @@ def cpu_sample(low, threads: int, budget_s: float = 15.0):
     return low.n_target * n / (dt * n / (n + 4)), n
 
 
-def precision_sample(low, threads: int, n_steps: int = 400):
+def precision_sample(low, n_steps: int = 800, dev: int = 0, trace_target=None):
     """Spike-time and voltage error of the batched GPU path against the
-    double-precision oracle over the first n_steps of the same network (a
-    bounded sample: the oracle runs on the host cores)."""
+    double-precision oracle (the C restatement built for the GPU in double,
+    oracle/gpu64) over the first n_steps of the same network."""
     sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
     import eden_port
     from eden_gb300.engine import MODE_BATCHED, Simulation
-    f64 = eden_port.run(low, n_steps=n_steps, threads=threads, spike_cap=1 << 22, double=True)
-    sim = Simulation(low, mode=MODE_BATCHED, record_capacity_steps=n_steps + 8)
+    tt = np.ascontiguousarray(low.trace_target if trace_target is None else trace_target, np.int32)
+    f64 = eden_port.run_gpu64(low, n_steps=n_steps, trace_target=tt, spike_cap=1 << 24, device=dev)
+    sim = Simulation(low, mode=MODE_BATCHED, device=dev, record_capacity_steps=n_steps + 8, trace_target=tt,
+                     spike_capacity=1 << 24)
     rec = sim.run(n_steps)
     sim.close()
     keep = f64["spike_step"] <= n_steps
@@ -177,9 +179,9 @@ def precision_sample(low, threads: int, n_steps: int = 400):
             worst = max(worst, max(abs(p - q) for p, q in zip(x, y)))
     dv = float(np.abs(rec.trace.astype(np.float64) - f64["trace"]).max()) if rec.trace.size else 0.0
     dt_ms = float(low.dt) * 1e-3
-    return {"reference": "double-precision oracle (oracle/port, EDEN_PORT_DOUBLE)", "steps": n_steps,
-            "spikes": int(keep.sum()), "cells_count_mismatch": mismatch, "max_spike_shift_ms": worst * dt_ms,
-            "max_abs_dv_mV": dv}
+    return {"reference": "double-precision GPU oracle (oracle/gpu64: the C restatement in FP64)",
+            "steps": n_steps, "ms": n_steps * dt_ms, "spikes": int(keep.sum()), "cells_count_mismatch": mismatch,
+            "max_spike_shift_ms": worst * dt_ms, "max_abs_dv_mV": dv}
 
 
 def adjoint_sample():
@@ -291,6 +293,9 @@ def scale_sample(dev: int):
                     "step_achieved_gbs": ab["total"] / (ms / steps * 1e-3) / 1e9,
                     "spikes_per_sim_step": spikes / steps}
     out["ratio_batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    # V of ten somas and ten izhikevich cells
+    tt = np.concatenate([low.phys_comp_off[:10], low.n_comp + np.arange(min(10, low.n_izh))])
+    out["spike_time_error"] = precision_sample(low, n_steps=400, dev=dev, trace_target=tt)
     out["fits_180_gb"] = max(out["batched"]["device_bytes"], out["plain"]["device_bytes"]) < 180e9
     return out
 
@@ -495,7 +500,7 @@ def main():
         cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} simulation steps of the same network (after 4 init passes), C restatement of "
                          f"the reference loop, OpenMP {threads} threads"}
-        precision = precision_sample(low, threads)
+        precision = precision_sample(low, dev=dev)
         adjoint = adjoint_sample()
         scale = scale_sample(dev)
 

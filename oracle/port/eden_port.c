@@ -49,8 +49,17 @@ typedef float real;
 
 #include "../../include/eden_gpu.h"
 
+/* The per-step functions also compile as CUDA device code: the GPU build
+ * (oracle/gpu64/eden_port_gpu.cu, double precision) runs this same source,
+ * one thread per cell, as the FP64 GPU oracle. */
+#ifdef __CUDACC__
+#define PORT_FN __host__ __device__
+#else
+#define PORT_FN
+#endif
+
 /* ---- RNG: Thomas Wang's 64-bit integer hash, as used by randof ---------- */
-static uint64_t hash64shift(uint64_t key) {
+static PORT_FN uint64_t hash64shift(uint64_t key) {
     key = (~key) + (key << 21);
     key = key ^ (key >> 24);
     key = (key + (key << 3)) + (key << 8);
@@ -61,7 +70,7 @@ static uint64_t hash64shift(uint64_t key) {
     return key;
 }
 
-static real randof(real x, int64_t work_item, int64_t instance, int64_t step, int invocation_id) {
+static PORT_FN real randof(real x, int64_t work_item, int64_t instance, int64_t step, int invocation_id) {
     uint64_t hi = ((uint64_t)work_item << 24) | ((uint64_t)instance & ((1ULL << 24) - 1));
     uint64_t lo = ((uint64_t)(int64_t)invocation_id << 40) | ((uint64_t)step & ((1ULL << 40) - 1));
     uint64_t sample = hash64shift(hash64shift(lo) ^ hi);
@@ -70,7 +79,7 @@ static real randof(real x, int64_t work_item, int64_t instance, int64_t step, in
     return x * r;
 }
 
-static real rate_value(int kind, real r, real mid, real s, real v) {
+static PORT_FN real rate_value(int kind, real r, real mid, real s, real v) {
     switch (kind) {
         case EDEN_RATE_EXP: return r * EXP((v - mid) / s);
         case EDEN_RATE_EXPLINEAR:
@@ -131,7 +140,7 @@ static void dfs_postorder(const int32_t *parent, int n, int32_t *order) {
 
 /* One synapse instance: trigger/pending logic, exposure, state update.
  * Returns the weighted current and conductance through *iw, *gw. */
-static inline void synapse_step(const EdenGpuSynapseType *st, int init, real t, real dt,
+static inline PORT_FN void synapse_step(const EdenGpuSynapseType *st, int init, real t, real dt,
                                 int spike_in_raw, real delay, real pend, real *pend_next,
                                 real a, real b, real *a_next, real *b_next, real v, real w,
                                 real *iw, real *gw, int *fired) {
@@ -183,7 +192,7 @@ static inline void synapse_step(const EdenGpuSynapseType *st, int init, real t, 
 }
 
 /* Poisson-driven synapse: the spiker fires its own synapse in the same step. */
-static inline void poisson_step(const Port *P, int cur, int64_t k, int init, real dt, int64_t step,
+static inline PORT_FN void poisson_step(const Port *P, int cur, int64_t k, int init, real dt, int64_t step,
                                 real v, real *iw, real *gw) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
@@ -238,7 +247,7 @@ static inline void poisson_step(const Port *P, int cur, int64_t k, int init, rea
 
 /* Synapse + input currents into one target (in the reference's order:
  * inputs then synapses are separate totals, each synapse type a block). */
-static void target_currents(Port *P, int cur, int64_t tgt, int init, real t, real dt, int64_t step,
+static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, real t, real dt, int64_t step,
                             real v, real *I_in, real *G_in, real *I_syn, real *G_syn) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
@@ -289,13 +298,18 @@ static void target_currents(Port *P, int cur, int64_t tgt, int init, real t, rea
     *I_in = Iin; *G_in = Gin; *I_syn = Isyn; *G_syn = Gsyn;
 }
 
-static void send_spike(Port *P, int nxt, int32_t src) {
-    for (int64_t e = P->fan_off[src]; e < P->fan_off[src + 1]; e++)
+static PORT_FN void send_spike(Port *P, int nxt, int32_t src) {
+    for (int64_t e = P->fan_off[src]; e < P->fan_off[src + 1]; e++) {
+#ifdef __CUDA_ARCH__
+        ((volatile unsigned char *)P->trig[nxt])[P->fan_syn[e]] = 1;  /* every writer stores 1 */
+#else
         __atomic_store_n(&P->trig[nxt][P->fan_syn[e]], (unsigned char)1, __ATOMIC_RELAXED);
+#endif
+    }
     P->spiked[nxt][src] = 1;
 }
 
-static void phys_cell_step(Port *P, int cur, int32_t cell, int init, real t, real dt, int64_t step) {
+static PORT_FN void phys_cell_step(Port *P, int cur, int32_t cell, int init, real t, real dt, int64_t step) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
     int32_t c0 = m->phys_comp_off[cell], c1 = m->phys_comp_off[cell + 1];
@@ -375,7 +389,7 @@ static void phys_cell_step(Port *P, int cur, int32_t cell, int init, real t, rea
     }
 }
 
-static void izh_step(Port *P, int cur, int32_t k, int init, real t, real dt, int64_t step) {
+static PORT_FN void izh_step(Port *P, int cur, int32_t k, int init, real t, real dt, int64_t step) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
     int64_t tgt = (int64_t)m->n_comp + k;
@@ -415,10 +429,9 @@ static void izh_step(Port *P, int cur, int32_t k, int init, real t, real dt, int
  * output phase into trace[step][col] and every logged spike as
  * (source, logging step).  Returns 0 or a negative code.
  */
-int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const int32_t *trace_target,
-                  float *trace, int64_t spike_cap, int32_t *spike_src, int64_t *spike_step,
-                  int64_t *n_spikes, int64_t *syn_fire_count, float *syn_final_pending, int32_t n_threads) {
-    if (!m || m->abi_version != EDEN_GPU_ABI_VERSION) return EDEN_GPU_E_INVALID;
+/* Host set-up of the loop's state (initial values, CSR tables, Hines
+ * orders); also used by the GPU build, which mirrors it to the device. */
+static void port_setup(Port *PP, const EdenGpuModel *m) {
     Port P;
     memset(&P, 0, sizeof(P));
     P.m = m;
@@ -473,6 +486,26 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
     P.src_of_target = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nt + 1));
     for (int64_t t = 0; t < nt; t++) P.src_of_target[t] = -1;
     for (int32_t s = 0; s < m->n_src; s++) P.src_of_target[m->src_target[s]] = s;
+    *PP = P;
+}
+
+static void port_free(Port *P) {
+    for (int b = 0; b < 2; b++) {
+        free(P->v[b]); free(P->gate[b]); free(P->izh_u[b]); free(P->syn_a[b]); free(P->syn_b[b]);
+        free(P->syn_pend[b]); free(P->trig[b]); free(P->pois_ts[b]); free(P->pois_isi[b]);
+        free(P->pois_a[b]); free(P->pois_b[b]); free(P->spiked[b]);
+    }
+    free(P->diag); free(P->syn_fire_count); free(P->gate_off); free(P->syn_off); free(P->pois_off);
+    free(P->pulse_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
+}
+
+int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const int32_t *trace_target,
+                  float *trace, int64_t spike_cap, int32_t *spike_src, int64_t *spike_step,
+                  int64_t *n_spikes, int64_t *syn_fire_count, float *syn_final_pending, int32_t n_threads) {
+    if (!m || m->abi_version != EDEN_GPU_ABI_VERSION) return EDEN_GPU_E_INVALID;
+    Port P;
+    port_setup(&P, m);
+    const int64_t ns = m->n_syn;
 
 #ifdef _OPENMP
     if (n_threads > 0) omp_set_num_threads(n_threads);
@@ -518,12 +551,6 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
     if (syn_fire_count) memcpy(syn_fire_count, P.syn_fire_count, sizeof(int64_t) * (size_t)ns);
     if (syn_final_pending)
         for (int64_t s = 0; s < ns; s++) syn_final_pending[s] = (float)P.syn_pend[cur][s];
-    for (int b = 0; b < 2; b++) {
-        free(P.v[b]); free(P.gate[b]); free(P.izh_u[b]); free(P.syn_a[b]); free(P.syn_b[b]);
-        free(P.syn_pend[b]); free(P.trig[b]); free(P.pois_ts[b]); free(P.pois_isi[b]);
-        free(P.pois_a[b]); free(P.pois_b[b]); free(P.spiked[b]);
-    }
-    free(P.diag); free(P.syn_fire_count); free(P.gate_off); free(P.syn_off); free(P.pois_off);
-    free(P.pulse_off); free(P.fan_off); free(P.fan_syn); free(P.order); free(P.src_of_target);
+    port_free(&P);
     return rc;
 }
