@@ -117,6 +117,25 @@ inline std::string channel_routines(const EdenGpuChannelType *types, const std::
     return s;
 }
 
+// The kinds of inputs and targets the model has: the generated build
+// compiles only their code (the EDEN_KIND_* switches of eden_kernels.cuh).
+struct Kinds {
+    bool pulse = false, pois = false, syn = false, expone = false, exptwo = false, forest = false, izh = false;
+};
+
+inline std::string kind_defines(const Kinds &k) {
+    std::string s;
+    auto def = [&](const char *name, bool on) { s += std::string("#define ") + name + (on ? " 1\n" : " 0\n"); };
+    def("EDEN_KIND_PULSE", k.pulse);
+    def("EDEN_KIND_POIS", k.pois);
+    def("EDEN_KIND_SYN", k.syn);
+    def("EDEN_KIND_EXPONE", k.expone);
+    def("EDEN_KIND_EXPTWO", k.exptwo);
+    def("EDEN_KIND_FOREST", k.forest);
+    def("EDEN_KIND_IZH", k.izh);
+    return s;
+}
+
 // The full source: integer types NVRTC has no headers for, the generated
 // routines (plain arithmetic, needing nothing else), then the library's
 // kernel sources, which call them where EDEN_RTC_CHANNELS is defined.

@@ -1109,7 +1109,22 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     const int codegen = opt ? opt->codegen : 0;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window && codegen >= 0) {
         phase("codegen");
-        ctx->codegen_source = eden_codegen::program_source(eden_codegen::channel_routines(m->chan_types, chan_sets));
+        eden_codegen::Kinds kinds;
+        for (int b = 0; b < n_block; b++) {
+            const int kb = bk_kind[b];
+            kinds.pulse |= kb == BK_PULSE;
+            kinds.pois |= kb == BK_POIS;
+            kinds.syn |= kb == BK_SYN;
+            if (kb != BK_PULSE) {
+                const int sk = m->syn_types[bk_type[b]].kind;
+                kinds.expone |= sk == EDEN_SYN_EXPONE;
+                kinds.exptwo |= sk == EDEN_SYN_EXPTWO;
+            }
+        }
+        kinds.forest = d.n_forest > 0;
+        kinds.izh = n_izh > 0;
+        ctx->codegen_source = eden_codegen::program_source(eden_codegen::kind_defines(kinds) +
+                                                           eden_codegen::channel_routines(m->chan_types, chan_sets));
         eden_codegen::Kernels kk;
         std::string why;
         if (eden_codegen::compile(ctx->codegen_source, ctx->device, kk, why, ctx->codegen_ms)) {

@@ -445,6 +445,19 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
     m.sy_last[it] = last;
 }
 
+// Input and target kinds the kernels handle: all of them in the library's
+// own build; a build generated for one model (eden_codegen.cuh) defines only
+// the model's, and the compiler drops the code of the others.
+#ifndef EDEN_KIND_PULSE
+#define EDEN_KIND_PULSE 1
+#define EDEN_KIND_POIS 1
+#define EDEN_KIND_SYN 1
+#define EDEN_KIND_EXPONE 1
+#define EDEN_KIND_EXPTWO 1
+#define EDEN_KIND_FOREST 1
+#define EDEN_KIND_IZH 1
+#endif
+
 // Per-warp accumulation tiles: row `lane` (stride kAccStride, padded so that
 // both a row write and a column read are free of bank conflicts) holds the
 // lane's terms for each step of the window.
@@ -464,7 +477,7 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     const int kind = info & 3;
     const int n = info >> 8;
     float *rowA = tileA + lane * kAccStride, *rowB = tileB + lane * kAccStride;
-    if (kind == BK_PULSE) {
+    if (EDEN_KIND_PULSE && kind == BK_PULSE) {
         for (int r = 0; lane + 32 * r < n; r++) {
             const int64_t it = ck_i0 + lane + 32 * r;
             const float st = m.pu_start[it], du = m.pu_dur[it], aw = m.pu_amp[it] * m.pu_w[it];
@@ -506,13 +519,16 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     for (int r = 0; r < kChunkItems / 32; r++) {
         if (lane + 32 * r < n) {
             const int64_t it = i0 + 32 * r;
+            // only the input kinds the kernels are compiled for (all, or the model's)
             if (kind == BK_POIS) {
-                if (two) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
-                else pois_window<EDEN_SYN_EXPONE>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
-            } else {
+                if (EDEN_KIND_POIS) {
+                    if (two) { if (EDEN_KIND_EXPTWO) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used); }
+                    else if (EDEN_KIND_EXPONE) pois_window<EDEN_SYN_EXPONE>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
+                }
+            } else if (EDEN_KIND_SYN) {
                 const uint32_t mask = __float_as_uint(s1v[r]);
-                if (two) syn_window<EDEN_SYN_EXPTWO>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
-                else syn_window<EDEN_SYN_EXPONE>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
+                if (two) { if (EDEN_KIND_EXPTWO) syn_window<EDEN_SYN_EXPTWO>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used); }
+                else if (EDEN_KIND_EXPONE) syn_window<EDEN_SYN_EXPONE>(m, it, w, st, tk, s0v[r], mask, rowA, rowB, used);
             }
         }
     }

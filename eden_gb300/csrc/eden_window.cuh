@@ -375,10 +375,10 @@ __global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const W
     for (int cta = cta_begin + blockIdx.x; cta < cta_end; cta += gridDim.x) {
         const int u = m.cta_u0[cta] + warp;
         if (u < m.cta_u0[cta + 1]) {
-            if (m.un_f[u] >= 0) forest_window(m, w, u, sm + m.un_off[u]);
-            else izh_window(m, w, u, sm + m.un_off[u]);
+            if (m.un_f[u] >= 0) { if (EDEN_KIND_FOREST) forest_window(m, w, u, sm + m.un_off[u]); }
+            else if (EDEN_KIND_IZH) izh_window(m, w, u, sm + m.un_off[u]);
         }
-        __syncthreads();
+        if (cta + (int)gridDim.x < cta_end) __syncthreads();
     }
 }
 
