@@ -81,6 +81,7 @@ struct EdenGpuCtx {
     int gcap = 0, forest_cap = 0;           // largest cell / compartments per staged forest
     bool smem_window = false;              // groups fit shared memory
     int max_cell_blocks = 0;               // most blocks of a k_cells_t launch
+    std::vector<int64_t> h_ext_step;       // logging steps of the spike sources' events
     size_t smem_hines = 0;
     struct CellClass { int cta_begin, cta_end; size_t smem; };
     std::vector<CellClass> classes;        // k_cells_t launches of one window
@@ -219,11 +220,30 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
     }
     int64_t nt = (int64_t)m->n_comp + m->n_izh;
     if (nt == 0) return ctx->fail(EDEN_GPU_E_INVALID, "empty network");
-    if (m->n_src != m->n_phys + m->n_izh)
+    if (m->n_src < m->n_phys + m->n_izh)
         return ctx->fail(EDEN_GPU_E_INVALID, "need one spike source per cell (n_src %d, cells %d)", m->n_src,
                          m->n_phys + m->n_izh);
-    for (int s = 0; s < m->n_src; s++)
-        if (m->src_target[s] < 0 || m->src_target[s] >= nt) return ctx->fail(EDEN_GPU_E_INVALID, "source %d: bad target", s);
+    {
+        int with_target = 0;
+        for (int s = 0; s < m->n_src; s++) {
+            if (m->src_target[s] == -1) continue;  // a spike list or generator
+            if (m->src_target[s] < 0 || m->src_target[s] >= nt) return ctx->fail(EDEN_GPU_E_INVALID, "source %d: bad target", s);
+            with_target++;
+        }
+        if (with_target != m->n_phys + m->n_izh)
+            return ctx->fail(EDEN_GPU_E_INVALID, "need one spike source per cell (%d with a target, cells %d)",
+                             with_target, m->n_phys + m->n_izh);
+    }
+    if (m->n_ext < 0 || m->n_ext > INT32_MAX / 2 || (m->n_ext > 0 && (!m->ext_src || !m->ext_step)))
+        return ctx->fail(EDEN_GPU_E_INVALID, "bad spike-source event list");
+    for (int64_t k = 0; k < m->n_ext; k++) {
+        const int s = m->ext_src[k];
+        if (s < 0 || s >= m->n_src || m->src_target[s] != -1)
+            return ctx->fail(EDEN_GPU_E_INVALID, "spike-source event %lld: source %d is not a source without target",
+                             (long long)k, s);
+        if (m->ext_step[k] < 2 || m->ext_step[k] > INT32_MAX || (k > 0 && m->ext_step[k] < m->ext_step[k - 1]))
+            return ctx->fail(EDEN_GPU_E_INVALID, "spike-source event %lld: steps must be >= 2 and sorted", (long long)k);
+    }
     for (int k = 0; k < m->n_syn_types; k++) {
         const EdenGpuSynapseType &t = m->syn_types[k];
         if (t.kind != EDEN_SYN_EXPONE && t.kind != EDEN_SYN_EXPTWO) return ctx->fail(EDEN_GPU_E_INVALID, "synapse type kind");
@@ -311,6 +331,10 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         std::vector<char> seen_phys(n_phys, 0), seen_izh(n_izh, 0);
         for (int g = 0; g < n_cells; g++) {
             int ut = m->src_target[g];
+            if (ut < 0) {
+                cell_n[g] = 0;  // a spike list or generator: no target
+                continue;
+            }
             if (ut < n_comp) {
                 int c = comp_cell[ut];
                 if (seen_phys[c]) return ctx->fail(EDEN_GPU_E_INVALID, "cell %d has two spike sources", c);
@@ -340,7 +364,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             for (int i = a; i < b; i++)
                 c += 6.0 + n_in_user[i] + 8.0 * (m->comp_chan_off[i + 1] - m->comp_chan_off[i]);
             max_cell = std::max(max_cell, b - a);
-        } else {
+        } else if (cell_izh[g] >= 0) {
             c = 6.0 + n_in_user[n_comp + cell_izh[g]];
         }
         cost[g] = c;
@@ -410,7 +434,10 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     std::vector<int> coff, kids, fill;
     {
         std::vector<int> phys, izhs;
-        for (int k = 0; k < n_cells; k++) (cell_phys[order[k]] >= 0 ? phys : izhs).push_back(order[k]);
+        for (int k = 0; k < n_cells; k++) {
+            if (cell_phys[order[k]] >= 0) phys.push_back(order[k]);
+            else if (cell_izh[order[k]] >= 0) izhs.push_back(order[k]);
+        }
         size_t pi = 0;
         while (pi < phys.size()) {
             std::vector<int> fc;
@@ -600,7 +627,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     std::vector<uint32_t> c_cep(nt, 0);
     {
         std::vector<char> is_src(nt, 0);
-        for (int s = 0; s < m->n_src; s++) is_src[u2i[m->src_target[s]]] = 1;
+        for (int s = 0; s < m->n_src; s++)
+            if (m->src_target[s] >= 0) is_src[u2i[m->src_target[s]]] = 1;
         for (size_t f = 0; f < fo_t0.size(); f++) {
             const int a = fo_t0[f], b = fo_t1[f];
             for (int it = b - 1; it >= a; it--) {
@@ -723,7 +751,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     std::vector<int32_t> t_src(nt, -1);
     std::vector<float> src_thr(m->n_src);
     for (int s = 0; s < m->n_src; s++) {
-        t_src[u2i[m->src_target[s]]] = s;
+        if (m->src_target[s] >= 0) t_src[u2i[m->src_target[s]]] = s;
         src_thr[s] = m->src_threshold[s];
     }
     phase("blocks");
@@ -999,6 +1027,13 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     ctx->h_sy_type = sy_type;
     TRY(upload_c(ctx, &d.t_src, t_src)); TRY(upload_c(ctx, &d.src_thr, src_thr));
     TRY(upload_c(ctx, &d.fan0, fan0)); TRY(upload_c(ctx, &d.fan_syn, fan_syn));
+    {
+        std::vector<int32_t> es(m->ext_src, m->ext_src + m->n_ext), ek((size_t)m->n_ext);
+        for (int64_t k = 0; k < m->n_ext; k++) ek[(size_t)k] = (int32_t)m->ext_step[k];
+        TRY(upload_c(ctx, &d.ext_src, es));
+        TRY(upload_c(ctx, &d.ext_step, ek));
+        ctx->h_ext_step.assign(m->ext_step, m->ext_step + m->n_ext);
+    }
     // a source spikes at most once per step: a window list never exceeds n_src * K
     size_t wcap = (size_t)m->n_src * (size_t)std::max(ctx->K, 4) + 32;
     for (int b = 0; b < 2; b++) {
@@ -1243,6 +1278,11 @@ static void fill_window(EdenGpuCtx *ctx, WindowArgs &w, WindowTimes &tt, int64_t
     w.Kprev = ctx->Kprev;
     w.par = ctx->par;
     w.wpar = ctx->wpar;
+    {
+        const auto &es = ctx->h_ext_step;
+        w.ext0 = (int32_t)(std::lower_bound(es.begin(), es.end(), s + 1) - es.begin());
+        w.ext1 = (int32_t)(std::lower_bound(es.begin(), es.end(), s + K + 1) - es.begin());
+    }
     double t = ctx->time;
     for (int j = 0; j < 32; j++) {
         tt.tk[j] = (float)t;

@@ -145,6 +145,8 @@ struct DevModel {
     const float *src_thr;
     const int64_t *fan0;
     const int32_t *fan_syn;
+    // spikes of the sources with no target, in step order: source, logging step
+    const int32_t *ext_src, *ext_step;
     // window spike lists (double-buffered by window parity) and the spike log
     int32_t *wspk_src[2];
     int32_t *wspk_step[2];
@@ -216,6 +218,7 @@ struct WindowArgs {
     int32_t K, Kprev;
     int32_t par;   // which V buffer holds the state at step0
     int32_t wpar;  // window parity: which spike list this window fills
+    int32_t ext0, ext1;  // the spikes of sources with no target logged in steps step0+1 .. step0+K
 };
 
 // Single-precision times (us) of the window's steps and of the previous

@@ -116,9 +116,13 @@ __global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs 
     // the other parity's list was consumed by the previous window's delivery
     // and is refilled only by the next window: clear it for that window
     if (blockIdx.x == 0 && threadIdx.x == 0) m.wspk_count[wp ^ 1] = 0;
-    for (int e = warp; e < n; e += nwarps) {
-        int src = m.wspk_src[wp][e];
-        int log_step = m.wspk_step[wp][e];
+    // then the window's spikes of sources with no target (spike lists and
+    // generators, computed in advance)
+    const int n_all = n + (w.ext1 - w.ext0);
+    for (int e = warp; e < n_all; e += nwarps) {
+        const bool own = e < n;
+        int src = own ? m.wspk_src[wp][e] : m.ext_src[w.ext0 + e - n];
+        int log_step = own ? m.wspk_step[wp][e] : m.ext_step[w.ext0 + e - n];
         uint32_t bit = 1u << (uint32_t)(log_step - w.step0);
         int64_t f0 = m.fan0[src], f1 = m.fan0[src + 1];
         for (int64_t f = f0 + lane; f < f1; f += 32) atomicOr(&m.sy_mask[m.fan_syn[f]], bit);

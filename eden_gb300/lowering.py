@@ -27,7 +27,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .network import (Izhikevich2007Cell, NetworkSpec, PhysicalCell,
+from .network import (SPIKE_SOURCE_TYPES, Izhikevich2007Cell, NetworkSpec, PhysicalCell, SpikeArrayCell,
                       SYN_EXPONE, SYN_EXPTWO)
 
 F32 = np.float32
@@ -120,6 +120,9 @@ class LoweredModel:
     # bookkeeping
     gid_target_base: np.ndarray = field(default=None)  # first target of each gid
     chan_density: np.ndarray = field(default=None)     # channel -> index of its channelDensity in the cell type
+    # spikes of the sources with no target, (source, logging step), in step order
+    ext_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    ext_step: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     phys_ra: np.ndarray = field(default=None)          # physical cell -> axial resistivity, ohm*cm
 
     @property
@@ -183,6 +186,51 @@ def _cable_geometry(cell: PhysicalCell):
     return c, r_axial, area, inv_rc
 
 
+def step_times_f32(dt: np.float32, n_steps: int) -> np.ndarray:
+    """Float time (us) of steps 1..n_steps: the double sum of k - 1 float
+    dts, as a float (eden/Eden.cpp:11486, 11931)."""
+    acc = np.concatenate([[0.0], np.add.accumulate(np.full(max(n_steps - 1, 0), float(np.float32(dt))))])
+    return acc[:n_steps].astype(F32)
+
+
+def spike_source_steps(ext_cells: dict, dt: np.float32, n_steps: int):
+    """(source, logging step) of every spike the spike sources emit in steps
+    1..n_steps, in step order and by source within a step.  A step n emits
+    when it crosses the next spike time: spikeArray (the reference's spike
+    list, eden/Eden.cpp:6738-6790) when the next listed time T < t_n + dt
+    in float, consuming every such time; spikeGenerator
+    (LEMS_CoreComponents.inc.xml:739-777) when tnext - t_n < 1e-9 ms, then
+    tnext += period (tnext = period at the start).  The spike is logged at
+    step n + 1, like a cell's threshold crossing."""
+    tk = step_times_f32(dt, n_steps)
+    th = (tk + F32(dt)).astype(F32)          # t_n + dt, in float
+    srcs, steps = [], []
+    for ct, gids in ext_cells.values():
+        if isinstance(ct, SpikeArrayCell):
+            times = np.sort(ms_to_us(np.asarray(ct.times, np.float64)).astype(F32))
+            idx = np.searchsorted(th, times, side="right")   # first n - 1 with T < t_n + dt
+            fire = np.unique(idx[idx < n_steps]) + 1
+        else:
+            period = F32(ct.period * 1000.0)
+            small = F32(1e-6)
+            fire = []
+            tnext = period
+            for n in range(1, n_steps + 1):
+                if F32(tnext - tk[n - 1]) < small:
+                    fire.append(n)
+                    tnext = F32(tnext + period)
+            fire = np.asarray(fire, np.int64)
+        for g in gids:
+            srcs.append(np.full(len(fire), g, np.int32))
+            steps.append(fire.astype(np.int64) + 1)
+    if not srcs:
+        return np.zeros(0, np.int32), np.zeros(0, np.int64)
+    src = np.concatenate(srcs)
+    step = np.concatenate(steps)
+    order = np.lexsort((src, step))
+    return src[order], step[order]
+
+
 def joined(parts, dtype) -> np.ndarray:
     return np.concatenate(parts).astype(dtype) if parts else np.zeros(0, dtype)
 
@@ -218,6 +266,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     chan_type, chan_g, chan_e = [], [], []
     chan_dens, phys_ra = [], []
     chan_cache, chan_count = {}, [0]
+    ext_cells = {}                         # spike-source cell type -> (type, gids)
     izh = []
     src_target = np.zeros(n_cells, np.int32)
     src_thr = np.full(n_cells, np.nan, np.float32)
@@ -267,6 +316,11 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                 phys_ra.append(float(ct.ra))
                 src_target[gid] = base  # segment 0 detects spikes
                 src_thr[gid] = _to_f32(ct.spike_thresh)
+            elif isinstance(ct, SPIKE_SOURCE_TYPES):
+                # a source with no target: its spikes are computed here
+                src_target[gid] = -1
+                gid_base[gid] = -1
+                ext_cells.setdefault(ct.name, (ct, []))[1].append(gid)
             elif isinstance(ct, Izhikevich2007Cell):
                 gid_is_izh[gid] = True
                 izh_index[gid] = len(izh)
@@ -283,8 +337,12 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     def target_of(gids, segs):
         gids = np.asarray(gids, np.int64)
         segs = np.asarray(segs, np.int64)
+        if len(gids) and (gid_base[gids] < 0).any():
+            raise ValueError("a spike source (spikeArray, spikeGenerator) has no membrane to target")
         t = gid_base[gids] + np.where(gid_is_izh[gids], 0, segs)
         return t.astype(np.int32)
+
+    ext_src, ext_step = spike_source_steps(ext_cells, dt, spec.n_steps())
 
     # ---- synapse types --------------------------------------------------------
     syn_types = np.zeros(len(spec.synapses), dtype=SYN_DTYPE)
@@ -386,13 +444,14 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         pulse_weight=np.ones(len(qt), F32),
         trace_target=trace_target, event_src=event_src, gid_target_base=gid_base,
         chan_density=joined(chan_dens, np.int32), phys_ra=np.asarray(phys_ra, np.float64),
+        ext_src=ext_src, ext_step=ext_step,
     )
 
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 1
+ABI_VERSION = 2
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -416,6 +475,7 @@ class CModel(ctypes.Structure):
         ("pois_rate", _f32p), ("pois_weight", _f32p), ("pois_src", _i32p), ("pois_instance", _i32p),
         ("n_pulse", ctypes.c_int64), ("pulse_target", _i32p), ("pulse_start", _f32p),
         ("pulse_duration", _f32p), ("pulse_amplitude", _f32p), ("pulse_weight", _f32p),
+        ("n_ext", ctypes.c_int64), ("ext_src", _i32p), ("ext_step", _i64p),
     ]
 
 
@@ -483,4 +543,7 @@ def to_cmodel(m: LoweredModel):
     cm.pulse_duration = p(m.pulse_duration, F32, _f32p)
     cm.pulse_amplitude = p(m.pulse_amplitude, F32, _f32p)
     cm.pulse_weight = p(m.pulse_weight, F32, _f32p)
+    cm.n_ext = len(m.ext_src)
+    cm.ext_src = p(m.ext_src, np.int32, _i32p)
+    cm.ext_step = p(m.ext_step, np.int64, _i64p)
     return cm, keep

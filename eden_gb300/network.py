@@ -129,6 +129,25 @@ class Izhikevich2007Cell:
     v0: float = -60.0     # mV
 
 
+@dataclass
+class SpikeArrayCell:
+    """spikeArray: a spike source with no membrane that emits spikes at the
+    listed times (ms); a step emits at most one spike."""
+    name: str
+    times: np.ndarray
+
+
+@dataclass
+class SpikeGeneratorCell:
+    """spikeGenerator: a spike source emitting every `period` ms, the first
+    one period after t = 0."""
+    name: str
+    period: float
+
+
+SPIKE_SOURCE_TYPES = (SpikeArrayCell, SpikeGeneratorCell)
+
+
 # ---------------------------------------------------------------------------
 # Synapses and inputs
 # ---------------------------------------------------------------------------
@@ -271,7 +290,8 @@ class NetworkSpec:
         total = 0
         for p in self.populations:
             ct = self.cell_type(p.cell_type)
-            total += p.size * (ct.n_seg if isinstance(ct, PhysicalCell) else 1)
+            total += p.size * (ct.n_seg if isinstance(ct, PhysicalCell) else
+                               0 if isinstance(ct, SPIKE_SOURCE_TYPES) else 1)
         return total
 
     def n_synapses(self) -> int:

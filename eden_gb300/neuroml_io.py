@@ -21,8 +21,8 @@ import numpy as np
 from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       Izhikevich2007Cell, NetworkSpec, OutputColumn,
                       PhysicalCell, PoissonInputs, Population, Projection,
-                      PulseInputs, Rate, SynapseType, RATE_TYPE_NAMES,
-                      SYN_EXPONE, SYN_EXPTWO)
+                      PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SynapseType,
+                      RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO)
 
 
 def _f(x: float) -> str:
@@ -70,7 +70,14 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
     for c in spec.cells:
         if c.name not in used_types:
             continue
-        if isinstance(c, Izhikevich2007Cell):
+        if isinstance(c, SpikeArrayCell):
+            w(f'<spikeArray id="{c.name}">')
+            for i, t in enumerate(c.times):
+                w(f'<spike id="{i}" time="{_f(t)}ms"/>')
+            w('</spikeArray>\n')
+        elif isinstance(c, SpikeGeneratorCell):
+            w(f'<spikeGenerator id="{c.name}" period="{_f(c.period)}ms"/>\n')
+        elif isinstance(c, Izhikevich2007Cell):
             w(f'<izhikevich2007Cell id="{c.name}" v0="{_f(c.v0)}mV" C="{_f(c.C)}pF" '
               f'k="{_f(c.k)}nS_per_mV" vr="{_f(c.vr)}mV" vt="{_f(c.vt)}mV" vpeak="{_f(c.vpeak)}mV" '
               f'a="{_f(c.a)}per_ms" b="{_f(c.b)}nS" c="{_f(c.c)}mV" d="{_f(c.d)}pA"/>\n')
@@ -438,6 +445,11 @@ def read_lems(path: str) -> NetworkSpec:
                 vr=_qty(e, "vr", "voltage"), vt=_qty(e, "vt", "voltage"), vpeak=_qty(e, "vpeak", "voltage"),
                 a=_qty(e, "a", "rate_per_ms"), b=_qty(e, "b", "conductance"), c=_qty(e, "c", "voltage"),
                 d=_qty(e, "d", "current") * 1e3, v0=_qty(e, "v0", "voltage"))  # d in pA
+        elif t == "spikeArray":
+            cells[e.get("id")] = SpikeArrayCell(e.get("id"),
+                                                np.array([_qty(sp, "time", "time") for sp in _children(e, "spike")]))
+        elif t == "spikeGenerator":
+            cells[e.get("id")] = SpikeGeneratorCell(e.get("id"), _qty(e, "period", "time"))
         elif t == "network" and e.get("id") == sim.get("target"):
             net = e
     for e in elems:

@@ -18,6 +18,8 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    per-instance parameters, 0.5 nA step for 150 ms;
                    dt 0.025 ms, 200 ms.
   mixed_scale      the multicomp and izhikevich populations together.
+  spike_sources    spikeArray and spikeGenerator populations driving
+                   izhikevich and single-compartment HH cells.
 
 Every generator takes scale arguments (cell count, in-degree, length) so the
 same distributions produce the small cases the CPU reference can finish.
@@ -30,8 +32,8 @@ import numpy as np
 
 from .network import (ChannelDensity, EventSelection, Izhikevich2007Cell,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
-                      Population, Projection, PulseInputs, SynapseType,
-                      SYN_EXPONE, SYN_EXPTWO, hh_channels)
+                      Population, Projection, PulseInputs, SpikeArrayCell,
+                      SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, hh_channels)
 
 # conductivities (mS/cm2) and reversal potentials (mV) of the HH cells
 G_NA, G_K, G_L = 120.0, 36.0, 0.3
@@ -259,10 +261,58 @@ def mixed_scale(n_izh: int = 160000, n_mc: int = 40000, in_degree: int = 100,
     return spec
 
 
+# ---------------------------------------------------------------------------
+def spike_sources(n_arrays: int = 6, n_generators: int = 3, n_izh: int = 12, n_hh: int = 8,
+                  fan_in: int = 6, length_ms: float = 100.0, dt_ms: float = 0.025, seed: int = 1234,
+                  n_recorded: int = 6) -> NetworkSpec:
+    """Spike sources with no membrane -- spikeArray populations (seeded
+    spike times, some on and next to step boundaries, one list unsorted) and
+    spikeGenerator populations (periods on and off the step grid) -- driving
+    izhikevich2007 and single-compartment HH cells through expTwo and expOne
+    synapses; the driven cells also connect among themselves."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("spike_sources", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=2.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+    spec.synapses.append(SynapseType("syn_e1", SYN_EXPONE, gbase=3.0, erev=0.0, tau_decay=2.0))
+    for k in range(n_arrays):
+        t = np.round(np.sort(rng.uniform(0.0, length_ms, size=rng.integers(5, 40))), 4)
+        if k == 0:   # step boundaries: on the grid, a hair before and after, and a duplicate
+            t = np.concatenate([t, [0.0, 10.0, 10.0, 9.9999, 10.0001, 20.025]])
+        if k == 1:   # listed out of order
+            t = t[::-1].copy()
+        spec.cells.append(SpikeArrayCell(f"sa{k}", t))
+        spec.populations.append(Population(f"psa{k}", f"sa{k}", int(rng.integers(1, 4))))
+    for k, period in enumerate([2.3, 3.7, 5.0, 1.025, 7.77][:n_generators]):
+        spec.cells.append(SpikeGeneratorCell(f"sg{k}", period))
+        spec.populations.append(Population(f"psg{k}", f"sg{k}", 2))
+    n_src = sum(p.size for p in spec.populations)
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    hh = PhysicalCell(name="hhcell", seg_parent=np.array([-1]), seg_len=np.array([0.0]), seg_diam=np.array([17.8]),
+                      densities=_hh_densities(1, np.ones(1, dtype=bool)), cm=1.0, ra=30.0, v0=-65.0,
+                      spike_thresh=-20.0)
+    spec.cells.append(hh)
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    n = n_src + n_izh + n_hh
+    post = np.repeat(np.arange(n_src, n), fan_in)
+    pre = rng.integers(0, n, size=post.size)
+    pre = np.where(pre == post, (pre + 1) % n, pre)
+    delay = _round_us(rng.uniform(0.5, 4.0, size=post.size))
+    w = np.round(rng.uniform(0.5, 3.0, size=post.size), 4)
+    two = rng.random(post.size) < 0.6
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre[two], post[two], "syn_e2", w[two], delay[two]))
+    spec.projections.append(_flat_projection(spec, "proj_e1", pre[~two], post[~two], "syn_e1", w[~two], delay[~two]))
+    rec = np.sort(rng.choice(np.arange(n_src, n), size=min(n_recorded, n - n_src), replace=False))
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, int(g)), 0) for g in rec]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
     "izh_net": izh_net,
     "ball_and_stick": ball_and_stick,
     "mixed_scale": mixed_scale,
+    "spike_sources": spike_sources,
 }

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 1
+#define EDEN_GPU_ABI_VERSION 2
 
 enum {
     EDEN_GPU_OK = 0,
@@ -144,6 +144,15 @@ typedef struct EdenGpuModel {
 
     /* per-target input order: within each target the reference sums channel,
      * then input (pulse, Poisson), then synapse currents (eden/Eden.cpp:6057-6060) */
+
+    /* spikes of sources with no target (src_target -1: spikeArray and
+     * spikeGenerator populations, eden/Eden.cpp:6738-6790), known in advance:
+     * source and the step at which each is logged (the step after the one
+     * that emits it), sorted by step; delivered through the fan-out like a
+     * cell's spikes */
+    int64_t n_ext;
+    const int32_t *ext_src;
+    const int64_t *ext_step;
 } EdenGpuModel;
 
 /* Execution options. */

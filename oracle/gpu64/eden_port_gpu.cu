@@ -65,6 +65,11 @@ __global__ void k_output(Port P, int cur, int64_t step, int32_t n_trace, const i
     }
 }
 
+__global__ void k_ext(Port P, int nxt, const int32_t *ext_src, int64_t e0, int64_t e1) {
+    const int64_t e = e0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < e1) send_spike(&P, nxt, ext_src[e]);
+}
+
 __global__ void k_items(Port P, int cur, int init, double t, double dt, int64_t step, int32_t n_phys, int32_t n_items) {
     const int item = blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= n_items) return;
@@ -130,6 +135,8 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         dm.pulse_duration = g.copy(m->pulse_duration, (size_t)m->n_pulse);
         dm.pulse_amplitude = g.copy(m->pulse_amplitude, (size_t)m->n_pulse);
         dm.pulse_weight = g.copy(m->pulse_weight, (size_t)m->n_pulse);
+        dm.ext_src = g.copy(m->ext_src, (size_t)m->n_ext);
+        dm.ext_step = g.copy(m->ext_step, (size_t)m->n_ext);
         // the loop's state, set up on the host
         Port D = H;
         D.m = g.copy(&dm, 1);
@@ -172,6 +179,7 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         const int64_t n_out = n_trace > m->n_src ? n_trace : m->n_src;
         const int grid_out = (int)((n_out + threads - 1) / threads);
         int cur = 0;
+        int64_t ext = 0;
         double time = 0.0;
         const double dt = m->dt;
         for (int64_t step = -3; step <= n_steps; step++) {
@@ -179,6 +187,14 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
             if (!init && grid_out > 0)
                 k_output<<<grid_out, threads>>>(D, cur, step, n_trace, d_tt, d_trace, spike_cap, d_lsrc, d_lstep, d_ln);
             if (grid_items > 0) k_items<<<grid_items, threads>>>(D, cur, init, time, dt, step, m->n_phys, n_items);
+            // the spike sources' events emitted this step
+            int64_t e1 = ext;
+            while (e1 < m->n_ext && m->ext_step[e1] <= step + 1) e1++;
+            int64_t e0 = ext;
+            while (e0 < e1 && m->ext_step[e0] < step + 1) e0++;
+            if (e1 > e0)
+                k_ext<<<(int)((e1 - e0 + threads - 1) / threads), threads>>>(D, cur ^ 1, dm.ext_src, e0, e1);
+            ext = e1;
             if (!init) time += dt;
             cur ^= 1;
         }

@@ -18,6 +18,7 @@
  *   pulseGenerator                            eden/Eden.cpp:3798-3826
  *   izhikevich2007Cell (LEMS)                 LEMS_CoreComponents.inc.xml:1140-1185, eden/Eden.cpp:6821-6914
  *   threshold crossing + spike send           eden/Eden.cpp:6247-6252, 3946-3995
+ *   spike-list / generator sources            eden/Eden.cpp:6738-6790 (their steps come with the model)
  *   trajectory / event loggers                eden/Eden.cpp:11555-11635
  *
  * Its parity with the reference itself is pinned by tests/test_oracle_vs_reference.py
@@ -485,7 +486,8 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
     }
     P.src_of_target = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nt + 1));
     for (int64_t t = 0; t < nt; t++) P.src_of_target[t] = -1;
-    for (int32_t s = 0; s < m->n_src; s++) P.src_of_target[m->src_target[s]] = s;
+    for (int32_t s = 0; s < m->n_src; s++)
+        if (m->src_target[s] >= 0) P.src_of_target[m->src_target[s]] = s;  /* -1: a spike list or generator */
     *PP = P;
 }
 
@@ -516,6 +518,7 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
     int64_t nsp = 0;
     int rc = 0;
     int64_t last_step = n_steps;  /* steps 1..n_steps are the non-init ones */
+    int64_t ext = 0;              /* next spike-source event */
     for (int64_t step = -3; step <= last_step; step++) {
         int init = step <= 0;
         if (!init) {
@@ -543,6 +546,12 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
                 phys_cell_step(&P, cur, item, init, t, dt, step);
             else
                 izh_step(&P, cur, item - m->n_phys, init, t, dt, step);
+        }
+        /* sources with no target (spike lists, generators): the spikes this
+         * step emits, logged at the next step like a cell's */
+        while (ext < m->n_ext && m->ext_step[ext] <= step + 1) {
+            if (m->ext_step[ext] == step + 1) send_spike(&P, cur ^ 1, m->ext_src[ext]);
+            ext++;
         }
         if (!init) time += dt;
         cur ^= 1;

@@ -13,6 +13,7 @@ CASES = {
     "multicomp_recurrent": ("multicomp_net", dict(n_cells=24, in_degree=20, length_ms=15.0, max_seg=80,
                                                   n_recorded=6), 1.0, None),
     "ball_and_stick": ("ball_and_stick", dict(n_inst=8, length_ms=40.0), 1.0, None),
+    "spike_sources": ("spike_sources", dict(), 1.0, None),
 }
 
 

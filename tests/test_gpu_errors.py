@@ -70,3 +70,18 @@ def test_spike_log_overflow_is_reported():
         assert e.value.code == E_RANGE and "spike" in str(e.value)
     finally:
         sim.close()
+
+
+@pytest.mark.parametrize("fault", ["source_with_target", "unsorted", "early"])
+def test_bad_spike_source_events_are_refused(fault):
+    low = lowering.lower(workloads.spike_sources(length_ms=10.0))
+    low.ext_src, low.ext_step = low.ext_src.copy(), low.ext_step.copy()
+    if fault == "source_with_target":
+        low.ext_src[0] = int(np.nonzero(low.src_target >= 0)[0][0])
+    elif fault == "unsorted":
+        low.ext_step[0] = low.ext_step[-1] + 5
+    else:
+        low.ext_step[0] = 1          # logged before any step has run
+    with pytest.raises(EdenGpuError) as e:
+        Simulation(low)
+    assert e.value.code == E_INVALID and "spike-source event" in str(e.value)
