@@ -27,7 +27,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .network import (SPIKE_SOURCE_TYPES, Izhikevich2007Cell, NetworkSpec, PhysicalCell, SpikeArrayCell,
+from .network import (SPIKE_SOURCE_TYPES, EventSetReaderCell, Izhikevich2007Cell, NetworkSpec, PhysicalCell,
+                      SpikeArrayCell,
                       SYN_EXPONE, SYN_EXPTWO)
 
 F32 = np.float32
@@ -206,6 +207,11 @@ def spike_source_steps(ext_cells: dict, dt: np.float32, n_steps: int):
     th = (tk + F32(dt)).astype(F32)          # t_n + dt, in float
     srcs, steps = [], []
     for ct, gids in ext_cells.values():
+        if isinstance(ct, EventSetReaderCell):
+            s_, k_ = event_set_steps(ct, gids, dt, n_steps)
+            srcs.append(s_)
+            steps.append(k_)
+            continue
         if isinstance(ct, SpikeArrayCell):
             times = np.sort(ms_to_us(np.asarray(ct.times, np.float64)).astype(F32))
             idx = np.searchsorted(th, times, side="right")   # first n - 1 with T < t_n + dt
@@ -229,6 +235,39 @@ def spike_source_steps(ext_cells: dict, dt: np.float32, n_steps: int):
     step = np.concatenate(steps)
     order = np.lexsort((src, step))
     return src[order], step[order]
+
+
+def event_set_steps(ct, gids, dt: np.float32, n_steps: int):
+    """(source, logging step) of an event-set reader's events
+    (eden/Eden.cpp:11760-11829).  Frames whose timestamp does not exceed the
+    last accepted one are ignored, as are negative timestamps; a frame is
+    applied in the first step n whose double time satisfies
+    timestamp < max(t_n - 1e-9 s, 0), raising its sources' trigger flags
+    before the step's work items run, so their synapses read them in that
+    same step -- in this library's terms a spike logged at step n."""
+    gids = np.asarray(gids, np.int64)
+    tn = np.concatenate([[0.0], np.add.accumulate(np.full(max(n_steps - 1, 0), float(np.float32(dt))))])[:n_steps]
+    until = np.maximum(tn - 1e-3, 0.0)           # us
+    src, step = [], []
+    last = -np.inf
+    n_ports = len(ct.ports)
+    for ts_s, pairs in ct.frames:
+        ts = ts_s * 1e6
+        if not ts > last:
+            continue
+        last = ts
+        if ts < 0 or not pairs:
+            continue
+        n = int(np.searchsorted(until, ts, side="right")) + 1   # first step with ts < until
+        if n > n_steps:
+            continue
+        for inst, port in pairs:
+            src.append(int(gids[int(inst) * n_ports + int(port)]))
+            step.append(n)
+    if not src:
+        return np.zeros(0, np.int32), np.zeros(0, np.int64)
+    pairs_ = np.unique(np.stack([np.asarray(step, np.int64), np.asarray(src, np.int64)], 1), axis=0)
+    return pairs_[:, 1].astype(np.int32), pairs_[:, 0]
 
 
 def joined(parts, dtype) -> np.ndarray:

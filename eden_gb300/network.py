@@ -145,7 +145,20 @@ class SpikeGeneratorCell:
     period: float
 
 
-SPIKE_SOURCE_TYPES = (SpikeArrayCell, SpikeGeneratorCell)
+@dataclass
+class EventSetReaderCell:
+    """EdenEventSetReader: spike events streamed from a file, one source per
+    (instance, port); `frames` are the file's lines in order, each a
+    timestamp (s) and the (instance, port) pairs it names.  A population of
+    instances * len(ports) sources, source instance * len(ports) + port."""
+    name: str
+    instances: int
+    ports: list
+    frames: list
+    href: str = "events.txt"
+
+
+SPIKE_SOURCE_TYPES = (SpikeArrayCell, SpikeGeneratorCell, EventSetReaderCell)
 
 
 # ---------------------------------------------------------------------------

@@ -22,6 +22,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       Izhikevich2007Cell, NetworkSpec, OutputColumn,
                       PhysicalCell, PoissonInputs, Population, Projection,
                       PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SynapseType,
+                      EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO)
 
 
@@ -70,6 +71,8 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
     for c in spec.cells:
         if c.name not in used_types:
             continue
+        if isinstance(c, EventSetReaderCell):
+            continue                      # written in the network
         if isinstance(c, SpikeArrayCell):
             w(f'<spikeArray id="{c.name}">')
             for i, t in enumerate(c.times):
@@ -100,8 +103,21 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
           f'spikeTarget="./{po.synapse}"/>\n')
 
     w('<network id="net">\n')
+    readers = {}
     for p in spec.populations:
+        ct = spec.cell_type(p.cell_type)
+        if isinstance(ct, EventSetReaderCell):
+            readers[p.name] = ct
+            continue
         w(f' <population id="{p.name}" component="{p.cell_type}" size="{p.size}"/>\n')
+    for name, ct in readers.items():
+        w(f' <EdenEventSetReader id="{name}" href="./{ct.href}" format="ascii_v0" instances="{ct.instances}">\n')
+        for port in ct.ports:
+            w(f'  <Port id="{port}"/>\n')
+        w(' </EdenEventSetReader>\n')
+        with open(os.path.join(dirname, ct.href), "w") as f:
+            for ts, pairs in ct.frames:
+                f.write(repr(float(ts)) + "".join(f" {i}!{q}" for i, q in pairs) + "\n")
     pop_of, local_of = _gid_maps(spec)
     for pr in spec.projections:
         # consecutive runs of one (pre, post) population pair, so the file's
@@ -117,6 +133,12 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w(f' <projection id="{pr.name}_{gi}" presynapticPopulation="{pa}" '
               f'postsynapticPopulation="{pb}" synapse="{pr.synapse}">\n')
             for n, i in enumerate(idx):
+                if pa in readers:
+                    inst, port = divmod(local_of[pr.pre_cell[i]], len(readers[pa].ports))
+                    w(f'  <connectionWD id="{n}" preCellId="{inst}" preSegmentId="{readers[pa].ports[port]}" '
+                      f'postCellId="../{pb}[{local_of[pr.post_cell[i]]}]" postSegmentId="{pr.post_seg[i]}" '
+                      f'weight="{_f(pr.weight[i])}" delay="{_f(pr.delay[i])}ms"/>\n')
+                    continue
                 w(f'  <connectionWD id="{n}" preCellId="../{pa}[{local_of[pr.pre_cell[i]]}]" '
                   f'postCellId="../{pb}[{local_of[pr.post_cell[i]]}]" postSegmentId="{pr.post_seg[i]}" '
                   f'weight="{_f(pr.weight[i])}" delay="{_f(pr.delay[i])}ms"/>\n')
@@ -374,9 +396,32 @@ def _parse_cell(el, channels_by_name):
     return cell
 
 
-def _cell_ref(text, pops):
-    """'../pop[3]', '../pop/3/celltype', 'pop[3]' or 'pop/3' -> (population, index)."""
+def read_event_set(path: str, instances: int, ports: int) -> list:
+    """An event-set file in EDEN's ascii_v0 form: per line a timestamp (s)
+    and tokens `instance` or `instance!port` (eden/Eden.cpp:10759-10826)."""
+    frames = []
+    with open(path) as f:
+        for line in f:
+            tok = line.split()
+            if not tok:
+                continue
+            pairs = []
+            for t in tok[1:]:
+                inst, _, port = t.partition("!")
+                i, p_ = int(inst), int(port or 0)
+                if not (0 <= i < instances and 0 <= p_ < ports):
+                    raise ValueError(f"{path}: event {t!r} out of range")
+                pairs.append((i, p_))
+            frames.append((float(tok[0]), pairs))
+    return frames
+
+
+def _cell_ref(text, pops, default_pop=None):
+    """'../pop[3]', '../pop/3/celltype', 'pop[3]', 'pop/3', or a bare index
+    of the projection's population -> (population, index)."""
     t = text.strip()
+    if default_pop is not None and re.fullmatch(r"\d+", t):
+        return default_pop, int(t)
     while t.startswith("../"):
         t = t[3:]
     m = re.match(r"^([^/\[\]]+)\[(\d+)\]", t)
@@ -468,10 +513,41 @@ def read_lems(path: str) -> NetworkSpec:
         size = int(p.get("size")) if p.get("size") else len(_children(p, "instance"))
         pops[p.get("id")] = Population(p.get("id"), comp, size)
         spec.populations.append(pops[p.get("id")])
+    # EDEN's event-set readers (eden/NeuroML.cpp:6455-6495): their sources
+    # follow the cells in global order, as they are no work items
+    readers = {}
+    for r in _children(net, "EdenEventSetReader"):
+        if r.get("format") != "ascii_v0":
+            raise ValueError(f"EdenEventSetReader {r.get('id')}: format {r.get('format')!r} not supported")
+        href = r.get("href") or ""
+        if href.startswith("file://"):
+            href = href[len("file://"):]
+        fpath = os.path.join(base, href)
+        if not os.path.isfile(fpath):
+            raise ValueError(f"EdenEventSetReader {r.get('id')}: {href} is not a readable file")
+        ports = [pt.get("id") for pt in _children(r, "Port")]
+        n_inst = int(r.get("instances"))
+        cell = EventSetReaderCell(r.get("id"), n_inst, ports, read_event_set(fpath, n_inst, len(ports)),
+                                  href=os.path.basename(href))
+        cells[cell.name] = cell
+        readers[cell.name] = cell
+        pops[cell.name] = Population(cell.name, cell.name, n_inst * len(ports))
+        spec.populations.append(pops[cell.name])
     used = {p.cell_type for p in spec.populations}
     spec.cells = [c for n_, c in cells.items() if n_ in used]
     off = spec.pop_offsets()
     gid = lambda pop_idx: off[pop_idx[0]] + pop_idx[1]
+
+    def pre_gid(c, pr):
+        # a connection's presynaptic source; an event-set reader's is its
+        # (instance, port), the port named by preSegmentId
+        pop = pr.get("presynapticPopulation")
+        if pop in readers:
+            ports = readers[pop].ports
+            seg = c.get("preSegmentId")
+            port = ports.index(seg) if seg in ports else int(seg or 0)
+            return off[pop] + int(c.get("preCellId")) * len(ports) + port
+        return gid(_cell_ref(c.get("preCellId"), pops, pop))
     # projections
     by_syn = {}
     for pr in _children(net, "projection"):
@@ -482,8 +558,8 @@ def read_lems(path: str) -> NetworkSpec:
         for c in pr:
             if _tag(c) not in ("connectionWD", "connection"):
                 continue
-            rows[0].append(gid(_cell_ref(c.get("preCellId"), pops)))
-            rows[1].append(gid(_cell_ref(c.get("postCellId"), pops)))
+            rows[0].append(pre_gid(c, pr))
+            rows[1].append(gid(_cell_ref(c.get("postCellId"), pops, pr.get("postsynapticPopulation"))))
             rows[2].append(int(c.get("postSegmentId", "0")))
             rows[3].append(float(c.get("weight", "1")))
             rows[4].append(_qty(c, "delay", "time", 0.0) if c.get("delay") else 0.0)

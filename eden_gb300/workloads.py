@@ -20,6 +20,8 @@ network of a stated shape from numpy's `default_rng(seed)`:
   mixed_scale      the multicomp and izhikevich populations together.
   spike_sources    spikeArray and spikeGenerator populations driving
                    izhikevich and single-compartment HH cells.
+  event_sets       an EdenEventSetReader (spike events from a file, several
+                   instances and ports) driving izhikevich and HH cells.
 
 Every generator takes scale arguments (cell count, in-degree, length) so the
 same distributions produce the small cases the CPU reference can finish.
@@ -32,7 +34,7 @@ import numpy as np
 
 from .network import (ChannelDensity, EventSelection, Izhikevich2007Cell,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
-                      Population, Projection, PulseInputs, SpikeArrayCell,
+                      Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
                       SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, hh_channels)
 
 # conductivities (mS/cm2) and reversal potentials (mV) of the HH cells
@@ -308,6 +310,53 @@ def spike_sources(n_arrays: int = 6, n_generators: int = 3, n_izh: int = 12, n_h
     return spec
 
 
+# ---------------------------------------------------------------------------
+def event_sets(n_inst: int = 3, ports=("zero", "one"), n_frames: int = 60, n_izh: int = 8, n_hh: int = 6,
+               fan_in: int = 4, length_ms: float = 60.0, dt_ms: float = 0.025, seed: int = 1234,
+               n_recorded: int = 6) -> NetworkSpec:
+    """Spike events read from a file (EDEN's EdenEventSetReader, ascii_v0)
+    driving izhikevich2007 and single-compartment HH cells, which also
+    connect among themselves.  The frames are seeded, with timestamps on
+    and next to step boundaries, a frame out of order (ignored), a negative
+    timestamp (never applied) and a repeated source within a frame."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("event_sets", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=2.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    hh = PhysicalCell(name="hhcell", seg_parent=np.array([-1]), seg_len=np.array([0.0]), seg_diam=np.array([17.8]),
+                      densities=_hh_densities(1, np.ones(1, dtype=bool)), cm=1.0, ra=30.0, v0=-65.0,
+                      spike_thresh=-20.0)
+    spec.cells.append(hh)
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    n_cells = n_izh + n_hh
+    times = np.sort(np.round(rng.uniform(0.0, length_ms * 1e-3, n_frames), 6))
+    times[:4] = [0.0, 0.001, 0.0010001, 0.00099999]
+    frames = []
+    for t in np.sort(times):
+        k = int(rng.integers(1, 4))
+        pairs = [(int(rng.integers(0, n_inst)), int(rng.integers(0, len(ports)))) for _ in range(k)]
+        frames.append((float(t), pairs))
+    frames.insert(10, (frames[5][0], [(0, 0)]))            # not after the previous frame: ignored
+    frames.insert(0, (-0.001, [(1, 1)]))                    # negative: never applied
+    frames[20] = (frames[20][0], frames[20][1] + frames[20][1][:1])   # a source twice in one frame
+    reader = EventSetReaderCell("evr", n_inst, list(ports), frames, href="evr_events.txt")
+    spec.cells.append(reader)
+    spec.populations.append(Population("evr", "evr", n_inst * len(ports)))
+    n_src = n_inst * len(ports)
+    post = np.repeat(np.arange(n_cells), fan_in)
+    from_reader = rng.random(post.size) < 0.5
+    pre = np.where(from_reader, n_cells + rng.integers(0, n_src, post.size), rng.integers(0, n_cells, post.size))
+    pre = np.where(pre == post, (pre + 1) % n_cells, pre)
+    delay = _round_us(rng.uniform(0.5, 3.0, size=post.size))
+    w = np.round(rng.uniform(1.0, 4.0, size=post.size), 4)
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre, post, "syn_e2", w, delay))
+    rec = np.sort(rng.choice(n_cells, size=min(n_recorded, n_cells), replace=False))
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, int(g)), 0) for g in rec]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n_cells)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
@@ -315,4 +364,5 @@ CONFIGS = {
     "ball_and_stick": ball_and_stick,
     "mixed_scale": mixed_scale,
     "spike_sources": spike_sources,
+    "event_sets": event_sets,
 }

@@ -26,7 +26,7 @@ def run(lems_path: str, threads: int = 1, extra=(), keep_dir=None):
     src_dir = os.path.dirname(os.path.abspath(lems_path))
     work = keep_dir or tempfile.mkdtemp(prefix="eden_ref_")
     for f in os.listdir(src_dir):
-        if f.endswith(".nml") or f.endswith(".xml"):
+        if f.endswith(".nml") or f.endswith(".xml") or f.endswith(".txt"):
             shutil.copy(os.path.join(src_dir, f), work)
     env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_SCHEDULE="static")
     p = subprocess.run([EDEN, "nml", os.path.basename(lems_path), "gcc", *extra], cwd=work,

@@ -14,6 +14,7 @@ CASES = {
                                                   n_recorded=6), 1.0, None),
     "ball_and_stick": ("ball_and_stick", dict(n_inst=8, length_ms=40.0), 1.0, None),
     "spike_sources": ("spike_sources", dict(), 1.0, None),
+    "event_sets": ("event_sets", dict(), 1.0, None),
 }
 
 

@@ -16,3 +16,11 @@ def load(name, lowered):
     # an event stamped t_n was emitted in step n and is logged at step n + 1
     step = np.rint(z["event_time_s"] / dt_s).astype(np.int64) + 1
     return trace, src, step
+
+
+def logged(src, step, lowered):
+    """The spikes of the sources the reference's event file records (an
+    event-set reader's events are delivered as spikes of its sources, which
+    the reference does not log)."""
+    keep = np.isin(np.asarray(src), lowered.event_src)
+    return np.asarray(src)[keep], np.asarray(step)[keep]

@@ -16,7 +16,7 @@ from eden_gb300 import lowering, workloads
 from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
 from criteria import box_violations, samecount
 from golden.cases import CASES, spec_of
-from golden_io import load
+from golden_io import load, logged
 from helpers import spike_trains
 
 pytestmark = pytest.mark.gpu
@@ -85,7 +85,7 @@ def test_gpu_matches_reference_outputs(name, oracle_runs):
     rec = sim.run()
     sim.close()
     dt_ms = float(low.dt) * 1e-3
-    wrong, far = samecount(spike_trains(ref_src, ref_step), spike_trains(rec.spike_src, rec.spike_step),
+    wrong, far = samecount(spike_trains(ref_src, ref_step), spike_trains(*logged(rec.spike_src, rec.spike_step, low)),
                            int(round(0.1 / dt_ms)))
     assert not wrong and not far, f"spike trains differ: counts {wrong[:5]}, timing {far[:5]}"
     nbad, worst = box_violations(ref_trace, rec.trace, dt_ms, 0.1, CASES[name][2])

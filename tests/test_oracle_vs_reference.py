@@ -14,7 +14,7 @@ import eden_port
 from criteria import box_violations, samecount
 from eden_gb300 import lowering
 from golden.cases import CASES, spec_of
-from golden_io import load
+from golden_io import load, logged
 from helpers import spike_trains
 
 
@@ -26,7 +26,7 @@ def test_oracle_matches_reference(name):
     assert out["rc"] == 0
     assert out["trace"].shape == ref_trace.shape
     dt_ms = float(low.dt) * 1e-3
-    wrong, far = samecount(spike_trains(ref_src, ref_step), spike_trains(out["spike_src"], out["spike_step"]),
+    wrong, far = samecount(spike_trains(ref_src, ref_step), spike_trains(*logged(out["spike_src"], out["spike_step"], low)),
                            int(round(0.1 / dt_ms)))
     assert not wrong, f"spike counts differ for cells {wrong[:10]}"
     assert not far, f"spikes more than 0.1 ms apart for cells {far[:10]}"

@@ -53,3 +53,37 @@ def test_a_spike_source_is_not_a_target():
     spec.event_selections = [EventSelection("p", 0, 0)]
     with pytest.raises(ValueError, match="no membrane"):
         lowering.lower(spec)
+
+
+def test_event_set_steps_match_the_reference(tmp_path):
+    # the reference run on this file, with zero-delay expTwo connections
+    # from each (instance, port) to its own izhikevich cell, fired the
+    # synapses of 0!0 in step 2, of 1!0 in step 42 and of 0!1 and 1!1 in
+    # step 82: a frame is applied in the first step whose time less 1e-9 s
+    # exceeds its timestamp, and the synapses read it in that step; the
+    # frame at 0.0019 s follows a later one and is ignored
+    from eden_gb300.network import EventSetReaderCell
+    f = tmp_path / "events.txt"
+    f.write_text("0.000000 0\n0.001000 1!0\n0.002000 0!1 1!1\n0.0019 1\n0.002512 0!0 0!1\n"
+                 "0.0025125 1!1\n0.004000 1!0\n0.004010 0\n")
+    frames = neuroml_io.read_event_set(str(f), 2, 2)
+    assert len(frames) == 8 and frames[2][1] == [(0, 1), (1, 1)]
+    reader = EventSetReaderCell("r", 2, ["zero", "one"], frames)
+    src, step = lowering.spike_source_steps({"r": (reader, [10, 11, 12, 13])}, np.float32(25.0), 321)
+    got = sorted(zip(src.tolist(), step.tolist()))
+    want = sorted([(10, 2), (12, 42), (11, 82), (13, 82), (10, 102), (11, 102), (13, 102), (12, 162), (10, 162)])
+    assert got == want
+
+
+def test_event_set_round_trip():
+    spec = workloads.event_sets(length_ms=20.0)
+    with tempfile.TemporaryDirectory() as d:
+        lems = neuroml_io.write_lems(spec, d)
+        assert os.path.exists(os.path.join(d, "evr_events.txt"))
+        back = neuroml_io.read_lems(lems)
+    a, b = lowering.lower(spec), lowering.lower(back)
+    np.testing.assert_array_equal(a.ext_src, b.ext_src)
+    np.testing.assert_array_equal(a.ext_step, b.ext_step)
+    np.testing.assert_array_equal(a.syn_src, b.syn_src)
+    # reader sources follow the cells: the cells' global ids (and RNG seeds) are unchanged
+    assert a.event_src.max() < a.ext_src.min()
