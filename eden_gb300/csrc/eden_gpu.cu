@@ -220,6 +220,15 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
     }
     int64_t nt = (int64_t)m->n_comp + m->n_izh;
     if (nt == 0) return ctx->fail(EDEN_GPU_E_INVALID, "empty network");
+    if (m->n_izh > 0 && !m->izh_params) return ctx->fail(EDEN_GPU_E_INVALID, "point-neuron parameters missing");
+    for (int k = 0; k < m->n_izh; k++) {
+        const int kind = m->izh_kind ? m->izh_kind[k] : EDEN_POINT_IZH2007;
+        if (kind < 0 || kind >= EDEN_POINT_KINDS)
+            return ctx->fail(EDEN_GPU_E_INVALID, "point neuron %d: kind %d unknown", k, kind);
+        for (int f = 0; f < EDEN_POINT_PARAMS; f++)
+            if (!std::isfinite(m->izh_params[EDEN_POINT_PARAMS * (int64_t)k + f]))
+                return ctx->fail(EDEN_GPU_E_INVALID, "point neuron %d: parameter %d not finite", k, f);
+    }
     if (m->n_src < m->n_phys + m->n_izh)
         return ctx->fail(EDEN_GPU_E_INVALID, "need one spike source per cell (n_src %d, cells %d)", m->n_src,
                          m->n_phys + m->n_izh);
@@ -573,7 +582,11 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             v0[it] = m->comp_v0[ut];
             c_chan0[it + 1] = m->comp_chan_off[ut + 1] - m->comp_chan_off[ut];
         } else {
-            v0[it] = m->izh_params[10 * (int64_t)(ut - n_comp) + 1];
+            // the value the initialisation passes give V (OnStart)
+            const int64_t uk = ut - n_comp;
+            const int kind = m->izh_kind ? m->izh_kind[uk] : EDEN_POINT_IZH2007;
+            const int f = kind == EDEN_POINT_IZH2007 ? 1 : (kind == EDEN_POINT_IAF_TAU || kind == EDEN_POINT_IAF_TAU_REF) ? 0 : 2;
+            v0[it] = m->izh_params[EDEN_POINT_PARAMS * uk + f];
         }
     }
     for (int it = 0; it < nt; it++) c_chan0[it + 1] += c_chan0[it];
@@ -670,11 +683,14 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         }
     }
 
-    // izhikevich structure of arrays, in slot (internal) order
-    std::vector<float> iz[10];
-    for (int f = 0; f < 10; f++) {
-        iz[f].resize(n_izh);
-        for (int k = 0; k < n_izh; k++) iz[f][k] = m->izh_params[10 * (int64_t)izh_user_of_slot[k] + f];
+    // point neurons: kinds and parameters (field-major) in slot (internal) order
+    std::vector<int32_t> iz_kind(n_izh);
+    std::vector<float> iz_p((size_t)EDEN_POINT_PARAMS * std::max(n_izh, 1), 0.0f);
+    for (int k = 0; k < n_izh; k++) {
+        const int64_t uk = izh_user_of_slot[k];
+        iz_kind[k] = m->izh_kind ? m->izh_kind[uk] : EDEN_POINT_IZH2007;
+        for (int f = 0; f < EDEN_POINT_PARAMS; f++)
+            iz_p[(size_t)f * n_izh + k] = m->izh_params[EDEN_POINT_PARAMS * uk + f];
     }
 
     phase("inputs-sort");
@@ -1004,9 +1020,11 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.c_chan0, c_chan0)); TRY(upload_c(ctx, &d.ch_type, ch_type));
     TRY(upload_c(ctx, &d.ch_gate0, ch_gate0)); TRY(upload_c(ctx, &d.ch_gbase, ch_g)); TRY(upload_c(ctx, &d.ch_erev, ch_e));
     TRY(upload(ctx, &d.gate, (const float *)nullptr, (size_t)n_gate));
-    const float **izp[10] = {&d.iz_C, &d.iz_v0, &d.iz_k, &d.iz_vr, &d.iz_vt, &d.iz_vpeak, &d.iz_a, &d.iz_b, &d.iz_c, &d.iz_d};
-    for (int f = 0; f < 10; f++) TRY(upload_c(ctx, izp[f], iz[f]));
+    d.n_izh = n_izh;
+    TRY(upload_c(ctx, &d.iz_kind, iz_kind));
+    TRY(upload_c(ctx, &d.iz_p, iz_p));
     TRY(upload(ctx, &d.iz_u, (const float *)nullptr, (size_t)n_izh));
+    TRY(upload(ctx, &d.iz_s, (const float *)nullptr, (size_t)n_izh));
     TRY(upload_c(ctx, &d.pu_start, pu_s)); TRY(upload_c(ctx, &d.pu_dur, pu_d));
     TRY(upload_c(ctx, &d.pu_amp, pu_a)); TRY(upload_c(ctx, &d.pu_w, pu_w));
     TRY(upload(ctx, &d.po_ts, (const float *)nullptr, (size_t)m->n_pois));
@@ -1332,8 +1350,8 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
         tmark(ctx, EDEN_KERNEL_CELLS, true);
         for (const auto &cl : ctx->classes) {
             const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->max_cell_blocks);
-            launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, d, (const WindowArgs *)ctx->d_wtab, base, idx,
-                     cl.cta_begin, cl.cta_end);
+            launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, d, (const WindowArgs *)ctx->d_wtab,
+                     (const WindowTimes *)ctx->d_wtimes, base, idx, cl.cta_begin, cl.cta_end);
             n++;
         }
         tmark(ctx, EDEN_KERNEL_CELLS, false);
@@ -1348,7 +1366,7 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
              (const WindowTimes *)ctx->d_wtimes, base, idx);
     tmark(ctx, EDEN_KERNEL_INPUTS, false);
     tmark(ctx, EDEN_KERNEL_TARGETS, true);
-    k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(d, ctx->d_wtab, base, idx);
+    k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(d, ctx->d_wtab, ctx->d_wtimes, base, idx);
     tmark(ctx, EDEN_KERNEL_TARGETS, false);
     tmark(ctx, EDEN_KERNEL_HINES, true);
     k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(d, ctx->d_wtab, base, idx, ctx->forest_cap);
@@ -1627,14 +1645,15 @@ static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const Windo
         int n = 1;
         for (const auto &cl : ctx->classes) {
             const int nb = std::min(cl.cta_end - cl.cta_begin, ctx->max_cell_blocks);
-            launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, dm, tab, zero, idx, cl.cta_begin, cl.cta_end);
+            launch_k(ctx->fn_cells, nb, kCellThreads, cl.smem, s, dm, tab, times, zero, idx, cl.cta_begin,
+                     cl.cta_end);
             n++;
         }
         launch_k(ctx->fn_deliver, ctx->grid_deliver, kThreads, 0, s, dm, tab, zero, idx);
         return n + 1;
     }
     launch_k(ctx->fn_inputs, ctx->grid_inputs, kInputThreads, 0, s, dm, tab, times, zero, idx);
-    k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(dm, tab, zero, idx);
+    k_targets_t<<<ctx->grid_targets, kThreads, 0, s>>>(dm, tab, times, zero, idx);
     k_hines_t<<<ctx->grid_hines, kHinesThreads, ctx->smem_hines, s>>>(dm, tab, zero, idx, ctx->forest_cap);
     launch_k(ctx->fn_deliver, ctx->grid_deliver, kThreads, 0, s, dm, tab, zero, idx);
     return 4;

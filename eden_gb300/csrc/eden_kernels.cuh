@@ -102,9 +102,12 @@ struct DevModel {
     const int32_t *c_chan0, *ch_type, *ch_gate0;
     const float *ch_gbase, *ch_erev;
     float *gate;
-    // izhikevich, structure of arrays
-    const float *iz_C, *iz_v0, *iz_k, *iz_vr, *iz_vt, *iz_vpeak, *iz_a, *iz_b, *iz_c, *iz_d;
-    float *iz_u;
+    // point neurons: kind, parameters field-major ([EDEN_POINT_PARAMS][n_izh]),
+    // two state variables besides V (izhikevich u, adEx w; last spike time)
+    int32_t n_izh;
+    const int32_t *iz_kind;
+    const float *iz_p;
+    float *iz_u, *iz_s;
     // input blocks: each target's pulses, then Poisson inputs and connection
     // synapses in runs of one synapse type; a block's conductance (or, for
     // pulses, current) for step k of the window is G[k * n_block + block]
@@ -207,7 +210,7 @@ __host__ __device__ inline int forest_words(int n, int nf, int nfch, int ngt, in
                                             int kcap) {
     return 7 * n + 10 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck;
 }
-__host__ __device__ inline int izh_words(int n) { return 13 * n + 1; }
+__host__ __device__ inline int izh_words(int n) { return (2 + EDEN_POINT_PARAMS + 3) * n + 1; }
 
 // Per-window arguments: the window covers steps [step0, step0 + K); steps
 // <= 0 are initialisation passes.  The previous window began at step
@@ -628,14 +631,114 @@ __device__ __forceinline__ float gate_next_p(const float *P, bool init, float dt
 }
 
 // ---------------------------------------------------------------------------
+// point neurons
+// ---------------------------------------------------------------------------
+// One step of a point neuron from its now state (V v, states u and s) with
+// external current iext (synaptic then input currents), following the LEMS
+// semantics the reference generates code from (eden/Eden.cpp:2832-2994):
+// every state is integrated by forward Euler from the now state, then, where
+// an OnCondition holds on the now state, its assignments (from now values)
+// override; the initialisation passes apply OnStart.  Parameters are read as
+// p[f * ps].  Returns whether the neuron spiked.
+__device__ __forceinline__ bool point_update(int kind, const float *p, int ps, bool init, float t, float dt,
+                                             float v, float iext, float &u, float &s, float &vn) {
+#define PP(f) p[(f) * ps]
+    bool spike = false;
+    switch (kind) {
+    case EDEN_POINT_IAF_TAU:
+    case EDEN_POINT_IAF_TAU_REF: {
+        // iafTauCell / iafTauRefCell: v' = (leakReversal - v) / tau, no synaptic input
+        const bool ref = kind == EDEN_POINT_IAF_TAU_REF;
+        if (init) {
+            vn = PP(0);
+            if (ref) s = t - PP(4);
+            break;
+        }
+        const bool active = !ref || t > s + PP(4);
+        const float rate = active ? (PP(0) - v) / PP(1) : 0.0f;
+        vn = v + dt * rate;
+        if (v > PP(2) && active) {
+            if (ref) s = t;
+            vn = PP(3);
+            spike = true;
+        }
+        break;
+    }
+    case EDEN_POINT_IAF:
+    case EDEN_POINT_IAF_REF: {
+        // iafCell / iafRefCell: iMemb = leakConductance (leakReversal - v) + iSyn, v' = iMemb / C
+        const bool ref = kind == EDEN_POINT_IAF_REF;
+        if (init) {
+            vn = PP(2);
+            if (ref) s = t - PP(5);
+            break;
+        }
+        const float imemb = PP(1) * (PP(2) - v) + iext;
+        const bool active = !ref || t > s + PP(5);
+        const float rate = active ? imemb / PP(0) : 0.0f;
+        vn = v + dt * rate;
+        if (v > PP(3) && active) {
+            if (ref) s = t;
+            vn = PP(4);
+            spike = true;
+        }
+        break;
+    }
+    case EDEN_POINT_ADEX: {
+        // adExIaFCell: iMemb = -gL (v - EL) + gL delT exp((v - VT) / delT) - w + iSyn,
+        // v' = iMemb / C outside the refractory period, w' = (a (v - EL) - w) / tauw
+        if (init) {
+            vn = PP(2);
+            u = 0.0f;
+            s = t - PP(8);
+            break;
+        }
+        const float w = u;
+        const float imemb = (-1.0f * PP(1)) * (v - PP(2)) + (PP(1) * PP(6)) * expf((v - PP(3)) / PP(6)) - w + iext;
+        const bool active = t > s + PP(8);
+        const float rate = active ? imemb / PP(0) : 0.0f;
+        vn = v + dt * rate;
+        u = w + dt * ((PP(9) * (v - PP(2)) - w) / PP(7));
+        if (v > PP(4) && active) {
+            s = t;
+            vn = PP(5);
+            u = w + PP(10);
+            spike = true;
+        }
+        break;
+    }
+    default: {
+        // izhikevich2007Cell (LEMS_CoreComponents.inc.xml:1140-1187)
+        const float uu = u, vr = PP(3);
+        const float imemb = ((PP(2) * (v - vr)) * 1e-3f) * (v - PP(4)) + iext - uu;
+        if (init) {
+            vn = PP(1);
+            u = 0.0f;
+        } else {
+            vn = v + dt * (imemb / PP(0));
+            const float du = (PP(6) * ((PP(7) * (v - vr)) - uu)) * 1e-3f;
+            u = uu + dt * du * 1e3f;
+            if (v > PP(5)) {
+                vn = PP(8);
+                u = uu + PP(9);
+                spike = true;
+            }
+        }
+    }
+    }
+#undef PP
+    return spike;
+}
+
+// ---------------------------------------------------------------------------
 // targets
 // ---------------------------------------------------------------------------
 // One target for one step: the trajectory sample, then either the channels +
 // voltage pre-update of a compartment (eden/Eden.cpp:5013-6107), writing the
 // pre-updated V to *x and the Hines diagonal to *d, or the izhikevich2007
 // update (LEMS_CoreComponents.inc.xml:1140-1185), writing v' to *x.
-__device__ __forceinline__ void target_step(const DevModel &m, int t, bool init, int64_t step, float v, float Iin,
-                                            float Gin, float Isyn, float Gsyn, float *x, float *d, int wpar) {
+__device__ __forceinline__ void target_step(const DevModel &m, int t, bool init, int64_t step, float tnow, float v,
+                                            float Iin, float Gin, float Isyn, float Gsyn, float *x, float *d, int wpar) {
     if (!init) {
         for (int k = m.t_trace0[t]; k < m.t_trace0[t + 1]; k++) {
             int64_t row = (step - 1) % m.trace_cap;
@@ -665,27 +768,11 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
         *d = 1.0f * (G / C) + m.c_inv_rc[t];
         *x = init ? v : v + (m.dt * (I + (v * G))) / C;
     } else {
-        float u = m.iz_u[iz];
-        float vr = m.iz_vr[iz];
-        float iext = Isyn + Iin;
-        float imemb = ((m.iz_k[iz] * (v - vr)) * 1e-3f) * (v - m.iz_vt[iz]) + iext - u;
-        float vn, un;
-        bool spike = false;
-        if (init) {
-            vn = m.iz_v0[iz];
-            un = 0.0f;
-        } else {
-            vn = v + m.dt * (imemb / m.iz_C[iz]);
-            float du = (m.iz_a[iz] * ((m.iz_b[iz] * (v - vr)) - u)) * 1e-3f;
-            un = u + m.dt * du * 1e3f;
-            if (v > m.iz_vpeak[iz]) {
-                vn = m.iz_c[iz];
-                un = u + m.iz_d[iz];
-                spike = true;
-            }
-        }
+        float u = m.iz_u[iz], sv = m.iz_s[iz], vn;
+        const bool spike = point_update(m.iz_kind[iz], m.iz_p + iz, m.n_izh, init, tnow, m.dt, v, Isyn + Iin, u, sv, vn);
         *x = vn;
-        m.iz_u[iz] = un;
+        m.iz_u[iz] = u;
+        m.iz_s[iz] = sv;
         int src = m.t_src[t];
         push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), wpar);
     }

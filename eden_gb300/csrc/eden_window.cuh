@@ -50,8 +50,10 @@ __global__ void __launch_bounds__(kInputThreads) k_inputs_t(DevModel m, const Wi
 }
 
 // Per-step path, phase 2: one thread per target.
-__global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs *tab, const int *base, int idx) {
+__global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs *tab, const WindowTimes *ttab,
+                                                   const int *base, int idx) {
     const WindowArgs w = tab[*base + idx];
+    const float tnow = ttab[*base + idx].tk[0];
     const bool init = w.step0 <= 0;
     const float *vin = m.v[w.par];
     float *vout = m.v[w.par ^ 1];
@@ -62,7 +64,7 @@ __global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs 
             float v = vin[i], Iin, Gin, Isyn, Gsyn;
             block_currents(m.Gp, m.t_blk0[i], m.t_blk0[i + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
                            Gsyn);
-            target_step(m, i, init, w.step0, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar);
+            target_step(m, i, init, w.step0, tnow, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar);
         }
     }
 }
@@ -297,21 +299,24 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     for (int i = lane; i < ngt; i += 32) m.gate[gt0 + i] = GT[i];
 }
 
-// A batch of up to 32 izhikevich2007Cell neurons over the window
-// (LEMS_CoreComponents.inc.xml:1140-1185), one lane each.
-__device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &w, int u, float *S) {
+// A batch of up to 32 point neurons over the window (izhikevich2007Cell,
+// iaf*Cell, adExIaFCell; point_update), one lane each.
+__device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &w, const float *tk, int u, float *S) {
     const int lane = threadIdx.x & 31;
     const int t0 = m.un_t0[u], n = m.un_t1[u] - t0;
     const int r0 = m.un_r0[u], r1 = m.un_r1[u];
-    // slice: V (two buffers), then C, v0, k, vr, vt, vpeak, a, b, c, d, u
-#define IZ(f, i) S[(2 + (f)) * n + (i)]
+    // slice: V (two buffers), the parameters (stride n), then u, s and the kind
+    float *P = S + 2 * n;
+    float *SU = P + EDEN_POINT_PARAMS * n, *SS = SU + n;
+    int32_t *KIND = (int32_t *)(SS + n);
     const int izh0 = m.t_izh[t0];
     for (int i = lane; i < n; i += 32) {
         const int iz = izh0 + i;
         S[w.par * n + i] = m.v[w.par][t0 + i];
-        IZ(0, i) = m.iz_C[iz]; IZ(1, i) = m.iz_v0[iz]; IZ(2, i) = m.iz_k[iz]; IZ(3, i) = m.iz_vr[iz];
-        IZ(4, i) = m.iz_vt[iz]; IZ(5, i) = m.iz_vpeak[iz]; IZ(6, i) = m.iz_a[iz]; IZ(7, i) = m.iz_b[iz];
-        IZ(8, i) = m.iz_c[iz]; IZ(9, i) = m.iz_d[iz]; IZ(10, i) = m.iz_u[iz];
+        for (int f = 0; f < EDEN_POINT_PARAMS; f++) P[f * n + i] = m.iz_p[(size_t)f * m.n_izh + iz];
+        SU[i] = m.iz_u[iz];
+        SS[i] = m.iz_s[iz];
+        KIND[i] = m.iz_kind[iz];
     }
     __syncwarp();
     int par = w.par;
@@ -331,25 +336,11 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
             float Iin, Gin, Isyn, Gsyn;
             block_currents(Gpk, m.t_blk0[t], m.t_blk0[t + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
                            Gsyn);
-            const float uu = IZ(10, i);
-            const float vr = IZ(3, i);
-            const float imemb = ((IZ(2, i) * (v - vr)) * 1e-3f) * (v - IZ(4, i)) + (Isyn + Iin) - uu;
-            float vn, un;
-            if (init) {
-                vn = IZ(1, i);
-                un = 0.0f;
-            } else {
-                vn = v + dt * (imemb / IZ(0, i));
-                const float du = (IZ(6, i) * ((IZ(7, i) * (v - vr)) - uu)) * 1e-3f;
-                un = uu + dt * du * 1e3f;
-                if (v > IZ(5, i)) {
-                    vn = IZ(8, i);
-                    un = uu + IZ(9, i);
-                    spike = true;
-                }
-            }
+            float uu = SU[i], ss = SS[i], vn;
+            spike = point_update(KIND[i], P + i, n, init, tk[k], dt, v, Isyn + Iin, uu, ss, vn);
             vout[i] = vn;
-            IZ(10, i) = un;
+            SU[i] = uu;
+            SS[i] = ss;
             src = m.t_src[t];
         }
         push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar);
@@ -362,25 +353,26 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
     }
     for (int i = lane; i < n; i += 32) {
         m.v[par][t0 + i] = S[par * n + i];
-        m.iz_u[izh0 + i] = IZ(10, i);
+        m.iz_u[izh0 + i] = SU[i];
+        m.iz_s[izh0 + i] = SS[i];
     }
 }
-#undef IZ
 
 // This launch runs CTAs [cta_begin, cta_end), each a few units, one per warp.
 // A block runs several CTAs in turn when there are more CTAs than blocks;
 // their units are laid out differently in shared memory, so every warp of
 // the block finishes its unit before any starts on the next CTA.
-__global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const WindowArgs *tab, const int *base, int idx,
-                                                          int cta_begin, int cta_end) {
+__global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const WindowArgs *tab, const WindowTimes *ttab,
+                                                          const int *base, int idx, int cta_begin, int cta_end) {
     extern __shared__ float sm[];
     const WindowArgs w = tab[*base + idx];
+    const float *tk = ttab[*base + idx].tk;
     const int warp = threadIdx.x >> 5;
     for (int cta = cta_begin + blockIdx.x; cta < cta_end; cta += gridDim.x) {
         const int u = m.cta_u0[cta] + warp;
         if (u < m.cta_u0[cta + 1]) {
             if (m.un_f[u] >= 0) { if (EDEN_KIND_FOREST) forest_window(m, w, u, sm + m.un_off[u]); }
-            else if (EDEN_KIND_IZH) izh_window(m, w, u, sm + m.un_off[u]);
+            else if (EDEN_KIND_IZH) izh_window(m, w, tk, u, sm + m.un_off[u]);
         }
         if (cta + (int)gridDim.x < cta_end) __syncthreads();
     }

@@ -27,8 +27,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .network import (SPIKE_SOURCE_TYPES, EventSetReaderCell, Izhikevich2007Cell, NetworkSpec, PhysicalCell,
-                      SpikeArrayCell,
+from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, IafCell, Izhikevich2007Cell, NetworkSpec,
+                      PhysicalCell, SpikeArrayCell,
                       SYN_EXPONE, SYN_EXPTWO)
 
 F32 = np.float32
@@ -90,7 +90,7 @@ class LoweredModel:
     chan_gbase: np.ndarray
     chan_erev: np.ndarray
     # point neurons
-    izh_params: np.ndarray        # [n_izh, 10]
+    izh_params: np.ndarray        # [n_izh, POINT_PARAMS] point-neuron parameters, engine units
     # spike sources (one per gid)
     src_target: np.ndarray
     src_threshold: np.ndarray
@@ -124,6 +124,7 @@ class LoweredModel:
     # spikes of the sources with no target, (source, logging step), in step order
     ext_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     ext_step: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
+    izh_kind: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))  # POINT_* per point neuron
     phys_ra: np.ndarray = field(default=None)          # physical cell -> axial resistivity, ohm*cm
 
     @property
@@ -185,6 +186,32 @@ def _cable_geometry(cell: PhysicalCell):
         inv_rc[ci] = (1.0 / (r64 * c[ci].astype(np.float64))).astype(F32)
         np.add.at(inv_rc, pi, (1.0 / (r64 * c[pi].astype(np.float64))).astype(F32))
     return c, r_axial, area, inv_rc
+
+
+# point-neuron kinds and parameter layout (include/eden_gpu.h, EDEN_POINT_*)
+POINT_PARAMS = 16
+POINT_IZH2007, POINT_IAF_TAU, POINT_IAF_TAU_REF, POINT_IAF, POINT_IAF_REF, POINT_ADEX = range(6)
+_IAF_KINDS = {"iafTauCell": POINT_IAF_TAU, "iafTauRefCell": POINT_IAF_TAU_REF, "iafCell": POINT_IAF,
+              "iafRefCell": POINT_IAF_REF}
+
+
+def point_params(ct):
+    """(kind, parameters in engine units: pF, uS, mV, us, nA) of a point neuron."""
+    if isinstance(ct, Izhikevich2007Cell):
+        return POINT_IZH2007, [ct.C, ct.v0, ct.k, ct.vr, ct.vt, ct.vpeak, ct.a * 1e-3, ct.b * 1e-3, ct.c, ct.d * 1e-3]
+    if isinstance(ct, IafCell):
+        kind = _IAF_KINDS[ct.kind]
+        if kind in (POINT_IAF_TAU, POINT_IAF_TAU_REF):
+            p = [ct.leak_reversal, ct.tau * 1e3, ct.thresh, ct.reset]
+        else:
+            p = [ct.C, ct.leak_conductance * 1e-3, ct.leak_reversal, ct.thresh, ct.reset]
+        if kind in (POINT_IAF_TAU_REF, POINT_IAF_REF):
+            p.append(ct.refract * 1e3)
+        return kind, p
+    if isinstance(ct, AdExCell):
+        return POINT_ADEX, [ct.C, ct.gL * 1e-3, ct.EL, ct.VT, ct.thresh, ct.reset, ct.delT, ct.tauw * 1e3,
+                            ct.refract * 1e3, ct.a * 1e-3, ct.b]
+    raise ValueError(f"not a point neuron: {type(ct).__name__}")
 
 
 def step_times_f32(dt: np.float32, n_steps: int) -> np.ndarray:
@@ -305,6 +332,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     chan_type, chan_g, chan_e = [], [], []
     chan_dens, phys_ra = [], []
     chan_cache, chan_count = {}, [0]
+    izh_kind = []
     ext_cells = {}                         # spike-source cell type -> (type, gids)
     izh = []
     src_target = np.zeros(n_cells, np.int32)
@@ -312,6 +340,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     gid_base = np.zeros(n_cells, np.int64)
     gid_is_izh = np.zeros(n_cells, bool)
     izh_index = np.full(n_cells, -1, np.int64)
+    no_current = np.zeros(n_cells, bool)
     geom_cache = {}
     gid = 0
     for pop in spec.populations:
@@ -360,11 +389,13 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                 src_target[gid] = -1
                 gid_base[gid] = -1
                 ext_cells.setdefault(ct.name, (ct, []))[1].append(gid)
-            elif isinstance(ct, Izhikevich2007Cell):
+            elif isinstance(ct, (Izhikevich2007Cell, IafCell, AdExCell)):
                 gid_is_izh[gid] = True
                 izh_index[gid] = len(izh)
-                izh.append([ct.C, ct.v0, ct.k, ct.vr, ct.vt, ct.vpeak,
-                            ct.a * 1e-3, ct.b * 1e-3, ct.c, ct.d * 1e-3])
+                kind, params = point_params(ct)
+                no_current[gid] = kind in (POINT_IAF_TAU, POINT_IAF_TAU_REF)
+                izh.append(params + [0.0] * (POINT_PARAMS - len(params)))
+                izh_kind.append(kind)
             else:
                 raise ValueError(f"unsupported cell type {type(ct).__name__}")
             gid += 1
@@ -373,11 +404,13 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         gid_base[g] = n_comp + izh_index[g]
         src_target[g] = n_comp + izh_index[g]
 
-    def target_of(gids, segs):
+    def target_of(gids, segs, current=True):
         gids = np.asarray(gids, np.int64)
         segs = np.asarray(segs, np.int64)
         if len(gids) and (gid_base[gids] < 0).any():
             raise ValueError("a spike source (spikeArray, spikeGenerator) has no membrane to target")
+        if current and len(gids) and no_current[gids].any():
+            raise ValueError("iafTauCell and iafTauRefCell do not receive current (synapses or inputs)")
         t = gid_base[gids] + np.where(gid_is_izh[gids], 0, segs)
         return t.astype(np.int32)
 
@@ -456,11 +489,11 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         perm = np.argsort(qt, kind="stable")
         qt, qs, qd, qa = qt[perm], qs[perm], qd[perm], qa[perm]
 
-    trace_target = np.array([target_of([gid_off[c.pop] + c.cell], [c.seg])[0]
+    trace_target = np.array([target_of([gid_off[c.pop] + c.cell], [c.seg], current=False)[0]
                              for c in spec.trace_columns], dtype=np.int32)
     event_src = np.array([gid_off[e.pop] + e.cell for e in spec.event_selections], dtype=np.int32)
 
-    izh_arr = np.asarray(izh, np.float64).astype(F32).reshape(-1, 10)
+    izh_arr = np.asarray(izh, np.float64).astype(F32).reshape(-1, POINT_PARAMS)
 
     return LoweredModel(
         dt=dt, seed=int(spec.seed), n_steps=spec.n_steps(),
@@ -483,14 +516,14 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         pulse_weight=np.ones(len(qt), F32),
         trace_target=trace_target, event_src=event_src, gid_target_base=gid_base,
         chan_density=joined(chan_dens, np.int32), phys_ra=np.asarray(phys_ra, np.float64),
-        ext_src=ext_src, ext_step=ext_step,
+        ext_src=ext_src, ext_step=ext_step, izh_kind=np.asarray(izh_kind, np.int32),
     )
 
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 2
+ABI_VERSION = 3
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -515,6 +548,7 @@ class CModel(ctypes.Structure):
         ("n_pulse", ctypes.c_int64), ("pulse_target", _i32p), ("pulse_start", _f32p),
         ("pulse_duration", _f32p), ("pulse_amplitude", _f32p), ("pulse_weight", _f32p),
         ("n_ext", ctypes.c_int64), ("ext_src", _i32p), ("ext_step", _i64p),
+        ("izh_kind", _i32p),
     ]
 
 
@@ -585,4 +619,6 @@ def to_cmodel(m: LoweredModel):
     cm.n_ext = len(m.ext_src)
     cm.ext_src = p(m.ext_src, np.int32, _i32p)
     cm.ext_step = p(m.ext_step, np.int64, _i64p)
+    cm.izh_kind = p(m.izh_kind if m.izh_kind is not None and len(m.izh_kind) == m.n_izh
+                    else np.zeros(m.n_izh, np.int32), np.int32, _i32p)
     return cm, keep

@@ -130,6 +130,39 @@ class Izhikevich2007Cell:
 
 
 @dataclass
+class IafCell:
+    """iafTauCell, iafTauRefCell, iafCell or iafRefCell (`kind`), NeuroML
+    units: mV, ms, nS, pF.  The *Tau* kinds have no capacitance, leak
+    conductance or synaptic input; the *Ref* kinds a refractory period."""
+    name: str
+    kind: str                  # "iafTauCell", "iafTauRefCell", "iafCell", "iafRefCell"
+    leak_reversal: float
+    thresh: float
+    reset: float
+    tau: float = 0.0           # ms (Tau kinds)
+    C: float = 0.0             # pF (iafCell, iafRefCell)
+    leak_conductance: float = 0.0   # nS
+    refract: float = 0.0       # ms (Ref kinds)
+
+
+@dataclass
+class AdExCell:
+    """adExIaFCell (Brette and Gerstner 2005), NeuroML units: pF, nS, mV, ms, nA."""
+    name: str
+    C: float
+    gL: float
+    EL: float
+    VT: float
+    thresh: float
+    reset: float
+    delT: float
+    tauw: float
+    refract: float
+    a: float
+    b: float
+
+
+@dataclass
 class SpikeArrayCell:
     """spikeArray: a spike source with no membrane that emits spikes at the
     listed times (ms); a step emits at most one spike."""

@@ -23,7 +23,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       PhysicalCell, PoissonInputs, Population, Projection,
                       PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SynapseType,
                       EventSetReaderCell,
-                      RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO)
+                      RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, AdExCell, IafCell)
 
 
 def _f(x: float) -> str:
@@ -80,6 +80,20 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w('</spikeArray>\n')
         elif isinstance(c, SpikeGeneratorCell):
             w(f'<spikeGenerator id="{c.name}" period="{_f(c.period)}ms"/>\n')
+        elif isinstance(c, IafCell):
+            extra = ""
+            if c.kind in ("iafTauCell", "iafTauRefCell"):
+                extra += f' tau="{_f(c.tau)}ms"'
+            else:
+                extra += f' C="{_f(c.C)}pF" leakConductance="{_f(c.leak_conductance)}nS"'
+            if c.kind.endswith("RefCell"):
+                extra += f' refract="{_f(c.refract)}ms"'
+            w(f'<{c.kind} id="{c.name}" leakReversal="{_f(c.leak_reversal)}mV" thresh="{_f(c.thresh)}mV" '
+              f'reset="{_f(c.reset)}mV"{extra}/>\n')
+        elif isinstance(c, AdExCell):
+            w(f'<adExIaFCell id="{c.name}" C="{_f(c.C)}pF" gL="{_f(c.gL)}nS" EL="{_f(c.EL)}mV" VT="{_f(c.VT)}mV" '
+              f'thresh="{_f(c.thresh)}mV" reset="{_f(c.reset)}mV" delT="{_f(c.delT)}mV" tauw="{_f(c.tauw)}ms" '
+              f'refract="{_f(c.refract)}ms" a="{_f(c.a)}nS" b="{_f(c.b)}nA"/>\n')
         elif isinstance(c, Izhikevich2007Cell):
             w(f'<izhikevich2007Cell id="{c.name}" v0="{_f(c.v0)}mV" C="{_f(c.C)}pF" '
               f'k="{_f(c.k)}nS_per_mV" vr="{_f(c.vr)}mV" vt="{_f(c.vt)}mV" vpeak="{_f(c.vpeak)}mV" '
@@ -490,6 +504,21 @@ def read_lems(path: str) -> NetworkSpec:
                 vr=_qty(e, "vr", "voltage"), vt=_qty(e, "vt", "voltage"), vpeak=_qty(e, "vpeak", "voltage"),
                 a=_qty(e, "a", "rate_per_ms"), b=_qty(e, "b", "conductance"), c=_qty(e, "c", "voltage"),
                 d=_qty(e, "d", "current") * 1e3, v0=_qty(e, "v0", "voltage"))  # d in pA
+        elif t in ("iafTauCell", "iafTauRefCell", "iafCell", "iafRefCell"):
+            tau_kind = t.startswith("iafTau")
+            cells[e.get("id")] = IafCell(
+                e.get("id"), t, _qty(e, "leakReversal", "voltage"), _qty(e, "thresh", "voltage"),
+                _qty(e, "reset", "voltage"),
+                tau=_qty(e, "tau", "time") if tau_kind else 0.0,
+                C=0.0 if tau_kind else _qty(e, "C", "capacitance"),
+                leak_conductance=0.0 if tau_kind else _qty(e, "leakConductance", "conductance"),
+                refract=_qty(e, "refract", "time") if t.endswith("RefCell") else 0.0)
+        elif t == "adExIaFCell":
+            cells[e.get("id")] = AdExCell(
+                e.get("id"), C=_qty(e, "C", "capacitance"), gL=_qty(e, "gL", "conductance"),
+                EL=_qty(e, "EL", "voltage"), VT=_qty(e, "VT", "voltage"), thresh=_qty(e, "thresh", "voltage"),
+                reset=_qty(e, "reset", "voltage"), delT=_qty(e, "delT", "voltage"), tauw=_qty(e, "tauw", "time"),
+                refract=_qty(e, "refract", "time"), a=_qty(e, "a", "conductance"), b=_qty(e, "b", "current"))
         elif t == "spikeArray":
             cells[e.get("id")] = SpikeArrayCell(e.get("id"),
                                                 np.array([_qty(sp, "time", "time") for sp in _children(e, "spike")]))

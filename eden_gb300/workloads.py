@@ -22,6 +22,8 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    izhikevich and single-compartment HH cells.
   event_sets       an EdenEventSetReader (spike events from a file, several
                    instances and ports) driving izhikevich and HH cells.
+  point_neurons    iafTau, iafTauRef, iaf, iafRef and adExIaF cells with DC
+                   pulses and recurrent expTwo / expOne synapses.
 
 Every generator takes scale arguments (cell count, in-degree, length) so the
 same distributions produce the small cases the CPU reference can finish.
@@ -32,7 +34,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .network import (ChannelDensity, EventSelection, Izhikevich2007Cell,
+from .network import (AdExCell, ChannelDensity, EventSelection, IafCell, Izhikevich2007Cell,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
                       SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, hh_channels)
@@ -357,6 +359,51 @@ def event_sets(n_inst: int = 3, ports=("zero", "one"), n_frames: int = 60, n_izh
     return spec
 
 
+# ---------------------------------------------------------------------------
+def point_neurons(n_per_kind: int = 8, fan_in: int = 6, length_ms: float = 100.0, dt_ms: float = 0.025,
+                  seed: int = 1234, n_recorded: int = 10) -> NetworkSpec:
+    """One population of each of iafTauCell, iafTauRefCell, iafCell,
+    iafRefCell and adExIaFCell (seeded parameters around the NeuroML
+    examples'), a DC pulse into every cell that takes current and recurrent
+    expTwo (excitatory) and expOne (inhibitory) synapses onto them; the Tau
+    kinds take no input (they start at their leak reversal, above threshold,
+    and fire periodically) but drive the others."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("point_neurons", dt_ms, length_ms, seed)
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=2.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+    spec.synapses.append(SynapseType("syn_i1", SYN_EXPONE, gbase=2.0, erev=-80.0, tau_decay=3.0))
+    r = lambda lo, hi: float(np.round(rng.uniform(lo, hi), 4))
+    spec.cells.append(IafCell("iafTau", "iafTauCell", leak_reversal=-50.0, thresh=-55.0, reset=-70.0,
+                              tau=r(20.0, 40.0)))
+    spec.cells.append(IafCell("iafTauRef", "iafTauRefCell", leak_reversal=-50.0, thresh=-55.0, reset=-70.0,
+                              tau=r(20.0, 40.0), refract=r(3.0, 7.0)))
+    spec.cells.append(IafCell("iaf", "iafCell", leak_reversal=-70.0, thresh=-55.0, reset=-70.0, C=r(0.8, 1.2) * 1e3,
+                              leak_conductance=r(40.0, 60.0)))
+    spec.cells.append(IafCell("iafRef", "iafRefCell", leak_reversal=-70.0, thresh=-55.0, reset=-70.0,
+                              C=r(0.8, 1.2) * 1e3, leak_conductance=r(40.0, 60.0), refract=r(3.0, 7.0)))
+    spec.cells.append(AdExCell("adEx", C=281.0, gL=30.0, EL=-70.6, VT=-50.4, thresh=-40.4, reset=-48.5, delT=2.0,
+                               tauw=40.0, refract=r(0.0, 1.0), a=4.0, b=0.08))
+    for c in spec.cells:
+        spec.populations.append(Population(f"p_{c.name}", c.name, n_per_kind))
+    n = n_per_kind * len(spec.cells)
+    driven = np.arange(2 * n_per_kind, n)          # the Tau kinds receive no current
+    amp = np.round(rng.uniform(0.4, 1.2, len(driven)), 4)
+    spec.pulses.append(PulseInputs("*", driven, np.zeros(len(driven), int), np.full(len(driven), 5.0),
+                                   np.full(len(driven), length_ms - 20.0), amp))
+    post = np.repeat(driven, fan_in)
+    pre = rng.integers(0, n, size=post.size)
+    pre = np.where(pre == post, (pre + 1) % n, pre)
+    delay = _round_us(rng.uniform(0.5, 3.0, size=post.size))
+    w = np.round(rng.uniform(0.5, 2.0, size=post.size), 4)
+    exc = rng.random(post.size) < 0.75
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre[exc], post[exc], "syn_e2", w[exc], delay[exc]))
+    spec.projections.append(_flat_projection(spec, "proj_i1", pre[~exc], post[~exc], "syn_i1", w[~exc], delay[~exc]))
+    rec = np.sort(rng.choice(n, size=min(n_recorded, n), replace=False))
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, int(g)), 0) for g in rec]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
@@ -365,4 +412,5 @@ CONFIGS = {
     "mixed_scale": mixed_scale,
     "spike_sources": spike_sources,
     "event_sets": event_sets,
+    "point_neurons": point_neurons,
 }

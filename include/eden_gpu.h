@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 2
+#define EDEN_GPU_ABI_VERSION 3
 
 enum {
     EDEN_GPU_OK = 0,
@@ -49,6 +49,20 @@ enum {
 };
 
 #define EDEN_MAX_GATES 4
+
+/* Point-neuron kinds (LEMS_CoreComponents.inc.xml: izhikevich2007Cell
+ * 1140-1187, iafTauCell 957-983, iafTauRefCell 985-1021, iafCell 1023-1056,
+ * iafRefCell 1058-1095, adExIaFCell 1189-1240). */
+enum {
+    EDEN_POINT_IZH2007 = 0,
+    EDEN_POINT_IAF_TAU = 1,
+    EDEN_POINT_IAF_TAU_REF = 2,
+    EDEN_POINT_IAF = 3,
+    EDEN_POINT_IAF_REF = 4,
+    EDEN_POINT_ADEX = 5,
+    EDEN_POINT_KINDS = 6
+};
+#define EDEN_POINT_PARAMS 16
 
 /* One ionChannelHH type: up to EDEN_MAX_GATES gateHHrates, each contributing
  * q^instances to the open fraction (eden/Eden.cpp:5678-5717). Rates in 1/us. */
@@ -77,7 +91,8 @@ typedef struct EdenGpuSynapseType {
  * The lowered network.  "Targets" are the places a membrane potential lives:
  * targets [0, n_comp) are the compartments of physical cells (cell by cell,
  * each cell's compartments in the reference's compartment order), targets
- * [n_comp, n_comp + n_izh) are izhikevich2007Cell point neurons.
+ * [n_comp, n_comp + n_izh) are point neurons (izhikevich2007Cell, iaf*Cell,
+ * adExIaFCell).
  * Every array is host memory, read during edenGpuCreate only.
  */
 typedef struct EdenGpuModel {
@@ -104,9 +119,16 @@ typedef struct EdenGpuModel {
     const float *chan_gbase;        /* [n_chan] conductivity, mS/cm2 */
     const float *chan_erev;         /* [n_chan] mV */
 
-    /* izhikevich2007Cell point neurons, engine units (eden/Eden.cpp:6821-6914):
-     * params[10*i + k], k = C pF, v0 mV, k nS/mV, vr, vt, vpeak mV,
-     *                        a 1/us, b uS, c mV, d nA */
+    /* point neurons (the reference's LEMS-defined artificial cells,
+     * eden/Eden.cpp:6821-6914), one kind each (izh_kind, EDEN_POINT_*),
+     * parameters in engine units at izh_params[EDEN_POINT_PARAMS * i + k]:
+     *   IZH2007      C pF, v0 mV, k nS/mV, vr, vt, vpeak mV, a 1/us, b uS, c mV, d nA
+     *   IAF_TAU      leakReversal mV, tau us, thresh, reset mV
+     *   IAF_TAU_REF  leakReversal mV, tau us, thresh, reset mV, refract us
+     *   IAF          C pF, leakConductance uS, leakReversal, thresh, reset mV
+     *   IAF_REF      C pF, leakConductance uS, leakReversal, thresh, reset mV, refract us
+     *   ADEX         C pF, gL uS, EL, VT, thresh, reset, delT mV, tauw us, refract us,
+     *                a uS, b nA */
     int32_t n_izh;
     const float *izh_params;
 
@@ -153,6 +175,8 @@ typedef struct EdenGpuModel {
     int64_t n_ext;
     const int32_t *ext_src;
     const int64_t *ext_step;
+
+    const int32_t *izh_kind;        /* [n_izh] EDEN_POINT_* of each point neuron */
 } EdenGpuModel;
 
 /* Execution options. */

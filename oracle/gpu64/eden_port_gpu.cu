@@ -114,7 +114,8 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         dm.chan_type = g.copy(m->chan_type, (size_t)n_chan);
         dm.chan_gbase = g.copy(m->chan_gbase, (size_t)n_chan);
         dm.chan_erev = g.copy(m->chan_erev, (size_t)n_chan);
-        dm.izh_params = g.copy(m->izh_params, (size_t)m->n_izh * 10);
+        dm.izh_params = g.copy(m->izh_params, (size_t)m->n_izh * EDEN_POINT_PARAMS);
+        dm.izh_kind = m->izh_kind ? g.copy(m->izh_kind, (size_t)m->n_izh) : nullptr;
         dm.src_target = g.copy(m->src_target, (size_t)m->n_src);
         dm.src_threshold = g.copy(m->src_threshold, (size_t)m->n_src);
         dm.src_cell_seed = g.copy(m->src_cell_seed, (size_t)m->n_src);
@@ -144,6 +145,7 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
             D.v[b] = g.copy(H.v[b], (size_t)nt + 1);
             D.gate[b] = g.copy(H.gate[b], (size_t)n_gate + 1);
             D.izh_u[b] = g.copy(H.izh_u[b], (size_t)m->n_izh + 1);
+            D.izh_s[b] = g.copy(H.izh_s[b], (size_t)m->n_izh + 1);
             D.syn_a[b] = g.copy(H.syn_a[b], (size_t)ns + 1);
             D.syn_b[b] = g.copy(H.syn_b[b], (size_t)ns + 1);
             D.syn_pend[b] = g.copy(H.syn_pend[b], (size_t)ns + 1);

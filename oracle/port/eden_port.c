@@ -16,7 +16,8 @@
  *   expTwoSynapse (LEMS, forward Euler)       LEMS_CoreComponents.inc.xml:145-180, eden/Eden.cpp:2832-2994
  *   poissonFiringSynapse + randof hash RNG    LEMS_CoreComponents.inc.xml:623-672, eden/Eden.cpp:3199-3233, 3873-3912
  *   pulseGenerator                            eden/Eden.cpp:3798-3826
- *   izhikevich2007Cell (LEMS)                 LEMS_CoreComponents.inc.xml:1140-1185, eden/Eden.cpp:6821-6914
+ *   point neurons (LEMS): izhikevich2007Cell, iafTauCell, iafTauRefCell,
+ *   iafCell, iafRefCell, adExIaFCell          LEMS_CoreComponents.inc.xml:957-1240, eden/Eden.cpp:6821-6914
  *   threshold crossing + spike send           eden/Eden.cpp:6247-6252, 3946-3995
  *   spike-list / generator sources            eden/Eden.cpp:6738-6790 (their steps come with the model)
  *   trajectory / event loggers                eden/Eden.cpp:11555-11635
@@ -93,7 +94,7 @@ typedef struct {
     const EdenGpuModel *m;
     int64_t n_target;
     /* double-buffered state */
-    real *v[2], *gate[2], *izh_u[2];
+    real *v[2], *gate[2], *izh_u[2], *izh_s[2];
     real *syn_a[2], *syn_b[2], *syn_pend[2];
     unsigned char *trig[2];
     real *pois_ts[2], *pois_isi[2], *pois_a[2], *pois_b[2];
@@ -390,36 +391,101 @@ static PORT_FN void phys_cell_step(Port *P, int cur, int32_t cell, int init, rea
     }
 }
 
+/* A point neuron for one step (LEMS_CoreComponents.inc.xml: izhikevich2007Cell
+ * 1140-1187, iafTauCell 957-983, iafTauRefCell 985-1021, iafCell 1023-1056,
+ * iafRefCell 1058-1095, adExIaFCell 1189-1240), with the semantics of the
+ * reference's LEMS code (eden/Eden.cpp:2832-2994): forward Euler from the now
+ * state, OnCondition assignments (from now values) overriding, OnStart in the
+ * initialisation passes.  State u is izhikevich u / adEx w, s the last spike
+ * time. */
 static PORT_FN void izh_step(Port *P, int cur, int32_t k, int init, real t, real dt, int64_t step) {
     const EdenGpuModel *m = P->m;
     int nxt = cur ^ 1;
     int64_t tgt = (int64_t)m->n_comp + k;
-    const float *p = m->izh_params + 10 * (int64_t)k;
-    real C = p[0], v0 = p[1], kk = p[2], vr = p[3], vt = p[4], vpeak = p[5];
-    real a = p[6], b = p[7], c = p[8], d = p[9];
-    real v = P->v[cur][tgt], u = P->izh_u[cur][k];
+    const float *p = m->izh_params + EDEN_POINT_PARAMS * (int64_t)k;
+    int kind = m->izh_kind ? m->izh_kind[k] : EDEN_POINT_IZH2007;
+    real v = P->v[cur][tgt], u = P->izh_u[cur][k], s = P->izh_s[cur][k];
     real Iin, Gin, Isyn, Gsyn;
     target_currents(P, cur, tgt, init, t, dt, step, v, &Iin, &Gin, &Isyn, &Gsyn);
     real iext = Isyn + Iin;
-    real iMemb = ((kk * (v - vr)) * R(1e-3)) * (v - vt) + iext - u;
-    real vn, un;
+    real vn = v, un = u, sn = s;
     int spike = 0;
-    if (init) {
-        vn = v0;
-        un = R(0.0);
-    } else {
-        real dv = iMemb / C;
-        vn = v + dt * dv;
-        real du = (a * ((b * (v - vr)) - u)) * R(1e-3);
-        un = u + dt * du * R(1e3);
-        if (v > vpeak) {
-            vn = c;
-            un = u + d;
-            spike = 1;
+    if (kind == EDEN_POINT_IZH2007) {
+        real C = p[0], v0 = p[1], kk = p[2], vr = p[3], vt = p[4], vpeak = p[5];
+        real a = p[6], b = p[7], c = p[8], d = p[9];
+        real iMemb = ((kk * (v - vr)) * R(1e-3)) * (v - vt) + iext - u;
+        if (init) {
+            vn = v0;
+            un = R(0.0);
+        } else {
+            real dv = iMemb / C;
+            vn = v + dt * dv;
+            real du = (a * ((b * (v - vr)) - u)) * R(1e-3);
+            un = u + dt * du * R(1e3);
+            if (v > vpeak) {
+                vn = c;
+                un = u + d;
+                spike = 1;
+            }
+        }
+    } else if (kind == EDEN_POINT_IAF_TAU || kind == EDEN_POINT_IAF_TAU_REF) {
+        /* no synaptic current: v' = (leakReversal - v) / tau */
+        int ref = kind == EDEN_POINT_IAF_TAU_REF;
+        real EL = p[0], tau = p[1], thresh = p[2], reset = p[3], refract = ref ? p[4] : R(0.0);
+        if (init) {
+            vn = EL;
+            if (ref) sn = t - refract;
+        } else {
+            int active = !ref || t > s + refract;
+            real rate = active ? (EL - v) / tau : R(0.0);
+            vn = v + dt * rate;
+            if (v > thresh && active) {
+                if (ref) sn = t;
+                vn = reset;
+                spike = 1;
+            }
+        }
+    } else if (kind == EDEN_POINT_IAF || kind == EDEN_POINT_IAF_REF) {
+        int ref = kind == EDEN_POINT_IAF_REF;
+        real C = p[0], gL = p[1], EL = p[2], thresh = p[3], reset = p[4], refract = ref ? p[5] : R(0.0);
+        if (init) {
+            vn = EL;
+            if (ref) sn = t - refract;
+        } else {
+            real iMemb = gL * (EL - v) + iext;
+            int active = !ref || t > s + refract;
+            real rate = active ? iMemb / C : R(0.0);
+            vn = v + dt * rate;
+            if (v > thresh && active) {
+                if (ref) sn = t;
+                vn = reset;
+                spike = 1;
+            }
+        }
+    } else { /* EDEN_POINT_ADEX */
+        real C = p[0], gL = p[1], EL = p[2], VT = p[3], thresh = p[4], reset = p[5];
+        real delT = p[6], tauw = p[7], refract = p[8], a = p[9], b = p[10];
+        if (init) {
+            vn = EL;
+            un = R(0.0);
+            sn = t - refract;
+        } else {
+            real iMemb = (R(-1.0) * gL) * (v - EL) + (gL * delT) * EXP((v - VT) / delT) - u + iext;
+            int active = t > s + refract;
+            real rate = active ? iMemb / C : R(0.0);
+            vn = v + dt * rate;
+            un = u + dt * ((a * (v - EL) - u) / tauw);
+            if (v > thresh && active) {
+                sn = t;
+                vn = reset;
+                un = u + b;
+                spike = 1;
+            }
         }
     }
     P->v[nxt][tgt] = vn;
     P->izh_u[nxt][k] = un;
+    P->izh_s[nxt][k] = sn;
     int32_t src = P->src_of_target[tgt];
     if (spike && src >= 0) send_spike(P, nxt, src);
 }
@@ -448,6 +514,7 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
         P.v[b] = (real *)calloc((size_t)nt + 1, sizeof(real));
         P.gate[b] = (real *)calloc((size_t)n_gate + 1, sizeof(real));
         P.izh_u[b] = (real *)calloc((size_t)m->n_izh + 1, sizeof(real));
+        P.izh_s[b] = (real *)calloc((size_t)m->n_izh + 1, sizeof(real));
         P.syn_a[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
         P.syn_b[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
         P.syn_pend[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
@@ -463,7 +530,12 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
     /* initial state: V0, izhikevich v0, pending spikes at -inf (eden/Eden.cpp:9081-9094) */
     for (int b = 0; b < 2; b++) {
         for (int32_t c = 0; c < m->n_comp; c++) P.v[b][c] = m->comp_v0[c];
-        for (int32_t k = 0; k < m->n_izh; k++) P.v[b][m->n_comp + k] = m->izh_params[10 * (int64_t)k + 1];
+        for (int32_t k = 0; k < m->n_izh; k++) {
+            /* the value OnStart gives V */
+            int kind = m->izh_kind ? m->izh_kind[k] : EDEN_POINT_IZH2007;
+            int f = kind == EDEN_POINT_IZH2007 ? 1 : (kind == EDEN_POINT_IAF_TAU || kind == EDEN_POINT_IAF_TAU_REF) ? 0 : 2;
+            P.v[b][m->n_comp + k] = m->izh_params[EDEN_POINT_PARAMS * (int64_t)k + f];
+        }
         for (int64_t s = 0; s < ns; s++) P.syn_pend[b][s] = -INFINITY;
     }
     P.syn_off = csr_by_key(m->syn_target, ns, nt);
@@ -493,7 +565,7 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
 
 static void port_free(Port *P) {
     for (int b = 0; b < 2; b++) {
-        free(P->v[b]); free(P->gate[b]); free(P->izh_u[b]); free(P->syn_a[b]); free(P->syn_b[b]);
+        free(P->v[b]); free(P->gate[b]); free(P->izh_u[b]); free(P->izh_s[b]); free(P->syn_a[b]); free(P->syn_b[b]);
         free(P->syn_pend[b]); free(P->trig[b]); free(P->pois_ts[b]); free(P->pois_isi[b]);
         free(P->pois_a[b]); free(P->pois_b[b]); free(P->spiked[b]);
     }

@@ -15,6 +15,7 @@ CASES = {
     "ball_and_stick": ("ball_and_stick", dict(n_inst=8, length_ms=40.0), 1.0, None),
     "spike_sources": ("spike_sources", dict(), 1.0, None),
     "event_sets": ("event_sets", dict(), 1.0, None),
+    "point_neurons": ("point_neurons", dict(), 1.0, None),
 }
 
 

@@ -87,3 +87,27 @@ def test_event_set_round_trip():
     np.testing.assert_array_equal(a.syn_src, b.syn_src)
     # reader sources follow the cells: the cells' global ids (and RNG seeds) are unchanged
     assert a.event_src.max() < a.ext_src.min()
+
+
+def test_point_neuron_round_trip_and_kinds():
+    from eden_gb300.lowering import (POINT_ADEX, POINT_IAF, POINT_IAF_REF, POINT_IAF_TAU, POINT_IAF_TAU_REF,
+                                     POINT_PARAMS)
+    spec = workloads.point_neurons(n_per_kind=2, length_ms=5.0)
+    with tempfile.TemporaryDirectory() as d:
+        back = neuroml_io.read_lems(neuroml_io.write_lems(spec, d))
+    a, b = lowering.lower(spec), lowering.lower(back)
+    np.testing.assert_array_equal(a.izh_kind, [POINT_IAF_TAU] * 2 + [POINT_IAF_TAU_REF] * 2 + [POINT_IAF] * 2 +
+                                  [POINT_IAF_REF] * 2 + [POINT_ADEX] * 2)
+    assert a.izh_params.shape == (10, POINT_PARAMS)
+    np.testing.assert_array_equal(a.izh_params, b.izh_params)
+    # adExIaF in engine units: pF, uS, mV, us, nA
+    np.testing.assert_allclose(a.izh_params[-1, :11], [281.0, 0.03, -70.6, -50.4, -40.4, -48.5, 2.0, 40000.0,
+                                                       a.izh_params[-1, 8], 0.004, 0.08], rtol=1e-6)
+
+
+def test_current_into_tau_cells_is_refused():
+    spec = workloads.point_neurons(n_per_kind=2, length_ms=5.0)
+    spec.pulses[0].cell = spec.pulses[0].cell.copy()
+    spec.pulses[0].cell[0] = 0                     # an iafTauCell
+    with pytest.raises(ValueError, match="do not receive current"):
+        lowering.lower(spec)
