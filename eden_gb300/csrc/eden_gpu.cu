@@ -270,6 +270,18 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
         if (m->pois_target[k] < 0 || m->pois_target[k] >= nt || m->pois_type[k] < 0 || m->pois_type[k] >= m->n_syn_types ||
             m->pois_src[k] < 0 || m->pois_src[k] >= m->n_src || !finite_pos(m->pois_rate[k]))
             return ctx->fail(EDEN_GPU_E_INVALID, "poisson input %lld: bad field", (long long)k);
+    if (m->n_timed < 0 || m->n_timed > INT32_MAX / 2 ||
+        (m->n_timed > 0 && (!m->timed_target || !m->timed_type || !m->timed_weight || !m->timed_off || !m->timed_step)))
+        return ctx->fail(EDEN_GPU_E_INVALID, "bad timed-input arrays");
+    if (m->n_timed > 0 && m->timed_off[0] != 0) return ctx->fail(EDEN_GPU_E_INVALID, "timed_off[0] != 0");
+    for (int64_t k = 0; k < m->n_timed; k++) {
+        if (m->timed_target[k] < 0 || m->timed_target[k] >= nt || m->timed_type[k] < 0 ||
+            m->timed_type[k] >= m->n_syn_types || m->timed_off[k + 1] < m->timed_off[k] || !std::isfinite(m->timed_weight[k]))
+            return ctx->fail(EDEN_GPU_E_INVALID, "timed input %lld: bad field", (long long)k);
+        for (int64_t j = m->timed_off[k]; j < m->timed_off[k + 1]; j++)
+            if (m->timed_step[j] < 1 || (j > m->timed_off[k] && m->timed_step[j] <= m->timed_step[j - 1]))
+                return ctx->fail(EDEN_GPU_E_INVALID, "timed input %lld: steps must be >= 1 and increasing", (long long)k);
+    }
     for (int64_t k = 0; k < m->n_pulse; k++)
         if (m->pulse_target[k] < 0 || m->pulse_target[k] >= nt)
             return ctx->fail(EDEN_GPU_E_INVALID, "pulse %lld: bad target", (long long)k);
@@ -362,6 +374,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     std::vector<int64_t> n_in_user(nt, 0);
     for (int64_t s = 0; s < m->n_syn; s++) n_in_user[m->syn_target[s]]++;
     for (int64_t k = 0; k < m->n_pois; k++) n_in_user[m->pois_target[k]]++;
+    for (int64_t k = 0; k < m->n_timed; k++) n_in_user[m->timed_target[k]]++;
     for (int64_t k = 0; k < m->n_pulse; k++) n_in_user[m->pulse_target[k]]++;
     std::vector<double> cost(n_cells, 0.0);
     double total = 0;
@@ -738,6 +751,19 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         po_inst[k] = m->pois_instance[o];
         po_type[k] = (uint8_t)m->pois_type[o];
     }
+    // timedSynapticInput items sorted by internal target (then type, then input order)
+    std::vector<int64_t> tord = sort_items(m->n_timed, m->timed_target, m->timed_type);
+    std::vector<int64_t> toff = offsets(tord, m->timed_target);
+    std::vector<float> tm_w(m->n_timed);
+    std::vector<uint8_t> tm_type(m->n_timed);
+    std::vector<int64_t> tm_off(m->n_timed + 1, 0), tm_step;
+    for (int64_t k = 0; k < m->n_timed; k++) {
+        const int64_t o = tord[k];
+        tm_w[k] = m->timed_weight[o];
+        tm_type[k] = (uint8_t)m->timed_type[o];
+        tm_step.insert(tm_step.end(), m->timed_step + m->timed_off[o], m->timed_step + m->timed_off[o + 1]);
+        tm_off[k + 1] = (int64_t)tm_step.size();
+    }
     const int64_t ns = m->n_syn;
     ctx->n_syn = ns;
     std::vector<float> sy_w(ns), sy_d(ns), sy_pend(ns, -INFINITY);
@@ -771,7 +797,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         src_thr[s] = m->src_threshold[s];
     }
     phase("blocks");
-    // input blocks per target: pulses, then Poisson runs, then synapse runs of one type
+    // input blocks per target: pulses, then Poisson runs, timed-input runs, then synapse runs of one type
     std::vector<int32_t> t_blk0(nt + 1, 0);
     std::vector<int32_t> bk_kind;
     std::vector<uint8_t> bk_type;
@@ -788,6 +814,13 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             int64_t k1 = k;
             while (k1 < poff[t + 1] && po_type[k1] == po_type[k]) k1++;
             bk_kind.push_back(BK_POIS); bk_erev.push_back(m->syn_types[po_type[k]].erev); bk_type.push_back(po_type[k]);
+            bk_i0.push_back(k); bk_i1.push_back(k1);
+            k = k1;
+        }
+        for (int64_t k = toff[t]; k < toff[t + 1];) {
+            int64_t k1 = k;
+            while (k1 < toff[t + 1] && tm_type[k1] == tm_type[k]) k1++;
+            bk_kind.push_back(BK_TIMED); bk_erev.push_back(m->syn_types[tm_type[k]].erev); bk_type.push_back(tm_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
         }
@@ -1035,6 +1068,18 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.po_rate, po_rate)); TRY(upload_c(ctx, &d.po_w, po_w));
     TRY(upload_c(ctx, &d.po_seed, po_seed)); TRY(upload_c(ctx, &d.po_inst, po_inst));
     TRY(upload_c(ctx, &d.po_type, po_type));
+    TRY(upload(ctx, &d.tm_a, (const float *)nullptr, (size_t)m->n_timed));
+    TRY(upload(ctx, &d.tm_b, (const float *)nullptr, (size_t)m->n_timed));
+    TRY(upload(ctx, &d.tm_last, (const int32_t *)nullptr, (size_t)m->n_timed));
+    TRY(upload(ctx, &d.tm_cur, (const int64_t *)nullptr, (size_t)m->n_timed));
+    TRY(upload_c(ctx, &d.tm_w, tm_w)); TRY(upload_c(ctx, &d.tm_type, tm_type));
+    TRY(upload_c(ctx, &d.tm_off, tm_off)); TRY(upload_c(ctx, &d.tm_step, tm_step));
+    {
+        // each item's cursor starts at its first listed step
+        std::vector<int64_t> cur(tm_off.begin(), tm_off.end() - 1);
+        if (!cur.empty())
+            CUDA_TRY(ctx, cudaMemcpy(d.tm_cur, cur.data(), sizeof(int64_t) * cur.size(), cudaMemcpyHostToDevice));
+    }
     TRY(upload(ctx, &d.sy_a, (const float *)nullptr, (size_t)ns));
     TRY(upload(ctx, &d.sy_b, (const float *)nullptr, (size_t)ns));
     TRY(upload(ctx, &d.sy_last, (const int32_t *)nullptr, (size_t)ns));
@@ -1167,6 +1212,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             const int kb = bk_kind[b];
             kinds.pulse |= kb == BK_PULSE;
             kinds.pois |= kb == BK_POIS;
+            kinds.timed |= kb == BK_TIMED;
             kinds.syn |= kb == BK_SYN;
             if (kb != BK_PULSE) {
                 const int sk = m->syn_types[bk_type[b]].kind;

@@ -65,7 +65,7 @@ __device__ __forceinline__ float div_by_tau(float x, float tau, float r) {
 
 
 enum : int { ST_OK = 0, ST_LOG_OVERFLOW = 1 };
-enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2 };
+enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2, BK_TIMED = 3 };
 constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
 constexpr int kChunkItems = 128; // input items per chunk (one warp, up to four per lane)
 constexpr int kPowLen = 33;      // powers 0..32 of a synapse decay factor
@@ -113,7 +113,7 @@ struct DevModel {
     // pulses, current) for step k of the window is G[k * n_block + block]
     int32_t n_block;
     const int32_t *t_blk0;            // [n_target + 1]
-    const int32_t *bk_kind;           // BK_PULSE, BK_POIS, BK_SYN
+    const int32_t *bk_kind;           // BK_PULSE, BK_POIS, BK_SYN, BK_TIMED
     const uint8_t *bk_type;           // synapse type of a Poisson / synapse block
     const float *bk_erev;
     const int32_t *in_tgt;            // targets with any block
@@ -137,6 +137,15 @@ struct DevModel {
     const float *po_rate, *po_w;
     const int32_t *po_seed, *po_inst;
     const uint8_t *po_type;
+    // timedSynapticInput items: own synapse state (as Poisson items), weight,
+    // type, the steps each fires in (tm_step[tm_off[i] .. tm_off[i+1]]) and
+    // the next one due
+    float *tm_a, *tm_b;
+    int32_t *tm_last;
+    const float *tm_w;
+    const uint8_t *tm_type;
+    const int64_t *tm_off, *tm_step;
+    int64_t *tm_cur;
     // connection synapses
     float *sy_a, *sy_b, *sy_pend;     // sy_a/sy_b: state just after the synapse's last event
     int32_t *sy_last;                 // step of that event
@@ -457,12 +466,39 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
 #ifndef EDEN_KIND_PULSE
 #define EDEN_KIND_PULSE 1
 #define EDEN_KIND_POIS 1
+#define EDEN_KIND_TIMED 1
 #define EDEN_KIND_SYN 1
 #define EDEN_KIND_EXPONE 1
 #define EDEN_KIND_EXPTWO 1
 #define EDEN_KIND_FOREST 1
 #define EDEN_KIND_IZH 1
 #endif
+
+// A timedSynapticInput item over the window: its synapse fires in each
+// listed step (eden/Eden.cpp:3759-3790, 3859-3871: the first step whose
+// t + dt exceeds a listed time, the same step), which lowering has computed.
+template <int KIND>
+__device__ __forceinline__ void timed_window(const DevModel &m, int64_t it, const WindowArgs &w, const SynTypeDev &st,
+                                             float *rowA, float *rowB, bool &used) {
+    int64_t c = m.tm_cur[it];
+    const int64_t c1 = m.tm_off[it + 1];
+    const int64_t end = w.step0 + w.K;
+    if (c >= c1 || m.tm_step[c] >= end) return;
+    float a = m.tm_a[it], b = KIND == EDEN_SYN_EXPTWO ? m.tm_b[it] : 0.0f;
+    int32_t last = m.tm_last[it];
+    const float *pw = m.syn_pow + (size_t)m.tm_type[it] * 2 * kPowLen;
+    for (; c < c1 && m.tm_step[c] < end; c++) {
+        const int64_t s = m.tm_step[c];
+        if (s < w.step0) continue;
+        float dA, dB;
+        input_event<KIND>(st, pw, m.dt, m.tm_w[it], s, a, b, last, dA, dB);
+        put_event(rowA, rowB, used, w.K, (int)(s - w.step0), dA, dB);
+    }
+    m.tm_a[it] = a;
+    if (KIND == EDEN_SYN_EXPTWO) m.tm_b[it] = b;
+    m.tm_last[it] = last;
+    m.tm_cur[it] = c;
+}
 
 // Per-warp accumulation tiles: row `lane` (stride kAccStride, padded so that
 // both a row write and a column read are free of bank conflicts) holds the
@@ -518,7 +554,7 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
         if (lane + 32 * r < n) {
             const int64_t it = i0 + 32 * r;
             if (kind == BK_POIS) { s0v[r] = m.po_ts[it]; s1v[r] = m.po_isi[it]; }
-            else { s0v[r] = m.sy_pend[it]; s1v[r] = __uint_as_float(m.sy_mask[it]); }
+            else if (kind == BK_SYN) { s0v[r] = m.sy_pend[it]; s1v[r] = __uint_as_float(m.sy_mask[it]); }
         }
     }
 #pragma unroll
@@ -526,7 +562,12 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
         if (lane + 32 * r < n) {
             const int64_t it = i0 + 32 * r;
             // only the input kinds the kernels are compiled for (all, or the model's)
-            if (kind == BK_POIS) {
+            if (kind == BK_TIMED) {
+                if (EDEN_KIND_TIMED) {
+                    if (two) { if (EDEN_KIND_EXPTWO) timed_window<EDEN_SYN_EXPTWO>(m, it, w, st, rowA, rowB, used); }
+                    else if (EDEN_KIND_EXPONE) timed_window<EDEN_SYN_EXPONE>(m, it, w, st, rowA, rowB, used);
+                }
+            } else if (kind == BK_POIS) {
                 if (EDEN_KIND_POIS) {
                     if (two) { if (EDEN_KIND_EXPTWO) pois_window<EDEN_SYN_EXPTWO>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used); }
                     else if (EDEN_KIND_EXPONE) pois_window<EDEN_SYN_EXPONE>(m, it, w, st, s0v[r], s1v[r], rowA, rowB, used);
@@ -605,7 +646,7 @@ __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1,
         const int kind = BK_K[bk];
         if (kind == BK_PULSE) {
             Iin += g;
-        } else if (kind == BK_POIS) {
+        } else if (kind == BK_POIS || kind == BK_TIMED) {
             Iin += g * (BK_E[bk] - v);
             Gin += g;
         } else {

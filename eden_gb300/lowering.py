@@ -125,6 +125,12 @@ class LoweredModel:
     ext_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     ext_step: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     izh_kind: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))  # POINT_* per point neuron
+    # timedSynapticInput: target, synapse type, weight, and the steps each fires in
+    timed_target: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    timed_type: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    timed_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    timed_off: np.ndarray = field(default_factory=lambda: np.zeros(1, np.int64))
+    timed_step: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     phys_ra: np.ndarray = field(default=None)          # physical cell -> axial resistivity, ohm*cm
 
     @property
@@ -219,6 +225,15 @@ def step_times_f32(dt: np.float32, n_steps: int) -> np.ndarray:
     dts, as a float (eden/Eden.cpp:11486, 11931)."""
     acc = np.concatenate([[0.0], np.add.accumulate(np.full(max(n_steps - 1, 0), float(np.float32(dt))))])
     return acc[:n_steps].astype(F32)
+
+
+def timed_steps(times_ms, th: np.ndarray) -> np.ndarray:
+    """Steps (>= 1) in which a spike list fires, given th[n-1] = t_n + dt in
+    float: the first step whose t + dt exceeds each time, once per step
+    (eden/Eden.cpp:3759-3790)."""
+    times = np.sort(ms_to_us(np.asarray(times_ms, np.float64)).astype(F32))
+    idx = np.searchsorted(th, times, side="right")
+    return (np.unique(idx[idx < len(th)]) + 1).astype(np.int64)
 
 
 def spike_source_steps(ext_cells: dict, dt: np.float32, n_steps: int):
@@ -477,6 +492,20 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         perm = np.argsort(pt, kind="stable")
         pt, pty, pr_, pw, ps, pinst = pt[perm], pty[perm], pr_[perm], pw[perm], ps[perm], pinst[perm]
 
+    # ---- timed synaptic inputs: the steps each fires in -------------------------
+    tm_t, tm_ty, tm_w, tm_off, tm_steps = [], [], [], [0], []
+    if spec.timed:
+        th = (step_times_f32(dt, spec.n_steps()) + F32(dt)).astype(F32)
+        for ti in spec.timed:
+            k = syn_index[ti.synapse]
+            tm_t.append(target_of(ti.cell, ti.seg))
+            tm_ty.append(np.full(len(ti.cell), k, np.int32))
+            tm_w.append(np.asarray(ti.weight, np.float64).astype(F32))
+            for times in ti.times:
+                st = timed_steps(times, th)
+                tm_steps.append(st)
+                tm_off.append(tm_off[-1] + len(st))
+
     # ---- pulses ---------------------------------------------------------------
     qt, qs, qd, qa = [], [], [], []
     for pu in spec.pulses:
@@ -517,6 +546,8 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         trace_target=trace_target, event_src=event_src, gid_target_base=gid_base,
         chan_density=joined(chan_dens, np.int32), phys_ra=np.asarray(phys_ra, np.float64),
         ext_src=ext_src, ext_step=ext_step, izh_kind=np.asarray(izh_kind, np.int32),
+        timed_target=cat(tm_t, np.int32), timed_type=cat(tm_ty, np.int32), timed_weight=cat(tm_w, F32),
+        timed_off=np.asarray(tm_off, np.int64), timed_step=cat(tm_steps, np.int64),
     )
 
 
@@ -549,6 +580,8 @@ class CModel(ctypes.Structure):
         ("pulse_duration", _f32p), ("pulse_amplitude", _f32p), ("pulse_weight", _f32p),
         ("n_ext", ctypes.c_int64), ("ext_src", _i32p), ("ext_step", _i64p),
         ("izh_kind", _i32p),
+        ("n_timed", ctypes.c_int64), ("timed_target", _i32p), ("timed_type", _i32p), ("timed_weight", _f32p),
+        ("timed_off", _i64p), ("timed_step", _i64p),
     ]
 
 
@@ -621,4 +654,10 @@ def to_cmodel(m: LoweredModel):
     cm.ext_step = p(m.ext_step, np.int64, _i64p)
     cm.izh_kind = p(m.izh_kind if m.izh_kind is not None and len(m.izh_kind) == m.n_izh
                     else np.zeros(m.n_izh, np.int32), np.int32, _i32p)
+    cm.n_timed = len(m.timed_target)
+    cm.timed_target = p(m.timed_target, np.int32, _i32p)
+    cm.timed_type = p(m.timed_type, np.int32, _i32p)
+    cm.timed_weight = p(m.timed_weight, F32, _f32p)
+    cm.timed_off = p(m.timed_off, np.int64, _i64p)
+    cm.timed_step = p(m.timed_step, np.int64, _i64p)
     return cm, keep

@@ -273,6 +273,18 @@ class EventSelection:
 
 
 @dataclass
+class TimedInputs:
+    """timedSynapticInput instances: input i drives its own instance of
+    `synapse` on cell gid cell[i], segment seg[i], firing at times[i] (ms),
+    scaled by weight[i]."""
+    synapse: str
+    cell: np.ndarray
+    seg: np.ndarray
+    times: list
+    weight: np.ndarray
+
+
+@dataclass
 class NetworkSpec:
     name: str
     dt: float               # ms
@@ -285,6 +297,7 @@ class NetworkSpec:
     projections: List[Projection] = field(default_factory=list)
     pulses: List[PulseInputs] = field(default_factory=list)
     poissons: List[PoissonInputs] = field(default_factory=list)
+    timed: List[TimedInputs] = field(default_factory=list)
     trace_columns: List[OutputColumn] = field(default_factory=list)
     trace_file: str = "trajectory.txt"
     event_selections: List[EventSelection] = field(default_factory=list)

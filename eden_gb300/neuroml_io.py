@@ -23,7 +23,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       PhysicalCell, PoissonInputs, Population, Projection,
                       PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SynapseType,
                       EventSetReaderCell,
-                      RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, AdExCell, IafCell)
+                      RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, AdExCell, IafCell, TimedInputs)
 
 
 def _f(x: float) -> str:
@@ -116,6 +116,15 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
         w(f'<poissonFiringSynapse id="{pid}" averageRate="{_f(po.rate)} Hz" synapse="{po.synapse}" '
           f'spikeTarget="./{po.synapse}"/>\n')
 
+    timed_ids = []
+    for k, ti in enumerate(spec.timed):
+        for i, times in enumerate(ti.times):
+            tid = f"timed{k}_{i}"
+            timed_ids.append((tid, k, i))
+            w(f'<timedSynapticInput id="{tid}" synapse="{ti.synapse}" spikeTarget="./{ti.synapse}">')
+            for j, t in enumerate(times):
+                w(f'<spike id="{j}" time="{_f(t)}ms"/>')
+            w('</timedSynapticInput>\n')
     w('<network id="net">\n')
     readers = {}
     for p in spec.populations:
@@ -181,6 +190,14 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
                 w(f'  <input id="{n}" target="../{pop}[{local_of[po.cell[i]]}]" segmentId="{po.seg[i]}" '
                   f'fractionAlong="0.5" destination="synapses"/>\n')
             w(' </inputList>\n')
+    for tid, k, i in timed_ids:
+        ti = spec.timed[k]
+        pop = pop_of[ti.cell[i]]
+        w(f' <inputList id="il{n_list}" component="{tid}" population="{pop}">\n')
+        n_list += 1
+        w(f'  <inputW id="0" target="../{pop}[{local_of[ti.cell[i]]}]" segmentId="{ti.seg[i]}" '
+          f'fractionAlong="0.5" destination="synapses" weight="{_f(ti.weight[i])}"/>\n')
+        w(' </inputList>\n')
     w('</network>\n</neuroml>\n')
     with open(os.path.join(dirname, nml_name), "w") as f:
         f.write("".join(out))
@@ -470,6 +487,7 @@ def read_lems(path: str) -> NetworkSpec:
                        _qty(sim, "length", "time"), seed)
     # components
     channels_by_name, synapses, pulses_def, pois_def, cells = {}, {}, {}, {}, {}
+    timed_def = {}
     net = None
     for e in elems:
         t = _tag(e)
@@ -496,6 +514,8 @@ def read_lems(path: str) -> NetworkSpec:
         elif t == "pulseGenerator":
             pulses_def[e.get("id")] = (_qty(e, "delay", "time"), _qty(e, "duration", "time"),
                                        _qty(e, "amplitude", "current"))
+        elif t == "timedSynapticInput":
+            timed_def[e.get("id")] = (e.get("synapse"), [_qty(sp, "time", "time") for sp in _children(e, "spike")])
         elif t == "poissonFiringSynapse":
             pois_def[e.get("id")] = (_qty(e, "averageRate", "frequency_hz"), e.get("synapse"))
         elif t == "izhikevich2007Cell":
@@ -599,12 +619,16 @@ def read_lems(path: str) -> NetworkSpec:
     # inputs
     pcell, pseg, pdel, pdur, pamp = [], [], [], [], []
     pois_rows = {}
+    timed_rows = {}
     for il in _children(net, "inputList"):
         comp = il.get("component")
-        for inp in _children(il, "input"):
-            g = gid(_cell_ref(inp.get("target"), pops))
+        for inp in _children(il, "input") + _children(il, "inputW"):
+            g = gid(_cell_ref(inp.get("target"), pops, il.get("population")))
             seg = int(inp.get("segmentId", "0"))
-            if comp in pulses_def:
+            if comp in timed_def:
+                timed_rows.setdefault(timed_def[comp][0], []).append(
+                    (g, seg, timed_def[comp][1], float(inp.get("weight", "1"))))
+            elif comp in pulses_def:
                 d, du, a = pulses_def[comp]
                 pcell.append(g); pseg.append(seg); pdel.append(d); pdur.append(du); pamp.append(a)
             elif comp in pois_def:
@@ -621,6 +645,12 @@ def read_lems(path: str) -> NetworkSpec:
     if pcell:
         spec.pulses.append(PulseInputs("*", np.array(pcell), np.array(pseg), np.array(pdel), np.array(pdur),
                                        np.array(pamp)))
+    for syn, rows in timed_rows.items():
+        if syn not in synapses:
+            raise ValueError(f"timedSynapticInput: synapse {syn} not supported")
+        spec.timed.append(TimedInputs(syn, np.array([r[0] for r in rows], np.int64),
+                                      np.array([r[1] for r in rows], np.int64), [np.array(r[2]) for r in rows],
+                                      np.array([r[3] for r in rows])))
     for comp, rows in pois_rows.items():
         rate, syn = pois_def[comp]
         if syn not in synapses:

@@ -24,6 +24,8 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    instances and ports) driving izhikevich and HH cells.
   point_neurons    iafTau, iafTauRef, iaf, iafRef and adExIaF cells with DC
                    pulses and recurrent expTwo / expOne synapses.
+  timed_inputs     timedSynapticInput spike lists (expTwo and expOne) into
+                   HH and izhikevich cells.
 
 Every generator takes scale arguments (cell count, in-degree, length) so the
 same distributions produce the small cases the CPU reference can finish.
@@ -37,7 +39,7 @@ import numpy as np
 from .network import (AdExCell, ChannelDensity, EventSelection, IafCell, Izhikevich2007Cell,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
-                      SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, hh_channels)
+                      SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, TimedInputs, hh_channels)
 
 # conductivities (mS/cm2) and reversal potentials (mV) of the HH cells
 G_NA, G_K, G_L = 120.0, 36.0, 0.3
@@ -404,6 +406,47 @@ def point_neurons(n_per_kind: int = 8, fan_in: int = 6, length_ms: float = 100.0
     return spec
 
 
+# ---------------------------------------------------------------------------
+def timed_inputs(n_hh: int = 6, n_izh: int = 6, per_cell: int = 3, length_ms: float = 60.0, dt_ms: float = 0.025,
+                 seed: int = 1234, n_recorded: int = 8) -> NetworkSpec:
+    """timedSynapticInput spike lists (seeded times, some on and next to step
+    boundaries, some before the first step and after the run) driving expTwo
+    and expOne synapses on single-compartment HH and izhikevich2007 cells,
+    which also connect among themselves."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("timed_inputs", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=3.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+    spec.synapses.append(SynapseType("syn_e1", SYN_EXPONE, gbase=4.0, erev=0.0, tau_decay=2.0))
+    hh = PhysicalCell(name="hhcell", seg_parent=np.array([-1]), seg_len=np.array([0.0]), seg_diam=np.array([17.8]),
+                      densities=_hh_densities(1, np.ones(1, dtype=bool)), cm=1.0, ra=30.0, v0=-65.0,
+                      spike_thresh=-20.0)
+    spec.cells.append(hh)
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    n = n_hh + n_izh
+    for syn in ("syn_e2", "syn_e1"):
+        cells = np.repeat(np.arange(n), per_cell)
+        times = []
+        for k in range(len(cells)):
+            t = np.round(np.sort(rng.uniform(-2.0, length_ms + 5.0, size=rng.integers(2, 12))), 4)
+            if k == 0:
+                t = np.concatenate([t, [0.0, 10.0, 9.9999, 10.0001, 20.025, 20.0251]])
+            times.append(t)
+        spec.timed.append(TimedInputs(syn, cells, np.zeros(len(cells), np.int64), times,
+                                      np.round(rng.uniform(0.5, 2.0, len(cells)), 4)))
+    post = np.repeat(np.arange(n), 3)
+    pre = rng.integers(0, n, size=post.size)
+    pre = np.where(pre == post, (pre + 1) % n, pre)
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre, post, "syn_e2",
+                                             np.round(rng.uniform(0.2, 1.0, post.size), 4),
+                                             _round_us(rng.uniform(0.5, 3.0, size=post.size))))
+    rec = np.sort(rng.choice(n, size=min(n_recorded, n), replace=False))
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, int(g)), 0) for g in rec]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
@@ -413,4 +456,5 @@ CONFIGS = {
     "spike_sources": spike_sources,
     "event_sets": event_sets,
     "point_neurons": point_neurons,
+    "timed_inputs": timed_inputs,
 }

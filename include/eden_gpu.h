@@ -177,6 +177,16 @@ typedef struct EdenGpuModel {
     const int64_t *ext_step;
 
     const int32_t *izh_kind;        /* [n_izh] EDEN_POINT_* of each point neuron */
+
+    /* timedSynapticInput inputs, each with its own synapse instance, which
+     * fires in the listed steps (the first step whose t + dt exceeds a spike
+     * time, eden/Eden.cpp:3759-3790, 3859-3871; increasing, >= 1) */
+    int64_t n_timed;
+    const int32_t *timed_target;
+    const int32_t *timed_type;      /* synapse type it drives */
+    const float *timed_weight;
+    const int64_t *timed_off;       /* [n_timed + 1] into timed_step */
+    const int64_t *timed_step;
 } EdenGpuModel;
 
 /* Execution options. */

@@ -136,6 +136,11 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         dm.pulse_duration = g.copy(m->pulse_duration, (size_t)m->n_pulse);
         dm.pulse_amplitude = g.copy(m->pulse_amplitude, (size_t)m->n_pulse);
         dm.pulse_weight = g.copy(m->pulse_weight, (size_t)m->n_pulse);
+        dm.timed_target = g.copy(m->timed_target, (size_t)m->n_timed);
+        dm.timed_type = g.copy(m->timed_type, (size_t)m->n_timed);
+        dm.timed_weight = g.copy(m->timed_weight, (size_t)m->n_timed);
+        dm.timed_off = g.copy(m->timed_off, (size_t)m->n_timed + 1);
+        dm.timed_step = g.copy(m->timed_step, m->n_timed ? (size_t)m->timed_off[m->n_timed] : 0);
         dm.ext_src = g.copy(m->ext_src, (size_t)m->n_ext);
         dm.ext_step = g.copy(m->ext_step, (size_t)m->n_ext);
         // the loop's state, set up on the host
@@ -155,6 +160,8 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
             D.pois_a[b] = g.copy(H.pois_a[b], (size_t)np + 1);
             D.pois_b[b] = g.copy(H.pois_b[b], (size_t)np + 1);
             D.spiked[b] = g.copy(H.spiked[b], (size_t)m->n_src + 1);
+            D.timed_a[b] = g.copy(H.timed_a[b], (size_t)m->n_timed + 1);
+            D.timed_b[b] = g.copy(H.timed_b[b], (size_t)m->n_timed + 1);
         }
         D.diag = g.copy(H.diag, (size_t)m->n_comp + 1);
         D.gate_off = g.copy(H.gate_off, (size_t)n_chan + 1);
@@ -166,6 +173,9 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         D.order = g.copy(H.order, (size_t)m->n_comp + 1);
         D.src_of_target = g.copy(H.src_of_target, (size_t)nt + 1);
         D.syn_fire_count = g.copy(H.syn_fire_count, (size_t)ns + 1);
+        D.timed_cur = g.copy(H.timed_cur, (size_t)m->n_timed + 1);
+        D.timed_tgt_off = g.copy(H.timed_tgt_off, (size_t)nt + 1);
+        D.timed_order = g.copy(H.timed_order, (size_t)m->n_timed + 1);
         int32_t *d_tt = g.copy(trace_target, (size_t)n_trace);
         double *d_trace = g.zeros<double>((size_t)n_steps * (size_t)(n_trace > 0 ? n_trace : 1));
         int32_t *d_lsrc = g.zeros<int32_t>((size_t)spike_cap);

@@ -16,6 +16,7 @@
  *   expTwoSynapse (LEMS, forward Euler)       LEMS_CoreComponents.inc.xml:145-180, eden/Eden.cpp:2832-2994
  *   poissonFiringSynapse + randof hash RNG    LEMS_CoreComponents.inc.xml:623-672, eden/Eden.cpp:3199-3233, 3873-3912
  *   pulseGenerator                            eden/Eden.cpp:3798-3826
+ *   timedSynapticInput                        eden/Eden.cpp:3759-3790, 3859-3871
  *   point neurons (LEMS): izhikevich2007Cell, iafTauCell, iafTauRefCell,
  *   iafCell, iafRefCell, adExIaFCell          LEMS_CoreComponents.inc.xml:957-1240, eden/Eden.cpp:6821-6914
  *   threshold crossing + spike send           eden/Eden.cpp:6247-6252, 3946-3995
@@ -98,6 +99,10 @@ typedef struct {
     real *syn_a[2], *syn_b[2], *syn_pend[2];
     unsigned char *trig[2];
     real *pois_ts[2], *pois_isi[2], *pois_a[2], *pois_b[2];
+    real *timed_a[2], *timed_b[2];      /* timedSynapticInput synapse states */
+    int64_t *timed_cur;                 /* next listed step of each timed input */
+    int64_t *timed_tgt_off;             /* [n_target + 1] timed inputs by target */
+    int64_t *timed_order;               /* inputs in target order */
     unsigned char *spiked[2];           /* event-logger slot per source */
     real *diag;
     int64_t *gate_off;                  /* [n_chan + 1] */
@@ -247,6 +252,52 @@ static inline PORT_FN void poisson_step(const Port *P, int cur, int64_t k, int i
     *gw = g * m->pois_weight[k];
 }
 
+/* timedSynapticInput: its synapse fires in the listed steps (the first step
+ * whose t + dt exceeds a spike time, eden/Eden.cpp:3759-3790, 3859-3871;
+ * computed at lowering), with the synapse's own dynamics as in poisson_step. */
+static inline PORT_FN void timed_input_step(const Port *P, int cur, int64_t k, int init, real dt, int64_t step,
+                                            real v, real *iw, real *gw) {
+    const EdenGpuModel *m = P->m;
+    int nxt = cur ^ 1;
+    int fired = 0;
+    if (!init) {
+        int64_t c = P->timed_cur[k];
+        if (c < m->timed_off[k + 1] && m->timed_step[c] == step) {
+            fired = 1;
+            P->timed_cur[k] = c + 1;
+        }
+    }
+    const EdenGpuSynapseType *st = &m->syn_types[m->timed_type[k]];
+    real a = P->timed_a[cur][k], b = P->timed_b[cur][k];
+    real g = st->gbase * (b - a);
+    real i = g * (st->erev - v);
+    real an, bn;
+    if (st->kind == EDEN_SYN_EXPONE) {
+        g = a;
+        i = g * (st->erev - v);
+        if (!init) {
+            an = a - dt * (a / st->tau_decay);
+            if (fired) an = a + st->gbase;
+        } else {
+            an = a;
+        }
+        bn = b;
+    } else if (init) {
+        an = R(0.0); bn = R(0.0);
+    } else {
+        an = a + dt * (-a / st->tau_rise);
+        bn = b + dt * (-b / st->tau_decay);
+        if (fired) {
+            an = a + st->weight_prop * st->waveform_factor;
+            bn = b + st->weight_prop * st->waveform_factor;
+        }
+    }
+    P->timed_a[nxt][k] = an;
+    P->timed_b[nxt][k] = bn;
+    *iw = i * m->timed_weight[k];
+    *gw = g * m->timed_weight[k];
+}
+
 /* Synapse + input currents into one target (in the reference's order:
  * inputs then synapses are separate totals, each synapse type a block). */
 static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, real t, real dt, int64_t step,
@@ -271,6 +322,18 @@ static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, rea
         for (; k < P->pois_off[tgt + 1] && m->pois_type[k] == type; k++) {
             real iw, gw;
             poisson_step(P, cur, k, init, dt, step, v, &iw, &gw);
+            Ia += iw; Ga += gw;
+        }
+        Iin += Ia; Gin += Ga;
+    }
+    /* timed inputs, one block per synapse type run */
+    int64_t q = P->timed_tgt_off[tgt];
+    while (q < P->timed_tgt_off[tgt + 1]) {
+        int type = m->timed_type[P->timed_order[q]];
+        real Ia = R(0.0), Ga = R(0.0);
+        for (; q < P->timed_tgt_off[tgt + 1] && m->timed_type[P->timed_order[q]] == type; q++) {
+            real iw, gw;
+            timed_input_step(P, cur, P->timed_order[q], init, dt, step, v, &iw, &gw);
             Ia += iw; Ga += gw;
         }
         Iin += Ia; Gin += Ga;
@@ -525,6 +588,35 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
         P.pois_b[b] = (real *)calloc((size_t)np + 1, sizeof(real));
         P.spiked[b] = (unsigned char *)calloc((size_t)m->n_src + 1, 1);
     }
+    for (int b = 0; b < 2; b++) {
+        P.timed_a[b] = (real *)calloc((size_t)m->n_timed + 1, sizeof(real));
+        P.timed_b[b] = (real *)calloc((size_t)m->n_timed + 1, sizeof(real));
+    }
+    P.timed_cur = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m->n_timed + 1));
+    for (int64_t k = 0; k < m->n_timed; k++) P.timed_cur[k] = m->timed_off[k];
+    P.timed_tgt_off = csr_by_key(m->timed_target, m->n_timed, nt);
+    P.timed_order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m->n_timed + 1));
+    {
+        /* stable by target, then type (input order within a type) */
+        int64_t *fill = (int64_t *)calloc((size_t)nt + 1, sizeof(int64_t));
+        for (int pass = 0; pass < 1; pass++) {
+            for (int64_t k = 0; k < m->n_timed; k++) {
+                int32_t t = m->timed_target[k];
+                P.timed_order[P.timed_tgt_off[t] + fill[t]++] = k;
+            }
+        }
+        free(fill);
+        for (int64_t t = 0; t < nt; t++) {  /* insertion sort by type inside each target */
+            for (int64_t i = P.timed_tgt_off[t] + 1; i < P.timed_tgt_off[t + 1]; i++) {
+                int64_t x = P.timed_order[i], j = i - 1;
+                while (j >= P.timed_tgt_off[t] && m->timed_type[P.timed_order[j]] > m->timed_type[x]) {
+                    P.timed_order[j + 1] = P.timed_order[j];
+                    j--;
+                }
+                P.timed_order[j + 1] = x;
+            }
+        }
+    }
     P.diag = (real *)calloc((size_t)m->n_comp + 1, sizeof(real));
     P.syn_fire_count = (int64_t *)calloc((size_t)ns + 1, sizeof(int64_t));
     /* initial state: V0, izhikevich v0, pending spikes at -inf (eden/Eden.cpp:9081-9094) */
@@ -567,10 +659,11 @@ static void port_free(Port *P) {
     for (int b = 0; b < 2; b++) {
         free(P->v[b]); free(P->gate[b]); free(P->izh_u[b]); free(P->izh_s[b]); free(P->syn_a[b]); free(P->syn_b[b]);
         free(P->syn_pend[b]); free(P->trig[b]); free(P->pois_ts[b]); free(P->pois_isi[b]);
-        free(P->pois_a[b]); free(P->pois_b[b]); free(P->spiked[b]);
+        free(P->pois_a[b]); free(P->pois_b[b]); free(P->spiked[b]); free(P->timed_a[b]); free(P->timed_b[b]);
     }
     free(P->diag); free(P->syn_fire_count); free(P->gate_off); free(P->syn_off); free(P->pois_off);
     free(P->pulse_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
+    free(P->timed_cur); free(P->timed_tgt_off); free(P->timed_order);
 }
 
 int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const int32_t *trace_target,

@@ -16,6 +16,7 @@ CASES = {
     "spike_sources": ("spike_sources", dict(), 1.0, None),
     "event_sets": ("event_sets", dict(), 1.0, None),
     "point_neurons": ("point_neurons", dict(), 1.0, None),
+    "timed_inputs": ("timed_inputs", dict(), 1.0, None),
 }
 
 

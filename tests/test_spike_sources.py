@@ -111,3 +111,18 @@ def test_current_into_tau_cells_is_refused():
     spec.pulses[0].cell[0] = 0                     # an iafTauCell
     with pytest.raises(ValueError, match="do not receive current"):
         lowering.lower(spec)
+
+
+def test_timed_input_steps_and_round_trip():
+    # the first step whose t + dt exceeds each time, once per step; times
+    # before the run fire in step 1, times after it never
+    th = (lowering.step_times_f32(np.float32(25.0), 401) + np.float32(25.0)).astype(np.float32)
+    steps = lowering.timed_steps([-1.0, 0.0, 0.01, 2.5, 2.51, 2.525, 10.0, 10.01, 50.0], th)
+    np.testing.assert_array_equal(steps, [1, 101, 102, 401])
+    spec = workloads.timed_inputs(length_ms=20.0)
+    with tempfile.TemporaryDirectory() as d:
+        back = neuroml_io.read_lems(neuroml_io.write_lems(spec, d))
+    a, b = lowering.lower(spec), lowering.lower(back)
+    for f in ("timed_target", "timed_type", "timed_weight", "timed_off", "timed_step"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f))
+    assert a.timed_step.min() >= 1
