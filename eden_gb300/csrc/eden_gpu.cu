@@ -285,6 +285,23 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
     for (int64_t k = 0; k < m->n_pulse; k++)
         if (m->pulse_target[k] < 0 || m->pulse_target[k] >= nt)
             return ctx->fail(EDEN_GPU_E_INVALID, "pulse %lld: bad target", (long long)k);
+    if (m->n_wave < 0) return ctx->fail(EDEN_GPU_E_INVALID, "n_wave must be >= 0");
+    if (m->n_wave > 0 && (!m->wave_target || !m->wave_shape || !m->wave_params || !m->wave_weight))
+        return ctx->fail(EDEN_GPU_E_INVALID, "waveform inputs: null array");
+    for (int64_t k = 0; k < m->n_wave; k++) {
+        if (m->wave_target[k] < 0 || m->wave_target[k] >= nt)
+            return ctx->fail(EDEN_GPU_E_INVALID, "waveform input %lld: bad target", (long long)k);
+        if (m->wave_shape[k] < 0 || m->wave_shape[k] >= EDEN_WAVE_SHAPES)
+            return ctx->fail(EDEN_GPU_E_INVALID, "waveform input %lld: unknown shape %d", (long long)k,
+                             m->wave_shape[k]);
+        bool finite = std::isfinite(m->wave_weight[k]);
+        for (int j = 0; j < EDEN_WAVE_PARAMS; j++) finite = finite && std::isfinite(m->wave_params[EDEN_WAVE_PARAMS * k + j]);
+        if (!finite) return ctx->fail(EDEN_GPU_E_INVALID, "waveform input %lld: non-finite parameter", (long long)k);
+    }
+    if (m->pois_rng_base)
+        for (int64_t k = 0; k < m->n_pois; k++)
+            if (m->pois_rng_base[k] < 0)
+                return ctx->fail(EDEN_GPU_E_INVALID, "Poisson input %lld: negative random-call id", (long long)k);
     return 0;
 }
 
@@ -376,6 +393,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (int64_t k = 0; k < m->n_pois; k++) n_in_user[m->pois_target[k]]++;
     for (int64_t k = 0; k < m->n_timed; k++) n_in_user[m->timed_target[k]]++;
     for (int64_t k = 0; k < m->n_pulse; k++) n_in_user[m->pulse_target[k]]++;
+    for (int64_t k = 0; k < m->n_wave; k++) n_in_user[m->wave_target[k]]++;
     std::vector<double> cost(n_cells, 0.0);
     double total = 0;
     int max_cell = 1;
@@ -626,6 +644,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = 0; k < m->n_pulse; k++) has_input[u2i[m->pulse_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_pois; k++) has_input[u2i[m->pois_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_syn; k++) has_input[u2i[m->syn_target[k]]] = 1;
+        for (int64_t k = 0; k < m->n_timed; k++) has_input[u2i[m->timed_target[k]]] = 1;
+        for (int64_t k = 0; k < m->n_wave; k++) has_input[u2i[m->wave_target[k]]] = 1;
         for (int it = 0; it < nt; it++) {
             if (t_izh[it] >= 0 || has_input[it]) continue;
             if (c_chan0[it + 1] - c_chan0[it] != 1) continue;
@@ -741,14 +761,26 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         pu_s[k] = m->pulse_start[o]; pu_d[k] = m->pulse_duration[o];
         pu_a[k] = m->pulse_amplitude[o]; pu_w[k] = m->pulse_weight[o];
     }
+    // sine / ramp generators by internal target, then shape (input order within a shape)
+    std::vector<int64_t> word = sort_items(m->n_wave, m->wave_target, m->wave_shape);
+    std::vector<int64_t> woff = offsets(word, m->wave_target);
+    std::vector<float> wv_p((size_t)m->n_wave * kWaveWords, 0.f);
+    std::vector<uint8_t> wv_shape(m->n_wave);
+    for (int64_t k = 0; k < m->n_wave; k++) {
+        const int64_t o = word[k];
+        for (int j = 0; j < EDEN_WAVE_PARAMS; j++) wv_p[k * kWaveWords + j] = m->wave_params[EDEN_WAVE_PARAMS * o + j];
+        wv_p[k * kWaveWords + EDEN_WAVE_PARAMS] = m->wave_weight[o];
+        wv_shape[k] = (uint8_t)m->wave_shape[o];
+    }
     std::vector<float> po_rate(m->n_pois), po_w(m->n_pois);
-    std::vector<int32_t> po_seed(m->n_pois), po_inst(m->n_pois);
+    std::vector<int32_t> po_seed(m->n_pois), po_inst(m->n_pois), po_rng(m->n_pois);
     std::vector<uint8_t> po_type(m->n_pois);
     for (int64_t k = 0; k < m->n_pois; k++) {
         int64_t o = pord[k];
         po_rate[k] = m->pois_rate[o]; po_w[k] = m->pois_weight[o];
         po_seed[k] = m->src_cell_seed[m->pois_src[o]];
         po_inst[k] = m->pois_instance[o];
+        po_rng[k] = m->pois_rng_base ? m->pois_rng_base[o] : 0;
         po_type[k] = (uint8_t)m->pois_type[o];
     }
     // timedSynapticInput items sorted by internal target (then type, then input order)
@@ -809,6 +841,13 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         if (qoff[t + 1] > qoff[t]) {
             bk_kind.push_back(BK_PULSE); bk_erev.push_back(0.f); bk_type.push_back(0);
             bk_i0.push_back(qoff[t]); bk_i1.push_back(qoff[t + 1]);
+        }
+        for (int64_t k = woff[t]; k < woff[t + 1];) {
+            int64_t k1 = k;
+            while (k1 < woff[t + 1] && wv_shape[k1] == wv_shape[k]) k1++;
+            bk_kind.push_back(BK_PULSE); bk_erev.push_back(0.f); bk_type.push_back((uint8_t)(1 + wv_shape[k]));
+            bk_i0.push_back(k); bk_i1.push_back(k1);
+            k = k1;
         }
         for (int64_t k = poff[t]; k < poff[t + 1];) {
             int64_t k1 = k;
@@ -1067,6 +1106,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload(ctx, &d.po_last, (const int32_t *)nullptr, (size_t)m->n_pois));
     TRY(upload_c(ctx, &d.po_rate, po_rate)); TRY(upload_c(ctx, &d.po_w, po_w));
     TRY(upload_c(ctx, &d.po_seed, po_seed)); TRY(upload_c(ctx, &d.po_inst, po_inst));
+    TRY(upload_c(ctx, &d.po_rng, po_rng));
+    TRY(upload_c(ctx, &d.wv_p, wv_p));
     TRY(upload_c(ctx, &d.po_type, po_type));
     TRY(upload(ctx, &d.tm_a, (const float *)nullptr, (size_t)m->n_timed));
     TRY(upload(ctx, &d.tm_b, (const float *)nullptr, (size_t)m->n_timed));
@@ -1210,7 +1251,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         eden_codegen::Kinds kinds;
         for (int b = 0; b < n_block; b++) {
             const int kb = bk_kind[b];
-            kinds.pulse |= kb == BK_PULSE;
+            kinds.pulse |= kb == BK_PULSE && bk_type[b] == 0;
+            kinds.sine |= kb == BK_PULSE && bk_type[b] == 1 + EDEN_WAVE_SINE;
+            kinds.ramp |= kb == BK_PULSE && bk_type[b] == 1 + EDEN_WAVE_RAMP;
             kinds.pois |= kb == BK_POIS;
             kinds.timed |= kb == BK_TIMED;
             kinds.syn |= kb == BK_SYN;

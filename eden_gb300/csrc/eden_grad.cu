@@ -612,11 +612,12 @@ int validate(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
     if (m->abi_version != EDEN_GPU_ABI_VERSION)
         return g->fail(EDEN_GPU_E_INVALID, "ABI version %d, library is %d", m->abi_version, EDEN_GPU_ABI_VERSION);
     if (!finite_pos(m->dt)) return g->fail(EDEN_GPU_E_INVALID, "dt must be positive");
-    if (m->n_izh != 0 || m->n_syn != 0 || m->n_pois != 0)
+    if (m->n_izh != 0 || m->n_syn != 0 || m->n_pois != 0 || m->n_timed != 0 || m->n_wave != 0)
         return g->fail(EDEN_GPU_E_INVALID,
                        "gradients cover independent physical cells with HH channels and pulse inputs: the model has "
-                       "%d point neurons, %lld synapses and %lld Poisson inputs",
-                       m->n_izh, (long long)m->n_syn, (long long)m->n_pois);
+                       "%d point neurons, %lld synapses, %lld Poisson, %lld timed and %lld waveform inputs",
+                       m->n_izh, (long long)m->n_syn, (long long)m->n_pois, (long long)m->n_timed,
+                       (long long)m->n_wave);
     if (m->n_phys <= 0 || m->n_comp <= 0) return g->fail(EDEN_GPU_E_INVALID, "no physical cells");
     if (m->phys_comp_off[0] != 0 || m->phys_comp_off[m->n_phys] != m->n_comp)
         return g->fail(EDEN_GPU_E_INVALID, "phys_comp_off must span [0, n_comp]");

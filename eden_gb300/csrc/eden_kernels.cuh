@@ -69,6 +69,7 @@ enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2, BK_TIMED = 3 };
 constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
 constexpr int kChunkItems = 128; // input items per chunk (one warp, up to four per lane)
 constexpr int kPowLen = 33;      // powers 0..32 of a synapse decay factor
+constexpr int kWaveWords = 8;    // waveform input record: delay, duration, 3 shape parameters, weight, 2 spare
 
 struct DevModel {
     int32_t n_target, n_src, n_group, n_forest, n_in;
@@ -131,11 +132,13 @@ struct DevModel {
     int32_t pois_exact;               // dt is a whole number of us: Poisson clocks advance exactly
     float *ck_a, *ck_b;               // aggregate synapse state of each chunk (weighted sums)
     const float *pu_start, *pu_dur, *pu_amp, *pu_w;
+    const float *wv_p;                // sine / ramp generators, kWaveWords per item
     // Poisson inputs
     float *po_ts, *po_isi, *po_a, *po_b;  // po_a/po_b: own synapse state just after its last event
     int32_t *po_last;                      // step of that event
     const float *po_rate, *po_w;
     const int32_t *po_seed, *po_inst;
+    const int32_t *po_rng;                 // random-call id of the input's first draw
     const uint8_t *po_type;
     // timedSynapticInput items: own synapse state (as Poisson items), weight,
     // type, the steps each fires in (tm_step[tm_off[i] .. tm_off[i+1]]) and
@@ -352,7 +355,8 @@ __device__ __forceinline__ void put_event(float *rowA, float *rowB, bool &used, 
 // is a whole number of us and the times stay below 2^24 us, every such sum
 // is exact, so the firing step is found directly instead of step by step.
 __device__ __forceinline__ float pois_draw(const DevModel &m, int64_t it, int64_t step, int invocation) {
-    return (-(1.0f / m.po_rate[it])) * logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], step, invocation));
+    return (-(1.0f / m.po_rate[it])) *
+           logf(1.0f - randof(1.0f, (int64_t)m.po_seed[it], m.po_inst[it], step, m.po_rng[it] + invocation));
 }
 
 template <int KIND>
@@ -465,6 +469,8 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
 // the model's, and the compiler drops the code of the others.
 #ifndef EDEN_KIND_PULSE
 #define EDEN_KIND_PULSE 1
+#define EDEN_KIND_SINE 1
+#define EDEN_KIND_RAMP 1
 #define EDEN_KIND_POIS 1
 #define EDEN_KIND_TIMED 1
 #define EDEN_KIND_SYN 1
@@ -519,6 +525,36 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     const int kind = info & 3;
     const int n = info >> 8;
     float *rowA = tileA + lane * kAccStride, *rowB = tileB + lane * kAccStride;
+    if ((EDEN_KIND_SINE || EDEN_KIND_RAMP) && kind == BK_PULSE && ((info >> 2) & 63) != 0) {
+        // sineGenerator / rampGenerator (LEMS_CoreComponents.inc.xml:430-458,
+        // 489-521): the value the OnConditions assign at the step's time,
+        // which the reference's LEMS code exposes in the same step; OnStart's
+        // in the initialisation passes
+        const bool sine = ((info >> 2) & 63) == 1 + EDEN_WAVE_SINE;
+        for (int r = 0; lane + 32 * r < n; r++) {
+            const float *p = m.wv_p + (size_t)(ck_i0 + lane + 32 * r) * kWaveWords;
+            const float del = p[0], dur = p[1], a = p[2], b = p[3], cc = p[4], wt = p[5];
+            for (int j = 0; j < w.K; j++) {
+                const float tf = tk[j];
+                const bool init = w.step0 + j <= 0;
+                const bool off = tf < del || !(tf < dur + del);
+                float i;
+                if (sine) i = (init || off) ? 0.0f : (1.0f * a) * sinf(cc + ((2.0f * 3.14159265f) * (tf - del)) / b);
+                else i = init ? cc : off ? 1.0f * cc : 1.0f * (a + ((b - a) * (tf - del)) / dur);
+                const float term = __fmul_rn(i, wt);
+                rowA[j] = r > 0 ? rowA[j] + term : term;
+            }
+        }
+        __syncwarp();
+        if (lane < w.K) {
+            const int rows = n < 32 ? n : 32;
+            float tot = 0.0f;
+            for (int r = 0; r < rows; r++) tot += tileA[r * kAccStride + lane];
+            m.Gp[(size_t)lane * m.n_chunk + c] = tot;
+        }
+        __syncwarp();
+        return;
+    }
     if (EDEN_KIND_PULSE && kind == BK_PULSE) {
         for (int r = 0; lane + 32 * r < n; r++) {
             const int64_t it = ck_i0 + lane + 32 * r;

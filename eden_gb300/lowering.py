@@ -28,7 +28,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, IafCell, Izhikevich2007Cell, NetworkSpec,
-                      PhysicalCell, SpikeArrayCell,
+                      PhysicalCell, SpikeArrayCell, WAVE_RAMP, WAVE_SINE,
                       SYN_EXPONE, SYN_EXPTWO)
 
 F32 = np.float32
@@ -132,6 +132,13 @@ class LoweredModel:
     timed_off: np.ndarray = field(default_factory=lambda: np.zeros(1, np.int64))
     timed_step: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     phys_ra: np.ndarray = field(default=None)          # physical cell -> axial resistivity, ohm*cm
+    # sineGenerator / rampGenerator: target, WAVE_* shape, [n, WAVE_PARAMS] parameters (engine units), weight
+    wave_target: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    wave_shape: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    wave_params: np.ndarray = field(default_factory=lambda: np.zeros((0, 5), np.float32))
+    wave_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    # per Poisson input, the random-call id of its first draw
+    pois_rng_base: np.ndarray = field(default=None)
 
     @property
     def n_comp(self) -> int:
@@ -196,6 +203,9 @@ def _cable_geometry(cell: PhysicalCell):
 
 # point-neuron kinds and parameter layout (include/eden_gpu.h, EDEN_POINT_*)
 POINT_PARAMS = 16
+# waveform inputs (include/eden_gpu.h EDEN_WAVE_*)
+WAVE_PARAMS = 5
+WAVE_SHAPES = {WAVE_SINE: 0, WAVE_RAMP: 1}
 POINT_IZH2007, POINT_IAF_TAU, POINT_IAF_TAU_REF, POINT_IAF, POINT_IAF_REF, POINT_ADEX = range(6)
 _IAF_KINDS = {"iafTauCell": POINT_IAF_TAU, "iafTauRefCell": POINT_IAF_TAU_REF, "iafCell": POINT_IAF,
               "iafRefCell": POINT_IAF_REF}
@@ -312,6 +322,41 @@ def event_set_steps(ct, gids, dt: np.float32, n_steps: int):
     return pairs_[:, 1].astype(np.int32), pairs_[:, 0]
 
 
+def poisson_rng_bases(spec: NetworkSpec, gid_ctype: np.ndarray, gid_is_point: np.ndarray) -> list:
+    """Per Poisson component of `spec`, the random-call id of each of its
+    inputs' first draw.  The reference numbers a cell type's random() calls
+    as it generates code: compartment by compartment (eden/Eden.cpp:6540,
+    the compartment's offset is the count so far), and within a compartment
+    one code block per input component present on it in any cell of the
+    type, in the order the components are defined (eden/Eden.cpp:1812-1830,
+    5943), each Poisson block making two calls (eden/Eden.cpp:2450-2458)."""
+    if not spec.poissons:
+        return []
+    span = 1 << 20
+    keys = []
+    for po in spec.poissons:
+        cells = np.asarray(po.cell, np.int64)
+        local = np.where(gid_is_point[cells], 0, np.asarray(po.seg, np.int64))
+        keys.append(gid_ctype[cells].astype(np.int64) * span + local)
+    # the Poisson components on each (cell type, compartment)
+    present = {}
+    for k, kk in enumerate(keys):
+        for key in np.unique(kk).tolist():
+            present.setdefault(key, []).append(k)
+    offset = {}
+    for key in sorted(present):
+        ty = key // span
+        prev = offset.get(("end", ty), 0)
+        offset[key] = prev
+        offset[("end", ty)] = prev + 2 * len(present[key])
+    out = []
+    for k, kk in enumerate(keys):
+        uniq, inv = np.unique(kk, return_inverse=True)
+        base = np.array([offset[key] + 2 * present[key].index(k) for key in uniq.tolist()], np.int64)
+        out.append(base[inv].astype(np.int32) if len(kk) else np.zeros(0, np.int32))
+    return out
+
+
 def joined(parts, dtype) -> np.ndarray:
     return np.concatenate(parts).astype(dtype) if parts else np.zeros(0, dtype)
 
@@ -357,9 +402,12 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     izh_index = np.full(n_cells, -1, np.int64)
     no_current = np.zeros(n_cells, bool)
     geom_cache = {}
+    gid_ctype = np.zeros(n_cells, np.int32)
+    ctype_index = {c.name: k for k, c in enumerate(spec.cells)}
     gid = 0
     for pop in spec.populations:
         ct = spec.cell_type(pop.cell_type)
+        gid_ctype[gid:gid + pop.size] = ctype_index[ct.name]
         for _ in range(pop.size):
             if isinstance(ct, PhysicalCell):
                 if ct.name not in geom_cache:
@@ -469,8 +517,9 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         wgt = np.zeros(0, F32); dly = np.zeros(0, F32)
 
     # ---- poisson inputs -----------------------------------------------------
-    pt, pty, pr_, pw, ps, pinst = [], [], [], [], [], []
-    for po in spec.poissons:
+    pt, pty, pr_, pw, ps, pinst, prng = [], [], [], [], [], [], []
+    rng_base = poisson_rng_bases(spec, gid_ctype, gid_is_izh)
+    for k_po, po in enumerate(spec.poissons):
         k = syn_index[po.synapse]
         cells = np.asarray(po.cell, np.int64)
         segs = np.asarray(po.seg, np.int64)
@@ -485,12 +534,15 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         pt.append(t); pty.append(np.full(len(cells), k, np.int32))
         pr_.append(np.full(len(cells), _to_f32(po.rate * 1e-6), F32))
         pw.append(np.ones(len(cells), F32)); ps.append(cells.astype(np.int32)); pinst.append(inst)
+        prng.append(rng_base[k_po])
     cat = lambda xs, dt_: (np.concatenate(xs) if xs else np.zeros(0, dt_))
     pt, pty, pr_, pw, ps, pinst = (cat(pt, np.int32), cat(pty, np.int32), cat(pr_, F32),
                                    cat(pw, F32), cat(ps, np.int32), cat(pinst, np.int32))
+    prng = cat(prng, np.int32)
     if len(pt):
         perm = np.argsort(pt, kind="stable")
         pt, pty, pr_, pw, ps, pinst = pt[perm], pty[perm], pr_[perm], pw[perm], ps[perm], pinst[perm]
+        prng = prng[perm]
 
     # ---- timed synaptic inputs: the steps each fires in -------------------------
     tm_t, tm_ty, tm_w, tm_off, tm_steps = [], [], [], [0], []
@@ -517,6 +569,28 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     if len(qt):
         perm = np.argsort(qt, kind="stable")
         qt, qs, qd, qa = qt[perm], qs[perm], qd[perm], qa[perm]
+
+    # ---- sine / ramp generators ----------------------------------------------
+    wt, wsh, wpar, wwt = [], [], [], []
+    for wv in spec.waves:
+        if wv.shape not in WAVE_SHAPES:
+            raise ValueError(f"unknown waveform input shape {wv.shape!r}")
+        n = len(wv.cell)
+        wt.append(target_of(wv.cell, wv.seg))
+        wsh.append(np.full(n, WAVE_SHAPES[wv.shape], np.int32))
+        par = np.zeros((n, WAVE_PARAMS), np.float64)
+        par[:, 0] = ms_to_us(wv.delay)
+        par[:, 1] = ms_to_us(wv.duration)
+        par[:, 2] = wv.p0
+        par[:, 3] = ms_to_us(wv.p1) if wv.shape == WAVE_SINE else wv.p1
+        par[:, 4] = wv.p2
+        wpar.append(par.astype(F32))
+        wwt.append(np.asarray(wv.weight, np.float64).astype(F32))
+    wt, wsh, wwt = cat(wt, np.int32), cat(wsh, np.int32), cat(wwt, F32)
+    wpar = np.concatenate(wpar) if wpar else np.zeros((0, WAVE_PARAMS), F32)
+    if len(wt):
+        perm = np.argsort(wt, kind="stable")
+        wt, wsh, wpar, wwt = wt[perm], wsh[perm], wpar[perm], wwt[perm]
 
     trace_target = np.array([target_of([gid_off[c.pop] + c.cell], [c.seg], current=False)[0]
                              for c in spec.trace_columns], dtype=np.int32)
@@ -548,13 +622,15 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         ext_src=ext_src, ext_step=ext_step, izh_kind=np.asarray(izh_kind, np.int32),
         timed_target=cat(tm_t, np.int32), timed_type=cat(tm_ty, np.int32), timed_weight=cat(tm_w, F32),
         timed_off=np.asarray(tm_off, np.int64), timed_step=cat(tm_steps, np.int64),
+        wave_target=wt, wave_shape=wsh, wave_params=wpar, wave_weight=wwt,
+        pois_rng_base=prng,
     )
 
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 3
+ABI_VERSION = 4
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -582,6 +658,9 @@ class CModel(ctypes.Structure):
         ("izh_kind", _i32p),
         ("n_timed", ctypes.c_int64), ("timed_target", _i32p), ("timed_type", _i32p), ("timed_weight", _f32p),
         ("timed_off", _i64p), ("timed_step", _i64p),
+        ("n_wave", ctypes.c_int64), ("wave_target", _i32p), ("wave_shape", _i32p), ("wave_params", _f32p),
+        ("wave_weight", _f32p),
+        ("pois_rng_base", _i32p),
     ]
 
 
@@ -660,4 +739,11 @@ def to_cmodel(m: LoweredModel):
     cm.timed_weight = p(m.timed_weight, F32, _f32p)
     cm.timed_off = p(m.timed_off, np.int64, _i64p)
     cm.timed_step = p(m.timed_step, np.int64, _i64p)
+    cm.n_wave = len(m.wave_target)
+    cm.wave_target = p(m.wave_target, np.int32, _i32p)
+    cm.wave_shape = p(m.wave_shape, np.int32, _i32p)
+    cm.wave_params = p(np.asarray(m.wave_params).reshape(-1), F32, _f32p)
+    cm.wave_weight = p(m.wave_weight, F32, _f32p)
+    if m.pois_rng_base is not None:
+        cm.pois_rng_base = p(m.pois_rng_base, np.int32, _i32p)
     return cm, keep

@@ -3,9 +3,10 @@
 A `NetworkSpec` holds, in numpy arrays, exactly the NeuroML content the
 GPU path supports: physical (multi-compartment) cells with ionChannelHH
 channels, izhikevich2007Cell point neurons, expOneSynapse / expTwoSynapse
-synapses reached through `connectionWD` projections, pulseGenerator and
-poissonFiringSynapse inputs, and the LEMS `<Simulation>` with its
-`OutputFile` / `EventOutputFile` recorders.
+synapses reached through `connectionWD` projections, pulseGenerator,
+sineGenerator, rampGenerator, poissonFiringSynapse and timedSynapticInput
+inputs, and the LEMS
+`<Simulation>` with its `OutputFile` / `EventOutputFile` recorders.
 
 Three producers/consumers share it:
   * workloads.py builds it from a seed (the synthetic configurations);
@@ -249,12 +250,34 @@ class PulseInputs:
 @dataclass
 class PoissonInputs:
     """poissonFiringSynapse instances (`rate` Hz, each driving its own
-    instance of `synapse`) on cell gid `cell`, segment `seg`."""
+    instance of `synapse`) on cell gid `cell`, segment `seg`.  The order of
+    a spec's entries is the order the components are defined in."""
     pop: str
     synapse: str
     rate: float
     cell: np.ndarray
     seg: np.ndarray
+
+
+WAVE_SINE = "sine"
+WAVE_RAMP = "ramp"
+
+
+@dataclass
+class WaveInputs:
+    """sineGenerator (shape "sine": p0 amplitude nA, p1 period ms, p2 phase)
+    or rampGenerator (shape "ramp": p0 startAmplitude, p1 finishAmplitude,
+    p2 baselineAmplitude, nA) instances, active from `delay` for `duration`
+    (ms), on cell gid `cell`, segment `seg`, scaled by `weight`."""
+    shape: str
+    cell: np.ndarray
+    seg: np.ndarray
+    delay: np.ndarray
+    duration: np.ndarray
+    p0: np.ndarray
+    p1: np.ndarray
+    p2: np.ndarray
+    weight: np.ndarray
 
 
 @dataclass
@@ -298,6 +321,7 @@ class NetworkSpec:
     pulses: List[PulseInputs] = field(default_factory=list)
     poissons: List[PoissonInputs] = field(default_factory=list)
     timed: List[TimedInputs] = field(default_factory=list)
+    waves: List[WaveInputs] = field(default_factory=list)
     trace_columns: List[OutputColumn] = field(default_factory=list)
     trace_file: str = "trajectory.txt"
     event_selections: List[EventSelection] = field(default_factory=list)

@@ -23,7 +23,8 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       PhysicalCell, PoissonInputs, Population, Projection,
                       PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SynapseType,
                       EventSetReaderCell,
-                      RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, AdExCell, IafCell, TimedInputs)
+                      RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
+                      TimedInputs, WaveInputs)
 
 
 def _f(x: float) -> str:
@@ -125,6 +126,22 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             for j, t in enumerate(times):
                 w(f'<spike id="{j}" time="{_f(t)}ms"/>')
             w('</timedSynapticInput>\n')
+    # sine / ramp generators: one component per distinct parameter set
+    wave_ids = {}
+    for wv in spec.waves:
+        for i in range(len(wv.cell)):
+            key = _wave_key(wv, i)
+            if key in wave_ids:
+                continue
+            wid = f"wave{len(wave_ids)}"
+            wave_ids[key] = wid
+            _, d, du, a, b, c = key
+            if wv.shape == WAVE_SINE:
+                w(f'<sineGenerator id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" amplitude="{_f(a)}nA" '
+                  f'period="{_f(b)}ms" phase="{_f(c)}"/>\n')
+            else:
+                w(f'<rampGenerator id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" startAmplitude="{_f(a)}nA" '
+                  f'finishAmplitude="{_f(b)}nA" baselineAmplitude="{_f(c)}nA"/>\n')
     w('<network id="net">\n')
     readers = {}
     for p in spec.populations:
@@ -189,6 +206,17 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             for n, i in enumerate(idx):
                 w(f'  <input id="{n}" target="../{pop}[{local_of[po.cell[i]]}]" segmentId="{po.seg[i]}" '
                   f'fractionAlong="0.5" destination="synapses"/>\n')
+            w(' </inputList>\n')
+    for wv in spec.waves:
+        by_comp = defaultdict(list)
+        for i in range(len(wv.cell)):
+            by_comp[(wave_ids[_wave_key(wv, i)], pop_of[wv.cell[i]])].append(i)
+        for (wid, pop), idx in by_comp.items():
+            w(f' <inputList id="il{n_list}" component="{wid}" population="{pop}">\n')
+            n_list += 1
+            for n, i in enumerate(idx):
+                w(f'  <inputW id="{n}" target="../{pop}[{local_of[wv.cell[i]]}]" segmentId="{wv.seg[i]}" '
+                  f'fractionAlong="0.5" destination="synapses" weight="{_f(wv.weight[i])}"/>\n')
             w(' </inputList>\n')
     for tid, k, i in timed_ids:
         ti = spec.timed[k]
@@ -327,6 +355,11 @@ def _qty(el, attr, dim, default=None):
     if unit not in table:
         raise ValueError(f"<{_tag(el)}> {attr}: unit {unit!r} not supported for {dim} (known: {sorted(table)})")
     return value * table[unit]
+
+
+def _wave_key(wv, i):
+    return (wv.shape, float(wv.delay[i]), float(wv.duration[i]), float(wv.p0[i]), float(wv.p1[i]),
+            float(wv.p2[i]))
 
 
 def _tag(el):
@@ -487,7 +520,7 @@ def read_lems(path: str) -> NetworkSpec:
                        _qty(sim, "length", "time"), seed)
     # components
     channels_by_name, synapses, pulses_def, pois_def, cells = {}, {}, {}, {}, {}
-    timed_def = {}
+    timed_def, wave_def = {}, {}
     net = None
     for e in elems:
         t = _tag(e)
@@ -518,6 +551,19 @@ def read_lems(path: str) -> NetworkSpec:
             timed_def[e.get("id")] = (e.get("synapse"), [_qty(sp, "time", "time") for sp in _children(e, "spike")])
         elif t == "poissonFiringSynapse":
             pois_def[e.get("id")] = (_qty(e, "averageRate", "frequency_hz"), e.get("synapse"))
+        elif t == "transientPoissonFiringSynapse":
+            # the reference writes this component's LONG_TIME constant (1e9
+            # hour) as `inf` into its generated C, which then fails to compile
+            raise ValueError(f"transientPoissonFiringSynapse {e.get('id')}: not supported (the reference "
+                             f"simulator cannot run it either)")
+        elif t == "sineGenerator":
+            wave_def[e.get("id")] = (WAVE_SINE, _qty(e, "delay", "time"), _qty(e, "duration", "time"),
+                                     _qty(e, "amplitude", "current"), _qty(e, "period", "time"),
+                                     _qty(e, "phase", None))
+        elif t == "rampGenerator":
+            wave_def[e.get("id")] = (WAVE_RAMP, _qty(e, "delay", "time"), _qty(e, "duration", "time"),
+                                     _qty(e, "startAmplitude", "current"), _qty(e, "finishAmplitude", "current"),
+                                     _qty(e, "baselineAmplitude", "current"))
         elif t == "izhikevich2007Cell":
             cells[e.get("id")] = Izhikevich2007Cell(
                 e.get("id"), C=_qty(e, "C", "capacitance"), k=_qty(e, "k", "cond_per_voltage"),
@@ -618,7 +664,7 @@ def read_lems(path: str) -> NetworkSpec:
                                            np.array(rows[3]), np.array(rows[4])))
     # inputs
     pcell, pseg, pdel, pdur, pamp = [], [], [], [], []
-    pois_rows = {}
+    pois_rows, wave_rows = {}, {}
     timed_rows = {}
     for il in _children(net, "inputList"):
         comp = il.get("component")
@@ -633,6 +679,8 @@ def read_lems(path: str) -> NetworkSpec:
                 pcell.append(g); pseg.append(seg); pdel.append(d); pdur.append(du); pamp.append(a)
             elif comp in pois_def:
                 pois_rows.setdefault(comp, []).append((g, seg))
+            elif comp in wave_def:
+                wave_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1"))))
             else:
                 raise ValueError(f"inputList component {comp} not supported")
     for ei in _children(net, "explicitInput"):
@@ -651,12 +699,23 @@ def read_lems(path: str) -> NetworkSpec:
         spec.timed.append(TimedInputs(syn, np.array([r[0] for r in rows], np.int64),
                                       np.array([r[1] for r in rows], np.int64), [np.array(r[2]) for r in rows],
                                       np.array([r[3] for r in rows])))
-    for comp, rows in pois_rows.items():
-        rate, syn = pois_def[comp]
+    # Poisson components in the order they are defined (the reference numbers
+    # their random draws in that order)
+    for comp, (rate, syn) in pois_def.items():
+        rows = pois_rows.get(comp)
+        if not rows:
+            continue
         if syn not in synapses:
             raise ValueError(f"poissonFiringSynapse {comp}: synapse {syn} not supported")
         spec.poissons.append(PoissonInputs("*", syn, rate, np.array([r[0] for r in rows]),
                                            np.array([r[1] for r in rows])))
+    for comp, rows in wave_rows.items():
+        shape, d, du, a, b, c = wave_def[comp]
+        n = len(rows)
+        spec.waves.append(WaveInputs(shape, np.array([r[0] for r in rows], np.int64),
+                                     np.array([r[1] for r in rows], np.int64), np.full(n, d), np.full(n, du),
+                                     np.full(n, a), np.full(n, b), np.full(n, c),
+                                     np.array([r[2] for r in rows])))
     # recorders: OutputFile / EventOutputFile and EDEN's EdenOutputFile /
     # EdenEventOutputFile with their time window, sampling interval or explicit
     # sample points, and heartbeat interval (eden/NeuroML.cpp:8037-8290);

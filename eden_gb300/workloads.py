@@ -26,6 +26,10 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    pulses and recurrent expTwo / expOne synapses.
   timed_inputs     timedSynapticInput spike lists (expTwo and expOne) into
                    HH and izhikevich cells.
+  input_kinds      every input kind on one branching cell type (HH soma,
+                   passive dendrites) and on izhikevich cells: pulse, sine and
+                   ramp generators, several Poisson components sharing
+                   compartments, and timed inputs on passive dendrites.
 
 Every generator takes scale arguments (cell count, in-degree, length) so the
 same distributions produce the small cases the CPU reference can finish.
@@ -39,7 +43,8 @@ import numpy as np
 from .network import (AdExCell, ChannelDensity, EventSelection, IafCell, Izhikevich2007Cell,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
-                      SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, TimedInputs, hh_channels)
+                      SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, TimedInputs, WAVE_RAMP,
+                      WAVE_SINE, WaveInputs, hh_channels)
 
 # conductivities (mS/cm2) and reversal potentials (mV) of the HH cells
 G_NA, G_K, G_L = 120.0, 36.0, 0.3
@@ -447,6 +452,84 @@ def timed_inputs(n_hh: int = 6, n_izh: int = 6, per_cell: int = 3, length_ms: fl
     return spec
 
 
+def input_kinds(n_mc: int = 6, n_izh: int = 4, length_ms: float = 80.0, dt_ms: float = 0.025,
+                seed: int = 1234) -> NetworkSpec:
+    """Every input kind on the same compartments: one branching cell type
+    (HH soma, five passive dendrite segments) in two populations plus
+    izhikevich2007 cells, with pulse, sine and ramp generators (weighted),
+    several Poisson components (up to three on one soma, others on
+    dendrites, so their random draws are numbered past the first), timed
+    inputs on passive dendrites, and recurrent expTwo connections."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("input_kinds", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=2.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+    spec.synapses.append(SynapseType("syn_e1", SYN_EXPONE, gbase=1.5, erev=0.0, tau_decay=3.0))
+    parent = np.array([-1, 0, 1, 2, 1, 4])
+    soma = np.zeros(len(parent), dtype=bool)
+    soma[0] = True
+    spec.cells.append(PhysicalCell("mc", parent, np.array([20.0, 60.0, 50.0, 40.0, 70.0, 30.0]),
+                                   np.array([20.0, 2.0, 1.5, 1.0, 1.5, 1.0]),
+                                   _hh_densities(len(parent), soma), cm=1.0, ra=150.0, v0=-65.0,
+                                   spike_thresh=-20.0, seg_groups={"soma_group": soma, "dend_group": ~soma}))
+    n_a = n_mc // 2
+    spec.populations.append(Population("mcA", "mc", n_a))
+    spec.populations.append(Population("mcB", "mc", n_mc - n_a))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    mc = np.arange(n_mc)
+    iz = n_mc + np.arange(n_izh)
+    # pulse on two somata
+    spec.pulses.append(PulseInputs("*", mc[:2], np.zeros(2, int), np.array([5.0, 30.0]), np.array([20.0, 40.0]),
+                                   np.array([0.25, 0.4])))
+    # sine generators: somata, a dendrite, izhikevich cells
+    cells = np.concatenate([mc[:3], mc[3:5], iz[:2]])
+    segs = np.concatenate([np.zeros(3, int), np.array([3, 5]), np.zeros(2, int)])
+    n = len(cells)
+    spec.waves.append(WaveInputs(WAVE_SINE, cells, segs, np.round(rng.uniform(0.0, 20.0, n), 3),
+                                 np.round(rng.uniform(20.0, 60.0, n), 3),
+                                 np.where(cells >= n_mc, 0.4, 0.3) * np.round(rng.uniform(0.5, 1.0, n), 3),
+                                 np.round(rng.uniform(5.0, 25.0, n), 3), np.round(rng.uniform(-1.0, 1.0, n), 3),
+                                 np.round(rng.uniform(0.5, 1.8, n), 3)))
+    # ramp generators (baseline before and after the ramp)
+    cells = np.concatenate([mc[2:5], iz[1:3]])
+    segs = np.array([2, 0, 4, 0, 0])
+    n = len(cells)
+    scale = np.where(cells >= n_mc, 0.5, 0.3)
+    spec.waves.append(WaveInputs(WAVE_RAMP, cells, segs, np.round(rng.uniform(0.0, 20.0, n), 3),
+                                 np.round(rng.uniform(20.0, 50.0, n), 3),
+                                 np.round(scale * rng.uniform(0.0, 0.5, n), 4),
+                                 np.round(scale * rng.uniform(0.5, 1.0, n), 4),
+                                 np.round(scale * rng.uniform(0.0, 0.2, n), 4),
+                                 np.round(rng.uniform(0.5, 1.5, n), 3)))
+    # Poisson components, in definition order: somata of every mc cell; a
+    # second one on some somata and dendrites; a third on a dendrite and some
+    # somata; two on the izhikevich cells
+    spec.poissons.append(PoissonInputs("*", "syn_e2", 60.0, np.repeat(mc, 2), np.zeros(2 * n_mc, int)))
+    spec.poissons.append(PoissonInputs("*", "syn_e1", 40.0, np.concatenate([mc[::2], mc[1::2]]),
+                                       np.concatenate([np.zeros(len(mc[::2]), int), np.full(len(mc[1::2]), 2)])))
+    spec.poissons.append(PoissonInputs("*", "syn_e2", 150.0, np.concatenate([mc, mc[:3]]),
+                                       np.concatenate([np.full(n_mc, 4), np.zeros(3, int)])))
+    spec.poissons.append(PoissonInputs("*", "syn_e1", 30.0, iz, np.zeros(n_izh, int)))
+    spec.poissons.append(PoissonInputs("*", "syn_e2", 200.0, np.repeat(iz, 2), np.zeros(2 * n_izh, int)))
+    # timed inputs on passive dendrite compartments
+    times = [np.round(np.sort(rng.uniform(0.0, length_ms, rng.integers(3, 9))), 4) for _ in range(n_mc)]
+    spec.timed.append(TimedInputs("syn_e2", mc, np.full(n_mc, 5), times, np.round(rng.uniform(0.5, 2.0, n_mc), 4)))
+    # recurrent connections
+    n_all = n_mc + n_izh
+    post = np.repeat(np.arange(n_all), 2)
+    pre = rng.integers(0, n_all, size=post.size)
+    pre = np.where(pre == post, (pre + 1) % n_all, pre)
+    post_seg = np.where(post < n_mc, rng.integers(0, len(parent), size=post.size), 0)
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre, post, "syn_e2",
+                                             np.round(rng.uniform(0.2, 0.8, post.size), 4),
+                                             _round_us(rng.uniform(0.5, 3.0, size=post.size)), post_seg=post_seg))
+    cols = [(int(c), 0) for c in mc] + [(int(mc[1]), 2), (int(mc[3]), 3), (int(mc[4]), 5), (int(mc[0]), 4)]
+    cols += [(int(c), 0) for c in iz]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), seg) for g, seg in cols]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n_all)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
@@ -457,4 +540,5 @@ CONFIGS = {
     "event_sets": event_sets,
     "point_neurons": point_neurons,
     "timed_inputs": timed_inputs,
+    "input_kinds": input_kinds,
 }

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 3
+#define EDEN_GPU_ABI_VERSION 4
 
 enum {
     EDEN_GPU_OK = 0,
@@ -63,6 +63,18 @@ enum {
     EDEN_POINT_KINDS = 6
 };
 #define EDEN_POINT_PARAMS 16
+
+/* Waveform current inputs (LEMS_CoreComponents.inc.xml: sineGenerator
+ * 430-458, rampGenerator 489-521). Parameters of input k at
+ * wave_params[EDEN_WAVE_PARAMS * k + j]: j = 0 delay (us), 1 duration (us),
+ * then for a sine 2 amplitude (nA), 3 period (us), 4 phase (rad); for a ramp
+ * 2 startAmplitude, 3 finishAmplitude, 4 baselineAmplitude (nA). */
+enum {
+    EDEN_WAVE_SINE = 0,
+    EDEN_WAVE_RAMP = 1,
+    EDEN_WAVE_SHAPES = 2
+};
+#define EDEN_WAVE_PARAMS 5
 
 /* One ionChannelHH type: up to EDEN_MAX_GATES gateHHrates, each contributing
  * q^instances to the open fraction (eden/Eden.cpp:5678-5717). Rates in 1/us. */
@@ -187,6 +199,22 @@ typedef struct EdenGpuModel {
     const float *timed_weight;
     const int64_t *timed_off;       /* [n_timed + 1] into timed_step */
     const int64_t *timed_step;
+
+    /* sineGenerator / rampGenerator inputs: the current at a step is
+     * wave_weight * f(t), t the step's time, as the reference's LEMS code
+     * exposes the value its OnConditions assign in the same step
+     * (eden/Eden.cpp:3107-3133, 2832-2994) */
+    int64_t n_wave;
+    const int32_t *wave_target;
+    const int32_t *wave_shape;      /* EDEN_WAVE_* */
+    const float *wave_params;       /* [n_wave * EDEN_WAVE_PARAMS] */
+    const float *wave_weight;
+
+    /* per Poisson input, the random-call id of its first draw (its second
+     * is the next): the random calls of the compartments before it in its
+     * cell type plus two per Poisson component before it on its own
+     * compartment (eden/Eden.cpp:6540, 2450-2458); NULL for all 0 */
+    const int32_t *pois_rng_base;
 } EdenGpuModel;
 
 /* Execution options. */

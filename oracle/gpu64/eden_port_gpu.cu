@@ -143,6 +143,11 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         dm.timed_step = g.copy(m->timed_step, m->n_timed ? (size_t)m->timed_off[m->n_timed] : 0);
         dm.ext_src = g.copy(m->ext_src, (size_t)m->n_ext);
         dm.ext_step = g.copy(m->ext_step, (size_t)m->n_ext);
+        dm.wave_target = g.copy(m->wave_target, (size_t)m->n_wave);
+        dm.wave_shape = g.copy(m->wave_shape, (size_t)m->n_wave);
+        dm.wave_params = g.copy(m->wave_params, (size_t)m->n_wave * EDEN_WAVE_PARAMS);
+        dm.wave_weight = g.copy(m->wave_weight, (size_t)m->n_wave);
+        dm.pois_rng_base = m->pois_rng_base ? g.copy(m->pois_rng_base, (size_t)np) : nullptr;
         // the loop's state, set up on the host
         Port D = H;
         D.m = g.copy(&dm, 1);
@@ -168,6 +173,7 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         D.syn_off = g.copy(H.syn_off, (size_t)nt + 1);
         D.pois_off = g.copy(H.pois_off, (size_t)nt + 1);
         D.pulse_off = g.copy(H.pulse_off, (size_t)nt + 1);
+        D.wave_off = g.copy(H.wave_off, (size_t)nt + 1);
         D.fan_off = g.copy(H.fan_off, (size_t)m->n_src + 1);
         D.fan_syn = g.copy(H.fan_syn, (size_t)ns + 1);
         D.order = g.copy(H.order, (size_t)m->n_comp + 1);

@@ -15,7 +15,9 @@
  *   expOneSynapse                             eden/Eden.cpp:3424-3466
  *   expTwoSynapse (LEMS, forward Euler)       LEMS_CoreComponents.inc.xml:145-180, eden/Eden.cpp:2832-2994
  *   poissonFiringSynapse + randof hash RNG    LEMS_CoreComponents.inc.xml:623-672, eden/Eden.cpp:3199-3233, 3873-3912
+ *   random-call numbering per compartment     eden/Eden.cpp:2450-2458, 6540
  *   pulseGenerator                            eden/Eden.cpp:3798-3826
+ *   sineGenerator, rampGenerator (LEMS)       LEMS_CoreComponents.inc.xml:430-458, 489-521, eden/Eden.cpp:3107-3133
  *   timedSynapticInput                        eden/Eden.cpp:3759-3790, 3859-3871
  *   point neurons (LEMS): izhikevich2007Cell, iafTauCell, iafTauRefCell,
  *   iafCell, iafRefCell, adExIaFCell          LEMS_CoreComponents.inc.xml:957-1240, eden/Eden.cpp:6821-6914
@@ -37,11 +39,13 @@ typedef double real;
 #define R(x) x
 #define EXP exp
 #define LOG log
+#define SIN sin
 #else
 typedef float real;
 #define R(x) x##f
 #define EXP expf
 #define LOG logf
+#define SIN sinf
 #endif
 #include <stdint.h>
 #include <stdlib.h>
@@ -106,7 +110,7 @@ typedef struct {
     unsigned char *spiked[2];           /* event-logger slot per source */
     real *diag;
     int64_t *gate_off;                  /* [n_chan + 1] */
-    int64_t *syn_off, *pois_off, *pulse_off; /* [n_target + 1] */
+    int64_t *syn_off, *pois_off, *pulse_off, *wave_off; /* [n_target + 1] */
     int64_t *fan_off, *fan_syn;         /* CSR source -> synapses */
     int32_t *order;                     /* per-cell DFS post-order, local ids */
     int32_t *src_of_target;             /* source id detecting at a target, or -1 */
@@ -207,17 +211,18 @@ static inline PORT_FN void poisson_step(const Port *P, int cur, int64_t k, int i
     real avg_isi = R(1.0) / rate;
     int64_t work_item = (int64_t)m->src_cell_seed[m->pois_src[k]];
     int64_t inst = m->pois_instance[k];
+    const int base = m->pois_rng_base ? m->pois_rng_base[k] : 0;
     real ts = P->pois_ts[cur][k], isi = P->pois_isi[cur][k];
     int fired = 0;
     if (init) {
         P->pois_ts[nxt][k] = R(0.0);
-        P->pois_isi[nxt][k] = (-avg_isi) * LOG(R(1.0) - randof(R(1.0), work_item, inst, step, 0));
+        P->pois_isi[nxt][k] = (-avg_isi) * LOG(R(1.0) - randof(R(1.0), work_item, inst, step, base));
     } else {
         P->pois_ts[nxt][k] = ts + dt * R(1.0);
         P->pois_isi[nxt][k] = isi;
         if (ts > isi) {
             P->pois_ts[nxt][k] = R(0.0);
-            P->pois_isi[nxt][k] = (-avg_isi) * LOG(R(1.0) - randof(R(1.0), work_item, inst, step, 1));
+            P->pois_isi[nxt][k] = (-avg_isi) * LOG(R(1.0) - randof(R(1.0), work_item, inst, step, base + 1));
             fired = 1;
         }
     }
@@ -313,6 +318,27 @@ static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, rea
             if (s <= t && t <= s + m->pulse_duration[k]) Ip += m->pulse_amplitude[k] * m->pulse_weight[k];
         }
         Iin += Ip;
+    }
+    /* sine and ramp generators: each adds its weighted current at once, the
+     * value its OnConditions assign at this step's time (OnStart's in the
+     * initialisation passes) */
+    for (int64_t k = P->wave_off[tgt]; k < P->wave_off[tgt + 1]; k++) {
+        const float *p = m->wave_params + (int64_t)EDEN_WAVE_PARAMS * k;
+        const real del = p[0], dur = p[1];
+        real i;
+        if (m->wave_shape[k] == EDEN_WAVE_SINE) {
+            const real amp = p[2], period = p[3], phase = p[4];
+            if (init || t < del) i = R(0.0);
+            else if (t < dur + del) i = (R(1.0) * amp) * SIN(phase + ((R(2.0) * R(3.14159265)) * (t - del)) / period);
+            else i = R(0.0);
+        } else {
+            const real start = p[2], finish = p[3], base = p[4];
+            if (init) i = base;
+            else if (t < del) i = R(1.0) * base;
+            else if (t < dur + del) i = R(1.0) * (start + ((finish - start) * (t - del)) / dur);
+            else i = R(1.0) * base;
+        }
+        Iin += i * (real)m->wave_weight[k];
     }
     /* Poisson inputs, one block per synapse type run */
     int64_t k = P->pois_off[tgt];
@@ -633,6 +659,7 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
     P.syn_off = csr_by_key(m->syn_target, ns, nt);
     P.pois_off = csr_by_key(m->pois_target, np, nt);
     P.pulse_off = csr_by_key(m->pulse_target, m->n_pulse, nt);
+    P.wave_off = csr_by_key(m->wave_target, m->n_wave, nt);
     P.fan_off = csr_by_key(m->syn_src, ns, m->n_src);
     P.fan_syn = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ns + 1));
     {
@@ -662,7 +689,7 @@ static void port_free(Port *P) {
         free(P->pois_a[b]); free(P->pois_b[b]); free(P->spiked[b]); free(P->timed_a[b]); free(P->timed_b[b]);
     }
     free(P->diag); free(P->syn_fire_count); free(P->gate_off); free(P->syn_off); free(P->pois_off);
-    free(P->pulse_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
+    free(P->pulse_off); free(P->wave_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
     free(P->timed_cur); free(P->timed_tgt_off); free(P->timed_order);
 }
 

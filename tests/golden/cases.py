@@ -17,6 +17,7 @@ CASES = {
     "event_sets": ("event_sets", dict(), 1.0, None),
     "point_neurons": ("point_neurons", dict(), 1.0, None),
     "timed_inputs": ("timed_inputs", dict(), 1.0, None),
+    "input_kinds": ("input_kinds", dict(), 1.0, None),
 }
 
 
