@@ -559,16 +559,17 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                 tm_off.append(tm_off[-1] + len(st))
 
     # ---- pulses ---------------------------------------------------------------
-    qt, qs, qd, qa = [], [], [], []
+    qt, qs, qd, qa, qw = [], [], [], [], []
     for pu in spec.pulses:
         qt.append(target_of(pu.cell, pu.seg))
         qs.append(ms_to_us(pu.delay).astype(F32))
         qd.append(ms_to_us(pu.duration).astype(F32))
         qa.append(np.asarray(pu.amplitude, np.float64).astype(F32))
-    qt, qs, qd, qa = cat(qt, np.int32), cat(qs, F32), cat(qd, F32), cat(qa, F32)
+        qw.append(np.ones(len(pu.cell), F32) if pu.weight is None else np.asarray(pu.weight, np.float64).astype(F32))
+    qt, qs, qd, qa, qw = cat(qt, np.int32), cat(qs, F32), cat(qd, F32), cat(qa, F32), cat(qw, F32)
     if len(qt):
         perm = np.argsort(qt, kind="stable")
-        qt, qs, qd, qa = qt[perm], qs[perm], qd[perm], qa[perm]
+        qt, qs, qd, qa, qw = qt[perm], qs[perm], qd[perm], qa[perm], qw[perm]
 
     # ---- sine / ramp generators ----------------------------------------------
     wt, wsh, wpar, wwt = [], [], [], []
@@ -616,7 +617,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         pois_target=pt, pois_type=pty, pois_rate=pr_, pois_weight=pw, pois_src=ps,
         pois_instance=pinst,
         pulse_target=qt, pulse_start=qs, pulse_duration=qd, pulse_amplitude=qa,
-        pulse_weight=np.ones(len(qt), F32),
+        pulse_weight=qw,
         trace_target=trace_target, event_src=event_src, gid_target_base=gid_base,
         chan_density=joined(chan_dens, np.int32), phys_ra=np.asarray(phys_ra, np.float64),
         ext_src=ext_src, ext_step=ext_step, izh_kind=np.asarray(izh_kind, np.int32),

@@ -238,13 +238,15 @@ class Projection:
 @dataclass
 class PulseInputs:
     """One pulseGenerator per entry (delay/duration ms, amplitude nA) on
-    cell gid `cell`, segment `seg`."""
+    cell gid `cell`, segment `seg`, scaled by `weight` (an inputW's; 1 when
+    None)."""
     pop: str
     cell: np.ndarray
     seg: np.ndarray
     delay: np.ndarray
     duration: np.ndarray
     amplitude: np.ndarray
+    weight: Optional[np.ndarray] = None
 
 
 @dataclass

@@ -193,6 +193,10 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w(f' <inputList id="il{n_list}" component="{pid}" population="{pop}">\n')
             n_list += 1
             for n, i in enumerate(idx):
+                if pi.weight is not None:
+                    w(f'  <inputW id="{n}" target="../{pop}[{local_of[pi.cell[i]]}]" segmentId="{pi.seg[i]}" '
+                      f'fractionAlong="0.5" destination="synapses" weight="{_f(pi.weight[i])}"/>\n')
+                    continue
                 w(f'  <input id="{n}" target="../{pop}[{local_of[pi.cell[i]]}]" segmentId="{pi.seg[i]}" '
                   f'fractionAlong="0.5" destination="synapses"/>\n')
             w(' </inputList>\n')
@@ -663,7 +667,7 @@ def read_lems(path: str) -> NetworkSpec:
                                            np.array(rows[1], np.int64), np.array(rows[2], np.int64),
                                            np.array(rows[3]), np.array(rows[4])))
     # inputs
-    pcell, pseg, pdel, pdur, pamp = [], [], [], [], []
+    pcell, pseg, pdel, pdur, pamp, pwt = [], [], [], [], [], []
     pois_rows, wave_rows = {}, {}
     timed_rows = {}
     for il in _children(net, "inputList"):
@@ -677,6 +681,7 @@ def read_lems(path: str) -> NetworkSpec:
             elif comp in pulses_def:
                 d, du, a = pulses_def[comp]
                 pcell.append(g); pseg.append(seg); pdel.append(d); pdur.append(du); pamp.append(a)
+                pwt.append(float(inp.get("weight", "1")))
             elif comp in pois_def:
                 pois_rows.setdefault(comp, []).append((g, seg))
             elif comp in wave_def:
@@ -689,10 +694,10 @@ def read_lems(path: str) -> NetworkSpec:
         if comp not in pulses_def:
             raise ValueError(f"explicitInput {comp} not supported")
         d, du, a = pulses_def[comp]
-        pcell.append(g); pseg.append(0); pdel.append(d); pdur.append(du); pamp.append(a)
+        pcell.append(g); pseg.append(0); pdel.append(d); pdur.append(du); pamp.append(a); pwt.append(1.0)
     if pcell:
         spec.pulses.append(PulseInputs("*", np.array(pcell), np.array(pseg), np.array(pdel), np.array(pdur),
-                                       np.array(pamp)))
+                                       np.array(pamp), None if all(x == 1.0 for x in pwt) else np.array(pwt)))
     for syn, rows in timed_rows.items():
         if syn not in synapses:
             raise ValueError(f"timedSynapticInput: synapse {syn} not supported")

@@ -478,9 +478,9 @@ def input_kinds(n_mc: int = 6, n_izh: int = 4, length_ms: float = 80.0, dt_ms: f
     spec.populations.append(Population("iz", "izRS", n_izh))
     mc = np.arange(n_mc)
     iz = n_mc + np.arange(n_izh)
-    # pulse on two somata
+    # weighted pulses (inputW) on two somata
     spec.pulses.append(PulseInputs("*", mc[:2], np.zeros(2, int), np.array([5.0, 30.0]), np.array([20.0, 40.0]),
-                                   np.array([0.25, 0.4])))
+                                   np.array([0.25, 0.4]), np.array([0.7, 1.3])))
     # sine generators: somata, a dendrite, izhikevich cells
     cells = np.concatenate([mc[:3], mc[3:5], iz[:2]])
     segs = np.concatenate([np.zeros(3, int), np.array([3, 5]), np.zeros(2, int)])

@@ -119,7 +119,7 @@ def test_neuroml_round_trip_keeps_waves_and_poisson_order(tmp_path):
     lems = neuroml_io.write_lems(spec, str(tmp_path))
     back = neuroml_io.read_lems(lems)
     a, b = lowering.lower(spec), lowering.lower(back)
-    for f in ("wave_target", "wave_shape", "wave_params", "wave_weight", "pois_target", "pois_rng_base",
+    for f in ("wave_target", "wave_shape", "wave_params", "wave_weight", "pulse_weight", "pois_target", "pois_rng_base",
               "pois_instance", "pois_rate", "timed_target"):
         np.testing.assert_array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(b, f)), err_msg=f)
 
