@@ -214,8 +214,18 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
         if (t.n_gates < 0 || t.n_gates > EDEN_MAX_GATES) return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d: gate count", k);
         for (int g = 0; g < t.n_gates; g++) {
             if (t.gate_instances[g] < 0 || t.gate_instances[g] > 16) return ctx->fail(EDEN_GPU_E_INVALID, "gate instances");
-            if (t.fwd_kind[g] < 0 || t.fwd_kind[g] > 2 || t.rev_kind[g] < 0 || t.rev_kind[g] > 2)
+            if (t.gate_kind[g] < 0 || t.gate_kind[g] >= EDEN_GATE_KINDS)
+                return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: gate kind %d", k, g, t.gate_kind[g]);
+            const int gk = t.gate_kind[g];
+            if (gk != EDEN_GATE_TAUINF &&
+                (t.fwd_kind[g] < 0 || t.fwd_kind[g] > 2 || t.rev_kind[g] < 0 || t.rev_kind[g] > 2))
                 return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: rate kind", k, g);
+            if ((gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESTAU || gk == EDEN_GATE_RATESTAUINF) &&
+                (t.tau_kind[g] < 0 || t.tau_kind[g] > EDEN_RATE_FIXED))
+                return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: timeCourse form", k, g);
+            if ((gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESINF || gk == EDEN_GATE_RATESTAUINF) &&
+                (t.inf_kind[g] < 0 || t.inf_kind[g] > EDEN_RATE_FIXED))
+                return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: steadyState form", k, g);
         }
     }
     int64_t nt = (int64_t)m->n_comp + m->n_izh;
@@ -710,9 +720,26 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int g = 0; g < ty.n_gates; g++) {
             float *r = &gate_par[((size_t)k * EDEN_MAX_GATES + g) * kGateWords];
             int32_t fk = ty.fwd_kind[g], rk = ty.rev_kind[g];
+            if (ty.gate_kind[g] != EDEN_GATE_RATES) fk |= (1 + k * EDEN_MAX_GATES + g) << 8;
             memcpy(&r[0], &fk, 4); r[1] = ty.fwd_rate[g]; r[2] = ty.fwd_mid[g]; r[3] = ty.fwd_scale[g];
             memcpy(&r[4], &rk, 4); r[5] = ty.rev_rate[g]; r[6] = ty.rev_mid[g]; r[7] = ty.rev_scale[g];
             r[8] = ty.q10[g];
+        }
+    }
+
+    // kinds and timeCourse / steadyState forms of the gates of other kinds
+    // than gateHHrates, by channel type and gate (gate_next_p)
+    std::vector<float> gate_ext((size_t)std::max(m->n_chan_types, 1) * EDEN_MAX_GATES * kGateExtWords, 0.f);
+    bool gate_forms = false;
+    for (int k = 0; k < m->n_chan_types; k++) {
+        const EdenGpuChannelType &ty = m->chan_types[k];
+        for (int g = 0; g < ty.n_gates; g++) {
+            float *r = &gate_ext[((size_t)k * EDEN_MAX_GATES + g) * kGateExtWords];
+            int32_t gk = ty.gate_kind[g], tk = ty.tau_kind[g], ik = ty.inf_kind[g];
+            gate_forms |= gk != EDEN_GATE_RATES;
+            memcpy(&r[0], &gk, 4);
+            memcpy(&r[1], &tk, 4); r[2] = ty.tau_rate[g]; r[3] = ty.tau_mid[g]; r[4] = ty.tau_scale[g];
+            memcpy(&r[5], &ik, 4); r[6] = ty.inf_rate[g]; r[7] = ty.inf_mid[g]; r[8] = ty.inf_scale[g];
         }
     }
 
@@ -1161,6 +1188,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.gr_t, gr_t)); TRY(upload_c(ctx, &d.gr_col, gr_col));
     TRY(upload_c(ctx, &d.un_nf0, un_nf0)); TRY(upload_c(ctx, &d.un_nf1, un_nf1)); TRY(upload_c(ctx, &d.nf_t, nf_t));
     TRY(upload_c(ctx, &d.lvl_info, lvl_info)); TRY(upload_c(ctx, &d.gate_par, gate_par));
+    TRY(upload_c(ctx, &d.gate_ext, gate_ext));
     TRY(upload_c(ctx, &d.nf_c0, nf_c0)); TRY(upload_c(ctx, &d.nf_c1, nf_c1)); TRY(upload_c(ctx, &d.nf_sig, nf_sig));
     TRY(upload_c(ctx, &d.nfc_g, nfc_g)); TRY(upload_c(ctx, &d.nfc_e, nfc_e));
     TRY(upload_c(ctx, &d.nfc_q, nfc_q)); TRY(upload_c(ctx, &d.nfc_i, nfc_i));
@@ -1180,6 +1208,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             ct[k].fk[g] = s.fwd_kind[g]; ct[k].fr[g] = s.fwd_rate[g]; ct[k].fm[g] = s.fwd_mid[g]; ct[k].fs[g] = s.fwd_scale[g];
             ct[k].rk[g] = s.rev_kind[g]; ct[k].rr[g] = s.rev_rate[g]; ct[k].rm[g] = s.rev_mid[g]; ct[k].rs[g] = s.rev_scale[g];
             ct[k].q10[g] = s.q10[g];
+            ct[k].gk[g] = s.gate_kind[g];
+            ct[k].tk[g] = s.tau_kind[g]; ct[k].tr[g] = s.tau_rate[g]; ct[k].tm[g] = s.tau_mid[g]; ct[k].ts[g] = s.tau_scale[g];
+            ct[k].ik[g] = s.inf_kind[g]; ct[k].ir[g] = s.inf_rate[g]; ct[k].im[g] = s.inf_mid[g]; ct[k].is[g] = s.inf_scale[g];
         }
     }
     SynTypeDev st[kMaxSynTypes];
@@ -1264,6 +1295,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             }
         }
         kinds.forest = d.n_forest > 0;
+        kinds.gateforms = gate_forms;
         kinds.izh = n_izh > 0;
         ctx->codegen_source = eden_codegen::program_source(eden_codegen::kind_defines(kinds) +
                                                            eden_codegen::channel_routines(m->chan_types, chan_sets));

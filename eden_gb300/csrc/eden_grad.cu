@@ -619,6 +619,11 @@ int validate(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
                        m->n_izh, (long long)m->n_syn, (long long)m->n_pois, (long long)m->n_timed,
                        (long long)m->n_wave);
     if (m->n_phys <= 0 || m->n_comp <= 0) return g->fail(EDEN_GPU_E_INVALID, "no physical cells");
+    for (int k = 0; k < m->n_chan_types; k++)
+        for (int q = 0; q < m->chan_types[k].n_gates && q < EDEN_MAX_GATES; q++)
+            if (m->chan_types[k].gate_kind[q] != EDEN_GATE_RATES)
+                return g->fail(EDEN_GPU_E_INVALID,
+                               "gradients cover gateHHrates gates: channel type %d gate %d is of another kind", k, q);
     if (m->phys_comp_off[0] != 0 || m->phys_comp_off[m->n_phys] != m->n_comp)
         return g->fail(EDEN_GPU_E_INVALID, "phys_comp_off must span [0, n_comp]");
     for (int c = 0; c < m->n_phys; c++) {

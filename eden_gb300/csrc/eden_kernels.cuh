@@ -36,6 +36,11 @@ struct ChanTypeDev {
     int rk[EDEN_MAX_GATES];
     float rr[EDEN_MAX_GATES], rm[EDEN_MAX_GATES], rs[EDEN_MAX_GATES];
     float q10[EDEN_MAX_GATES];
+    int gk[EDEN_MAX_GATES];  // EDEN_GATE_*, then the timeCourse and steadyState forms
+    int tk[EDEN_MAX_GATES];
+    float tr[EDEN_MAX_GATES], tm[EDEN_MAX_GATES], ts[EDEN_MAX_GATES];
+    int ik[EDEN_MAX_GATES];
+    float ir[EDEN_MAX_GATES], im[EDEN_MAX_GATES], is[EDEN_MAX_GATES];
 };
 struct SynTypeDev {
     int kind;
@@ -132,6 +137,7 @@ struct DevModel {
     int32_t pois_exact;               // dt is a whole number of us: Poisson clocks advance exactly
     float *ck_a, *ck_b;               // aggregate synapse state of each chunk (weighted sums)
     const float *pu_start, *pu_dur, *pu_amp, *pu_w;
+    const float *gate_ext;            // per channel type and gate, kGateExtWords (gate_next_p)
     const float *wv_p;                // sine / ramp generators, kWaveWords per item
     // Poisson inputs
     float *po_ts, *po_isi, *po_a, *po_b;  // po_a/po_b: own synapse state just after its last event
@@ -207,6 +213,7 @@ constexpr int kCepBeginShift = 10;
 constexpr int kCepParentShift = 20;
 constexpr uint32_t kCepNonFlat = 1u << 30;
 constexpr int kGateWords = 9;  // gate parameter record (gate_next_p)
+constexpr int kGateExtWords = 9;  // a non-rates gate's kind and timeCourse / steadyState forms
 
 // Shared-memory words of a unit's slice in the windowed kernel.  A forest:
 // 7 per compartment (V, c_kc, L, pivot, elimination factor, U, packed
@@ -469,6 +476,7 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
 // the model's, and the compiler drops the code of the others.
 #ifndef EDEN_KIND_PULSE
 #define EDEN_KIND_PULSE 1
+#define EDEN_KIND_GATEFORMS 1
 #define EDEN_KIND_SINE 1
 #define EDEN_KIND_RAMP 1
 #define EDEN_KIND_POIS 1
@@ -693,6 +701,10 @@ __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1,
 }
 
 __device__ __forceinline__ float gate_next(const ChanTypeDev &ct, int gi, bool init, float dt, float v, float qo) {
+    if (EDEN_KIND_GATEFORMS && ct.gk[gi] != EDEN_GATE_RATES)
+        return gate_general(ct.gk[gi], ct.fk[gi], ct.fr[gi], ct.fm[gi], ct.fs[gi], ct.rk[gi], ct.rr[gi], ct.rm[gi],
+                            ct.rs[gi], ct.tk[gi], ct.tr[gi], ct.tm[gi], ct.ts[gi], ct.ik[gi], ct.ir[gi], ct.im[gi],
+                            ct.is[gi], ct.q10[gi], init, dt, v, qo);
     const float alpha = rate_value(ct.fk[gi], ct.fr[gi], ct.fm[gi], ct.fs[gi], v);
     const float beta = rate_value(ct.rk[gi], ct.rr[gi], ct.rm[gi], ct.rs[gi], v);
     return gate_relax(alpha, beta, ct.q10[gi], init, dt, qo);
@@ -700,9 +712,20 @@ __device__ __forceinline__ float gate_next(const ChanTypeDev &ct, int gi, bool i
 
 // The same from a gate's 9-word parameter record (forward form, rate,
 // midpoint, scale; reverse form, rate, midpoint, scale; q10 factor), kept
-// in shared memory by the windowed kernel.
-__device__ __forceinline__ float gate_next_p(const float *P, bool init, float dt, float v, float qo) {
-    const float alpha = rate_value(__float_as_int(P[0]), P[1], P[2], P[3], v);
+// in shared memory by the windowed kernel.  A gate of another kind than
+// gateHHrates carries 1 + its row of `ext` (kind, timeCourse form and its
+// three values, steadyState form and its three values) in the bits of the
+// first word above the forward form.
+__device__ __forceinline__ float gate_next_p(const float *P, const float *ext, bool init, float dt, float v,
+                                             float qo) {
+    const int w0 = __float_as_int(P[0]);
+    if (EDEN_KIND_GATEFORMS && (w0 >> 8) != 0) {
+        const float *X = ext + (size_t)((w0 >> 8) - 1) * kGateExtWords;
+        return gate_general(__float_as_int(X[0]), w0 & 0xff, P[1], P[2], P[3], __float_as_int(P[4]), P[5], P[6], P[7],
+                            __float_as_int(X[1]), X[2], X[3], X[4], __float_as_int(X[5]), X[6], X[7], X[8], P[8],
+                            init, dt, v, qo);
+    }
+    const float alpha = rate_value(w0, P[1], P[2], P[3], v);
     const float beta = rate_value(__float_as_int(P[4]), P[5], P[6], P[7], v);
     return gate_relax(alpha, beta, P[8], init, dt, qo);
 }

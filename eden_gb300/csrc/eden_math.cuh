@@ -53,15 +53,40 @@ __device__ __forceinline__ float rate_value(int kind, float r, float mid, float 
 // One HH gate for one step (eden/Eden.cpp:5126-5259): exponential-Euler
 // relaxation towards inf(V) with time constant tau(V), clamped to
 // [1e-6, 1 - 1e-6]; initialisation sets it to inf(V).
-__device__ __forceinline__ float gate_relax(float alpha, float beta, float q10, bool init, float dt, float qo) {
-    const float tau = 1.0f / (alpha + beta);
-    const float inf = alpha / (alpha + beta);
+__device__ __forceinline__ float gate_relax_ti(float tau, float inf, float q10, bool init, float dt, float qo) {
     if (init) return inf;
     const float blend = expf(-((dt * q10) / tau));
     float qn = blend * qo + (1.0f - blend) * inf;
     if (!(qn > 1e-6f)) qn = 1e-6f;
     if (!(qn < (float)(1 - 1e-6))) qn = (float)(1 - 1e-6);
     return qn;
+}
+
+// A gate from its forward and reverse rates: tau = 1 / (a + b), inf = a / (a + b).
+__device__ __forceinline__ float gate_relax(float alpha, float beta, float q10, bool init, float dt, float qo) {
+    return gate_relax_ti(1.0f / (alpha + beta), alpha / (alpha + beta), q10, init, dt, qo);
+}
+
+// A timeCourse / steadyState form: a rate form, or a constant (fixedTimeCourse).
+__device__ __forceinline__ float form_value(int kind, float r, float mid, float s, float v) {
+    return kind == EDEN_RATE_FIXED ? r : rate_value(kind, r, mid, s, v);
+}
+
+// A gate of any kind (eden/Eden.cpp:5290-5375): tau and inf from its own
+// timeCourse / steadyState where the kind has them, else from the rates.
+__device__ __forceinline__ float gate_general(int gk, int fk, float fr, float fm, float fs, int rk, float rr, float rm,
+                                              float rs, int tk, float tr, float tm, float ts, int ik, float ir,
+                                              float im, float is, float q10, bool init, float dt, float v, float qo) {
+    float a = 0.0f, b = 0.0f;
+    if (gk != EDEN_GATE_TAUINF) {
+        a = rate_value(fk, fr, fm, fs, v);
+        b = rate_value(rk, rr, rm, rs, v);
+    }
+    const bool own_tau = gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESTAU || gk == EDEN_GATE_RATESTAUINF;
+    const bool own_inf = gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESINF || gk == EDEN_GATE_RATESTAUINF;
+    const float tau = own_tau ? form_value(tk, tr, tm, ts, v) : 1.0f / (a + b);
+    const float inf = own_inf ? form_value(ik, ir, im, is, v) : a / (a + b);
+    return gate_relax_ti(tau, inf, q10, init, dt, qo);
 }
 
 // Channel type table in constant memory (a handful of ionChannelHH types).

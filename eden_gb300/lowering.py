@@ -164,6 +164,11 @@ CHAN_DTYPE = np.dtype([
     ("rev_kind", np.int32, MAX_GATES), ("rev_rate", np.float32, MAX_GATES),
     ("rev_mid", np.float32, MAX_GATES), ("rev_scale", np.float32, MAX_GATES),
     ("q10", np.float32, MAX_GATES),
+    ("gate_kind", np.int32, MAX_GATES),
+    ("tau_kind", np.int32, MAX_GATES), ("tau_rate", np.float32, MAX_GATES),
+    ("tau_mid", np.float32, MAX_GATES), ("tau_scale", np.float32, MAX_GATES),
+    ("inf_kind", np.int32, MAX_GATES), ("inf_rate", np.float32, MAX_GATES),
+    ("inf_mid", np.float32, MAX_GATES), ("inf_scale", np.float32, MAX_GATES),
 ], align=True)
 
 SYN_DTYPE = np.dtype([
@@ -203,6 +208,26 @@ def _cable_geometry(cell: PhysicalCell):
 
 # point-neuron kinds and parameter layout (include/eden_gpu.h, EDEN_POINT_*)
 POINT_PARAMS = 16
+# gate kinds and the fixed rate form (include/eden_gpu.h EDEN_GATE_*, EDEN_RATE_FIXED)
+RATE_FIXED = 3
+GATE_KINDS = {"rates": 0, "tauInf": 1, "ratesTau": 2, "ratesInf": 3, "ratesTauInf": 4}
+
+
+def gate_q10(gate, temperature_degc: float) -> np.float32:
+    """A gate's rate scale: 1 without q10Settings, the fixed factor for
+    q10Fixed, and q10Factor^((T - experimentalTemp) / 10) for q10ExpTemp
+    with both temperatures in kelvin, in single precision as the
+    reference's kernel evaluates it (eden/Eden.cpp:5232-5246)."""
+    q = gate.q10
+    if q is None:
+        return F32(1.0)
+    if q[0] == "fixed":
+        return _to_f32(q[1])
+    t = _to_f32(temperature_degc + 273.15)
+    tb = _to_f32(q[2] + 273.15)
+    return F32(np.power(_to_f32(q[1]), F32(F32(t - tb) / F32(10.0))))
+
+
 # waveform inputs (include/eden_gpu.h EDEN_WAVE_*)
 WAVE_PARAMS = 5
 WAVE_SHAPES = {WAVE_SINE: 0, WAVE_RAMP: 1}
@@ -375,15 +400,34 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         ct["n_gates"] = len(ch.gates)
         for g, gate in enumerate(ch.gates):
             ct["gate_instances"][g] = gate.instances
-            ct["fwd_kind"][g] = gate.forward.kind
-            ct["fwd_rate"][g] = _to_f32(gate.forward.rate * 1e-3)   # per_ms -> per_us
-            ct["fwd_mid"][g] = _to_f32(gate.forward.midpoint)
-            ct["fwd_scale"][g] = _to_f32(gate.forward.scale)
-            ct["rev_kind"][g] = gate.reverse.kind
-            ct["rev_rate"][g] = _to_f32(gate.reverse.rate * 1e-3)
-            ct["rev_mid"][g] = _to_f32(gate.reverse.midpoint)
-            ct["rev_scale"][g] = _to_f32(gate.reverse.scale)
-            ct["q10"][g] = 1.0
+            if gate.kind not in GATE_KINDS:
+                raise ValueError(f"channel {ch.name} gate {gate.name}: unknown kind {gate.kind!r}")
+            needs = {"rates": (1, 0, 0), "tauInf": (0, 1, 1), "ratesTau": (1, 1, 0), "ratesInf": (1, 0, 1),
+                     "ratesTauInf": (1, 1, 1)}[gate.kind]
+            have = (gate.forward is not None and gate.reverse is not None, gate.tau is not None, gate.inf is not None)
+            if tuple(bool(x) for x in needs) != have:
+                want = [n for n, k in zip(("forward/reverse rates", "timeCourse", "steadyState"), needs) if k]
+                raise ValueError(f"channel {ch.name} gate {gate.name}: a {gate.kind} gate has exactly "
+                                 f"{', '.join(want)}")
+            if gate.forward is not None:
+                ct["fwd_kind"][g] = gate.forward.kind
+                ct["fwd_rate"][g] = _to_f32(gate.forward.rate * 1e-3)   # per_ms -> per_us
+                ct["fwd_mid"][g] = _to_f32(gate.forward.midpoint)
+                ct["fwd_scale"][g] = _to_f32(gate.forward.scale)
+                ct["rev_kind"][g] = gate.reverse.kind
+                ct["rev_rate"][g] = _to_f32(gate.reverse.rate * 1e-3)
+                ct["rev_mid"][g] = _to_f32(gate.reverse.midpoint)
+                ct["rev_scale"][g] = _to_f32(gate.reverse.scale)
+            ct["q10"][g] = gate_q10(gate, spec.temperature)
+            ct["gate_kind"][g] = GATE_KINDS[gate.kind]
+            if gate.tau is not None:      # fixedTimeCourse: tau in us
+                ct["tau_kind"][g] = RATE_FIXED
+                ct["tau_rate"][g] = _to_f32(gate.tau * 1000.0)
+            if gate.inf is not None:      # HH*Variable: dimensionless
+                ct["inf_kind"][g] = gate.inf.kind
+                ct["inf_rate"][g] = _to_f32(gate.inf.rate)
+                ct["inf_mid"][g] = _to_f32(gate.inf.midpoint)
+                ct["inf_scale"][g] = _to_f32(gate.inf.scale)
 
     # ---- cells, in gid order ------------------------------------------------
     phys_off = [0]
@@ -631,7 +675,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 4
+ABI_VERSION = 5
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)

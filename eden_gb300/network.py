@@ -50,10 +50,19 @@ class Rate:
 
 @dataclass
 class Gate:
+    """An HH gate.  `kind` is "rates" (gateHHrates), "tauInf", "ratesTau",
+    "ratesInf" or "ratesTauInf"; `tau` a fixedTimeCourse (ms) and `inf` an
+    HH*Variable steady state (dimensionless rate) where the kind has them;
+    `q10` None, ("fixed", factor) or ("exp", q10Factor, experimentalTemp
+    degC)."""
     name: str
     instances: int
-    forward: Rate
-    reverse: Rate
+    forward: Optional[Rate] = None
+    reverse: Optional[Rate] = None
+    kind: str = "rates"
+    tau: Optional[float] = None
+    inf: Optional[Rate] = None
+    q10: Optional[tuple] = None
 
 
 @dataclass
@@ -324,6 +333,7 @@ class NetworkSpec:
     poissons: List[PoissonInputs] = field(default_factory=list)
     timed: List[TimedInputs] = field(default_factory=list)
     waves: List[WaveInputs] = field(default_factory=list)
+    temperature: float = 6.3  # degC: the network's, or the reference's default when it has none
     trace_columns: List[OutputColumn] = field(default_factory=list)
     trace_file: str = "trajectory.txt"
     event_selections: List[EventSelection] = field(default_factory=list)

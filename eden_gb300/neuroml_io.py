@@ -55,11 +55,24 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             continue
         w(f'<ionChannelHH id="{ch.name}" conductance="10pS"{sp}>\n')
         for g in ch.gates:
-            w(f' <gateHHrates id="{g.name}" instances="{g.instances}">\n')
-            for tag, r in (("forwardRate", g.forward), ("reverseRate", g.reverse)):
-                w(f'  <{tag} type="{RATE_TYPE_NAMES[r.kind]}" rate="{_f(r.rate)}per_ms" '
-                  f'midpoint="{_f(r.midpoint)}mV" scale="{_f(r.scale)}mV"/>\n')
-            w(' </gateHHrates>\n')
+            tag = _GATE_TAGS[g.kind]
+            w(f' <{tag} id="{g.name}" instances="{g.instances}">\n')
+            if g.q10 is not None:
+                if g.q10[0] == "fixed":
+                    w(f'  <q10Settings type="q10Fixed" fixedQ10="{_f(g.q10[1])}"/>\n')
+                else:
+                    w(f'  <q10Settings type="q10ExpTemp" q10Factor="{_f(g.q10[1])}" '
+                      f'experimentalTemp="{_f(g.q10[2])} degC"/>\n')
+            if g.forward is not None:
+                for rtag, r in (("forwardRate", g.forward), ("reverseRate", g.reverse)):
+                    w(f'  <{rtag} type="{RATE_TYPE_NAMES[r.kind]}" rate="{_f(r.rate)}per_ms" '
+                      f'midpoint="{_f(r.midpoint)}mV" scale="{_f(r.scale)}mV"/>\n')
+            if g.tau is not None:
+                w(f'  <timeCourse type="fixedTimeCourse" tau="{_f(g.tau)}ms"/>\n')
+            if g.inf is not None:
+                w(f'  <steadyState type="{_VARIABLE_TYPE_NAMES[g.inf.kind]}" rate="{_f(g.inf.rate)}" '
+                  f'midpoint="{_f(g.inf.midpoint)}mV" scale="{_f(g.inf.scale)}mV"/>\n')
+            w(f' </{tag}>\n')
         w('</ionChannelHH>\n')
     for s in spec.synapses:
         if s.kind == SYN_EXPONE:
@@ -142,7 +155,11 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             else:
                 w(f'<rampGenerator id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" startAmplitude="{_f(a)}nA" '
                   f'finishAmplitude="{_f(b)}nA" baselineAmplitude="{_f(c)}nA"/>\n')
-    w('<network id="net">\n')
+    if spec.temperature != 6.3 or any(g.q10 is not None and g.q10[0] == "exp" for ch in spec.channels
+                                      for g in ch.gates):
+        w(f'<network id="net" type="networkWithTemperature" temperature="{_f(spec.temperature)} degC">\n')
+    else:
+        w('<network id="net">\n')
     readers = {}
     for p in spec.populations:
         ct = spec.cell_type(p.cell_type)
@@ -377,6 +394,29 @@ def _children(el, tag):
 _RATE_KIND = {v: k for k, v in RATE_TYPE_NAMES.items()}
 
 
+_GATE_TAGS = {"rates": "gateHHrates", "tauInf": "gateHHtauInf", "ratesTau": "gateHHratesTau",
+              "ratesInf": "gateHHratesInf", "ratesTauInf": "gateHHratesTauInf"}
+_GATE_KINDS = {v: k for k, v in _GATE_TAGS.items()}
+_VARIABLE_KIND = {"HHExpVariable": 0, "HHExpLinearVariable": 1, "HHSigmoidVariable": 2}
+_VARIABLE_TYPE_NAMES = {v: k for k, v in _VARIABLE_KIND.items()}
+
+
+def _parse_variable(el):
+    kind = el.get("type")
+    if kind not in _VARIABLE_KIND:
+        raise ValueError(f"steadyState type {kind!r} not supported ({', '.join(_VARIABLE_KIND)})")
+    return Rate(_VARIABLE_KIND[kind], _qty(el, "rate", None), _qty(el, "midpoint", "voltage"),
+                _qty(el, "scale", "voltage"))
+
+
+def _temperature_degc(text):
+    m = _QTY.match(text or "")
+    if not m or m.group(2) not in ("degC", "K"):
+        raise ValueError(f"temperature {text!r}: a number in degC or K is required")
+    value = float(m.group(1))
+    return value - 273.15 if m.group(2) == "K" else value
+
+
 def _parse_rate(el):
     kind = el.get("type")
     if kind not in _RATE_KIND:
@@ -534,11 +574,30 @@ def read_lems(path: str) -> NetworkSpec:
                 gt = _tag(g)
                 if gt in ("notes", "annotation"):
                     continue
-                if gt != "gateHHrates":
-                    raise ValueError(f"ionChannel {e.get('id')}: <{gt}> not supported (gateHHrates only)")
-                fwd = _parse_rate(_children(g, "forwardRate")[0])
-                rev = _parse_rate(_children(g, "reverseRate")[0])
-                gates.append(Gate(g.get("id"), int(g.get("instances", "1")), fwd, rev))
+                if gt not in _GATE_KINDS:
+                    raise ValueError(f"ionChannel {e.get('id')}: <{gt}> not supported "
+                                     f"({', '.join(sorted(_GATE_KINDS))})")
+                kind = _GATE_KINDS[gt]
+                fwd = rev = tau = inf = q10 = None
+                if kind != "tauInf":
+                    fwd = _parse_rate(_children(g, "forwardRate")[0])
+                    rev = _parse_rate(_children(g, "reverseRate")[0])
+                if kind in ("tauInf", "ratesTau", "ratesTauInf"):
+                    tc = _children(g, "timeCourse")[0]
+                    if tc.get("type") != "fixedTimeCourse":
+                        raise ValueError(f"ionChannel {e.get('id')} gate {g.get('id')}: timeCourse type "
+                                         f"{tc.get('type')!r} not supported (fixedTimeCourse)")
+                    tau = _qty(tc, "tau", "time")
+                if kind in ("tauInf", "ratesInf", "ratesTauInf"):
+                    inf = _parse_variable(_children(g, "steadyState")[0])
+                for qs in _children(g, "q10Settings"):
+                    if qs.get("type") == "q10Fixed":
+                        q10 = ("fixed", _qty(qs, "fixedQ10", None))
+                    elif qs.get("type") == "q10ExpTemp":
+                        q10 = ("exp", _qty(qs, "q10Factor", None), _temperature_degc(qs.get("experimentalTemp")))
+                    else:
+                        raise ValueError(f"q10Settings type {qs.get('type')!r} not supported")
+                gates.append(Gate(g.get("id"), int(g.get("instances", "1")), fwd, rev, kind, tau, inf, q10))
             channels_by_name[e.get("id")] = len(spec.channels)
             spec.channels.append(Channel(e.get("id"), gates, e.get("species")))
         elif t == "expOneSynapse":
@@ -594,13 +653,15 @@ def read_lems(path: str) -> NetworkSpec:
                                                 np.array([_qty(sp, "time", "time") for sp in _children(e, "spike")]))
         elif t == "spikeGenerator":
             cells[e.get("id")] = SpikeGeneratorCell(e.get("id"), _qty(e, "period", "time"))
-        elif t == "network" and e.get("id") == sim.get("target"):
+        elif t in ("network", "networkWithTemperature") and e.get("id") == sim.get("target"):
             net = e
     for e in elems:
         if _tag(e) == "cell":
             cells[e.get("id")] = _parse_cell(e, channels_by_name)
     if net is None:
         raise ValueError(f"network {sim.get('target')} not found")
+    if _tag(net) == "networkWithTemperature" or net.get("type") == "networkWithTemperature":
+        spec.temperature = _temperature_degc(net.get("temperature"))
     spec.synapses = list(synapses.values())
     syn_names = list(synapses)
     # populations (declaration order = gid order)

@@ -30,6 +30,10 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    passive dendrites) and on izhikevich cells: pulse, sine and
                    ramp generators, several Poisson components sharing
                    compartments, and timed inputs on passive dendrites.
+  gate_kinds       channels with every built-in gate kind (gateHHrates,
+                   gateHHtauInf, gateHHratesTau, gateHHratesInf,
+                   gateHHratesTauInf), q10Fixed and q10ExpTemp settings at
+                   16.3 degC, on single-compartment and branching cells.
 
 Every generator takes scale arguments (cell count, in-degree, length) so the
 same distributions produce the small cases the CPU reference can finish.
@@ -40,7 +44,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .network import (AdExCell, ChannelDensity, EventSelection, IafCell, Izhikevich2007Cell,
+from .network import (RATE_EXP, RATE_EXPLINEAR, RATE_SIGMOID, AdExCell, Channel, ChannelDensity, EventSelection,
+                      Gate, IafCell, Izhikevich2007Cell, Rate,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
                       SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, TimedInputs, WAVE_RAMP,
@@ -530,6 +535,74 @@ def input_kinds(n_mc: int = 6, n_izh: int = 4, length_ms: float = 80.0, dt_ms: f
     return spec
 
 
+def gate_kind_channels() -> list:
+    """Leak plus sodium, delayed-rectifier and A-type potassium channels
+    whose gates use each built-in gate kind and both q10 settings."""
+    q10 = ("exp", 3.0, 6.3)
+    leak = Channel("passiveChan")
+    na = Channel("naT", [
+        Gate("m", 3, Rate(RATE_EXPLINEAR, 1.0, -40.0, 10.0), Rate(RATE_EXP, 4.0, -65.0, -18.0), "ratesInf",
+             inf=Rate(RATE_SIGMOID, 1.0, -40.0, 9.0), q10=q10),
+        Gate("h", 1, kind="tauInf", tau=3.0, inf=Rate(RATE_SIGMOID, 1.0, -62.0, -7.0), q10=q10),
+    ], species="na")
+    kdr = Channel("kdr", [
+        Gate("n", 4, Rate(RATE_EXPLINEAR, 0.1, -55.0, 10.0), Rate(RATE_EXP, 0.125, -65.0, -80.0), "ratesTau",
+             tau=3.5, q10=("fixed", 1.5)),
+    ], species="k")
+    ka = Channel("kA", [
+        Gate("a", 3, Rate(RATE_EXP, 0.2, -50.0, 20.0), Rate(RATE_SIGMOID, 0.3, -70.0, -10.0), "ratesTauInf",
+             tau=2.0, inf=Rate(RATE_SIGMOID, 1.0, -45.0, 12.0), q10=q10),
+        Gate("b", 1, Rate(RATE_EXP, 0.02, -80.0, -15.0), Rate(RATE_SIGMOID, 0.05, -60.0, 8.0), q10=q10),
+    ], species="k")
+    return [leak, na, kdr, ka]
+
+
+def gate_kinds(n_single: int = 8, n_branch: int = 4, length_ms: float = 60.0, dt_ms: float = 0.025,
+               seed: int = 1234, temperature: float = 16.3) -> NetworkSpec:
+    """Cells whose channels use every built-in gate kind (gate_kind_channels)
+    at 16.3 degC: single compartments with DC pulses of seeded amplitude and
+    branching cells with the active channels on soma and first dendrite,
+    Poisson drive and connections among all cells."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("gate_kinds", dt_ms, length_ms, seed, channels=gate_kind_channels())
+    spec.temperature = temperature
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=3.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+
+    def dens(n_seg, active):
+        allseg = np.ones(n_seg, bool)
+        return [ChannelDensity(0, 0.3, -54.387, allseg), ChannelDensity(1, 120.0, 50.0, active.copy()),
+                ChannelDensity(2, 36.0, -77.0, active.copy()), ChannelDensity(3, 8.0, -77.0, active.copy())]
+
+    one = np.ones(1, bool)
+    spec.cells.append(PhysicalCell("single", np.array([-1]), np.array([0.0]), np.array([17.8]), dens(1, one),
+                                   cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0))
+    parent = np.array([-1, 0, 1, 1, 0])
+    active = np.array([True, True, False, False, False])
+    spec.cells.append(PhysicalCell("branch", parent, np.array([20.0, 40.0, 60.0, 60.0, 80.0]),
+                                   np.array([20.0, 3.0, 1.5, 1.5, 2.0]), dens(len(parent), active), cm=1.0,
+                                   ra=120.0, v0=-65.0, spike_thresh=-20.0,
+                                   seg_groups={"soma_group": parent < 0, "dend_group": parent >= 0,
+                                               "active_group": active}))
+    spec.populations.append(Population("single", "single", n_single))
+    spec.populations.append(Population("branch", "branch", n_branch))
+    n = n_single + n_branch
+    spec.pulses.append(PulseInputs("*", np.arange(n_single), np.zeros(n_single, int),
+                                   np.round(rng.uniform(0.0, 10.0, n_single), 3), np.full(n_single, length_ms),
+                                   np.round(rng.uniform(0.05, 0.35, n_single), 4)))
+    br = n_single + np.arange(n_branch)
+    spec.poissons.append(PoissonInputs("*", "syn_e2", 400.0, np.repeat(br, 4), np.tile([0, 0, 2, 4], n_branch)))
+    post = np.repeat(np.arange(n), 2)
+    pre = rng.integers(0, n, size=post.size)
+    pre = np.where(pre == post, (pre + 1) % n, pre)
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre, post, "syn_e2",
+                                             np.round(rng.uniform(0.1, 0.5, post.size), 4),
+                                             _round_us(rng.uniform(0.5, 3.0, size=post.size))))
+    cols = [(g, 0) for g in range(0, n_single, 2)] + [(int(br[0]), 0), (int(br[1]), 2), (int(br[2]), 4)]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), seg) for g, seg in cols]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
@@ -541,4 +614,5 @@ CONFIGS = {
     "point_neurons": point_neurons,
     "timed_inputs": timed_inputs,
     "input_kinds": input_kinds,
+    "gate_kinds": gate_kinds,
 }

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 4
+#define EDEN_GPU_ABI_VERSION 5
 
 enum {
     EDEN_GPU_OK = 0,
@@ -45,7 +45,20 @@ enum {
 enum {
     EDEN_RATE_EXP = 0,        /* r * exp((V - mid) / s)                     */
     EDEN_RATE_EXPLINEAR = 1,  /* r * x / (1 - exp(-x)), x = (V - mid) / s; r at V == mid */
-    EDEN_RATE_SIGMOID = 2     /* r / (1 + exp((mid - V) / s))               */
+    EDEN_RATE_SIGMOID = 2,    /* r / (1 + exp((mid - V) / s))               */
+    EDEN_RATE_FIXED = 3       /* r (fixedTimeCourse: tau, us)               */
+};
+
+/* Gate kinds (eden/NeuroML.cpp:4172-4177; dynamics eden/Eden.cpp:5290-5375):
+ * each derives tau and inf from the forward/reverse rates (tau = 1/(a+b),
+ * inf = a/(a+b)) unless it has its own timeCourse / steadyState form. */
+enum {
+    EDEN_GATE_RATES = 0,        /* gateHHrates: forward, reverse            */
+    EDEN_GATE_TAUINF = 1,       /* gateHHtauInf: timeCourse, steadyState    */
+    EDEN_GATE_RATESTAU = 2,     /* gateHHratesTau: rates, timeCourse        */
+    EDEN_GATE_RATESINF = 3,     /* gateHHratesInf: rates, steadyState       */
+    EDEN_GATE_RATESTAUINF = 4,  /* gateHHratesTauInf: all four              */
+    EDEN_GATE_KINDS = 5
 };
 
 #define EDEN_MAX_GATES 4
@@ -85,7 +98,12 @@ typedef struct EdenGpuChannelType {
     float fwd_rate[EDEN_MAX_GATES], fwd_mid[EDEN_MAX_GATES], fwd_scale[EDEN_MAX_GATES];
     int32_t rev_kind[EDEN_MAX_GATES];
     float rev_rate[EDEN_MAX_GATES], rev_mid[EDEN_MAX_GATES], rev_scale[EDEN_MAX_GATES];
-    float q10[EDEN_MAX_GATES];
+    float q10[EDEN_MAX_GATES];      /* rate scale of each gate (q10Settings at the network's temperature) */
+    int32_t gate_kind[EDEN_MAX_GATES];                                   /* EDEN_GATE_* */
+    int32_t tau_kind[EDEN_MAX_GATES];                                    /* timeCourse form */
+    float tau_rate[EDEN_MAX_GATES], tau_mid[EDEN_MAX_GATES], tau_scale[EDEN_MAX_GATES];
+    int32_t inf_kind[EDEN_MAX_GATES];                                    /* steadyState form (rate dimensionless) */
+    float inf_rate[EDEN_MAX_GATES], inf_mid[EDEN_MAX_GATES], inf_scale[EDEN_MAX_GATES];
 } EdenGpuChannelType;
 
 enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1 };

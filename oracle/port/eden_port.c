@@ -9,6 +9,7 @@
  *
  *   step loop, 4 init passes, now/next swap   eden/Eden.cpp:11488-11938
  *   HH gates (exp-Euler, clamp) + currents    eden/Eden.cpp:5126-5259, 5678-5717, 5805-5898
+ *   gate kinds (tau/inf forms), q10           eden/Eden.cpp:5223-5246, 5290-5375
  *   voltage pre-update                        eden/Eden.cpp:6057-6107
  *   Hines backward-Euler tree solve           eden/Eden.cpp:6114-6225 (order 4416-4473)
  *   synapse trigger + single pending spike    eden/Eden.cpp:3646-3686
@@ -91,6 +92,7 @@ static PORT_FN real rate_value(int kind, real r, real mid, real s, real v) {
         case EDEN_RATE_EXP: return r * EXP((v - mid) / s);
         case EDEN_RATE_EXPLINEAR:
             return r * ((v == mid) ? R(1.0) : (((v - mid) / s) / (R(1.0) - EXP(-(v - mid) / s))));
+        case EDEN_RATE_FIXED: return r;
         default: return r / (R(1.0) + EXP((mid - v) / s));
     }
 }
@@ -415,10 +417,23 @@ static PORT_FN void phys_cell_step(Port *P, int cur, int32_t cell, int init, rea
             int64_t go = P->gate_off[ch];
             for (int g = 0; g < ct->n_gates; g++) {
                 real q = P->gate[cur][go + g];
-                real alpha = rate_value(ct->fwd_kind[g], ct->fwd_rate[g], ct->fwd_mid[g], ct->fwd_scale[g], Vc);
-                real beta = rate_value(ct->rev_kind[g], ct->rev_rate[g], ct->rev_mid[g], ct->rev_scale[g], Vc);
-                real tau = R(1.0) / (alpha + beta);
-                real inf = alpha / (alpha + beta);
+                /* tau and inf from the rates unless the gate kind has its
+                 * own timeCourse / steadyState (eden/Eden.cpp:5290-5375) */
+                const int gk = ct->gate_kind[g];
+                real alpha = R(0.0), beta = R(0.0);
+                if (gk != EDEN_GATE_TAUINF) {
+                    alpha = rate_value(ct->fwd_kind[g], ct->fwd_rate[g], ct->fwd_mid[g], ct->fwd_scale[g], Vc);
+                    beta = rate_value(ct->rev_kind[g], ct->rev_rate[g], ct->rev_mid[g], ct->rev_scale[g], Vc);
+                }
+                real tau, inf;
+                if (gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESTAU || gk == EDEN_GATE_RATESTAUINF)
+                    tau = rate_value(ct->tau_kind[g], ct->tau_rate[g], ct->tau_mid[g], ct->tau_scale[g], Vc);
+                else
+                    tau = R(1.0) / (alpha + beta);
+                if (gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESINF || gk == EDEN_GATE_RATESTAUINF)
+                    inf = rate_value(ct->inf_kind[g], ct->inf_rate[g], ct->inf_mid[g], ct->inf_scale[g], Vc);
+                else
+                    inf = alpha / (alpha + beta);
                 real qn;
                 if (init) {
                     qn = inf;

@@ -18,6 +18,7 @@ CASES = {
     "point_neurons": ("point_neurons", dict(), 1.0, None),
     "timed_inputs": ("timed_inputs", dict(), 1.0, None),
     "input_kinds": ("input_kinds", dict(), 1.0, None),
+    "gate_kinds": ("gate_kinds", dict(), 1.0, None),
 }
 
 

@@ -28,11 +28,37 @@ def test_library_exports_all_symbols():
     assert lib.edenGpuAbiVersion() == lowering.ABI_VERSION
 
 
-def test_struct_layouts_match_header():
-    # sizes of the ctypes mirrors against offsets a C compiler computes
-    assert ctypes.sizeof(lowering.CModel) % 8 == 0
-    assert lowering.CHAN_DTYPE.itemsize == 4 + 10 * 4 * 4
-    assert lowering.SYN_DTYPE.itemsize == 7 * 4
+def _c_layout(tmp_path, struct, fields):
+    """sizeof(struct) and offsetof(struct, f) for each field, as the C
+    compiler lays out include/eden_gpu.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "probe.c"
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "eden_gpu.h"', "int main(void) {",
+             f'  printf("%zu\\n", sizeof({struct}));']
+    lines += [f'  printf("%zu\\n", offsetof({struct}, {f}));' for f in fields]
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", os.path.join(root, "include"), str(src), "-o", str(exe)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    return out[0], out[1:]
+
+
+def test_struct_layouts_match_header(tmp_path):
+    # the ctypes / numpy mirrors against the offsets a C compiler computes
+    for dtype, struct in ((lowering.CHAN_DTYPE, "EdenGpuChannelType"), (lowering.SYN_DTYPE, "EdenGpuSynapseType")):
+        size, offs = _c_layout(tmp_path, struct, dtype.names)
+        assert dtype.itemsize == size, struct
+        assert [dtype.fields[f][1] for f in dtype.names] == offs, struct
+    names = [f[0] for f in lowering.CModel._fields_]
+    size, offs = _c_layout(tmp_path, "EdenGpuModel", names)
+    assert ctypes.sizeof(lowering.CModel) == size
+    assert [getattr(lowering.CModel, f).offset for f in names] == offs
 
 
 def test_create_without_gpu_fails_loudly():
