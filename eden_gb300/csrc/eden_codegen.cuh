@@ -121,7 +121,7 @@ inline std::string channel_routines(const EdenGpuChannelType *types, const std::
 // compiles only their code (the EDEN_KIND_* switches of eden_kernels.cuh).
 struct Kinds {
     bool pulse = false, sine = false, ramp = false, pois = false, timed = false, syn = false, expone = false,
-         exptwo = false, forest = false, izh = false, gateforms = false;
+         exptwo = false, forest = false, izh = false, gateforms = false, clamp = false;
 };
 
 inline std::string kind_defines(const Kinds &k) {
@@ -129,6 +129,7 @@ inline std::string kind_defines(const Kinds &k) {
     auto def = [&](const char *name, bool on) { s += std::string("#define ") + name + (on ? " 1\n" : " 0\n"); };
     def("EDEN_KIND_PULSE", k.pulse);
     def("EDEN_KIND_GATEFORMS", k.gateforms);
+    def("EDEN_KIND_CLAMP", k.clamp);
     def("EDEN_KIND_SINE", k.sine);
     def("EDEN_KIND_RAMP", k.ramp);
     def("EDEN_KIND_POIS", k.pois);

@@ -308,6 +308,17 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
         for (int j = 0; j < EDEN_WAVE_PARAMS; j++) finite = finite && std::isfinite(m->wave_params[EDEN_WAVE_PARAMS * k + j]);
         if (!finite) return ctx->fail(EDEN_GPU_E_INVALID, "waveform input %lld: non-finite parameter", (long long)k);
     }
+    if (m->n_clamp < 0) return ctx->fail(EDEN_GPU_E_INVALID, "n_clamp must be >= 0");
+    if (m->n_clamp > 0 && (!m->clamp_target || !m->clamp_params || !m->clamp_weight))
+        return ctx->fail(EDEN_GPU_E_INVALID, "voltage clamps: null array");
+    for (int64_t k = 0; k < m->n_clamp; k++) {
+        const float *p = m->clamp_params + EDEN_CLAMP_PARAMS * k;
+        if (m->clamp_target[k] < 0 || m->clamp_target[k] >= nt)
+            return ctx->fail(EDEN_GPU_E_INVALID, "voltage clamp %lld: bad target", (long long)k);
+        if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[5]) || p[5] == 0.0f ||
+            !std::isfinite(m->clamp_weight[k]) || std::isinf(p[2]) || std::isinf(p[3]) || std::isinf(p[4]))
+            return ctx->fail(EDEN_GPU_E_INVALID, "voltage clamp %lld: bad parameter", (long long)k);
+    }
     if (m->pois_rng_base)
         for (int64_t k = 0; k < m->n_pois; k++)
             if (m->pois_rng_base[k] < 0)
@@ -404,6 +415,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (int64_t k = 0; k < m->n_timed; k++) n_in_user[m->timed_target[k]]++;
     for (int64_t k = 0; k < m->n_pulse; k++) n_in_user[m->pulse_target[k]]++;
     for (int64_t k = 0; k < m->n_wave; k++) n_in_user[m->wave_target[k]]++;
+    for (int64_t k = 0; k < m->n_clamp; k++) n_in_user[m->clamp_target[k]] += 2;
     std::vector<double> cost(n_cells, 0.0);
     double total = 0;
     int max_cell = 1;
@@ -656,6 +668,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = 0; k < m->n_syn; k++) has_input[u2i[m->syn_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_timed; k++) has_input[u2i[m->timed_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_wave; k++) has_input[u2i[m->wave_target[k]]] = 1;
+        for (int64_t k = 0; k < m->n_clamp; k++) has_input[u2i[m->clamp_target[k]]] = 1;
         for (int it = 0; it < nt; it++) {
             if (t_izh[it] >= 0 || has_input[it]) continue;
             if (c_chan0[it + 1] - c_chan0[it] != 1) continue;
@@ -799,6 +812,15 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         wv_p[k * kWaveWords + EDEN_WAVE_PARAMS] = m->wave_weight[o];
         wv_shape[k] = (uint8_t)m->wave_shape[o];
     }
+    // voltage clamps by internal target (input order within a target)
+    std::vector<int64_t> clord = sort_items(m->n_clamp, m->clamp_target, nullptr);
+    std::vector<int64_t> cloff = offsets(clord, m->clamp_target);
+    std::vector<float> cl_p((size_t)m->n_clamp * kClampWords, 0.f);
+    for (int64_t k = 0; k < m->n_clamp; k++) {
+        const int64_t o = clord[k];
+        for (int j = 0; j < EDEN_CLAMP_PARAMS; j++) cl_p[k * kClampWords + j] = m->clamp_params[EDEN_CLAMP_PARAMS * o + j];
+        cl_p[k * kClampWords + EDEN_CLAMP_PARAMS] = m->clamp_weight[o];
+    }
     std::vector<float> po_rate(m->n_pois), po_w(m->n_pois);
     std::vector<int32_t> po_seed(m->n_pois), po_inst(m->n_pois), po_rng(m->n_pois);
     std::vector<uint8_t> po_type(m->n_pois);
@@ -869,6 +891,12 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             bk_kind.push_back(BK_PULSE); bk_erev.push_back(0.f); bk_type.push_back(0);
             bk_i0.push_back(qoff[t]); bk_i1.push_back(qoff[t + 1]);
         }
+        if (cloff[t + 1] > cloff[t]) {
+            bk_kind.push_back(BK_PULSE); bk_erev.push_back(0.f); bk_type.push_back((uint8_t)kClampA);
+            bk_i0.push_back(cloff[t]); bk_i1.push_back(cloff[t + 1]);
+            bk_kind.push_back(BK_CLAMPV); bk_erev.push_back(0.f); bk_type.push_back((uint8_t)kClampB);
+            bk_i0.push_back(cloff[t]); bk_i1.push_back(cloff[t + 1]);
+        }
         for (int64_t k = woff[t]; k < woff[t + 1];) {
             int64_t k1 = k;
             while (k1 < woff[t + 1] && wv_shape[k1] == wv_shape[k]) k1++;
@@ -916,7 +944,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     const int n_chunk = (int)ck_blk.size();
     std::vector<int32_t> ck_info(n_chunk);
     for (int c = 0; c < n_chunk; c++)
-        ck_info[c] = bk_kind[ck_blk[c]] | ((int32_t)bk_type[ck_blk[c]] << 2) | (ck_n[c] << 8);
+        ck_info[c] = (bk_kind[ck_blk[c]] == BK_CLAMPV ? BK_PULSE : bk_kind[ck_blk[c]]) |
+                     ((int32_t)bk_type[ck_blk[c]] << 2) | (ck_n[c] << 8);
 
     // ---- window length: every delay must cover the window (see k_window)
     int kmax = kMaxWindow;
@@ -1135,6 +1164,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.po_seed, po_seed)); TRY(upload_c(ctx, &d.po_inst, po_inst));
     TRY(upload_c(ctx, &d.po_rng, po_rng));
     TRY(upload_c(ctx, &d.wv_p, wv_p));
+    TRY(upload_c(ctx, &d.cl_p, cl_p));
     TRY(upload_c(ctx, &d.po_type, po_type));
     TRY(upload(ctx, &d.tm_a, (const float *)nullptr, (size_t)m->n_timed));
     TRY(upload(ctx, &d.tm_b, (const float *)nullptr, (size_t)m->n_timed));
@@ -1283,12 +1313,13 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int b = 0; b < n_block; b++) {
             const int kb = bk_kind[b];
             kinds.pulse |= kb == BK_PULSE && bk_type[b] == 0;
+            kinds.clamp |= kb == BK_CLAMPV;
             kinds.sine |= kb == BK_PULSE && bk_type[b] == 1 + EDEN_WAVE_SINE;
             kinds.ramp |= kb == BK_PULSE && bk_type[b] == 1 + EDEN_WAVE_RAMP;
             kinds.pois |= kb == BK_POIS;
             kinds.timed |= kb == BK_TIMED;
             kinds.syn |= kb == BK_SYN;
-            if (kb != BK_PULSE) {
+            if (kb != BK_PULSE && kb != BK_CLAMPV) {
                 const int sk = m->syn_types[bk_type[b]].kind;
                 kinds.expone |= sk == EDEN_SYN_EXPONE;
                 kinds.exptwo |= sk == EDEN_SYN_EXPTWO;

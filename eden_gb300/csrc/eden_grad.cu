@@ -612,7 +612,7 @@ int validate(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
     if (m->abi_version != EDEN_GPU_ABI_VERSION)
         return g->fail(EDEN_GPU_E_INVALID, "ABI version %d, library is %d", m->abi_version, EDEN_GPU_ABI_VERSION);
     if (!finite_pos(m->dt)) return g->fail(EDEN_GPU_E_INVALID, "dt must be positive");
-    if (m->n_izh != 0 || m->n_syn != 0 || m->n_pois != 0 || m->n_timed != 0 || m->n_wave != 0)
+    if (m->n_izh != 0 || m->n_syn != 0 || m->n_pois != 0 || m->n_timed != 0 || m->n_wave != 0 || m->n_clamp != 0)
         return g->fail(EDEN_GPU_E_INVALID,
                        "gradients cover independent physical cells with HH channels and pulse inputs: the model has "
                        "%d point neurons, %lld synapses, %lld Poisson, %lld timed and %lld waveform inputs",

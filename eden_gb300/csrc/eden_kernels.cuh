@@ -71,10 +71,16 @@ __device__ __forceinline__ float div_by_tau(float x, float tau, float r) {
 
 enum : int { ST_OK = 0, ST_LOG_OVERFLOW = 1 };
 enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2, BK_TIMED = 3 };
+// block-level only: a voltage clamp's sum of weight / R, applied as -V g
+// (its chunks run as pulse-block type kClampB)
+enum : int { BK_CLAMPV = 4 };
+// pulse-block types: 0 pulses, then the waveform shapes, then the two halves of a clamp
+enum : int { kPulseSine = 1 + EDEN_WAVE_SINE, kPulseRamp = 1 + EDEN_WAVE_RAMP, kClampA = 3, kClampB = 4 };
 constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
 constexpr int kChunkItems = 128; // input items per chunk (one warp, up to four per lane)
 constexpr int kPowLen = 33;      // powers 0..32 of a synapse decay factor
 constexpr int kWaveWords = 8;    // waveform input record: delay, duration, 3 shape parameters, weight, 2 spare
+constexpr int kClampWords = 8;   // clamp record: delay, duration, 3 phase targets, R, weight, spare
 
 struct DevModel {
     int32_t n_target, n_src, n_group, n_forest, n_in;
@@ -139,6 +145,7 @@ struct DevModel {
     const float *pu_start, *pu_dur, *pu_amp, *pu_w;
     const float *gate_ext;            // per channel type and gate, kGateExtWords (gate_next_p)
     const float *wv_p;                // sine / ramp generators, kWaveWords per item
+    const float *cl_p;                // voltage clamps, kClampWords per item
     // Poisson inputs
     float *po_ts, *po_isi, *po_a, *po_b;  // po_a/po_b: own synapse state just after its last event
     int32_t *po_last;                      // step of that event
@@ -477,6 +484,7 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
 #ifndef EDEN_KIND_PULSE
 #define EDEN_KIND_PULSE 1
 #define EDEN_KIND_GATEFORMS 1
+#define EDEN_KIND_CLAMP 1
 #define EDEN_KIND_SINE 1
 #define EDEN_KIND_RAMP 1
 #define EDEN_KIND_POIS 1
@@ -533,12 +541,39 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     const int kind = info & 3;
     const int n = info >> 8;
     float *rowA = tileA + lane * kAccStride, *rowB = tileB + lane * kAccStride;
+    if (EDEN_KIND_CLAMP && kind == BK_PULSE && ((info >> 2) & 63) >= kClampA) {
+        // voltage clamps (LEMS_CoreComponents.inc.xml:555-620): the target
+        // of the phase each step's time is in (the last OnCondition that
+        // holds assigns); half A sums weight * target / R, half B weight / R,
+        // and the cell kernel takes A - V B at the step's starting V
+        const bool half_a = ((info >> 2) & 63) == kClampA;
+        for (int r = 0; lane + 32 * r < n; r++) {
+            const float *p = m.cl_p + (size_t)(ck_i0 + lane + 32 * r) * kClampWords;
+            const float del = p[0], dur = p[1], vb = p[2], vd = p[3], va = p[4], res = p[5], wt = p[6];
+            for (int j = 0; j < w.K; j++) {
+                const float tf = tk[j];
+                const float tv = (tf > dur + del) ? va : (tf < del) ? vb : vd;
+                const bool on = w.step0 + j > 0 && tv == tv;
+                const float term = on ? __fmul_rn(half_a ? tv / res : 1.0f / res, wt) : 0.0f;
+                rowA[j] = r > 0 ? rowA[j] + term : term;
+            }
+        }
+        __syncwarp();
+        if (lane < w.K) {
+            const int rows = n < 32 ? n : 32;
+            float tot = 0.0f;
+            for (int r = 0; r < rows; r++) tot += tileA[r * kAccStride + lane];
+            m.Gp[(size_t)lane * m.n_chunk + c] = tot;
+        }
+        __syncwarp();
+        return;
+    }
     if ((EDEN_KIND_SINE || EDEN_KIND_RAMP) && kind == BK_PULSE && ((info >> 2) & 63) != 0) {
         // sineGenerator / rampGenerator (LEMS_CoreComponents.inc.xml:430-458,
         // 489-521): the value the OnConditions assign at the step's time,
         // which the reference's LEMS code exposes in the same step; OnStart's
         // in the initialisation passes
-        const bool sine = ((info >> 2) & 63) == 1 + EDEN_WAVE_SINE;
+        const bool sine = ((info >> 2) & 63) == kPulseSine;
         for (int r = 0; lane + 32 * r < n; r++) {
             const float *p = m.wv_p + (size_t)(ck_i0 + lane + 32 * r) * kWaveWords;
             const float del = p[0], dur = p[1], a = p[2], b = p[3], cc = p[4], wt = p[5];
@@ -690,6 +725,8 @@ __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1,
         const int kind = BK_K[bk];
         if (kind == BK_PULSE) {
             Iin += g;
+        } else if (EDEN_KIND_CLAMP && kind == BK_CLAMPV) {
+            Iin -= v * g;
         } else if (kind == BK_POIS || kind == BK_TIMED) {
             Iin += g * (BK_E[bk] - v);
             Gin += g;

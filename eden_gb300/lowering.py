@@ -139,6 +139,10 @@ class LoweredModel:
     wave_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     # per Poisson input, the random-call id of its first draw
     pois_rng_base: np.ndarray = field(default=None)
+    # voltage clamps: target, [n, CLAMP_PARAMS] parameters (engine units), weight
+    clamp_target: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    clamp_params: np.ndarray = field(default_factory=lambda: np.zeros((0, 6), np.float32))
+    clamp_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
 
     @property
     def n_comp(self) -> int:
@@ -637,6 +641,26 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         perm = np.argsort(wt, kind="stable")
         wt, wsh, wpar, wwt = wt[perm], wsh[perm], wpar[perm], wwt[perm]
 
+    # ---- voltage clamps ---------------------------------------------------------
+    ct_, cpar, cwt = [], [], []
+    for cl in spec.clamps:
+        n = len(cl.cell)
+        ct_.append(target_of(cl.cell, cl.seg))
+        par = np.zeros((n, 6), np.float64)
+        par[:, 0] = ms_to_us(cl.delay)
+        par[:, 1] = ms_to_us(cl.duration)
+        par[:, 2] = cl.v_before if cl.triple else np.nan
+        par[:, 3] = cl.v_during
+        par[:, 4] = cl.v_after if cl.triple else np.nan
+        par[:, 5] = cl.resistance
+        cpar.append(par.astype(F32))
+        cwt.append(np.asarray(cl.weight, np.float64).astype(F32))
+    ct_, cwt = cat(ct_, np.int32), cat(cwt, F32)
+    cpar = np.concatenate(cpar) if cpar else np.zeros((0, 6), F32)
+    if len(ct_):
+        perm = np.argsort(ct_, kind="stable")
+        ct_, cpar, cwt = ct_[perm], cpar[perm], cwt[perm]
+
     trace_target = np.array([target_of([gid_off[c.pop] + c.cell], [c.seg], current=False)[0]
                              for c in spec.trace_columns], dtype=np.int32)
     event_src = np.array([gid_off[e.pop] + e.cell for e in spec.event_selections], dtype=np.int32)
@@ -668,14 +692,14 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         timed_target=cat(tm_t, np.int32), timed_type=cat(tm_ty, np.int32), timed_weight=cat(tm_w, F32),
         timed_off=np.asarray(tm_off, np.int64), timed_step=cat(tm_steps, np.int64),
         wave_target=wt, wave_shape=wsh, wave_params=wpar, wave_weight=wwt,
-        pois_rng_base=prng,
+        pois_rng_base=prng, clamp_target=ct_, clamp_params=cpar, clamp_weight=cwt,
     )
 
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 5
+ABI_VERSION = 6
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -706,6 +730,7 @@ class CModel(ctypes.Structure):
         ("n_wave", ctypes.c_int64), ("wave_target", _i32p), ("wave_shape", _i32p), ("wave_params", _f32p),
         ("wave_weight", _f32p),
         ("pois_rng_base", _i32p),
+        ("n_clamp", ctypes.c_int64), ("clamp_target", _i32p), ("clamp_params", _f32p), ("clamp_weight", _f32p),
     ]
 
 
@@ -791,4 +816,8 @@ def to_cmodel(m: LoweredModel):
     cm.wave_weight = p(m.wave_weight, F32, _f32p)
     if m.pois_rng_base is not None:
         cm.pois_rng_base = p(m.pois_rng_base, np.int32, _i32p)
+    cm.n_clamp = len(m.clamp_target)
+    cm.clamp_target = p(m.clamp_target, np.int32, _i32p)
+    cm.clamp_params = p(np.asarray(m.clamp_params).reshape(-1), F32, _f32p)
+    cm.clamp_weight = p(m.clamp_weight, F32, _f32p)
     return cm, keep

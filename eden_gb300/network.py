@@ -259,6 +259,24 @@ class PulseInputs:
 
 
 @dataclass
+class ClampInputs:
+    """voltageClamp (`triple` False: clamps to `v_during` from `delay` for
+    `duration`, no current otherwise) or voltageClampTriple (True, active:
+    `v_before`, `v_during`, `v_after`) instances (ms, mV, series resistance
+    `resistance` MOhm) on cell gid `cell`, segment `seg`, scaled by `weight`."""
+    triple: bool
+    cell: np.ndarray
+    seg: np.ndarray
+    delay: np.ndarray
+    duration: np.ndarray
+    v_before: np.ndarray
+    v_during: np.ndarray
+    v_after: np.ndarray
+    resistance: np.ndarray
+    weight: np.ndarray
+
+
+@dataclass
 class PoissonInputs:
     """poissonFiringSynapse instances (`rate` Hz, each driving its own
     instance of `synapse`) on cell gid `cell`, segment `seg`.  The order of
@@ -333,6 +351,7 @@ class NetworkSpec:
     poissons: List[PoissonInputs] = field(default_factory=list)
     timed: List[TimedInputs] = field(default_factory=list)
     waves: List[WaveInputs] = field(default_factory=list)
+    clamps: List[ClampInputs] = field(default_factory=list)
     temperature: float = 6.3  # degC: the network's, or the reference's default when it has none
     trace_columns: List[OutputColumn] = field(default_factory=list)
     trace_file: str = "trajectory.txt"

@@ -24,7 +24,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SynapseType,
                       EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
-                      TimedInputs, WaveInputs)
+                      ClampInputs, TimedInputs, WaveInputs)
 
 
 def _f(x: float) -> str:
@@ -155,6 +155,22 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             else:
                 w(f'<rampGenerator id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" startAmplitude="{_f(a)}nA" '
                   f'finishAmplitude="{_f(b)}nA" baselineAmplitude="{_f(c)}nA"/>\n')
+    clamp_ids = {}
+    for cl in spec.clamps:
+        for i in range(len(cl.cell)):
+            key = _clamp_key(cl, i)
+            if key in clamp_ids:
+                continue
+            cid = f"clamp{len(clamp_ids)}"
+            clamp_ids[key] = cid
+            _, d, du, vb, vd, va, r = key
+            if cl.triple:
+                w(f'<voltageClampTriple id="{cid}" delay="{_f(d)}ms" duration="{_f(du)}ms" active="1" '
+                  f'conditioningVoltage="{_f(vb)}mV" testingVoltage="{_f(vd)}mV" returnVoltage="{_f(va)}mV" '
+                  f'simpleSeriesResistance="{_f(r)}Mohm"/>\n')
+            else:
+                w(f'<voltageClamp id="{cid}" delay="{_f(d)}ms" duration="{_f(du)}ms" targetVoltage="{_f(vd)}mV" '
+                  f'simpleSeriesResistance="{_f(r)}Mohm"/>\n')
     if spec.temperature != 6.3 or any(g.q10 is not None and g.q10[0] == "exp" for ch in spec.channels
                                       for g in ch.gates):
         w(f'<network id="net" type="networkWithTemperature" temperature="{_f(spec.temperature)} degC">\n')
@@ -227,6 +243,17 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             for n, i in enumerate(idx):
                 w(f'  <input id="{n}" target="../{pop}[{local_of[po.cell[i]]}]" segmentId="{po.seg[i]}" '
                   f'fractionAlong="0.5" destination="synapses"/>\n')
+            w(' </inputList>\n')
+    for cl in spec.clamps:
+        by_comp = defaultdict(list)
+        for i in range(len(cl.cell)):
+            by_comp[(clamp_ids[_clamp_key(cl, i)], pop_of[cl.cell[i]])].append(i)
+        for (cid, pop), idx in by_comp.items():
+            w(f' <inputList id="il{n_list}" component="{cid}" population="{pop}">\n')
+            n_list += 1
+            for n, i in enumerate(idx):
+                w(f'  <inputW id="{n}" target="../{pop}[{local_of[cl.cell[i]]}]" segmentId="{cl.seg[i]}" '
+                  f'fractionAlong="0.5" destination="synapses" weight="{_f(cl.weight[i])}"/>\n')
             w(' </inputList>\n')
     for wv in spec.waves:
         by_comp = defaultdict(list)
@@ -353,6 +380,7 @@ _UNITS = {
     "resistivity": {"ohm_cm": 1.0, "kohm_cm": 1e3, "ohm_m": 100.0},
     "frequency_hz": {"Hz": 1.0, "per_s": 1.0, "per_ms": 1e3, "kHz": 1e3, "per_us": 1e6, "MHz": 1e6},
     "rate_per_ms": {"per_ms": 1.0, "kHz": 1.0, "per_s": 1e-3, "Hz": 1e-3, "per_us": 1e3, "MHz": 1e3},
+    "resistance": {"ohm": 1e-6, "kohm": 1e-3, "Mohm": 1.0, "Gohm": 1e3},
     "cond_per_voltage": {"nS_per_mV": 1.0, "S_per_V": 1e9 / 1e3, "uS_per_mV": 1e3, "pS_per_mV": 1e-3},
 }
 _QTY = re.compile(r"^\s*([-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?)\s*([A-Za-z_0-9]*)\s*$")
@@ -376,6 +404,12 @@ def _qty(el, attr, dim, default=None):
     if unit not in table:
         raise ValueError(f"<{_tag(el)}> {attr}: unit {unit!r} not supported for {dim} (known: {sorted(table)})")
     return value * table[unit]
+
+
+def _clamp_key(cl, i):
+    side = (lambda x: float(x)) if cl.triple else (lambda x: None)   # a voltageClamp has no before/after targets
+    return (cl.triple, float(cl.delay[i]), float(cl.duration[i]), side(cl.v_before[i]), float(cl.v_during[i]),
+            side(cl.v_after[i]), float(cl.resistance[i]))
 
 
 def _wave_key(wv, i):
@@ -564,7 +598,7 @@ def read_lems(path: str) -> NetworkSpec:
                        _qty(sim, "length", "time"), seed)
     # components
     channels_by_name, synapses, pulses_def, pois_def, cells = {}, {}, {}, {}, {}
-    timed_def, wave_def = {}, {}
+    timed_def, wave_def, clamp_def = {}, {}, {}
     net = None
     for e in elems:
         t = _tag(e)
@@ -619,6 +653,22 @@ def read_lems(path: str) -> NetworkSpec:
             # hour) as `inf` into its generated C, which then fails to compile
             raise ValueError(f"transientPoissonFiringSynapse {e.get('id')}: not supported (the reference "
                              f"simulator cannot run it either)")
+        elif t in ("voltageClamp", "voltageClampTriple"):
+            if e.get("simpleSeriesResistance") is not None:
+                res = _qty(e, "simpleSeriesResistance", "resistance")
+            else:   # the reference scales the older attribute by 1e5 (eden/NeuroML.cpp:7091-7100)
+                res = _qty(e, "seriesResistance", "resistance") * 1e5
+            if t == "voltageClamp":
+                v = _qty(e, "targetVoltage", "voltage")
+                clamp_def[e.get("id")] = (False, _qty(e, "delay", "time"), _qty(e, "duration", "time"),
+                                          np.nan, v, np.nan, res)
+            else:
+                if _qty(e, "active", None) != 1.0:
+                    raise ValueError(f"voltageClampTriple {e.get('id')}: only active=\"1\" is supported")
+                clamp_def[e.get("id")] = (True, _qty(e, "delay", "time"), _qty(e, "duration", "time"),
+                                          _qty(e, "conditioningVoltage", "voltage"),
+                                          _qty(e, "testingVoltage", "voltage"), _qty(e, "returnVoltage", "voltage"),
+                                          res)
         elif t == "sineGenerator":
             wave_def[e.get("id")] = (WAVE_SINE, _qty(e, "delay", "time"), _qty(e, "duration", "time"),
                                      _qty(e, "amplitude", "current"), _qty(e, "period", "time"),
@@ -729,7 +779,7 @@ def read_lems(path: str) -> NetworkSpec:
                                            np.array(rows[3]), np.array(rows[4])))
     # inputs
     pcell, pseg, pdel, pdur, pamp, pwt = [], [], [], [], [], []
-    pois_rows, wave_rows = {}, {}
+    pois_rows, wave_rows, clamp_rows = {}, {}, {}
     timed_rows = {}
     for il in _children(net, "inputList"):
         comp = il.get("component")
@@ -747,6 +797,8 @@ def read_lems(path: str) -> NetworkSpec:
                 pois_rows.setdefault(comp, []).append((g, seg))
             elif comp in wave_def:
                 wave_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1"))))
+            elif comp in clamp_def:
+                clamp_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1"))))
             else:
                 raise ValueError(f"inputList component {comp} not supported")
     for ei in _children(net, "explicitInput"):
@@ -775,6 +827,13 @@ def read_lems(path: str) -> NetworkSpec:
             raise ValueError(f"poissonFiringSynapse {comp}: synapse {syn} not supported")
         spec.poissons.append(PoissonInputs("*", syn, rate, np.array([r[0] for r in rows]),
                                            np.array([r[1] for r in rows])))
+    for comp, rows in clamp_rows.items():
+        triple, d, du, vb, vd, va, res = clamp_def[comp]
+        n = len(rows)
+        spec.clamps.append(ClampInputs(triple, np.array([r[0] for r in rows], np.int64),
+                                       np.array([r[1] for r in rows], np.int64), np.full(n, d), np.full(n, du),
+                                       np.full(n, vb), np.full(n, vd), np.full(n, va), np.full(n, res),
+                                       np.array([r[2] for r in rows])))
     for comp, rows in wave_rows.items():
         shape, d, du, a, b, c = wave_def[comp]
         n = len(rows)

@@ -30,6 +30,8 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    passive dendrites) and on izhikevich cells: pulse, sine and
                    ramp generators, several Poisson components sharing
                    compartments, and timed inputs on passive dendrites.
+  voltage_clamps   voltageClamp and voltageClampTriple on HH somata,
+                   passive dendrites and izhikevich cells, with pulses.
   gate_kinds       channels with every built-in gate kind (gateHHrates,
                    gateHHtauInf, gateHHratesTau, gateHHratesInf,
                    gateHHratesTauInf), q10Fixed and q10ExpTemp settings at
@@ -45,7 +47,7 @@ from __future__ import annotations
 import numpy as np
 
 from .network import (RATE_EXP, RATE_EXPLINEAR, RATE_SIGMOID, AdExCell, Channel, ChannelDensity, EventSelection,
-                      Gate, IafCell, Izhikevich2007Cell, Rate,
+                      ClampInputs, Gate, IafCell, Izhikevich2007Cell, Rate,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
                       SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, TimedInputs, WAVE_RAMP,
@@ -603,6 +605,47 @@ def gate_kinds(n_single: int = 8, n_branch: int = 4, length_ms: float = 60.0, dt
     return spec
 
 
+def voltage_clamps(n_hh: int = 4, n_branch: int = 2, n_izh: int = 2, length_ms: float = 60.0,
+                   dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
+    """voltageClamp (one target between delay and delay + duration) and
+    voltageClampTriple (conditioning, testing and return targets) on HH
+    somata, a passive dendrite and izhikevich cells, series resistances
+    10-100 MOhm, weighted; DC pulses make the cells fire outside the
+    clamped phases."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("voltage_clamps", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.cells.append(PhysicalCell("hhcell", np.array([-1]), np.array([0.0]), np.array([17.8]),
+                                   _hh_densities(1, np.ones(1, bool)), cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0))
+    parent = np.array([-1, 0, 1])
+    soma = parent < 0
+    spec.cells.append(PhysicalCell("branch", parent, np.array([20.0, 80.0, 60.0]), np.array([20.0, 2.0, 1.5]),
+                                   _hh_densities(3, soma), cm=1.0, ra=150.0, v0=-65.0, spike_thresh=-20.0,
+                                   seg_groups={"soma_group": soma, "dend_group": ~soma}))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    spec.populations.append(Population("branch", "branch", n_branch))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    n = n_hh + n_branch + n_izh
+    spec.pulses.append(PulseInputs("*", np.arange(n), np.zeros(n, int), np.zeros(n), np.full(n, length_ms),
+                                   np.round(rng.uniform(0.05, 0.3, n), 4)))
+    br = n_hh + np.arange(n_branch)
+    iz = n_hh + n_branch + np.arange(n_izh)
+    cells = np.concatenate([np.arange(n_hh), br, iz])
+    segs = np.concatenate([np.zeros(n_hh, int), np.full(n_branch, 2), np.zeros(n_izh, int)])
+    k = len(cells)
+    spec.clamps.append(ClampInputs(False, cells, segs, np.round(rng.uniform(5.0, 20.0, k), 3),
+                                   np.round(rng.uniform(10.0, 25.0, k), 3), np.full(k, np.nan),
+                                   np.round(rng.uniform(-80.0, -40.0, k), 2), np.full(k, np.nan),
+                                   np.round(rng.uniform(10.0, 100.0, k), 2), np.round(rng.uniform(0.5, 1.5, k), 3)))
+    spec.clamps.append(ClampInputs(True, br, np.zeros(n_branch, int), np.full(n_branch, 15.0),
+                                   np.full(n_branch, 20.0), np.array([-63.77, -70.0]), np.array([-30.0, -45.0]),
+                                   np.array([-40.77, -55.0]), np.array([50.0, 80.0]), np.ones(n_branch)))
+    cols = [(g, 0) for g in range(n)] + [(int(br[0]), 2)]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), seg) for g, seg in cols]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
@@ -615,4 +658,5 @@ CONFIGS = {
     "timed_inputs": timed_inputs,
     "input_kinds": input_kinds,
     "gate_kinds": gate_kinds,
+    "voltage_clamps": voltage_clamps,
 }

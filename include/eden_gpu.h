@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 5
+#define EDEN_GPU_ABI_VERSION 6
 
 enum {
     EDEN_GPU_OK = 0,
@@ -88,6 +88,14 @@ enum {
     EDEN_WAVE_SHAPES = 2
 };
 #define EDEN_WAVE_PARAMS 5
+
+/* Voltage clamps (LEMS_CoreComponents.inc.xml: voltageClamp 555-586,
+ * voltageClampTriple 588-620). Parameters of clamp k at
+ * clamp_params[EDEN_CLAMP_PARAMS * k + j]: 0 delay (us), 1 duration (us),
+ * target potential (mV) 2 before the delay, 3 from the delay to delay +
+ * duration, 4 after that (NaN: no current in that phase), 5 series
+ * resistance (MOhm). */
+#define EDEN_CLAMP_PARAMS 6
 
 /* One ionChannelHH type: up to EDEN_MAX_GATES gateHHrates, each contributing
  * q^instances to the open fraction (eden/Eden.cpp:5678-5717). Rates in 1/us. */
@@ -233,6 +241,14 @@ typedef struct EdenGpuModel {
      * cell type plus two per Poisson component before it on its own
      * compartment (eden/Eden.cpp:6540, 2450-2458); NULL for all 0 */
     const int32_t *pois_rng_base;
+
+    /* voltage clamps: current clamp_weight * (target - V) / R, V the
+     * compartment's potential at the start of the step, the target of the
+     * step's phase (the OnConditions' last assignment at its time) */
+    int64_t n_clamp;
+    const int32_t *clamp_target;
+    const float *clamp_params;      /* [n_clamp * EDEN_CLAMP_PARAMS] */
+    const float *clamp_weight;
 } EdenGpuModel;
 
 /* Execution options. */

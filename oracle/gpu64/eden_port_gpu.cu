@@ -147,6 +147,9 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         dm.wave_shape = g.copy(m->wave_shape, (size_t)m->n_wave);
         dm.wave_params = g.copy(m->wave_params, (size_t)m->n_wave * EDEN_WAVE_PARAMS);
         dm.wave_weight = g.copy(m->wave_weight, (size_t)m->n_wave);
+        dm.clamp_target = g.copy(m->clamp_target, (size_t)m->n_clamp);
+        dm.clamp_params = g.copy(m->clamp_params, (size_t)m->n_clamp * EDEN_CLAMP_PARAMS);
+        dm.clamp_weight = g.copy(m->clamp_weight, (size_t)m->n_clamp);
         dm.pois_rng_base = m->pois_rng_base ? g.copy(m->pois_rng_base, (size_t)np) : nullptr;
         // the loop's state, set up on the host
         Port D = H;
@@ -174,6 +177,7 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         D.pois_off = g.copy(H.pois_off, (size_t)nt + 1);
         D.pulse_off = g.copy(H.pulse_off, (size_t)nt + 1);
         D.wave_off = g.copy(H.wave_off, (size_t)nt + 1);
+        D.clamp_off = g.copy(H.clamp_off, (size_t)nt + 1);
         D.fan_off = g.copy(H.fan_off, (size_t)m->n_src + 1);
         D.fan_syn = g.copy(H.fan_syn, (size_t)ns + 1);
         D.order = g.copy(H.order, (size_t)m->n_comp + 1);

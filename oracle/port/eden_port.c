@@ -19,6 +19,7 @@
  *   random-call numbering per compartment     eden/Eden.cpp:2450-2458, 6540
  *   pulseGenerator                            eden/Eden.cpp:3798-3826
  *   sineGenerator, rampGenerator (LEMS)       LEMS_CoreComponents.inc.xml:430-458, 489-521, eden/Eden.cpp:3107-3133
+ *   voltageClamp, voltageClampTriple (LEMS)   LEMS_CoreComponents.inc.xml:555-620
  *   timedSynapticInput                        eden/Eden.cpp:3759-3790, 3859-3871
  *   point neurons (LEMS): izhikevich2007Cell, iafTauCell, iafTauRefCell,
  *   iafCell, iafRefCell, adExIaFCell          LEMS_CoreComponents.inc.xml:957-1240, eden/Eden.cpp:6821-6914
@@ -112,7 +113,7 @@ typedef struct {
     unsigned char *spiked[2];           /* event-logger slot per source */
     real *diag;
     int64_t *gate_off;                  /* [n_chan + 1] */
-    int64_t *syn_off, *pois_off, *pulse_off, *wave_off; /* [n_target + 1] */
+    int64_t *syn_off, *pois_off, *pulse_off, *wave_off, *clamp_off; /* [n_target + 1] */
     int64_t *fan_off, *fan_syn;         /* CSR source -> synapses */
     int32_t *order;                     /* per-cell DFS post-order, local ids */
     int32_t *src_of_target;             /* source id detecting at a target, or -1 */
@@ -341,6 +342,15 @@ static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, rea
             else i = R(1.0) * base;
         }
         Iin += i * (real)m->wave_weight[k];
+    }
+    /* voltage clamps: the target of the phase the step's time is in (the
+     * OnConditions in order, the last that holds assigns), against the
+     * potential at the start of the step; none in the initialisation passes */
+    for (int64_t k = P->clamp_off[tgt]; k < P->clamp_off[tgt + 1]; k++) {
+        const float *p = m->clamp_params + (int64_t)EDEN_CLAMP_PARAMS * k;
+        const real del = p[0], dur = p[1];
+        const real tv = (t > dur + del) ? (real)p[4] : (t < del) ? (real)p[2] : (real)p[3];
+        if (!init && tv == tv) Iin += ((R(1.0) * (tv - v)) / (real)p[5]) * (real)m->clamp_weight[k];
     }
     /* Poisson inputs, one block per synapse type run */
     int64_t k = P->pois_off[tgt];
@@ -675,6 +685,7 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
     P.pois_off = csr_by_key(m->pois_target, np, nt);
     P.pulse_off = csr_by_key(m->pulse_target, m->n_pulse, nt);
     P.wave_off = csr_by_key(m->wave_target, m->n_wave, nt);
+    P.clamp_off = csr_by_key(m->clamp_target, m->n_clamp, nt);
     P.fan_off = csr_by_key(m->syn_src, ns, m->n_src);
     P.fan_syn = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ns + 1));
     {
@@ -704,7 +715,7 @@ static void port_free(Port *P) {
         free(P->pois_a[b]); free(P->pois_b[b]); free(P->spiked[b]); free(P->timed_a[b]); free(P->timed_b[b]);
     }
     free(P->diag); free(P->syn_fire_count); free(P->gate_off); free(P->syn_off); free(P->pois_off);
-    free(P->pulse_off); free(P->wave_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
+    free(P->pulse_off); free(P->wave_off); free(P->clamp_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
     free(P->timed_cur); free(P->timed_tgt_off); free(P->timed_order);
 }
 

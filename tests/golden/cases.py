@@ -19,6 +19,7 @@ CASES = {
     "timed_inputs": ("timed_inputs", dict(), 1.0, None),
     "input_kinds": ("input_kinds", dict(), 1.0, None),
     "gate_kinds": ("gate_kinds", dict(), 1.0, None),
+    "voltage_clamps": ("voltage_clamps", dict(), 1.0, None),
 }
 
 

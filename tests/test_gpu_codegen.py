@@ -11,7 +11,8 @@ from golden.cases import spec_of
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["multicomp_poisson", "ball_and_stick", "izh_net", "input_kinds", "gate_kinds"])
+@pytest.mark.parametrize("name", ["multicomp_poisson", "ball_and_stick", "izh_net", "input_kinds", "gate_kinds",
+                                  "voltage_clamps"])
 def test_generated_kernels_match_builtin(name):
     low = lowering.lower(spec_of(name))
     builtin = Simulation(low, mode=MODE_BATCHED, codegen=-1)

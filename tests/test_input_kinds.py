@@ -140,3 +140,22 @@ def test_unknown_wave_shape_is_refused():
     spec.waves[0].shape = "square"
     with pytest.raises(ValueError, match="shape"):
         lowering.lower(spec)
+
+
+def test_voltage_clamp_round_trip(tmp_path):
+    spec = spec_of("voltage_clamps")
+    back = neuroml_io.read_lems(neuroml_io.write_lems(spec, str(tmp_path)))
+    a, b = lowering.lower(spec), lowering.lower(back)
+    for f in ("clamp_target", "clamp_params", "clamp_weight"):
+        np.testing.assert_array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(b, f)), err_msg=f)
+    # a voltageClamp has no current before its delay or after delay + duration
+    simple = ~np.isnan(a.clamp_params[:, 3]) & np.isnan(a.clamp_params[:, 2])
+    assert simple.sum() == 8 and np.isnan(a.clamp_params[simple, 4]).all()
+
+
+def test_inactive_triple_clamp_is_refused(tmp_path):
+    lems = neuroml_io.write_lems(spec_of("voltage_clamps"), str(tmp_path))
+    nml = tmp_path / "voltage_clamps.nml"
+    nml.write_text(nml.read_text().replace('active="1"', 'active="0"'))
+    with pytest.raises(ValueError, match="active"):
+        neuroml_io.read_lems(lems)

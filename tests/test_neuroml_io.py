@@ -40,9 +40,8 @@ def test_unsupported_elements_fail_loudly(tmp_path):
     spec = workloads.single_comp_hh(n_cells=2, length_ms=1.0)
     path = neuroml_io.write_lems(spec, str(tmp_path))
     nml = tmp_path / f"{spec.name}.nml"
-    text = nml.read_text().replace("<pulseGenerator ", '<voltageClamp targetVoltage="-60mV" '
-                                   'simpleSeriesResistance="1e6ohm" ')
-    nml.write_text(text.replace("</pulseGenerator>", "</voltageClamp>"))
+    text = nml.read_text().replace("<pulseGenerator ", "<pulseGeneratorDL ")
+    nml.write_text(text.replace("</pulseGenerator>", "</pulseGeneratorDL>"))
     with pytest.raises(ValueError):
         neuroml_io.read_lems(path)
 
