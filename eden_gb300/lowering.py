@@ -28,7 +28,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, IafCell, Izhikevich2007Cell, NetworkSpec,
-                      PhysicalCell, SpikeArrayCell, WAVE_RAMP, WAVE_SINE,
+                      PhysicalCell, SpikeArrayCell, SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
+                      WAVE_RAMP, WAVE_SINE,
                       SYN_EXPONE, SYN_EXPTWO)
 
 F32 = np.float32
@@ -275,7 +276,82 @@ def timed_steps(times_ms, th: np.ndarray) -> np.ndarray:
     return (np.unique(idx[idx < len(th)]) + 1).astype(np.int64)
 
 
-def spike_source_steps(ext_cells: dict, dt: np.float32, n_steps: int):
+_MASK64 = (1 << 64) - 1
+NOT_AN_INSTANCE = ~0xFEE1600D   # the `instance` of a cell's own LEMS code (eden/Eden.cpp:3255-3256)
+
+
+def _hash64shift(key: int) -> int:
+    key = ((~key) + (key << 21)) & _MASK64
+    key ^= key >> 24
+    key = (key + (key << 3) + (key << 8)) & _MASK64
+    key ^= key >> 14
+    key = (key + (key << 2) + (key << 4)) & _MASK64
+    key ^= key >> 28
+    return (key + (key << 31)) & _MASK64
+
+
+def randof(x, work_item: int, instance: int, step: int, invocation: int) -> np.float32:
+    """The reference's random(x) (eden/Eden.cpp:3216-3233): x times a 23-bit
+    uniform from the integer hash of (work item, instance, step, call id)."""
+    hi = ((int(work_item) << 24) | (int(instance) & 0xFFFFFF)) & _MASK64
+    lo = ((int(invocation) << 40) | (int(step) & ((1 << 40) - 1))) & _MASK64
+    sample = _hash64shift(_hash64shift(lo) ^ hi)
+    r = F32(sample % (1 << 23)) / F32(1 << 23)
+    return F32(F32(x) * F32(r))
+
+
+def random_source_steps(ct, seed: int, tk: np.ndarray) -> np.ndarray:
+    """Steps (1-based) in which a spikeGeneratorRandom / spikeGeneratorPoisson
+    / spikeGeneratorRefPoisson emits (LEMS_CoreComponents.inc.xml:778-930 as
+    the reference's LEMS code runs them, eden/Eden.cpp:2832-2994): the
+    OnStart draw of the last initialisation pass (step 0, call id 0) sets
+    the first spike time; a step whose float time exceeds it emits, draws
+    the next interval (step n, call id 1) and moves the spike time on."""
+    n_steps = len(tk)
+    us = F32(1000.0)
+
+    def first_after(n0, tnext):
+        # first step >= n0 (1-based) whose time exceeds tnext
+        return max(n0, int(np.searchsorted(tk, tnext, side="right")) + 1)
+
+    fire = []
+    with np.errstate(all="ignore"):
+        if isinstance(ct, SpikeGeneratorRandomCell):
+            lo, hi = _to_f32(ct.min_isi * 1000.0), _to_f32(ct.max_isi * 1000.0)
+            x = F32(F32(hi - lo) / us)
+            draw = lambda n, inv: F32(lo + F32(us * randof(x, seed, NOT_AN_INSTANCE, n, inv)))
+            tnext = draw(0, 0)
+            n = first_after(1, tnext)
+            while n <= n_steps:
+                fire.append(n)
+                tnext = F32(tnext + draw(n, 1))
+                n = first_after(n + 1, tnext)
+        else:
+            rate = _to_f32(ct.rate * 1e-6)
+            if ct.min_isi is None:
+                draw = lambda n, inv: F32(F32(F32(-1.0) * np.log(randof(1.0, seed, NOT_AN_INSTANCE, n, inv))) / rate)
+            else:
+                mi = _to_f32(ct.min_isi * 1000.0)
+                avg = F32(F32(1.0) / rate)
+                draw = lambda n, inv: F32(mi - F32(F32(avg - mi) *
+                                                   np.log(randof(1.0, seed, NOT_AN_INSTANCE, n, inv))))
+            small = F32(1e-6)   # SMALL_TIME, 1e-9 ms in us
+            t_ideal = t_used = draw(0, 0)
+            n = first_after(1, t_used)
+            while n <= n_steps:
+                fire.append(n)
+                t = tk[n - 1]
+                t_ideal = F32(t_ideal + draw(n, 1))
+                h1 = F32(0.0) if F32(F32(t_ideal - t) / t) < 0 else F32(1.0)
+                h2 = F32(0.0) if F32(F32(t - t_ideal) / t) < 0 else F32(1.0)
+                t_used = F32(F32(t_ideal * h1) + F32(F32(t + small) * h2))
+                if not np.isfinite(t_used):
+                    break
+                n = first_after(n + 1, t_used)
+    return np.asarray(fire, np.int64)
+
+
+def spike_source_steps(ext_cells: dict, dt: np.float32, n_steps: int, seeds: np.ndarray = None):
     """(source, logging step) of every spike the spike sources emit in steps
     1..n_steps, in step order and by source within a step.  A step n emits
     when it crosses the next spike time: spikeArray (the reference's spike
@@ -292,6 +368,12 @@ def spike_source_steps(ext_cells: dict, dt: np.float32, n_steps: int):
             s_, k_ = event_set_steps(ct, gids, dt, n_steps)
             srcs.append(s_)
             steps.append(k_)
+            continue
+        if isinstance(ct, (SpikeGeneratorRandomCell, SpikeGeneratorPoissonCell)):
+            for g in gids:
+                fire = random_source_steps(ct, int(seeds[g]), tk)
+                srcs.append(np.full(len(fire), g, np.int32))
+                steps.append(fire + 1)
             continue
         if isinstance(ct, SpikeArrayCell):
             times = np.sort(ms_to_us(np.asarray(ct.times, np.float64)).astype(F32))
@@ -525,7 +607,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         t = gid_base[gids] + np.where(gid_is_izh[gids], 0, segs)
         return t.astype(np.int32)
 
-    ext_src, ext_step = spike_source_steps(ext_cells, dt, spec.n_steps())
+    ext_src, ext_step = spike_source_steps(ext_cells, dt, spec.n_steps(), cell_seeds(spec.seed, n_cells))
 
     # ---- synapse types --------------------------------------------------------
     syn_types = np.zeros(len(spec.synapses), dtype=SYN_DTYPE)

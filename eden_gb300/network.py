@@ -189,6 +189,23 @@ class SpikeGeneratorCell:
 
 
 @dataclass
+class SpikeGeneratorRandomCell:
+    """spikeGeneratorRandom: intervals uniform in [min_isi, max_isi) ms."""
+    name: str
+    min_isi: float
+    max_isi: float
+
+
+@dataclass
+class SpikeGeneratorPoissonCell:
+    """spikeGeneratorPoisson (`min_isi` None) or spikeGeneratorRefPoisson
+    (`min_isi` ms, a refractory floor on the intervals) at `rate` Hz."""
+    name: str
+    rate: float
+    min_isi: Optional[float] = None
+
+
+@dataclass
 class EventSetReaderCell:
     """EdenEventSetReader: spike events streamed from a file, one source per
     (instance, port); `frames` are the file's lines in order, each a
@@ -201,7 +218,8 @@ class EventSetReaderCell:
     href: str = "events.txt"
 
 
-SPIKE_SOURCE_TYPES = (SpikeArrayCell, SpikeGeneratorCell, EventSetReaderCell)
+SPIKE_SOURCE_TYPES = (SpikeArrayCell, SpikeGeneratorCell, EventSetReaderCell, SpikeGeneratorRandomCell,
+                      SpikeGeneratorPoissonCell)
 
 
 # ---------------------------------------------------------------------------

@@ -21,7 +21,8 @@ import numpy as np
 from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       Izhikevich2007Cell, NetworkSpec, OutputColumn,
                       PhysicalCell, PoissonInputs, Population, Projection,
-                      PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SynapseType,
+                      PulseInputs, Rate, SpikeArrayCell, SpikeGeneratorCell, SpikeGeneratorPoissonCell,
+                      SpikeGeneratorRandomCell, SynapseType,
                       EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
                       ClampInputs, TimedInputs, WaveInputs)
@@ -94,6 +95,14 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w('</spikeArray>\n')
         elif isinstance(c, SpikeGeneratorCell):
             w(f'<spikeGenerator id="{c.name}" period="{_f(c.period)}ms"/>\n')
+        elif isinstance(c, SpikeGeneratorRandomCell):
+            w(f'<spikeGeneratorRandom id="{c.name}" minISI="{_f(c.min_isi)}ms" maxISI="{_f(c.max_isi)}ms"/>\n')
+        elif isinstance(c, SpikeGeneratorPoissonCell):
+            if c.min_isi is None:
+                w(f'<spikeGeneratorPoisson id="{c.name}" averageRate="{_f(c.rate)} Hz"/>\n')
+            else:
+                w(f'<spikeGeneratorRefPoisson id="{c.name}" averageRate="{_f(c.rate)} Hz" '
+                  f'minimumISI="{_f(c.min_isi)}ms"/>\n')
         elif isinstance(c, IafCell):
             extra = ""
             if c.kind in ("iafTauCell", "iafTauRefCell"):
@@ -703,6 +712,14 @@ def read_lems(path: str) -> NetworkSpec:
                                                 np.array([_qty(sp, "time", "time") for sp in _children(e, "spike")]))
         elif t == "spikeGenerator":
             cells[e.get("id")] = SpikeGeneratorCell(e.get("id"), _qty(e, "period", "time"))
+        elif t == "spikeGeneratorRandom":
+            cells[e.get("id")] = SpikeGeneratorRandomCell(e.get("id"), _qty(e, "minISI", "time"),
+                                                          _qty(e, "maxISI", "time"))
+        elif t == "spikeGeneratorPoisson":
+            cells[e.get("id")] = SpikeGeneratorPoissonCell(e.get("id"), _qty(e, "averageRate", "frequency_hz"))
+        elif t == "spikeGeneratorRefPoisson":
+            cells[e.get("id")] = SpikeGeneratorPoissonCell(e.get("id"), _qty(e, "averageRate", "frequency_hz"),
+                                                           _qty(e, "minimumISI", "time"))
         elif t in ("network", "networkWithTemperature") and e.get("id") == sim.get("target"):
             net = e
     for e in elems:

@@ -30,6 +30,9 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    passive dendrites) and on izhikevich cells: pulse, sine and
                    ramp generators, several Poisson components sharing
                    compartments, and timed inputs on passive dendrites.
+  random_sources   spikeGeneratorRandom, spikeGeneratorPoisson and
+                   spikeGeneratorRefPoisson populations driving izhikevich
+                   and HH cells.
   voltage_clamps   voltageClamp and voltageClampTriple on HH somata,
                    passive dendrites and izhikevich cells, with pulses.
   gate_kinds       channels with every built-in gate kind (gateHHrates,
@@ -50,6 +53,7 @@ from .network import (RATE_EXP, RATE_EXPLINEAR, RATE_SIGMOID, AdExCell, Channel,
                       ClampInputs, Gate, IafCell, Izhikevich2007Cell, Rate,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
+                      SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, TimedInputs, WAVE_RAMP,
                       WAVE_SINE, WaveInputs, hh_channels)
 
@@ -605,6 +609,36 @@ def gate_kinds(n_single: int = 8, n_branch: int = 4, length_ms: float = 60.0, dt
     return spec
 
 
+def random_sources(n_each: int = 4, n_izh: int = 8, n_hh: int = 6, fan_out: int = 3, length_ms: float = 100.0,
+                   dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
+    """Random spike generators (uniform intervals, Poisson, Poisson with a
+    refractory floor), several instances each, so their per-cell seeds
+    differ, connected to izhikevich and single-compartment HH cells through
+    expOne synapses."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("random_sources", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses.append(SynapseType("syn_e1", SYN_EXPONE, gbase=6.0, erev=0.0, tau_decay=2.0))
+    spec.cells += [SpikeGeneratorRandomCell("rnd", 3.0, 9.0), SpikeGeneratorPoissonCell("poi", 150.0),
+                   SpikeGeneratorPoissonCell("refpoi", 120.0, 4.0),
+                   Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0),
+                   PhysicalCell("hhcell", np.array([-1]), np.array([0.0]), np.array([17.8]),
+                                _hh_densities(1, np.ones(1, bool)), cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0)]
+    for name in ("rnd", "poi", "refpoi"):
+        spec.populations.append(Population(name, name, n_each))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    n_src = 3 * n_each
+    targets = n_src + np.arange(n_izh + n_hh)
+    pre = np.repeat(np.arange(n_src), fan_out)
+    post = rng.choice(targets, size=pre.size)
+    spec.projections.append(_flat_projection(spec, "proj_e1", pre, post, "syn_e1",
+                                             np.round(rng.uniform(0.3, 1.0, pre.size), 4),
+                                             _round_us(rng.uniform(0.5, 2.0, size=pre.size))))
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, int(g)), 0) for g in targets[::3]]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n_src + n_izh + n_hh)]
+    return spec
+
+
 def voltage_clamps(n_hh: int = 4, n_branch: int = 2, n_izh: int = 2, length_ms: float = 60.0,
                    dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
     """voltageClamp (one target between delay and delay + duration) and
@@ -659,4 +693,5 @@ CONFIGS = {
     "input_kinds": input_kinds,
     "gate_kinds": gate_kinds,
     "voltage_clamps": voltage_clamps,
+    "random_sources": random_sources,
 }

@@ -20,6 +20,7 @@ CASES = {
     "input_kinds": ("input_kinds", dict(), 1.0, None),
     "gate_kinds": ("gate_kinds", dict(), 1.0, None),
     "voltage_clamps": ("voltage_clamps", dict(), 1.0, None),
+    "random_sources": ("random_sources", dict(), 1.0, None),
 }
 
 
