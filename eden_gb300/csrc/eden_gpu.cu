@@ -217,13 +217,14 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
             if (t.gate_kind[g] < 0 || t.gate_kind[g] >= EDEN_GATE_KINDS)
                 return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: gate kind %d", k, g, t.gate_kind[g]);
             const int gk = t.gate_kind[g];
-            if (gk != EDEN_GATE_TAUINF &&
+            if (gk != EDEN_GATE_TAUINF && gk != EDEN_GATE_INSTANTANEOUS &&
                 (t.fwd_kind[g] < 0 || t.fwd_kind[g] > 2 || t.rev_kind[g] < 0 || t.rev_kind[g] > 2))
                 return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: rate kind", k, g);
             if ((gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESTAU || gk == EDEN_GATE_RATESTAUINF) &&
                 (t.tau_kind[g] < 0 || t.tau_kind[g] > EDEN_RATE_FIXED))
                 return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: timeCourse form", k, g);
-            if ((gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESINF || gk == EDEN_GATE_RATESTAUINF) &&
+            if ((gk == EDEN_GATE_TAUINF || gk == EDEN_GATE_RATESINF || gk == EDEN_GATE_RATESTAUINF ||
+                 gk == EDEN_GATE_INSTANTANEOUS) &&
                 (t.inf_kind[g] < 0 || t.inf_kind[g] > EDEN_RATE_FIXED))
                 return ctx->fail(EDEN_GPU_E_INVALID, "channel type %d gate %d: steadyState form", k, g);
         }

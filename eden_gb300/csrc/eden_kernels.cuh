@@ -753,14 +753,18 @@ __device__ __forceinline__ float gate_next(const ChanTypeDev &ct, int gi, bool i
 // gateHHrates carries 1 + its row of `ext` (kind, timeCourse form and its
 // three values, steadyState form and its three values) in the bits of the
 // first word above the forward form.
+// An instantaneous gate keeps the steady state at the compartment's
+// potential after the step (`vnew`), which is what the next step's currents
+// read as its value.
 __device__ __forceinline__ float gate_next_p(const float *P, const float *ext, bool init, float dt, float v,
-                                             float qo) {
+                                             float vnew, float qo) {
     const int w0 = __float_as_int(P[0]);
     if (EDEN_KIND_GATEFORMS && (w0 >> 8) != 0) {
         const float *X = ext + (size_t)((w0 >> 8) - 1) * kGateExtWords;
-        return gate_general(__float_as_int(X[0]), w0 & 0xff, P[1], P[2], P[3], __float_as_int(P[4]), P[5], P[6], P[7],
+        const int gk = __float_as_int(X[0]);
+        return gate_general(gk, w0 & 0xff, P[1], P[2], P[3], __float_as_int(P[4]), P[5], P[6], P[7],
                             __float_as_int(X[1]), X[2], X[3], X[4], __float_as_int(X[5]), X[6], X[7], X[8], P[8],
-                            init, dt, v, qo);
+                            init, dt, gk == EDEN_GATE_INSTANTANEOUS ? vnew : v, qo);
     }
     const float alpha = rate_value(w0, P[1], P[2], P[3], v);
     const float beta = rate_value(__float_as_int(P[4]), P[5], P[6], P[7], v);
@@ -892,8 +896,11 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
             float *q = m.gate + m.ch_gate0[ch];
             for (int g = 0; g < ct.n_gates; g++) {
                 const float qo = q[g];
-                q[g] = gate_next(ct, g, init, m.dt, v, qo);
-                for (int r = 0; r < ct.inst[g]; r++) fopen = fopen * qo;
+                const float qn = gate_next(ct, g, init, m.dt, v, qo);
+                q[g] = qn;
+                // an instantaneous gate's value is its steady state at this V
+                const float qf = (EDEN_KIND_GATEFORMS && ct.gk[g] == EDEN_GATE_INSTANTANEOUS) ? qn : qo;
+                for (int r = 0; r < ct.inst[g]; r++) fopen = fopen * qf;
             }
             float gs = m.ch_gbase[ch] * fopen;
             Ich += (gs * (m.ch_erev[ch] - v) * 1e-5f) * A;

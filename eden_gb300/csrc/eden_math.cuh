@@ -77,6 +77,7 @@ __device__ __forceinline__ float form_value(int kind, float r, float mid, float 
 __device__ __forceinline__ float gate_general(int gk, int fk, float fr, float fm, float fs, int rk, float rr, float rm,
                                               float rs, int tk, float tr, float tm, float ts, int ik, float ir,
                                               float im, float is, float q10, bool init, float dt, float v, float qo) {
+    if (gk == EDEN_GATE_INSTANTANEOUS) return form_value(ik, ir, im, is, v);
     float a = 0.0f, b = 0.0f;
     if (gk != EDEN_GATE_TAUINF) {
         a = rate_value(fk, fr, fm, fs, v);

@@ -278,7 +278,8 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
         // gate updates from this step's starting V and gate values (the
         // currents above used the values before the update, as the reference does)
         for (int q = lane; q < ngt; q += 32)
-            GT[q] = gate_next_p(GP + q * kGateWords, m.gate_ext, init, dt, VO[GI_S[q]], GT[q]);
+            GT[q] = gate_next_p(GP + q * kGateWords, m.gate_ext, init, dt, VO[GI_S[q]],
+                                EDEN_KIND_GATEFORMS ? X[NT[GI_S[q]]] : 0.0f, GT[q]);
         // threshold crossings of the unit's spike sources (eden/Eden.cpp:6247-6252)
         for (int q0 = 0; q0 < ns; q0 += 32) {
             const int q = q0 + lane;

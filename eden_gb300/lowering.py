@@ -215,7 +215,7 @@ def _cable_geometry(cell: PhysicalCell):
 POINT_PARAMS = 16
 # gate kinds and the fixed rate form (include/eden_gpu.h EDEN_GATE_*, EDEN_RATE_FIXED)
 RATE_FIXED = 3
-GATE_KINDS = {"rates": 0, "tauInf": 1, "ratesTau": 2, "ratesInf": 3, "ratesTauInf": 4}
+GATE_KINDS = {"rates": 0, "tauInf": 1, "ratesTau": 2, "ratesInf": 3, "ratesTauInf": 4, "instantaneous": 5}
 
 
 def gate_q10(gate, temperature_degc: float) -> np.float32:
@@ -489,7 +489,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
             if gate.kind not in GATE_KINDS:
                 raise ValueError(f"channel {ch.name} gate {gate.name}: unknown kind {gate.kind!r}")
             needs = {"rates": (1, 0, 0), "tauInf": (0, 1, 1), "ratesTau": (1, 1, 0), "ratesInf": (1, 0, 1),
-                     "ratesTauInf": (1, 1, 1)}[gate.kind]
+                     "ratesTauInf": (1, 1, 1), "instantaneous": (0, 0, 1)}[gate.kind]
             have = (gate.forward is not None and gate.reverse is not None, gate.tau is not None, gate.inf is not None)
             if tuple(bool(x) for x in needs) != have:
                 want = [n for n, k in zip(("forward/reverse rates", "timeCourse", "steadyState"), needs) if k]

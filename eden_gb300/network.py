@@ -51,7 +51,7 @@ class Rate:
 @dataclass
 class Gate:
     """An HH gate.  `kind` is "rates" (gateHHrates), "tauInf", "ratesTau",
-    "ratesInf" or "ratesTauInf"; `tau` a fixedTimeCourse (ms) and `inf` an
+    "ratesInf", "ratesTauInf" or "instantaneous"; `tau` a fixedTimeCourse (ms) and `inf` an
     HH*Variable steady state (dimensionless rate) where the kind has them;
     `q10` None, ("fixed", factor) or ("exp", q10Factor, experimentalTemp
     degC)."""

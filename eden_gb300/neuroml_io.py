@@ -438,7 +438,8 @@ _RATE_KIND = {v: k for k, v in RATE_TYPE_NAMES.items()}
 
 
 _GATE_TAGS = {"rates": "gateHHrates", "tauInf": "gateHHtauInf", "ratesTau": "gateHHratesTau",
-              "ratesInf": "gateHHratesInf", "ratesTauInf": "gateHHratesTauInf"}
+              "ratesInf": "gateHHratesInf", "ratesTauInf": "gateHHratesTauInf",
+              "instantaneous": "gateHHInstantaneous"}
 _GATE_KINDS = {v: k for k, v in _GATE_TAGS.items()}
 _VARIABLE_KIND = {"HHExpVariable": 0, "HHExpLinearVariable": 1, "HHSigmoidVariable": 2}
 _VARIABLE_TYPE_NAMES = {v: k for k, v in _VARIABLE_KIND.items()}
@@ -622,7 +623,7 @@ def read_lems(path: str) -> NetworkSpec:
                                      f"({', '.join(sorted(_GATE_KINDS))})")
                 kind = _GATE_KINDS[gt]
                 fwd = rev = tau = inf = q10 = None
-                if kind != "tauInf":
+                if kind not in ("tauInf", "instantaneous"):
                     fwd = _parse_rate(_children(g, "forwardRate")[0])
                     rev = _parse_rate(_children(g, "reverseRate")[0])
                 if kind in ("tauInf", "ratesTau", "ratesTauInf"):
@@ -631,7 +632,7 @@ def read_lems(path: str) -> NetworkSpec:
                         raise ValueError(f"ionChannel {e.get('id')} gate {g.get('id')}: timeCourse type "
                                          f"{tc.get('type')!r} not supported (fixedTimeCourse)")
                     tau = _qty(tc, "tau", "time")
-                if kind in ("tauInf", "ratesInf", "ratesTauInf"):
+                if kind in ("tauInf", "ratesInf", "ratesTauInf", "instantaneous"):
                     inf = _parse_variable(_children(g, "steadyState")[0])
                 for qs in _children(g, "q10Settings"):
                     if qs.get("type") == "q10Fixed":

@@ -543,7 +543,8 @@ def input_kinds(n_mc: int = 6, n_izh: int = 4, length_ms: float = 80.0, dt_ms: f
 
 def gate_kind_channels() -> list:
     """Leak plus sodium, delayed-rectifier and A-type potassium channels
-    whose gates use each built-in gate kind and both q10 settings."""
+    whose gates use each built-in gate kind and both q10 settings, and a
+    persistent sodium channel with an instantaneous gate."""
     q10 = ("exp", 3.0, 6.3)
     leak = Channel("passiveChan")
     na = Channel("naT", [
@@ -560,7 +561,8 @@ def gate_kind_channels() -> list:
              tau=2.0, inf=Rate(RATE_SIGMOID, 1.0, -45.0, 12.0), q10=q10),
         Gate("b", 1, Rate(RATE_EXP, 0.02, -80.0, -15.0), Rate(RATE_SIGMOID, 0.05, -60.0, 8.0), q10=q10),
     ], species="k")
-    return [leak, na, kdr, ka]
+    nap = Channel("naP", [Gate("m", 1, kind="instantaneous", inf=Rate(RATE_SIGMOID, 1.0, -52.0, 5.0))], species="na")
+    return [leak, na, kdr, ka, nap]
 
 
 def gate_kinds(n_single: int = 8, n_branch: int = 4, length_ms: float = 60.0, dt_ms: float = 0.025,
@@ -577,7 +579,8 @@ def gate_kinds(n_single: int = 8, n_branch: int = 4, length_ms: float = 60.0, dt
     def dens(n_seg, active):
         allseg = np.ones(n_seg, bool)
         return [ChannelDensity(0, 0.3, -54.387, allseg), ChannelDensity(1, 120.0, 50.0, active.copy()),
-                ChannelDensity(2, 36.0, -77.0, active.copy()), ChannelDensity(3, 8.0, -77.0, active.copy())]
+                ChannelDensity(2, 36.0, -77.0, active.copy()), ChannelDensity(3, 8.0, -77.0, active.copy()),
+                ChannelDensity(4, 0.8, 50.0, active.copy())]
 
     one = np.ones(1, bool)
     spec.cells.append(PhysicalCell("single", np.array([-1]), np.array([0.0]), np.array([17.8]), dens(1, one),

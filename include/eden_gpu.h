@@ -58,7 +58,9 @@ enum {
     EDEN_GATE_RATESTAU = 2,     /* gateHHratesTau: rates, timeCourse        */
     EDEN_GATE_RATESINF = 3,     /* gateHHratesInf: rates, steadyState       */
     EDEN_GATE_RATESTAUINF = 4,  /* gateHHratesTauInf: all four              */
-    EDEN_GATE_KINDS = 5
+    EDEN_GATE_INSTANTANEOUS = 5,/* gateHHInstantaneous: the steady state at
+                                   the step's own V, no state of its own     */
+    EDEN_GATE_KINDS = 6
 };
 
 #define EDEN_MAX_GATES 4

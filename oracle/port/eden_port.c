@@ -430,6 +430,13 @@ static PORT_FN void phys_cell_step(Port *P, int cur, int32_t cell, int init, rea
                 /* tau and inf from the rates unless the gate kind has its
                  * own timeCourse / steadyState (eden/Eden.cpp:5290-5375) */
                 const int gk = ct->gate_kind[g];
+                if (gk == EDEN_GATE_INSTANTANEOUS) {
+                    /* no state: the steady state at this step's V (eden/Eden.cpp:5268-5282) */
+                    const real x = rate_value(ct->inf_kind[g], ct->inf_rate[g], ct->inf_mid[g], ct->inf_scale[g], Vc);
+                    P->gate[nxt][go + g] = x;
+                    for (int r = 0; r < ct->gate_instances[g]; r++) fopen = fopen * x;
+                    continue;
+                }
                 real alpha = R(0.0), beta = R(0.0);
                 if (gk != EDEN_GATE_TAUINF) {
                     alpha = rate_value(ct->fwd_kind[g], ct->fwd_rate[g], ct->fwd_mid[g], ct->fwd_scale[g], Vc);

@@ -52,7 +52,7 @@ def test_incomplete_gate_is_refused():
 
 @pytest.mark.parametrize("old,new", [
     ('<timeCourse type="fixedTimeCourse" tau="3.0ms"/>', '<timeCourse type="myTau" tau="3.0ms"/>'),
-    ('<gateHHtauInf id="h"', '<gateHHInstantaneous id="h"'),
+    ('<gateHHtauInf id="h"', '<gateKS id="h"'),
 ])
 def test_unsupported_gate_forms_are_refused(tmp_path, old, new):
     lems = neuroml_io.write_lems(workloads.gate_kinds(), str(tmp_path))
@@ -60,8 +60,8 @@ def test_unsupported_gate_forms_are_refused(tmp_path, old, new):
     text = nml.read_text()
     assert old in text
     text = text.replace(old, new)
-    if "Instantaneous" in new:
-        text = text.replace("</gateHHtauInf>", "</gateHHInstantaneous>")
+    if "gateKS" in new:
+        text = text.replace("</gateHHtauInf>", "</gateKS>")
     nml.write_text(text)
     with pytest.raises(ValueError):
         neuroml_io.read_lems(lems)
