@@ -1,0 +1,158 @@
+"""EdenCustomSetup files: per-instance overrides of a network's properties.
+
+The reference reads `set` statements from the file an `<EdenCustomSetup
+filename=...>` element of the LEMS `<Simulation>` names
+(eden/NeuroML.cpp:7240-7330 tokenising, 7629-7790 `set cell`, 7430-7500
+values and units) and applies them to the instances' tables before the run
+(eden/Eden.cpp:9437-9649):
+
+    set cell <population> <instance ids | all> all <property> <value> <unit>
+    set cell <population> <instance ids | all> all <property> multi <unit>
+    values <one value per selected instance>
+
+Instance ids are comma-separated; a dimensional property needs its unit.
+Built here: `set cell` on point neurons (izhikevich2007Cell, iaf*Cell,
+adExIaFCell), whose LEMS parameters become per-instance values in the
+lowered model.  Not built: properties of physical cells (segment states,
+channel gates), `set input` and `set synapse` statements; they are refused
+by name.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import List, Optional
+
+from .network import AdExCell, IafCell, Izhikevich2007Cell
+
+# LEMS parameter -> (dataclass field, dimension of the unit table, factor to the field's unit)
+_IZH = {"v0": ("v0", "voltage", 1.0), "C": ("C", "capacitance", 1.0), "k": ("k", "cond_per_voltage", 1.0),
+        "vr": ("vr", "voltage", 1.0), "vt": ("vt", "voltage", 1.0), "vpeak": ("vpeak", "voltage", 1.0),
+        "a": ("a", "rate_per_ms", 1.0), "b": ("b", "conductance", 1.0), "c": ("c", "voltage", 1.0),
+        "d": ("d", "current", 1e3)}
+_IAF = {"leakReversal": ("leak_reversal", "voltage", 1.0), "thresh": ("thresh", "voltage", 1.0),
+        "reset": ("reset", "voltage", 1.0), "tau": ("tau", "time", 1.0), "C": ("C", "capacitance", 1.0),
+        "leakConductance": ("leak_conductance", "conductance", 1.0), "refract": ("refract", "time", 1.0)}
+_ADEX = {"C": ("C", "capacitance", 1.0), "gL": ("gL", "conductance", 1.0), "EL": ("EL", "voltage", 1.0),
+         "VT": ("VT", "voltage", 1.0), "thresh": ("thresh", "voltage", 1.0), "reset": ("reset", "voltage", 1.0),
+         "delT": ("delT", "voltage", 1.0), "tauw": ("tauw", "time", 1.0), "refract": ("refract", "time", 1.0),
+         "a": ("a", "conductance", 1.0), "b": ("b", "current", 1.0)}
+
+
+def _params_of(ct):
+    if isinstance(ct, Izhikevich2007Cell):
+        return _IZH
+    if isinstance(ct, IafCell):
+        return _IAF
+    if isinstance(ct, AdExCell):
+        return _ADEX
+    return None
+
+
+@dataclass
+class SetCell:
+    """One `set cell` statement: `values` (field units) for the listed
+    instances of `pop` (`ids` None: all, in instance order)."""
+    pop: str
+    ids: Optional[List[int]]
+    prop: str
+    values: List[float]
+    text: str = ""
+
+
+def parse(text: str, spec) -> List[SetCell]:
+    """The statements of a custom setup file, checked against `spec`."""
+    from .neuroml_io import _UNITS
+    lines = [ln.split("#", 1)[0].split() for ln in text.splitlines()]
+    out = []
+    i = 0
+    while i < len(lines):
+        tok = lines[i]
+        i += 1
+        if not tok:
+            continue
+        if tok[0] != "set":
+            raise ValueError(f"custom setup line {i}: unknown statement {tok[0]!r}")
+        if len(tok) < 2 or tok[1] != "cell":
+            raise ValueError(f"custom setup line {i}: 'set {tok[1] if len(tok) > 1 else ''}' is not supported "
+                             f"(only 'set cell' on point neurons)")
+        if len(tok) < 7:
+            raise ValueError(f"custom setup line {i}: 'set cell' needs population, instances, segments, "
+                             f"property and value")
+        pop, ids_s, segs, prop, value = tok[2], tok[3], tok[4], tok[5], tok[6]
+        pops = {p.name: p for p in spec.populations}
+        if pop not in pops:
+            raise ValueError(f"custom setup line {i}: population {pop} not found")
+        ct = spec.cell_type(pops[pop].cell_type)
+        table = _params_of(ct)
+        if table is None:
+            raise ValueError(f"custom setup line {i}: properties of {type(ct).__name__} cells are not supported "
+                             f"(point neurons only)")
+        if segs != "all":
+            raise ValueError(f"custom setup line {i}: segment specifier must be 'all' for point neurons")
+        if prop not in table:
+            raise ValueError(f"custom setup line {i}: {type(ct).__name__} has no settable property {prop!r}")
+        ids = None
+        if ids_s != "all":
+            ids = [int(x) for x in ids_s.split(",")]
+            if len(set(ids)) != len(ids):
+                raise ValueError(f"custom setup line {i}: an instance is listed twice")
+            bad = [x for x in ids if not 0 <= x < pops[pop].size]
+            if bad:
+                raise ValueError(f"custom setup line {i}: instance {bad[0]} not in population {pop}")
+        field, dim, factor = table[prop]
+        unit = tok[7] if len(tok) > 7 else None
+        scale = 1.0
+        if dim is not None:
+            if unit is None:
+                raise ValueError(f"custom setup line {i}: property {prop} needs units")
+            if unit not in _UNITS[dim]:
+                raise ValueError(f"custom setup line {i}: unit {unit!r} not known for {dim}")
+            scale = _UNITS[dim][unit] * factor
+        n_sel = pops[pop].size if ids is None else len(ids)
+        if value == "multi":
+            if i >= len(lines) or not lines[i] or lines[i][0] != "values":
+                raise ValueError(f"custom setup line {i}: 'multi' needs a 'values' line after it")
+            vals = [float(x) * scale for x in lines[i][1:]]
+            i += 1
+            if len(vals) != n_sel:
+                raise ValueError(f"custom setup line {i}: {len(vals)} values for {n_sel} instances")
+        else:
+            vals = [float(value) * scale] * n_sel
+        out.append(SetCell(pop, ids, field, vals))
+    return out
+
+
+def overrides(spec) -> dict:
+    """(population, instance) -> {field: value} after every statement of
+    `spec.custom_setup`, later statements overriding earlier ones."""
+    res = {}
+    pops = {p.name: p for p in spec.populations}
+    for st in spec.custom_setup:
+        ids = list(range(pops[st.pop].size)) if st.ids is None else st.ids
+        for inst, v in zip(ids, st.values):
+            res.setdefault((st.pop, inst), {})[st.prop] = float(v)
+    return res
+
+
+def write(spec, path: str) -> None:
+    """Write `spec.custom_setup` as a setup file (values in field units)."""
+    from .neuroml_io import _f
+    unit_of = {"voltage": "mV", "capacitance": "pF", "cond_per_voltage": "nS_per_mV", "rate_per_ms": "per_ms",
+               "conductance": "nS", "current": "nA", "time": "ms"}
+    with open(path, "w") as f:
+        for st in spec.custom_setup:
+            ct = spec.cell_type({p.name: p for p in spec.populations}[st.pop].cell_type)
+            prop, (field, dim, factor) = next((k, v) for k, v in _params_of(ct).items() if v[0] == st.prop)
+            ids = "all" if st.ids is None else ",".join(str(x) for x in st.ids)
+            vals = [v / factor for v in st.values]
+            f.write(f"set cell {st.pop} {ids} all {prop} multi {unit_of[dim]}\n")
+            f.write("values " + " ".join(_f(v) for v in vals) + "\n")
+
+
+def apply_to(ct, fields: dict):
+    """A copy of cell type `ct` with `fields` overridden."""
+    import dataclasses
+    return dataclasses.replace(ct, **fields)
+
+
+__all__ = ["SetCell", "parse", "overrides", "write", "apply_to"]

@@ -534,11 +534,14 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     geom_cache = {}
     gid_ctype = np.zeros(n_cells, np.int32)
     ctype_index = {c.name: k for k, c in enumerate(spec.cells)}
+    from .custom_setup import apply_to, overrides
+    setup = overrides(spec) if spec.custom_setup else {}
     gid = 0
     for pop in spec.populations:
-        ct = spec.cell_type(pop.cell_type)
-        gid_ctype[gid:gid + pop.size] = ctype_index[ct.name]
-        for _ in range(pop.size):
+        ct_pop = spec.cell_type(pop.cell_type)
+        gid_ctype[gid:gid + pop.size] = ctype_index[ct_pop.name]
+        for inst in range(pop.size):
+            ct = apply_to(ct_pop, setup[(pop.name, inst)]) if (pop.name, inst) in setup else ct_pop
             if isinstance(ct, PhysicalCell):
                 if ct.name not in geom_cache:
                     geom_cache[ct.name] = _cable_geometry(ct)

@@ -371,6 +371,7 @@ class NetworkSpec:
     waves: List[WaveInputs] = field(default_factory=list)
     clamps: List[ClampInputs] = field(default_factory=list)
     temperature: float = 6.3  # degC: the network's, or the reference's default when it has none
+    custom_setup: list = field(default_factory=list)   # EdenCustomSetup statements (custom_setup.SetCell)
     trace_columns: List[OutputColumn] = field(default_factory=list)
     trace_file: str = "trajectory.txt"
     event_selections: List[EventSelection] = field(default_factory=list)

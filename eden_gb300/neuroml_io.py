@@ -303,6 +303,10 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
         for i, ev in enumerate(spec.event_selections):
             lw.append(f'  <EventSelection id="{i}" select="{_select_path(spec, ev)}" eventPort="spike"/>\n')
         lw.append(' </EventOutputFile>\n')
+    if spec.custom_setup:
+        from .custom_setup import write as write_setup
+        write_setup(spec, os.path.join(dirname, f"{spec.name}_setup.txt"))
+        lw.append(f' <EdenCustomSetup filename="./{spec.name}_setup.txt"/>\n')
     lw.append('</Simulation>\n</Lems>\n')
     with open(lems_path, "w") as f:
         f.write("".join(lw))
@@ -909,6 +913,10 @@ def read_lems(path: str) -> NetworkSpec:
                                  "start": _us(ef, "starting_from", -inf), "end": _us(ef, "up_to_excluding", inf),
                                  "max_interval": _us(ef, "maximum_interval", inf)})
         spec.event_selections.extend(EventSelection(s[2][0], s[2][1], 0) for s in sels)
+    for cs in _children(sim, "EdenCustomSetup"):
+        from .custom_setup import parse as parse_setup
+        with open(os.path.join(os.path.dirname(os.path.abspath(path)), cs.get("filename"))) as f:
+            spec.custom_setup += parse_setup(f.read(), spec)
     return spec
 
 

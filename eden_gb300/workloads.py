@@ -30,6 +30,8 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    passive dendrites) and on izhikevich cells: pulse, sine and
                    ramp generators, several Poisson components sharing
                    compartments, and timed inputs on passive dendrites.
+  custom_setup     izhikevich, iafRef and adExIaF populations whose
+                   parameters an EdenCustomSetup file overrides per instance.
   random_sources   spikeGeneratorRandom, spikeGeneratorPoisson and
                    spikeGeneratorRefPoisson populations driving izhikevich
                    and HH cells.
@@ -612,6 +614,48 @@ def gate_kinds(n_single: int = 8, n_branch: int = 4, length_ms: float = 60.0, dt
     return spec
 
 
+CUSTOM_SETUP_TEXT = """
+# izhikevich2007Cell instances
+set cell izh 1,3 all v0 -64 mV
+set cell izh all all d multi pA
+values 80 100 120 60 90 150
+set cell izh 2,4 all a 0.05 per_ms
+set cell izh 5 all vpeak 30 mV
+# iafRefCell instances
+set cell iaf 0,2 all thresh -52 mV
+set cell iaf all all refract multi ms
+values 2 4 6 8
+# adExIaFCell instances
+set cell adex 1 all b 0.1 nA
+set cell adex all all EL multi mV
+values -70.6 -68 -72 -66
+set cell izh 3 all v0 -58 mV
+"""
+
+
+def custom_setup(length_ms: float = 100.0, dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
+    """Point-neuron populations whose parameters an EdenCustomSetup file
+    overrides per instance (single values, per-instance lists, repeated
+    statements on the same instance), driven by DC pulses."""
+    from .custom_setup import parse
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("custom_setup", dt_ms, length_ms, seed)
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.cells.append(IafCell("iafRef", "iafRefCell", leak_reversal=-65.0, thresh=-50.0, reset=-65.0, C=200.0,
+                              leak_conductance=10.0, refract=3.0))
+    spec.cells.append(AdExCell("adex", C=281.0, gL=30.0, EL=-70.6, VT=-50.4, thresh=-40.4, reset=-70.6, delT=2.0,
+                               tauw=144.0, refract=0.0, a=4.0, b=0.0805))
+    spec.populations += [Population("izh", "izRS", 6), Population("iaf", "iafRef", 4), Population("adex", "adex", 4)]
+    n = 14
+    amp = np.concatenate([np.round(rng.uniform(0.1, 0.3, 6), 4), np.round(rng.uniform(0.2, 0.4, 4), 4),
+                          np.round(rng.uniform(0.6, 1.0, 4), 4)])
+    spec.pulses.append(PulseInputs("*", np.arange(n), np.zeros(n, int), np.full(n, 5.0), np.full(n, length_ms), amp))
+    spec.custom_setup = parse(CUSTOM_SETUP_TEXT, spec)
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 def random_sources(n_each: int = 4, n_izh: int = 8, n_hh: int = 6, fan_out: int = 3, length_ms: float = 100.0,
                    dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
     """Random spike generators (uniform intervals, Poisson, Poisson with a
@@ -697,4 +741,5 @@ CONFIGS = {
     "gate_kinds": gate_kinds,
     "voltage_clamps": voltage_clamps,
     "random_sources": random_sources,
+    "custom_setup": custom_setup,
 }

@@ -21,6 +21,7 @@ CASES = {
     "gate_kinds": ("gate_kinds", dict(), 1.0, None),
     "voltage_clamps": ("voltage_clamps", dict(), 1.0, None),
     "random_sources": ("random_sources", dict(), 1.0, None),
+    "custom_setup": ("custom_setup", dict(), 1.0, None),
 }
 
 
