@@ -825,6 +825,27 @@ __device__ __forceinline__ bool point_update(int kind, const float *p, int ps, b
         }
         break;
     }
+    case EDEN_POINT_IZH_DL: {
+        // izhikevichCell: v' = (0.04 v^2 / mV + 5 v + (140 - U + I) mV) / ms,
+        // U' = a (b v / mV - U) / ms; above thresh v = c mV, U += d
+        const float MV = 1.0f, MS = 1000.0f;
+        if (init) {
+            vn = PP(0);
+            u = (PP(0) * PP(3)) / MV;
+            break;
+        }
+        const float uu = u;
+        const float dv = ((0.04f * ((v * v) / MV) + 5.0f * v) + ((140.0f - uu) + iext) * MV) / MS;
+        const float du = (PP(2) * ((PP(3) * v) / MV - uu)) / MS;
+        vn = v + dt * dv;
+        u = uu + dt * du;
+        if (v > PP(1)) {
+            vn = PP(4) * MV;
+            u = uu + PP(5);
+            spike = true;
+        }
+        break;
+    }
     case EDEN_POINT_ADEX: {
         // adExIaFCell: iMemb = -gL (v - EL) + gL delT exp((v - VT) / delT) - w + iSyn,
         // v' = iMemb / C outside the refractory period, w' = (a (v - EL) - w) / tauw

@@ -27,7 +27,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, IafCell, Izhikevich2007Cell, NetworkSpec,
+from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, IafCell, Izhikevich2007Cell, IzhikevichCell,
+                      NetworkSpec,
                       PhysicalCell, SpikeArrayCell, SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       WAVE_RAMP, WAVE_SINE,
                       SYN_EXPONE, SYN_EXPTWO)
@@ -236,7 +237,7 @@ def gate_q10(gate, temperature_degc: float) -> np.float32:
 # waveform inputs (include/eden_gpu.h EDEN_WAVE_*)
 WAVE_PARAMS = 5
 WAVE_SHAPES = {WAVE_SINE: 0, WAVE_RAMP: 1}
-POINT_IZH2007, POINT_IAF_TAU, POINT_IAF_TAU_REF, POINT_IAF, POINT_IAF_REF, POINT_ADEX = range(6)
+POINT_IZH2007, POINT_IAF_TAU, POINT_IAF_TAU_REF, POINT_IAF, POINT_IAF_REF, POINT_ADEX, POINT_IZH_DL = range(7)
 _IAF_KINDS = {"iafTauCell": POINT_IAF_TAU, "iafTauRefCell": POINT_IAF_TAU_REF, "iafCell": POINT_IAF,
               "iafRefCell": POINT_IAF_REF}
 
@@ -257,6 +258,8 @@ def point_params(ct):
     if isinstance(ct, AdExCell):
         return POINT_ADEX, [ct.C, ct.gL * 1e-3, ct.EL, ct.VT, ct.thresh, ct.reset, ct.delT, ct.tauw * 1e3,
                             ct.refract * 1e3, ct.a * 1e-3, ct.b]
+    if isinstance(ct, IzhikevichCell):
+        return POINT_IZH_DL, [ct.v0, ct.thresh, ct.a, ct.b, ct.c, ct.d]
     raise ValueError(f"not a point neuron: {type(ct).__name__}")
 
 
@@ -531,6 +534,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     gid_is_izh = np.zeros(n_cells, bool)
     izh_index = np.full(n_cells, -1, np.int64)
     no_current = np.zeros(n_cells, bool)
+    dl_cell = np.zeros(n_cells, bool)      # cells whose input current is dimensionless (izhikevichCell)
     geom_cache = {}
     gid_ctype = np.zeros(n_cells, np.int32)
     ctype_index = {c.name: k for k, c in enumerate(spec.cells)}
@@ -585,11 +589,12 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                 src_target[gid] = -1
                 gid_base[gid] = -1
                 ext_cells.setdefault(ct.name, (ct, []))[1].append(gid)
-            elif isinstance(ct, (Izhikevich2007Cell, IafCell, AdExCell)):
+            elif isinstance(ct, (Izhikevich2007Cell, IafCell, AdExCell, IzhikevichCell)):
                 gid_is_izh[gid] = True
                 izh_index[gid] = len(izh)
                 kind, params = point_params(ct)
                 no_current[gid] = kind in (POINT_IAF_TAU, POINT_IAF_TAU_REF)
+                dl_cell[gid] = kind == POINT_IZH_DL
                 izh.append(params + [0.0] * (POINT_PARAMS - len(params)))
                 izh_kind.append(kind)
             else:
@@ -600,13 +605,16 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         gid_base[g] = n_comp + izh_index[g]
         src_target[g] = n_comp + izh_index[g]
 
-    def target_of(gids, segs, current=True):
+    def target_of(gids, segs, current=True, dimensionless=False):
         gids = np.asarray(gids, np.int64)
         segs = np.asarray(segs, np.int64)
         if len(gids) and (gid_base[gids] < 0).any():
             raise ValueError("a spike source (spikeArray, spikeGenerator) has no membrane to target")
         if current and len(gids) and no_current[gids].any():
             raise ValueError("iafTauCell and iafTauRefCell do not receive current (synapses or inputs)")
+        if current and len(gids) and (dl_cell[gids] != dimensionless).any():
+            raise ValueError("izhikevichCell takes the dimensionless inputs (pulse/sine/rampGeneratorDL) only, "
+                             "and those drive no other cell")
         t = gid_base[gids] + np.where(gid_is_izh[gids], 0, segs)
         return t.astype(np.int32)
 
@@ -694,7 +702,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     # ---- pulses ---------------------------------------------------------------
     qt, qs, qd, qa, qw = [], [], [], [], []
     for pu in spec.pulses:
-        qt.append(target_of(pu.cell, pu.seg))
+        qt.append(target_of(pu.cell, pu.seg, dimensionless=pu.dimensionless))
         qs.append(ms_to_us(pu.delay).astype(F32))
         qd.append(ms_to_us(pu.duration).astype(F32))
         qa.append(np.asarray(pu.amplitude, np.float64).astype(F32))
@@ -710,7 +718,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         if wv.shape not in WAVE_SHAPES:
             raise ValueError(f"unknown waveform input shape {wv.shape!r}")
         n = len(wv.cell)
-        wt.append(target_of(wv.cell, wv.seg))
+        wt.append(target_of(wv.cell, wv.seg, dimensionless=wv.dimensionless))
         wsh.append(np.full(n, WAVE_SHAPES[wv.shape], np.int32))
         par = np.zeros((n, WAVE_PARAMS), np.float64)
         par[:, 0] = ms_to_us(wv.delay)

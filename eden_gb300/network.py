@@ -140,6 +140,20 @@ class Izhikevich2007Cell:
 
 
 @dataclass
+class IzhikevichCell:
+    """izhikevichCell (the dimensionless form): v0, thresh mV; a, b, c, d
+    dimensionless.  Its input current is dimensionless: it takes the
+    *GeneratorDL inputs only."""
+    name: str
+    v0: float
+    thresh: float
+    a: float
+    b: float
+    c: float
+    d: float
+
+
+@dataclass
 class IafCell:
     """iafTauCell, iafTauRefCell, iafCell or iafRefCell (`kind`), NeuroML
     units: mV, ms, nS, pF.  The *Tau* kinds have no capacitance, leak
@@ -274,6 +288,7 @@ class PulseInputs:
     duration: np.ndarray
     amplitude: np.ndarray
     weight: Optional[np.ndarray] = None
+    dimensionless: bool = False   # pulseGeneratorDL (amplitude without unit, into izhikevichCell)
 
 
 @dataclass
@@ -325,6 +340,7 @@ class WaveInputs:
     p1: np.ndarray
     p2: np.ndarray
     weight: np.ndarray
+    dimensionless: bool = False   # sine/rampGeneratorDL (amplitudes without unit, into izhikevichCell)
 
 
 @dataclass

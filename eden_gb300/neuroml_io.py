@@ -25,7 +25,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       SpikeGeneratorRandomCell, SynapseType,
                       EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
-                      ClampInputs, TimedInputs, WaveInputs)
+                      ClampInputs, IzhikevichCell, TimedInputs, WaveInputs)
 
 
 def _f(x: float) -> str:
@@ -117,6 +117,9 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w(f'<adExIaFCell id="{c.name}" C="{_f(c.C)}pF" gL="{_f(c.gL)}nS" EL="{_f(c.EL)}mV" VT="{_f(c.VT)}mV" '
               f'thresh="{_f(c.thresh)}mV" reset="{_f(c.reset)}mV" delT="{_f(c.delT)}mV" tauw="{_f(c.tauw)}ms" '
               f'refract="{_f(c.refract)}ms" a="{_f(c.a)}nS" b="{_f(c.b)}nA"/>\n')
+        elif isinstance(c, IzhikevichCell):
+            w(f'<izhikevichCell id="{c.name}" v0="{_f(c.v0)}mV" thresh="{_f(c.thresh)}mV" a="{_f(c.a)}" '
+              f'b="{_f(c.b)}" c="{_f(c.c)}" d="{_f(c.d)}"/>\n')
         elif isinstance(c, Izhikevich2007Cell):
             w(f'<izhikevich2007Cell id="{c.name}" v0="{_f(c.v0)}mV" C="{_f(c.C)}pF" '
               f'k="{_f(c.k)}nS_per_mV" vr="{_f(c.vr)}mV" vt="{_f(c.vt)}mV" vpeak="{_f(c.vpeak)}mV" '
@@ -127,11 +130,15 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
     pulse_ids = {}
     for pi in spec.pulses:
         for d, du, a in zip(pi.delay, pi.duration, pi.amplitude):
-            key = (float(d), float(du), float(a))
+            key = (float(d), float(du), float(a), pi.dimensionless)
             if key not in pulse_ids:
                 pid = f"pg{len(pulse_ids)}"
                 pulse_ids[key] = pid
-                w(f'<pulseGenerator id="{pid}" delay="{_f(d)}ms" duration="{_f(du)}ms" amplitude="{_f(a)}nA"/>\n')
+                if pi.dimensionless:
+                    w(f'<pulseGeneratorDL id="{pid}" delay="{_f(d)}ms" duration="{_f(du)}ms" amplitude="{_f(a)}"/>\n')
+                else:
+                    w(f'<pulseGenerator id="{pid}" delay="{_f(d)}ms" duration="{_f(du)}ms" '
+                      f'amplitude="{_f(a)}nA"/>\n')
     pois_ids = {}
     for k, po in enumerate(spec.poissons):
         pid = f"poisson{k}"
@@ -158,12 +165,13 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             wid = f"wave{len(wave_ids)}"
             wave_ids[key] = wid
             _, d, du, a, b, c = key
+            dl, na = ("DL", "") if wv.dimensionless else ("", "nA")
             if wv.shape == WAVE_SINE:
-                w(f'<sineGenerator id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" amplitude="{_f(a)}nA" '
+                w(f'<sineGenerator{dl} id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" amplitude="{_f(a)}{na}" '
                   f'period="{_f(b)}ms" phase="{_f(c)}"/>\n')
             else:
-                w(f'<rampGenerator id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" startAmplitude="{_f(a)}nA" '
-                  f'finishAmplitude="{_f(b)}nA" baselineAmplitude="{_f(c)}nA"/>\n')
+                w(f'<rampGenerator{dl} id="{wid}" delay="{_f(d)}ms" duration="{_f(du)}ms" '
+                  f'startAmplitude="{_f(a)}{na}" finishAmplitude="{_f(b)}{na}" baselineAmplitude="{_f(c)}{na}"/>\n')
     clamp_ids = {}
     for cl in spec.clamps:
         for i in range(len(cl.cell)):
@@ -229,7 +237,7 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
     for pi in spec.pulses:
         by_comp = defaultdict(list)
         for i in range(len(pi.cell)):
-            key = (float(pi.delay[i]), float(pi.duration[i]), float(pi.amplitude[i]))
+            key = (float(pi.delay[i]), float(pi.duration[i]), float(pi.amplitude[i]), pi.dimensionless)
             by_comp[(pulse_ids[key], pop_of[pi.cell[i]])].append(i)
         for (pid, pop), idx in by_comp.items():
             w(f' <inputList id="il{n_list}" component="{pid}" population="{pop}">\n')
@@ -426,7 +434,7 @@ def _clamp_key(cl, i):
 
 
 def _wave_key(wv, i):
-    return (wv.shape, float(wv.delay[i]), float(wv.duration[i]), float(wv.p0[i]), float(wv.p1[i]),
+    return (wv.shape + ("DL" if wv.dimensionless else ""), float(wv.delay[i]), float(wv.duration[i]), float(wv.p0[i]), float(wv.p1[i]),
             float(wv.p2[i]))
 
 
@@ -655,9 +663,14 @@ def read_lems(path: str) -> NetworkSpec:
             synapses[e.get("id")] = SynapseType(e.get("id"), SYN_EXPTWO, _qty(e, "gbase", "conductance"),
                                                 _qty(e, "erev", "voltage"), _qty(e, "tauDecay", "time"),
                                                 _qty(e, "tauRise", "time"))
-        elif t == "pulseGenerator":
+        elif t in ("pulseGenerator", "pulseGeneratorDL"):
+            dl = t.endswith("DL")
             pulses_def[e.get("id")] = (_qty(e, "delay", "time"), _qty(e, "duration", "time"),
-                                       _qty(e, "amplitude", "current"))
+                                       _qty(e, "amplitude", None if dl else "current"), dl)
+        elif t == "izhikevichCell":
+            cells[e.get("id")] = IzhikevichCell(e.get("id"), _qty(e, "v0", "voltage"), _qty(e, "thresh", "voltage"),
+                                                _qty(e, "a", None), _qty(e, "b", None), _qty(e, "c", None),
+                                                _qty(e, "d", None))
         elif t == "timedSynapticInput":
             timed_def[e.get("id")] = (e.get("synapse"), [_qty(sp, "time", "time") for sp in _children(e, "spike")])
         elif t == "poissonFiringSynapse":
@@ -683,14 +696,16 @@ def read_lems(path: str) -> NetworkSpec:
                                           _qty(e, "conditioningVoltage", "voltage"),
                                           _qty(e, "testingVoltage", "voltage"), _qty(e, "returnVoltage", "voltage"),
                                           res)
-        elif t == "sineGenerator":
+        elif t in ("sineGenerator", "sineGeneratorDL"):
+            cur = None if t.endswith("DL") else "current"
             wave_def[e.get("id")] = (WAVE_SINE, _qty(e, "delay", "time"), _qty(e, "duration", "time"),
-                                     _qty(e, "amplitude", "current"), _qty(e, "period", "time"),
-                                     _qty(e, "phase", None))
-        elif t == "rampGenerator":
+                                     _qty(e, "amplitude", cur), _qty(e, "period", "time"),
+                                     _qty(e, "phase", None), cur is None)
+        elif t in ("rampGenerator", "rampGeneratorDL"):
+            cur = None if t.endswith("DL") else "current"
             wave_def[e.get("id")] = (WAVE_RAMP, _qty(e, "delay", "time"), _qty(e, "duration", "time"),
-                                     _qty(e, "startAmplitude", "current"), _qty(e, "finishAmplitude", "current"),
-                                     _qty(e, "baselineAmplitude", "current"))
+                                     _qty(e, "startAmplitude", cur), _qty(e, "finishAmplitude", cur),
+                                     _qty(e, "baselineAmplitude", cur), cur is None)
         elif t == "izhikevich2007Cell":
             cells[e.get("id")] = Izhikevich2007Cell(
                 e.get("id"), C=_qty(e, "C", "capacitance"), k=_qty(e, "k", "cond_per_voltage"),
@@ -800,7 +815,7 @@ def read_lems(path: str) -> NetworkSpec:
                                            np.array(rows[1], np.int64), np.array(rows[2], np.int64),
                                            np.array(rows[3]), np.array(rows[4])))
     # inputs
-    pcell, pseg, pdel, pdur, pamp, pwt = [], [], [], [], [], []
+    pcell, pseg, pdel, pdur, pamp, pwt, pdl = [], [], [], [], [], [], []
     pois_rows, wave_rows, clamp_rows = {}, {}, {}
     timed_rows = {}
     for il in _children(net, "inputList"):
@@ -812,9 +827,9 @@ def read_lems(path: str) -> NetworkSpec:
                 timed_rows.setdefault(timed_def[comp][0], []).append(
                     (g, seg, timed_def[comp][1], float(inp.get("weight", "1"))))
             elif comp in pulses_def:
-                d, du, a = pulses_def[comp]
+                d, du, a, dl = pulses_def[comp]
                 pcell.append(g); pseg.append(seg); pdel.append(d); pdur.append(du); pamp.append(a)
-                pwt.append(float(inp.get("weight", "1")))
+                pwt.append(float(inp.get("weight", "1"))); pdl.append(dl)
             elif comp in pois_def:
                 pois_rows.setdefault(comp, []).append((g, seg))
             elif comp in wave_def:
@@ -828,11 +843,17 @@ def read_lems(path: str) -> NetworkSpec:
         g = gid(_cell_ref(ei.get("target"), pops))
         if comp not in pulses_def:
             raise ValueError(f"explicitInput {comp} not supported")
-        d, du, a = pulses_def[comp]
+        d, du, a, dl = pulses_def[comp]
         pcell.append(g); pseg.append(0); pdel.append(d); pdur.append(du); pamp.append(a); pwt.append(1.0)
-    if pcell:
-        spec.pulses.append(PulseInputs("*", np.array(pcell), np.array(pseg), np.array(pdel), np.array(pdur),
-                                       np.array(pamp), None if all(x == 1.0 for x in pwt) else np.array(pwt)))
+        pdl.append(dl)
+    for dl in (False, True):
+        sel = [i for i in range(len(pcell)) if pdl[i] == dl]
+        if not sel:
+            continue
+        pick = lambda xs: np.array([xs[i] for i in sel])
+        wts = pick(pwt)
+        spec.pulses.append(PulseInputs("*", pick(pcell), pick(pseg), pick(pdel), pick(pdur), pick(pamp),
+                                       None if (wts == 1.0).all() else wts, dl))
     for syn, rows in timed_rows.items():
         if syn not in synapses:
             raise ValueError(f"timedSynapticInput: synapse {syn} not supported")
@@ -857,12 +878,12 @@ def read_lems(path: str) -> NetworkSpec:
                                        np.full(n, vb), np.full(n, vd), np.full(n, va), np.full(n, res),
                                        np.array([r[2] for r in rows])))
     for comp, rows in wave_rows.items():
-        shape, d, du, a, b, c = wave_def[comp]
+        shape, d, du, a, b, c, dl = wave_def[comp]
         n = len(rows)
         spec.waves.append(WaveInputs(shape, np.array([r[0] for r in rows], np.int64),
                                      np.array([r[1] for r in rows], np.int64), np.full(n, d), np.full(n, du),
                                      np.full(n, a), np.full(n, b), np.full(n, c),
-                                     np.array([r[2] for r in rows])))
+                                     np.array([r[2] for r in rows]), dl))
     # recorders: OutputFile / EventOutputFile and EDEN's EdenOutputFile /
     # EdenEventOutputFile with their time window, sampling interval or explicit
     # sample points, and heartbeat interval (eden/NeuroML.cpp:8037-8290);

@@ -30,6 +30,9 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    passive dendrites) and on izhikevich cells: pulse, sine and
                    ramp generators, several Poisson components sharing
                    compartments, and timed inputs on passive dendrites.
+  dl_inputs        izhikevichCell (dimensionless) driven by pulse, sine and
+                   ramp generators of the DL kind, beside izhikevich2007
+                   cells with the dimensional ones.
   custom_setup     izhikevich, iafRef and adExIaF populations whose
                    parameters an EdenCustomSetup file overrides per instance.
   random_sources   spikeGeneratorRandom, spikeGeneratorPoisson and
@@ -52,7 +55,7 @@ from __future__ import annotations
 import numpy as np
 
 from .network import (RATE_EXP, RATE_EXPLINEAR, RATE_SIGMOID, AdExCell, Channel, ChannelDensity, EventSelection,
-                      ClampInputs, Gate, IafCell, Izhikevich2007Cell, Rate,
+                      ClampInputs, Gate, IafCell, Izhikevich2007Cell, IzhikevichCell, Rate,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
                       SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
@@ -614,6 +617,40 @@ def gate_kinds(n_single: int = 8, n_branch: int = 4, length_ms: float = 60.0, dt
     return spec
 
 
+def dl_inputs(n_dl: int = 6, length_ms: float = 100.0, dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
+    """izhikevichCell instances (mixed-mode parameters) driven by
+    pulseGeneratorDL, sineGeneratorDL and rampGeneratorDL inputs with seeded
+    amplitudes, weighted, beside izhikevich2007 cells with pulse and sine
+    generators; the two kinds connect through expOne synapses only into the
+    izhikevich2007 cells."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("dl_inputs", dt_ms, length_ms, seed)
+    spec.cells.append(IzhikevichCell("izMixed", v0=-70.0, thresh=30.0, a=0.02, b=0.2, c=-55.0, d=4.0))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.synapses.append(SynapseType("syn_e1", SYN_EXPONE, gbase=2.0, erev=0.0, tau_decay=2.0))
+    spec.populations += [Population("dl", "izMixed", n_dl), Population("iz", "izRS", 3)]
+    dl = np.arange(n_dl)
+    spec.pulses.append(PulseInputs("*", dl, np.zeros(n_dl, int), np.round(rng.uniform(0.0, 20.0, n_dl), 3),
+                                   np.round(rng.uniform(30.0, 70.0, n_dl), 3), np.round(rng.uniform(5.0, 15.0, n_dl), 3),
+                                   np.round(rng.uniform(0.6, 1.2, n_dl), 3), dimensionless=True))
+    k = n_dl // 2
+    one = lambda x: np.full(k, x)
+    spec.waves.append(WaveInputs(WAVE_SINE, dl[:k], np.zeros(k, int), one(20.0), one(50.0),
+                                 np.round(rng.uniform(10.0, 40.0, k), 3), one(10.0), one(1.0), np.ones(k),
+                                 dimensionless=True))
+    spec.waves.append(WaveInputs(WAVE_RAMP, dl[k:], np.zeros(n_dl - k, int), np.full(n_dl - k, 30.0),
+                                 np.full(n_dl - k, 60.0), np.full(n_dl - k, -32.0), np.full(n_dl - k, 50.0),
+                                 np.full(n_dl - k, -2.0), np.full(n_dl - k, 0.5), dimensionless=True))
+    iz = n_dl + np.arange(3)
+    spec.pulses.append(PulseInputs("*", iz, np.zeros(3, int), np.zeros(3), np.full(3, length_ms),
+                                   np.array([0.08, 0.1, 0.12])))
+    spec.projections.append(_flat_projection(spec, "proj_e1", dl[:3], iz, "syn_e1", np.full(3, 0.5),
+                                             np.full(3, 1.0)))
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), 0) for g in range(n_dl + 3)]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n_dl + 3)]
+    return spec
+
+
 CUSTOM_SETUP_TEXT = """
 # izhikevich2007Cell instances
 set cell izh 1,3 all v0 -64 mV
@@ -742,4 +779,5 @@ CONFIGS = {
     "voltage_clamps": voltage_clamps,
     "random_sources": random_sources,
     "custom_setup": custom_setup,
+    "dl_inputs": dl_inputs,
 }

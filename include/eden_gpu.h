@@ -75,7 +75,10 @@ enum {
     EDEN_POINT_IAF = 3,
     EDEN_POINT_IAF_REF = 4,
     EDEN_POINT_ADEX = 5,
-    EDEN_POINT_KINDS = 6
+    EDEN_POINT_IZH_DL = 6,      /* izhikevichCell (LEMS_CoreComponents.inc.xml izhikevichCell):
+                                   v0, thresh (mV), a, b, c, d (dimensionless); its input
+                                   current is dimensionless (the *GeneratorDL inputs) */
+    EDEN_POINT_KINDS = 7
 };
 #define EDEN_POINT_PARAMS 16
 

@@ -514,7 +514,7 @@ static PORT_FN void phys_cell_step(Port *P, int cur, int32_t cell, int init, rea
 
 /* A point neuron for one step (LEMS_CoreComponents.inc.xml: izhikevich2007Cell
  * 1140-1187, iafTauCell 957-983, iafTauRefCell 985-1021, iafCell 1023-1056,
- * iafRefCell 1058-1095, adExIaFCell 1189-1240), with the semantics of the
+ * iafRefCell 1058-1095, adExIaFCell 1189-1240, izhikevichCell), with the semantics of the
  * reference's LEMS code (eden/Eden.cpp:2832-2994): forward Euler from the now
  * state, OnCondition assignments (from now values) overriding, OnStart in the
  * initialisation passes.  State u is izhikevich u / adEx w, s the last spike
@@ -580,6 +580,24 @@ static PORT_FN void izh_step(Port *P, int cur, int32_t k, int init, real t, real
             if (v > thresh && active) {
                 if (ref) sn = t;
                 vn = reset;
+                spike = 1;
+            }
+        }
+    } else if (kind == EDEN_POINT_IZH_DL) {
+        /* izhikevichCell: forward Euler with MSEC = 1000 us, MVOLT = 1 mV */
+        real v0 = p[0], thresh = p[1], a = p[2], b = p[3], c = p[4], d = p[5];
+        const real MV = R(1.0), MS = R(1000.0);
+        if (init) {
+            vn = v0;
+            un = (v0 * b) / MV;
+        } else {
+            real dv = ((R(0.04) * ((v * v) / MV) + R(5.0) * v) + ((R(140.0) - u) + iext) * MV) / MS;
+            real du = (a * ((b * v) / MV - u)) / MS;
+            vn = v + dt * dv;
+            un = u + dt * du;
+            if (v > thresh) {
+                vn = c * MV;
+                un = u + d;
                 spike = 1;
             }
         }

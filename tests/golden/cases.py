@@ -22,6 +22,7 @@ CASES = {
     "voltage_clamps": ("voltage_clamps", dict(), 1.0, None),
     "random_sources": ("random_sources", dict(), 1.0, None),
     "custom_setup": ("custom_setup", dict(), 1.0, None),
+    "dl_inputs": ("dl_inputs", dict(), 1.0, None),
 }
 
 

@@ -159,3 +159,22 @@ def test_inactive_triple_clamp_is_refused(tmp_path):
     nml.write_text(nml.read_text().replace('active="1"', 'active="0"'))
     with pytest.raises(ValueError, match="active"):
         neuroml_io.read_lems(lems)
+
+
+def test_dimensionless_inputs_round_trip_and_dimension_checks(tmp_path):
+    spec = spec_of("dl_inputs")
+    back = neuroml_io.read_lems(neuroml_io.write_lems(spec, str(tmp_path)))
+    a, b = lowering.lower(spec), lowering.lower(back)
+    for f in ("pulse_target", "pulse_amplitude", "pulse_weight", "wave_target", "wave_params", "izh_params",
+              "izh_kind"):
+        np.testing.assert_array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(b, f)), err_msg=f)
+    assert (a.izh_kind == lowering.POINT_IZH_DL).sum() == 6
+    # a dimensional pulse into an izhikevichCell, and a DL pulse into an izhikevich2007Cell, are refused
+    bad = spec_of("dl_inputs")
+    bad.pulses[0].dimensionless = False
+    with pytest.raises(ValueError, match="dimensionless"):
+        lowering.lower(bad)
+    bad = spec_of("dl_inputs")
+    bad.pulses[1].dimensionless = True
+    with pytest.raises(ValueError, match="dimensionless"):
+        lowering.lower(bad)
