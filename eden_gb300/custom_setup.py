@@ -10,19 +10,26 @@ values and units) and applies them to the instances' tables before the run
     set cell <population> <instance ids | all> all <property> multi <unit>
     values <one value per selected instance>
 
+    set input <inputList> <input ids | all> <property> <value | multi> [<unit>]
+
 Instance ids are comma-separated; a dimensional property needs its unit.
 Built here: `set cell` on point neurons (izhikevich2007Cell, iaf*Cell,
-adExIaFCell), whose LEMS parameters become per-instance values in the
-lowered model.  Not built: properties of physical cells (segment states,
-channel gates), `set input` and `set synapse` statements; they are refused
-by name.
+adExIaFCell, izhikevichCell), whose LEMS parameters become per-instance
+values in the lowered model, and `set input` on the pulse, sine, ramp (and
+their DL forms) and voltage-clamp inputs of lists read from NeuroML.  Not
+built: properties of physical cells (segment states, channel gates) and
+`set synapse` statements; they are refused by name.
 """
 from __future__ import annotations
 
 from dataclasses import dataclass
 from typing import List, Optional
 
-from .network import AdExCell, IafCell, Izhikevich2007Cell
+import copy
+
+import numpy as np
+
+from .network import WAVE_SINE, AdExCell, IafCell, Izhikevich2007Cell, IzhikevichCell
 
 # LEMS parameter -> (dataclass field, dimension of the unit table, factor to the field's unit)
 _IZH = {"v0": ("v0", "voltage", 1.0), "C": ("C", "capacitance", 1.0), "k": ("k", "cond_per_voltage", 1.0),
@@ -38,7 +45,13 @@ _ADEX = {"C": ("C", "capacitance", 1.0), "gL": ("gL", "conductance", 1.0), "EL":
          "a": ("a", "conductance", 1.0), "b": ("b", "current", 1.0)}
 
 
+_IZH_DL = {"v0": ("v0", "voltage", 1.0), "thresh": ("thresh", "voltage", 1.0), "a": ("a", None, 1.0),
+           "b": ("b", None, 1.0), "c": ("c", None, 1.0), "d": ("d", None, 1.0)}
+
+
 def _params_of(ct):
+    if isinstance(ct, IzhikevichCell):
+        return _IZH_DL
     if isinstance(ct, Izhikevich2007Cell):
         return _IZH
     if isinstance(ct, IafCell):
@@ -59,9 +72,50 @@ class SetCell:
     text: str = ""
 
 
-def parse(text: str, spec) -> List[SetCell]:
+@dataclass
+class SetInput:
+    """One `set input` statement: `values` (field units) of `prop` for the
+    inputs of list `lst` with the given input ids (None: all, by id)."""
+    lst: str
+    ids: Optional[List[int]]
+    prop: str
+    values: List[float]
+
+
+def _input_table(obj):
+    """Settable properties of an input object: NeuroML name -> (field, dimension, column)."""
+    from .network import ClampInputs, PulseInputs
+    cur = None if getattr(obj, "dimensionless", False) else "current"
+    common = {"delay": ("delay", "time", None), "duration": ("duration", "time", None)}
+    if isinstance(obj, PulseInputs):
+        return dict(common, amplitude=("amplitude", cur, None))
+    if isinstance(obj, ClampInputs):
+        t = dict(common, simpleSeriesResistance=("resistance", "resistance", None))
+        if obj.triple:
+            t.update(conditioningVoltage=("v_before", "voltage", None), testingVoltage=("v_during", "voltage", None),
+                     returnVoltage=("v_after", "voltage", None))
+        else:
+            t.update(targetVoltage=("v_during", "voltage", None))
+        return t
+    if obj.shape == WAVE_SINE:
+        return dict(common, amplitude=("p0", cur, None), period=("p1", "time", None), phase=("p2", None, None))
+    return dict(common, startAmplitude=("p0", cur, None), finishAmplitude=("p1", cur, None),
+                baselineAmplitude=("p2", cur, None))
+
+
+def _list_members(spec, lst):
+    """(input object, [(input id, item index)]) of inputList `lst`."""
+    for obj in list(spec.pulses) + list(spec.waves) + list(spec.clamps):
+        if not obj.list_ids:
+            continue
+        members = [(iid, i) for i, (name, iid) in enumerate(obj.list_ids) if name == lst]
+        if members:
+            return obj, sorted(members)
+    return None, []
+
+
+def parse(text: str, spec) -> list:
     """The statements of a custom setup file, checked against `spec`."""
-    from .neuroml_io import _UNITS
     lines = [ln.split("#", 1)[0].split() for ln in text.splitlines()]
     out = []
     i = 0
@@ -72,9 +126,33 @@ def parse(text: str, spec) -> List[SetCell]:
             continue
         if tok[0] != "set":
             raise ValueError(f"custom setup line {i}: unknown statement {tok[0]!r}")
+        if len(tok) >= 2 and tok[1] == "input":
+            if len(tok) < 6:
+                raise ValueError(f"custom setup line {i}: 'set input' needs list, inputs, property and value")
+            lst, ids_s, prop, value = tok[2], tok[3], tok[4], tok[5]
+            obj, members = _list_members(spec, lst)
+            if obj is None:
+                raise ValueError(f"custom setup line {i}: input list {lst} not found (or of a kind 'set input' "
+                                 f"does not cover)")
+            table = _input_table(obj)
+            if prop not in table:
+                raise ValueError(f"custom setup line {i}: input list {lst} has no settable property {prop!r}")
+            known = [iid for iid, _ in members]
+            ids = None
+            if ids_s != "all":
+                ids = [int(x) for x in ids_s.split(",")]
+                if len(set(ids)) != len(ids):
+                    raise ValueError(f"custom setup line {i}: an input is listed twice")
+                if any(x not in known for x in ids):
+                    raise ValueError(f"custom setup line {i}: input not in list {lst}")
+            field, dim, _ = table[prop]
+            vals, i = _values(lines, i, value, tok[6] if len(tok) > 6 else None, dim, 1.0,
+                              len(known) if ids is None else len(ids))
+            out.append(SetInput(lst, ids, field, vals))
+            continue
         if len(tok) < 2 or tok[1] != "cell":
             raise ValueError(f"custom setup line {i}: 'set {tok[1] if len(tok) > 1 else ''}' is not supported "
-                             f"(only 'set cell' on point neurons)")
+                             f"(only 'set cell' on point neurons and 'set input')")
         if len(tok) < 7:
             raise ValueError(f"custom setup line {i}: 'set cell' needs population, instances, segments, "
                              f"property and value")
@@ -100,25 +178,52 @@ def parse(text: str, spec) -> List[SetCell]:
             if bad:
                 raise ValueError(f"custom setup line {i}: instance {bad[0]} not in population {pop}")
         field, dim, factor = table[prop]
-        unit = tok[7] if len(tok) > 7 else None
-        scale = 1.0
-        if dim is not None:
-            if unit is None:
-                raise ValueError(f"custom setup line {i}: property {prop} needs units")
-            if unit not in _UNITS[dim]:
-                raise ValueError(f"custom setup line {i}: unit {unit!r} not known for {dim}")
-            scale = _UNITS[dim][unit] * factor
-        n_sel = pops[pop].size if ids is None else len(ids)
-        if value == "multi":
-            if i >= len(lines) or not lines[i] or lines[i][0] != "values":
-                raise ValueError(f"custom setup line {i}: 'multi' needs a 'values' line after it")
-            vals = [float(x) * scale for x in lines[i][1:]]
-            i += 1
-            if len(vals) != n_sel:
-                raise ValueError(f"custom setup line {i}: {len(vals)} values for {n_sel} instances")
-        else:
-            vals = [float(value) * scale] * n_sel
+        vals, i = _values(lines, i, value, tok[7] if len(tok) > 7 else None, dim, factor,
+                          pops[pop].size if ids is None else len(ids))
         out.append(SetCell(pop, ids, field, vals))
+    return out
+
+
+def _values(lines, i, value, unit, dim, factor, n_sel):
+    """The statement's values in field units, and the next line index."""
+    from .neuroml_io import _UNITS
+    scale = 1.0
+    if dim is not None:
+        if unit is None:
+            raise ValueError(f"custom setup line {i}: the property needs units")
+        if unit not in _UNITS[dim]:
+            raise ValueError(f"custom setup line {i}: unit {unit!r} not known for {dim}")
+        scale = _UNITS[dim][unit] * factor
+    if value == "multi":
+        if i >= len(lines) or not lines[i] or lines[i][0] != "values":
+            raise ValueError(f"custom setup line {i}: 'multi' needs a 'values' line after it")
+        vals = [float(x) * scale for x in lines[i][1:]]
+        i += 1
+        if len(vals) != n_sel:
+            raise ValueError(f"custom setup line {i}: {len(vals)} values for {n_sel} instances")
+    else:
+        vals = [float(value) * scale] * n_sel
+    return vals, i
+
+
+def apply_inputs(spec):
+    """A copy of `spec` whose input objects carry the `set input`
+    statements' values (later statements win); `spec` itself is unchanged."""
+    stmts = [st for st in spec.custom_setup if isinstance(st, SetInput)]
+    if not stmts:
+        return spec
+    out = copy.copy(spec)
+    out.pulses = [copy.copy(x) for x in spec.pulses]
+    out.waves = [copy.copy(x) for x in spec.waves]
+    out.clamps = [copy.copy(x) for x in spec.clamps]
+    for st in stmts:
+        obj, members = _list_members(out, st.lst)
+        by_id = dict(members)
+        ids = [iid for iid, _ in members] if st.ids is None else st.ids
+        arr = np.array(getattr(obj, st.prop), dtype=np.float64, copy=True)
+        for iid, v in zip(ids, st.values):
+            arr[by_id[iid]] = v
+        setattr(obj, st.prop, arr)
     return out
 
 
@@ -128,6 +233,8 @@ def overrides(spec) -> dict:
     res = {}
     pops = {p.name: p for p in spec.populations}
     for st in spec.custom_setup:
+        if not isinstance(st, SetCell):
+            continue
         ids = list(range(pops[st.pop].size)) if st.ids is None else st.ids
         for inst, v in zip(ids, st.values):
             res.setdefault((st.pop, inst), {})[st.prop] = float(v)
@@ -141,6 +248,14 @@ def write(spec, path: str) -> None:
                "conductance": "nS", "current": "nA", "time": "ms"}
     with open(path, "w") as f:
         for st in spec.custom_setup:
+            if isinstance(st, SetInput):
+                obj, members = _list_members(spec, st.lst)
+                prop, (field, dim, _) = next((k, v) for k, v in _input_table(obj).items() if v[0] == st.prop)
+                ids = "all" if st.ids is None else ",".join(str(x) for x in st.ids)
+                unit = {None: "", "current": " nA", "time": " ms", "voltage": " mV", "resistance": " Mohm"}[dim]
+                f.write(f"set input {st.lst} {ids} {prop} multi{unit}\n")
+                f.write("values " + " ".join(_f(v) for v in st.values) + "\n")
+                continue
             ct = spec.cell_type({p.name: p for p in spec.populations}[st.pop].cell_type)
             prop, (field, dim, factor) = next((k, v) for k, v in _params_of(ct).items() if v[0] == st.prop)
             ids = "all" if st.ids is None else ",".join(str(x) for x in st.ids)
@@ -155,4 +270,4 @@ def apply_to(ct, fields: dict):
     return dataclasses.replace(ct, **fields)
 
 
-__all__ = ["SetCell", "parse", "overrides", "write", "apply_to"]
+__all__ = ["SetCell", "SetInput", "parse", "overrides", "write", "apply_to", "apply_inputs"]

@@ -289,6 +289,7 @@ class PulseInputs:
     amplitude: np.ndarray
     weight: Optional[np.ndarray] = None
     dimensionless: bool = False   # pulseGeneratorDL (amplitude without unit, into izhikevichCell)
+    list_ids: Optional[list] = None   # per input, (inputList id, input id) as read from NeuroML
 
 
 @dataclass
@@ -307,6 +308,7 @@ class ClampInputs:
     v_after: np.ndarray
     resistance: np.ndarray
     weight: np.ndarray
+    list_ids: Optional[list] = None   # per input, (inputList id, input id) as read from NeuroML
 
 
 @dataclass
@@ -341,6 +343,7 @@ class WaveInputs:
     p2: np.ndarray
     weight: np.ndarray
     dimensionless: bool = False   # sine/rampGeneratorDL (amplitudes without unit, into izhikevichCell)
+    list_ids: Optional[list] = None   # per input, (inputList id, input id) as read from NeuroML
 
 
 @dataclass

@@ -234,22 +234,31 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
                   f'weight="{_f(pr.weight[i])}" delay="{_f(pr.delay[i])}ms"/>\n')
             w(' </projection>\n')
     n_list = 0
-    for pi in spec.pulses:
+
+    def input_lists(obj, comp_of, weighted):
+        # one inputList per component and population, or the lists (and
+        # input ids) the items were read from
+        nonlocal n_list
         by_comp = defaultdict(list)
-        for i in range(len(pi.cell)):
-            key = (float(pi.delay[i]), float(pi.duration[i]), float(pi.amplitude[i]), pi.dimensionless)
-            by_comp[(pulse_ids[key], pop_of[pi.cell[i]])].append(i)
-        for (pid, pop), idx in by_comp.items():
-            w(f' <inputList id="il{n_list}" component="{pid}" population="{pop}">\n')
+        for i in range(len(obj.cell)):
+            lname = obj.list_ids[i][0] if obj.list_ids else None
+            by_comp[(comp_of(i), pop_of[obj.cell[i]], lname)].append(i)
+        for (cid, pop, lname), idx in by_comp.items():
+            w(f' <inputList id="{lname or f"il{n_list}"}" component="{cid}" population="{pop}">\n')
             n_list += 1
             for n, i in enumerate(idx):
-                if pi.weight is not None:
-                    w(f'  <inputW id="{n}" target="../{pop}[{local_of[pi.cell[i]]}]" segmentId="{pi.seg[i]}" '
-                      f'fractionAlong="0.5" destination="synapses" weight="{_f(pi.weight[i])}"/>\n')
-                    continue
-                w(f'  <input id="{n}" target="../{pop}[{local_of[pi.cell[i]]}]" segmentId="{pi.seg[i]}" '
-                  f'fractionAlong="0.5" destination="synapses"/>\n')
+                iid = obj.list_ids[i][1] if obj.list_ids else n
+                tgt = f'target="../{pop}[{local_of[obj.cell[i]]}]" segmentId="{obj.seg[i]}" fractionAlong="0.5"'
+                if weighted:
+                    w(f'  <inputW id="{iid}" {tgt} destination="synapses" weight="{_f(obj.weight[i])}"/>\n')
+                else:
+                    w(f'  <input id="{iid}" {tgt} destination="synapses"/>\n')
             w(' </inputList>\n')
+
+    for pi in spec.pulses:
+        input_lists(pi, lambda i, pi=pi: pulse_ids[(float(pi.delay[i]), float(pi.duration[i]),
+                                                     float(pi.amplitude[i]), pi.dimensionless)],
+                    pi.weight is not None)
     for k, po in enumerate(spec.poissons):
         by_pop = defaultdict(list)
         for i in range(len(po.cell)):
@@ -262,27 +271,9 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
                   f'fractionAlong="0.5" destination="synapses"/>\n')
             w(' </inputList>\n')
     for cl in spec.clamps:
-        by_comp = defaultdict(list)
-        for i in range(len(cl.cell)):
-            by_comp[(clamp_ids[_clamp_key(cl, i)], pop_of[cl.cell[i]])].append(i)
-        for (cid, pop), idx in by_comp.items():
-            w(f' <inputList id="il{n_list}" component="{cid}" population="{pop}">\n')
-            n_list += 1
-            for n, i in enumerate(idx):
-                w(f'  <inputW id="{n}" target="../{pop}[{local_of[cl.cell[i]]}]" segmentId="{cl.seg[i]}" '
-                  f'fractionAlong="0.5" destination="synapses" weight="{_f(cl.weight[i])}"/>\n')
-            w(' </inputList>\n')
+        input_lists(cl, lambda i, cl=cl: clamp_ids[_clamp_key(cl, i)], True)
     for wv in spec.waves:
-        by_comp = defaultdict(list)
-        for i in range(len(wv.cell)):
-            by_comp[(wave_ids[_wave_key(wv, i)], pop_of[wv.cell[i]])].append(i)
-        for (wid, pop), idx in by_comp.items():
-            w(f' <inputList id="il{n_list}" component="{wid}" population="{pop}">\n')
-            n_list += 1
-            for n, i in enumerate(idx):
-                w(f'  <inputW id="{n}" target="../{pop}[{local_of[wv.cell[i]]}]" segmentId="{wv.seg[i]}" '
-                  f'fractionAlong="0.5" destination="synapses" weight="{_f(wv.weight[i])}"/>\n')
-            w(' </inputList>\n')
+        input_lists(wv, lambda i, wv=wv: wave_ids[_wave_key(wv, i)], True)
     for tid, k, i in timed_ids:
         ti = spec.timed[k]
         pop = pop_of[ti.cell[i]]
@@ -815,7 +806,7 @@ def read_lems(path: str) -> NetworkSpec:
                                            np.array(rows[1], np.int64), np.array(rows[2], np.int64),
                                            np.array(rows[3]), np.array(rows[4])))
     # inputs
-    pcell, pseg, pdel, pdur, pamp, pwt, pdl = [], [], [], [], [], [], []
+    pcell, pseg, pdel, pdur, pamp, pwt, pdl, plist = [], [], [], [], [], [], [], []
     pois_rows, wave_rows, clamp_rows = {}, {}, {}
     timed_rows = {}
     for il in _children(net, "inputList"):
@@ -830,12 +821,15 @@ def read_lems(path: str) -> NetworkSpec:
                 d, du, a, dl = pulses_def[comp]
                 pcell.append(g); pseg.append(seg); pdel.append(d); pdur.append(du); pamp.append(a)
                 pwt.append(float(inp.get("weight", "1"))); pdl.append(dl)
+                plist.append((il.get("id"), int(inp.get("id"))))
             elif comp in pois_def:
                 pois_rows.setdefault(comp, []).append((g, seg))
             elif comp in wave_def:
-                wave_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1"))))
+                wave_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1")),
+                                                       (il.get("id"), int(inp.get("id")))))
             elif comp in clamp_def:
-                clamp_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1"))))
+                clamp_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1")),
+                                                        (il.get("id"), int(inp.get("id")))))
             else:
                 raise ValueError(f"inputList component {comp} not supported")
     for ei in _children(net, "explicitInput"):
@@ -845,15 +839,17 @@ def read_lems(path: str) -> NetworkSpec:
             raise ValueError(f"explicitInput {comp} not supported")
         d, du, a, dl = pulses_def[comp]
         pcell.append(g); pseg.append(0); pdel.append(d); pdur.append(du); pamp.append(a); pwt.append(1.0)
-        pdl.append(dl)
+        pdl.append(dl); plist.append(None)
     for dl in (False, True):
         sel = [i for i in range(len(pcell)) if pdl[i] == dl]
         if not sel:
             continue
         pick = lambda xs: np.array([xs[i] for i in sel])
         wts = pick(pwt)
+        lids = [plist[i] for i in sel]
         spec.pulses.append(PulseInputs("*", pick(pcell), pick(pseg), pick(pdel), pick(pdur), pick(pamp),
-                                       None if (wts == 1.0).all() else wts, dl))
+                                       None if (wts == 1.0).all() else wts, dl,
+                                       None if any(x is None for x in lids) else lids))
     for syn, rows in timed_rows.items():
         if syn not in synapses:
             raise ValueError(f"timedSynapticInput: synapse {syn} not supported")
@@ -876,14 +872,14 @@ def read_lems(path: str) -> NetworkSpec:
         spec.clamps.append(ClampInputs(triple, np.array([r[0] for r in rows], np.int64),
                                        np.array([r[1] for r in rows], np.int64), np.full(n, d), np.full(n, du),
                                        np.full(n, vb), np.full(n, vd), np.full(n, va), np.full(n, res),
-                                       np.array([r[2] for r in rows])))
+                                       np.array([r[2] for r in rows]), [r[3] for r in rows]))
     for comp, rows in wave_rows.items():
         shape, d, du, a, b, c, dl = wave_def[comp]
         n = len(rows)
         spec.waves.append(WaveInputs(shape, np.array([r[0] for r in rows], np.int64),
                                      np.array([r[1] for r in rows], np.int64), np.full(n, d), np.full(n, du),
                                      np.full(n, a), np.full(n, b), np.full(n, c),
-                                     np.array([r[2] for r in rows]), dl))
+                                     np.array([r[2] for r in rows]), dl, [r[3] for r in rows]))
     # recorders: OutputFile / EventOutputFile and EDEN's EdenOutputFile /
     # EdenEventOutputFile with their time window, sampling interval or explicit
     # sample points, and heartbeat interval (eden/NeuroML.cpp:8037-8290);

@@ -673,7 +673,9 @@ set cell izh 3 all v0 -58 mV
 def custom_setup(length_ms: float = 100.0, dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
     """Point-neuron populations whose parameters an EdenCustomSetup file
     overrides per instance (single values, per-instance lists, repeated
-    statements on the same instance), driven by DC pulses."""
+    statements on the same instance), driven by DC pulses from one input
+    list per population whose amplitudes, delays and durations the file
+    sets per input."""
     from .custom_setup import parse
     rng = np.random.default_rng(seed)
     spec = NetworkSpec("custom_setup", dt_ms, length_ms, seed)
@@ -684,10 +686,21 @@ def custom_setup(length_ms: float = 100.0, dt_ms: float = 0.025, seed: int = 123
                                tauw=144.0, refract=0.0, a=4.0, b=0.0805))
     spec.populations += [Population("izh", "izRS", 6), Population("iaf", "iafRef", 4), Population("adex", "adex", 4)]
     n = 14
-    amp = np.concatenate([np.round(rng.uniform(0.1, 0.3, 6), 4), np.round(rng.uniform(0.2, 0.4, 4), 4),
-                          np.round(rng.uniform(0.6, 1.0, 4), 4)])
-    spec.pulses.append(PulseInputs("*", np.arange(n), np.zeros(n, int), np.full(n, 5.0), np.full(n, length_ms), amp))
-    spec.custom_setup = parse(CUSTOM_SETUP_TEXT, spec)
+    # one input list per population, one pulse component each; the setup
+    # file varies their amplitudes and timing per input
+    sizes = {"stim_izh": (0, 6, 0.2), "stim_iaf": (6, 4, 0.3), "stim_adex": (10, 4, 0.8)}
+    for lst, (g0, k, a) in sizes.items():
+        spec.pulses.append(PulseInputs("*", g0 + np.arange(k), np.zeros(k, int), np.full(k, 5.0),
+                                       np.full(k, length_ms), np.full(k, a),
+                                       list_ids=[(lst, j) for j in range(k)]))
+    text = CUSTOM_SETUP_TEXT + "".join([
+        "set input stim_izh all amplitude multi nA\n",
+        "values " + " ".join(str(x) for x in np.round(rng.uniform(0.1, 0.3, 6), 4)) + "\n",
+        "set input stim_iaf 1,3 delay 20 ms\n",
+        "set input stim_adex all duration multi ms\n",
+        "values 30 50 70 90\n",
+        "set input stim_adex 2 amplitude 1.0 nA\n"])
+    spec.custom_setup = parse(text, spec)
     spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), 0) for g in range(n)]
     spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
     return spec

@@ -46,7 +46,9 @@ def test_round_trip(tmp_path):
 
 
 @pytest.mark.parametrize("text,match", [
-    ("set input Input0 0 amplitude 14\n", "not supported"),
+    ("set input Input0 0 amplitude 14\n", "not found"),
+    ("set input stim_izh 0 period 2 ms\n", "settable"),
+    ("set input stim_izh 9 amplitude 0.1 nA\n", "not in list"),
     ("set synapse proj all post erev 0.05 V\n", "not supported"),
     ("set cell izh 1 all v0 -64\n", "units"),
     ("set cell izh 1 all w0 -64 mV\n", "settable"),
@@ -64,3 +66,15 @@ def test_physical_cells_are_refused():
     spec = workloads.single_comp_hh(n_cells=2, length_ms=1.0)
     with pytest.raises(ValueError, match="point neurons only"):
         custom_setup.parse(f"set cell {spec.populations[0].name} all all v -60 mV\n", spec)
+
+
+def test_oracle_needs_the_input_statements():
+    """Dropping only the 'set input' statements: the fixture no longer matches."""
+    import copy
+    spec = spec_of("custom_setup")
+    ref, _, _ = load("custom_setup", lowering.lower(spec))
+    s = copy.copy(spec)
+    s.custom_setup = [st for st in spec.custom_setup if not isinstance(st, custom_setup.SetInput)]
+    assert len(s.custom_setup) < len(spec.custom_setup)
+    bad = eden_port.run(lowering.lower(s))
+    assert np.abs(bad["trace"] - ref).max() > 5.0
