@@ -69,7 +69,6 @@ class SetCell:
     ids: Optional[List[int]]
     prop: str
     values: List[float]
-    text: str = ""
 
 
 @dataclass

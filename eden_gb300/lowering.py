@@ -31,7 +31,7 @@ from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, IafCell,
                       NetworkSpec,
                       PhysicalCell, SpikeArrayCell, SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       WAVE_RAMP, WAVE_SINE,
-                      SYN_EXPONE, SYN_EXPTWO)
+                      SYN_EXPTWO)
 
 F32 = np.float32
 MAX_GATES = 4
