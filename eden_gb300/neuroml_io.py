@@ -573,10 +573,10 @@ def read_event_set(path: str, instances: int, ports: int) -> list:
 
 def _cell_ref(text, pops, default_pop=None):
     """'../pop[3]', '../pop/3/celltype', 'pop[3]', 'pop/3', or a bare index
-    of the projection's population -> (population, index)."""
+    ('3' or '/3') of the projection's population -> (population, index)."""
     t = text.strip()
-    if default_pop is not None and re.fullmatch(r"\d+", t):
-        return default_pop, int(t)
+    if default_pop is not None and re.fullmatch(r"/?\d+", t):
+        return default_pop, int(t.lstrip("/"))
     while t.startswith("../"):
         t = t[3:]
     m = re.match(r"^([^/\[\]]+)\[(\d+)\]", t)
@@ -612,6 +612,7 @@ def read_lems(path: str) -> NetworkSpec:
     # components
     channels_by_name, synapses, pulses_def, pois_def, cells = {}, {}, {}, {}, {}
     timed_def, wave_def, clamp_def = {}, {}, {}
+    refused_inputs = {}
     net = None
     for e in elems:
         t = _tag(e)
@@ -668,9 +669,10 @@ def read_lems(path: str) -> NetworkSpec:
             pois_def[e.get("id")] = (_qty(e, "averageRate", "frequency_hz"), e.get("synapse"))
         elif t == "transientPoissonFiringSynapse":
             # the reference writes this component's LONG_TIME constant (1e9
-            # hour) as `inf` into its generated C, which then fails to compile
-            raise ValueError(f"transientPoissonFiringSynapse {e.get('id')}: not supported (the reference "
-                             f"simulator cannot run it either)")
+            # hour) as `inf` into its generated C, which then fails to compile:
+            # refused where an input list uses it (a definition alone is fine)
+            refused_inputs[e.get("id")] = (f"transientPoissonFiringSynapse {e.get('id')}: not supported (the "
+                                           f"reference simulator cannot run it either)")
         elif t in ("voltageClamp", "voltageClampTriple"):
             if e.get("simpleSeriesResistance") is not None:
                 res = _qty(e, "simpleSeriesResistance", "resistance")
@@ -830,6 +832,8 @@ def read_lems(path: str) -> NetworkSpec:
             elif comp in clamp_def:
                 clamp_rows.setdefault(comp, []).append((g, seg, float(inp.get("weight", "1")),
                                                         (il.get("id"), int(inp.get("id")))))
+            elif comp in refused_inputs:
+                raise ValueError(refused_inputs[comp])
             else:
                 raise ValueError(f"inputList component {comp} not supported")
     for ei in _children(net, "explicitInput"):

@@ -20,6 +20,18 @@ def available() -> bool:
     return os.path.exists(EDEN)
 
 
+# the reference source tree (as oracle/Makefile's REF); its validation
+# networks are read from there when it is present
+REF = os.environ.get("EDEN_REFERENCE_TREE", "/root/reference")
+
+
+def validation_network(name: str):
+    """Path of one of the reference's own validation networks
+    (testing/validation_tests/neuroml/<name>), or None without the tree."""
+    p = os.path.join(REF, "testing", "validation_tests", "neuroml", name)
+    return p if os.path.exists(p) else None
+
+
 def run(lems_path: str, threads: int = 1, extra=(), keep_dir=None):
     """Returns dict(trajectory=[n, 1+cols] float64 (time s, values SI),
     events=list of (time s, id), run_s=float, stdout=str)."""

@@ -1,0 +1,42 @@
+"""The reference's own validation networks (its testing/validation_tests),
+read by this package's NeuroML reader and run by the oracle, against the
+reference simulator's output on the same files.  Runs where the reference
+tree and its build (oracle/_ref) are present; skipped elsewhere.  The GPU
+path is checked against the oracle by the parity tests on the seeded cases
+that cover the same input kinds."""
+import os
+import shutil
+import tempfile
+
+import numpy as np
+import pytest
+
+import eden_port
+import reference_runner
+from eden_gb300 import lowering, neuroml_io
+
+
+@pytest.mark.parametrize("name,outfile", [
+    ("LEMS_EdenTest_CoreInputs.xml", "results.gen.txt"),
+    ("LEMS_EdenTest_PassiveCompartment.xml", None),
+])
+def test_oracle_matches_the_reference_on_its_validation_network(name, outfile):
+    path = reference_runner.validation_network(name)
+    if path is None or not reference_runner.available():
+        pytest.skip("reference tree or its build not present")
+    spec = neuroml_io.read_lems(path)
+    low = lowering.lower(spec)
+    work = tempfile.mkdtemp(prefix="eden_val_")
+    try:
+        reference_runner.run(path, threads=2, keep_dir=work)
+        files = [outfile] if outfile else [f for f in os.listdir(work) if f.endswith(".txt") and "spike" not in f
+                                           and f not in os.listdir(os.path.dirname(path))]
+        ref = np.loadtxt(os.path.join(work, files[0]), ndmin=2)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    out = eden_port.run(low)
+    assert out["rc"] == 0
+    mine = out["trace"].astype(np.float64)
+    ref_mv = ref[:, 1:] * 1e3
+    assert mine.shape == ref_mv.shape
+    assert np.abs(mine - ref_mv).max() < 0.01
