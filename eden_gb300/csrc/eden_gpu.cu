@@ -639,7 +639,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             // the value the initialisation passes give V (OnStart)
             const int64_t uk = ut - n_comp;
             const int kind = m->izh_kind ? m->izh_kind[uk] : EDEN_POINT_IZH2007;
-            const int f = kind == EDEN_POINT_IZH2007 ? 1
+            const int f = kind == EDEN_POINT_FN ? 1
+                          : kind == EDEN_POINT_IZH2007 ? 1
                           : (kind == EDEN_POINT_IAF_TAU || kind == EDEN_POINT_IAF_TAU_REF || kind == EDEN_POINT_IZH_DL) ? 0
                                                                                                                    : 2;
             v0[it] = m->izh_params[EDEN_POINT_PARAMS * uk + f];

@@ -825,6 +825,18 @@ __device__ __forceinline__ bool point_update(int kind, const float *p, int ps, b
         }
         break;
     }
+    case EDEN_POINT_FN: {
+        // fitzHughNagumoCell: V' = ((V - V^3 / 3) - W + I) / s, W' = 0.08 (V + 0.7 - 0.8 W) / s
+        const float SEC = 1.0e6f;
+        if (init) {
+            vn = v;
+            break;
+        }
+        const float w = u;
+        vn = v + dt * ((((v - powf(v, 3.0f) / 3.0f) - w) + PP(0)) / SEC);
+        u = w + dt * ((0.08f * ((v + 0.7f) - 0.8f * w)) / SEC);
+        break;
+    }
     case EDEN_POINT_IZH_DL: {
         // izhikevichCell: v' = (0.04 v^2 / mV + 5 v + (140 - U + I) mV) / ms,
         // U' = a (b v / mV - U) / ms; above thresh v = c mV, U += d

@@ -27,7 +27,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, IafCell, Izhikevich2007Cell, IzhikevichCell,
+from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, FitzHughNagumoCell, IafCell,
+                      Izhikevich2007Cell, IzhikevichCell,
                       NetworkSpec,
                       PhysicalCell, SpikeArrayCell, SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       WAVE_RAMP, WAVE_SINE,
@@ -237,7 +238,7 @@ def gate_q10(gate, temperature_degc: float) -> np.float32:
 # waveform inputs (include/eden_gpu.h EDEN_WAVE_*)
 WAVE_PARAMS = 5
 WAVE_SHAPES = {WAVE_SINE: 0, WAVE_RAMP: 1}
-POINT_IZH2007, POINT_IAF_TAU, POINT_IAF_TAU_REF, POINT_IAF, POINT_IAF_REF, POINT_ADEX, POINT_IZH_DL = range(7)
+POINT_IZH2007, POINT_IAF_TAU, POINT_IAF_TAU_REF, POINT_IAF, POINT_IAF_REF, POINT_ADEX, POINT_IZH_DL, POINT_FN = range(8)
 _IAF_KINDS = {"iafTauCell": POINT_IAF_TAU, "iafTauRefCell": POINT_IAF_TAU_REF, "iafCell": POINT_IAF,
               "iafRefCell": POINT_IAF_REF}
 
@@ -260,6 +261,8 @@ def point_params(ct):
                             ct.refract * 1e3, ct.a * 1e-3, ct.b]
     if isinstance(ct, IzhikevichCell):
         return POINT_IZH_DL, [ct.v0, ct.thresh, ct.a, ct.b, ct.c, ct.d]
+    if isinstance(ct, FitzHughNagumoCell):
+        return POINT_FN, [ct.I, 0.0]          # I, and V's value before the run (W starts at 0 too)
     raise ValueError(f"not a point neuron: {type(ct).__name__}")
 
 
@@ -592,11 +595,11 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                 src_target[gid] = -1
                 gid_base[gid] = -1
                 ext_cells.setdefault(ct.name, (ct, []))[1].append(gid)
-            elif isinstance(ct, (Izhikevich2007Cell, IafCell, AdExCell, IzhikevichCell)):
+            elif isinstance(ct, (Izhikevich2007Cell, IafCell, AdExCell, IzhikevichCell, FitzHughNagumoCell)):
                 gid_is_izh[gid] = True
                 izh_index[gid] = len(izh)
                 kind, params = point_params(ct)
-                no_current[gid] = kind in (POINT_IAF_TAU, POINT_IAF_TAU_REF)
+                no_current[gid] = kind in (POINT_IAF_TAU, POINT_IAF_TAU_REF, POINT_FN)
                 dl_cell[gid] = kind == POINT_IZH_DL
                 izh.append(params + [0.0] * (POINT_PARAMS - len(params)))
                 izh_kind.append(kind)

@@ -154,6 +154,14 @@ class IzhikevichCell:
 
 
 @dataclass
+class FitzHughNagumoCell:
+    """fitzHughNagumoCell: dimensionless V and W driven by the constant I;
+    takes no input current and emits no spikes (its V is recorded as "V")."""
+    name: str
+    I: float
+
+
+@dataclass
 class IafCell:
     """iafTauCell, iafTauRefCell, iafCell or iafRefCell (`kind`), NeuroML
     units: mV, ms, nS, pF.  The *Tau* kinds have no capacitance, leak

@@ -25,7 +25,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       SpikeGeneratorRandomCell, SynapseType,
                       EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
-                      ClampInputs, IzhikevichCell, TimedInputs, WaveInputs)
+                      ClampInputs, FitzHughNagumoCell, IzhikevichCell, TimedInputs, WaveInputs)
 
 
 def _f(x: float) -> str:
@@ -117,6 +117,8 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w(f'<adExIaFCell id="{c.name}" C="{_f(c.C)}pF" gL="{_f(c.gL)}nS" EL="{_f(c.EL)}mV" VT="{_f(c.VT)}mV" '
               f'thresh="{_f(c.thresh)}mV" reset="{_f(c.reset)}mV" delT="{_f(c.delT)}mV" tauw="{_f(c.tauw)}ms" '
               f'refract="{_f(c.refract)}ms" a="{_f(c.a)}nS" b="{_f(c.b)}nA"/>\n')
+        elif isinstance(c, FitzHughNagumoCell):
+            w(f'<fitzHughNagumoCell id="{c.name}" I="{_f(c.I)}"/>\n')
         elif isinstance(c, IzhikevichCell):
             w(f'<izhikevichCell id="{c.name}" v0="{_f(c.v0)}mV" thresh="{_f(c.thresh)}mV" a="{_f(c.a)}" '
               f'b="{_f(c.b)}" c="{_f(c.c)}" d="{_f(c.d)}"/>\n')
@@ -316,7 +318,8 @@ def _quantity_path(spec, col: OutputColumn) -> str:
     ct = spec.cell_type(spec.population(col.pop).cell_type)
     if isinstance(ct, PhysicalCell):
         return f"{col.pop}/{col.cell}/{ct.name}/{col.seg}/v"
-    return f"{col.pop}/{col.cell}/{ct.name}/v"
+    # a fitzHughNagumoCell's membrane variable is the dimensionless V
+    return f"{col.pop}/{col.cell}/{ct.name}/{'V' if isinstance(ct, FitzHughNagumoCell) else 'v'}"
 
 
 def _select_path(spec, ev: EventSelection) -> str:
@@ -659,6 +662,8 @@ def read_lems(path: str) -> NetworkSpec:
             dl = t.endswith("DL")
             pulses_def[e.get("id")] = (_qty(e, "delay", "time"), _qty(e, "duration", "time"),
                                        _qty(e, "amplitude", None if dl else "current"), dl)
+        elif t == "fitzHughNagumoCell":
+            cells[e.get("id")] = FitzHughNagumoCell(e.get("id"), _qty(e, "I", None))
         elif t == "izhikevichCell":
             cells[e.get("id")] = IzhikevichCell(e.get("id"), _qty(e, "v0", "voltage"), _qty(e, "thresh", "voltage"),
                                                 _qty(e, "a", None), _qty(e, "b", None), _qty(e, "c", None),
@@ -913,8 +918,10 @@ def read_lems(path: str) -> NetworkSpec:
             units = col.get("output_units") if _tag(of) == "EdenOutputFile" else "V"
             if units not in volt_out:
                 raise ValueError(f"OutputColumn {col.get('id')}: output_units {units!r} not supported")
+            # a fitzHughNagumoCell's V is dimensionless: written as it is
+            scale = 1.0 if col.get("quantity").strip().endswith("/V") else volt_out[units]
             cols.append((col.get("id"), col.get("quantity"), _quantity_target(col.get("quantity"), pops, cells),
-                         volt_out[units]))
+                         scale))
         points = None
         for sp in _children(of, "SamplePoints"):
             points = [_qty(x, "t", "time") * 1e3 for x in _children(sp, "s")]
@@ -944,8 +951,9 @@ def read_lems(path: str) -> NetworkSpec:
 def _quantity_target(q, pops, cells):
     """'pop/3/celltype/seg/v', 'pop/3/celltype/v' or 'pop[3]/v' -> (pop, cell, seg)."""
     parts = q.strip().split("/")
-    if parts[-1] != "v":
-        raise ValueError(f"recorded quantity {q!r}: only membrane potential v is supported")
+    if parts[-1] not in ("v", "V"):
+        raise ValueError(f"recorded quantity {q!r}: only membrane potential v (a fitzHughNagumoCell's V) "
+                         f"is supported")
     m = re.match(r"^([^/\[\]]+)\[(\d+)\]$", parts[0])
     if m:
         pop, idx, rest = m.group(1), int(m.group(2)), parts[1:-1]

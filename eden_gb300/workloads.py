@@ -55,7 +55,7 @@ from __future__ import annotations
 import numpy as np
 
 from .network import (RATE_EXP, RATE_EXPLINEAR, RATE_SIGMOID, AdExCell, Channel, ChannelDensity, EventSelection,
-                      ClampInputs, Gate, IafCell, Izhikevich2007Cell, IzhikevichCell, Rate,
+                      ClampInputs, FitzHughNagumoCell, Gate, IafCell, Izhikevich2007Cell, IzhikevichCell, Rate,
                       NetworkSpec, OutputColumn, PhysicalCell, PoissonInputs,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
                       SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
@@ -622,13 +622,15 @@ def dl_inputs(n_dl: int = 6, length_ms: float = 100.0, dt_ms: float = 0.025, see
     pulseGeneratorDL, sineGeneratorDL and rampGeneratorDL inputs with seeded
     amplitudes, weighted, beside izhikevich2007 cells with pulse and sine
     generators; the two kinds connect through expOne synapses only into the
-    izhikevich2007 cells."""
+    izhikevich2007 cells.  Two fitzHughNagumoCell oscillators run beside
+    them (no inputs)."""
     rng = np.random.default_rng(seed)
     spec = NetworkSpec("dl_inputs", dt_ms, length_ms, seed)
     spec.cells.append(IzhikevichCell("izMixed", v0=-70.0, thresh=30.0, a=0.02, b=0.2, c=-55.0, d=4.0))
     spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
     spec.synapses.append(SynapseType("syn_e1", SYN_EXPONE, gbase=2.0, erev=0.0, tau_decay=2.0))
-    spec.populations += [Population("dl", "izMixed", n_dl), Population("iz", "izRS", 3)]
+    spec.cells.append(FitzHughNagumoCell("fn1", I=0.8))
+    spec.populations += [Population("dl", "izMixed", n_dl), Population("iz", "izRS", 3), Population("fn", "fn1", 2)]
     dl = np.arange(n_dl)
     spec.pulses.append(PulseInputs("*", dl, np.zeros(n_dl, int), np.round(rng.uniform(0.0, 20.0, n_dl), 3),
                                    np.round(rng.uniform(30.0, 70.0, n_dl), 3), np.round(rng.uniform(5.0, 15.0, n_dl), 3),
@@ -646,7 +648,7 @@ def dl_inputs(n_dl: int = 6, length_ms: float = 100.0, dt_ms: float = 0.025, see
                                    np.array([0.08, 0.1, 0.12])))
     spec.projections.append(_flat_projection(spec, "proj_e1", dl[:3], iz, "syn_e1", np.full(3, 0.5),
                                              np.full(3, 1.0)))
-    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), 0) for g in range(n_dl + 3)]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), 0) for g in range(n_dl + 5)]
     spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n_dl + 3)]
     return spec
 

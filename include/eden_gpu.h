@@ -78,7 +78,9 @@ enum {
     EDEN_POINT_IZH_DL = 6,      /* izhikevichCell (LEMS_CoreComponents.inc.xml izhikevichCell):
                                    v0, thresh (mV), a, b, c, d (dimensionless); its input
                                    current is dimensionless (the *GeneratorDL inputs) */
-    EDEN_POINT_KINDS = 7
+    EDEN_POINT_FN = 7,          /* fitzHughNagumoCell: I (dimensionless); V, W dimensionless,
+                                   no input current, no spikes */
+    EDEN_POINT_KINDS = 8
 };
 #define EDEN_POINT_PARAMS 16
 

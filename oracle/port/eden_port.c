@@ -42,12 +42,14 @@ typedef double real;
 #define EXP exp
 #define LOG log
 #define SIN sin
+#define POW pow
 #else
 typedef float real;
 #define R(x) x##f
 #define EXP expf
 #define LOG logf
 #define SIN sinf
+#define POW powf
 #endif
 #include <stdint.h>
 #include <stdlib.h>
@@ -583,6 +585,14 @@ static PORT_FN void izh_step(Port *P, int cur, int32_t k, int init, real t, real
                 spike = 1;
             }
         }
+    } else if (kind == EDEN_POINT_FN) {
+        /* fitzHughNagumoCell: forward Euler with SEC = 1e6 us; V and W keep
+         * their initial values through the initialisation passes */
+        const real SEC = R(1.0e6);
+        if (!init) {
+            vn = v + dt * ((((v - POW(v, R(3.0)) / R(3.0)) - u) + (real)p[0]) / SEC);
+            un = u + dt * ((R(0.08) * ((v + R(0.7)) - R(0.8) * u)) / SEC);
+        }
     } else if (kind == EDEN_POINT_IZH_DL) {
         /* izhikevichCell: forward Euler with MSEC = 1000 us, MVOLT = 1 mV */
         real v0 = p[0], thresh = p[1], a = p[2], b = p[3], c = p[4], d = p[5];
@@ -701,7 +711,8 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
         for (int32_t k = 0; k < m->n_izh; k++) {
             /* the value OnStart gives V */
             int kind = m->izh_kind ? m->izh_kind[k] : EDEN_POINT_IZH2007;
-            int f = kind == EDEN_POINT_IZH2007 ? 1 : (kind == EDEN_POINT_IAF_TAU || kind == EDEN_POINT_IAF_TAU_REF) ? 0 : 2;
+            int f = (kind == EDEN_POINT_IZH2007 || kind == EDEN_POINT_FN) ? 1
+                    : (kind == EDEN_POINT_IAF_TAU || kind == EDEN_POINT_IAF_TAU_REF || kind == EDEN_POINT_IZH_DL) ? 0 : 2;
             P.v[b][m->n_comp + k] = m->izh_params[EDEN_POINT_PARAMS * (int64_t)k + f];
         }
         for (int64_t s = 0; s < ns; s++) P.syn_pend[b][s] = -INFINITY;

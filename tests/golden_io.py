@@ -9,7 +9,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 def load(name, lowered):
     """Returns (trace_mV [samples, columns], spike_src, spike_log_step)."""
     z = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
-    trace = z["values_si"].astype(np.float64) * 1e3
+    # volts to mV, except dimensionless columns (a fitzHughNagumoCell's V)
+    scale = np.full(len(lowered.trace_target), 1e3)
+    for j, t in enumerate(lowered.trace_target):
+        k = int(t) - lowered.n_comp
+        if k >= 0 and len(lowered.izh_kind) > k and int(lowered.izh_kind[k]) == 7:
+            scale[j] = 1.0
+    trace = z["values_si"].astype(np.float64) * scale
     dt_s = float(lowered.dt) * 1e-6
     ids = z["event_id"]
     src = lowered.event_src[ids] if len(ids) else np.zeros(0, np.int32)
