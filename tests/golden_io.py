@@ -3,6 +3,8 @@ import os
 
 import numpy as np
 
+from eden_gb300.lowering import POINT_FN
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -13,7 +15,7 @@ def load(name, lowered):
     scale = np.full(len(lowered.trace_target), 1e3)
     for j, t in enumerate(lowered.trace_target):
         k = int(t) - lowered.n_comp
-        if k >= 0 and len(lowered.izh_kind) > k and int(lowered.izh_kind[k]) == 7:
+        if k >= 0 and len(lowered.izh_kind) > k and int(lowered.izh_kind[k]) == POINT_FN:
             scale[j] = 1.0
     trace = z["values_si"].astype(np.float64) * scale
     dt_s = float(lowered.dt) * 1e-6
