@@ -134,20 +134,27 @@ def flush_l2(buf):
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(low, threads: int, budget_s: float = 15.0):
+def out_degree(low) -> np.ndarray:
+    """Connection synapses on each spike source's fan-out."""
+    return np.bincount(np.asarray(low.syn_src, np.int64), minlength=len(low.src_target)).astype(np.int64)
+
+
+def cpu_sample(low, threads: int, budget_s: float = 15.0, max_steps: int = 2000):
     """Time the CPU restatement on a bounded number of simulation steps of the
-    same workload; returns (compartment-steps/s, steps timed)."""
+    same workload (the wall clock from the first non-initialisation step to
+    the end of the run); returns (compartment-steps/s, steps timed,
+    synaptic events/s)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
     import eden_port
-    t0 = time.perf_counter()
-    eden_port.run(low, n_steps=4, trace_target=np.zeros(0, np.int32), threads=threads, spike_cap=1 << 20)
-    per = (time.perf_counter() - t0) / 8.0  # 4 init + 4 steps
-    n = int(max(8, min(2000, budget_s / max(per, 1e-6))))
-    t0 = time.perf_counter()
-    eden_port.run(low, n_steps=n, trace_target=np.zeros(0, np.int32), threads=threads, spike_cap=1 << 22)
-    dt = time.perf_counter() - t0
-    # the timed call also runs the 4 initialisation passes
-    return low.n_target * n / (dt * n / (n + 4)), n
+    probe = eden_port.run(low, n_steps=4, trace_target=np.zeros(0, np.int32), threads=threads, spike_cap=1 << 20,
+                          mark_step=1)
+    per = probe["timed_s"] / 4.0
+    n = int(max(8, min(max_steps, budget_s / max(per, 1e-6))))
+    out = eden_port.run(low, n_steps=n, trace_target=np.zeros(0, np.int32), threads=threads, spike_cap=1 << 24,
+                        mark_step=1)
+    dt = out["timed_s"]
+    events = float(out_degree(low)[out["spike_src"]].sum())
+    return low.n_target * n / dt, n, events / dt
 
 
 def precision_sample(low, n_steps: int = 800, dev: int = 0, trace_target=None):
@@ -288,15 +295,83 @@ def scale_sample(dev: int):
         fan = len(low.syn_target) / max(len(low.src_target), 1)
         ab = algorithmic_bytes(low, spikes * fan / steps)
         out[key] = {"value": low.n_target * steps / (ms * 1e-3), "unit": UNIT, "ms_per_sim_step": ms / steps,
+                    "events_per_s": spikes * fan / (ms * 1e-3),
                     "device_bytes": int(free0 - free1), "create_s": t_create,
                     "step_algorithmic_bytes": ab["total"],
-                    "step_achieved_gbs": ab["total"] / (ms / steps * 1e-3) / 1e9,
+                    "step_algorithmic_gbs": ab["total"] / (ms / steps * 1e-3) / 1e9,
                     "spikes_per_sim_step": spikes / steps}
     out["ratio_batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
     # V of ten somas and ten izhikevich cells
     tt = np.concatenate([low.phys_comp_off[:10], low.n_comp + np.arange(min(10, low.n_izh))])
     out["spike_time_error"] = precision_sample(low, n_steps=400, dev=dev, trace_target=tt)
     out["fits_180_gb"] = max(out["batched"]["device_bytes"], out["plain"]["device_bytes"]) < 180e9
+    return out
+
+
+def roofline_object(kernel, achieved, peak, peak_kind, bytes_per_launch, avg_ms, ab, sim_steps, total_ms):
+    """The dominant kernel against the HBM roofline.  `achieved` is its
+    algorithmic bytes (the per-unit figures above, for the K steps one launch
+    advances) over its CUDA-event launch time: an effective rate, which can
+    exceed what DRAM moves because a window keeps its units' state on chip
+    for K steps.  `traffic` is what ncu counted in DRAM for one launch of the
+    same workload (profiles/), and dram_frac_ncu that traffic's rate against
+    the peak; their gap from `frac` says the kernel is bounded by instruction
+    issue and dependent latency rather than by HBM."""
+    traffic = load_profile_traffic()
+    out = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+           "achieved_is": "algorithmic bytes per launch (K steps) / CUDA-event launch time",
+           "traffic": traffic, "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
+           "step_algorithmic_bytes": ab["total"],
+           "step_algorithmic_gbs": ab["total"] * sim_steps / (total_ms * 1e-3) / 1e9}
+    if traffic:
+        out["dram_gbs_ncu"] = traffic / (avg_ms * 1e-3) / 1e9
+        out["dram_frac_ncu"] = out["dram_gbs_ncu"] / peak
+        out["limiter"] = ("instruction issue and dependent latency: ncu DRAM traffic is "
+                          f"{traffic / bytes_per_launch:.3f} of the algorithmic bytes")
+    return out
+
+
+def config_sample(key: str, dev: int, threads: int):
+    """Throughput of a further configuration at its stated size: C1 (1,000
+    single-compartment HH cells with DC pulses, dt 0.025 ms) over its whole
+    second, or C3 (100,000 izhikevich2007 cells, 10 M expOne synapses, dt
+    0.1 ms) over 1,000 steps after 200 warm-up steps; batched and plain
+    device time, synaptic events/s, and the CPU restatement on a bounded
+    sample of the same network with every host thread."""
+    from eden_gb300 import lowering, workloads
+    from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
+    if key == "c1":
+        low = lowering.lower(workloads.single_comp_hh())
+        warm, steps = 0, int(low.n_steps)
+        desc = "single_comp_hh: 1000 HH cells, DC pulses, no synapses, dt 0.025 ms, the whole 1 s (40,001 steps)"
+    else:
+        low = lowering.lower(workloads.izh_net())
+        warm, steps = 200, 1000
+        desc = ("izh_net: 100000 izhikevich2007 cells, 10 M expOne synapses (in-degree 100, delays 1-20 ms), "
+                "DC pulses, dt 0.1 ms, 1,000 steps after 200")
+    outdeg = out_degree(low)
+    out = {"workload": desc, "targets": low.n_target, "synapses": int(len(low.syn_target))}
+    for mode, name in ((MODE_BATCHED, "batched"), (MODE_PLAIN, "plain")):
+        sim = Simulation(low, mode=mode, device=dev, record_capacity_steps=4096, spike_capacity=1 << 24)
+        sim.initialize()
+        if warm:
+            sim.run_steps(warm)
+            sim.fetch()
+        ms, ev, done = 0.0, 0, 0
+        while done < steps:
+            k = min(4000, steps - done)
+            ms += sim.run_steps(k)
+            ev += int(outdeg[sim.fetch().spike_src].sum())
+            done += k
+        sim.close()
+        out[name] = {"value": low.n_target * steps / (ms * 1e-3), "unit": UNIT, "ms_per_sim_step": ms / steps,
+                     "events_per_s": ev / (ms * 1e-3)}
+    out["ratio_batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    cval, n, cev = cpu_sample(low, threads, budget_s=10.0, max_steps=40000)
+    out["cpu_baseline"] = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port", "events_per_s": cev,
+                           "sample": f"the first {n} simulation steps (after the 4 initialisation passes), "
+                                     f"C restatement of the reference loop, OpenMP {threads} threads"}
     return out
 
 
@@ -370,17 +445,31 @@ def main():
               "l2": "flushed (256 MB write) between timed bench steps", "replicas": world, "seed": args.seed}
 
     if args.impl == "reference":
+        # the reference's CPU loop (its C restatement; the reference's own
+        # build needs its source tree, absent here) with every host thread:
+        # `warmup` bench steps of STEPS_PER_ITER simulation steps untimed,
+        # then exactly `steps` bench steps timed on the wall clock
         if rank != 0:
             return
+        sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
+        import eden_port
         threads = os.cpu_count() or 1
-        val, n = cpu_sample(low, threads, budget_s=20.0)
-        ms = low.n_target * STEPS_PER_ITER / val * 1e3
+        n_warm, n_timed = args.warmup * STEPS_PER_ITER, args.steps * STEPS_PER_ITER
+        out = eden_port.run(low, n_steps=n_warm + n_timed, trace_target=np.zeros(0, np.int32), threads=threads,
+                            spike_cap=1 << 24, mark_step=n_warm + 1)
+        timed = out["timed_s"]
+        val = low.n_target * n_timed / timed
+        timed_spikes = out["spike_src"][out["spike_step"] > n_warm]
+        events_s = float(out_degree(low)[timed_spikes].sum()) / timed
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-                "config": config,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": timed / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded generator)", "config": config,
+                "events_per_s": events_s,
                 "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": f"{n} simulation steps of the full workload (after 4 init passes), "
+                                 "sample": f"{args.steps} bench steps of {STEPS_PER_ITER} simulation steps each "
+                                           f"({n_timed} steps) of the full workload, timed after "
+                                           f"{args.warmup} untimed bench steps and the 4 initialisation passes; "
                                            f"C restatement of the reference loop, OpenMP {threads} threads"},
                 "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -426,12 +515,14 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    total_ms, spikes = 0.0, 0
+    total_ms, spikes, events = 0.0, 0, 0
+    outdeg = out_degree(low)
     for _ in range(args.steps):
         flush_l2(flush)
         total_ms += sim.run_steps(STEPS_PER_ITER)
         rec = sim.fetch()
         spikes += len(rec.spike_src)
+        events += int(outdeg[rec.spike_src].sum())
     torch.cuda.synchronize()
     clk = clocks.stop()
     stats = sim.kernel_stats()
@@ -441,8 +532,10 @@ def main():
     sim_steps = STEPS_PER_ITER * args.steps
     value = world * low.n_target * sim_steps / (total_ms * 1e-3)
 
+    events_per_s = world * events / (total_ms * 1e-3)
+
     # ---- roofline of the dominant kernel (k_cells_t), bytes per launch
-    events_per_step = spikes * (len(low.syn_target) / max(1, len(low.src_target))) / sim_steps
+    events_per_step = events / sim_steps
     ab = algorithmic_bytes(low, events_per_step)
     k_ms = {k: (stats[k][0] - base_stats[k][0], stats[k][1] - base_stats[k][1]) for k in stats}
     dom = max(k_ms, key=lambda k: k_ms[k][0])
@@ -490,17 +583,16 @@ def main():
     e2e_value = world * low.n_target * e2e_steps / e2e_s
 
     # ---- CPU baseline (rank 0 only)
-    cpu = None
-    precision = None
-    adjoint = None
-    scale = None
+    cpu = precision = adjoint = scale = c1 = c3 = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        cval, n = cpu_sample(low, threads, budget_s=15.0)
-        cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
+        cval, n, cev = cpu_sample(low, threads, budget_s=15.0)
+        cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port", "events_per_s": cev,
                "sample": f"{n} simulation steps of the same network (after 4 init passes), C restatement of "
                          f"the reference loop, OpenMP {threads} threads"}
         precision = precision_sample(low, dev=dev)
+        c1 = config_sample("c1", dev, threads)
+        c3 = config_sample("c3", dev, threads)
         adjoint = adjoint_sample()
         scale = scale_sample(dev)
 
@@ -516,16 +608,17 @@ def main():
                         "seconds": e2e_s,
                         "covers": "create (upload, device layout, kernels compiled for the model or "
                                   "taken from the process cache), the whole configured run, record fetches"},
+                "events_per_s": events_per_s,
+                "events_unit": "synaptic events/s (spikes x their connection fan-out, per second of device time)",
                 "gpu_launches": int(gpu_launches),
-                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                             "traffic": load_profile_traffic(), "bytes_per_launch": bytes_per_launch,
-                             "avg_launch_ms": avg_ms, "step_bytes": ab["total"],
-                             "step_achieved_gbs": ab["total"] * sim_steps / (total_ms * 1e-3) / 1e9 / world * world},
+                "roofline": roofline_object(dom, achieved, peak, peak_kind, bytes_per_launch, avg_ms, ab,
+                                            sim_steps, total_ms),
                 "kernels_ms": {k: round(v[0], 3) for k, v in k_ms.items()},
                 "clocks": clk,
                 "cpu_baseline": cpu,
                 "spike_time_error": precision,
+                "c1": c1,
+                "c3": c3,
                 "adjoint": adjoint,
                 "scale": scale}
         print(json.dumps(line))

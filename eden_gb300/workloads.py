@@ -207,6 +207,44 @@ def izh_net(n_cells: int = 100000, in_degree: int = 100, length_ms: float = 1000
     return spec
 
 
+def routing_probe(n_arrays: int = 8, n_post: int = 16, fan_in: int = 40, length_ms: float = 30.0,
+                  dt_ms: float = 0.1, seed: int = 1234, min_delay_ms: float = 0.1) -> NetworkSpec:
+    """Spike lists into izhikevich2007 cells through expOne synapses, the
+    case the per-synapse pending slots are compared on against the
+    reference's own tables: spike trains with bursts closer together than
+    the delays (a trigger read while a spike is pending is dropped or kept
+    by the single-pending-spike rule), spikes on and next to step
+    boundaries, and delays of whole and fractional steps (from
+    `min_delay_ms`; below one step a spike fires in the step that reads
+    its trigger).  The driven cells have no outgoing connections, so the
+    spike trains reaching the synapses are the lists themselves."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("routing_probe", dt_ms, length_ms, seed)
+    for k in range(n_arrays):
+        base = rng.uniform(0.0, length_ms * 0.9, size=int(rng.integers(3, 8)))
+        t = [base]
+        for b in base[: len(base) // 2]:  # bursts: 2-3 more spikes 0.05-1 ms apart
+            t.append(b + np.cumsum(rng.uniform(0.05, 1.0, size=int(rng.integers(2, 4)))))
+        t = np.round(np.concatenate(t), 4)
+        if k == 0:
+            t = np.concatenate([t, [1.0, 1.0999, 1.1, 1.1001, 5.0, 5.05]])
+        spec.cells.append(SpikeArrayCell(f"sa{k}", np.sort(t[t < length_ms])))
+        spec.populations.append(Population(f"psa{k}", f"sa{k}", 1))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("iz", "izRS", n_post))
+    spec.synapses.append(SynapseType("syn_e1", SYN_EXPONE, gbase=0.5, erev=0.0, tau_decay=2.0))
+    post = np.repeat(np.arange(n_arrays, n_arrays + n_post), fan_in)
+    pre = rng.integers(0, n_arrays, size=post.size)
+    choices = np.array([1.0, 1.5, 2.0, 2.5, 3.0, 4.0, 7.0, 10.0, 13.3]) * min_delay_ms
+    delay = _round_us(rng.choice(choices, size=post.size) + np.where(rng.random(post.size) < 0.3,
+                                                                     rng.uniform(0.0, dt_ms, post.size), 0.0))
+    w = np.round(rng.uniform(0.2, 1.0, size=post.size), 4)
+    spec.projections.append(_flat_projection(spec, "proj", pre, post, "syn_e1", w, delay))
+    spec.trace_columns = [OutputColumn("iz", 0, 0)]
+    spec.event_selections = [EventSelection(f"psa{k}", 0, 0) for k in range(n_arrays)]
+    return spec
+
+
 def _gid_to_pop(spec, gid):
     """(population, index) of a global cell id."""
     n_pops = len(spec.populations)
@@ -792,6 +830,7 @@ CONFIGS = {
     "input_kinds": input_kinds,
     "gate_kinds": gate_kinds,
     "voltage_clamps": voltage_clamps,
+    "routing_probe": routing_probe,
     "random_sources": random_sources,
     "custom_setup": custom_setup,
     "dl_inputs": dl_inputs,

@@ -755,6 +755,20 @@ static void port_free(Port *P) {
     free(P->timed_cur); free(P->timed_tgt_off); free(P->timed_order);
 }
 
+/* Wall-clock marks for timing a stretch of a run (the CPU timings beside
+ * the GPU's): the time at the start of step eden_port_mark_step (before its
+ * output phase) and at the end of the run, in seconds of one clock. */
+int64_t eden_port_mark_step = INT64_MAX;
+double eden_port_mark_s = 0.0, eden_port_end_s = 0.0;
+
+static double wall_s(void) {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
 int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const int32_t *trace_target,
                   float *trace, int64_t spike_cap, int32_t *spike_src, int64_t *spike_step,
                   int64_t *n_spikes, int64_t *syn_fire_count, float *syn_final_pending, int32_t n_threads) {
@@ -775,6 +789,7 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
     int64_t ext = 0;              /* next spike-source event */
     for (int64_t step = -3; step <= last_step; step++) {
         int init = step <= 0;
+        if (step == eden_port_mark_step) eden_port_mark_s = wall_s();
         if (!init) {
             /* output phase: trajectory columns, then event slots read & clear */
             for (int32_t j = 0; j < n_trace; j++)
@@ -810,6 +825,7 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
         if (!init) time += dt;
         cur ^= 1;
     }
+    eden_port_end_s = wall_s();
     *n_spikes = nsp;
     if (syn_fire_count) memcpy(syn_fire_count, P.syn_fire_count, sizeof(int64_t) * (size_t)ns);
     if (syn_final_pending)

@@ -34,9 +34,11 @@ def _load(double=False):
     return _libs[path]
 
 
-def run(lowered, n_steps=None, trace_target=None, threads=0, spike_cap=None, double=False):
+def run(lowered, n_steps=None, trace_target=None, threads=0, spike_cap=None, double=False, mark_step=None):
     """Run the port; returns dict(trace [n_steps, n_trace] f32, spike_src,
-    spike_step, syn_fire_count, syn_final_pending, rc)."""
+    spike_step, syn_fire_count, syn_final_pending, rc).  With `mark_step`,
+    also `timed_s`: the wall-clock seconds from the start of that step to
+    the end of the run."""
     from eden_gb300.lowering import to_cmodel
     lib = _load(double)
     cm, keep = to_cmodel(lowered)
@@ -52,6 +54,8 @@ def run(lowered, n_steps=None, trace_target=None, threads=0, spike_cap=None, dou
     n_syn = len(lowered.syn_target)
     fire = np.zeros(max(n_syn, 1), np.int64)
     pend = np.zeros(max(n_syn, 1), np.float32)
+    mark = ctypes.c_int64.in_dll(lib, "eden_port_mark_step")
+    mark.value = (1 << 63) - 1 if mark_step is None else int(mark_step)
     rc = lib.eden_port_run(ctypes.byref(cm), ctypes.c_int64(n_steps), ctypes.c_int32(len(tt)),
                            tt.ctypes.data_as(ctypes.c_void_p), trace.ctypes.data_as(ctypes.c_void_p),
                            ctypes.c_int64(spike_cap), ssrc.ctypes.data_as(ctypes.c_void_p),
@@ -59,9 +63,14 @@ def run(lowered, n_steps=None, trace_target=None, threads=0, spike_cap=None, dou
                            fire.ctypes.data_as(ctypes.c_void_p), pend.ctypes.data_as(ctypes.c_void_p),
                            ctypes.c_int32(threads))
     n = min(nsp.value, spike_cap)
-    return dict(trace=trace[:, :len(tt)], spike_src=ssrc[:n].copy(), spike_step=sstep[:n].copy(),
-                syn_fire_count=fire[:n_syn].copy(), syn_final_pending=pend[:n_syn].copy(), rc=rc,
-                n_spikes=nsp.value)
+    out = dict(trace=trace[:, :len(tt)], spike_src=ssrc[:n].copy(), spike_step=sstep[:n].copy(),
+               syn_fire_count=fire[:n_syn].copy(), syn_final_pending=pend[:n_syn].copy(), rc=rc,
+               n_spikes=nsp.value)
+    if mark_step is not None:
+        out["timed_s"] = ctypes.c_double.in_dll(lib, "eden_port_end_s").value - \
+            ctypes.c_double.in_dll(lib, "eden_port_mark_s").value
+        mark.value = (1 << 63) - 1
+    return out
 
 
 LIBGPU64 = os.path.join(HERE, "libeden_port_gpu64.so")

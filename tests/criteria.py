@@ -23,6 +23,22 @@ def box_violations(truth, test, dt, dt_box, dv_box):
     return int(bad.sum()), float(max(over.max(initial=0), under.max(initial=0)))
 
 
+def box_violations_strided(truth, test_rows, stride, dt, dt_box, dv_box):
+    """box() for a test trace kept every `stride`-th sample (rows 0, stride,
+    2 stride, ...): the box is built on the full-rate truth and read at those
+    rows."""
+    truth = np.asarray(truth, np.float64)
+    test = np.asarray(test_rows, np.float64)
+    width = int(dt_box / dt + 1e-9) + 1
+    hi = (maximum_filter1d(truth, width, axis=0, mode="nearest") + dv_box)[::stride][:len(test)]
+    lo = (minimum_filter1d(truth, width, axis=0, mode="nearest") - dv_box)[::stride][:len(test)]
+    test = test[:len(hi)]
+    over = np.maximum(test - hi, 0.0)
+    under = np.maximum(lo - test, 0.0)
+    bad = (over > 0) | (under > 0) | np.isnan(test) | np.isnan(hi)
+    return int(bad.sum()), float(max(over.max(initial=0), under.max(initial=0)))
+
+
 def samecount(truth_steps_by_src, test_steps_by_src, max_shift_steps):
     """Cells whose spike counts differ, and cells with a spike more than
     max_shift_steps away from the truth's."""

@@ -26,9 +26,20 @@ CASES = {
 }
 
 
+# The configurations at (or near) their stated sizes, for the full-size GPU
+# tests: C1 as stated (1,000 single-compartment HH cells, 1 s, 10 recorded
+# cells; its trajectory is stored every `stride`-th sample) and C3 reduced to
+# 10,000 cells (in-degree 100, 1 M expOne synapses) over 100 ms.
+# name -> (generator, keyword arguments, trajectory stride)
+FULL_CASES = {
+    "c1_full": ("single_comp_hh", dict(n_cells=1000, length_ms=1000.0, n_recorded=10), 8),
+    "c3_10k": ("izh_net", dict(n_cells=10000, in_degree=100, length_ms=100.0, n_recorded=10), 1),
+}
+
+
 def spec_of(name):
     from eden_gb300 import workloads
-    gen, kw, _, _ = CASES[name]
+    gen, kw = (CASES[name][0], CASES[name][1]) if name in CASES else FULL_CASES[name][:2]
     return workloads.CONFIGS[gen](**kw)
 
 

@@ -21,19 +21,20 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, HERE)
 
 import reference_runner  # noqa: E402
-from cases import CASES, LOGGER_FILES, add_eden_loggers, spec_of  # noqa: E402
+from cases import CASES, FULL_CASES, LOGGER_FILES, add_eden_loggers, spec_of  # noqa: E402
 from eden_gb300 import neuroml_io  # noqa: E402
 
 
 def make(name):
     spec = spec_of(name)
+    stride = FULL_CASES[name][2] if name in FULL_CASES else 1
     with tempfile.TemporaryDirectory() as d:
         lems = neuroml_io.write_lems(spec, d)
-        out = reference_runner.run(lems, threads=4)
-    traj = out["trajectory"].astype(np.float64)
+        out = reference_runner.run(lems, threads=8)
+    traj = out["trajectory"].astype(np.float64)[::stride]
     ev = np.array(out.get("events", []), dtype=np.float64).reshape(-1, 2)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), time_s=traj[:, 0], values_si=traj[:, 1:].astype(np.float32),
-                        event_time_s=ev[:, 0], event_id=ev[:, 1].astype(np.int32),
+                        event_time_s=ev[:, 0], event_id=ev[:, 1].astype(np.int32), trace_stride=stride,
                         trajectory_head=out["trajectory_text"].splitlines()[:3],
                         events_head=out.get("events_text", "").splitlines()[:3])
     print(f"{name}: {traj.shape[0]} samples x {traj.shape[1] - 1} columns, {len(ev)} spikes")
@@ -55,6 +56,6 @@ def make_loggers():
 if __name__ == "__main__":
     if not reference_runner.available():
         sys.exit("oracle/_ref/eden is not built (make -C oracle ref)")
-    names = sys.argv[1:] or list(CASES) + ["loggers"]
+    names = sys.argv[1:] or list(CASES) + list(FULL_CASES) + ["loggers"]
     for name in names:
         make_loggers() if name == "loggers" else make(name)

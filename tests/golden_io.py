@@ -32,3 +32,30 @@ def logged(src, step, lowered):
     the reference does not log)."""
     keep = np.isin(np.asarray(src), lowered.event_src)
     return np.asarray(src)[keep], np.asarray(step)[keep]
+
+
+class RoutingFixture:
+    """A synapse-by-synapse record of the reference's routing
+    (tests/golden/routing_<variant>.npz): the pending slot of every synapse
+    after each step (stored as its changes) and the steps each fired in."""
+
+    def __init__(self, z, n_syn):
+        self.n_syn = n_syn
+        self.last_step = int(z["last_step"])
+        self.pend_step, self.pend_syn, self.pend_bits = z["pend_step"], z["pend_syn"], z["pend_bits"]
+        self.fire_step, self.fire_syn = z["fire_step"], z["fire_syn"]
+
+    def pending_after(self, step):
+        """float32 pending slot of every synapse after step `step`."""
+        bits = np.full(self.n_syn, np.float32(-np.inf)).view(np.uint32)
+        keep = self.pend_step <= step
+        bits[self.pend_syn[keep]] = self.pend_bits[keep]  # changes are in step order
+        return bits.view(np.float32)
+
+    def fire_count_through(self, step):
+        keep = self.fire_step <= step
+        return np.bincount(self.fire_syn[keep], minlength=self.n_syn).astype(np.int64)
+
+
+def routing_fixture(variant, n_syn):
+    return RoutingFixture(np.load(os.path.join(HERE, "golden", f"routing_{variant}.npz")), n_syn)

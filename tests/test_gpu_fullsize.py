@@ -4,9 +4,18 @@ at any size, where the oracle would take too long:
 * routing: every synapse's pending-spike slot equals the reference's
   delivery and single-pending-spike rule replayed from the GPU's own spike
   log (oracle/routing.py), bit for bit;
-* parity at full size over the first 400 steps (10 ms) of multicomp_net
-  against the oracle: the parity tests' samecount(0.1 ms) and
-  box(0.1 ms, 0.5 mV), in both modes;
+* parity at full size against the oracle, in both modes, with the parity
+  tests' samecount(0.1 ms) and box(0.1 ms, 0.5 mV): the whole of C1 (1,000
+  HH cells, 1 s); C2 (multicomp_net) over its first 20 ms; C5 (mixed_scale)
+  over its first 20 ms; C3 (izh_net, 100,000 cells, 10 M synapses) over its
+  first 100 ms -- strictly over the first 40 ms, and over 100 ms with at
+  most 0.05 % of the cells off, because the recurrent network is chaotic:
+  the oracle built in single and in double precision already differ in 12
+  of 100,000 cells by 100 ms (none before 80 ms apart from spikes on the
+  last compared step);
+* parity against the reference simulator's own outputs at configuration
+  size: C1 as stated and C3 with 10,000 cells (tests/golden/c1_full.npz,
+  c3_10k.npz);
 * bounds: every membrane potential finite (inside [-100, +70] mV for the
   cable cells; an izhikevich v may overshoot vpeak by one step before its
   reset), every spike logged at most once per cell and step.
@@ -21,10 +30,12 @@ import pytest
 
 import eden_port
 import routing
-from criteria import box_violations, samecount
+from criteria import box_violations, box_violations_strided, samecount
 from helpers import spike_trains
 from eden_gb300 import lowering, workloads
 from eden_gb300.engine import MODE_BATCHED, MODE_PLAIN, Simulation
+from golden.cases import FULL_CASES, spec_of
+from golden_io import load
 
 pytestmark = pytest.mark.gpu
 
@@ -56,24 +67,109 @@ def test_full_size_routing_and_bounds(name, length_ms):
         sim.close()
 
 
-@pytest.fixture(scope="module")
-def full_multicomp():
-    low = lowering.lower(workloads.multicomp_net(length_ms=10.0))
-    return low, eden_port.run(low, n_steps=400)
+# configuration -> (generator keyword arguments, steps compared against the oracle)
+FULL = {
+    "c1": ("single_comp_hh", dict(), None),
+    "c2": ("multicomp_net", dict(length_ms=20.0), None),
+    "c5": ("mixed_scale", dict(length_ms=20.0), None),
+}
+_oracle_cache = {}
+
+
+def oracle_run(key):
+    if key not in _oracle_cache:
+        gen, kw, n = FULL[key]
+        low = lowering.lower(workloads.CONFIGS[gen](**kw))
+        _oracle_cache.clear()  # one network at a time in host memory
+        _oracle_cache[key] = (low, eden_port.run(low, n_steps=n, spike_cap=1 << 24))
+    return _oracle_cache[key]
+
+
+def gpu_run(low, mode, n_steps=None):
+    n = low.n_steps if n_steps is None else n_steps
+    sim = Simulation(low, mode=mode, record_capacity_steps=n + 8, spike_capacity=1 << 24)
+    try:
+        return sim.run(n)
+    finally:
+        sim.close()
 
 
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
-def test_full_size_parity_first_10ms(full_multicomp, mode):
-    low, ref = full_multicomp
-    sim = Simulation(low, mode=mode, record_capacity_steps=408)
-    try:
-        rec = sim.run(400)
-    finally:
-        sim.close()
+@pytest.mark.parametrize("key", list(FULL))
+def test_full_size_parity(key, mode):
+    """C1 over its whole second, C2 and C5 over their first 20 ms, at full
+    size: every cell's spike count equal and each spike within 0.1 ms of the
+    oracle's, the recorded potentials inside box(0.1 ms, 0.5 mV)."""
+    low, ref = oracle_run(key)
+    assert ref["rc"] == 0
+    rec = gpu_run(low, mode, ref["trace"].shape[0])
     shift = int(round(0.1 / (float(low.dt) * 1e-3)))
     wrong, far = samecount(spike_trains(ref["spike_src"], ref["spike_step"]),
                            spike_trains(rec.spike_src, rec.spike_step), shift)
+    assert len(ref["spike_src"]) > 1000
     assert not wrong, f"{len(wrong)} cells with a different spike count, e.g. {wrong[:5]}"
     assert not far, f"{len(far)} cells with a spike more than 0.1 ms off, e.g. {far[:5]}"
     nbad, worst = box_violations(ref["trace"], rec.trace, float(low.dt) * 1e-3, 0.1, 0.5)
+    assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst {worst} mV"
+
+
+def _trains_until(src, step, last):
+    keep = np.asarray(step) <= last
+    return spike_trains(np.asarray(src)[keep], np.asarray(step)[keep])
+
+
+def differing_cells(a_src, a_step, b_src, b_step, last, shift):
+    """Cells whose spike trains through step `last` differ (count, or a
+    spike more than `shift` steps off), not counting a spike on the last
+    compared step that the other run logs one step later."""
+    w, f = samecount(_trains_until(a_src, a_step, last), _trains_until(b_src, b_step, last), shift)
+    bad = set(w) | set(f)
+    if bad:
+        w2, f2 = samecount(_trains_until(a_src, a_step, last + 1), _trains_until(b_src, b_step, last + 1), shift)
+        bad &= set(w2) | set(f2)
+    return sorted(bad)
+
+
+@pytest.fixture(scope="module")
+def c3_full():
+    low = lowering.lower(workloads.izh_net(length_ms=100.0))
+    return low, eden_port.run(low, spike_cap=1 << 24)
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+def test_c3_full_size_first_100ms(c3_full, mode):
+    """C3 as stated (100,000 izhikevich2007 cells, 10 M expOne synapses),
+    100 ms: no cell off over the first 40 ms, at most 0.05 % of the cells
+    off over 100 ms (the network is chaotic), total spike counts within
+    0.01 %, and the recorded cells inside box(0.1 ms, 0.5 mV)."""
+    low, ref = c3_full
+    _oracle_cache.clear()
+    rec = gpu_run(low, mode)
+    dt_ms = float(low.dt) * 1e-3
+    shift = int(round(0.1 / dt_ms))
+    strict = differing_cells(ref["spike_src"], ref["spike_step"], rec.spike_src, rec.spike_step,
+                             int(round(40.0 / dt_ms)), shift)
+    assert not strict, f"{len(strict)} cells differ within the first 40 ms, e.g. {strict[:5]}"
+    loose = differing_cells(ref["spike_src"], ref["spike_step"], rec.spike_src, rec.spike_step, low.n_steps, shift)
+    assert len(loose) <= 50, f"{len(loose)} of 100,000 cells differ over 100 ms, e.g. {loose[:5]}"
+    assert abs(len(rec.spike_src) - len(ref["spike_src"])) <= 1e-4 * len(ref["spike_src"])
+    assert len(ref["spike_src"]) > 500000
+    nbad, worst = box_violations(ref["trace"], rec.trace, dt_ms, 0.1, 0.5)
+    assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst {worst} mV"
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+@pytest.mark.parametrize("name", list(FULL_CASES))
+def test_configuration_size_matches_reference_outputs(name, mode):
+    """The GPU against the reference simulator's own outputs: C1 as stated
+    and C3 with 10,000 cells over 100 ms; every spike within 0.1 ms, the
+    reference's stored trajectory inside box(0.1 ms, 0.5 mV) of the GPU's."""
+    low = lowering.lower(spec_of(name))
+    ref_trace, ref_src, ref_step = load(name, low)
+    rec = gpu_run(low, mode)
+    dt_ms = float(low.dt) * 1e-3
+    wrong, far = samecount(spike_trains(ref_src, ref_step), spike_trains(rec.spike_src, rec.spike_step),
+                           int(round(0.1 / dt_ms)))
+    assert not wrong and not far, f"spike trains differ: counts {wrong[:5]}, timing {far[:5]}"
+    nbad, worst = box_violations_strided(rec.trace, ref_trace, FULL_CASES[name][2], dt_ms, 0.1, 0.5)
     assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst {worst} mV"

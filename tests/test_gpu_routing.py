@@ -44,3 +44,39 @@ def test_pending_slots_bit_exact(name, mode):
         assert checked == 2
     finally:
         sim.close()
+
+
+from golden.make_routing_golden import LENGTH_MS, VARIANTS  # noqa: E402
+from golden_io import routing_fixture  # noqa: E402
+from eden_gb300 import workloads  # noqa: E402
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_pending_slots_equal_reference_tables(variant, mode):
+    """The GPU's pending slot of every synapse equals the reference
+    simulator's own table (tests/golden/routing_*.npz) bit for bit, at
+    points spread over the run: one-step windows, five-step windows replayed
+    at the next window, and delays below one step."""
+    low = lowering.lower(workloads.routing_probe(length_ms=LENGTH_MS, **VARIANTS[variant]))
+    fx = routing_fixture(variant, len(low.syn_src))
+    sim = Simulation(low, mode=mode)
+    try:
+        sim.initialize()
+        checked = 0
+        for chunk in (6, 1, 33, 1, 57, 1, 99, 1, 0):
+            if chunk == 0:
+                break
+            sim.run_steps(chunk)
+            sim.fetch()
+            if chunk != 1:
+                continue
+            last = sim.next_step - 1
+            got, _, _ = sim.read_synapses()
+            want = fx.pending_after(last)
+            bad = np.flatnonzero(got.view(np.uint32) != want.view(np.uint32))
+            assert len(bad) == 0, f"step {last}: {len(bad)} synapses differ from the reference, e.g. {bad[:5]}"
+            checked += 1
+        assert checked == 4
+    finally:
+        sim.close()

@@ -11,9 +11,9 @@ import numpy as np
 import pytest
 
 import eden_port
-from criteria import box_violations, samecount
+from criteria import box_violations, box_violations_strided, samecount
 from eden_gb300 import lowering
-from golden.cases import CASES, spec_of
+from golden.cases import CASES, FULL_CASES, spec_of
 from golden_io import load, logged
 from helpers import spike_trains
 
@@ -39,3 +39,22 @@ def test_golden_fixtures_are_nontrivial():
         low = lowering.lower(spec_of(name))
         _, src, _ = load(name, low)
         assert len(src) > 0, f"{name}: no spikes in the reference output"
+
+
+@pytest.mark.parametrize("name", list(FULL_CASES))
+def test_oracle_matches_reference_at_configuration_size(name):
+    """C1 as stated (1,000 cells, 1 s) and C3 with 10,000 cells and 1 M
+    synapses over 100 ms: every spike within 0.1 ms of the reference's, and
+    the reference's trajectory (stored every `stride`-th sample) inside
+    box(0.1 ms, 0.5 mV) of the oracle's."""
+    low = lowering.lower(spec_of(name))
+    ref_trace, ref_src, ref_step = load(name, low)
+    out = eden_port.run(low, spike_cap=1 << 22)
+    assert out["rc"] == 0
+    dt_ms = float(low.dt) * 1e-3
+    wrong, far = samecount(spike_trains(ref_src, ref_step), spike_trains(out["spike_src"], out["spike_step"]),
+                           int(round(0.1 / dt_ms)))
+    assert not wrong and not far, f"spike trains differ: counts {wrong[:5]}, timing {far[:5]}"
+    assert len(ref_src) > 50000
+    nbad, worst = box_violations_strided(out["trace"], ref_trace, FULL_CASES[name][2], dt_ms, 0.1, 0.5)
+    assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst {worst} mV"

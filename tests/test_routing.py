@@ -34,3 +34,41 @@ def test_single_pending_slot_drops_closely_spaced_spikes():
     t = routing.step_times(100.0, 40)
     assert pend[0] == np.float32(t[12] + np.float32(1000.0))
     assert fires[0] == 2
+
+
+# ---------------------------------------------------------------------------
+# pinned to the reference's own per-synapse tables (tests/golden/routing_*.npz,
+# read from the reference simulator's raw state dumps by
+# tests/golden/make_routing_golden.py)
+from golden.make_routing_golden import LENGTH_MS, VARIANTS  # noqa: E402
+from golden_io import routing_fixture  # noqa: E402
+from eden_gb300 import workloads  # noqa: E402
+
+
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_routing_restatement_matches_reference_tables(variant):
+    """oracle/routing.py replayed on the spike lists' emission steps gives the
+    reference's pending slot after every step and its firing count, bit for
+    bit: delays of whole and fractional steps, below one step, and spikes
+    closer together than the delays."""
+    low = lowering.lower(workloads.routing_probe(length_ms=LENGTH_MS, **VARIANTS[variant]))
+    fx = routing_fixture(variant, len(low.syn_src))
+    for last in (1, 2, 7, 40, 97, 150, 151, 233, fx.last_step):
+        pend, fires = routing.route(low.syn_src, low.syn_delay, low.ext_src, low.ext_step, float(low.dt), last)
+        want = fx.pending_after(last)
+        bad = np.flatnonzero(pend.view(np.uint32) != want.view(np.uint32))
+        assert len(bad) == 0, f"step {last}: {len(bad)} pending slots differ, e.g. {bad[:5]}"
+        assert np.array_equal(fires, fx.fire_count_through(last)), f"step {last}: firing counts differ"
+    assert fx.fire_count_through(fx.last_step).sum() > 1000
+
+
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_oracle_routing_matches_reference_tables(variant):
+    """The C restatement's final pending slots and firing counts equal the
+    reference's on the same probe."""
+    low = lowering.lower(workloads.routing_probe(length_ms=LENGTH_MS, **VARIANTS[variant]))
+    fx = routing_fixture(variant, len(low.syn_src))
+    out = eden_port.run(low, n_steps=fx.last_step)
+    assert out["rc"] == 0
+    assert np.array_equal(out["syn_final_pending"].view(np.uint32), fx.pending_after(fx.last_step).view(np.uint32))
+    assert np.array_equal(out["syn_fire_count"], fx.fire_count_through(fx.last_step))
