@@ -85,7 +85,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(" ".join(cmd), file=sys.stderr)
         subprocess.check_call(cmd)
         os.replace(LIB + ".tmp", LIB)
+    build_host(verbose)
     return LIB
+
+
+HOST_SRC = os.path.join(HERE, "host", "eden_gpu_host.cpp")
+HOST_BIN = os.path.join(HERE, "host", "eden_gpu_host")
+
+
+def build_host(verbose: bool = False) -> str:
+    """The C++ host program (eden_gb300/host/eden_gpu_host.cpp), linked
+    against the library next to it."""
+    if not os.path.exists(HOST_BIN) or any(os.path.getmtime(p) > os.path.getmtime(HOST_BIN)
+                                           for p in (HOST_SRC, HEADER, LIB)):
+        cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+               HOST_SRC, "-L", HERE, "-leden_gpu", "-Wl,-rpath,$ORIGIN/..", "-o", HOST_BIN + ".tmp"]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.check_call(cmd)
+        os.replace(HOST_BIN + ".tmp", HOST_BIN)
+    return HOST_BIN
 
 
 if __name__ == "__main__":

@@ -95,6 +95,16 @@ struct EdenGpuCtx {
     double k_ms[EDEN_KERNEL_KINDS] = {0};
     int64_t k_n[EDEN_KERNEL_KINDS] = {0};
     int sticky_status = 0;
+    // set when a run failed after its kernels began to change the device
+    // state: the host clock and the device state may then disagree, so
+    // later runs are refused
+    bool broken = false;
+    bool launched = false;      // the current run has issued a kernel
+    // edenGpuRunStaticScratch: device addresses of the static arrays, looked
+    // up on the context's first such call (the context's device current)
+    float *static_gp = nullptr;
+    WindowArgs *static_tab = nullptr;
+    WindowTimes *static_times = nullptr;
     // the windowed kernels launched: the built-in ones or those compiled for
     // this model at creation (eden_codegen.cuh)
     const void *fn_inputs = nullptr, *fn_cells = nullptr, *fn_deliver = nullptr;
@@ -1473,6 +1483,48 @@ static void fill_window(EdenGpuCtx *ctx, WindowArgs &w, WindowTimes &tt, int64_t
     ctx->wpar ^= 1;
 }
 
+// The host clock and buffer parities fill_window advances, saved at the
+// start of a run so that a run that fails before any kernel is issued leaves
+// the context as it was.
+struct ClockState {
+    double time, t_prev0;
+    int par, wpar, Kprev;
+    float prev_tk[32];
+};
+static ClockState save_clock(const EdenGpuCtx *ctx) {
+    ClockState c{ctx->time, ctx->t_prev0, ctx->par, ctx->wpar, ctx->Kprev, {}};
+    std::copy(ctx->prev_tk, ctx->prev_tk + 32, c.prev_tk);
+    return c;
+}
+static void restore_clock(EdenGpuCtx *ctx, const ClockState &c) {
+    ctx->time = c.time;
+    ctx->t_prev0 = c.t_prev0;
+    ctx->par = c.par;
+    ctx->wpar = c.wpar;
+    ctx->Kprev = c.Kprev;
+    std::copy(c.prev_tk, c.prev_tk + 32, ctx->prev_tk);
+}
+
+// A run's outcome: on failure before any kernel was issued the clock is put
+// back (the same first_step can be retried); on failure after, with the
+// steps not completed, the context refuses later runs.
+static int finish_run(EdenGpuCtx *ctx, int rc, const ClockState &c, int64_t next_before) {
+    if (rc != 0 && ctx->next_step == next_before) {
+        if (!ctx->launched) restore_clock(ctx, c);
+        else ctx->broken = true;
+    }
+    return rc;
+}
+
+static int check_runnable(EdenGpuCtx *ctx) {
+    if (ctx->broken)
+        return ctx->fail(EDEN_GPU_E_CUDA, "an earlier run failed after launching its kernels (%s); the device state "
+                                          "is not the host's, destroy the context",
+                         ctx->err.c_str());
+    ctx->launched = false;
+    return 0;
+}
+
 // Event pair around a launch when kernel timing is on.
 static void tmark(EdenGpuCtx *ctx, int kind, bool before) {
     if (!ctx->kernel_timing) return;
@@ -1495,6 +1547,7 @@ static void tmark(EdenGpuCtx *ctx, int kind, bool before) {
 
 // Launch the kernels of window `idx` of the current table; returns launches.
 static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
+    ctx->launched = true;
     DevModel &d = ctx->d;
     cudaStream_t s = ctx->stream;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
@@ -1533,8 +1586,17 @@ static int launch_window(EdenGpuCtx *ctx, const int *base, int idx, int K) {
     return 4;
 }
 
+static int run_windows(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
+
 extern "C" int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) {
     if (!ctx) return EDEN_GPU_E_INVALID;
+    TRY(check_runnable(ctx));
+    const ClockState c = save_clock(ctx);
+    const int64_t next_before = ctx->next_step;
+    return finish_run(ctx, run_windows(ctx, first_step, n_steps), c, next_before);
+}
+
+static int run_windows(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) {
     if (n_steps < 0) return ctx->fail(EDEN_GPU_E_INVALID, "negative step count");
     if (first_step != ctx->next_step)
         return ctx->fail(EDEN_GPU_E_INVALID, "steps must be contiguous: expected first_step %lld",
@@ -1591,6 +1653,7 @@ extern "C" int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) 
                 CUDA_TRY(ctx, cudaGraphInstantiate(&ctx->graph, g, 0));
                 cudaGraphDestroy(g);
             }
+            ctx->launched = true;
             CUDA_TRY(ctx, cudaGraphLaunch(ctx->graph, ctx->stream));
             launches += kGraphWindows * (2 + (int64_t)ctx->classes.size()) + 1;
             i += kGraphWindows;
@@ -1743,9 +1806,12 @@ extern "C" int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *st
 //     g_static_wtab and g_static_wtimes, filled from stack buffers at most
 //     kStaticWindows windows at a time;
 //   - plain launches: no graph, no kernel-timing events.
-// The first call on a device looks up both arrays' device addresses with
-// cudaGetSymbolAddress, with that device current.  That set-up should happen
-// before any stream capture begins: a call with n_steps = 0 does only it.
+// The first call on a context looks up the arrays' device addresses with
+// cudaGetSymbolAddress, with the context's device current.  That set-up
+// should happen before any stream capture begins: a call with n_steps = 0
+// does only it.  The arrays belong to the library's module: every device
+// that loads it holds them (16 MiB and a few KB) until the process exits,
+// whether or not this entry point is ever called.
 // Nothing in either array has to start at zero: every window writes rows
 // 0..K-1 of every chunk before the cell kernels read them, and each launch
 // reads only table entries written by the copy before it.
@@ -1756,37 +1822,29 @@ extern "C" int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *st
 namespace {
 constexpr int kStaticGpChunks = 131072;  // input chunks the static scratch holds
 constexpr int kStaticWindows = 64;       // window arguments copied per batch
-constexpr int kStaticMaxDevices = 64;
-std::mutex g_static_mu;
-float *g_static_gp_ptr[kStaticMaxDevices];
-WindowArgs *g_static_wtab_ptr[kStaticMaxDevices];
-WindowTimes *g_static_wtimes_ptr[kStaticMaxDevices];
 }  // namespace
 
 static __device__ __align__(256) float g_static_gp[32 * kStaticGpChunks];
 static __device__ __align__(256) WindowArgs g_static_wtab[kStaticWindows];
 static __device__ __align__(256) WindowTimes g_static_wtimes[kStaticWindows];
 
-// Device addresses of the static arrays on ctx's device (which is current).
+// Device addresses of the static arrays on ctx's device (which is current),
+// looked up on the context's first call.  A context does not outlive its
+// device's primary context (a device reset frees its buffers), so the
+// addresses it keeps stay valid for as long as it can run.
 static int static_scratch(EdenGpuCtx *ctx, float **gp, WindowArgs **tab, WindowTimes **times) {
-    const int dev = ctx->device;
-    if (dev < 0 || dev >= kStaticMaxDevices)
-        return ctx->fail(EDEN_GPU_E_RANGE, "edenGpuRunStaticScratch: device %d beyond the %d supported", dev,
-                         kStaticMaxDevices);
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_gp_ptr[dev]) {
-        void *p = nullptr, *q = nullptr;
+    if (!ctx->static_gp) {
+        void *p = nullptr, *q = nullptr, *r = nullptr;
         CUDA_TRY(ctx, cudaGetSymbolAddress(&p, g_static_gp));
         CUDA_TRY(ctx, cudaGetSymbolAddress(&q, g_static_wtab));
-        void *r = nullptr;
         CUDA_TRY(ctx, cudaGetSymbolAddress(&r, g_static_wtimes));
-        g_static_wtimes_ptr[dev] = (WindowTimes *)r;
-        g_static_gp_ptr[dev] = (float *)p;
-        g_static_wtab_ptr[dev] = (WindowArgs *)q;
+        ctx->static_gp = (float *)p;
+        ctx->static_tab = (WindowArgs *)q;
+        ctx->static_times = (WindowTimes *)r;
     }
-    *gp = g_static_gp_ptr[dev];
-    *tab = g_static_wtab_ptr[dev];
-    *times = g_static_wtimes_ptr[dev];
+    *gp = ctx->static_gp;
+    *tab = ctx->static_tab;
+    *times = ctx->static_times;
     return 0;
 }
 
@@ -1794,6 +1852,7 @@ static int static_scratch(EdenGpuCtx *ctx, float **gp, WindowArgs **tab, WindowT
 // `dm` (the context's, scratch pointer replaced) and without timing marks.
 static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const WindowArgs *tab, const WindowTimes *times,
                                 int idx) {
+    ctx->launched = true;
     cudaStream_t s = ctx->stream;
     const int *zero = ctx->d_zero;
     if (ctx->mode == EDEN_MODE_BATCHED && ctx->smem_window) {
@@ -1815,8 +1874,17 @@ static int launch_window_static(EdenGpuCtx *ctx, const DevModel &dm, const Windo
     return 4;
 }
 
+static int run_static(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
+
 extern "C" int edenGpuRunStaticScratch(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) {
     if (!ctx) return EDEN_GPU_E_INVALID;
+    TRY(check_runnable(ctx));
+    const ClockState c = save_clock(ctx);
+    const int64_t next_before = ctx->next_step;
+    return finish_run(ctx, run_static(ctx, first_step, n_steps), c, next_before);
+}
+
+static int run_static(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps) {
     if (n_steps < 0) return ctx->fail(EDEN_GPU_E_INVALID, "negative step count");
     if (first_step != ctx->next_step)
         return ctx->fail(EDEN_GPU_E_INVALID, "steps must be contiguous: expected first_step %lld",

@@ -340,11 +340,16 @@ int edenGpuRun(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
  * inputs of one type on one compartment; larger models get EDEN_GPU_E_RANGE), window arguments in a static device table, and the
  * launches are direct (no graph, no kernel timing).  Results equal
  * edenGpuRun's; the two may be interleaved on one context.
- * The first call on a device performs a one-time set-up (looking up the
- * static arrays' device addresses); n_steps = 0 does only that, and it should
- * come before any stream capture starts.  The static arrays are shared by all
- * contexts on a device: calls that overlap in time on one device race on
- * them, so serialise them. */
+ * The first call on a context performs a one-time set-up (looking up the
+ * static arrays' device addresses with the context's device current);
+ * n_steps = 0 does only that, and it should come before any stream capture
+ * starts.  The static arrays belong to the library's module, so every device
+ * that loads the library's kernels holds their 16 MiB until the process
+ * exits, whether or not this entry point is used.  They are shared by all
+ * contexts on a device and keep the last call's contents: calls that
+ * overlap in time on one device race on them, so serialise them.
+ * A run that fails before issuing any kernel leaves the context as it was;
+ * one that fails after (edenGpuRun too) leaves it refusing further runs. */
 int edenGpuRunStaticScratch(EdenGpuCtx *ctx, int64_t first_step, int64_t n_steps);
 
 /* Copy records accumulated since the last fetch into caller buffers. */
