@@ -206,7 +206,7 @@ def adjoint_sample():
     from cable_grad import Cable, loss_and_trace_grad
     from eden_gb300 import lowering, workloads
     from eden_gb300.engine import MODE_BATCHED, Simulation
-    from eden_gb300.gradient import CableGradient, per_cell_density_map
+    from eden_gb300.gradient import CableGradient, per_cell_density_map, with_weights
     dens = [1, 2, 0, 4, 5, 3]
     spec = workloads.ball_and_stick(seed=1234)
     tspec = workloads.ball_and_stick(seed=4321)
@@ -248,8 +248,46 @@ def adjoint_sample():
     g64 = np.einsum("nc,jnc->cj", tg_s, dtr)
     rel = float((np.abs(grad_s - g64).max(0) / np.abs(g64).max(0)).max())
     f_ms, b_ms = min(fwd), min(bwd)
+    # the same cells with synaptic drive fixed in advance: 8 spike-list expTwo
+    # connections per cell on the dendrite and 2 timed expOne inputs on the
+    # soma, every weight a parameter as well
+    dlow = lowering.lower(workloads.ball_and_stick(seed=1234, syn_drive=8))
+    dpm = with_weights(dlow, per_cell_density_map(dlow, dens))
+    gd = CableGradient(dlow, dpm, rec_comp=rec, checkpoint_every=100)
+    dfwd, dbwd = [], []
+    for _ in range(3):
+        tr = gd.forward(dpm.values)
+        _, tg = loss_and_trace_grad(tr.astype(np.float64), target)
+        gd.backward(tg)
+        f, b = gd.timing()
+        dfwd.append(f)
+        dbwd.append(b)
+    gd.close()
+    dsub = lowering.lower(workloads.ball_and_stick(n_inst=n_sub, length_ms=sub_ms, params=spec.params[:n_sub],
+                                                   syn_drive=8))
+    dspm = with_weights(dsub, per_cell_density_map(dsub, dens))
+    gs = CableGradient(dsub, dspm, rec_comp=srec)
+    tr_s = gs.forward(dspm.values).astype(np.float64)
+    _, tg_s = loss_and_trace_grad(tr_s, target[:dsub.n_steps, :n_sub])
+    grad_d = gs.backward(tg_s)
+    gs.close()
+    wpar = np.concatenate([dspm.syn_param, dspm.timed_param])
+    dcab = Cable(dsub, dspm.chan_param, dspm.cell_ra_param, dsub.phys_ra, dspm.syn_param, dspm.timed_param)
+    wdirs = np.zeros((len(wpar), dspm.n_params))
+    wdirs[np.arange(len(wpar)), wpar] = 1.0
+    _, wdtr = dcab.run(dspm.values, dsub.n_steps, srec, wdirs)
+    gw64 = np.einsum("nc,jnc->j", tg_s, wdtr)
+    wrel = float(np.abs(grad_d[wpar] - gw64).max() / np.abs(gw64).max())
+    f_d, b_d = min(dfwd), min(dbwd)
     return {"config": "ball_and_stick: 256 cells x 51 compartments, 7 parameters each (1792), "
                       "dt 0.025 ms, 200 ms (8001 steps), checkpoints every 100 steps",
+            "synaptic_drive": {
+                "config": f"the same cells with 8 spike-list expTwo connections and 2 timed expOne inputs each, "
+                          f"every weight a parameter too ({dpm.n_params} parameters)",
+                "forward_ms": f_d, "backward_ms": b_d, "backward_over_forward": b_d / f_d,
+                "weight_grad_max_rel_err_vs_fp64": wrel,
+                "grad_check": f"first {n_sub} cells, first {sub_ms:g} ms: the weights' GPU adjoint against "
+                              "double-precision forward sensitivities, relative to the largest"},
             "loss": loss, "grad_norm": float(np.linalg.norm(grad)),
             "forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
             "batched_simulation_ms": sim_ms, "backward_over_batched_simulation": b_ms / sim_ms,

@@ -23,6 +23,21 @@
 //   dQ/dq + g_bar gbase 1e-5 A dfopen/dq.  dQ/dq = b and dQ/dV = b'(q - inf)
 //   + (1 - b) inf' where the gate did not clamp, 0 where it did.
 //
+// Synaptic drive with event steps fixed in advance -- timedSynapticInput
+// inputs and connection synapses whose presynaptic cell is a spike source
+// (spike lists, generators, event-set readers) -- enters each step as
+// conductances g_k = sum_s w_s g^_s(n) per group k (one compartment, one
+// synapse type, inputs or connections), with g^_s the unit-weight exposure
+// of synapse s at step n (expTwo gbase (B - A), expOne G;
+// LEMS_CoreComponents.inc.xml:145-180, eden/Eden.cpp:3424-3466): forward
+// Euler between events, the event's jump instead of the decay in its step.
+// g^_s does not depend on V or on the weights, so a k_grad_drive launch
+// tabulates g_k(n) for the run before the forward, and the adjoint gives
+// g_bar_k(n) = (d_bar + mu dt E_k) / C like a channel's; a weight's gradient
+// is then sum_n g_bar_k(n) g^_s(n) (eden/Eden.cpp:3708-3710 multiplies the
+// synapse's current and conductance by its weight), summed per synapse in
+// double by k_grad_weights.
+//
 // Cells are independent, so one warp carries one cell through the whole run
 // in one launch, synchronising only within the warp.  The forward kernel
 // writes the trace and a checkpoint of (V, q) every S steps; the backward
@@ -51,6 +66,13 @@ namespace eden_grad {
 
 constexpr int kMaxSlots = 32;  // distinct parameters one cell may use
 
+// A synapse type as the drive needs it: kind, gbase (uS), time constants
+// (us) and expTwo's jump weight_prop * waveform_factor.
+struct GradSyn {
+    int32_t kind;
+    float gbase, tau_decay, tau_rise, wf_w;
+};
+
 struct GradDev {
     int n_cells = 0, n_rec = 0, S = 100, n_types = 0;
     int64_t N = 0, n_comp = 0, n_gate = 0;
@@ -72,6 +94,20 @@ struct GradDev {
     // recorded compartments (local index) and their trace columns
     const int32_t *rec_local, *rec_col;
     const float *tk;  // [N + 1]: tk[n] = time of step n
+    // synaptic drive: groups of each compartment (breadth-first order),
+    // each group's reversal potential, kind (0 inputs, 1 connections) and
+    // items; each item's synapse type, weight (or parameter) and event steps
+    int32_t n_grp = 0;
+    int64_t n_item = 0;
+    const int32_t *comp_gr0, *gr_kind, *gr_it0, *it_grp, *it_type, *it_param, *it_ev;
+    const int64_t *it_ev0;
+    const float *gr_erev, *it_w;
+    const GradSyn *syn;
+    float *it_a, *it_b;      // unit-weight synapse state while tabulating
+    int64_t *it_cur;         // its next event
+    float *gtab;             // [N + 1][n_grp] group conductance at step n (weights applied)
+    float *gbar;             // [N + 1][n_grp] its adjoint
+    double *item_grad;       // [n_item] d loss / d weight
     const float *params;
     float *ck_v, *ck_q;  // checkpoints [n_ck][n_comp], [n_ck][n_gate]
     float *tr_v, *tr_q;  // one segment's trajectory [S + 1][n_comp], [S + 1][n_gate]
@@ -200,8 +236,8 @@ __device__ __forceinline__ float rate_slope(int kind, float r, float mid, float 
 // Channels and V pre-update of compartment j at time t: advances its gates
 // in place and returns the pre-updated V (x) and the diagonal term d, with
 // the plain path's operations (target_step).
-__device__ __forceinline__ void comp_pre(const GradDev &m, const Cell &c, int j, float t, float v, bool init,
-                                         float &x, float &d) {
+__device__ __forceinline__ void comp_pre(const GradDev &m, const Cell &c, int j, int64_t n, float t, float v,
+                                         bool init, float &x, float &d) {
     const float A = c.Ac[j];
     float Ich = 0.0f, Gch = 0.0f;
     for (int k = c.ch0[j]; k < c.ch0[j + 1]; k++) {
@@ -225,11 +261,36 @@ __device__ __forceinline__ void comp_pre(const GradDev &m, const Cell &c, int j,
         const float st = m.pu_start[k], du = m.pu_dur[k];
         Iin += (st <= t && t <= st + du) ? m.pu_aw[k] : 0.0f;
     }
-    const float I = Ich + Iin;
-    const float G = Gch;
+    // synaptic drive: inputs, then connections (eden/Eden.cpp:6057-6060)
+    float Gin = 0.0f, Isyn = 0.0f, Gsyn = 0.0f;
+    if (!init)
+        for (int k = m.comp_gr0[gc]; k < m.comp_gr0[gc + 1]; k++) {
+            const float g = m.gtab[n * m.n_grp + k];
+            if (m.gr_kind[k] == 0) {
+                Iin += g * (m.gr_erev[k] - v);
+                Gin += g;
+            } else {
+                Isyn += g * (m.gr_erev[k] - v);
+                Gsyn += g;
+            }
+        }
+    const float I = Ich + Iin + Isyn;
+    const float G = Gch + Gin + Gsyn;
     const float C = c.Cc[j];
     d = 1.0f * (G / C) + c.IRCs[j];
     x = init ? v : v + (m.dt * (I + (v * G))) / C;
+}
+
+// The total conductance of compartment gc at step n, its channels' Gch
+// plus its drive groups', summed in comp_pre's order.
+__device__ __forceinline__ float total_g(const GradDev &m, int gc, int64_t n, float Gch) {
+    float Gin = 0.0f, Gsyn = 0.0f;
+    for (int k = m.comp_gr0[gc]; k < m.comp_gr0[gc + 1]; k++) {
+        const float g = m.gtab[n * m.n_grp + k];
+        if (m.gr_kind[k] == 0) Gin += g;
+        else Gsyn += g;
+    }
+    return Gch + Gin + Gsyn;
 }
 
 // Backward-Euler Hines solve of the cell (eden/Eden.cpp:6114-6225): D holds
@@ -344,11 +405,12 @@ __device__ __forceinline__ void hines_cell(float dt, const Cell &c, bool transpo
 }
 
 // One forward step n -> n + 1 of the staged cell.
-__device__ __forceinline__ void forward_step(const GradDev &m, const Cell &c, float t) {
+__device__ __forceinline__ void forward_step(const GradDev &m, const Cell &c, int64_t n) {
     const int lane = threadIdx.x & 31;
+    const float t = m.tk[n];
     for (int j = lane; j < c.nc; j += 32) {
         float x, d;
-        comp_pre(m, c, j, t, c.V[j], false, x, d);
+        comp_pre(m, c, j, n, t, c.V[j], false, x, d);
         c.X[j] = x;
         c.D[j] = d;
     }
@@ -367,7 +429,7 @@ __global__ void __launch_bounds__(32) k_grad_forward(GradDev m, Dims dm) {
     // the four initialisation passes leave V and set every gate to inf(V)
     for (int j = lane; j < c.nc; j += 32) {
         float x, d;
-        comp_pre(m, c, j, 0.0f, c.V[j], true, x, d);
+        comp_pre(m, c, j, 0, 0.0f, c.V[j], true, x, d);
     }
     const int r0 = m.cell_r0[cell], r1 = m.cell_r0[cell + 1];
     int64_t ck = 0;
@@ -382,7 +444,7 @@ __global__ void __launch_bounds__(32) k_grad_forward(GradDev m, Dims dm) {
         }
         to_ck--;
         for (int r = r0 + lane; r < r1; r += 32) m.trace[(n - 1) * m.n_rec + m.rec_col[r]] = c.V[m.rec_local[r]];
-        if (n < m.N) forward_step(m, c, m.tk[n]);
+        if (n < m.N) forward_step(m, c, n);
     }
 }
 
@@ -398,7 +460,7 @@ __device__ __forceinline__ void add_trace_grad(const GradDev &m, int cell, int64
 // Adjoint of step n -> n + 1: on entry V = V^n, VN = V^{n+1}, q = q^n, LV and
 // LQ the adjoints of V^{n+1} and q^{n+1}; on return LV and LQ are those of
 // V^n and q^n, and the parameter terms of the step are in acc.
-__device__ __forceinline__ void adjoint_step(const GradDev &m, const Cell &c) {
+__device__ __forceinline__ void adjoint_step(const GradDev &m, const Cell &c, int64_t n) {
     const int lane = threadIdx.x & 31;
     const float dt = m.dt;
     for (int j = lane; j < c.nc; j += 32) {
@@ -412,7 +474,8 @@ __device__ __forceinline__ void adjoint_step(const GradDev &m, const Cell &c) {
                 for (int r = 0; r < ct.gate_instances[g]; r++) fopen = fopen * qq[g];
             Gch += ((c.cgb[k] * fopen) * 1e-5f) * A;
         }
-        c.D[j] = 1.0f * (Gch / c.Cc[j]) + c.IRCs[j];
+        const float G = m.n_grp ? total_g(m, c.c0 + j, n, Gch) : Gch;
+        c.D[j] = 1.0f * (G / c.Cc[j]) + c.IRCs[j];
         c.X[j] = c.LV[j];
     }
     __syncwarp();
@@ -429,6 +492,9 @@ __device__ __forceinline__ void adjoint_step(const GradDev &m, const Cell &c) {
             acc[c.ra_slot * 32] += r;
         }
         const float C = c.Cc[j], A = c.Ac[j];
+        // the drive groups' conductance adjoints, for the weight gradients
+        for (int k = m.comp_gr0[c.c0 + j]; k < m.comp_gr0[c.c0 + j + 1]; k++)
+            m.gbar[n * m.n_grp + k] = (dbar + mu * dt * m.gr_erev[k]) / C;
         for (int k = c.ch0[j]; k < c.ch0[j + 1]; k++) {
             const EdenGpuChannelType &ct = c.types[c.ctype[k]];
             const int q0 = c.cg0[k];
@@ -515,7 +581,7 @@ __global__ void __launch_bounds__(32) k_grad_backward(GradDev m, Dims dm) {
         }
         __syncwarp();
         for (int64_t n = n0; n < n1; n++) {
-            forward_step(m, c, m.tk[n]);
+            forward_step(m, c, n);
             const int64_t k = n + 1 - n0;
             for (int j = lane; j < c.nc; j += 32) m.tr_v[k * m.n_comp + c.c0 + j] = c.V[j];
             for (int g = lane; g < c.ng; g += 32) m.tr_q[k * m.n_gate + c.g0 + g] = c.q[g];
@@ -530,7 +596,7 @@ __global__ void __launch_bounds__(32) k_grad_backward(GradDev m, Dims dm) {
             }
             for (int g = lane; g < c.ng; g += 32) c.q[g] = m.tr_q[k * m.n_gate + c.g0 + g];
             __syncwarp();
-            adjoint_step(m, c);
+            adjoint_step(m, c, n);
             add_trace_grad(m, cell, n, c.LV);
         }
     }
@@ -541,6 +607,75 @@ __global__ void __launch_bounds__(32) k_grad_backward(GradDev m, Dims dm) {
         if (k == c.ra_slot) tot /= (double)m.params[m.cell_ra_param[cell]];
         m.slot_grad[s0 + k] = tot;
     }
+}
+
+// The unit-weight exposure of item s at step n and its state update
+// (forward Euler; the event's jump instead of the decay in its step).
+__device__ __forceinline__ float item_exposure(const GradSyn &st, float a, float b) {
+    return st.kind == EDEN_SYN_EXPTWO ? st.gbase * (b - a) : a;
+}
+__device__ __forceinline__ void item_update(const GradSyn &st, float dt, bool event, float &a, float &b) {
+    if (st.kind == EDEN_SYN_EXPTWO) {
+        if (event) {
+            a = a + st.wf_w;
+            b = b + st.wf_w;
+        } else {
+            a = a + dt * (-a / st.tau_rise);
+            b = b + dt * (-b / st.tau_decay);
+        }
+    } else {
+        a = event ? a + st.gbase : a - dt * (a / st.tau_decay);
+    }
+}
+
+// gtab[n][k] = sum over the group's items of weight * unit-weight exposure,
+// for steps 1 .. N - 1 (one thread per group; items in group order).
+__global__ void k_grad_drive(GradDev m) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_grp) return;
+    const int i0 = m.gr_it0[k], i1 = m.gr_it0[k + 1];
+    for (int i = i0; i < i1; i++) {
+        m.it_a[i] = 0.0f;
+        m.it_b[i] = 0.0f;
+        m.it_cur[i] = m.it_ev0[i];
+    }
+    m.gtab[k] = 0.0f;
+    for (int64_t n = 1; n <= m.N; n++) {
+        float g = 0.0f;
+        for (int i = i0; i < i1; i++) {
+            const GradSyn st = m.syn[m.it_type[i]];
+            float a = m.it_a[i], b = m.it_b[i];
+            const float w = m.it_param[i] >= 0 ? m.params[m.it_param[i]] : m.it_w[i];
+            g += w * item_exposure(st, a, b);
+            const int64_t e = m.it_cur[i];
+            const bool event = e < m.it_ev0[i + 1] && m.it_ev[e] == (int32_t)n;
+            if (event) m.it_cur[i] = e + 1;
+            item_update(st, m.dt, event, a, b);
+            m.it_a[i] = a;
+            m.it_b[i] = b;
+        }
+        m.gtab[n * m.n_grp + k] = g;
+    }
+}
+
+// d loss / d weight of each item: sum over steps 1 .. N - 1 of the group's
+// conductance adjoint times the item's unit-weight exposure, in double.
+__global__ void k_grad_weights(GradDev m) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.n_item) return;
+    const int k = m.it_grp[i];
+    const GradSyn st = m.syn[m.it_type[i]];
+    float a = 0.0f, b = 0.0f;
+    int64_t e = m.it_ev0[i];
+    const int64_t e1 = m.it_ev0[i + 1];
+    double acc = 0.0;
+    for (int64_t n = 1; n < m.N; n++) {
+        acc += (double)m.gbar[n * m.n_grp + k] * (double)item_exposure(st, a, b);
+        const bool event = e < e1 && m.it_ev[e] == (int32_t)n;
+        if (event) e++;
+        item_update(st, m.dt, event, a, b);
+    }
+    m.item_grad[i] = acc;
 }
 
 }  // namespace eden_grad
@@ -559,6 +694,7 @@ struct EdenGpuGrad {
     size_t smem = 0;
     std::vector<int32_t> slot_param;     // slot -> parameter
     std::vector<int32_t> cell_ra_param;  // host copy, for the forward's checks
+    std::vector<int32_t> item_param;     // parameter that is each drive item's weight, or -1
     std::vector<float> h_params;
     float *d_params = nullptr, *d_trace = nullptr, *d_tgrad = nullptr;
     double *d_slot = nullptr;
@@ -612,12 +748,40 @@ int validate(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
     if (m->abi_version != EDEN_GPU_ABI_VERSION)
         return g->fail(EDEN_GPU_E_INVALID, "ABI version %d, library is %d", m->abi_version, EDEN_GPU_ABI_VERSION);
     if (!finite_pos(m->dt)) return g->fail(EDEN_GPU_E_INVALID, "dt must be positive");
-    if (m->n_izh != 0 || m->n_syn != 0 || m->n_pois != 0 || m->n_timed != 0 || m->n_wave != 0 || m->n_clamp != 0)
+    if (m->n_izh != 0 || m->n_pois != 0 || m->n_wave != 0 || m->n_clamp != 0)
         return g->fail(EDEN_GPU_E_INVALID,
-                       "gradients cover independent physical cells with HH channels and pulse inputs: the model has "
-                       "%d point neurons, %lld synapses, %lld Poisson, %lld timed and %lld waveform inputs",
-                       m->n_izh, (long long)m->n_syn, (long long)m->n_pois, (long long)m->n_timed,
-                       (long long)m->n_wave);
+                       "gradients cover independent physical cells with HH channels, pulse inputs and synaptic drive "
+                       "with fixed events: the model has %d point neurons, %lld Poisson, %lld waveform and %lld clamp "
+                       "inputs",
+                       m->n_izh, (long long)m->n_pois, (long long)m->n_wave, (long long)m->n_clamp);
+    for (int k = 0; k < m->n_syn_types; k++) {
+        const EdenGpuSynapseType &t = m->syn_types[k];
+        if ((t.kind != EDEN_SYN_EXPONE && t.kind != EDEN_SYN_EXPTWO) || !std::isfinite(t.gbase) ||
+            !std::isfinite(t.erev) || !finite_pos(t.tau_decay) || (t.kind == EDEN_SYN_EXPTWO && !finite_pos(t.tau_rise)))
+            return g->fail(EDEN_GPU_E_INVALID, "synapse type %d: bad parameters", k);
+    }
+    for (int64_t k = 0; k < m->n_syn; k++) {
+        const int src = m->syn_src[k];
+        if (src < 0 || src >= m->n_src) return g->fail(EDEN_GPU_E_INVALID, "synapse %lld: bad source", (long long)k);
+        if (m->src_target[src] >= 0)
+            return g->fail(EDEN_GPU_E_INVALID,
+                           "synapse %lld: its presynaptic cell %d spikes, so its events depend on the parameters; "
+                           "gradients need synaptic events fixed in advance (spike sources without a membrane)",
+                           (long long)k, src);
+        if (m->syn_target[k] < 0 || m->syn_target[k] >= m->n_comp || m->syn_type[k] < 0 ||
+            m->syn_type[k] >= m->n_syn_types || !(m->syn_delay[k] >= 0.0f) || !std::isfinite(m->syn_delay[k]) ||
+            !std::isfinite(m->syn_weight[k]))
+            return g->fail(EDEN_GPU_E_INVALID, "synapse %lld: bad target, type, delay or weight", (long long)k);
+    }
+    for (int64_t k = 0; k < m->n_timed; k++) {
+        if (m->timed_target[k] < 0 || m->timed_target[k] >= m->n_comp || m->timed_type[k] < 0 ||
+            m->timed_type[k] >= m->n_syn_types || !std::isfinite(m->timed_weight[k]) ||
+            m->timed_off[k + 1] < m->timed_off[k])
+            return g->fail(EDEN_GPU_E_INVALID, "timed input %lld: bad target, type, weight or steps", (long long)k);
+    }
+    for (int64_t e = 0; e < m->n_ext; e++)
+        if (m->ext_src[e] < 0 || m->ext_src[e] >= m->n_src || (e > 0 && m->ext_step[e] < m->ext_step[e - 1]))
+            return g->fail(EDEN_GPU_E_INVALID, "spike-source events must name a source and be sorted by step");
     if (m->n_phys <= 0 || m->n_comp <= 0) return g->fail(EDEN_GPU_E_INVALID, "no physical cells");
     for (int k = 0; k < m->n_chan_types; k++)
         for (int q = 0; q < m->chan_types[k].n_gates && q < EDEN_MAX_GATES; q++)
@@ -687,7 +851,20 @@ int validate(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
     for (int p = 0; p < s->n_params; p++)
         if (chan_use[p] && ra_use[p])
             return g->fail(EDEN_GPU_E_INVALID, "parameter %d is both a conductivity and a resistivity", p);
-    return 0;
+    auto weight_params = [&](const int32_t *par, int64_t n, const char *what) {
+        if (!par) return 0;
+        for (int64_t k = 0; k < n; k++) {
+            const int p = par[k];
+            if (p < -1 || p >= s->n_params)
+                return g->fail(EDEN_GPU_E_INVALID, "%s %lld: parameter %d out of range", what, (long long)k, p);
+            if (p >= 0 && (chan_use[p] || ra_use[p]))
+                return g->fail(EDEN_GPU_E_INVALID, "parameter %d is both a weight and a conductivity or resistivity", p);
+        }
+        return 0;
+    };
+    int rc = weight_params(s->syn_param, m->n_syn, "synapse");
+    if (rc) return rc;
+    return weight_params(s->timed_param, m->n_timed, "timed input");
 }
 
 // Host layout: each cell's compartments breadth-first (children in increasing
@@ -829,6 +1006,84 @@ int build(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
         tk[n] = (float)time;
         time += (double)dt;
     }
+    // ---- synaptic drive: each item's firing steps (timed inputs: listed;
+    // connections from spike sources: the reference's delivery and single
+    // pending-spike rule, eden/Eden.cpp:3646-3686, replayed on the source's
+    // spikes), then groups of one compartment, kind and synapse type --
+    // inputs before connections, types in increasing order -- with their
+    // items in model order
+    struct Item { int comp, kind, type, param; float w; std::vector<int32_t> ev; };
+    std::vector<Item> items;
+    {
+        std::vector<std::vector<int64_t>> spikes_of(m->n_src);
+        for (int64_t e = 0; e < m->n_ext; e++)
+            if (m->ext_step[e] >= 1 && m->ext_step[e] < d.N) spikes_of[m->ext_src[e]].push_back(m->ext_step[e]);
+        auto due_step = [&](float p) -> int64_t {  // step k in 1 .. N-1 with tk[k] <= p < tk[k] + dt
+            const auto it = std::upper_bound(tk.begin() + 1, tk.begin() + d.N, p);
+            const int64_t j = (int64_t)(it - tk.begin()) - 1;
+            for (int64_t k = std::max<int64_t>(1, j - 1); k <= j && k < d.N; k++)
+                if (tk[k] <= p && p < tk[k] + dt) return k;
+            return 0;
+        };
+        for (int64_t k = 0; k < m->n_timed; k++) {
+            Item it{new_of[m->timed_target[k]], 0, m->timed_type[k], s->timed_param ? s->timed_param[k] : -1,
+                    m->timed_weight[k], {}};
+            for (int64_t e = m->timed_off[k]; e < m->timed_off[k + 1]; e++)
+                if (m->timed_step[e] >= 1 && m->timed_step[e] < d.N) it.ev.push_back((int32_t)m->timed_step[e]);
+            items.push_back(std::move(it));
+        }
+        for (int64_t k = 0; k < m->n_syn; k++) {
+            Item it{new_of[m->syn_target[k]], 1, m->syn_type[k], s->syn_param ? s->syn_param[k] : -1,
+                    m->syn_weight[k], {}};
+            const float delay = m->syn_delay[k];
+            float pend = -INFINITY;
+            for (int64_t step : spikes_of[m->syn_src[k]]) {
+                const float t = tk[step], fresh = t + delay, tdt = t + dt;
+                if (t <= fresh && fresh < tdt) it.ev.push_back((int32_t)step);
+                if (pend < tdt && pend < fresh) {
+                    pend = fresh;
+                    const int64_t kd = due_step(pend);
+                    if (kd > 0) it.ev.push_back((int32_t)kd);
+                }
+            }
+            std::sort(it.ev.begin(), it.ev.end());
+            it.ev.erase(std::unique(it.ev.begin(), it.ev.end()), it.ev.end());
+            items.push_back(std::move(it));
+        }
+        std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) {
+            if (a.comp != b.comp) return a.comp < b.comp;
+            if (a.kind != b.kind) return a.kind < b.kind;
+            return a.type < b.type;
+        });
+    }
+    std::vector<int32_t> comp_gr0(m->n_comp + 1, 0), gr_kind, gr_it0, it_grp, it_type, it_param, it_ev;
+    std::vector<int64_t> it_ev0{0};
+    std::vector<float> gr_erev, it_w;
+    for (size_t i = 0; i < items.size(); i++) {
+        const Item &it = items[i];
+        if (i == 0 || it.comp != items[i - 1].comp || it.kind != items[i - 1].kind || it.type != items[i - 1].type) {
+            gr_kind.push_back(it.kind);
+            gr_erev.push_back(m->syn_types[it.type].erev);
+            gr_it0.push_back((int32_t)i);
+            comp_gr0[it.comp + 1]++;
+        }
+        it_grp.push_back((int32_t)gr_kind.size() - 1);
+        it_type.push_back(it.type);
+        it_param.push_back(it.param);
+        it_w.push_back(it.w);
+        it_ev.insert(it_ev.end(), it.ev.begin(), it.ev.end());
+        it_ev0.push_back((int64_t)it_ev.size());
+    }
+    gr_it0.push_back((int32_t)items.size());
+    for (int i = 0; i < m->n_comp; i++) comp_gr0[i + 1] += comp_gr0[i];
+    std::vector<GradSyn> syn(std::max(m->n_syn_types, 1));
+    for (int k = 0; k < m->n_syn_types; k++) {
+        const EdenGpuSynapseType &t = m->syn_types[k];
+        syn[k] = GradSyn{t.kind, t.gbase, t.tau_decay, t.tau_rise, t.weight_prop * t.waveform_factor};
+    }
+    d.n_grp = (int32_t)gr_kind.size();
+    d.n_item = (int64_t)items.size();
+    g->item_param = it_param;
     g->cell_ra_param = cell_ra_param;
     // shared memory per warp
     const Dims &dm = g->dims;
@@ -857,7 +1112,20 @@ int build(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
     UP(ch_gbase, ch_gbase); UP(ch_erev, ch_erev); UP(types, types);
     UP(pu_start, pu_start); UP(pu_dur, pu_dur); UP(pu_aw, pu_aw);
     UP(rec_local, rec_local); UP(rec_col, rec_col); UP(tk, tk);
+    UP(comp_gr0, comp_gr0); UP(gr_kind, gr_kind); UP(gr_it0, gr_it0); UP(it_grp, it_grp); UP(it_type, it_type);
+    UP(it_param, it_param); UP(it_ev, it_ev); UP(it_ev0, it_ev0); UP(gr_erev, gr_erev); UP(it_w, it_w);
+    UP(syn, syn);
 #undef UP
+    if (d.n_grp > 0) {
+        const size_t rows = (size_t)(d.N + 1) * d.n_grp;
+        if ((rc = alloc(g, &d.gtab, rows)) != 0) return rc;
+        if ((rc = alloc(g, &d.gbar, rows)) != 0) return rc;
+        if ((rc = alloc(g, &d.it_a, (size_t)d.n_item)) != 0) return rc;
+        if ((rc = alloc(g, &d.it_b, (size_t)d.n_item)) != 0) return rc;
+        if ((rc = alloc(g, &d.it_cur, (size_t)d.n_item)) != 0) return rc;
+        if ((rc = alloc(g, &d.item_grad, (size_t)d.n_item)) != 0) return rc;
+        GTRY(g, cudaMemset(d.gbar, 0, rows * sizeof(float)));
+    }
     const int64_t n_ck = d.N >= 2 ? (d.N - 2) / d.S + 1 : 1;
     if ((rc = alloc(g, &g->d_params, (size_t)std::max(s->n_params, 1))) != 0) return rc;
     d.params = g->d_params;
@@ -921,6 +1189,7 @@ extern "C" int edenGpuGradForward(EdenGpuGrad *g, const float *params, float *tr
     GTRY(g, cudaMemcpyAsync(g->d_params, g->h_params.data(), sizeof(float) * g->h_params.size(), cudaMemcpyHostToDevice,
                             g->stream));
     GTRY(g, cudaEventRecord(g->e0, g->stream));
+    if (g->d.n_grp > 0) k_grad_drive<<<(g->d.n_grp + 127) / 128, 128, 0, g->stream>>>(g->d);
     k_grad_forward<<<g->n_cells, 32, g->smem, g->stream>>>(g->d, g->dims);
     GTRY(g, cudaGetLastError());
     GTRY(g, cudaEventRecord(g->e1, g->stream));
@@ -946,11 +1215,15 @@ extern "C" int edenGpuGradBackward(EdenGpuGrad *g, const float *trace_grad, floa
                                 g->stream));
     GTRY(g, cudaEventRecord(g->e0, g->stream));
     k_grad_backward<<<g->n_cells, 32, g->smem, g->stream>>>(g->d, g->dims);
+    if (g->d.n_item > 0) k_grad_weights<<<(unsigned)((g->d.n_item + 127) / 128), 128, 0, g->stream>>>(g->d);
     GTRY(g, cudaGetLastError());
     GTRY(g, cudaEventRecord(g->e1, g->stream));
-    std::vector<double> slots(g->slot_param.size());
+    std::vector<double> slots(g->slot_param.size()), items((size_t)g->d.n_item);
     if (!slots.empty())
         GTRY(g, cudaMemcpyAsync(slots.data(), g->d_slot, sizeof(double) * slots.size(), cudaMemcpyDeviceToHost, g->stream));
+    if (!items.empty())
+        GTRY(g, cudaMemcpyAsync(items.data(), g->d.item_grad, sizeof(double) * items.size(), cudaMemcpyDeviceToHost,
+                                g->stream));
     GTRY(g, cudaStreamSynchronize(g->stream));
     float ms = 0.0f;
     GTRY(g, cudaEventElapsedTime(&ms, g->e0, g->e1));
@@ -958,6 +1231,8 @@ extern "C" int edenGpuGradBackward(EdenGpuGrad *g, const float *trace_grad, floa
     // per parameter, the cells' terms in cell order
     std::vector<double> acc(std::max(g->n_params, 1), 0.0);
     for (size_t k = 0; k < slots.size(); k++) acc[g->slot_param[k]] += slots[k];
+    for (size_t k = 0; k < items.size(); k++)  // the weights' terms in item order
+        if (g->item_param[k] >= 0) acc[g->item_param[k]] += items[k];
     std::vector<float> out(std::max(g->n_params, 1));
     for (int p = 0; p < g->n_params; p++) out[p] = (float)acc[p];
     if (g->n_params > 0) GTRY(g, cudaMemcpy(param_grad, out.data(), sizeof(float) * g->n_params, cudaMemcpyDefault));

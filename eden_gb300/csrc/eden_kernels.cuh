@@ -1031,11 +1031,54 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
 // G/C + sum 1/(RC) on entry, X its pre-updated V) and its children's
 // factors, in increasing child order as the reference's post-order visits
 // them.  A depth's compartments are spread over the lanes (at most 64 per
-// depth, two per lane, unless a single cell is wider); LV packs each depth's first
-// compartment and whether it holds a non-flat one.
+// depth, two per lane, unless a single cell is wider); LV packs each
+// depth's first compartment and whether it holds a non-flat one.
 // Back-substitution runs root-first.  X holds V_next on return.
+//
+// The step's critical path is the chain of dependent shared-memory loads,
+// so each lane loads everything its (up to two) compartments of a depth
+// need -- descriptors, values, and the first kPull children's factors and
+// eliminated values -- before it runs their subtraction chains, which keep
+// the reference's order: a compartment subtracts its children's terms one
+// by one in increasing child order.
 constexpr int32_t kLvMask = 0xffff;
 constexpr int32_t kLvNonFlat = 1 << 16;
+constexpr int kPull = 4;  // children whose terms are loaded up front
+
+// The children [kb, ke) of one compartment: their elimination factors and
+// eliminated values (and, for a non-flat parent, their U), loaded together.
+struct Pull {
+    float r[kPull], x[kPull], u[kPull];
+};
+__device__ __forceinline__ void pull_load(Pull &p, const float *RT, const float *X, const float *U, int kb, int ke,
+                                          bool with_u) {
+#pragma unroll
+    for (int q = 0; q < kPull; q++) {
+        const bool on = kb + q < ke;
+        p.r[q] = on ? RT[kb + q] : 0.0f;
+        p.x[q] = on ? X[kb + q] : 0.0f;
+        p.u[q] = (on && with_u) ? U[kb + q] : 0.0f;
+    }
+}
+
+// Eliminate one compartment's children from its right-hand side xj (and,
+// non-flat, from its diagonal dj), in child order.
+__device__ __forceinline__ void pull_apply(const Pull &p, const float *RT, const float *X, const float *U, int kb,
+                                           int ke, bool nonflat, float &xj, float &dj) {
+#pragma unroll
+    for (int q = 0; q < kPull; q++) {
+        if (kb + q < ke) {
+            if (nonflat) dj -= p.r[q] * p.u[q];
+            xj -= p.r[q] * p.x[q];
+        }
+    }
+    for (int i = kb + kPull; i < ke; i++) {
+        const float r = RT[i];
+        if (nonflat) dj -= r * U[i];
+        xj -= r * X[i];
+    }
+}
+
 __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC, const float *L, float *PV,
                                              float *RT, const float *U, const uint32_t *CEP, const int32_t *LV,
                                              int nlev) {
@@ -1043,41 +1086,55 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
     int end = LV[nlev] & kLvMask;
     for (int lev = nlev - 1; lev >= 0; lev--) {
         const int32_t lw = LV[lev];
+        const int beg = lw & kLvMask;
+        const bool lvl_nf = (lw & kLvNonFlat) != 0;
         // a depth holds at most 64 compartments unless one cell alone is wider
-        for (int j = (lw & kLvMask) + lane; j < end; j += 32) {
-            const uint32_t cep = CEP[j];
-            const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
-            float xj = X[j] + KC[j];
-            if ((lw & kLvNonFlat) && (cep & kCepNonFlat)) {
-                float dj = 1.0f + PV[j] * dt;
-                for (int i = kb; i < ke; i++) {
-                    const float r = RT[i];
-                    dj -= r * U[i];
-                    xj -= r * X[i];
-                }
-                const float inv = __fdividef(1.0f, dj);
-                PV[j] = inv;
-                RT[j] = L[j] * inv;
-            } else {
-                // most compartments have at most two children: take those
-                // without a loop, in order
-                int i = kb;
-                if (i < ke) xj -= RT[i] * X[i];
-                if (i + 1 < ke) xj -= RT[i + 1] * X[i + 1];
-                for (i = kb + 2; i < ke; i++) xj -= RT[i] * X[i];
+        for (int j0 = beg + lane; j0 < end; j0 += 64) {
+            const int j1 = j0 + 32;
+            const bool has1 = j1 < end;
+            const uint32_t cep0 = CEP[j0], cep1 = has1 ? CEP[j1] : 0u;
+            const int ke0 = (int)(cep0 & kCepMask), kb0 = (int)((cep0 >> kCepBeginShift) & kCepMask);
+            const int ke1 = (int)(cep1 & kCepMask), kb1 = (int)((cep1 >> kCepBeginShift) & kCepMask);
+            const bool nf0 = lvl_nf && (cep0 & kCepNonFlat), nf1 = lvl_nf && (cep1 & kCepNonFlat);
+            float x0 = X[j0] + KC[j0];
+            float x1 = has1 ? X[j1] + KC[j1] : 0.0f;
+            float d0 = nf0 ? 1.0f + PV[j0] * dt : 0.0f;
+            float d1 = nf1 ? 1.0f + PV[j1] * dt : 0.0f;
+            Pull p0, p1;
+            pull_load(p0, RT, X, U, kb0, ke0, nf0);
+            pull_load(p1, RT, X, U, kb1, ke1, nf1);
+            pull_apply(p0, RT, X, U, kb0, ke0, nf0, x0, d0);
+            pull_apply(p1, RT, X, U, kb1, ke1, nf1, x1, d1);
+            if (nf0) {
+                const float inv = __fdividef(1.0f, d0);
+                PV[j0] = inv;
+                RT[j0] = L[j0] * inv;
             }
-            X[j] = xj;
+            if (nf1) {
+                const float inv = __fdividef(1.0f, d1);
+                PV[j1] = inv;
+                RT[j1] = L[j1] * inv;
+            }
+            X[j0] = x0;
+            if (has1) X[j1] = x1;
         }
-        end = lw & kLvMask;
+        end = beg;
         __syncwarp();
     }
     for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) X[r] = X[r] * PV[r];
     __syncwarp();
     for (int lev = 1; lev < nlev; lev++) {
         const int i1 = LV[lev + 1] & kLvMask;
-        for (int i = (LV[lev] & kLvMask) + lane; i < i1; i += 32) {
-            const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
-            X[i] = (X[i] - U[i] * X[p]) * PV[i];
+        for (int i0 = (LV[lev] & kLvMask) + lane; i0 < i1; i0 += 64) {
+            const int i1b = i0 + 32;
+            const bool has1 = i1b < i1;
+            const int p0 = (int)((CEP[i0] >> kCepParentShift) & kCepMask) - 1;
+            const int p1 = has1 ? (int)((CEP[i1b] >> kCepParentShift) & kCepMask) - 1 : p0;
+            const float xp0 = X[p0], xp1 = X[p1];
+            const float a0 = X[i0], u0 = U[i0], v0 = PV[i0];
+            const float a1 = has1 ? X[i1b] : 0.0f, u1 = has1 ? U[i1b] : 0.0f, v1 = has1 ? PV[i1b] : 0.0f;
+            X[i0] = (a0 - u0 * xp0) * v0;
+            if (has1) X[i1b] = (a1 - u1 * xp1) * v1;
         }
         __syncwarp();
     }

@@ -36,6 +36,7 @@ class CGradSpec(ctypes.Structure):
                 ("cell_ra_param", ctypes.c_void_p), ("cell_ra", ctypes.c_void_p),
                 ("n_rec", ctypes.c_int32), ("rec_comp", ctypes.c_void_p), ("n_steps", ctypes.c_int64),
                 ("checkpoint_every", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("syn_param", ctypes.c_void_p), ("timed_param", ctypes.c_void_p),
                 ("reserved", ctypes.c_int32 * 4)]
 
 
@@ -63,11 +64,33 @@ def _bind(lib):
 class ParamMap:
     """Which model quantities are parameters: chan_param[ch] (or -1) for each
     channel instance of the lowered model, cell_ra_param[c] (or -1) for each
-    physical cell, and the parameter values the model was lowered with."""
+    physical cell, syn_param[s] / timed_param[i] (or -1) for each connection
+    synapse and timed input (its weight), and the parameter values the model
+    was lowered with."""
     n_params: int
     chan_param: np.ndarray
     cell_ra_param: np.ndarray
     values: np.ndarray
+    syn_param: np.ndarray | None = None
+    timed_param: np.ndarray | None = None
+
+
+def with_weights(low: LoweredModel, pmap: ParamMap, synapses: bool = True, timed: bool = True) -> ParamMap:
+    """pmap extended by one parameter per connection synapse and per timed
+    input (their weights), numbered after pmap's."""
+    n = pmap.n_params
+    syn = np.full(len(low.syn_target), -1, np.int32)
+    tim = np.full(len(low.timed_target), -1, np.int32)
+    vals = [pmap.values]
+    if synapses and len(syn):
+        syn[:] = n + np.arange(len(syn))
+        n += len(syn)
+        vals.append(np.asarray(low.syn_weight, np.float32))
+    if timed and len(tim):
+        tim[:] = n + np.arange(len(tim))
+        n += len(tim)
+        vals.append(np.asarray(low.timed_weight, np.float32))
+    return ParamMap(n, pmap.chan_param, pmap.cell_ra_param, np.concatenate(vals).astype(np.float32), syn, tim)
 
 
 def per_cell_density_map(low: LoweredModel, densities: list[int], ra: bool = True) -> ParamMap:
@@ -113,10 +136,14 @@ class CableGradient:
         self._chan = np.ascontiguousarray(pmap.chan_param, np.int32)
         self._rap = np.ascontiguousarray(pmap.cell_ra_param, np.int32)
         self._ra = np.ascontiguousarray(low.phys_ra, np.float32)
+        self._sp = None if pmap.syn_param is None else np.ascontiguousarray(pmap.syn_param, np.int32)
+        self._tp = None if pmap.timed_param is None else np.ascontiguousarray(pmap.timed_param, np.int32)
         spec = CGradSpec(n_params=pmap.n_params, chan_param=self._chan.ctypes.data,
                          cell_ra_param=self._rap.ctypes.data, cell_ra=self._ra.ctypes.data,
                          n_rec=self.n_rec, rec_comp=self.rec_comp.ctypes.data, n_steps=self.n_steps,
-                         checkpoint_every=checkpoint_every, device=device)
+                         checkpoint_every=checkpoint_every, device=device,
+                         syn_param=None if self._sp is None or not len(self._sp) else self._sp.ctypes.data,
+                         timed_param=None if self._tp is None or not len(self._tp) else self._tp.ctypes.data)
         h = ctypes.c_void_p()
         rc = self.lib.edenGpuGradCreate(ctypes.byref(cm), ctypes.byref(spec), ctypes.byref(h))
         self.h = h

@@ -264,9 +264,18 @@ def _gid_to_pop(spec, gid):
 def ball_and_stick(n_inst: int = 256, n_dend: int = 50, length_ms: float = 200.0,
                    dt_ms: float = 0.025, seed: int = 1234, sigma: float = 0.3,
                    amp_na: float = 0.5, pulse_ms: float = 150.0,
-                   params: np.ndarray | None = None) -> NetworkSpec:
+                   params: np.ndarray | None = None, syn_drive: int = 0) -> NetworkSpec:
     """Per-instance parameters (7): soma gNa, gK, gL, dendrite gNa, gK, gL
-    (mS/cm2) and Ra (ohm*cm), lognormal around the HH defaults."""
+    (mS/cm2) and Ra (ohm*cm), lognormal around the HH defaults.
+
+    syn_drive > 0 adds synaptic drive whose events are fixed in advance, the
+    case for synaptic-weight gradients: four spikeArray sources (seeded
+    spike trains over the run) with syn_drive excitatory expTwoSynapse
+    connections per cell (0.5 / 5 ms, 2 nS, 0 mV; weights 0.5-1.5, delays
+    1-3 ms) onto random dendrite segments, and two inhibitory
+    timedSynapticInput expOneSynapse inputs per cell (5 ms, 3 nS, -80 mV;
+    weights 0.5-1.5) onto the soma.  They come from a second generator, so
+    the cells and their parameters are those of the network without drive."""
     rng = np.random.default_rng(seed)
     base = np.array([G_NA, G_K, G_L, G_NA, G_K, G_L, 150.0])
     if params is None:
@@ -293,6 +302,26 @@ def ball_and_stick(n_inst: int = 256, n_dend: int = 50, length_ms: float = 200.0
         spec.populations.append(Population(f"pop{i}", f"bs{i}", 1))
     spec.pulses.append(PulseInputs("*", np.arange(n_inst), np.zeros(n_inst, int), np.zeros(n_inst),
                                    np.full(n_inst, pulse_ms), np.full(n_inst, amp_na)))
+    if syn_drive:
+        r2 = np.random.default_rng(seed + 7)
+        spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=2.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+        spec.synapses.append(SynapseType("syn_i1", SYN_EXPONE, gbase=3.0, erev=-80.0, tau_decay=5.0))
+        n_arr = 4
+        for k in range(n_arr):
+            t = np.round(np.sort(r2.uniform(0.0, length_ms, size=max(3, int(length_ms / 5)))), 4)
+            spec.cells.append(SpikeArrayCell(f"sa{k}", t))
+            spec.populations.append(Population(f"psa{k}", f"sa{k}", 1))
+        post = np.repeat(np.arange(n_inst), syn_drive)
+        pre = n_inst + r2.integers(0, n_arr, size=post.size)
+        seg = r2.integers(1, n_seg, size=post.size)
+        spec.projections.append(_flat_projection(spec, "proj_drive", pre, post, "syn_e2",
+                                                 np.round(r2.uniform(0.5, 1.5, post.size), 4),
+                                                 _round_us(r2.uniform(1.0, 3.0, post.size)), post_seg=seg))
+        cells = np.repeat(np.arange(n_inst), 2)
+        times = [np.round(np.sort(r2.uniform(0.0, length_ms, size=max(2, int(length_ms / 10)))), 4)
+                 for _ in range(len(cells))]
+        spec.timed.append(TimedInputs("syn_i1", cells, np.zeros(len(cells), np.int64), times,
+                                      np.round(r2.uniform(0.5, 1.5, len(cells)), 4)))
     spec.trace_columns = [OutputColumn(f"pop{i}", 0, 0) for i in range(min(n_inst, 10))]
     spec.event_selections = [EventSelection(f"pop{i}", 0, 0) for i in range(n_inst)]
     spec.params = params

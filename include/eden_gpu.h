@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 6
+#define EDEN_GPU_ABI_VERSION 7
 
 enum {
     EDEN_GPU_OK = 0,
@@ -387,11 +387,16 @@ int edenGpuAbiVersion(void);
  * Gradients (no counterpart in the reference, which has no gradient path).
  *
  * For models of independent physical cells -- HH channels
- * (ionChannelHH/gateHHrates) and pulse inputs; no synapses, Poisson inputs
- * or point neurons -- the library runs the same step as edenGpuRun's plain
- * path (gates eden/Eden.cpp:5126-5259, channel currents 5805-5898, V
- * pre-update 6057-6107, Hines solve 6114-6225) with chosen channel
- * conductivities and cell axial resistivities taken from a parameter vector,
+ * (ionChannelHH/gateHHrates), pulse inputs, and synaptic drive whose events
+ * are fixed in advance: timedSynapticInput inputs and connection synapses
+ * from spike sources without a membrane (spike lists, generators, event-set
+ * readers); no Poisson inputs, no point neurons, no synapse from a cell that
+ * spikes -- the library runs the same step as edenGpuRun's plain
+ * path (gates eden/Eden.cpp:5126-5259, channel currents 5805-5898, synapses
+ * 3424-3466 and LEMS_CoreComponents.inc.xml:145-180 with the weight product
+ * of 3708-3710, V pre-update 6057-6107, Hines solve 6114-6225) with chosen
+ * channel conductivities, cell axial resistivities and synaptic weights
+ * taken from a parameter vector,
  * records the membrane potential of chosen compartments at the start of
  * steps 1..n_steps, and returns the gradient of any scalar function of that
  * trace with respect to the parameters, given the function's gradient with
@@ -415,6 +420,10 @@ typedef struct EdenGpuGradSpec {
     int64_t n_steps;               /* trace rows: steps 1..n_steps */
     int32_t checkpoint_every;      /* steps per recomputed segment; 0 = 100 */
     int32_t device;
+    const int32_t *syn_param;      /* [n_syn] parameter that is the connection's weight, or -1 to
+                                      keep syn_weight; may be null */
+    const int32_t *timed_param;    /* [n_timed] parameter that is the input's weight, or -1 to keep
+                                      timed_weight; may be null */
     int32_t reserved[4];
 } EdenGpuGradSpec;
 

@@ -19,12 +19,22 @@ over all compartments:
   diagonal, -dt/(R C_child) in the child's row and -dt/(R C_parent) in the
   parent's row.
 
+* synaptic drive with events fixed in advance (timedSynapticInput inputs
+  and connections from spike sources; their firing steps from the listed
+  steps and from the reference's single-pending-spike rule,
+  oracle/routing.py): each synapse's unit-weight exposure g^(n) -- expTwo
+  gbase (B - A), expOne G -- by forward Euler between events and the
+  event's jump instead of the decay in its step
+  (LEMS_CoreComponents.inc.xml:145-180, eden/Eden.cpp:3424-3466), times its
+  weight (3708-3710), adds g (E - V) and g to the compartment's I and G.
+
 A cell's axial resistances scale with its resistivity Ra, so every axial
 term is multiplied by s = Ra_lowered / Ra.
 
 Tangents (forward mode) go through the same phases for any set of
 directions in parameter space: dq' = dQ/dV dV + dQ/dq dq (0 where the gate
-clamped), dg = (dgbase fopen + gbase dfopen) 1e-5 A, dx = dV + dt dGE / C,
+clamped), dg = (dgbase fopen + gbase dfopen) 1e-5 A plus dw g^ for a weight,
+dx = dV + dt dGE / C,
 dV' = M^-1 (dx - dM V').  The trace is V at the start of steps 1..N of the
 recorded compartments; its derivative along a direction is returned per
 step, so any loss's directional derivative follows by the chain rule.
@@ -61,9 +71,13 @@ class Cable:
     """The cells of a lowered model (physical cells only), with a parameter
     map: chan_param[ch] / cell_ra_param[c] give the parameter index or -1."""
 
-    def __init__(self, low, chan_param, cell_ra_param=None, cell_ra=None):
-        if low.n_izh or len(low.syn_target) or len(low.pois_target):
-            raise ValueError("physical cells with HH channels and pulse inputs only")
+    def __init__(self, low, chan_param, cell_ra_param=None, cell_ra=None, syn_param=None, timed_param=None):
+        if low.n_izh or len(low.pois_target):
+            raise ValueError("physical cells with HH channels, pulse inputs and fixed synaptic drive only")
+        self.low = low
+        self.syn_param = np.full(len(low.syn_target), -1) if syn_param is None else np.asarray(syn_param, np.int64)
+        self.timed_param = (np.full(len(low.timed_target), -1) if timed_param is None
+                            else np.asarray(timed_param, np.int64))
         self.dt = float(low.dt)
         n = low.n_comp
         self.n = n
@@ -156,10 +170,52 @@ class Cable:
         dqdv = np.where(clamped, 0.0, db * (q - inf) + (1.0 - b) * dinf)
         return qn, dqdq, dqdv, inf
 
+    def drive(self, n_steps):
+        """The synaptic drive over steps 1..n_steps: (compartment, reversal
+        potential, weight parameter or -1, fixed weight) per item and its
+        unit-weight exposure [n_items, n_steps + 1] (column n = step n)."""
+        import routing
+        low = self.low
+        st = low.syn_types
+        items = []
+        for k in range(len(low.timed_target)):
+            ev = np.asarray(low.timed_step[low.timed_off[k]:low.timed_off[k + 1]], np.int64)
+            items.append((int(low.timed_target[k]), int(low.timed_type[k]), int(self.timed_param[k]),
+                          float(low.timed_weight[k]), set(ev.tolist())))
+        if len(low.syn_target):
+            if (np.asarray(low.src_target)[np.asarray(low.syn_src)] >= 0).any():
+                raise ValueError("a synapse's presynaptic cell spikes: its events are not fixed")
+            _, steps = routing.route_steps(low.syn_src, low.syn_delay, low.ext_src, low.ext_step, float(low.dt),
+                                           n_steps)
+            for k in range(len(low.syn_target)):
+                items.append((int(low.syn_target[k]), int(low.syn_type[k]), int(self.syn_param[k]),
+                              float(low.syn_weight[k]), set(steps[k].tolist())))
+        ghat = np.zeros((len(items), n_steps + 1))
+        meta = []
+        dt = self.dt
+        for i, (comp, ty, par, w, ev) in enumerate(items):
+            two = int(st["kind"][ty]) == 1
+            gb, td, tr = float(st["gbase"][ty]), float(st["tau_decay"][ty]), float(st["tau_rise"][ty])
+            wf = float(st["weight_prop"][ty]) * float(st["waveform_factor"][ty]) if two else 0.0
+            a = b = 0.0
+            for n in range(1, n_steps + 1):
+                ghat[i, n] = gb * (b - a) if two else a
+                if n in ev:
+                    a, b = (a + wf, b + wf) if two else (a + gb, b)
+                else:
+                    a, b = (a - dt * a / tr, b - dt * b / td) if two else (a - dt * a / td, b)
+            meta.append((comp, float(st["erev"][ty]), par, w))
+        return meta, ghat
+
     def run(self, params, n_steps, rec_comp, directions=None):
         """trace [N, n_rec] (float64) and, with directions [k, n_params], its
         derivatives [k, N, n_rec] along each direction."""
         params = np.asarray(params, np.float64)
+        meta, ghat = self.drive(n_steps)
+        d_comp = np.array([x[0] for x in meta], np.int64)
+        d_erev = np.array([x[1] for x in meta])
+        d_par = np.array([x[2] for x in meta], np.int64)
+        d_w = np.where(d_par >= 0, params[np.where(d_par >= 0, d_par, 0)], np.array([x[3] for x in meta]))
         D0 = np.zeros((0, len(params))) if directions is None else np.asarray(directions, np.float64)
         k = D0.shape[0]
         n, dt = self.n, self.dt
@@ -210,6 +266,14 @@ class Cable:
             dGE = np.stack([np.bincount(self.chan_comp, dgc[j] * self.erev, minlength=n) for j in range(k)]) if k else dV
             on = (self.ps <= t) & (t <= self.ps + self.pd)
             Iin = np.bincount(self.pt, np.where(on, self.paw, 0.0), minlength=n)
+            if len(meta):
+                gs = d_w * ghat[:, step]
+                G = G + np.bincount(d_comp, gs, minlength=n)
+                GE = GE + np.bincount(d_comp, gs * d_erev, minlength=n)
+                if k:
+                    dgs = np.where(d_par[None, :] >= 0, D0[:, np.where(d_par >= 0, d_par, 0)], 0.0) * ghat[:, step]
+                    dG = dG + np.stack([np.bincount(d_comp, dgs[j], minlength=n) for j in range(k)])
+                    dGE = dGE + np.stack([np.bincount(d_comp, dgs[j] * d_erev, minlength=n) for j in range(k)])
             I = GE - G * V + Iin
             d = G / self.C + irc
             x = V + dt * (I + V * G) / self.C

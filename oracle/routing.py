@@ -38,6 +38,13 @@ def route(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step):
     <= last_step, and how many steps each synapse fired in (steps 1..last_step).
 
     Returns (pending float32 [n_syn], fire_count int64 [n_syn])."""
+    pend, steps = route_steps(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step)
+    return pend, np.array([len(x) for x in steps], np.int64)
+
+
+def route_steps(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step):
+    """route(), with each synapse's firing steps (sorted) in place of the
+    count: returns (pending float32 [n_syn], list of int64 arrays)."""
     syn_src = np.asarray(syn_src)
     syn_delay = np.asarray(syn_delay, F32)
     times = step_times(dt_us, last_step + 1)
@@ -50,7 +57,7 @@ def route(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step):
             by_src[int(spike_src[i])].append(k)
     n = len(syn_src)
     pend = np.full(n, -np.inf, F32)
-    fires = np.zeros(n, np.int64)
+    steps_of = [np.zeros(0, np.int64) for _ in range(n)]
     t_end = times[1:last_step + 1]           # times of steps 1..last_step
     t_end_dt = (t_end + dt).astype(F32)
 
@@ -81,8 +88,8 @@ def route(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step):
                 if ks is not None:
                     fired.add(ks)
         pend[s] = p
-        fires[s] = len(fired)
-    return pend, fires
+        steps_of[s] = np.array(sorted(k for k in fired if k <= last_step), np.int64)
+    return pend, steps_of
 
 
 def route_pending(syn_src, syn_delay, spike_src, spike_step, dt_us, last_step):

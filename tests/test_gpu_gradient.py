@@ -10,7 +10,7 @@ from eden_gb300 import engine, lowering, workloads
 from eden_gb300.gradient import CableGradient, per_cell_density_map
 from oracle.cable_grad import Cable, loss_and_trace_grad
 
-from test_cable_grad_oracle import K, fd_grad_linear, per_cell_directions, small_ball_and_stick
+from test_cable_grad_oracle import K, driven_ball_and_stick, fd_grad_linear, per_cell_directions, small_ball_and_stick
 
 pytestmark = pytest.mark.gpu
 
@@ -140,7 +140,12 @@ def test_errors():
     pm = per_cell_density_map(low, [0], ra=False)
     with pytest.raises(engine.EdenGpuError) as e:
         CableGradient(low, pm)
-    assert e.value.code == -1 and "synapses" in str(e.value)
+    assert e.value.code == -1 and "Poisson" in str(e.value)
+    # synapses from cells that spike: their events depend on the parameters
+    low = lowering.lower(workloads.multicomp_net(n_cells=4, in_degree=2, length_ms=1.0, poisson_rate_hz=0.0))
+    with pytest.raises(engine.EdenGpuError) as e:
+        CableGradient(low, per_cell_density_map(low, [0], ra=False))
+    assert e.value.code == -1 and "fixed in advance" in str(e.value)
     _, low, pm, rec = _case(n_inst=2, n_dend=5, length_ms=2.0)
     g = CableGradient(low, pm, rec_comp=rec)
     try:
@@ -155,3 +160,65 @@ def test_errors():
         g.forward(pm.values)                                # still usable
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("amp_na", [-0.05, 0.5], ids=["subthreshold", "spiking"])
+def test_synaptic_weight_gradients(amp_na):
+    """Gradients with respect to every synaptic weight (spike-list expTwo
+    connections on the dendrite, timed expOne inputs on the soma) and the
+    seven per-cell parameters, against the FP64 forward sensitivities
+    contracted with the same trace gradient and against FP64 central
+    differences of the same linear functional: per parameter kind, relative
+    to that kind's largest gradient."""
+    _, low, pm = driven_ball_and_stick(n_inst=3, n_dend=10, length_ms=30.0, amp_na=amp_na)
+    rec = np.ascontiguousarray(low.phys_comp_off[:-1], np.int32)
+    cab = Cable(low, pm.chan_param, pm.cell_ra_param, low.phys_ra, pm.syn_param, pm.timed_param)
+    nw = len(pm.syn_param) + len(pm.timed_param)
+    wpar = np.concatenate([pm.syn_param, pm.timed_param])
+    dirs = np.zeros((K + nw, pm.n_params))
+    dirs[:K] = per_cell_directions(pm.n_params)
+    dirs[:K, -nw:] = 0.0
+    dirs[K + np.arange(nw), wpar] = 1.0
+    tr64, dtr = cab.run(pm.values, low.n_steps, rec, dirs)
+    g = CableGradient(low, pm, rec_comp=rec)
+    try:
+        tr = g.forward(pm.values)
+        np.testing.assert_allclose(tr, tr64, rtol=0, atol=0.05 if tr64.max() > 0 else 1e-3)
+        _, tg = loss_and_trace_grad(tr.astype(np.float64), _target(tr64))
+        grad = g.backward(tg)
+    finally:
+        g.close()
+    ref_cell = np.einsum("nc,jnc->cj", tg, dtr[:K])
+    _close_per_param(grad[:-nw].reshape(-1, K), ref_cell, GRAD_RTOL_TL)
+    ref_w = np.einsum("nc,jnc->j", tg, dtr[K:])
+    assert np.abs(ref_w).max() > 0.0
+    np.testing.assert_allclose(grad[wpar], ref_w, rtol=0, atol=GRAD_RTOL_TL * np.abs(ref_w).max())
+    h = 1e-4
+    fd = np.zeros(nw)
+    for j, p in enumerate(wpar):
+        up = pm.values.astype(np.float64).copy()
+        dn = up.copy()
+        up[p] += h
+        dn[p] -= h
+        fd[j] = ((cab.run(up, low.n_steps, rec)[0] - cab.run(dn, low.n_steps, rec)[0]) * tg).sum() / (2 * h)
+    np.testing.assert_allclose(grad[wpar], fd, rtol=0, atol=GRAD_RTOL_FD * np.abs(fd).max())
+
+
+def test_synaptic_drive_forward_matches_plain_simulation():
+    """The gradient path's forward with synaptic drive against the plain
+    simulation path on the same model: the same spikes and potentials to the
+    rounding of the synapses' event-driven sums."""
+    _, low, pm = driven_ball_and_stick(n_inst=4, n_dend=10, length_ms=40.0)
+    rec = np.ascontiguousarray(low.phys_comp_off[:-1], np.int32)
+    g = CableGradient(low, pm, rec_comp=rec)
+    try:
+        tr = g.forward(pm.values)
+    finally:
+        g.close()
+    sim = engine.Simulation(low, mode=engine.MODE_PLAIN, trace_target=rec)
+    try:
+        ref = sim.run()
+    finally:
+        sim.close()
+    assert tr.max() > 0.0
+    np.testing.assert_allclose(tr, ref.trace, rtol=0, atol=0.05)

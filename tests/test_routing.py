@@ -72,3 +72,19 @@ def test_oracle_routing_matches_reference_tables(variant):
     assert out["rc"] == 0
     assert np.array_equal(out["syn_final_pending"].view(np.uint32), fx.pending_after(fx.last_step).view(np.uint32))
     assert np.array_equal(out["syn_fire_count"], fx.fire_count_through(fx.last_step))
+
+
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_firing_steps_match_reference_tables(variant):
+    """Every synapse fires in the same steps as in the reference's tables
+    (the steps its conductance jumps instead of decaying)."""
+    low = lowering.lower(workloads.routing_probe(length_ms=LENGTH_MS, **VARIANTS[variant]))
+    fx = routing_fixture(variant, len(low.syn_src))
+    _, steps = routing.route_steps(low.syn_src, low.syn_delay, low.ext_src, low.ext_step, float(low.dt),
+                                   fx.last_step)
+    order = np.lexsort((fx.fire_step, fx.fire_syn))
+    ref_syn, ref_step = fx.fire_syn[order], fx.fire_step[order]
+    mine_syn = np.concatenate([np.full(len(x), s) for s, x in enumerate(steps)])
+    mine_step = np.concatenate(steps)
+    np.testing.assert_array_equal(mine_syn, ref_syn)
+    np.testing.assert_array_equal(mine_step, ref_step)
