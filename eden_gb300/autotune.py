@@ -47,7 +47,7 @@ def candidates(low) -> dict:
     if low.n_comp == 0:
         return {"segments_per_depth": [0], "segments_per_warp": [0], "steps_per_launch": steps}
     return {"segments_per_depth": [0, 32, 128],
-            "segments_per_warp": [0, 384, 192, 1023],
+            "segments_per_warp": [0, 512, 384, 256, 192, 64, 1023],
             "steps_per_launch": steps}
 
 

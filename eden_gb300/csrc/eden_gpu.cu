@@ -493,7 +493,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             }
         const int64_t units = 4 * (int64_t)std::max(ctx->n_sm, 1);
         const int64_t even = (n_phys_comp + units - 1) / units;
-        forest_node_cap = (int)std::min<int64_t>(kForestNodes, std::max<int64_t>({even, (int64_t)largest, 32}));
+        forest_node_cap = (int)std::min<int64_t>(kForestNodes, std::max<int64_t>({even, (int64_t)largest, 8}));
     }
     std::vector<int32_t> u2i(nt, -1), i2u(nt, -1);
     std::vector<int32_t> c_parent(nt, -1), c_child0(nt, 0), c_nchild(nt, 0), t_izh(nt, -1);
@@ -1069,29 +1069,82 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         }
     }
     phase("packing");
-    // CTAs of up to four units, packed longest-first onto the CTA with the
-    // fewest words so that every CTA needs about the same shared memory
+    // CTAs of up to four units.  Every CTA of one window's launch is resident
+    // at once when the CTA count is a multiple of the SM count and the
+    // shared memory of that many CTAs fits an SM: each SM then runs the same
+    // number of CTAs, and an SM's time is the sum of its units' work.  So
+    // the units are spread longest-first, by an estimate of their per-step
+    // work, onto the CTA with the least work that still has room -- a free
+    // warp and shared memory under the cap -- so that the CTAs' work, and
+    // with it the SMs', is even.
     const int upc = kCellThreads / 32;
-    const int n_cta = (n_unit + upc - 1) / upc;
+    std::vector<double> un_cost(n_unit, 0.0);
+    for (int u = 0; u < n_unit; u++) {
+        if (un_f[u] < 0) {
+            un_cost[u] = 4.0;  // a batch of point neurons: one pass per step
+            continue;
+        }
+        // the cable solve's depth passes (two per depth) and its iterations
+        // (one per 32 compartments of a depth), the non-flat compartments'
+        // currents and the gates, in units of one solve iteration
+        const int f = un_f[u], nl = fo_nlev[f];
+        double iters = 0.0;
+        for (int l = 0; l < nl; l++) iters += std::ceil((lvl[fo_l0[f] + l + 1] - lvl[fo_l0[f] + l]) / 32.0);
+        const int nf = un_nf1[u] - un_nf0[u];
+        un_cost[u] = 2.0 * iters + nl + 8.0 * std::ceil(nf / 32.0) + 3.0 * std::ceil(un_ngt[u] / 32.0);
+    }
+    int max_words = 1;
+    for (int u = 0; u < n_unit; u++) max_words = std::max(max_words, un_words[u]);
+    const int min_cta = (n_unit + upc - 1) / upc;
+    const int nsm = std::max(ctx->n_sm, 1);
+    const int per_sm = (min_cta + nsm - 1) / nsm;
+    const int n_cta = std::max(1, std::min(n_unit, per_sm * nsm));
+    // shared memory cap per CTA: an SM's share for per_sm CTAs, but never
+    // less than the largest unit or the words-balanced average
+    int64_t words_total = 0;
+    for (int u = 0; u < n_unit; u++) words_total += un_words[u];
+    const int share = (int)(ctx->smem_per_sm / (int)sizeof(float) / std::max(per_sm, 1)) - 256;
+    const int word_cap = std::max({max_words, share, (int)((words_total + n_cta - 1) / n_cta) + max_words});
     std::vector<int> uorder(n_unit);
     std::iota(uorder.begin(), uorder.end(), 0);
-    std::stable_sort(uorder.begin(), uorder.end(), [&](int x, int y) { return un_words[x] > un_words[y]; });
+    std::stable_sort(uorder.begin(), uorder.end(), [&](int x, int y) {
+        return un_cost[x] != un_cost[y] ? un_cost[x] > un_cost[y] : un_words[x] > un_words[y];
+    });
     std::vector<std::vector<int>> cta_units(n_cta);
     std::vector<int> cta_words(n_cta, 0);
     {
-        // min-heap of (words, cta) over CTAs that still have room
-        std::vector<std::pair<int, int>> heap;
-        for (int c = 0; c < n_cta; c++) heap.push_back({0, c});
-        auto cmp = [](const std::pair<int, int> &x, const std::pair<int, int> &y) { return x > y; };
+        // min-heap of (work, cta) over CTAs that still have a free warp
+        std::vector<double> cta_cost(n_cta, 0.0);
+        std::vector<std::pair<double, int>> heap;
+        for (int c = 0; c < n_cta; c++) heap.push_back({0.0, c});
+        auto cmp = [](const std::pair<double, int> &x, const std::pair<double, int> &y) { return x > y; };
         std::make_heap(heap.begin(), heap.end(), cmp);
+        std::vector<std::pair<double, int>> skipped;
         for (int uu : uorder) {
-            std::pop_heap(heap.begin(), heap.end(), cmp);
-            auto top = heap.back();
-            heap.pop_back();
-            cta_units[top.second].push_back(uu);
-            cta_words[top.second] += un_words[uu];
-            if ((int)cta_units[top.second].size() < upc) {
-                heap.push_back({cta_words[top.second], top.second});
+            // the least-loaded CTA whose shared memory takes the unit (else the
+            // least-loaded one with a free warp)
+            int pick = -1;
+            skipped.clear();
+            while (!heap.empty()) {
+                std::pop_heap(heap.begin(), heap.end(), cmp);
+                auto top = heap.back();
+                heap.pop_back();
+                if (cta_words[top.second] + un_words[uu] <= word_cap) { pick = top.second; break; }
+                skipped.push_back(top);
+            }
+            if (pick < 0) {
+                pick = skipped.front().second;
+                skipped.erase(skipped.begin());
+            }
+            for (auto &sk : skipped) {
+                heap.push_back(sk);
+                std::push_heap(heap.begin(), heap.end(), cmp);
+            }
+            cta_units[pick].push_back(uu);
+            cta_words[pick] += un_words[uu];
+            cta_cost[pick] += un_cost[uu];
+            if ((int)cta_units[pick].size() < upc) {
+                heap.push_back({cta_cost[pick], pick});
                 std::push_heap(heap.begin(), heap.end(), cmp);
             }
         }
@@ -1214,10 +1267,12 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (int b = 0; b < 2; b++) {
         TRY(upload(ctx, &d.wspk_src[b], (const int32_t *)nullptr, wcap));
         TRY(upload(ctx, &d.wspk_step[b], (const int32_t *)nullptr, wcap));
+        TRY(upload(ctx, &d.wspk_time[b], (const double *)nullptr, wcap));
     }
     TRY(upload(ctx, &d.wspk_count, (const int32_t *)nullptr, 2));
     TRY(upload(ctx, &d.log_src, (const int32_t *)nullptr, (size_t)log_cap));
     TRY(upload(ctx, &d.log_step, (const int64_t *)nullptr, (size_t)log_cap));
+    TRY(upload(ctx, &d.log_time, (const double *)nullptr, (size_t)log_cap));
     TRY(upload(ctx, &d.log_count, (const unsigned long long *)nullptr, 1));
     d.log_cap = log_cap;
     TRY(upload_c(ctx, &d.t_trace0, t_trace0)); TRY(upload_c(ctx, &d.trace_col, trace_col));
@@ -1457,6 +1512,7 @@ static int ensure_wtab(EdenGpuCtx *ctx, int64_t n) {
 // the host clock advanced past it; the previous window's times are kept for
 // the trigger replay.
 static void fill_window(EdenGpuCtx *ctx, WindowArgs &w, WindowTimes &tt, int64_t s, int K) {
+    w.t0 = ctx->time;
     w.step0 = s;
     w.K = K;
     w.Kprev = ctx->Kprev;
@@ -1726,6 +1782,8 @@ extern "C" int edenGpuFetchRecords(EdenGpuCtx *ctx, EdenGpuRecords *rec) {
     if (ns > 0) {
         CUDA_TRY(ctx, cudaMemcpy(rec->spike_src, ctx->d.log_src, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost));
         CUDA_TRY(ctx, cudaMemcpy(rec->spike_step, ctx->d.log_step, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost));
+        if (rec->spike_time_us)
+            CUDA_TRY(ctx, cudaMemcpy(rec->spike_time_us, ctx->d.log_time, sizeof(double) * ns, cudaMemcpyDeviceToHost));
     }
     rec->n_spikes = ns;
     CUDA_TRY(ctx, cudaMemset(ctx->d.log_count, 0, sizeof(unsigned long long)));

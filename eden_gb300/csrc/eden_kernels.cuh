@@ -175,12 +175,17 @@ struct DevModel {
     const int32_t *fan_syn;
     // spikes of the sources with no target, in step order: source, logging step
     const int32_t *ext_src, *ext_step;
-    // window spike lists (double-buffered by window parity) and the spike log
+    // window spike lists (double-buffered by window parity) and the spike log;
+    // *_time: the threshold-crossing time (us) interpolated in double
+    // between the step's starting and final potential (NaN where there is
+    // none: point neurons and sources with no membrane)
     int32_t *wspk_src[2];
     int32_t *wspk_step[2];
+    double *wspk_time[2];
     int32_t *wspk_count;  // [2]
     int32_t *log_src;
     int64_t *log_step;
+    double *log_time;
     unsigned long long *log_count;
     int64_t log_cap;
     // trajectory recording: CSR target -> recorded columns
@@ -243,6 +248,7 @@ __host__ __device__ inline int izh_words(int n) { return (2 + EDEN_POINT_PARAMS 
 // step0 - Kprev; its triggers are the mask bits 1..Kprev-1 (replayed before
 // step0) and bit Kprev (the trigger of step0 itself).
 struct WindowArgs {
+    double t0;     // simulation time of step0 (us), accumulated in double on the host
     int64_t step0;
     int32_t K, Kprev;
     int32_t par;   // which V buffer holds the state at step0
@@ -267,8 +273,11 @@ __device__ __forceinline__ float warp_sum(float x) {
 // ---------------------------------------------------------------------------
 // spike compaction: warp ballot, one atomic per warp
 // ---------------------------------------------------------------------------
+// NaN: a spike with no interpolated crossing time
+__device__ __forceinline__ double no_time() { return __longlong_as_double(0x7ff8000000000000ll); }
+
 __device__ __forceinline__ void push_spike(const DevModel &m, bool spiked, int32_t src, int32_t log_step,
-                                           int wpar) {
+                                           int wpar, double tcross) {
     unsigned active = __activemask();
     unsigned ballot = __ballot_sync(active, spiked);
     if (ballot == 0) return;
@@ -281,7 +290,16 @@ __device__ __forceinline__ void push_spike(const DevModel &m, bool spiked, int32
         int rank = __popc(ballot & ((1u << lane) - 1));
         m.wspk_src[wpar][base + rank] = src;
         m.wspk_step[wpar][base + rank] = log_step;
+        m.wspk_time[wpar][base + rank] = tcross;
     }
+}
+
+// The time (us) at which V crossed thr during a step that starts at time t
+// (double) with potential v0 and ends with v1 (v0 < thr < v1), by linear
+// interpolation in double.  A diagnostic beside the logged step: the
+// reference quantises spike times to the step (eden/Eden.cpp:6247-6252).
+__device__ __forceinline__ double crossing_time(double t, float dt, float v0, float v1, float thr) {
+    return t + (double)dt * (((double)thr - (double)v0) / ((double)v1 - (double)v0));
 }
 
 // ---------------------------------------------------------------------------
@@ -951,7 +969,7 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
         m.iz_u[iz] = u;
         m.iz_s[iz] = sv;
         int src = m.t_src[t];
-        push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), wpar);
+        push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), wpar, no_time());
     }
 }
 
@@ -970,10 +988,10 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
 // pivot.  Back-substitution then runs root-first.  When check_spikes is set
 // it ends with the threshold test V < thr < V_next of the forest's spike
 // sources (eden/Eden.cpp:6247-6252).
-__device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64_t step, float *D, float *X,
-                                             const float *U, const float *L, const int32_t *CE, const int32_t *P,
-                                             const int32_t *LV, int nlev, const float *Vin, int base, int wpar,
-                                             bool check_spikes) {
+__device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64_t step, double tstep, float *D,
+                                             float *X, const float *U, const float *L, const int32_t *CE,
+                                             const int32_t *P, const int32_t *LV, int nlev, const float *Vin, int base,
+                                             int wpar, bool check_spikes) {
     const int lane = threadIdx.x & 31;
     const int c0 = LV[0], c1 = LV[nlev];
     if (!init && c1 > c0) {
@@ -1011,14 +1029,16 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
         const int c = c0w + lane;
         bool spk = false;
         int src = -1;
+        double tc = 0.0;
         if (c < c1) {
             src = m.t_src[c + base];
             if (src >= 0) {
                 const float thr = m.src_thr[src];
                 spk = (Vin[c] < thr && thr < X[c]);
+                if (spk) tc = crossing_time(tstep, m.dt, Vin[c], X[c], thr);
             }
         }
-        push_spike(m, spk, src, (int32_t)(step + 1), wpar);
+        push_spike(m, spk, src, (int32_t)(step + 1), wpar, tc);
     }
 }
 
@@ -1031,54 +1051,11 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
 // G/C + sum 1/(RC) on entry, X its pre-updated V) and its children's
 // factors, in increasing child order as the reference's post-order visits
 // them.  A depth's compartments are spread over the lanes (at most 64 per
-// depth, two per lane, unless a single cell is wider); LV packs each
-// depth's first compartment and whether it holds a non-flat one.
+// depth, two per lane, unless a single cell is wider); LV packs each depth's first
+// compartment and whether it holds a non-flat one.
 // Back-substitution runs root-first.  X holds V_next on return.
-//
-// The step's critical path is the chain of dependent shared-memory loads,
-// so each lane loads everything its (up to two) compartments of a depth
-// need -- descriptors, values, and the first kPull children's factors and
-// eliminated values -- before it runs their subtraction chains, which keep
-// the reference's order: a compartment subtracts its children's terms one
-// by one in increasing child order.
 constexpr int32_t kLvMask = 0xffff;
 constexpr int32_t kLvNonFlat = 1 << 16;
-constexpr int kPull = 4;  // children whose terms are loaded up front
-
-// The children [kb, ke) of one compartment: their elimination factors and
-// eliminated values (and, for a non-flat parent, their U), loaded together.
-struct Pull {
-    float r[kPull], x[kPull], u[kPull];
-};
-__device__ __forceinline__ void pull_load(Pull &p, const float *RT, const float *X, const float *U, int kb, int ke,
-                                          bool with_u) {
-#pragma unroll
-    for (int q = 0; q < kPull; q++) {
-        const bool on = kb + q < ke;
-        p.r[q] = on ? RT[kb + q] : 0.0f;
-        p.x[q] = on ? X[kb + q] : 0.0f;
-        p.u[q] = (on && with_u) ? U[kb + q] : 0.0f;
-    }
-}
-
-// Eliminate one compartment's children from its right-hand side xj (and,
-// non-flat, from its diagonal dj), in child order.
-__device__ __forceinline__ void pull_apply(const Pull &p, const float *RT, const float *X, const float *U, int kb,
-                                           int ke, bool nonflat, float &xj, float &dj) {
-#pragma unroll
-    for (int q = 0; q < kPull; q++) {
-        if (kb + q < ke) {
-            if (nonflat) dj -= p.r[q] * p.u[q];
-            xj -= p.r[q] * p.x[q];
-        }
-    }
-    for (int i = kb + kPull; i < ke; i++) {
-        const float r = RT[i];
-        if (nonflat) dj -= r * U[i];
-        xj -= r * X[i];
-    }
-}
-
 __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC, const float *L, float *PV,
                                              float *RT, const float *U, const uint32_t *CEP, const int32_t *LV,
                                              int nlev) {
@@ -1086,55 +1063,41 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
     int end = LV[nlev] & kLvMask;
     for (int lev = nlev - 1; lev >= 0; lev--) {
         const int32_t lw = LV[lev];
-        const int beg = lw & kLvMask;
-        const bool lvl_nf = (lw & kLvNonFlat) != 0;
         // a depth holds at most 64 compartments unless one cell alone is wider
-        for (int j0 = beg + lane; j0 < end; j0 += 64) {
-            const int j1 = j0 + 32;
-            const bool has1 = j1 < end;
-            const uint32_t cep0 = CEP[j0], cep1 = has1 ? CEP[j1] : 0u;
-            const int ke0 = (int)(cep0 & kCepMask), kb0 = (int)((cep0 >> kCepBeginShift) & kCepMask);
-            const int ke1 = (int)(cep1 & kCepMask), kb1 = (int)((cep1 >> kCepBeginShift) & kCepMask);
-            const bool nf0 = lvl_nf && (cep0 & kCepNonFlat), nf1 = lvl_nf && (cep1 & kCepNonFlat);
-            float x0 = X[j0] + KC[j0];
-            float x1 = has1 ? X[j1] + KC[j1] : 0.0f;
-            float d0 = nf0 ? 1.0f + PV[j0] * dt : 0.0f;
-            float d1 = nf1 ? 1.0f + PV[j1] * dt : 0.0f;
-            Pull p0, p1;
-            pull_load(p0, RT, X, U, kb0, ke0, nf0);
-            pull_load(p1, RT, X, U, kb1, ke1, nf1);
-            pull_apply(p0, RT, X, U, kb0, ke0, nf0, x0, d0);
-            pull_apply(p1, RT, X, U, kb1, ke1, nf1, x1, d1);
-            if (nf0) {
-                const float inv = __fdividef(1.0f, d0);
-                PV[j0] = inv;
-                RT[j0] = L[j0] * inv;
+        for (int j = (lw & kLvMask) + lane; j < end; j += 32) {
+            const uint32_t cep = CEP[j];
+            const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
+            float xj = X[j] + KC[j];
+            if ((lw & kLvNonFlat) && (cep & kCepNonFlat)) {
+                float dj = 1.0f + PV[j] * dt;
+                for (int i = kb; i < ke; i++) {
+                    const float r = RT[i];
+                    dj -= r * U[i];
+                    xj -= r * X[i];
+                }
+                const float inv = __fdividef(1.0f, dj);
+                PV[j] = inv;
+                RT[j] = L[j] * inv;
+            } else {
+                // most compartments have at most two children: take those
+                // without a loop, in order
+                int i = kb;
+                if (i < ke) xj -= RT[i] * X[i];
+                if (i + 1 < ke) xj -= RT[i + 1] * X[i + 1];
+                for (i = kb + 2; i < ke; i++) xj -= RT[i] * X[i];
             }
-            if (nf1) {
-                const float inv = __fdividef(1.0f, d1);
-                PV[j1] = inv;
-                RT[j1] = L[j1] * inv;
-            }
-            X[j0] = x0;
-            if (has1) X[j1] = x1;
+            X[j] = xj;
         }
-        end = beg;
+        end = lw & kLvMask;
         __syncwarp();
     }
     for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) X[r] = X[r] * PV[r];
     __syncwarp();
     for (int lev = 1; lev < nlev; lev++) {
         const int i1 = LV[lev + 1] & kLvMask;
-        for (int i0 = (LV[lev] & kLvMask) + lane; i0 < i1; i0 += 64) {
-            const int i1b = i0 + 32;
-            const bool has1 = i1b < i1;
-            const int p0 = (int)((CEP[i0] >> kCepParentShift) & kCepMask) - 1;
-            const int p1 = has1 ? (int)((CEP[i1b] >> kCepParentShift) & kCepMask) - 1 : p0;
-            const float xp0 = X[p0], xp1 = X[p1];
-            const float a0 = X[i0], u0 = U[i0], v0 = PV[i0];
-            const float a1 = has1 ? X[i1b] : 0.0f, u1 = has1 ? U[i1b] : 0.0f, v1 = has1 ? PV[i1b] : 0.0f;
-            X[i0] = (a0 - u0 * xp0) * v0;
-            if (has1) X[i1b] = (a1 - u1 * xp1) * v1;
+        for (int i = (LV[lev] & kLvMask) + lane; i < i1; i += 32) {
+            const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
+            X[i] = (X[i] - U[i] * X[p]) * PV[i];
         }
         __syncwarp();
     }

@@ -95,12 +95,13 @@ __global__ void __launch_bounds__(kHinesThreads) k_hines_t(DevModel m, const Win
             }
             for (int i = lane; i <= nlev; i += 32) sLV[i] = lv[i] - c0;
             __syncwarp();
-            hines_forest(m, init, w.step0, sD, sX, sU, sL, sCE, sP, sLV, nlev, sV, c0, w.wpar, true);
+            hines_forest(m, init, w.step0, w.t0, sD, sX, sU, sL, sCE, sP, sLV, nlev, sV, c0, w.wpar, true);
             __syncwarp();
             for (int i = lane; i < n; i += 32) x[c0 + i] = sX[i];
             __syncwarp();
         } else {
-            hines_forest(m, init, w.step0, m.diag, x, m.c_u, m.c_l, m.c_cend, m.c_parent, lv, nlev, vin, 0, w.wpar, true);
+            hines_forest(m, init, w.step0, w.t0, m.diag, x, m.c_u, m.c_l, m.c_cend, m.c_parent, lv, nlev, vin, 0, w.wpar,
+                         true);
         }
     }
 }
@@ -125,6 +126,7 @@ __global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs 
         const bool own = e < n;
         int src = own ? m.wspk_src[wp][e] : m.ext_src[w.ext0 + e - n];
         int log_step = own ? m.wspk_step[wp][e] : m.ext_step[w.ext0 + e - n];
+        const double tcross = own ? m.wspk_time[wp][e] : no_time();
         uint32_t bit = 1u << (uint32_t)(log_step - w.step0);
         int64_t f0 = m.fan0[src], f1 = m.fan0[src + 1];
         for (int64_t f = f0 + lane; f < f1; f += 32) atomicOr(&m.sy_mask[m.fan_syn[f]], bit);
@@ -133,6 +135,7 @@ __global__ void __launch_bounds__(256) k_deliver_t(DevModel m, const WindowArgs 
             if ((int64_t)slot < m.log_cap) {
                 m.log_src[slot] = src;
                 m.log_step[slot] = log_step;
+                m.log_time[slot] = tcross;
             } else {
                 atomicOr(m.status, ST_LOG_OVERFLOW);
             }
@@ -231,6 +234,7 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
         for (int c = lane; c < nck; c += 32) GS[k * nck + c] = m.Gp[(size_t)k * m.n_chunk + uc0 + c];
     __syncwarp();
     const float dt = m.dt;
+    double tstep = w.t0;  // this step's time, accumulated in double as the host does
     for (int k = 0; k < w.K; k++) {
         const int64_t step = w.step0 + k;
         const bool init = step <= 0;
@@ -285,14 +289,18 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             const int q = q0 + lane;
             bool spk = false;
             int src = -1;
+            double tc = 0.0;
             if (q < ns) {
                 const int sl = ST[q];
                 src = SSRC[q];
-                spk = VO[sl] < STHR[q] && STHR[q] < X[NT[sl]];
+                const float vo = VO[sl], vn = X[NT[sl]];
+                spk = vo < STHR[q] && STHR[q] < vn;
+                if (spk) tc = crossing_time(tstep, dt, vo, vn, STHR[q]);
             }
-            push_spike(m, spk, src, (int32_t)(step + 1), w.wpar);
+            push_spike(m, spk, src, (int32_t)(step + 1), w.wpar, tc);
         }
         __syncwarp();
+        if (!init) tstep += (double)dt;
     }
     // ---- write the unit back into the buffer that holds the window's final state
     float *vdst = m.v[w.par ^ (w.K & 1)];
@@ -344,7 +352,7 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
             SS[i] = ss;
             src = m.t_src[t];
         }
-        push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar);
+        push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar, no_time());
         if (!init) {
             const int64_t row = (step - 1) % m.trace_cap;
             for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = vin[m.gr_t[q]];

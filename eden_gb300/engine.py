@@ -44,7 +44,8 @@ class CRecords(ctypes.Structure):
     _fields_ = [("trace", ctypes.POINTER(ctypes.c_float)), ("trace_step", ctypes.POINTER(ctypes.c_int64)),
                 ("trace_capacity", ctypes.c_int64), ("spike_src", ctypes.POINTER(ctypes.c_int32)),
                 ("spike_step", ctypes.POINTER(ctypes.c_int64)), ("spike_capacity", ctypes.c_int64),
-                ("n_trace_samples", ctypes.c_int64), ("n_spikes", ctypes.c_int64)]
+                ("n_trace_samples", ctypes.c_int64), ("n_spikes", ctypes.c_int64),
+                ("spike_time_us", ctypes.POINTER(ctypes.c_double))]
 
 
 EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuRunStaticScratch", "edenGpuFetchRecords", "edenGpuGeneratedSource", "edenGpuReadV", "edenGpuWriteV",
@@ -106,6 +107,7 @@ class Records:
     trace_step: np.ndarray   # [n_samples] step index of each sample
     spike_src: np.ndarray    # [n_spikes] spike source (gid)
     spike_step: np.ndarray   # [n_spikes] logging step (the step after the crossing)
+    spike_time: np.ndarray | None = None  # [n_spikes] crossing time in us interpolated in double (NaN: none)
 
 
 class Simulation:
@@ -197,6 +199,7 @@ class Simulation:
         tstep = np.zeros(cap, np.int64)
         ssrc = np.zeros(self.spike_capacity, np.int32)
         sstep = np.zeros(self.spike_capacity, np.int64)
+        stime = np.zeros(self.spike_capacity, np.float64)
         rec = CRecords()
         rec.trace = trace.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
         rec.trace_step = tstep.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
@@ -204,11 +207,12 @@ class Simulation:
         rec.spike_src = ssrc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
         rec.spike_step = sstep.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
         rec.spike_capacity = self.spike_capacity
+        rec.spike_time_us = stime.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         self._check(self.lib.edenGpuFetchRecords(self.ctx, ctypes.byref(rec)))
         n, m = int(rec.n_trace_samples), int(rec.n_spikes)
         order = np.lexsort((ssrc[:m], sstep[:m]))
         return Records(trace[:n, :len(self.trace_target)].copy(), tstep[:n].copy(),
-                       ssrc[:m][order].copy(), sstep[:m][order].copy())
+                       ssrc[:m][order].copy(), sstep[:m][order].copy(), stime[:m][order].copy())
 
     def run(self, n_steps: int | None = None, chunk: int | None = None) -> Records:
         """Initialise, then run n_steps non-initialisation steps (default: the
@@ -230,10 +234,11 @@ class Simulation:
         rec = Records(np.concatenate([p.trace for p in parts]) if parts else np.zeros((0, len(self.trace_target)), np.float32),
                       np.concatenate([p.trace_step for p in parts]) if parts else np.zeros(0, np.int64),
                       np.concatenate([p.spike_src for p in parts]) if parts else np.zeros(0, np.int32),
-                      np.concatenate([p.spike_step for p in parts]) if parts else np.zeros(0, np.int64))
+                      np.concatenate([p.spike_step for p in parts]) if parts else np.zeros(0, np.int64),
+                      np.concatenate([p.spike_time for p in parts]) if parts else np.zeros(0, np.float64))
         # a spike in the final step would be logged at a step that never runs
         keep = rec.spike_step <= self.next_step - 1
-        rec.spike_src, rec.spike_step = rec.spike_src[keep], rec.spike_step[keep]
+        rec.spike_src, rec.spike_step, rec.spike_time = rec.spike_src[keep], rec.spike_step[keep], rec.spike_time[keep]
         return rec
 
     def kernel_stats(self) -> dict:

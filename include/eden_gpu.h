@@ -307,6 +307,13 @@ typedef struct EdenGpuRecords {
     /* filled in */
     int64_t n_trace_samples;
     int64_t n_spikes;
+    /* optional (NULL: not copied), [spike_capacity]: each spike's
+     * threshold-crossing time in us, interpolated in double between the
+     * potential at the start and at the end of the step that crossed
+     * (NaN for point neurons and sources with no membrane).  A diagnostic
+     * beside spike_step, which stays the reference's quantised time
+     * (eden/Eden.cpp:6247-6252). */
+    double *spike_time_us;
 } EdenGpuRecords;
 
 typedef struct EdenGpuCtx EdenGpuCtx;

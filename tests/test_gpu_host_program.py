@@ -61,7 +61,7 @@ def test_host_program_matches_reference_outputs(name, mode, tmp_path):
 def test_host_program_writes_what_the_python_front_end_writes(mode, tmp_path):
     spec, low, traj, ev = _run_host("izh_net", mode, tmp_path, chunk=333)
     sim = Simulation(low, mode=MODE_BATCHED if mode == "batched" else MODE_PLAIN)
-    rec = sim.run()
+    rec = sim.run(chunk=333)  # the same calls: each edenGpuRun starts its own windows
     sim.close()
     out = tmp_path / "py"
     out.mkdir()

@@ -69,3 +69,53 @@ def test_full_length_multicomp_against_gpu_double_oracle():
     bad, worst = compare_spikes(f64["spike_src"][fa], f64["spike_step"][fa], rec.spike_src[fb], rec.spike_step[fb],
                                 shift)
     assert bad == 0 and worst <= shift
+
+
+# Interpolated crossing times: the FP32 oracle's differ from the FP64
+# oracle's by at most 1.3 us on these cases; the GPU's are held to 5 us.
+CROSSING_ATOL_US = 5.0
+
+
+def _fp64_crossings(low, trace, srcs):
+    """(source, logging step) -> crossing time (us) from the FP64 trace of
+    each source's compartment, interpolated linearly within the step."""
+    dt = float(low.dt)
+    out = {}
+    for j, s in enumerate(srcs):
+        v = trace[:, j].astype(np.float64)
+        th = float(low.src_threshold[s])
+        n = np.flatnonzero((v[:-1] < th) & (th < v[1:]))  # trace row n is the start of step n + 1
+        t = n * dt + dt * (th - v[n]) / (v[n + 1] - v[n])
+        for k, tc in zip(n, t):
+            out[(int(s), int(k) + 2)] = tc
+    return out
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+@pytest.mark.parametrize("name", ["single_comp_hh", "multicomp_poisson", "ball_and_stick", "gate_kinds",
+                                  "spike_sources"])
+def test_interpolated_crossing_times_against_double(name, mode):
+    """Each spike of a physical cell carries its threshold-crossing time,
+    interpolated in double between the step's starting and final potential;
+    it lies within CROSSING_ATOL_US of the same interpolation on the FP64
+    oracle's trace, inside its logged step.  Point neurons and sources with
+    no membrane carry NaN."""
+    low = lowering.lower(spec_of(name))
+    srcs = np.flatnonzero((low.src_target >= 0) & (low.src_target < low.n_comp))
+    f64 = eden_port.run(low, trace_target=low.src_target[srcs].astype(np.int32), double=True)
+    ref = _fp64_crossings(low, f64["trace"], srcs)
+    sim = Simulation(low, mode=mode)
+    rec = sim.run()
+    sim.close()
+    phys = np.isin(rec.spike_src, srcs)
+    assert np.isnan(rec.spike_time[~phys]).all()
+    assert np.isfinite(rec.spike_time[phys]).all() and phys.any()
+    dt = float(low.dt)
+    matched = 0
+    for s, k, tc in zip(rec.spike_src[phys], rec.spike_step[phys], rec.spike_time[phys]):
+        # inside the step that crossed (logged one step later)
+        assert (k - 2) * dt - 1e-6 <= tc <= (k - 1) * dt + 1e-6
+        if (int(s), int(k)) in ref:
+            assert abs(tc - ref[(int(s), int(k))]) <= CROSSING_ATOL_US
+            matched += 1
+    assert matched >= 0.9 * phys.sum()
