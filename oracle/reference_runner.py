@@ -20,15 +20,25 @@ def available() -> bool:
     return os.path.exists(EDEN)
 
 
-# the reference source tree (as oracle/Makefile's REF); its validation
-# networks are read from there when it is present
-REF = os.environ.get("EDEN_REFERENCE_TREE", "/root/reference")
+def reference_tree():
+    """The reference source tree: EDEN_REFERENCE_DIR, else the tree
+    oracle/_ref was built from (oracle/Makefile records it), else None."""
+    env = os.environ.get("EDEN_REFERENCE_DIR")
+    if env:
+        return env
+    src = os.path.join(HERE, "_ref", "SOURCE")
+    if os.path.exists(src):
+        return open(src).read().strip() or None
+    return None
 
 
 def validation_network(name: str):
     """Path of one of the reference's own validation networks
     (testing/validation_tests/neuroml/<name>), or None without the tree."""
-    p = os.path.join(REF, "testing", "validation_tests", "neuroml", name)
+    ref = reference_tree()
+    if ref is None:
+        return None
+    p = os.path.join(ref, "testing", "validation_tests", "neuroml", name)
     return p if os.path.exists(p) else None
 
 
