@@ -99,6 +99,7 @@ struct EdenGpuCtx {
     // state: the host clock and the device state may then disagree, so
     // later runs are refused
     bool broken = false;
+    int64_t n_f64_cells = 0;    // cells whose cable solve runs in double precision
     bool launched = false;      // the current run has issued a kernel
     // edenGpuRunStaticScratch: device addresses of the static arrays, looked
     // up on the context's first such call (the context's device current)
@@ -444,9 +445,42 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         total += c;
     }
 
+    // ---- diagonal dominance: row i of a cell's backward-Euler cable matrix
+    // (eden/Eden.cpp:6114-6225) has 1 + dt (G_i / C_i + sum_j 1/(R_ij C_i))
+    // on the diagonal and dt / (R_ij C_i) off it, so it dominates whenever
+    // the membrane conductance G_i >= 0.  G_i is a sum of channel
+    // conductances (gbase fopen, fopen >= 0) and synaptic / input
+    // conductances (weight times an exposure whose sign is that of gbase
+    // times the event jump), so a cell can lose dominance only through a
+    // negative channel density, synaptic gbase, expTwo jump or weight.  Such
+    // cells are flagged: their elimination runs in double precision.
+    std::vector<char> cell_f64(n_phys, 0);
+    {
+        auto syn_sign = [&](int type, float w) {
+            const EdenGpuSynapseType &st = m->syn_types[type];
+            float sg = st.gbase * w;
+            if (st.kind == EDEN_SYN_EXPTWO) sg *= st.waveform_factor * st.weight_prop;
+            return sg;
+        };
+        auto flag_comp = [&](int32_t t) { if (t >= 0 && t < n_comp) cell_f64[comp_cell[t]] = 1; };
+        for (int i = 0; i < n_comp; i++)
+            for (int ch = m->comp_chan_off[i]; ch < m->comp_chan_off[i + 1]; ch++)
+                if (m->chan_gbase[ch] < 0.0f) flag_comp(i);
+        for (int64_t k = 0; k < m->n_syn; k++)
+            if (syn_sign(m->syn_type[k], m->syn_weight[k]) < 0.0f) flag_comp(m->syn_target[k]);
+        for (int64_t k = 0; k < m->n_pois; k++)
+            if (syn_sign(m->pois_type[k], m->pois_weight[k]) < 0.0f) flag_comp(m->pois_target[k]);
+        for (int64_t k = 0; k < m->n_timed; k++)
+            if (syn_sign(m->timed_type[k], m->timed_weight[k]) < 0.0f) flag_comp(m->timed_target[k]);
+    }
+    ctx->n_f64_cells = 0;
+    for (int c = 0; c < n_phys; c++) ctx->n_f64_cells += cell_f64[c];
+
     phase("order");
     // ---- schedule order: physical cells by tree depth (then size), then point
-    // neurons, so that a CTA's warps finish their cable solves together
+    // neurons, so that a CTA's warps finish their cable solves together; the
+    // cells flagged for a double-precision solve after the others, in forests
+    // of their own
     std::vector<int32_t> cell_levels(n_cells, 0);
     std::vector<std::vector<int>> cell_width(n_cells);
     for (int g = 0; g < n_cells; g++) {
@@ -464,9 +498,11 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     }
     std::vector<int32_t> order(n_cells);
     std::iota(order.begin(), order.end(), 0);
+    auto flagged = [&](int g) { return cell_phys[g] >= 0 && cell_f64[cell_phys[g]]; };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
         bool ix = cell_phys[x] < 0, iy = cell_phys[y] < 0;
         if (ix != iy) return iy;  // physical cells first
+        if (flagged(x) != flagged(y)) return flagged(y);
         if (cell_levels[x] != cell_levels[y]) return cell_levels[x] < cell_levels[y];
         return cell_n[x] < cell_n[y];
     });
@@ -499,6 +535,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     std::vector<int32_t> c_parent(nt, -1), c_child0(nt, 0), c_nchild(nt, 0), t_izh(nt, -1);
     std::vector<float> c_u(nt, 0.f), c_l(nt, 0.f);
     std::vector<int32_t> fo_t0, fo_t1, fo_l0, fo_nlev, lvl;     // forests (also the per-step path's)
+    std::vector<uint8_t> fo_f64;                                // forests solved in double precision
     std::vector<int32_t> un_t0, un_t1, un_f;                    // units: targets, forest or -1
     int next = 0;
     int max_forest = 1;
@@ -519,7 +556,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             while (pi < phys.size()) {
                 const int c = phys[pi];
                 const std::vector<int> &cw = cell_width[c];
-                bool fits = fc.empty() || nodes + cell_n[c] <= forest_node_cap;
+                bool fits = fc.empty() || (nodes + cell_n[c] <= forest_node_cap && flagged(c) == flagged(fc.front()));
                 for (size_t d = 0; fits && d < cw.size(); d++)
                     if ((d < fw.size() ? fw[d] : 0) + cw[d] > forest_width) fits = false;
                 if (!fits && !fc.empty()) break;
@@ -534,6 +571,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             std::vector<Node> q;
             for (int g : fc) q.push_back({m->phys_comp_off[cell_phys[g]], 0, 0});
             const int f_t0 = next;
+            fo_f64.push_back(flagged(fc.front()) ? 1 : 0);
             un_t0.push_back(f_t0);
             un_f.push_back((int)fo_t0.size());
             fo_t0.push_back(f_t0);
@@ -1063,7 +1101,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             const int nck = bk_c0[t_blk0[b]] - bk_c0[t_blk0[a]];
             const int nfch = un_nf1[u] > un_nf0[u] ? nf_c1[un_nf1[u] - 1] - nf_c0[un_nf0[u]] : 0;
             un_words[u] = forest_words(b - a, un_nf1[u] - un_nf0[u], nfch, un_ngt[u], fo_nlev[un_f[u]],
-                                       un_s1[u] - un_s0[u], nblk, nck, std::max(ctx->K, 4));
+                                       un_s1[u] - un_s0[u], nblk, nck, std::max(ctx->K, 4), fo_f64[un_f[u]] != 0);
         } else {
             un_words[u] = izh_words(b - a);
         }
@@ -1099,56 +1137,63 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     const int nsm = std::max(ctx->n_sm, 1);
     const int per_sm = (min_cta + nsm - 1) / nsm;
     const int n_cta = std::max(1, std::min(n_unit, per_sm * nsm));
-    // shared memory cap per CTA: an SM's share for per_sm CTAs, but never
-    // less than the largest unit or the words-balanced average
-    int64_t words_total = 0;
-    for (int u = 0; u < n_unit; u++) words_total += un_words[u];
+    // shared memory cap per CTA: an SM's share for per_sm CTAs (less the
+    // 1 KB the runtime reserves per CTA), never less than the largest unit
     const int share = (int)(ctx->smem_per_sm / (int)sizeof(float) / std::max(per_sm, 1)) - 256;
-    const int word_cap = std::max({max_words, share, (int)((words_total + n_cta - 1) / n_cta) + max_words});
-    std::vector<int> uorder(n_unit);
-    std::iota(uorder.begin(), uorder.end(), 0);
-    std::stable_sort(uorder.begin(), uorder.end(), [&](int x, int y) {
-        return un_cost[x] != un_cost[y] ? un_cost[x] > un_cost[y] : un_words[x] > un_words[y];
-    });
-    std::vector<std::vector<int>> cta_units(n_cta);
-    std::vector<int> cta_words(n_cta, 0);
-    {
-        // min-heap of (work, cta) over CTAs that still have a free warp
-        std::vector<double> cta_cost(n_cta, 0.0);
+    const int word_cap = std::max(max_words, share);
+    // longest-first onto the least-loaded CTA with room, by work under the
+    // cap, or (if that packing needs more shared memory than the share, which
+    // would leave an SM fewer CTAs) by shared memory alone
+    auto pack = [&](bool by_cost, std::vector<std::vector<int>> &units_of, std::vector<int> &words_of) {
+        std::vector<int> uorder(n_unit);
+        std::iota(uorder.begin(), uorder.end(), 0);
+        std::stable_sort(uorder.begin(), uorder.end(), [&](int x, int y) {
+            if (by_cost && un_cost[x] != un_cost[y]) return un_cost[x] > un_cost[y];
+            return un_words[x] > un_words[y];
+        });
+        units_of.assign(n_cta, {});
+        words_of.assign(n_cta, 0);
+        std::vector<double> load(n_cta, 0.0);
         std::vector<std::pair<double, int>> heap;
         for (int c = 0; c < n_cta; c++) heap.push_back({0.0, c});
         auto cmp = [](const std::pair<double, int> &x, const std::pair<double, int> &y) { return x > y; };
         std::make_heap(heap.begin(), heap.end(), cmp);
         std::vector<std::pair<double, int>> skipped;
         for (int uu : uorder) {
-            // the least-loaded CTA whose shared memory takes the unit (else the
-            // least-loaded one with a free warp)
             int pick = -1;
             skipped.clear();
             while (!heap.empty()) {
                 std::pop_heap(heap.begin(), heap.end(), cmp);
                 auto top = heap.back();
                 heap.pop_back();
-                if (cta_words[top.second] + un_words[uu] <= word_cap) { pick = top.second; break; }
+                if (!by_cost || words_of[top.second] + un_words[uu] <= word_cap) { pick = top.second; break; }
                 skipped.push_back(top);
             }
             if (pick < 0) {
-                pick = skipped.front().second;
-                skipped.erase(skipped.begin());
+                // nothing under the cap: the CTA with the fewest words
+                size_t best = 0;
+                for (size_t k = 1; k < skipped.size(); k++)
+                    if (words_of[skipped[k].second] < words_of[skipped[best].second]) best = k;
+                pick = skipped[best].second;
+                skipped.erase(skipped.begin() + best);
             }
             for (auto &sk : skipped) {
                 heap.push_back(sk);
                 std::push_heap(heap.begin(), heap.end(), cmp);
             }
-            cta_units[pick].push_back(uu);
-            cta_words[pick] += un_words[uu];
-            cta_cost[pick] += un_cost[uu];
-            if ((int)cta_units[pick].size() < upc) {
-                heap.push_back({cta_cost[pick], pick});
+            units_of[pick].push_back(uu);
+            words_of[pick] += un_words[uu];
+            load[pick] += by_cost ? un_cost[uu] : (double)un_words[uu];
+            if ((int)units_of[pick].size() < upc) {
+                heap.push_back({load[pick], pick});
                 std::push_heap(heap.begin(), heap.end(), cmp);
             }
         }
-    }
+        return *std::max_element(words_of.begin(), words_of.end());
+    };
+    std::vector<std::vector<int>> cta_units;
+    std::vector<int> cta_words;
+    if (pack(true, cta_units, cta_words) > share) pack(false, cta_units, cta_words);
     std::vector<int32_t> cta_u0, un_off(n_unit, 0), unit_of_slot;
     for (int c = 0; c < n_cta; c++) {
         cta_u0.push_back((int)unit_of_slot.size());
@@ -1177,6 +1222,18 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         int mx = 1;
         for (int c = 0; c < n_cta; c++) mx = std::max(mx, cta_words[c]);
         ctx->classes.push_back({0, n_cta, (size_t)mx * sizeof(float)});
+        if (verbose) {
+            double cmin = 1e300, cmax = 0.0, csum = 0.0;
+            for (int c = 0; c < n_cta; c++) {
+                double cc = 0.0;
+                for (int uu : cta_units[c]) cc += un_cost[uu];
+                cmin = std::min(cmin, cc);
+                cmax = std::max(cmax, cc);
+                csum += cc;
+            }
+            fprintf(stderr, "eden_gpu: %d units in %d CTAs (%d per SM), CTA words max %d cap %d, CTA work min %.1f "
+                            "mean %.1f max %.1f\n", n_unit, n_cta, per_sm, mx, word_cap, cmin, csum / n_cta, cmax);
+        }
     }
     size_t max_smem_class = 0;
     for (auto &cl : ctx->classes) max_smem_class = std::max(max_smem_class, cl.smem);
@@ -1203,6 +1260,15 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.c_rt0, c_rt0)); TRY(upload_c(ctx, &d.c_cep, c_cep)); TRY(upload_c(ctx, &d.t_izh, t_izh));
     TRY(upload_c(ctx, &d.fo_t0, fo_t0)); TRY(upload_c(ctx, &d.fo_t1, fo_t1)); TRY(upload_c(ctx, &d.fo_l0, fo_l0));
     TRY(upload_c(ctx, &d.fo_nlev, fo_nlev)); TRY(upload_c(ctx, &d.lvl, lvl));
+    {
+        // double-precision forests: flags, the flat compartments' constant
+        // diagonal terms, and the per-step path's double scratch
+        std::vector<float> c_d0(nt, 0.0f);
+        for (int it = 0; it < nt; it++)
+            if (!nonflat[it]) c_d0[it] = flat_d0[it];
+        TRY(upload_c(ctx, &d.fo_f64, fo_f64)); TRY(upload_c(ctx, &d.c_d0, c_d0));
+        TRY(upload(ctx, &d.dscr, (const double *)nullptr, ctx->n_f64_cells > 0 ? (size_t)2 * nt : (size_t)1));
+    }
     TRY(upload_c(ctx, &d.in_tgt, in_tgt));
     TRY(upload_c(ctx, &d.t_blk0, t_blk0)); TRY(upload_c(ctx, &d.bk_kind, bk_kind));
     TRY(upload_c(ctx, &d.bk_type, bk_type)); TRY(upload_c(ctx, &d.bk_erev, bk_erev));
@@ -1742,6 +1808,12 @@ extern "C" int edenGpuKernelStats(EdenGpuCtx *ctx, int32_t kind, double *total_m
     if (kind < 0 || kind >= EDEN_KERNEL_KINDS) return ctx->fail(EDEN_GPU_E_RANGE, "kernel kind %d", kind);
     if (total_ms) *total_ms = ctx->k_ms[kind];
     if (launches) *launches = ctx->k_n[kind];
+    return 0;
+}
+
+extern "C" int edenGpuFp64Cells(EdenGpuCtx *ctx, int64_t *n_cells) {
+    if (!ctx) return EDEN_GPU_E_INVALID;
+    if (n_cells) *n_cells = ctx->n_f64_cells;
     return 0;
 }
 

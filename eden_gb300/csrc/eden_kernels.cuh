@@ -218,6 +218,13 @@ struct DevModel {
     // per channel type and gate, the 9-word gate parameter record (gate_next_p)
     const float *gate_par;
     int32_t *status;
+    // forests whose cells may lose diagonal dominance: their elimination runs
+    // in double precision (hines_window_f64, hines_forest_f64); c_d0 is a
+    // flat compartment's constant diagonal term G/C + sum 1/(R C); dscr is
+    // the per-step path's double scratch (two per target)
+    const uint8_t *fo_f64;
+    const float *c_d0;
+    double *dscr;
 };
 
 constexpr uint32_t kCepMask = 0x3ffu;
@@ -238,8 +245,11 @@ constexpr int kGateExtWords = 9;  // a non-rates gate's kind and timeCourse / st
 // (kcap steps).  A batch of izhikevich neurons: V
 // twice and 11 parameter / state words per neuron.
 __host__ __device__ inline int forest_words(int n, int nf, int nfch, int ngt, int nlev, int ns, int nblk, int nck,
-                                            int kcap) {
-    return 7 * n + 10 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck;
+                                            int kcap, bool f64 = false) {
+    // a double-precision forest adds its eliminated values, pivots and
+    // factors in double (6 words per compartment, 8-byte aligned)
+    return 7 * n + 10 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck +
+           (f64 ? 6 * n + 2 : 0);
 }
 __host__ __device__ inline int izh_words(int n) { return (2 + EDEN_POINT_PARAMS + 3) * n + 1; }
 
@@ -1042,6 +1052,66 @@ __device__ __forceinline__ void hines_forest(const DevModel &m, bool init, int64
     }
 }
 
+// The same solve in double precision for a forest whose rows may lose
+// diagonal dominance (the per-step path; D and X are global, XD and DD the
+// forest's double scratch): the pre-updated V and diagonal terms stay the
+// single-precision values the step computed, the elimination and the
+// back-substitution carry doubles, and X receives V_next rounded once.
+__device__ __forceinline__ void hines_forest_f64(const DevModel &m, bool init, int64_t step, double tstep,
+                                                 const float *D, float *X, const float *U, const float *L,
+                                                 const int32_t *CE, const int32_t *P, const int32_t *LV, int nlev,
+                                                 const float *Vin, double *XD, double *DD, int wpar) {
+    const int lane = threadIdx.x & 31;
+    const int c0 = LV[0], c1 = LV[nlev];
+    if (!init && c1 > c0) {
+        const double dt = m.dt;
+        for (int c = c0 + lane; c < c1; c += 32) {
+            DD[c] = 1.0 + (double)D[c] * dt;
+            XD[c] = X[c];
+        }
+        __syncwarp();
+        for (int lev = nlev - 1; lev >= 0; lev--) {
+            const int j0 = LV[lev], j1 = LV[lev + 1];
+            for (int j = j0 + lane; j < j1; j += 32) {
+                const int kb = (j == j0) ? j1 : CE[j - 1];
+                const int ke = CE[j];
+                double dj = DD[j], xj = XD[j];
+                for (int i = kb; i < ke; i++) {
+                    const double ratio = (double)L[i] * DD[i];  // DD[i]: the child's reciprocal pivot
+                    dj -= ratio * (double)U[i];
+                    xj -= ratio * XD[i];
+                }
+                XD[j] = xj;
+                DD[j] = 1.0 / dj;
+            }
+            __syncwarp();
+        }
+        for (int r = LV[0] + lane; r < LV[1]; r += 32) XD[r] = XD[r] * DD[r];
+        __syncwarp();
+        for (int lev = 1; lev < nlev; lev++) {
+            for (int i = LV[lev] + lane; i < LV[lev + 1]; i += 32) XD[i] = (XD[i] - (double)U[i] * XD[P[i]]) * DD[i];
+            __syncwarp();
+        }
+        for (int c = c0 + lane; c < c1; c += 32) X[c] = (float)XD[c];
+        __syncwarp();
+    }
+    for (int c0w = c0; c0w < c1; c0w += 32) {
+        const int c = c0w + lane;
+        bool spk = false;
+        int src = -1;
+        double tc = 0.0;
+        if (c < c1) {
+            src = m.t_src[c];
+            if (src >= 0) {
+                const float thr = m.src_thr[src];
+                spk = (Vin[c] < thr && thr < X[c]);
+                if (spk) tc = crossing_time(tstep, m.dt, Vin[c], X[c], thr);
+            }
+        }
+        push_spike(m, spk, src, (int32_t)(step + 1), wpar, tc);
+    }
+}
+
 // Backward-Euler Hines solve of one forest by one warp for the windowed path,
 // on the unit's shared-memory slice (eden/Eden.cpp:6114-6225).  Flat
 // compartments keep the reciprocal pivot PV and the elimination factor RT
@@ -1101,6 +1171,53 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
         }
         __syncwarp();
     }
+}
+
+// hines_window in double precision, for a forest whose rows may lose
+// diagonal dominance: every compartment's pivot is rebuilt each step from
+// its diagonal term (PV: G/C + sum 1/(RC), the flat ones' constant one staged
+// from c_d0), and the elimination and back-substitution carry doubles in
+// XD / PVD / RTD; X receives V_next rounded once.  The operations are
+// hines_window's, in its order.
+__device__ __forceinline__ void hines_window_f64(float dt, float *X, const float *KC, const float *L, const float *PV,
+                                                 const float *U, const uint32_t *CEP, const int32_t *LV, int nlev,
+                                                 double *XD, double *PVD, double *RTD) {
+    const int lane = threadIdx.x & 31;
+    const double dtd = dt;
+    int end = LV[nlev] & kLvMask;
+    for (int lev = nlev - 1; lev >= 0; lev--) {
+        const int32_t lw = LV[lev];
+        for (int j = (lw & kLvMask) + lane; j < end; j += 32) {
+            const uint32_t cep = CEP[j];
+            const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
+            double xj = (double)X[j] + (double)KC[j];
+            double dj = 1.0 + (double)PV[j] * dtd;
+            for (int i = kb; i < ke; i++) {
+                const double r = RTD[i];
+                dj -= r * (double)U[i];
+                xj -= r * XD[i];
+            }
+            const double inv = 1.0 / dj;
+            PVD[j] = inv;
+            RTD[j] = (double)L[j] * inv;
+            XD[j] = xj;
+        }
+        end = lw & kLvMask;
+        __syncwarp();
+    }
+    for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) XD[r] = XD[r] * PVD[r];
+    __syncwarp();
+    for (int lev = 1; lev < nlev; lev++) {
+        const int i1 = LV[lev + 1] & kLvMask;
+        for (int i = (LV[lev] & kLvMask) + lane; i < i1; i += 32) {
+            const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
+            XD[i] = (XD[i] - (double)U[i] * XD[p]) * PVD[i];
+        }
+        __syncwarp();
+    }
+    const int n = LV[nlev] & kLvMask;
+    for (int i = lane; i < n; i += 32) X[i] = (float)XD[i];
+    __syncwarp();
 }
 
 }  // namespace eden

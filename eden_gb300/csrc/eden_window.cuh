@@ -87,7 +87,10 @@ __global__ void __launch_bounds__(kHinesThreads) k_hines_t(DevModel m, const Win
     for (int f = warp; f < m.n_forest; f += nwarps) {
         const int c0 = m.fo_t0[f], n = m.fo_t1[f] - c0, nlev = m.fo_nlev[f];
         const int32_t *lv = m.lvl + m.fo_l0[f];
-        if (n <= cap && nlev < cap) {
+        if (m.fo_f64[f]) {
+            hines_forest_f64(m, init, w.step0, w.t0, m.diag, x, m.c_u, m.c_l, m.c_cend, m.c_parent, lv, nlev, vin,
+                             m.dscr, m.dscr + m.n_target, w.wpar);
+        } else if (n <= cap && nlev < cap) {
             for (int i = lane; i < n; i += 32) {
                 sD[i] = m.diag[c0 + i]; sX[i] = x[c0 + i]; sU[i] = m.c_u[c0 + i];
                 sL[i] = m.c_l[c0 + i]; sV[i] = vin[c0 + i];
@@ -193,11 +196,15 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     float *BKE = (float *)(BKK + nblk);
     int32_t *BKC = (int32_t *)(BKE + nblk);
     float *GS = (float *)(BKC + nblk + 1);
+    // a double-precision forest's eliminated values, pivots and factors
+    const bool f64 = m.fo_f64[fi] != 0;
+    double *XD = reinterpret_cast<double *>(((uintptr_t)(GS + w.K * nck) + 7) & ~(uintptr_t)7);
+    double *PVD = XD + n, *RTD = PVD + n;
     // ---- stage the unit
     const float *vsrc = m.v[w.par];
     for (int i = lane; i < n; i += 32) {
         const int t = t0 + i;
-        X[i] = vsrc[t]; KC[i] = m.c_kc[t]; L[i] = m.c_l[t]; PV[i] = m.c_pv0[t];
+        X[i] = vsrc[t]; KC[i] = m.c_kc[t]; L[i] = m.c_l[t]; PV[i] = f64 ? m.c_d0[t] : m.c_pv0[t];
         RT[i] = m.c_rt0[t]; U[i] = m.c_u[t]; CEP[i] = m.c_cep[t];
     }
     for (int j = lane; j < nf; j += 32) {
@@ -278,7 +285,10 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             X[ti] = init ? v : v + (dt * (I + (v * G))) / C;
         }
         __syncwarp();
-        if (!init) hines_window(dt, X, KC, L, PV, RT, U, CEP, LV, nlev);
+        if (!init) {
+            if (f64) hines_window_f64(dt, X, KC, L, PV, U, CEP, LV, nlev, XD, PVD, RTD);
+            else hines_window(dt, X, KC, L, PV, RT, U, CEP, LV, nlev);
+        }
         // gate updates from this step's starting V and gate values (the
         // currents above used the values before the update, as the reference does)
         for (int q = lane; q < ngt; q += 32)

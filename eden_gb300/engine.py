@@ -48,7 +48,7 @@ class CRecords(ctypes.Structure):
                 ("spike_time_us", ctypes.POINTER(ctypes.c_double))]
 
 
-EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuRunStaticScratch", "edenGpuFetchRecords", "edenGpuGeneratedSource", "edenGpuReadV", "edenGpuWriteV",
+EXPORTED = ["edenGpuCreate", "edenGpuRun", "edenGpuRunStaticScratch", "edenGpuFetchRecords", "edenGpuGeneratedSource", "edenGpuReadV", "edenGpuWriteV", "edenGpuFp64Cells",
             "edenGpuReadSynapses", "edenGpuLastRunStats", "edenGpuKernelStats", "edenGpuLastError",
             "edenGpuDestroy", "edenGpuAbiVersion", "edenGpuGradCreate", "edenGpuGradForward",
             "edenGpuGradBackward", "edenGpuGradTiming", "edenGpuGradLastError", "edenGpuGradDestroy"]
@@ -272,6 +272,13 @@ class Simulation:
     def write_v(self, v: np.ndarray):
         v = np.ascontiguousarray(v, np.float32)
         self._check(self.lib.edenGpuWriteV(self.ctx, _ptr(v), ctypes.c_int64(self.n_target)))
+
+    def fp64_cells(self) -> int:
+        """Physical cells whose cable solve runs in double precision (those
+        that can lose diagonal dominance; edenGpuFp64Cells)."""
+        n = ctypes.c_int64()
+        self._check(self.lib.edenGpuFp64Cells(self.ctx, ctypes.byref(n)))
+        return n.value
 
     def read_synapses(self):
         n = len(self.lowered.syn_target)

@@ -369,6 +369,16 @@ int edenGpuWriteV(EdenGpuCtx *ctx, const float *v_host, int64_t n);
 /* Per-synapse pending spike times (us) and synapse state, for routing checks. */
 int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *state_a, float *state_b, int64_t n);
 
+/* The number of physical cells whose cable solve runs in double precision.
+ * A row of the backward-Euler cable matrix (eden/Eden.cpp:6114-6225) is
+ * diagonally dominant whenever its compartment's membrane conductance is
+ * not negative; edenGpuCreate flags every cell that can get a negative one
+ * (a negative channel density, synaptic gbase, expTwo jump or weight on any
+ * of its compartments) and eliminates its matrix in double precision, the
+ * state staying single precision.  (No reference counterpart: the reference
+ * solves every cell in single precision.) */
+int edenGpuFp64Cells(EdenGpuCtx *ctx, int64_t *n_cells);
+
 /* Device time of the last edenGpuRun in milliseconds and the number of
  * kernel launches it issued. */
 int edenGpuLastRunStats(EdenGpuCtx *ctx, double *device_ms, int64_t *launches);

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     text = open(os.path.join(ROOT, "include", "eden_gpu.h")).read()
-    return sorted(set(re.findall(r"\b(edenGpu[A-Za-z]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(edenGpu[A-Za-z0-9]+)\s*\(", text)))
 
 
 def test_header_matches_binding_list():

@@ -119,3 +119,43 @@ def test_interpolated_crossing_times_against_double(name, mode):
             assert abs(tc - ref[(int(s), int(k))]) <= CROSSING_ATOL_US
             matched += 1
     assert matched >= 0.9 * phys.sum()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+def test_cells_that_can_lose_diagonal_dominance_are_solved_in_double(mode):
+    """Negative weights on the synapses onto six cells' somas make their
+    membrane conductance able to go negative, and with it a cable-matrix
+    row's diagonal dominance: edenGpuCreate flags exactly those six cells,
+    eliminates their matrices in double precision, and the network stays
+    within the parity tolerances of the FP64 oracle: samecount(0.1 ms) and
+    box(0.1 ms, 0.5 mV) on every soma over the recurrent network's first
+    15 ms."""
+    from criteria import box_violations
+    from eden_gb300 import workloads
+    low = lowering.lower(workloads.multicomp_net(n_cells=24, in_degree=20, length_ms=15.0, max_seg=80))
+    neg = np.isin(low.syn_target, low.phys_comp_off[:6])
+    low.syn_weight = np.where(neg, -0.5 * low.syn_weight, low.syn_weight).astype(np.float32)
+    somas = np.ascontiguousarray(low.phys_comp_off[:-1], np.int32)
+    f64 = eden_port.run(low, trace_target=somas, double=True)
+    sim = Simulation(low, mode=mode, trace_target=somas)
+    try:
+        assert sim.fp64_cells() == 6
+        rec = sim.run()
+    finally:
+        sim.close()
+    shift = int(round(0.1 / (float(low.dt) * 1e-3)))
+    bad, worst = compare_spikes(f64["spike_src"], f64["spike_step"], rec.spike_src, rec.spike_step, shift)
+    assert bad == 0 and worst <= shift
+    assert len(rec.spike_src) > 0
+    nbad, w = box_violations(f64["trace"], rec.trace, float(low.dt) * 1e-3, 0.1, 0.5)
+    assert nbad == 0, f"{nbad} samples outside box(0.1 ms, 0.5 mV), worst {w} mV"
+
+
+def test_no_cell_is_flagged_without_negative_conductances():
+    from eden_gb300 import workloads
+    low = lowering.lower(workloads.multicomp_net(n_cells=12, in_degree=10, length_ms=1.0, max_seg=40))
+    sim = Simulation(low)
+    try:
+        assert sim.fp64_cells() == 0
+    finally:
+        sim.close()
