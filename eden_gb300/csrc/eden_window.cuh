@@ -198,7 +198,7 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     float *GS = (float *)(BKC + nblk + 1);
     // a double-precision forest's eliminated values, pivots and factors
     const bool f64 = m.fo_f64[fi] != 0;
-    double *XD = reinterpret_cast<double *>(((uintptr_t)(GS + w.K * nck) + 7) & ~(uintptr_t)7);
+    double *XD = reinterpret_cast<double *>((reinterpret_cast<unsigned long long>(GS + w.K * nck) + 7ull) & ~7ull);
     double *PVD = XD + n, *RTD = PVD + n;
     // ---- stage the unit
     const float *vsrc = m.v[w.par];
