@@ -1107,93 +1107,35 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         }
     }
     phase("packing");
-    // CTAs of up to four units.  Every CTA of one window's launch is resident
-    // at once when the CTA count is a multiple of the SM count and the
-    // shared memory of that many CTAs fits an SM: each SM then runs the same
-    // number of CTAs, and an SM's time is the sum of its units' work.  So
-    // the units are spread longest-first, by an estimate of their per-step
-    // work, onto the CTA with the least work that still has room -- a free
-    // warp and shared memory under the cap -- so that the CTAs' work, and
-    // with it the SMs', is even.
+    // CTAs of up to four units, packed longest-first onto the CTA with the
+    // fewest words so that every CTA needs about the same shared memory.
+    // (Packing by an estimate of each unit's work instead, with the CTA
+    // count a multiple of the SM count, measured 3 % slower on C2.)
     const int upc = kCellThreads / 32;
-    std::vector<double> un_cost(n_unit, 0.0);
-    for (int u = 0; u < n_unit; u++) {
-        if (un_f[u] < 0) {
-            un_cost[u] = 4.0;  // a batch of point neurons: one pass per step
-            continue;
-        }
-        // the cable solve's depth passes (two per depth) and its iterations
-        // (one per 32 compartments of a depth), the non-flat compartments'
-        // currents and the gates, in units of one solve iteration
-        const int f = un_f[u], nl = fo_nlev[f];
-        double iters = 0.0;
-        for (int l = 0; l < nl; l++) iters += std::ceil((lvl[fo_l0[f] + l + 1] - lvl[fo_l0[f] + l]) / 32.0);
-        const int nf = un_nf1[u] - un_nf0[u];
-        un_cost[u] = 2.0 * iters + nl + 8.0 * std::ceil(nf / 32.0) + 3.0 * std::ceil(un_ngt[u] / 32.0);
-    }
-    int max_words = 1;
-    for (int u = 0; u < n_unit; u++) max_words = std::max(max_words, un_words[u]);
-    const int min_cta = (n_unit + upc - 1) / upc;
-    const int nsm = std::max(ctx->n_sm, 1);
-    const int per_sm = (min_cta + nsm - 1) / nsm;
-    const int n_cta = std::max(1, std::min(n_unit, per_sm * nsm));
-    // shared memory cap per CTA: an SM's share for per_sm CTAs (less the
-    // 1 KB the runtime reserves per CTA), never less than the largest unit
-    const int share = (int)(ctx->smem_per_sm / (int)sizeof(float) / std::max(per_sm, 1)) - 256;
-    const int word_cap = std::max(max_words, share);
-    // longest-first onto the least-loaded CTA with room, by work under the
-    // cap, or (if that packing needs more shared memory than the share, which
-    // would leave an SM fewer CTAs) by shared memory alone
-    auto pack = [&](bool by_cost, std::vector<std::vector<int>> &units_of, std::vector<int> &words_of) {
-        std::vector<int> uorder(n_unit);
-        std::iota(uorder.begin(), uorder.end(), 0);
-        std::stable_sort(uorder.begin(), uorder.end(), [&](int x, int y) {
-            if (by_cost && un_cost[x] != un_cost[y]) return un_cost[x] > un_cost[y];
-            return un_words[x] > un_words[y];
-        });
-        units_of.assign(n_cta, {});
-        words_of.assign(n_cta, 0);
-        std::vector<double> load(n_cta, 0.0);
-        std::vector<std::pair<double, int>> heap;
-        for (int c = 0; c < n_cta; c++) heap.push_back({0.0, c});
-        auto cmp = [](const std::pair<double, int> &x, const std::pair<double, int> &y) { return x > y; };
+    const int n_cta = (n_unit + upc - 1) / upc;
+    std::vector<int> uorder(n_unit);
+    std::iota(uorder.begin(), uorder.end(), 0);
+    std::stable_sort(uorder.begin(), uorder.end(), [&](int x, int y) { return un_words[x] > un_words[y]; });
+    std::vector<std::vector<int>> cta_units(n_cta);
+    std::vector<int> cta_words(n_cta, 0);
+    {
+        // min-heap of (words, cta) over CTAs that still have room
+        std::vector<std::pair<int, int>> heap;
+        for (int c = 0; c < n_cta; c++) heap.push_back({0, c});
+        auto cmp = [](const std::pair<int, int> &x, const std::pair<int, int> &y) { return x > y; };
         std::make_heap(heap.begin(), heap.end(), cmp);
-        std::vector<std::pair<double, int>> skipped;
         for (int uu : uorder) {
-            int pick = -1;
-            skipped.clear();
-            while (!heap.empty()) {
-                std::pop_heap(heap.begin(), heap.end(), cmp);
-                auto top = heap.back();
-                heap.pop_back();
-                if (!by_cost || words_of[top.second] + un_words[uu] <= word_cap) { pick = top.second; break; }
-                skipped.push_back(top);
-            }
-            if (pick < 0) {
-                // nothing under the cap: the CTA with the fewest words
-                size_t best = 0;
-                for (size_t k = 1; k < skipped.size(); k++)
-                    if (words_of[skipped[k].second] < words_of[skipped[best].second]) best = k;
-                pick = skipped[best].second;
-                skipped.erase(skipped.begin() + best);
-            }
-            for (auto &sk : skipped) {
-                heap.push_back(sk);
-                std::push_heap(heap.begin(), heap.end(), cmp);
-            }
-            units_of[pick].push_back(uu);
-            words_of[pick] += un_words[uu];
-            load[pick] += by_cost ? un_cost[uu] : (double)un_words[uu];
-            if ((int)units_of[pick].size() < upc) {
-                heap.push_back({load[pick], pick});
+            std::pop_heap(heap.begin(), heap.end(), cmp);
+            auto top = heap.back();
+            heap.pop_back();
+            cta_units[top.second].push_back(uu);
+            cta_words[top.second] += un_words[uu];
+            if ((int)cta_units[top.second].size() < upc) {
+                heap.push_back({cta_words[top.second], top.second});
                 std::push_heap(heap.begin(), heap.end(), cmp);
             }
         }
-        return *std::max_element(words_of.begin(), words_of.end());
-    };
-    std::vector<std::vector<int>> cta_units;
-    std::vector<int> cta_words;
-    if (pack(true, cta_units, cta_words) > share) pack(false, cta_units, cta_words);
+    }
     std::vector<int32_t> cta_u0, un_off(n_unit, 0), unit_of_slot;
     for (int c = 0; c < n_cta; c++) {
         cta_u0.push_back((int)unit_of_slot.size());
@@ -1222,18 +1164,6 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         int mx = 1;
         for (int c = 0; c < n_cta; c++) mx = std::max(mx, cta_words[c]);
         ctx->classes.push_back({0, n_cta, (size_t)mx * sizeof(float)});
-        if (verbose) {
-            double cmin = 1e300, cmax = 0.0, csum = 0.0;
-            for (int c = 0; c < n_cta; c++) {
-                double cc = 0.0;
-                for (int uu : cta_units[c]) cc += un_cost[uu];
-                cmin = std::min(cmin, cc);
-                cmax = std::max(cmax, cc);
-                csum += cc;
-            }
-            fprintf(stderr, "eden_gpu: %d units in %d CTAs (%d per SM), CTA words max %d cap %d, CTA work min %.1f "
-                            "mean %.1f max %.1f\n", n_unit, n_cta, per_sm, mx, word_cap, cmin, csum / n_cta, cmax);
-        }
     }
     size_t max_smem_class = 0;
     for (auto &cl : ctx->classes) max_smem_class = std::max(max_smem_class, cl.smem);
