@@ -335,6 +335,16 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
         for (int64_t k = 0; k < m->n_pois; k++)
             if (m->pois_rng_base[k] < 0)
                 return ctx->fail(EDEN_GPU_E_INVALID, "Poisson input %lld: negative random-call id", (long long)k);
+    if (m->n_gap < 0) return ctx->fail(EDEN_GPU_E_INVALID, "n_gap must be >= 0");
+    if (m->n_gap > 0 && (!m->gap_target || !m->gap_peer || !m->gap_conductance || !m->gap_weight))
+        return ctx->fail(EDEN_GPU_E_INVALID, "gap junctions: null array");
+    for (int64_t k = 0; k < m->n_gap; k++) {
+        if (m->gap_target[k] < 0 || m->gap_target[k] >= m->n_comp || m->gap_peer[k] < 0 || m->gap_peer[k] >= m->n_comp)
+            return ctx->fail(EDEN_GPU_E_INVALID, "gap junction %lld: ends must be compartments of physical cells",
+                             (long long)k);
+        if (!std::isfinite(m->gap_conductance[k]) || !std::isfinite(m->gap_weight[k]))
+            return ctx->fail(EDEN_GPU_E_INVALID, "gap junction %lld: non-finite conductance or weight", (long long)k);
+    }
     return 0;
 }
 
@@ -428,6 +438,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (int64_t k = 0; k < m->n_pulse; k++) n_in_user[m->pulse_target[k]]++;
     for (int64_t k = 0; k < m->n_wave; k++) n_in_user[m->wave_target[k]]++;
     for (int64_t k = 0; k < m->n_clamp; k++) n_in_user[m->clamp_target[k]] += 2;
+    for (int64_t k = 0; k < m->n_gap; k++) n_in_user[m->gap_target[k]]++;
     std::vector<double> cost(n_cells, 0.0);
     double total = 0;
     int max_cell = 1;
@@ -721,6 +732,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = 0; k < m->n_timed; k++) has_input[u2i[m->timed_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_wave; k++) has_input[u2i[m->wave_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_clamp; k++) has_input[u2i[m->clamp_target[k]]] = 1;
+        for (int64_t k = 0; k < m->n_gap; k++) has_input[u2i[m->gap_target[k]]] = 1;
         for (int it = 0; it < nt; it++) {
             if (t_izh[it] >= 0 || has_input[it]) continue;
             if (c_chan0[it + 1] - c_chan0[it] != 1) continue;
@@ -1005,6 +1017,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         double dsteps = std::floor((double)min_delay / (double)dt);
         kmax = (int)std::max(1.0, std::min((double)kMaxWindow, dsteps));
     }
+    // gap junctions couple cells within a step: one-step windows, each
+    // reading its peers' potentials from the buffer the previous one wrote
+    if (m->n_gap > 0) kmax = 1;
     ctx->mode = opt ? opt->mode : EDEN_MODE_PLAIN;
     ctx->kernel_timing = opt && opt->kernel_timing;
     int kreq = (opt && opt->steps_per_launch > 0) ? opt->steps_per_launch : kmax;
@@ -1198,6 +1213,22 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             if (!nonflat[it]) c_d0[it] = flat_d0[it];
         TRY(upload_c(ctx, &d.fo_f64, fo_f64)); TRY(upload_c(ctx, &d.c_d0, c_d0));
         TRY(upload(ctx, &d.dscr, (const double *)nullptr, ctx->n_f64_cells > 0 ? (size_t)2 * nt : (size_t)1));
+    }
+    {
+        // gap-junction ends per internal target, in the model's order
+        std::vector<int32_t> t_gap0(nt + 1, 0), gj_peer(m->n_gap);
+        std::vector<float> gj_g(m->n_gap), gj_w(m->n_gap);
+        for (int64_t k = 0; k < m->n_gap; k++) t_gap0[u2i[m->gap_target[k]] + 1]++;
+        for (int t = 0; t < nt; t++) t_gap0[t + 1] += t_gap0[t];
+        std::vector<int32_t> fill(t_gap0.begin(), t_gap0.end() - 1);
+        for (int64_t k = 0; k < m->n_gap; k++) {
+            const int32_t o = fill[u2i[m->gap_target[k]]]++;
+            gj_peer[o] = u2i[m->gap_peer[k]];
+            gj_g[o] = m->gap_conductance[k];
+            gj_w[o] = m->gap_weight[k];
+        }
+        TRY(upload_c(ctx, &d.t_gap0, t_gap0)); TRY(upload_c(ctx, &d.gap_peer, gj_peer));
+        TRY(upload_c(ctx, &d.gap_g, gj_g)); TRY(upload_c(ctx, &d.gap_w, gj_w));
     }
     TRY(upload_c(ctx, &d.in_tgt, in_tgt));
     TRY(upload_c(ctx, &d.t_blk0, t_blk0)); TRY(upload_c(ctx, &d.bk_kind, bk_kind));
@@ -1393,6 +1424,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         kinds.forest = d.n_forest > 0;
         kinds.gateforms = gate_forms;
         kinds.izh = n_izh > 0;
+        kinds.gap = m->n_gap > 0;
         ctx->codegen_source = eden_codegen::program_source(eden_codegen::kind_defines(kinds) +
                                                            eden_codegen::channel_routines(m->chan_types, chan_sets));
         eden_codegen::Kernels kk;

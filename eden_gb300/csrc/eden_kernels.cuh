@@ -225,7 +225,21 @@ struct DevModel {
     const uint8_t *fo_f64;
     const float *c_d0;
     double *dscr;
+    // gap-junction ends of each target [t_gap0[t], t_gap0[t+1]): the peer
+    // (internal target), conductance (uS) and weight
+    const int32_t *t_gap0, *gap_peer;
+    const float *gap_g, *gap_w;
 };
+
+// The gap-junction current into target t at potential v, its peers read
+// from the step's starting potentials vnow: each end contributes
+// (g (V_peer - v)) w, as the reference sums a synapse's exposure times its
+// weight (eden/Eden.cpp:3407-3422, 3708-3710); no conductance term.
+__device__ __forceinline__ float gap_current(const DevModel &m, int t, float v, const float *vnow) {
+    float i = 0.0f;
+    for (int k = m.t_gap0[t]; k < m.t_gap0[t + 1]; k++) i += (m.gap_g[k] * (vnow[m.gap_peer[k]] - v)) * m.gap_w[k];
+    return i;
+}
 
 constexpr uint32_t kCepMask = 0x3ffu;
 constexpr int kCepBeginShift = 10;
@@ -522,6 +536,7 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
 #define EDEN_KIND_EXPTWO 1
 #define EDEN_KIND_FOREST 1
 #define EDEN_KIND_IZH 1
+#define EDEN_KIND_GAP 1
 #endif
 
 // A timedSynapticInput item over the window: its synapse fires in each

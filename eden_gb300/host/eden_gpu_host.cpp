@@ -128,6 +128,8 @@ void fill_model(const Reader &r, EdenGpuModel &m) {
     PTR(wave_weight, float);
     PTR(pois_rng_base, int32_t);
     I64(n_clamp); PTR(clamp_target, int32_t); PTR(clamp_params, float); PTR(clamp_weight, float);
+    I64(n_gap); PTR(gap_target, int32_t); PTR(gap_peer, int32_t); PTR(gap_conductance, float);
+    PTR(gap_weight, float);
 #undef I32
 #undef I64
 #undef PTR

@@ -146,6 +146,12 @@ class LoweredModel:
     clamp_target: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     clamp_params: np.ndarray = field(default_factory=lambda: np.zeros((0, 6), np.float32))
     clamp_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    # gap junctions: one entry per end (the compartment it sits on, the peer
+    # compartment, conductance uS, weight)
+    gap_target: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    gap_peer: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    gap_conductance: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    gap_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
 
     @property
     def n_comp(self) -> int:
@@ -641,6 +647,26 @@ def lower(spec: NetworkSpec) -> LoweredModel:
                                  if s.kind == SYN_EXPTWO else 1.0)
         st["weight_prop"] = 1.0
 
+    # ---- gap junctions: each electrical connection puts an instance on both
+    # ends, each taking weight * conductance * (V_peer - V_own) as synaptic
+    # current (eden/Eden.cpp:9233-9251, 3407-3422); physical compartments only
+    gap_of = {g.name: g for g in spec.gap_types}
+    gj_t, gj_p, gj_g, gj_w = [], [], [], []
+    for ep in spec.electrical:
+        pre = np.asarray(ep.pre_cell, np.int64)
+        post = np.asarray(ep.post_cell, np.int64)
+        if len(pre) and (gid_is_izh[pre].any() or gid_is_izh[post].any()):
+            raise ValueError(f"{ep.name}: gap junctions join compartments of physical cells")
+        a = target_of(pre, ep.pre_seg, current=False)
+        b = target_of(post, ep.post_seg, current=False)
+        g = _to_f32(gap_of[ep.synapse].conductance * 1e-3)   # nS -> uS
+        w = np.asarray(ep.weight, np.float64).astype(F32)
+        for i in range(len(pre)):
+            gj_t += [a[i], b[i]]
+            gj_p += [b[i], a[i]]
+            gj_g += [g, g]
+            gj_w += [w[i], w[i]]
+
     # ---- connection synapses: grouped per target, type order, then connection order
     tgt, typ, src, wgt, dly, order_key = [], [], [], [], [], []
     seq = 0
@@ -792,13 +818,15 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         timed_off=np.asarray(tm_off, np.int64), timed_step=cat(tm_steps, np.int64),
         wave_target=wt, wave_shape=wsh, wave_params=wpar, wave_weight=wwt,
         pois_rng_base=prng, clamp_target=ct_, clamp_params=cpar, clamp_weight=cwt,
+        gap_target=np.asarray(gj_t, np.int32), gap_peer=np.asarray(gj_p, np.int32),
+        gap_conductance=np.asarray(gj_g, F32), gap_weight=np.asarray(gj_w, F32),
     )
 
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 7
+ABI_VERSION = 8
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -830,6 +858,8 @@ class CModel(ctypes.Structure):
         ("wave_weight", _f32p),
         ("pois_rng_base", _i32p),
         ("n_clamp", ctypes.c_int64), ("clamp_target", _i32p), ("clamp_params", _f32p), ("clamp_weight", _f32p),
+        ("n_gap", ctypes.c_int64), ("gap_target", _i32p), ("gap_peer", _i32p), ("gap_conductance", _f32p),
+        ("gap_weight", _f32p),
     ]
 
 
@@ -919,4 +949,9 @@ def to_cmodel(m: LoweredModel):
     cm.clamp_target = p(m.clamp_target, np.int32, _i32p)
     cm.clamp_params = p(np.asarray(m.clamp_params).reshape(-1), F32, _f32p)
     cm.clamp_weight = p(m.clamp_weight, F32, _f32p)
+    cm.n_gap = len(m.gap_target)
+    cm.gap_target = p(m.gap_target, np.int32, _i32p)
+    cm.gap_peer = p(m.gap_peer, np.int32, _i32p)
+    cm.gap_conductance = p(m.gap_conductance, F32, _f32p)
+    cm.gap_weight = p(m.gap_weight, F32, _f32p)
     return cm, keep

@@ -285,6 +285,29 @@ class Projection:
 
 
 @dataclass
+class GapJunctionType:
+    """gapJunction: a linear electrical synapse of `conductance` (nS)."""
+    name: str
+    conductance: float
+
+
+@dataclass
+class ElectricalProjection:
+    """electricalConnection(Instance)(W) list of one gapJunction type: each
+    connection puts an instance on both ends -- cell gid pre_cell, segment
+    pre_seg, and cell gid post_cell, segment post_seg -- and each end takes
+    weight * conductance * (V_other - V_own) as synaptic current, with no
+    conductance term (eden/Eden.cpp:3407-3422, 9233-9251)."""
+    name: str
+    synapse: str
+    pre_cell: np.ndarray
+    pre_seg: np.ndarray
+    post_cell: np.ndarray
+    post_seg: np.ndarray
+    weight: np.ndarray
+
+
+@dataclass
 class PulseInputs:
     """One pulseGenerator per entry (delay/duration ms, amplitude nA) on
     cell gid `cell`, segment `seg`, scaled by `weight` (an inputW's; 1 when
@@ -392,6 +415,8 @@ class NetworkSpec:
     synapses: List[SynapseType] = field(default_factory=list)
     populations: List[Population] = field(default_factory=list)
     projections: List[Projection] = field(default_factory=list)
+    gap_types: List[GapJunctionType] = field(default_factory=list)
+    electrical: List[ElectricalProjection] = field(default_factory=list)
     pulses: List[PulseInputs] = field(default_factory=list)
     poissons: List[PoissonInputs] = field(default_factory=list)
     timed: List[TimedInputs] = field(default_factory=list)

@@ -25,7 +25,8 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       SpikeGeneratorRandomCell, SynapseType,
                       EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
-                      ClampInputs, FitzHughNagumoCell, IzhikevichCell, TimedInputs, WaveInputs)
+                      ClampInputs, FitzHughNagumoCell, IzhikevichCell, TimedInputs, WaveInputs,
+                      ElectricalProjection, GapJunctionType)
 
 
 def _f(x: float) -> str:
@@ -82,6 +83,8 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
         else:
             w(f'<expTwoSynapse id="{s.name}" gbase="{_f(s.gbase)}nS" erev="{_f(s.erev)}mV" '
               f'tauRise="{_f(s.tau_rise)}ms" tauDecay="{_f(s.tau_decay)}ms"/>\n')
+    for gt in spec.gap_types:
+        w(f'<gapJunction id="{gt.name}" conductance="{_f(gt.conductance)}nS"/>\n')
     used_types = {p.cell_type for p in spec.populations}
     for c in spec.cells:
         if c.name not in used_types:
@@ -235,6 +238,23 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
                   f'postCellId="../{pb}[{local_of[pr.post_cell[i]]}]" postSegmentId="{pr.post_seg[i]}" '
                   f'weight="{_f(pr.weight[i])}" delay="{_f(pr.delay[i])}ms"/>\n')
             w(' </projection>\n')
+    for ep in spec.electrical:
+        # one electricalProjection per (pre population, post population) run
+        groups = []
+        for i in range(len(ep.pre_cell)):
+            key = (pop_of[ep.pre_cell[i]], pop_of[ep.post_cell[i]])
+            if not groups or groups[-1][0] != key:
+                groups.append((key, []))
+            groups[-1][1].append(i)
+        for gi, ((pa, pb), idx) in enumerate(groups):
+            w(f' <electricalProjection id="{ep.name}_{gi}" presynapticPopulation="{pa}" '
+              f'postsynapticPopulation="{pb}">\n')
+            for n, i in enumerate(idx):
+                w(f'  <electricalConnectionInstanceW id="{n}" preCell="../{pa}/{local_of[ep.pre_cell[i]]}/'
+                  f'{spec.population(pa).cell_type}" preSegment="{ep.pre_seg[i]}" '
+                  f'postCell="../{pb}/{local_of[ep.post_cell[i]]}/{spec.population(pb).cell_type}" '
+                  f'postSegment="{ep.post_seg[i]}" synapse="{ep.synapse}" weight="{_f(ep.weight[i])}"/>\n')
+            w(' </electricalProjection>\n')
     n_list = 0
 
     def input_lists(obj, comp_of, weighted):
@@ -614,7 +634,7 @@ def read_lems(path: str) -> NetworkSpec:
                        _qty(sim, "length", "time"), seed)
     # components
     channels_by_name, synapses, pulses_def, pois_def, cells = {}, {}, {}, {}, {}
-    timed_def, wave_def, clamp_def = {}, {}, {}
+    timed_def, wave_def, clamp_def, gap_def = {}, {}, {}, {}
     refused_inputs = {}
     net = None
     for e in elems:
@@ -658,6 +678,8 @@ def read_lems(path: str) -> NetworkSpec:
             synapses[e.get("id")] = SynapseType(e.get("id"), SYN_EXPTWO, _qty(e, "gbase", "conductance"),
                                                 _qty(e, "erev", "voltage"), _qty(e, "tauDecay", "time"),
                                                 _qty(e, "tauRise", "time"))
+        elif t == "gapJunction":
+            gap_def[e.get("id")] = GapJunctionType(e.get("id"), _qty(e, "conductance", "conductance"))
         elif t in ("pulseGenerator", "pulseGeneratorDL"):
             dl = t.endswith("DL")
             pulses_def[e.get("id")] = (_qty(e, "delay", "time"), _qty(e, "duration", "time"),
@@ -748,6 +770,7 @@ def read_lems(path: str) -> NetworkSpec:
     if _tag(net) == "networkWithTemperature" or net.get("type") == "networkWithTemperature":
         spec.temperature = _temperature_degc(net.get("temperature"))
     spec.synapses = list(synapses.values())
+    spec.gap_types = list(gap_def.values())
     syn_names = list(synapses)
     # populations (declaration order = gid order)
     pops = {}
@@ -812,6 +835,28 @@ def read_lems(path: str) -> NetworkSpec:
         spec.projections.append(Projection(f"proj_{syn}", "*", "*", syn, np.array(rows[0], np.int64),
                                            np.array(rows[1], np.int64), np.array(rows[2], np.int64),
                                            np.array(rows[3]), np.array(rows[4])))
+    # electrical projections: gap junctions, an instance on each end
+    # (eden/NeuroML.cpp:6057-6125: electricalConnection with cell indices,
+    # electricalConnectionInstance(W) with cell paths, W with a weight)
+    by_gap = {}
+    for pr in _children(net, "electricalProjection"):
+        pa, pb = pr.get("presynapticPopulation"), pr.get("postsynapticPopulation")
+        for c in pr:
+            tag = _tag(c)
+            if tag not in ("electricalConnection", "electricalConnectionInstance", "electricalConnectionInstanceW"):
+                continue
+            syn = c.get("synapse")
+            if syn not in gap_def:
+                raise ValueError(f"electricalProjection {pr.get('id')}: synapse {syn} is not a gapJunction")
+            rows = by_gap.setdefault(syn, [[], [], [], [], []])
+            rows[0].append(gid(_cell_ref(c.get("preCell"), pops, pa)))
+            rows[1].append(int(c.get("preSegment", "0")))
+            rows[2].append(gid(_cell_ref(c.get("postCell"), pops, pb)))
+            rows[3].append(int(c.get("postSegment", "0")))
+            rows[4].append(float(c.get("weight", "1")) if tag.endswith("W") else 1.0)
+    for syn, rows in by_gap.items():
+        spec.electrical.append(ElectricalProjection(f"gap_{syn}", syn, *(np.array(r, np.int64) for r in rows[:4]),
+                                                    np.array(rows[4])))
     # inputs
     pcell, pseg, pdel, pdur, pamp, pwt, pdl, plist = [], [], [], [], [], [], [], []
     pois_rows, wave_rows, clamp_rows = {}, {}, {}

@@ -40,6 +40,11 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    and HH cells.
   voltage_clamps   voltageClamp and voltageClampTriple on HH somata,
                    passive dendrites and izhikevich cells, with pulses.
+  gap_junctions    gapJunction types of two conductances on soma-soma and
+                   soma-dendrite electrical connections (weighted) between
+                   single-compartment HH cells and branching cells, with DC
+                   pulses on some somata and expTwo synapses onto coupled
+                   compartments.
   gate_kinds       channels with every built-in gate kind (gateHHrates,
                    gateHHtauInf, gateHHratesTau, gateHHratesInf,
                    gateHHratesTauInf), q10Fixed and q10ExpTemp settings at
@@ -60,7 +65,7 @@ from .network import (RATE_EXP, RATE_EXPLINEAR, RATE_SIGMOID, AdExCell, Channel,
                       Population, Projection, PulseInputs, SpikeArrayCell, EventSetReaderCell,
                       SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       SpikeGeneratorCell, SynapseType, SYN_EXPONE, SYN_EXPTWO, TimedInputs, WAVE_RAMP,
-                      WAVE_SINE, WaveInputs, hh_channels)
+                      WAVE_SINE, WaveInputs, hh_channels, ElectricalProjection, GapJunctionType)
 
 # conductivities (mS/cm2) and reversal potentials (mV) of the HH cells
 G_NA, G_K, G_L = 120.0, 36.0, 0.3
@@ -846,6 +851,67 @@ def voltage_clamps(n_hh: int = 4, n_branch: int = 2, n_izh: int = 2, length_ms: 
     return spec
 
 
+def gap_junctions(n_hh: int = 10, n_branch: int = 4, n_izh: int = 2, length_ms: float = 80.0,
+                  dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
+    """Gap junctions (two gapJunction types, 1 and 4 nS, weights 0.5-1.5)
+    joining HH somata in a ring with random chords and HH somata to the
+    passive dendrites of branching cells; DC pulses drive a third of the
+    somata, so the rest are driven through the junctions, and expTwo
+    synapses from the HH cells land on coupled compartments and on
+    izhikevich cells."""
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("gap_junctions", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=1.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+    spec.gap_types.append(GapJunctionType("gap_weak", 1.0))
+    spec.gap_types.append(GapJunctionType("gap_strong", 4.0))
+    spec.cells.append(PhysicalCell("hhcell", np.array([-1]), np.array([0.0]), np.array([17.8]),
+                                   _hh_densities(1, np.ones(1, bool)), cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0))
+    parent = np.array([-1, 0, 1, 0])
+    soma = parent < 0
+    spec.cells.append(PhysicalCell("branch", parent, np.array([20.0, 80.0, 60.0, 70.0]),
+                                   np.array([20.0, 2.0, 1.5, 1.8]), _hh_densities(len(parent), soma), cm=1.0,
+                                   ra=150.0, v0=-65.0, spike_thresh=-20.0,
+                                   seg_groups={"soma_group": soma, "dend_group": ~soma}))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    spec.populations.append(Population("branch", "branch", n_branch))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    hh = np.arange(n_hh)
+    br = n_hh + np.arange(n_branch)
+    iz = n_hh + n_branch + np.arange(n_izh)
+    driven = hh[::3]
+    spec.pulses.append(PulseInputs("*", driven, np.zeros(len(driven), int),
+                                   np.round(rng.uniform(2.0, 10.0, len(driven)), 3), np.full(len(driven), length_ms),
+                                   np.round(rng.uniform(0.1, 0.3, len(driven)), 4)))
+    spec.pulses.append(PulseInputs("*", iz, np.zeros(n_izh, int), np.zeros(n_izh), np.full(n_izh, length_ms),
+                                   np.full(n_izh, 0.1)))
+    # weak junctions: a ring of somata plus random chords
+    pre = np.concatenate([hh, rng.choice(hh, n_hh // 2)])
+    post = np.concatenate([np.roll(hh, -1), rng.choice(hh, n_hh // 2)])
+    post = np.where(pre == post, (post + 1) % n_hh, post)
+    spec.electrical.append(ElectricalProjection("gap_weak", "gap_weak", pre, np.zeros(len(pre), int), post,
+                                                np.zeros(len(pre), int),
+                                                np.round(rng.uniform(0.5, 1.5, len(pre)), 4)))
+    # strong junctions: somata to the dendrites of the branching cells
+    pre = rng.choice(hh, 2 * n_branch)
+    post = np.repeat(br, 2)
+    post_seg = np.tile([2, 3], n_branch)
+    spec.electrical.append(ElectricalProjection("gap_strong", "gap_strong", pre, np.zeros(len(pre), int), post,
+                                                post_seg, np.round(rng.uniform(0.5, 1.5, len(pre)), 4)))
+    # chemical synapses onto coupled somata and dendrites, and izhikevich cells
+    post = np.concatenate([hh[1::3], br, iz])
+    pre = rng.choice(driven, len(post))
+    post_seg = np.concatenate([np.zeros(len(hh[1::3]), int), np.full(n_branch, 2), np.zeros(n_izh, int)])
+    spec.projections.append(_flat_projection(spec, "proj_e2", pre, post, "syn_e2",
+                                             np.round(rng.uniform(0.5, 1.5, len(post)), 4),
+                                             _round_us(rng.uniform(0.5, 3.0, len(post))), post_seg=post_seg))
+    n = n_hh + n_branch + n_izh
+    cols = [(g, 0) for g in range(n)] + [(int(b), 2) for b in br] + [(int(br[0]), 3)]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), seg) for g, seg in cols]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 CONFIGS = {
     "single_comp_hh": single_comp_hh,
     "multicomp_net": multicomp_net,
@@ -859,6 +925,7 @@ CONFIGS = {
     "input_kinds": input_kinds,
     "gate_kinds": gate_kinds,
     "voltage_clamps": voltage_clamps,
+    "gap_junctions": gap_junctions,
     "routing_probe": routing_probe,
     "random_sources": random_sources,
     "custom_setup": custom_setup,

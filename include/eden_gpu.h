@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 7
+#define EDEN_GPU_ABI_VERSION 8
 
 enum {
     EDEN_GPU_OK = 0,
@@ -256,6 +256,19 @@ typedef struct EdenGpuModel {
     const int32_t *clamp_target;
     const float *clamp_params;      /* [n_clamp * EDEN_CLAMP_PARAMS] */
     const float *clamp_weight;
+
+    /* gap junctions (gapJunction on electricalConnection(Instance)(W)): one
+     * entry per end, each on a physical compartment, taking
+     * weight * conductance * (V_peer - V) as synaptic current with the
+     * peer's potential at the start of the step and no conductance term
+     * (eden/Eden.cpp:3407-3422, 3689-3704; both ends 9233-9251).  Cells
+     * coupled this way influence each other within a step, so a model with
+     * gap junctions runs one-step windows. */
+    int64_t n_gap;
+    const int32_t *gap_target;      /* compartment the end sits on */
+    const int32_t *gap_peer;        /* compartment at the other end */
+    const float *gap_conductance;   /* uS */
+    const float *gap_weight;
 } EdenGpuModel;
 
 /* Execution options. */

@@ -150,6 +150,10 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         dm.clamp_target = g.copy(m->clamp_target, (size_t)m->n_clamp);
         dm.clamp_params = g.copy(m->clamp_params, (size_t)m->n_clamp * EDEN_CLAMP_PARAMS);
         dm.clamp_weight = g.copy(m->clamp_weight, (size_t)m->n_clamp);
+        dm.gap_target = g.copy(m->gap_target, (size_t)m->n_gap);
+        dm.gap_peer = g.copy(m->gap_peer, (size_t)m->n_gap);
+        dm.gap_conductance = g.copy(m->gap_conductance, (size_t)m->n_gap);
+        dm.gap_weight = g.copy(m->gap_weight, (size_t)m->n_gap);
         dm.pois_rng_base = m->pois_rng_base ? g.copy(m->pois_rng_base, (size_t)np) : nullptr;
         // the loop's state, set up on the host
         Port D = H;
@@ -186,6 +190,8 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         D.timed_cur = g.copy(H.timed_cur, (size_t)m->n_timed + 1);
         D.timed_tgt_off = g.copy(H.timed_tgt_off, (size_t)nt + 1);
         D.timed_order = g.copy(H.timed_order, (size_t)m->n_timed + 1);
+        D.gap_off = g.copy(H.gap_off, (size_t)nt + 1);
+        D.gap_order = g.copy(H.gap_order, (size_t)m->n_gap + 1);
         int32_t *d_tt = g.copy(trace_target, (size_t)n_trace);
         double *d_trace = g.zeros<double>((size_t)n_steps * (size_t)(n_trace > 0 ? n_trace : 1));
         int32_t *d_lsrc = g.zeros<int32_t>((size_t)spike_cap);

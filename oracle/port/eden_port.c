@@ -112,6 +112,7 @@ typedef struct {
     int64_t *timed_cur;                 /* next listed step of each timed input */
     int64_t *timed_tgt_off;             /* [n_target + 1] timed inputs by target */
     int64_t *timed_order;               /* inputs in target order */
+    int64_t *gap_off, *gap_order;       /* gap-junction ends by target, model order within one */
     unsigned char *spiked[2];           /* event-logger slot per source */
     real *diag;
     int64_t *gate_off;                  /* [n_chan + 1] */
@@ -399,6 +400,17 @@ static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, rea
             Ia += iw; Ga += gw;
         }
         Isyn += Ia; Gsyn += Ga;
+    }
+    /* gap junctions: each end adds (g (V_peer - V)) w with the peer's
+     * potential at the step's start, and no conductance term
+     * (eden/Eden.cpp:3407-3422 exposure, 3689-3704 Vpeer, 3708-3710 sum) */
+    if (P->gap_off[tgt] < P->gap_off[tgt + 1]) {
+        real Ia = R(0.0);
+        for (int64_t q = P->gap_off[tgt]; q < P->gap_off[tgt + 1]; q++) {
+            const int64_t k = P->gap_order[q];
+            Ia += ((real)m->gap_conductance[k] * (P->v[cur][m->gap_peer[k]] - v)) * (real)m->gap_weight[k];
+        }
+        Isyn += Ia;
     }
     *I_in = Iin; *G_in = Gin; *I_syn = Isyn; *G_syn = Gsyn;
 }
@@ -723,6 +735,16 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
     P.wave_off = csr_by_key(m->wave_target, m->n_wave, nt);
     P.clamp_off = csr_by_key(m->clamp_target, m->n_clamp, nt);
     P.fan_off = csr_by_key(m->syn_src, ns, m->n_src);
+    P.gap_off = csr_by_key(m->gap_target, m->n_gap, nt);
+    P.gap_order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m->n_gap + 1));
+    {
+        int64_t *fill = (int64_t *)calloc((size_t)nt + 1, sizeof(int64_t));
+        for (int64_t k = 0; k < m->n_gap; k++) {
+            int32_t t = m->gap_target[k];
+            P.gap_order[P.gap_off[t] + fill[t]++] = k;
+        }
+        free(fill);
+    }
     P.fan_syn = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ns + 1));
     {
         int64_t *fill = (int64_t *)calloc((size_t)m->n_src + 1, sizeof(int64_t));
@@ -752,7 +774,7 @@ static void port_free(Port *P) {
     }
     free(P->diag); free(P->syn_fire_count); free(P->gate_off); free(P->syn_off); free(P->pois_off);
     free(P->pulse_off); free(P->wave_off); free(P->clamp_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
-    free(P->timed_cur); free(P->timed_tgt_off); free(P->timed_order);
+    free(P->timed_cur); free(P->timed_tgt_off); free(P->timed_order); free(P->gap_off); free(P->gap_order);
 }
 
 /* Wall-clock marks for timing a stretch of a run (the CPU timings beside

@@ -23,6 +23,7 @@ CASES = {
     "random_sources": ("random_sources", dict(), 1.0, None),
     "custom_setup": ("custom_setup", dict(), 1.0, None),
     "dl_inputs": ("dl_inputs", dict(), 1.0, None),
+    "gap_junctions": ("gap_junctions", dict(), 1.0, None),
 }
 
 

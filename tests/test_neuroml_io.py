@@ -28,6 +28,7 @@ def _same(a, b):
     ("multicomp_net", dict(n_cells=6, in_degree=4, length_ms=5.0, max_seg=30)),
     ("izh_net", dict(n_cells=20, in_degree=5, length_ms=5.0)),
     ("ball_and_stick", dict(n_inst=3, length_ms=5.0)),
+    ("gap_junctions", dict(length_ms=5.0)),
 ])
 def test_write_read_round_trip(tmp_path, name, kw):
     spec = workloads.CONFIGS[name](**kw)
@@ -57,3 +58,39 @@ def test_units_follow_reference_scales(tmp_path):
     b = lowering.lower(neuroml_io.read_lems(path))
     np.testing.assert_allclose(a.chan_gbase, b.chan_gbase, rtol=1e-7)
     np.testing.assert_allclose(a.chan_erev, b.chan_erev, rtol=1e-7)
+
+
+def test_electrical_connection_forms(tmp_path):
+    """electricalConnection (cell indices, weight 1) and conductances in pS
+    read as the weighted instance form with nS does."""
+    spec = workloads.gap_junctions(length_ms=5.0)
+    path = neuroml_io.write_lems(spec, str(tmp_path))
+    nml = tmp_path / f"{spec.name}.nml"
+    text = nml.read_text().replace('conductance="4.0nS"', 'conductance="4000.0pS"')
+    nml.write_text(text)
+    a = lowering.lower(spec)
+    b = lowering.lower(neuroml_io.read_lems(path))
+    assert _same(a, b) == []
+    # the index form: preCell="i", no weight
+    import re
+    text = re.sub(r'<electricalConnectionInstanceW id="(\d+)" preCell="\.\./\w+/(\d+)/\w+" preSegment="(\d+)" '
+                  r'postCell="\.\./\w+/(\d+)/\w+" postSegment="(\d+)" synapse="(\w+)" weight="[^"]*"/>',
+                  r'<electricalConnection id="\1" preCell="\2" preSegment="\3" postCell="\4" postSegment="\5" '
+                  r'synapse="\6"/>', text)
+    assert "electricalConnectionInstanceW" not in text
+    nml.write_text(text)
+    c = lowering.lower(neuroml_io.read_lems(path))
+    np.testing.assert_array_equal(c.gap_target, a.gap_target)
+    np.testing.assert_array_equal(c.gap_peer, a.gap_peer)
+    np.testing.assert_array_equal(c.gap_conductance, a.gap_conductance)
+    np.testing.assert_array_equal(c.gap_weight, np.ones_like(a.gap_weight))
+
+
+def test_gap_junctions_on_point_neurons_fail_loudly():
+    from eden_gb300.network import ElectricalProjection
+    spec = workloads.gap_junctions(length_ms=5.0)
+    iz = spec.populations[0].size + spec.populations[1].size
+    spec.electrical.append(ElectricalProjection("bad", "gap_weak", np.array([0]), np.array([0]), np.array([iz]),
+                                                np.array([0]), np.array([1.0])))
+    with pytest.raises(ValueError, match="physical cells"):
+        lowering.lower(spec)
