@@ -751,7 +751,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         }
     }
 
-    // windowed-path constants (see DevModel::c_kc): a compartment is flat when
+    // windowed-path constants (see DevModel::c_kl): a compartment is flat when
     // it has one gateless channel and no inputs, is no spike source, and every
     // compartment below it is flat; its pivot and elimination factor are then
     // the same every step and are computed here once, deepest first
@@ -783,6 +783,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             }
         }
     }
+    // a flat compartment's pre-update increment, or a non-flat one's L
+    std::vector<float> c_kl(nt, 0.f);
+    for (int it = 0; it < nt; it++) c_kl[it] = nonflat[it] ? c_l[it] : c_kc[it];
 
     // per forest depth (parallel to lvl): non-flat flag
     std::vector<uint8_t> lvl_info(lvl.size(), 0);
@@ -1201,7 +1204,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.c_cm, c_cm)); TRY(upload_c(ctx, &d.c_inv_rc, c_inv)); TRY(upload_c(ctx, &d.c_area, c_area));
     TRY(upload_c(ctx, &d.c_u, c_u)); TRY(upload_c(ctx, &d.c_l, c_l));
     TRY(upload_c(ctx, &d.c_cend, c_cend)); TRY(upload_c(ctx, &d.c_parent, c_parent));
-    TRY(upload_c(ctx, &d.c_kc, c_kc)); TRY(upload_c(ctx, &d.c_pv0, c_pv0));
+    TRY(upload_c(ctx, &d.c_kl, c_kl)); TRY(upload_c(ctx, &d.c_pv0, c_pv0));
     TRY(upload_c(ctx, &d.c_rt0, c_rt0)); TRY(upload_c(ctx, &d.c_cep, c_cep)); TRY(upload_c(ctx, &d.t_izh, t_izh));
     TRY(upload_c(ctx, &d.fo_t0, fo_t0)); TRY(upload_c(ctx, &d.fo_t1, fo_t1)); TRY(upload_c(ctx, &d.fo_l0, fo_l0));
     TRY(upload_c(ctx, &d.fo_nlev, fo_nlev)); TRY(upload_c(ctx, &d.lvl, lvl));

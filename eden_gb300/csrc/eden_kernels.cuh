@@ -99,14 +99,15 @@ struct DevModel {
     // windowed-path constants of each physical compartment.  A "flat"
     // compartment has one gateless channel, no inputs, is no spike source and
     // has only flat compartments below it; everything else is "non-flat".
-    //   c_kc   flat: the pre-update increment dt*(G*E)/C (V' = V + c_kc, the
-    //          reference's V + dt*(I + V*G)/C with I = G*(E - V)); non-flat: 0
+    //   c_kl   flat: the pre-update increment dt*(G*E)/C (V' = V + c_kl, the
+    //          reference's V + dt*(I + V*G)/C with I = G*(E - V)); non-flat:
+    //          its L (its elimination factor is L / pivot, rebuilt each step)
     //   c_pv0  flat: reciprocal of its Hines pivot, which is the same every
     //          step because nothing below it changes; non-flat: unused
     //   c_rt0  flat: L / pivot, its elimination factor into its parent
     //   c_cep  child-range end | child-range begin << 10 | (parent + 1) << 20
     //          | non-flat << 30, all local to the compartment's forest
-    const float *c_kc, *c_pv0, *c_rt0;
+    const float *c_kl, *c_pv0, *c_rt0;
     const uint32_t *c_cep;
     // forests: physical compartments [fo_t0, fo_t1), depth boundaries lvl[fo_l0 .. fo_l0 + fo_nlev]
     const int32_t *fo_t0, *fo_t1, *fo_l0, *fo_nlev, *lvl;
@@ -248,9 +249,10 @@ constexpr uint32_t kCepNonFlat = 1u << 30;
 constexpr int kGateWords = 9;  // gate parameter record (gate_next_p)
 constexpr int kGateExtWords = 9;  // a non-rates gate's kind and timeCourse / steadyState forms
 
-// Shared-memory words of a unit's slice in the windowed kernel.  A forest:
-// 7 per compartment (V, c_kc, L, pivot, elimination factor, U, packed
-// child range/parent/flag), 10 per non-flat compartment (local index, V at
+// Shared-memory words of a unit's slice in the windowed kernel (an even
+// count, so that every slice starts 8-byte aligned).  A forest: 6 per
+// compartment in three pairs (V and elimination factor; c_kl and the packed
+// child range/parent/flag; U and pivot), 10 per non-flat compartment (local index, V at
 // the step start, area, C, sum of 1/(R C), input-block range, channel
 // range, channel set), 4 per channel of a non-flat compartment, 11 per gate (value,
 // non-flat slot, parameter record), the depth boundaries, 3 per spike
@@ -262,10 +264,11 @@ __host__ __device__ inline int forest_words(int n, int nf, int nfch, int ngt, in
                                             int kcap, bool f64 = false) {
     // a double-precision forest adds its eliminated values, pivots and
     // factors in double (6 words per compartment, 8-byte aligned)
-    return 7 * n + 10 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck +
-           (f64 ? 6 * n + 2 : 0);
+    const int w = 6 * n + 10 * nf + 4 * nfch + (2 + kGateWords) * ngt + (nlev + 1) + 3 * ns + 3 * nblk + 1 + kcap * nck +
+                  (f64 ? 6 * n + 2 : 0);
+    return (w + 1) & ~1;
 }
-__host__ __device__ inline int izh_words(int n) { return (2 + EDEN_POINT_PARAMS + 3) * n + 1; }
+__host__ __device__ inline int izh_words(int n) { return ((2 + EDEN_POINT_PARAMS + 3) * n + 1 + 1) & ~1; }
 
 // Per-window arguments: the window covers steps [step0, step0 + K); steps
 // <= 0 are initialisation passes.  The previous window began at step
@@ -299,6 +302,17 @@ __device__ __forceinline__ float warp_sum(float x) {
 // ---------------------------------------------------------------------------
 // NaN: a spike with no interpolated crossing time
 __device__ __forceinline__ double no_time() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+// Staging copies: one 4-byte word from global to shared memory without a
+// register round trip (cp.async), so that all of a lane's staging loads are
+// in flight together; stage_wait() waits for the lane's copies, and a
+// __syncwarp() after it publishes them to the warp.
+__device__ __forceinline__ void stage_word(void *smem_dst, const void *gmem_src) {
+    unsigned s;
+    asm("{\n .reg .u64 a;\n cvta.to.shared.u64 a, %1;\n cvt.u32.u64 %0, a;\n}" : "=r"(s) : "l"(smem_dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ void push_spike(const DevModel &m, bool spiked, int32_t src, int32_t log_step,
                                            int wpar, double tcross) {
@@ -438,6 +452,12 @@ __device__ __forceinline__ void pois_window(const DevModel &m, int64_t it, const
             isi = pois_draw(m, it, w.step0 + j, 0);
         }
     } else if (m.pois_exact && isi < 0x1p23f) {
+        // (exact sums: no firing in the window when even its last step's
+        // time since the spike stays within the interval)
+        if (ts + (float)(w.K - 1) * dt <= isi) {
+            m.po_ts[it] = ts + (float)w.K * dt;
+            return;
+        }
         int j = 0;
         while (true) {
             // first step from j on whose time since the last spike exceeds isi
@@ -1128,61 +1148,67 @@ __device__ __forceinline__ void hines_forest_f64(const DevModel &m, bool init, i
 }
 
 // Backward-Euler Hines solve of one forest by one warp for the windowed path,
-// on the unit's shared-memory slice (eden/Eden.cpp:6114-6225).  Flat
-// compartments keep the reciprocal pivot PV and the elimination factor RT
-// = L / pivot computed once, because their diagonals never change, and
-// their pre-update (V += KC) is folded into the elimination; a non-flat
-// compartment's pivot is rebuilt every step from its diagonal (PV holds
-// G/C + sum 1/(RC) on entry, X its pre-updated V) and its children's
-// factors, in increasing child order as the reference's post-order visits
-// them.  A depth's compartments are spread over the lanes (at most 64 per
-// depth, two per lane, unless a single cell is wider); LV packs each depth's first
-// compartment and whether it holds a non-flat one.
-// Back-substitution runs root-first.  X holds V_next on return.
+// on the unit's shared-memory slice (eden/Eden.cpp:6114-6225), whose
+// compartment terms sit in pairs so that one load brings two: XR (V, the
+// elimination factor), KL (c_kl, the packed child range / parent / non-flat
+// flag) and UP (U, the pivot).  Flat compartments keep the reciprocal pivot
+// and the elimination factor L / pivot computed once, because their
+// diagonals never change, and their pre-update (V += c_kl) is folded into
+// the elimination; a non-flat compartment's pivot is rebuilt every step
+// from its diagonal (UP.y holds G/C + sum 1/(RC) on entry, XR.x its
+// pre-updated V) and its children's factors, in increasing child order as
+// the reference's post-order visits them, and its factor from its L
+// (KL.x).  The forest's levels (LV: each level's first compartment and
+// whether it holds a non-flat one) put every compartment below its parent;
+// the elimination runs from the last level to the roots of level 0, a
+// level's compartments over the lanes, then the back-substitution runs
+// root-first.  XR.x holds V_next on return.
 constexpr int32_t kLvMask = 0xffff;
 constexpr int32_t kLvNonFlat = 1 << 16;
-__device__ __forceinline__ void hines_window(float dt, float *X, const float *KC, const float *L, float *PV,
-                                             float *RT, const float *U, const uint32_t *CEP, const int32_t *LV,
+__device__ __forceinline__ void hines_window(float dt, float2 *XR, const uint2 *KL, float2 *UP, const int32_t *LV,
                                              int nlev) {
     const int lane = threadIdx.x & 31;
     int end = LV[nlev] & kLvMask;
     for (int lev = nlev - 1; lev >= 0; lev--) {
         const int32_t lw = LV[lev];
-        // a depth holds at most 64 compartments unless one cell alone is wider
+        // a level wider than the warp takes two or more passes
         for (int j = (lw & kLvMask) + lane; j < end; j += 32) {
-            const uint32_t cep = CEP[j];
+            const uint2 kl = KL[j];
+            const uint32_t cep = kl.y;
             const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
-            float xj = X[j] + KC[j];
             if ((lw & kLvNonFlat) && (cep & kCepNonFlat)) {
-                float dj = 1.0f + PV[j] * dt;
+                float xj = XR[j].x + 0.0f;
+                float dj = 1.0f + UP[j].y * dt;
                 for (int i = kb; i < ke; i++) {
-                    const float r = RT[i];
-                    dj -= r * U[i];
-                    xj -= r * X[i];
+                    const float2 c = XR[i];
+                    dj -= c.y * UP[i].x;
+                    xj -= c.y * c.x;
                 }
                 const float inv = __fdividef(1.0f, dj);
-                PV[j] = inv;
-                RT[j] = L[j] * inv;
+                UP[j].y = inv;
+                XR[j] = make_float2(xj, __uint_as_float(kl.x) * inv);
             } else {
+                float xj = XR[j].x + __uint_as_float(kl.x);
                 // most compartments have at most two children: take those
                 // without a loop, in order
                 int i = kb;
-                if (i < ke) xj -= RT[i] * X[i];
-                if (i + 1 < ke) xj -= RT[i + 1] * X[i + 1];
-                for (i = kb + 2; i < ke; i++) xj -= RT[i] * X[i];
+                if (i < ke) { const float2 c = XR[i]; xj -= c.y * c.x; }
+                if (i + 1 < ke) { const float2 c = XR[i + 1]; xj -= c.y * c.x; }
+                for (i = kb + 2; i < ke; i++) { const float2 c = XR[i]; xj -= c.y * c.x; }
+                XR[j].x = xj;
             }
-            X[j] = xj;
         }
         end = lw & kLvMask;
         __syncwarp();
     }
-    for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) X[r] = X[r] * PV[r];
+    for (int r = (LV[0] & kLvMask) + lane; r < (LV[1] & kLvMask); r += 32) XR[r].x = XR[r].x * UP[r].y;
     __syncwarp();
     for (int lev = 1; lev < nlev; lev++) {
         const int i1 = LV[lev + 1] & kLvMask;
         for (int i = (LV[lev] & kLvMask) + lane; i < i1; i += 32) {
-            const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
-            X[i] = (X[i] - U[i] * X[p]) * PV[i];
+            const int p = (int)((KL[i].y >> kCepParentShift) & kCepMask) - 1;
+            const float2 up = UP[i];
+            XR[i].x = (XR[i].x - up.x * XR[p].x) * up.y;
         }
         __syncwarp();
     }
@@ -1190,31 +1216,34 @@ __device__ __forceinline__ void hines_window(float dt, float *X, const float *KC
 
 // hines_window in double precision, for a forest whose rows may lose
 // diagonal dominance: every compartment's pivot is rebuilt each step from
-// its diagonal term (PV: G/C + sum 1/(RC), the flat ones' constant one staged
+// its diagonal term (UP.y: G/C + sum 1/(RC), the flat ones' constant one staged
 // from c_d0), and the elimination and back-substitution carry doubles in
-// XD / PVD / RTD; X receives V_next rounded once.  The operations are
-// hines_window's, in its order.
-__device__ __forceinline__ void hines_window_f64(float dt, float *X, const float *KC, const float *L, const float *PV,
-                                                 const float *U, const uint32_t *CEP, const int32_t *LV, int nlev,
-                                                 double *XD, double *PVD, double *RTD) {
+// XD / PVD / RTD; XR.x receives V_next rounded once.  A flat compartment's
+// pre-update is its c_kl, and every compartment's L comes from Lg (global,
+// indexed like the forest).  The operations are hines_window's, in its order.
+__device__ __forceinline__ void hines_window_f64(float dt, float2 *XR, const uint2 *KL, const float2 *UP,
+                                                 const float *Lg, const int32_t *LV, int nlev, double *XD,
+                                                 double *PVD, double *RTD) {
     const int lane = threadIdx.x & 31;
     const double dtd = dt;
     int end = LV[nlev] & kLvMask;
     for (int lev = nlev - 1; lev >= 0; lev--) {
         const int32_t lw = LV[lev];
         for (int j = (lw & kLvMask) + lane; j < end; j += 32) {
-            const uint32_t cep = CEP[j];
+            const uint2 kl = KL[j];
+            const uint32_t cep = kl.y;
             const int ke = (int)(cep & kCepMask), kb = (int)((cep >> kCepBeginShift) & kCepMask);
-            double xj = (double)X[j] + (double)KC[j];
-            double dj = 1.0 + (double)PV[j] * dtd;
+            const float kc = (cep & kCepNonFlat) ? 0.0f : __uint_as_float(kl.x);
+            double xj = (double)XR[j].x + (double)kc;
+            double dj = 1.0 + (double)UP[j].y * dtd;
             for (int i = kb; i < ke; i++) {
                 const double r = RTD[i];
-                dj -= r * (double)U[i];
+                dj -= r * (double)UP[i].x;
                 xj -= r * XD[i];
             }
             const double inv = 1.0 / dj;
             PVD[j] = inv;
-            RTD[j] = (double)L[j] * inv;
+            RTD[j] = (double)Lg[j] * inv;
             XD[j] = xj;
         }
         end = lw & kLvMask;
@@ -1225,13 +1254,13 @@ __device__ __forceinline__ void hines_window_f64(float dt, float *X, const float
     for (int lev = 1; lev < nlev; lev++) {
         const int i1 = LV[lev + 1] & kLvMask;
         for (int i = (LV[lev] & kLvMask) + lane; i < i1; i += 32) {
-            const int p = (int)((CEP[i] >> kCepParentShift) & kCepMask) - 1;
-            XD[i] = (XD[i] - (double)U[i] * XD[p]) * PVD[i];
+            const int p = (int)((KL[i].y >> kCepParentShift) & kCepMask) - 1;
+            XD[i] = (XD[i] - (double)UP[i].x * XD[p]) * PVD[i];
         }
         __syncwarp();
     }
     const int n = LV[nlev] & kLvMask;
-    for (int i = lane; i < n; i += 32) X[i] = (float)XD[i];
+    for (int i = lane; i < n; i += 32) XR[i].x = (float)XD[i];
     __syncwarp();
 }
 

@@ -22,8 +22,9 @@ constexpr int kHinesThreads = 128;  // k_hines_t: four warps, each staging one f
 namespace eden {
 
 // Phase 1 of both paths: input blocks over the window, one warp per target
-// with inputs (the per-step path runs it with K = 1).
-__global__ void __launch_bounds__(kInputThreads) k_inputs_t(DevModel m, const WindowArgs *tab,
+// with inputs (the per-step path runs it with K = 1).  Six blocks fit an SM
+// by their event tiles; the register bound lets all six run.
+__global__ void __launch_bounds__(kInputThreads, 6) k_inputs_t(DevModel m, const WindowArgs *tab,
                                                              const WindowTimes *ttab, const int *base, int idx) {
     __shared__ float tiles[kInputThreads / 32][2][32 * kAccStride];
     __shared__ float tk[64];  // the window's step times, then the previous window's
@@ -178,9 +179,13 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     const int nlev = m.fo_nlev[fi], l0 = m.fo_l0[fi];
     const int ub0 = m.t_blk0[t0], nblk = m.t_blk0[t0 + n] - ub0;
     const int uc0 = m.bk_c0[ub0], nck = m.bk_c0[ub0 + nblk] - uc0;
-    float *X = S, *KC = S + n, *L = S + 2 * n, *PV = S + 3 * n, *RT = S + 4 * n, *U = S + 5 * n;
-    uint32_t *CEP = (uint32_t *)(S + 6 * n);
-    int32_t *NT = (int32_t *)(S + 7 * n);
+    // compartment terms in pairs (the slice is 8-byte aligned): V and the
+    // elimination factor, c_kl and the packed child range / parent / flag, U
+    // and the pivot
+    float2 *XR = reinterpret_cast<float2 *>(S);
+    uint2 *KL = reinterpret_cast<uint2 *>(S + 2 * n);
+    float2 *UP = reinterpret_cast<float2 *>(S + 4 * n);
+    int32_t *NT = (int32_t *)(S + 6 * n);
     float *VO = (float *)(NT + nf), *NA = VO + nf, *NC = NA + nf, *NIR = NC + nf;
     int32_t *NB0 = (int32_t *)(NIR + nf), *NB1 = NB0 + nf, *NCH0 = NB1 + nf, *NCH1 = NCH0 + nf;
     int32_t *NSIG = NCH1 + nf;
@@ -203,60 +208,67 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     double *PVD = XD + n, *RTD = PVD + n;
     // ---- stage the unit
     const float *vsrc = m.v[w.par];
+    const float *pv0 = f64 ? m.c_d0 : m.c_pv0;
     for (int i = lane; i < n; i += 32) {
         const int t = t0 + i;
-        X[i] = vsrc[t]; KC[i] = m.c_kc[t]; L[i] = m.c_l[t]; PV[i] = f64 ? m.c_d0[t] : m.c_pv0[t];
-        RT[i] = m.c_rt0[t]; U[i] = m.c_u[t]; CEP[i] = m.c_cep[t];
+        stage_word(&XR[i].x, &vsrc[t]); stage_word(&XR[i].y, &m.c_rt0[t]);
+        stage_word(&KL[i].x, &m.c_kl[t]); stage_word(&KL[i].y, &m.c_cep[t]);
+        stage_word(&UP[i].x, &m.c_u[t]); stage_word(&UP[i].y, &pv0[t]);
     }
     for (int j = lane; j < nf; j += 32) {
         const int ti = m.nf_t[nf0 + j], t = t0 + ti;
-        NT[j] = ti; NA[j] = m.c_area[t]; NC[j] = m.c_cm[t]; NIR[j] = m.c_inv_rc[t];
+        NT[j] = ti;
+        stage_word(&NA[j], &m.c_area[t]); stage_word(&NC[j], &m.c_cm[t]); stage_word(&NIR[j], &m.c_inv_rc[t]);
         NB0[j] = m.t_blk0[t] - ub0; NB1[j] = m.t_blk0[t + 1] - ub0;
         const int ch0 = m.c_chan0[t], ch1 = m.c_chan0[t + 1];
         NCH0[j] = m.nf_c0[nf0 + j] - uch0; NCH1[j] = m.nf_c1[nf0 + j] - uch0;
-        NSIG[j] = m.nf_sig[nf0 + j];
+        stage_word(&NSIG[j], &m.nf_sig[nf0 + j]);
         // gate update items: the non-flat slot and the gate's parameter record
         for (int ch = ch0; ch < ch1; ch++) {
             const int q0 = m.ch_gate0[ch] - gt0, q1 = m.ch_gate0[ch + 1] - gt0;
             const float *src = m.gate_par + (size_t)m.ch_type[ch] * EDEN_MAX_GATES * kGateWords;
             for (int q = q0; q < q1; q++) {
                 GI_S[q] = j;
-                for (int k = 0; k < kGateWords; k++) GP[q * kGateWords + k] = src[(q - q0) * kGateWords + k];
+                for (int k = 0; k < kGateWords; k++) stage_word(&GP[q * kGateWords + k], &src[(q - q0) * kGateWords + k]);
             }
         }
     }
     for (int c = lane; c < nch; c += 32) {
-        CHG[c] = m.nfc_g[uch0 + c]; CHE[c] = m.nfc_e[uch0 + c]; CHQ[c] = m.nfc_q[uch0 + c]; CHI[c] = m.nfc_i[uch0 + c];
+        stage_word(&CHG[c], &m.nfc_g[uch0 + c]); stage_word(&CHE[c], &m.nfc_e[uch0 + c]);
+        stage_word(&CHQ[c], &m.nfc_q[uch0 + c]); stage_word(&CHI[c], &m.nfc_i[uch0 + c]);
     }
-    for (int i = lane; i < ngt; i += 32) GT[i] = m.gate[gt0 + i];
+    for (int i = lane; i < ngt; i += 32) stage_word(&GT[i], &m.gate[gt0 + i]);
     for (int i = lane; i <= nlev; i += 32) {
         const int info = m.lvl_info[l0 + i];
         LV[i] = (m.lvl[l0 + i] - t0) | ((info & 0x80) ? kLvNonFlat : 0);
     }
-    for (int i = lane; i < ns; i += 32) { ST[i] = m.gs_t[s0 + i]; SSRC[i] = m.gs_src[s0 + i]; STHR[i] = m.gs_thr[s0 + i]; }
+    for (int i = lane; i < ns; i += 32) {
+        stage_word(&ST[i], &m.gs_t[s0 + i]); stage_word(&SSRC[i], &m.gs_src[s0 + i]); stage_word(&STHR[i], &m.gs_thr[s0 + i]);
+    }
     for (int b = lane; b <= nblk; b += 32) {
         BKC[b] = m.bk_c0[ub0 + b] - uc0;
-        if (b < nblk) { BKK[b] = m.bk_kind[ub0 + b]; BKE[b] = m.bk_erev[ub0 + b]; }
+        if (b < nblk) { stage_word(&BKK[b], &m.bk_kind[ub0 + b]); stage_word(&BKE[b], &m.bk_erev[ub0 + b]); }
     }
     for (int k = 0; k < w.K; k++)
-        for (int c = lane; c < nck; c += 32) GS[k * nck + c] = m.Gp[(size_t)k * m.n_chunk + uc0 + c];
+        for (int c = lane; c < nck; c += 32) stage_word(&GS[k * nck + c], &m.Gp[(size_t)k * m.n_chunk + uc0 + c]);
+    stage_wait();
     __syncwarp();
     const float dt = m.dt;
     double tstep = w.t0;  // this step's time, accumulated in double as the host does
     for (int k = 0; k < w.K; k++) {
         const int64_t step = w.step0 + k;
         const bool init = step <= 0;
-        if (!init) {
+        if (!init && r1 > r0) {
             // trajectory samples of this step's starting state
             const int64_t row = (step - 1) % m.trace_cap;
-            for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = X[m.gr_t[q]];
+            for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = XR[m.gr_t[q]].x;
         }
         __syncwarp();
         const float *Gk = GS + k * nck;
         for (int j = lane; j < nf; j += 32) {
             // channels + voltage pre-update (eden/Eden.cpp:5013-6107)
             const int ti = NT[j];
-            const float v = X[ti];
+            const float v = XR[ti].x;
             VO[j] = v;
             float Iin, Gin, Isyn, Gsyn;
             block_currents(Gk, NB0[j], NB1[j], BKK, BKE, BKC, 0, v, Iin, Gin, Isyn, Gsyn);
@@ -285,19 +297,19 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             const float I = Ich + Iin + Isyn;
             const float G = Gch + Gin + Gsyn;
             const float C = NC[j];
-            PV[ti] = 1.0f * (G / C) + NIR[j];
-            X[ti] = init ? v : v + (dt * (I + (v * G))) / C;
+            UP[ti].y = 1.0f * (G / C) + NIR[j];
+            XR[ti].x = init ? v : v + (dt * (I + (v * G))) / C;
         }
         __syncwarp();
         if (!init) {
-            if (f64) hines_window_f64(dt, X, KC, L, PV, U, CEP, LV, nlev, XD, PVD, RTD);
-            else hines_window(dt, X, KC, L, PV, RT, U, CEP, LV, nlev);
+            if (f64) hines_window_f64(dt, XR, KL, UP, m.c_l + t0, LV, nlev, XD, PVD, RTD);
+            else hines_window(dt, XR, KL, UP, LV, nlev);
         }
         // gate updates from this step's starting V and gate values (the
         // currents above used the values before the update, as the reference does)
         for (int q = lane; q < ngt; q += 32)
             GT[q] = gate_next_p(GP + q * kGateWords, m.gate_ext, init, dt, VO[GI_S[q]],
-                                EDEN_KIND_GATEFORMS ? X[NT[GI_S[q]]] : 0.0f, GT[q]);
+                                EDEN_KIND_GATEFORMS ? XR[NT[GI_S[q]]].x : 0.0f, GT[q]);
         // threshold crossings of the unit's spike sources (eden/Eden.cpp:6247-6252)
         for (int q0 = 0; q0 < ns; q0 += 32) {
             const int q = q0 + lane;
@@ -307,7 +319,7 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             if (q < ns) {
                 const int sl = ST[q];
                 src = SSRC[q];
-                const float vo = VO[sl], vn = X[NT[sl]];
+                const float vo = VO[sl], vn = XR[NT[sl]].x;
                 spk = vo < STHR[q] && STHR[q] < vn;
                 if (spk) tc = crossing_time(tstep, dt, vo, vn, STHR[q]);
             }
@@ -318,7 +330,7 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
     }
     // ---- write the unit back into the buffer that holds the window's final state
     float *vdst = m.v[w.par ^ (w.K & 1)];
-    for (int i = lane; i < n; i += 32) vdst[t0 + i] = X[i];
+    for (int i = lane; i < n; i += 32) vdst[t0 + i] = XR[i].x;
     for (int i = lane; i < ngt; i += 32) m.gate[gt0 + i] = GT[i];
 }
 
@@ -335,12 +347,13 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
     const int izh0 = m.t_izh[t0];
     for (int i = lane; i < n; i += 32) {
         const int iz = izh0 + i;
-        S[w.par * n + i] = m.v[w.par][t0 + i];
-        for (int f = 0; f < EDEN_POINT_PARAMS; f++) P[f * n + i] = m.iz_p[(size_t)f * m.n_izh + iz];
-        SU[i] = m.iz_u[iz];
-        SS[i] = m.iz_s[iz];
-        KIND[i] = m.iz_kind[iz];
+        stage_word(&S[w.par * n + i], &m.v[w.par][t0 + i]);
+        for (int f = 0; f < EDEN_POINT_PARAMS; f++) stage_word(&P[f * n + i], &m.iz_p[(size_t)f * m.n_izh + iz]);
+        stage_word(&SU[i], &m.iz_u[iz]);
+        stage_word(&SS[i], &m.iz_s[iz]);
+        stage_word(&KIND[i], &m.iz_kind[iz]);
     }
+    stage_wait();
     __syncwarp();
     int par = w.par;
     const float dt = m.dt;
@@ -367,7 +380,7 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
             src = m.t_src[t];
         }
         push_spike(m, spike && src >= 0, src, (int32_t)(step + 1), w.wpar, no_time());
-        if (!init) {
+        if (!init && r1 > r0) {
             const int64_t row = (step - 1) % m.trace_cap;
             for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = vin[m.gr_t[q]];
         }
@@ -387,7 +400,7 @@ __device__ __forceinline__ void izh_window(const DevModel &m, const WindowArgs &
 // the block finishes its unit before any starts on the next CTA.
 __global__ void __launch_bounds__(kCellThreads, 8) k_cells_t(DevModel m, const WindowArgs *tab, const WindowTimes *ttab,
                                                           const int *base, int idx, int cta_begin, int cta_end) {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     const WindowArgs w = tab[*base + idx];
     const float *tk = ttab[*base + idx].tk;
     const int warp = threadIdx.x >> 5;
