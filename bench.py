@@ -199,9 +199,10 @@ def adjoint_sample():
     against the trace of a second seeded parameter draw.  Times one forward
     (trace + checkpoints every 100 steps) and one backward (recomputed
     segments + adjoint) through edenGpuGrad*, the batched simulation of the
-    same network, and checks the gradient of the first 8 cells over the first
-    50 ms against the double-precision forward sensitivities (oracle/cable_grad.py)
-    contracted with the same trace gradient."""
+    same network, and checks the gradient of the first 16 cells against the
+    double-precision forward sensitivities (oracle/cable_grad.py) contracted
+    with the same trace gradient over the first 100 ms, and against central
+    differences of the single-precision forward over the whole 200 ms."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from cable_grad import Cable, loss_and_trace_grad
     from eden_gb300 import lowering, workloads
@@ -229,9 +230,17 @@ def adjoint_sample():
     sim.run()
     sim_ms = sim.device_ms
     sim.close()
-    # accuracy on a bounded sample: the whole run's 200 ms (80 recomputed
-    # segments) for the first 16 cells (the FP64 oracle is numpy on the host)
-    n_sub, sub_ms = 16, 200.0
+    # accuracy on a bounded sample of 16 cells.  (1) Against the FP64 forward
+    # sensitivities over the first 100 ms, where the single- and
+    # double-precision trajectories still agree within a fraction of a mV;
+    # later a spike can land one step apart in the two, and gradients taken
+    # along different trajectories no longer compare.  (2) Over the whole
+    # 200 ms, against central differences of the same single-precision
+    # forward, on the (cell, parameter) pairs where the loss is smooth at
+    # that scale: differences with relative steps 1e-3 and 3e-3 agree within
+    # 1 %.  A cell near its firing threshold gains or loses a spike under
+    # such a step; those pairs are counted, not compared.
+    n_sub, sub_ms = 16, 100.0
     sub = workloads.ball_and_stick(n_inst=n_sub, length_ms=sub_ms, params=spec.params[:n_sub])
     slow = lowering.lower(sub)
     spm = per_cell_density_map(slow, dens)
@@ -248,6 +257,32 @@ def adjoint_sample():
     _, dtr = cab.run(spm.values, slow.n_steps, srec, dirs)
     g64 = np.einsum("nc,jnc->cj", tg_s, dtr)
     rel = float((np.abs(grad_s - g64).max(0) / np.abs(g64).max(0)).max())
+    full = workloads.ball_and_stick(n_inst=n_sub, params=spec.params[:n_sub])
+    flow = lowering.lower(full)
+    fpm = per_cell_density_map(flow, dens)
+    gf = CableGradient(flow, fpm, rec_comp=srec)
+    tr_f = gf.forward(fpm.values).astype(np.float64)
+    tgt_f = target[:flow.n_steps, :n_sub]
+    _, tg_f = loss_and_trace_grad(tr_f, tgt_f)
+    grad_f = gf.backward(tg_f).reshape(-1, 7)
+    vals = np.asarray(fpm.values, np.float64)
+
+    def central(h):
+        fd = np.zeros((n_sub, 7))
+        for j in range(7):
+            lp = []
+            for sgn in (1.0, -1.0):
+                v = vals.copy()
+                v[j::7] *= 1.0 + sgn * h
+                t = gf.forward(v.astype(np.float32)).astype(np.float64)
+                lp.append(((t - tgt_f) ** 2).sum(0) / tr_f.size)
+            fd[:, j] = (lp[0] - lp[1]) / (2.0 * h * vals[j::7])
+        return fd
+    fd1, fd3 = central(1e-3), central(3e-3)
+    gf.close()
+    scale_j = np.abs(fd1).max(0)
+    smooth = np.abs(fd1 - fd3) <= 1e-2 * scale_j
+    rel_fd = np.abs(grad_f - fd1) / scale_j
     f_ms, b_ms = min(fwd), min(bwd)
     # the same cells with synaptic drive fixed in advance: 8 spike-list expTwo
     # connections per cell on the dendrite and 2 timed expOne inputs on the
@@ -298,7 +333,14 @@ def adjoint_sample():
             "grad_max_rel_err_vs_fp64": rel,
             "grad_check": f"first {n_sub} cells, first {sub_ms:g} ms: GPU adjoint vs double-precision forward "
                           "sensitivities contracted with the same trace gradient, per parameter, relative "
-                          "to that parameter's largest gradient"}
+                          "to that parameter's largest gradient",
+            "whole_run_vs_central_differences": {
+                "cells": n_sub, "ms": 200.0, "pairs": int(smooth.size), "smooth_pairs": int(smooth.sum()),
+                "max_rel_err_smooth": float(rel_fd[smooth].max()) if smooth.any() else None,
+                "median_rel_err_all": float(np.median(rel_fd)),
+                "check": "GPU adjoint vs central differences (relative step 1e-3) of the same FP32 forward, "
+                         "relative to each parameter's largest difference; smooth pairs: steps 1e-3 and "
+                         "3e-3 agree within 1 %"}}
 
 
 def scale_sample(dev: int):

@@ -1029,18 +1029,38 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     ctx->K = ctx->mode == EDEN_MODE_BATCHED ? std::max(1, std::min(kreq, kmax)) : 1;
 
     // ---- recording
+    // each column on its target's list, with the internal gate slot it
+    // records or -1 for the membrane potential
     int32_t n_trace = opt ? opt->n_trace : 0;
-    std::vector<int32_t> t_trace0(nt + 1, 0), trace_col(n_trace);
+    std::vector<int32_t> t_trace0(nt + 1, 0), trace_col(n_trace), trace_gate(n_trace, -1);
     {
-        std::vector<std::vector<int>> cols(nt);
+        std::vector<int64_t> ugate0(m->comp_chan_off[n_comp] + 1, 0);  // user gate numbering
+        for (int32_t ch = 0; ch < m->comp_chan_off[n_comp]; ch++)
+            ugate0[ch + 1] = ugate0[ch] + m->chan_types[m->chan_type[ch]].n_gates;
+        std::vector<std::vector<std::pair<int, int>>> cols(nt);
         for (int j = 0; j < n_trace; j++) {
-            int ut = opt->trace_target[j];
-            if (ut < 0 || ut >= nt) return ctx->fail(EDEN_GPU_E_INVALID, "trace column %d: bad target", j);
-            cols[u2i[ut]].push_back(j);
+            const int32_t code = opt->trace_target[j];
+            if (code >= 0) {
+                if (code >= nt) return ctx->fail(EDEN_GPU_E_INVALID, "trace column %d: bad target", j);
+                cols[u2i[code]].push_back({j, -1});
+                continue;
+            }
+            const int64_t g = -2 - (int64_t)code;
+            if (code == -1 || g >= ugate0.back())
+                return ctx->fail(EDEN_GPU_E_INVALID, "trace column %d: bad gate", j);
+            const int32_t ch = (int32_t)(std::upper_bound(ugate0.begin(), ugate0.end(), g) - ugate0.begin()) - 1;
+            const int32_t comp = (int32_t)(std::upper_bound(m->comp_chan_off, m->comp_chan_off + n_comp + 1, ch) -
+                                           m->comp_chan_off) - 1;
+            const int it = u2i[comp];
+            const int o = c_chan0[it] + (ch - m->comp_chan_off[comp]);
+            cols[it].push_back({j, ch_gate0[o] + (int)(g - ugate0[ch])});
         }
         for (int t = 0; t < nt; t++) t_trace0[t + 1] = t_trace0[t] + (int)cols[t].size();
         for (int t = 0; t < nt; t++)
-            for (size_t k = 0; k < cols[t].size(); k++) trace_col[t_trace0[t] + k] = cols[t][k];
+            for (size_t k = 0; k < cols[t].size(); k++) {
+                trace_col[t_trace0[t] + k] = cols[t][k].first;
+                trace_gate[t_trace0[t] + k] = cols[t][k].second;
+            }
     }
     ctx->n_trace = n_trace;
     ctx->trace_cap = (opt && opt->record_capacity_steps > 0) ? opt->record_capacity_steps : 4096;
@@ -1108,11 +1128,15 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     }
     for (int u = 0; u < n_unit; u++) {
         const int a = un_t0[u], b = un_t1[u];
+        un_gt0[u] = ch_gate0[c_chan0[a]];
+        // a unit's trace columns: its local target, or -1 - its local gate slot
         un_r0[u] = (int)gr_t.size();
         for (int t = a; t < b; t++)
-            for (int k = t_trace0[t]; k < t_trace0[t + 1]; k++) { gr_t.push_back(t - a); gr_col.push_back(trace_col[k]); }
+            for (int k = t_trace0[t]; k < t_trace0[t + 1]; k++) {
+                gr_t.push_back(trace_gate[k] < 0 ? t - a : -1 - (trace_gate[k] - un_gt0[u]));
+                gr_col.push_back(trace_col[k]);
+            }
         un_r1[u] = (int)gr_t.size();
-        un_gt0[u] = ch_gate0[c_chan0[a]];
         un_ngt[u] = ch_gate0[c_chan0[b]] - un_gt0[u];
         if (un_f[u] >= 0) {
             const int nblk = t_blk0[b] - t_blk0[a];
@@ -1306,6 +1330,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload(ctx, &d.log_count, (const unsigned long long *)nullptr, 1));
     d.log_cap = log_cap;
     TRY(upload_c(ctx, &d.t_trace0, t_trace0)); TRY(upload_c(ctx, &d.trace_col, trace_col));
+    TRY(upload_c(ctx, &d.trace_gate, trace_gate));
     d.n_trace = n_trace;
     TRY(upload(ctx, &d.trace_buf, (const float *)nullptr, (size_t)ctx->trace_cap * (size_t)std::max(n_trace, 1)));
     d.trace_cap = ctx->trace_cap;

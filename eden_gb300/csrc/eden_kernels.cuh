@@ -191,6 +191,7 @@ struct DevModel {
     int64_t log_cap;
     // trajectory recording: CSR target -> recorded columns
     const int32_t *t_trace0, *trace_col;
+    const int32_t *trace_gate;  // per listed column: the gate slot it records, or -1 for V
     int32_t n_trace;
     float *trace_buf;
     int64_t trace_cap;
@@ -202,6 +203,9 @@ struct DevModel {
     int32_t n_unit;
     const int32_t *un_t0, *un_t1, *un_f, *un_off, *un_gt0, *un_ngt, *un_s0, *un_s1, *un_r0, *un_r1;
     const int32_t *cta_u0;
+    // per unit: spike sources (gs_*) and trace columns [un_r0, un_r1): gr_t is
+    // the unit-local target, or -1 - the unit-local gate slot of a gate's
+    // state; gr_col the column
     const int32_t *gs_t, *gs_src, *gr_t, *gr_col;
     const float *gs_thr;
     // non-flat compartments of forest units: nf_t[un_nf0[u] .. un_nf1[u]) are
@@ -979,7 +983,8 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
     if (!init) {
         for (int k = m.t_trace0[t]; k < m.t_trace0[t + 1]; k++) {
             int64_t row = (step - 1) % m.trace_cap;
-            m.trace_buf[row * m.n_trace + m.trace_col[k]] = v;
+            const int gq = m.trace_gate[k];
+            m.trace_buf[row * m.n_trace + m.trace_col[k]] = gq < 0 ? v : m.gate[gq];
         }
     }
     int iz = m.t_izh[t];

@@ -261,7 +261,10 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
         if (!init && r1 > r0) {
             // trajectory samples of this step's starting state
             const int64_t row = (step - 1) % m.trace_cap;
-            for (int q = r0 + lane; q < r1; q += 32) m.trace_buf[row * m.n_trace + m.gr_col[q]] = XR[m.gr_t[q]].x;
+            for (int q = r0 + lane; q < r1; q += 32) {
+                const int32_t tq = m.gr_t[q];  // a compartment, or -1 - a gate slot
+                m.trace_buf[row * m.n_trace + m.gr_col[q]] = tq >= 0 ? XR[tq].x : GT[-1 - tq];
+            }
         }
         __syncwarp();
         const float *Gk = GS + k * nck;

@@ -196,14 +196,23 @@ def _cable_geometry(cell: PhysicalCell):
     n = cell.n_seg
     L = np.asarray(cell.seg_len, np.float64)
     d = np.asarray(cell.seg_diam, np.float64)
-    # floats of the XML coordinates, as the reference parses them
-    area = np.where(L == 0, np.pi * d * d, (np.pi / 2.0) * (d + d) * np.sqrt(L * L)).astype(F32)
+    dp = d if cell.seg_dprox is None else np.asarray(cell.seg_dprox, np.float64)
+    # floats of the XML coordinates, as the reference parses them; the
+    # lateral area of each segment's frustum (eden/Eden.cpp:241-253)
+    area = np.where(L == 0, np.pi * d * d,
+                    (np.pi / 2.0) * (dp + d) * np.sqrt((dp - d) * (dp - d) / 4.0 + L * L)).astype(F32)
     cm_native = _to_f32(cell.cm)                      # uF/cm2, native
     c = (area.astype(np.float64) * float(cm_native) * 1e-2).astype(F32)
     ra_native = _to_f32(cell.ra * 1e-3)               # ohm*cm -> kohm*cm
+    # each half's resistance as a frustum from its end to the midpoint
+    # diameter, Ra (4 / pi) length / (d_from d_to) (eden/Eden.cpp:4234-4241,
+    # 4304-4305); a zero-length segment as a cylinder as long as it is wide
     half = np.where(L == 0, d / 2.0, L / 2.0)
-    r_half = (float(ra_native) * (4.0 / np.pi) * half / (d * d) * 10.0).astype(F32)
-    r_prox, r_dist = r_half, r_half
+    dpf, ddf = dp.astype(F32), d.astype(F32)
+    dm = np.where(L == 0, ddf, dpf + (ddf - dpf) * F32(0.5)).astype(np.float64)
+    dpx = np.where(L == 0, d, dp)
+    r_prox = (float(ra_native) * (4.0 / np.pi) * half / (dpx * dm) * 10.0).astype(F32)
+    r_dist = (float(ra_native) * (4.0 / np.pi) * half / (dm * d) * 10.0).astype(F32)
     parent = np.asarray(cell.seg_parent, np.int64)
     r_axial = np.full(n, np.nan, dtype=F32)
     inv_rc = np.zeros(n, dtype=F32)
@@ -786,8 +795,34 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         perm = np.argsort(ct_, kind="stable")
         ct_, cpar, cwt = ct_[perm], cpar[perm], cwt[perm]
 
-    trace_target = np.array([target_of([gid_off[c.pop] + c.cell], [c.seg], current=False)[0]
-                             for c in spec.trace_columns], dtype=np.int32)
+    # a trace column records V of a target, or (code -2 - g) the state of gate
+    # g, gates numbered channel instance by channel instance in comp_chan_off
+    # order and within an instance in its type's gate order
+    chan_off_all = np.concatenate(chan_off).astype(np.int64)
+    chan_type_all = joined(chan_type, np.int32)
+    chan_dens_all = joined(chan_dens, np.int32)
+    gates_per_type = np.array([len(ch.gates) for ch in spec.channels] or [0], np.int64)
+    gate_base = np.concatenate([[0], np.cumsum(gates_per_type[chan_type_all])]) if len(chan_type_all) else np.zeros(1)
+
+    def trace_code(c):
+        t = int(target_of([gid_off[c.pop] + c.cell], [c.seg], current=False)[0])
+        if c.quantity == "v":
+            return t
+        dname, gname = c.quantity[2:].split("/")
+        ct = spec.cell_type(spec.population(c.pop).cell_type)
+        if not isinstance(ct, PhysicalCell):
+            raise ValueError(f"recorded gate {c.quantity} of {c.pop}[{c.cell}]: not a physical cell")
+        kd = [k for k, d in enumerate(ct.densities) if (d.name or f"cd{k}") == dname]
+        if not kd:
+            raise ValueError(f"recorded gate {c.quantity} of {c.pop}[{c.cell}]: no channelDensity {dname}")
+        inst = [i for i in range(chan_off_all[t], chan_off_all[t + 1]) if chan_dens_all[i] == kd[0]]
+        if not inst:
+            raise ValueError(f"recorded gate {c.quantity}: channelDensity {dname} is not on segment {c.seg}")
+        gnames = [g.name for g in spec.channels[chan_type_all[inst[0]]].gates]
+        if gname not in gnames:
+            raise ValueError(f"recorded gate {c.quantity}: the channel has no gate {gname}")
+        return -2 - int(gate_base[inst[0]] + gnames.index(gname))
+    trace_target = np.array([trace_code(c) for c in spec.trace_columns], dtype=np.int32)
     event_src = np.array([gid_off[e.pop] + e.cell for e in spec.event_selections], dtype=np.int32)
 
     izh_arr = np.asarray(izh, np.float64).astype(F32).reshape(-1, POINT_PARAMS)

@@ -92,21 +92,25 @@ def hh_channels() -> List[Channel]:
 @dataclass
 class ChannelDensity:
     """channelDensity: `channel` (index into NetworkSpec.channels) on the
-    segments whose mask is set, conductivity `cond` mS/cm2, reversal mV."""
+    segments whose mask is set, conductivity `cond` mS/cm2, reversal mV;
+    `name` is its id, which paths to its gates' states use."""
     channel: int
     cond: float
     erev: float
     seg_mask: np.ndarray  # bool per segment
+    name: str = ""
 
 
 @dataclass
 class PhysicalCell:
-    """A NeuroML <cell>: an unbranched-or-branched tree of cylindrical
-    segments, one compartment per segment.
+    """A NeuroML <cell>: an unbranched-or-branched tree of segments, one
+    compartment per segment.
 
     seg_parent[i] < i (root = segment 0 with parent -1).  Segment i runs from
-    its parent's distal point along +x by seg_len[i] um with constant
-    diameter seg_diam[i] um; a zero-length root is a sphere of that diameter.
+    its parent's distal point along +x by seg_len[i] um, a frustum from
+    diameter seg_dprox[i] (proximal; None: seg_diam throughout, a cylinder)
+    to seg_diam[i] um (distal); a zero-length root is a sphere of its distal
+    diameter.
     """
     name: str
     seg_parent: np.ndarray
@@ -118,6 +122,7 @@ class PhysicalCell:
     v0: float = -65.0          # mV
     spike_thresh: float = -20.0  # mV
     seg_groups: dict = field(default_factory=dict)  # name -> bool mask (for writing)
+    seg_dprox: Optional[np.ndarray] = None  # proximal diameters, um
 
     @property
     def n_seg(self) -> int:
@@ -382,7 +387,7 @@ class OutputColumn:
     pop: str
     cell: int
     seg: int
-    quantity: str = "v"   # only membrane potential is recorded
+    quantity: str = "v"   # "v", or "q:<channelDensity id>/<gate id>" for a gate's state
 
 
 @dataclass

@@ -336,6 +336,11 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
 
 def _quantity_path(spec, col: OutputColumn) -> str:
     ct = spec.cell_type(spec.population(col.pop).cell_type)
+    if isinstance(ct, PhysicalCell) and col.quantity.startswith("q:"):
+        dname, gate = col.quantity[2:].split("/")
+        k = next(k for k, d in enumerate(ct.densities) if (d.name or f"cd{k}") == dname)
+        chan = spec.channels[ct.densities[k].channel].name
+        return f"{col.pop}/{col.cell}/{ct.name}/{col.seg}/bio/membraneProperties/{dname}/{chan}/{gate}/q"
     if isinstance(ct, PhysicalCell):
         return f"{col.pop}/{col.cell}/{ct.name}/{col.seg}/v"
     # a fitzHughNagumoCell's membrane variable is the dimensionless V
@@ -351,19 +356,20 @@ def _select_path(spec, ev: EventSelection) -> str:
 
 def _write_cell(w, spec: NetworkSpec, c: PhysicalCell) -> None:
     w(f'<cell id="{c.name}">\n <morphology id="{c.name}_morph">\n')
-    # cylinders laid out along +x from the parent's distal point
+    # segments laid out along +x from the parent's distal point
     dist_x = np.zeros(c.n_seg)
+    dprox = c.seg_diam if c.seg_dprox is None else c.seg_dprox
     for i in range(c.n_seg):
         p = int(c.seg_parent[i])
         x0 = 0.0 if p < 0 else dist_x[p]
         dist_x[i] = x0 + float(c.seg_len[i])
         if p < 0:
             w(f'  <segment id="{i}" name="seg{i}">\n'
-              f'   <proximal x="{_f(x0)}" y="0" z="0" diameter="{_f(c.seg_diam[i])}"/>\n'
+              f'   <proximal x="{_f(x0)}" y="0" z="0" diameter="{_f(dprox[i])}"/>\n'
               f'   <distal x="{_f(dist_x[i])}" y="0" z="0" diameter="{_f(c.seg_diam[i])}"/>\n  </segment>\n')
         else:
             w(f'  <segment id="{i}" name="seg{i}">\n   <parent segment="{p}"/>\n'
-              f'   <proximal x="{_f(x0)}" y="0" z="0" diameter="{_f(c.seg_diam[i])}"/>\n'
+              f'   <proximal x="{_f(x0)}" y="0" z="0" diameter="{_f(dprox[i])}"/>\n'
               f'   <distal x="{_f(dist_x[i])}" y="0" z="0" diameter="{_f(c.seg_diam[i])}"/>\n  </segment>\n')
     groups = dict(c.seg_groups)
     group_of_mask = {}
@@ -387,7 +393,7 @@ def _write_cell(w, spec: NetworkSpec, c: PhysicalCell) -> None:
             if gname is None:
                 raise ValueError(f"cell {c.name}: channel density {k} has no matching segment group")
             sg = f' segmentGroup="{gname}"'
-        w(f'   <channelDensity id="cd{k}" ionChannel="{ch.name}" condDensity="{_f(d.cond)} mS_per_cm2" '
+        w(f'   <channelDensity id="{d.name or f"cd{k}"}" ionChannel="{ch.name}" condDensity="{_f(d.cond)} mS_per_cm2" '
           f'erev="{_f(d.erev)}mV" ion="{ion}"{sg}/>\n')
     w(f'   <spikeThresh value="{_f(c.spike_thresh)}mV"/>\n')
     w(f'   <specificCapacitance value="{_f(c.cm)} uF_per_cm2"/>\n')
@@ -558,7 +564,7 @@ def _parse_cell(el, channels_by_name):
                 raise ValueError(f"cell {name}: unknown ionChannel {ch}")
             mask = groups[c.get("segmentGroup", "all")]
             dens.append(ChannelDensity(channels_by_name[ch], _qty(c, "condDensity", "conductivity"),
-                                       _qty(c, "erev", "voltage"), mask.copy()))
+                                       _qty(c, "erev", "voltage"), mask.copy(), c.get("id", "")))
         elif t == "specificCapacitance":
             cm = _qty(c, "value", "spec_capacitance")
         elif t == "initMembPotential":
@@ -569,8 +575,8 @@ def _parse_cell(el, channels_by_name):
             raise ValueError(f"cell {name}: <{t}> is not supported")
     ra = _qty(_children(intra, "resistivity")[0], "value", "resistivity")
     cell = PhysicalCell(name, parent, length, ddist.copy(), dens, cm=cm, ra=ra, v0=v0,
-                        spike_thresh=thr if thr is not None else 0.0, seg_groups=groups)
-    cell.seg_dprox = dprox
+                        spike_thresh=thr if thr is not None else 0.0, seg_groups=groups,
+                        seg_dprox=None if np.array_equal(dprox, ddist) else dprox.copy())
     return cell
 
 
@@ -963,8 +969,10 @@ def read_lems(path: str) -> NetworkSpec:
             units = col.get("output_units") if _tag(of) == "EdenOutputFile" else "V"
             if units not in volt_out:
                 raise ValueError(f"OutputColumn {col.get('id')}: output_units {units!r} not supported")
-            # a fitzHughNagumoCell's V is dimensionless: written as it is
-            scale = 1.0 if col.get("quantity").strip().endswith("/V") else volt_out[units]
+            # a fitzHughNagumoCell's V and a gate's state q are dimensionless:
+            # written as they are
+            qs = col.get("quantity").strip()
+            scale = 1.0 if qs.endswith("/V") or qs.endswith("/q") else volt_out[units]
             cols.append((col.get("id"), col.get("quantity"), _quantity_target(col.get("quantity"), pops, cells),
                          scale))
         points = None
@@ -994,11 +1002,21 @@ def read_lems(path: str) -> NetworkSpec:
 
 
 def _quantity_target(q, pops, cells):
-    """'pop/3/celltype/seg/v', 'pop/3/celltype/v' or 'pop[3]/v' -> (pop, cell, seg)."""
+    """'pop/3/celltype/seg/v', 'pop/3/celltype/v' or 'pop[3]/v' -> (pop, cell,
+    seg, "v"); a gate's state, 'pop/3/celltype/seg/<biophysicalProperties
+    id>/membraneProperties/<channelDensity id>/<ionChannel id>/<gate id>/q'
+    -> (pop, cell, seg, "q:<channelDensity id>/<gate id>")."""
     parts = q.strip().split("/")
+    if parts[-1] == "q" and "membraneProperties" in parts:
+        i = parts.index("membraneProperties")
+        if len(parts) != i + 5:
+            raise ValueError(f"recorded quantity {q!r}: expected .../membraneProperties/<channelDensity>/"
+                             f"<ionChannel>/<gate>/q")
+        pop, cell, seg, _ = _quantity_target("/".join(parts[:i - 1] + ["v"]), pops, cells)
+        return (pop, cell, seg, f"q:{parts[i + 1]}/{parts[i + 3]}")
     if parts[-1] not in ("v", "V"):
         raise ValueError(f"recorded quantity {q!r}: only membrane potential v (a fitzHughNagumoCell's V) "
-                         f"is supported")
+                         f"and gate states q are supported")
     m = re.match(r"^([^/\[\]]+)\[(\d+)\]$", parts[0])
     if m:
         pop, idx, rest = m.group(1), int(m.group(2)), parts[1:-1]
@@ -1009,4 +1027,4 @@ def _quantity_target(q, pops, cells):
     seg = int(rest[0]) if rest else 0
     if pop not in pops:
         raise ValueError(f"recorded quantity {q!r}: unknown population")
-    return (pop, idx, seg)
+    return (pop, idx, seg, "v")

@@ -281,8 +281,12 @@ typedef struct EdenGpuOptions {
     int32_t cells_per_block;  /* 0 = autotune */
     int32_t record_capacity_steps; /* trace samples buffered on the device between fetches */
     int32_t spike_capacity;   /* spike events buffered on the device between fetches */
-    int32_t n_trace;          /* recorded targets (membrane potential) */
-    const int32_t *trace_target;
+    int32_t n_trace;          /* recorded columns */
+    const int32_t *trace_target; /* per column: a target (its membrane potential), or -2 - g for
+                                    the state of gate g of the physical compartments' channel
+                                    instances, numbered instance by instance in comp_chan_off
+                                    order and within one in its type's gate order (the gate
+                                    paths of an OutputColumn, eden/NeuroML.cpp:8140-8183) */
     int32_t kernel_timing;    /* 1: bracket every kernel launch with CUDA events (no graph
                                  replay) and accumulate per-kernel device time */
     int32_t codegen;          /* batched mode: 0 = compile the windowed kernels for the

@@ -54,7 +54,7 @@ struct Gpu {
 __global__ void k_output(Port P, int cur, int64_t step, int32_t n_trace, const int32_t *tt, double *trace,
                          int64_t cap, int32_t *log_src, int64_t *log_step, unsigned long long *log_n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n_trace) trace[(step - 1) * n_trace + i] = P.v[cur][tt[i]];
+    if (i < n_trace) trace[(step - 1) * n_trace + i] = tt[i] >= 0 ? P.v[cur][tt[i]] : P.gate[cur][-2 - (int64_t)tt[i]];
     if (i < P.m->n_src && P.spiked[cur][i]) {
         const unsigned long long k = atomicAdd(log_n, 1ull);
         if ((int64_t)k < cap) {

@@ -653,7 +653,8 @@ static PORT_FN void izh_step(Port *P, int cur, int32_t k, int init, real t, real
 
 /*
  * Run the model for `n_steps` non-initialisation steps (after the 4
- * initialisation passes), recording V of `trace_target` at every step's
+ * initialisation passes), recording V of `trace_target` (or, for an entry
+ * -2 - g, the state of gate g in channel-instance order) at every step's
  * output phase into trace[step][col] and every logged spike as
  * (source, logging step).  Returns 0 or a negative code.
  */
@@ -814,8 +815,9 @@ int eden_port_run(const EdenGpuModel *m, int64_t n_steps, int32_t n_trace, const
         if (step == eden_port_mark_step) eden_port_mark_s = wall_s();
         if (!init) {
             /* output phase: trajectory columns, then event slots read & clear */
-            for (int32_t j = 0; j < n_trace; j++)
-                trace[(step - 1) * n_trace + j] = P.v[cur][trace_target[j]];
+            for (int32_t j = 0; j < n_trace; j++)  /* V of a target, or (-2 - g) gate g's state */
+                trace[(step - 1) * n_trace + j] =
+                    trace_target[j] >= 0 ? P.v[cur][trace_target[j]] : P.gate[cur][-2 - (int64_t)trace_target[j]];
             for (int32_t s = 0; s < m->n_src; s++) {
                 if (P.spiked[cur][s]) {
                     if (nsp < spike_cap) {

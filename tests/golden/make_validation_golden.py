@@ -1,8 +1,9 @@
 """Fixtures of the reference's own validation networks for the GPU.
 
-Reads two of the reference's validation networks
-(testing/validation_tests/neuroml/LEMS_EdenTest_CoreInputs.xml and
-LEMS_EdenTest_PassiveCompartment.xml) with this package's NeuroML reader,
+Reads four of the reference's validation networks
+(testing/validation_tests/neuroml/LEMS_EdenTest_CoreInputs.xml,
+LEMS_EdenTest_PassiveCompartment.xml, LEMS_EdenTest1.xml and
+LEMS_EdenTest2.xml) with this package's NeuroML reader,
 writes each lowered network as a model file (eden_gb300/model_file.py) that
 the C++ host program runs through the C ABI, and stores the reference
 simulator's own trajectory output for the same file (oracle/_ref/eden,
@@ -30,6 +31,8 @@ from eden_gb300 import lowering, model_file, neuroml_io  # noqa: E402
 NETWORKS = {
     "core_inputs": ("LEMS_EdenTest_CoreInputs.xml", "results.gen.txt", 1),
     "passive_compartment": ("LEMS_EdenTest_PassiveCompartment.xml", None, 16),
+    "edentest1": ("LEMS_EdenTest1.xml", "results1.txt", 1),
+    "edentest2": ("LEMS_EdenTest2.xml", "results1.txt", 1),
 }
 
 
@@ -50,8 +53,10 @@ def make(name):
         shutil.rmtree(work, ignore_errors=True)
     model_file.write_for_spec(os.path.join(HERE, f"validation_{name}.egm"), spec, low)
     ref = ref[::stride]
+    # per column: SI value = engine value x scale (mV -> V; gate states as they are)
+    scale = np.array([c[3] for of in spec.output_files for c in of["cols"]], np.float64)
     np.savez_compressed(os.path.join(HERE, f"validation_{name}.npz"), time_s=ref[:, 0], values_si=ref[:, 1:],
-                        network=fname, stride=stride)
+                        network=fname, stride=stride, scale=scale)
     print(f"{name}: {low.n_target} targets, {low.n_steps} steps, {ref.shape[1] - 1} columns")
 
 

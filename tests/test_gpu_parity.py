@@ -111,3 +111,38 @@ def test_blocks_running_several_ctas_in_turn(blocks):
     np.testing.assert_array_equal(a.trace, b.trace)
     np.testing.assert_array_equal(a.spike_src, b.spike_src)
     np.testing.assert_array_equal(a.spike_step, b.spike_step)
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_BATCHED], ids=["plain", "batched"])
+def test_gate_state_columns(mode):
+    """Trace columns of gate states (the OutputColumn path
+    .../membraneProperties/<channelDensity>/<ionChannel>/<gate>/q) beside
+    potentials, on HH somata and HH dendrite compartments inside forests:
+    the GPU's columns against the oracle's, potentials within box(0.1 ms,
+    0.5 mV) and gate states within box(0.1 ms, 0.005)."""
+    from eden_gb300.network import OutputColumn
+    spec = workloads.multicomp_net(n_cells=8, in_degree=10, length_ms=30.0, max_seg=40, n_recorded=4,
+                                   hh_dend_frac=0.3)
+    cols = []
+    for c in range(4):
+        ct = spec.cell_type(spec.populations[c].cell_type)
+        segs = [0] + [int(s) for s in np.nonzero(ct.densities[1].seg_mask)[0] if s > 0][:1]
+        for seg in segs:
+            cols.append(OutputColumn(spec.populations[c].name, 0, seg))
+            for k, gname in ((1, "m"), (1, "h"), (2, "n")):
+                cols.append(OutputColumn(spec.populations[c].name, 0, seg, f"q:cd{k}/{gname}"))
+    spec.trace_columns = cols
+    low = lowering.lower(spec)
+    assert (low.trace_target <= -2).sum() == 3 * (len(cols) // 4)
+    ref = eden_port.run(low)
+    sim = Simulation(low, mode=mode)
+    rec = sim.run()
+    sim.close()
+    dt_ms = float(low.dt) * 1e-3
+    is_q = np.array([c.quantity != "v" for c in cols])
+    assert rec.trace.shape == ref["trace"].shape
+    assert np.all((rec.trace[:, is_q] > 0) & (rec.trace[:, is_q] < 1))
+    nbad, worst = box_violations(ref["trace"][:, ~is_q], rec.trace[:, ~is_q], dt_ms, 0.1, 0.5)
+    assert nbad == 0, f"potentials: {nbad} samples outside the box, worst {worst} mV"
+    nbad, worst = box_violations(ref["trace"][:, is_q], rec.trace[:, is_q], dt_ms, 0.1, 0.005)
+    assert nbad == 0, f"gate states: {nbad} samples outside the box, worst {worst}"

@@ -1,11 +1,16 @@
-"""Two of the reference's own validation networks on the GPU, run by the C++
-host program (eden_gb300/host/eden_gpu_host) through the C ABI:
+"""Four of the reference's own validation networks on the GPU, run by the
+C++ host program (eden_gb300/host/eden_gpu_host) through the C ABI:
 LEMS_EdenTest_CoreInputs (pulse, weighted pulse, sine, ramp and their DL
-forms, voltage clamps, timed input, spike array and generator) and
-LEMS_EdenTest_PassiveCompartment, read by this package's NeuroML reader and
-lowered into model files (tests/golden/make_validation_golden.py), against
-the reference simulator's own output on the same files: every recorded
-potential within 0.01 mV."""
+forms, voltage clamps, timed input, spike array and generator),
+LEMS_EdenTest_PassiveCompartment, LEMS_EdenTest1 (three two-compartment
+cells with frustum dendrites, a gap junction, an expOne connection, a
+sodium gate's state recorded) and LEMS_EdenTest2 (an HH cell with its m, h
+and n recorded), read by this package's NeuroML reader and lowered into
+model files (tests/golden/make_validation_golden.py), against the
+reference simulator's own output on the same files: every recorded
+potential within the stated mV (0.01 for the networks without spikes; the
+reference's kernels are compiled with -Ofast, and on a spike's upstroke V
+moves 4-5 mV per step), every gate state within 1 % of that number."""
 import os
 import subprocess
 
@@ -20,8 +25,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.mark.parametrize("mode", ["batched", "plain"])
-@pytest.mark.parametrize("name", ["core_inputs", "passive_compartment"])
-def test_validation_network_on_gpu_matches_reference(name, mode, tmp_path):
+@pytest.mark.parametrize("name,tol_mv", [("core_inputs", 0.01), ("passive_compartment", 0.01), ("edentest1", 0.05),
+                                         ("edentest2", 0.05)])
+def test_validation_network_on_gpu_matches_reference(name, tol_mv, mode, tmp_path):
     z = np.load(os.path.join(HERE, "golden", f"validation_{name}.npz"))
     traj, ev = str(tmp_path / "traj.txt"), str(tmp_path / "ev.txt")
     p = subprocess.run([build.build_host(), os.path.join(HERE, "golden", f"validation_{name}.egm"), traj, ev, mode],
@@ -31,4 +37,7 @@ def test_validation_network_on_gpu_matches_reference(name, mode, tmp_path):
     ref = np.column_stack([z["time_s"], z["values_si"]])
     assert mine.shape == ref.shape
     np.testing.assert_allclose(mine[:, 0], ref[:, 0], rtol=0, atol=1e-9)
-    assert np.abs(mine[:, 1:] - ref[:, 1:]).max() * 1e3 < 0.01
+    scale = z["scale"]  # SI per engine unit: 1e-3 for potentials, 1 for gate states
+    err = np.abs(mine[:, 1:] - ref[:, 1:]) / scale  # engine units
+    tol = np.where(scale == 1.0, tol_mv * 1e-2, tol_mv)
+    assert (err <= tol).all(), err.max(0)

@@ -16,11 +16,17 @@ import reference_runner
 from eden_gb300 import lowering, neuroml_io
 
 
-@pytest.mark.parametrize("name,outfile", [
-    ("LEMS_EdenTest_CoreInputs.xml", "results.gen.txt"),
-    ("LEMS_EdenTest_PassiveCompartment.xml", None),
+# (network, its trajectory file, tolerance in mV; gate states within 1 %
+# of that in absolute terms).  The spiking networks reach 0.014 mV on the
+# upstroke of a spike, where V moves 4-5 mV per step: the reference's kernels
+# are compiled with -Ofast.
+@pytest.mark.parametrize("name,outfile,tol_mv", [
+    ("LEMS_EdenTest_CoreInputs.xml", "results.gen.txt", 0.01),
+    ("LEMS_EdenTest_PassiveCompartment.xml", None, 0.01),
+    ("LEMS_EdenTest1.xml", "results1.txt", 0.05),   # frustum dendrites, gap junction, synapse, a gate's state
+    ("LEMS_EdenTest2.xml", "results1.txt", 0.05),   # HH cell with its m, h and n recorded
 ])
-def test_oracle_matches_the_reference_on_its_validation_network(name, outfile):
+def test_oracle_matches_the_reference_on_its_validation_network(name, outfile, tol_mv):
     path = reference_runner.validation_network(name)
     if path is None or not reference_runner.available():
         pytest.skip("reference tree or its build not present")
@@ -37,6 +43,9 @@ def test_oracle_matches_the_reference_on_its_validation_network(name, outfile):
     out = eden_port.run(low)
     assert out["rc"] == 0
     mine = out["trace"].astype(np.float64)
-    ref_mv = ref[:, 1:] * 1e3
-    assert mine.shape == ref_mv.shape
-    assert np.abs(mine - ref_mv).max() < 0.01
+    # engine units: mV for potentials, gate states as they are
+    scale = np.array([c[3] for of in spec.output_files for c in of["cols"]], np.float64)
+    ref_eng = ref[:, 1:] / scale
+    assert mine.shape == ref_eng.shape
+    tol = np.where(scale == 1.0, tol_mv * 1e-2, tol_mv)
+    assert (np.abs(mine - ref_eng) <= tol).all(), np.abs(mine - ref_eng).max(0)
