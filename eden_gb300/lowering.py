@@ -208,8 +208,7 @@ def _cable_geometry(cell: PhysicalCell):
     # diameter, Ra (4 / pi) length / (d_from d_to) (eden/Eden.cpp:4234-4241,
     # 4304-4305); a zero-length segment as a cylinder as long as it is wide
     half = np.where(L == 0, d / 2.0, L / 2.0)
-    dpf, ddf = dp.astype(F32), d.astype(F32)
-    dm = np.where(L == 0, ddf, dpf + (ddf - dpf) * F32(0.5)).astype(np.float64)
+    dm = np.where(L == 0, d, dp + (d - dp) * 0.5)   # the midpoint's diameter (d for a cylinder)
     dpx = np.where(L == 0, d, dp)
     r_prox = (float(ra_native) * (4.0 / np.pi) * half / (dpx * dm) * 10.0).astype(F32)
     r_dist = (float(ra_native) * (4.0 / np.pi) * half / (dm * d) * 10.0).astype(F32)

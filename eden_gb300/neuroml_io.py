@@ -778,6 +778,11 @@ def read_lems(path: str) -> NetworkSpec:
     spec.synapses = list(synapses.values())
     spec.gap_types = list(gap_def.values())
     syn_names = list(synapses)
+    # network elements that carry dynamics and are not read fail loudly
+    # rather than drop out of the simulation
+    for el in net:
+        if _tag(el) in ("continuousProjection", "EdenTimeSeriesReader", "cellSet", "synapticConnection"):
+            raise ValueError(f"<{_tag(el)} id={el.get('id')}> is not supported")
     # populations (declaration order = gid order)
     pops = {}
     for p in _children(net, "population"):

@@ -1,9 +1,10 @@
 """Fixtures of the reference's own validation networks for the GPU.
 
-Reads four of the reference's validation networks
+Reads five of the reference's validation networks
 (testing/validation_tests/neuroml/LEMS_EdenTest_CoreInputs.xml,
-LEMS_EdenTest_PassiveCompartment.xml, LEMS_EdenTest1.xml and
-LEMS_EdenTest2.xml) with this package's NeuroML reader,
+LEMS_EdenTest_PassiveCompartment.xml, LEMS_EdenTest1.xml,
+LEMS_EdenTest2.xml and LEMS_EdenTest_DomainDecomposition.xml) with this
+package's NeuroML reader,
 writes each lowered network as a model file (eden_gb300/model_file.py) that
 the C++ host program runs through the C ABI, and stores the reference
 simulator's own trajectory output for the same file (oracle/_ref/eden,
@@ -33,6 +34,7 @@ NETWORKS = {
     "passive_compartment": ("LEMS_EdenTest_PassiveCompartment.xml", None, 16),
     "edentest1": ("LEMS_EdenTest1.xml", "results1.txt", 1),
     "edentest2": ("LEMS_EdenTest2.xml", "results1.txt", 1),
+    "domain_decomposition": ("LEMS_EdenTest_DomainDecomposition.xml", "results.gen.txt", 4),
 }
 
 
