@@ -121,7 +121,7 @@ inline std::string channel_routines(const EdenGpuChannelType *types, const std::
 // compiles only their code (the EDEN_KIND_* switches of eden_kernels.cuh).
 struct Kinds {
     bool pulse = false, sine = false, ramp = false, pois = false, timed = false, syn = false, expone = false,
-         exptwo = false, forest = false, izh = false, gateforms = false, clamp = false, gap = false;
+         exptwo = false, forest = false, izh = false, gateforms = false, clamp = false, gap = false, alpha = false;
 };
 
 inline std::string kind_defines(const Kinds &k) {
@@ -140,6 +140,7 @@ inline std::string kind_defines(const Kinds &k) {
     def("EDEN_KIND_FOREST", k.forest);
     def("EDEN_KIND_IZH", k.izh);
     def("EDEN_KIND_GAP", k.gap);
+    def("EDEN_KIND_ALPHA", k.alpha);
     return s;
 }
 

@@ -35,12 +35,12 @@ constexpr int kForestWidth = 64;    // most compartments of a forest at one dept
 constexpr int kGraphWindows = 16;  // windows per captured graph
 
 // Host set-up loops whose iterations are independent run on the host's
-// threads (at most 16), in contiguous blocks of the index range; small
-// ranges run inline.
+// threads (at most 16, at least `grain` iterations each), in contiguous
+// blocks of the index range; small ranges run inline.
 template <typename F>
-void parallel_for(int64_t n, F f) {
+void parallel_for(int64_t n, F f, int64_t grain = 16384) {
     const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, (int64_t)std::thread::hardware_concurrency()));
-    const int64_t nthr = std::min<int64_t>(hw, n / 16384);
+    const int64_t nthr = std::min<int64_t>(hw, n / grain);
     if (nthr <= 1) {
         for (int64_t i = 0; i < n; i++) f(i);
         return;
@@ -298,7 +298,8 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
     }
     for (int k = 0; k < m->n_syn_types; k++) {
         const EdenGpuSynapseType &t = m->syn_types[k];
-        if (t.kind != EDEN_SYN_EXPONE && t.kind != EDEN_SYN_EXPTWO) return ctx->fail(EDEN_GPU_E_INVALID, "synapse type kind");
+        if (t.kind < EDEN_SYN_EXPONE || t.kind > EDEN_SYN_ALPHA_CURRENT)
+            return ctx->fail(EDEN_GPU_E_INVALID, "synapse type kind");
         if (!finite_pos(t.tau_decay) || (t.kind == EDEN_SYN_EXPTWO && !finite_pos(t.tau_rise)))
             return ctx->fail(EDEN_GPU_E_INVALID, "synapse type %d: time constants", k);
     }
@@ -573,13 +574,14 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     int max_forest = 1;
     int izh_slot = 0;
     std::vector<int32_t> izh_user_of_slot;
-    std::vector<int> coff, kids, fill;
     {
         std::vector<int> phys, izhs;
         for (int k = 0; k < n_cells; k++) {
             if (cell_phys[order[k]] >= 0) phys.push_back(order[k]);
             else if (cell_izh[order[k]] >= 0) izhs.push_back(order[k]);
         }
+        // the forests' cells, packed in schedule order
+        std::vector<std::vector<int>> forests;
         size_t pi = 0;
         while (pi < phys.size()) {
             std::vector<int> fc;
@@ -598,17 +600,38 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
                 nodes += cell_n[c];
                 pi++;
             }
-            // joint BFS over the forest's cells
+            forests.push_back(std::move(fc));
+        }
+        // each forest's place: its first target and its depth boundaries
+        // (a forest of depth D has D + 1 levels and D + 2 boundaries)
+        const int nfo = (int)forests.size();
+        fo_t0.resize(nfo); fo_t1.resize(nfo); fo_l0.resize(nfo); fo_nlev.resize(nfo); fo_f64.resize(nfo);
+        for (int f = 0; f < nfo; f++) {
+            int fn = 0, nl = 1;
+            for (int g : forests[f]) { fn += cell_n[g]; nl = std::max(nl, (int)cell_levels[g]); }
+            fo_t0[f] = next;
+            fo_t1[f] = next + fn;
+            fo_nlev[f] = nl;
+            fo_l0[f] = (int)lvl.size();
+            fo_f64[f] = flagged(forests[f].front()) ? 1 : 0;
+            lvl.resize(lvl.size() + nl + 1);
+            un_t0.push_back(next);
+            un_f.push_back(f);
+            next += fn;
+            un_t1.push_back(next);
+            max_forest = std::max(max_forest, fn);
+        }
+        // joint breadth-first numbering of each forest's cells, forests on
+        // the host's threads (each writes only its own targets)
+        parallel_for(nfo, [&](int64_t f) {
+            const std::vector<int> &fc = forests[f];
             struct Node { int cell_base; int local; int depth; };
             std::vector<Node> q;
+            std::vector<int> coff, kids, fill;
             for (int g : fc) q.push_back({m->phys_comp_off[cell_phys[g]], 0, 0});
-            const int f_t0 = next;
-            fo_f64.push_back(flagged(fc.front()) ? 1 : 0);
-            un_t0.push_back(f_t0);
-            un_f.push_back((int)fo_t0.size());
-            fo_t0.push_back(f_t0);
-            fo_l0.push_back((int)lvl.size());
-            lvl.push_back(f_t0);
+            const int f_t0 = fo_t0[f];
+            int32_t *lv = &lvl[fo_l0[f]];
+            lv[0] = f_t0;
             int depth = 0;
             std::vector<std::vector<int>> cell_kids(fc.size());
             for (size_t ci = 0; ci < fc.size(); ci++) {
@@ -634,7 +657,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
                 const int ci = node_cell[h];
                 if (u.depth != depth) {
                     depth = u.depth;
-                    lvl.push_back(f_t0 + (int)h);
+                    lv[depth] = f_t0 + (int)h;
                 }
                 const int it = f_t0 + (int)h;
                 const int ut = u.cell_base + u.local;
@@ -651,14 +674,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
                     node_cell.push_back(ci);
                 }
             }
-            const int fn = (int)q.size();
-            lvl.push_back(f_t0 + fn);
-            fo_nlev.push_back(depth + 1);
-            fo_t1.push_back(f_t0 + fn);
-            max_forest = std::max(max_forest, fn);
-            next += fn;
-            un_t1.push_back(next);
-        }
+            lv[fo_nlev[f]] = f_t0 + (int)q.size();
+        }, 32);
         for (size_t k = 0; k < izhs.size(); k += 32) {
             un_t0.push_back(next);
             un_f.push_back(-1);
@@ -999,21 +1016,24 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = poff[t]; k < poff[t + 1];) {
             int64_t k1 = k;
             while (k1 < poff[t + 1] && po_type[k1] == po_type[k]) k1++;
-            bk_kind.push_back(BK_POIS); bk_erev.push_back(m->syn_types[po_type[k]].erev); bk_type.push_back(po_type[k]);
+            bk_kind.push_back(BK_POIS | (m->syn_types[po_type[k]].kind == EDEN_SYN_ALPHA_CURRENT ? BK_CURRENT : 0));
+            bk_erev.push_back(m->syn_types[po_type[k]].erev); bk_type.push_back(po_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
         }
         for (int64_t k = toff[t]; k < toff[t + 1];) {
             int64_t k1 = k;
             while (k1 < toff[t + 1] && tm_type[k1] == tm_type[k]) k1++;
-            bk_kind.push_back(BK_TIMED); bk_erev.push_back(m->syn_types[tm_type[k]].erev); bk_type.push_back(tm_type[k]);
+            bk_kind.push_back(BK_TIMED | (m->syn_types[tm_type[k]].kind == EDEN_SYN_ALPHA_CURRENT ? BK_CURRENT : 0));
+            bk_erev.push_back(m->syn_types[tm_type[k]].erev); bk_type.push_back(tm_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
         }
         for (int64_t k = soff[t]; k < soff[t + 1];) {
             int64_t k1 = k;
             while (k1 < soff[t + 1] && sy_type[k1] == sy_type[k]) k1++;
-            bk_kind.push_back(BK_SYN); bk_erev.push_back(m->syn_types[sy_type[k]].erev); bk_type.push_back(sy_type[k]);
+            bk_kind.push_back(BK_SYN | (m->syn_types[sy_type[k]].kind == EDEN_SYN_ALPHA_CURRENT ? BK_CURRENT : 0));
+            bk_erev.push_back(m->syn_types[sy_type[k]].erev); bk_type.push_back(sy_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
         }
@@ -1036,7 +1056,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     const int n_chunk = (int)ck_blk.size();
     std::vector<int32_t> ck_info(n_chunk);
     for (int c = 0; c < n_chunk; c++)
-        ck_info[c] = (bk_kind[ck_blk[c]] == BK_CLAMPV ? BK_PULSE : bk_kind[ck_blk[c]]) |
+        ck_info[c] = (bk_kind[ck_blk[c]] == BK_CLAMPV ? BK_PULSE : (bk_kind[ck_blk[c]] & BK_KIND_MASK)) |
                      ((int32_t)bk_type[ck_blk[c]] << 2) | (ck_n[c] << 8);
 
     // ---- window length: every delay must cover the window (see k_window)
@@ -1406,6 +1426,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         st[k].r_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f / s.tau_rise : 1.0f;
         st[k].f_decay = 1.0f - dt / s.tau_decay;
         st[k].f_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f - dt / s.tau_rise : 1.0f;
+        // an alpha kind's coupling e dt / tau: g' = f g + c A per step
+        st[k].c_alpha = s.kind >= EDEN_SYN_ALPHA ? (float)(2.7182818284590451 * (double)dt / (double)s.tau_decay) : 0.0f;
     }
     {
         const ChanTypeDev *pc = nullptr;
@@ -1463,7 +1485,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         phase("codegen");
         eden_codegen::Kinds kinds;
         for (int b = 0; b < n_block; b++) {
-            const int kb = bk_kind[b];
+            const int kb = bk_kind[b] & BK_KIND_MASK;
             kinds.pulse |= kb == BK_PULSE && bk_type[b] == 0;
             kinds.clamp |= kb == BK_CLAMPV;
             kinds.sine |= kb == BK_PULSE && bk_type[b] == 1 + EDEN_WAVE_SINE;
@@ -1473,8 +1495,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             kinds.syn |= kb == BK_SYN;
             if (kb != BK_PULSE && kb != BK_CLAMPV) {
                 const int sk = m->syn_types[bk_type[b]].kind;
-                kinds.expone |= sk == EDEN_SYN_EXPONE;
+                kinds.expone |= sk == EDEN_SYN_EXPONE || sk >= EDEN_SYN_ALPHA;  // alpha items step like expOne's
                 kinds.exptwo |= sk == EDEN_SYN_EXPTWO;
+                kinds.alpha |= sk >= EDEN_SYN_ALPHA;
             }
         }
         kinds.forest = d.n_forest > 0;

@@ -47,6 +47,7 @@ struct SynTypeDev {
     float gbase, erev, tau_decay, tau_rise, wf_w;  // wf_w = weight_prop * waveform_factor
     float r_decay, r_rise;                          // correctly rounded 1 / tau
     float f_decay, f_rise;                          // 1 - dt / tau, one step's decay factor
+    float c_alpha;                                  // alpha kinds: e dt / tau, g' = f g + c A
 };
 
 // x / tau, correctly rounded, from r = RN(1/tau): q = RN(x*r) is within an
@@ -74,6 +75,9 @@ enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2, BK_TIMED = 3 };
 // block-level only: a voltage clamp's sum of weight / R, applied as -V g
 // (its chunks run as pulse-block type kClampB)
 enum : int { BK_CLAMPV = 4 };
+// a synapse block of a current-based kind (alphaCurrentSynapse) carries this
+// flag beside its kind: its exposure is a current, with no conductance
+enum : int { BK_KIND_MASK = 7, BK_CURRENT = 8 };
 // pulse-block types: 0 pulses, then the waveform shapes, then the two halves of a clamp
 enum : int { kPulseSine = 1 + EDEN_WAVE_SINE, kPulseRamp = 1 + EDEN_WAVE_RAMP, kClampA = 3, kClampB = 4 };
 constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
@@ -561,6 +565,7 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
 #define EDEN_KIND_FOREST 1
 #define EDEN_KIND_IZH 1
 #define EDEN_KIND_GAP 1
+#define EDEN_KIND_ALPHA 1
 #endif
 
 // A timedSynapticInput item over the window: its synapse fires in each
@@ -593,6 +598,58 @@ __device__ __forceinline__ void timed_window(const DevModel &m, int64_t it, cons
 // both a row write and a column read are free of bank conflicts) holds the
 // lane's terms for each step of the window.
 constexpr int kAccStride = 33;
+
+// An alpha chunk's aggregate over the window (alphaSynapse: conductance g
+// and rise state A; alphaCurrentSynapse: current I and J).  Per step the
+// reference integrates A' = -A / tau and g' = (e A - g) / tau by forward
+// Euler (LEMS_CoreComponents.inc.xml:85-142), so over the chunk's weighted
+// sums A_{j+1} = f A_j + E_j and g_{j+1} = f g_j + c A_j, f = 1 - dt / tau,
+// c = e dt / tau, E_j the events of step j (each a synapse's skipped decay
+// plus its jump, as input_event gives them for the expOne-like rise state).
+// In closed form g_j = f^j g_0 + c j f^(j-1) A_0 + c T_j with S_j the
+// events' part of A_j (a scan over the lanes, as for the other kinds) and
+// T_j = sum_{k<j} f^(j-1-k) S_k a second scan over S.  Lane j keeps the
+// exposure g_j of step j for Gp.
+__device__ __forceinline__ void alpha_chunk_window(const DevModel &m, int c, int type, const SynTypeDev &st,
+                                                   const WindowArgs &w, unsigned rows, float A, float B,
+                                                   const float *tileA) {
+    const int lane = threadIdx.x & 31;
+    const float *pd = m.syn_pow + (size_t)type * 2 * kPowLen + kPowLen;
+    const float cc = st.c_alpha;
+    const float jf = (float)lane;
+    // the parts from the window's starting state
+    float gj = lane < w.K ? B * pd[lane] + (lane > 0 ? cc * (jf * pd[lane - 1]) * A : 0.0f) : 0.0f;
+    float Ak = A * pd[w.K], Bk = B * pd[w.K] + cc * ((float)w.K * pd[w.K - 1]) * A;
+    if (rows != 0) {
+        float ea = 0.0f;  // lane j: the chunk's events of step j
+        if (lane < w.K)
+            for (unsigned r = rows; r; r &= r - 1) ea += tileA[(__ffs(r) - 1) * kAccStride + lane];
+        // S: inclusive scan of the events with factor f, then exclusive
+        float va = lane < w.K ? ea : 0.0f;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const float u = __shfl_up_sync(0xffffffffu, va, d);
+            if (lane >= d) va = fmaf(pd[d], u, va);
+        }
+        float sj = __shfl_up_sync(0xffffffffu, va, 1);
+        if (lane == 0) sj = 0.0f;
+        // T: the same scan over S
+        float vt = lane < w.K ? sj : 0.0f;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const float u = __shfl_up_sync(0xffffffffu, vt, d);
+            if (lane >= d) vt = fmaf(pd[d], u, vt);
+        }
+        float tj = __shfl_up_sync(0xffffffffu, vt, 1);
+        if (lane == 0) tj = 0.0f;
+        if (lane < w.K) gj += cc * tj;
+        Ak += __shfl_sync(0xffffffffu, va, w.K - 1);
+        Bk += cc * __shfl_sync(0xffffffffu, vt, w.K - 1);
+    }
+    if (lane < w.K) m.Gp[(size_t)lane * m.n_chunk + c] = gj;
+    if (lane == 0 && w.step0 > 0) { m.ck_a[c] = Ak; m.ck_b[c] = Bk; }
+    __syncwarp();
+}
 
 // One chunk (at most kChunkItems items of one input block) over the K steps
 // of a window, lane l handling items l, l + 32, ...  Pulses add their
@@ -728,6 +785,10 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     const unsigned rows = __ballot_sync(0xffffffffu, used);
     __syncwarp();
     float gj = 0.0f;
+    if (EDEN_KIND_ALPHA && st.kind >= EDEN_SYN_ALPHA) {
+        alpha_chunk_window(m, c, type, st, w, rows, A, B, tileA);
+        return;
+    }
     if (rows == 0) {
         // no event in the window: the aggregate decays in closed form,
         // A f^j, from the factors' powers (syn_pow)
@@ -789,14 +850,21 @@ __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1,
     for (int bk = b0; bk < b1; bk++) {
         float g = 0.0f;
         for (int c = BC0[bk]; c < BC0[bk + 1]; c++) g += Gpk[c + chk0];
-        const int kind = BK_K[bk];
+        const int kind = BK_K[bk] & BK_KIND_MASK;
+        const bool current = EDEN_KIND_ALPHA && (BK_K[bk] & BK_CURRENT);
         if (kind == BK_PULSE) {
             Iin += g;
         } else if (EDEN_KIND_CLAMP && kind == BK_CLAMPV) {
             Iin -= v * g;
         } else if (kind == BK_POIS || kind == BK_TIMED) {
-            Iin += g * (BK_E[bk] - v);
-            Gin += g;
+            if (current) {
+                Iin += g;
+            } else {
+                Iin += g * (BK_E[bk] - v);
+                Gin += g;
+            }
+        } else if (current) {
+            Isyn += g;
         } else {
             Isyn += g * (BK_E[bk] - v);
             Gsyn += g;

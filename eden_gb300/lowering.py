@@ -32,7 +32,7 @@ from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, FitzHugh
                       NetworkSpec,
                       PhysicalCell, SpikeArrayCell, SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       WAVE_RAMP, WAVE_SINE,
-                      SYN_EXPTWO)
+                      SYN_EXPTWO, SYN_ALPHA_CURRENT)
 
 F32 = np.float32
 MAX_GATES = 4
@@ -647,7 +647,8 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         syn_index[s.name] = k
         st = syn_types[k]
         st["kind"] = s.kind
-        st["gbase"] = _to_f32(s.gbase * 1e-3)     # nS -> uS
+        # nS -> uS; an alphaCurrentSynapse's ibase stays in nA
+        st["gbase"] = _to_f32(s.gbase) if s.kind == SYN_ALPHA_CURRENT else _to_f32(s.gbase * 1e-3)
         st["erev"] = _to_f32(s.erev)
         st["tau_decay"] = _to_f32(s.tau_decay * 1000.0)
         st["tau_rise"] = _to_f32(s.tau_rise * 1000.0) if s.kind == SYN_EXPTWO else 0.0
@@ -860,7 +861,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 8
+ABI_VERSION = 9
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)

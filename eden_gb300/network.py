@@ -254,13 +254,18 @@ SPIKE_SOURCE_TYPES = (SpikeArrayCell, SpikeGeneratorCell, EventSetReaderCell, Sp
 # ---------------------------------------------------------------------------
 SYN_EXPONE = 0
 SYN_EXPTWO = 1
+SYN_ALPHA = 2           # alphaSynapse: conductance, rise and decay both tau
+SYN_ALPHA_CURRENT = 3   # alphaCurrentSynapse: current ibase, rise and decay both tau
 
 
 @dataclass
 class SynapseType:
+    """A core synapse: expOneSynapse, expTwoSynapse, alphaSynapse (tau_decay
+    holds its tau) or alphaCurrentSynapse (tau_decay holds its tau, gbase
+    its ibase in nA, erev unused)."""
     name: str
     kind: int
-    gbase: float          # nS
+    gbase: float          # nS (alphaCurrentSynapse: ibase, nA)
     erev: float           # mV
     tau_decay: float      # ms
     tau_rise: float = 0.0  # ms (expTwo only)

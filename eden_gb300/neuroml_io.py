@@ -26,7 +26,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
                       ClampInputs, FitzHughNagumoCell, IzhikevichCell, TimedInputs, WaveInputs,
-                      ElectricalProjection, GapJunctionType)
+                      ElectricalProjection, GapJunctionType, SYN_ALPHA, SYN_ALPHA_CURRENT)
 
 
 def _f(x: float) -> str:
@@ -80,6 +80,11 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
         if s.kind == SYN_EXPONE:
             w(f'<expOneSynapse id="{s.name}" gbase="{_f(s.gbase)}nS" erev="{_f(s.erev)}mV" '
               f'tauDecay="{_f(s.tau_decay)}ms"/>\n')
+        elif s.kind == SYN_ALPHA:
+            w(f'<alphaSynapse id="{s.name}" gbase="{_f(s.gbase)}nS" erev="{_f(s.erev)}mV" '
+              f'tau="{_f(s.tau_decay)}ms"/>\n')
+        elif s.kind == SYN_ALPHA_CURRENT:
+            w(f'<alphaCurrentSynapse id="{s.name}" ibase="{_f(s.gbase)}nA" tau="{_f(s.tau_decay)}ms"/>\n')
         else:
             w(f'<expTwoSynapse id="{s.name}" gbase="{_f(s.gbase)}nS" erev="{_f(s.erev)}mV" '
               f'tauRise="{_f(s.tau_rise)}ms" tauDecay="{_f(s.tau_decay)}ms"/>\n')
@@ -684,6 +689,12 @@ def read_lems(path: str) -> NetworkSpec:
             synapses[e.get("id")] = SynapseType(e.get("id"), SYN_EXPTWO, _qty(e, "gbase", "conductance"),
                                                 _qty(e, "erev", "voltage"), _qty(e, "tauDecay", "time"),
                                                 _qty(e, "tauRise", "time"))
+        elif t == "alphaSynapse":
+            synapses[e.get("id")] = SynapseType(e.get("id"), SYN_ALPHA, _qty(e, "gbase", "conductance"),
+                                                _qty(e, "erev", "voltage"), _qty(e, "tau", "time"))
+        elif t == "alphaCurrentSynapse":
+            synapses[e.get("id")] = SynapseType(e.get("id"), SYN_ALPHA_CURRENT, _qty(e, "ibase", "current"), 0.0,
+                                                _qty(e, "tau", "time"))
         elif t == "gapJunction":
             gap_def[e.get("id")] = GapJunctionType(e.get("id"), _qty(e, "conductance", "conductance"))
         elif t in ("pulseGenerator", "pulseGeneratorDL"):

@@ -45,6 +45,9 @@ network of a stated shape from numpy's `default_rng(seed)`:
                    single-compartment HH cells and branching cells, with DC
                    pulses on some somata and expTwo synapses onto coupled
                    compartments.
+  alpha_synapses   alphaSynapse and alphaCurrentSynapse connections, Poisson
+                   and timed inputs on HH somata and dendrites and
+                   izhikevich2007 cells, beside expTwo connections.
   gate_kinds       channels with every built-in gate kind (gateHHrates,
                    gateHHtauInf, gateHHratesTau, gateHHratesInf,
                    gateHHratesTauInf), q10Fixed and q10ExpTemp settings at
@@ -851,6 +854,66 @@ def voltage_clamps(n_hh: int = 4, n_branch: int = 2, n_izh: int = 2, length_ms: 
     return spec
 
 
+def alpha_synapses(n_hh: int = 6, n_izh: int = 6, n_branch: int = 3, length_ms: float = 80.0, dt_ms: float = 0.025,
+                   seed: int = 1234) -> NetworkSpec:
+    """alphaSynapse (conductance) and alphaCurrentSynapse (current) on
+    single-compartment HH cells, the dendrites of branching cells and
+    izhikevich2007 cells: recurrent connections of both kinds, Poisson
+    inputs driving each kind, and timed inputs (some in the same steps as
+    other events), beside an expTwo connection onto the same compartments."""
+    from .network import SYN_ALPHA, SYN_ALPHA_CURRENT
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("alpha_synapses", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses.append(SynapseType("syn_alpha", SYN_ALPHA, gbase=2.0, erev=0.0, tau_decay=2.0))
+    spec.synapses.append(SynapseType("syn_alpha_i", SYN_ALPHA_CURRENT, gbase=0.08, erev=0.0, tau_decay=3.0))
+    spec.synapses.append(SynapseType("syn_e2", SYN_EXPTWO, gbase=1.0, erev=0.0, tau_decay=5.0, tau_rise=0.5))
+    spec.cells.append(PhysicalCell("hhcell", np.array([-1]), np.array([0.0]), np.array([17.8]),
+                                   _hh_densities(1, np.ones(1, bool)), cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0))
+    parent = np.array([-1, 0, 1])
+    soma = parent < 0
+    spec.cells.append(PhysicalCell("branch", parent, np.array([20.0, 60.0, 50.0]), np.array([20.0, 2.0, 1.5]),
+                                   _hh_densities(3, soma), cm=1.0, ra=150.0, v0=-65.0, spike_thresh=-20.0,
+                                   seg_groups={"soma_group": soma, "dend_group": ~soma}))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    spec.populations.append(Population("branch", "branch", n_branch))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    hh = np.arange(n_hh)
+    br = n_hh + np.arange(n_branch)
+    iz = n_hh + n_branch + np.arange(n_izh)
+    n = n_hh + n_branch + n_izh
+    # a DC drive on a third of the cells
+    drv = np.arange(0, n, 3)
+    amp = np.where(drv >= n_hh + n_branch, 0.12, 0.12)
+    spec.pulses.append(PulseInputs("*", drv, np.zeros(len(drv), int), np.full(len(drv), 2.0),
+                                   np.full(len(drv), length_ms), np.round(amp * rng.uniform(0.8, 1.6, len(drv)), 4)))
+    # recurrent connections of each kind, somata and dendrites
+    for syn in ("syn_alpha", "syn_alpha_i", "syn_e2"):
+        post = np.repeat(np.arange(n), 2)
+        pre = rng.integers(0, n, size=post.size)
+        pre = np.where(pre == post, (pre + 1) % n, pre)
+        seg = np.where((post >= n_hh) & (post < n_hh + n_branch), rng.integers(0, 3, size=post.size), 0)
+        spec.projections.append(_flat_projection(spec, f"proj_{syn}", pre, post, syn,
+                                                 np.round(rng.uniform(0.5, 1.5, post.size), 4),
+                                                 _round_us(rng.uniform(0.5, 3.0, size=post.size)), post_seg=seg))
+    # Poisson inputs of both alpha kinds
+    spec.poissons.append(PoissonInputs("*", "syn_alpha", 60.0, np.concatenate([hh, br, iz]),
+                                       np.concatenate([np.zeros(n_hh, int), np.full(n_branch, 2), np.zeros(n_izh, int)])))
+    spec.poissons.append(PoissonInputs("*", "syn_alpha_i", 80.0, np.concatenate([hh, iz]),
+                                       np.zeros(n_hh + n_izh, int)))
+    # timed inputs of both alpha kinds
+    for syn in ("syn_alpha", "syn_alpha_i"):
+        cells = np.concatenate([hh[::2], iz[::2]])
+        times = [np.round(np.sort(rng.uniform(0.0, length_ms, rng.integers(3, 9))), 4) for _ in cells]
+        times[0] = np.concatenate([times[0], [10.0, 10.0001, 20.025]])
+        spec.timed.append(TimedInputs(syn, cells, np.zeros(len(cells), np.int64), times,
+                                      np.round(rng.uniform(0.5, 1.5, len(cells)), 4)))
+    cols = [(g, 0) for g in range(n)] + [(int(b), 2) for b in br]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), seg) for g, seg in cols]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 def gap_junctions(n_hh: int = 10, n_branch: int = 4, n_izh: int = 2, length_ms: float = 80.0,
                   dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
     """Gap junctions (two gapJunction types, 1 and 4 nS, weights 0.5-1.5)
@@ -926,6 +989,7 @@ CONFIGS = {
     "gate_kinds": gate_kinds,
     "voltage_clamps": voltage_clamps,
     "gap_junctions": gap_junctions,
+    "alpha_synapses": alpha_synapses,
     "routing_probe": routing_probe,
     "random_sources": random_sources,
     "custom_setup": custom_setup,

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 8
+#define EDEN_GPU_ABI_VERSION 9
 
 enum {
     EDEN_GPU_OK = 0,
@@ -121,12 +121,15 @@ typedef struct EdenGpuChannelType {
     float inf_rate[EDEN_MAX_GATES], inf_mid[EDEN_MAX_GATES], inf_scale[EDEN_MAX_GATES];
 } EdenGpuChannelType;
 
-enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1 };
+enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1, EDEN_SYN_ALPHA = 2, EDEN_SYN_ALPHA_CURRENT = 3 };
 
-/* expOneSynapse (native, eden/Eden.cpp:3424-3466) or expTwoSynapse (LEMS,
- * LEMS_CoreComponents.inc.xml:145-180).  gbase uS, erev mV, taus us.
- * `waveform_factor` is expTwo's derived 1/(-exp(-tp/tr)+exp(-tp/td)) and
- * `weight_prop` its LEMS `weight` property (default 1). */
+/* expOneSynapse (native, eden/Eden.cpp:3424-3466), expTwoSynapse,
+ * alphaSynapse or alphaCurrentSynapse (LEMS, LEMS_CoreComponents.inc.xml:
+ * 85-180).  gbase uS, erev mV, taus us.  `waveform_factor` is expTwo's
+ * derived 1/(-exp(-tp/tr)+exp(-tp/td)) and `weight_prop` its LEMS `weight`
+ * property (default 1).  The alpha kinds have one time constant, in
+ * tau_decay; an alphaCurrentSynapse carries its ibase (nA) in gbase and
+ * contributes current only (erev unused). */
 typedef struct EdenGpuSynapseType {
     int32_t kind;
     float gbase, erev, tau_decay, tau_rise, waveform_factor, weight_prop;

@@ -155,6 +155,56 @@ static void dfs_postorder(const int32_t *parent, int n, int32_t *order) {
     free(child_off); free(children); free(fill); free(stack); free(next);
 }
 
+/* One step of a synapse's own state (a, b) with `fired` this step: the
+ * exposure before the update -- conductance g and current i, or for the
+ * current-based alphaCurrentSynapse its current with g = 0 -- and the next
+ * state.  expOne as the reference's native code (eden/Eden.cpp:3424-3466);
+ * the LEMS kinds by forward Euler of their TimeDerivatives, an OnEvent
+ * assignment replacing the integrated value of the state it assigns
+ * (LEMS_CoreComponents.inc.xml:85-180): expTwo (a = A, b = B), alpha
+ * (a = A, b = g) and alphaCurrent (a = J, b = I). */
+static inline PORT_FN void syn_dyn(const EdenGpuSynapseType *st, int init, int fired, real dt, real v, real a,
+                                   real b, real *an, real *bn, real *g, real *i) {
+    const real e = (real)2.7182818284590451;
+    switch (st->kind) {
+    case EDEN_SYN_EXPONE:
+        *g = a;
+        *i = *g * (st->erev - v);
+        *an = init ? a : (fired ? a + st->gbase : a - dt * (a / st->tau_decay));
+        *bn = b;
+        return;
+    case EDEN_SYN_ALPHA:
+    case EDEN_SYN_ALPHA_CURRENT:
+        if (st->kind == EDEN_SYN_ALPHA) {
+            *g = b;
+            *i = *g * (st->erev - v);
+        } else {
+            *g = R(0.0);
+            *i = b;
+        }
+        if (init) {
+            *an = R(0.0); *bn = R(0.0);
+        } else {
+            *an = fired ? a + st->gbase * st->weight_prop : a + dt * (-a / st->tau_decay);
+            *bn = b + dt * ((e * a - b) / st->tau_decay);
+        }
+        return;
+    default:
+        *g = st->gbase * (b - a);
+        *i = *g * (st->erev - v);
+        if (init) {
+            *an = R(0.0); *bn = R(0.0);
+        } else if (fired) {
+            *an = a + st->weight_prop * st->waveform_factor;
+            *bn = b + st->weight_prop * st->waveform_factor;
+        } else {
+            *an = a + dt * (-a / st->tau_rise);
+            *bn = b + dt * (-b / st->tau_decay);
+        }
+        return;
+    }
+}
+
 /* One synapse instance: trigger/pending logic, exposure, state update.
  * Returns the weighted current and conductance through *iw, *gw. */
 static inline PORT_FN void synapse_step(const EdenGpuSynapseType *st, int init, real t, real dt,
@@ -173,39 +223,10 @@ static inline PORT_FN void synapse_step(const EdenGpuSynapseType *st, int init, 
     }
     *pend_next = next_next;
     *fired = spike_now;
-    if (st->kind == EDEN_SYN_EXPONE) {
-        real g = a;
-        real i = g * (st->erev - v);
-        real gn;
-        if (!init) {
-            gn = a - dt * (a / st->tau_decay);
-            if (spike_now) gn = a + st->gbase;
-        } else {
-            gn = a;
-        }
-        *a_next = gn;
-        *b_next = b;
-        *iw = i * w;
-        *gw = g * w;
-    } else {
-        real g = st->gbase * (b - a);
-        real i = g * (st->erev - v);
-        real an, bn;
-        if (init) {
-            an = R(0.0); bn = R(0.0);
-        } else {
-            an = a + dt * (-a / st->tau_rise);
-            bn = b + dt * (-b / st->tau_decay);
-            if (spike_now) {
-                an = a + st->weight_prop * st->waveform_factor;
-                bn = b + st->weight_prop * st->waveform_factor;
-            }
-        }
-        *a_next = an;
-        *b_next = bn;
-        *iw = i * w;
-        *gw = g * w;
-    }
+    real g, i;
+    syn_dyn(st, init, spike_now, dt, v, a, b, a_next, b_next, &g, &i);
+    *iw = i * w;
+    *gw = g * w;
 }
 
 /* Poisson-driven synapse: the spiker fires its own synapse in the same step. */
@@ -233,30 +254,8 @@ static inline PORT_FN void poisson_step(const Port *P, int cur, int64_t k, int i
         }
     }
     const EdenGpuSynapseType *st = &m->syn_types[m->pois_type[k]];
-    real a = P->pois_a[cur][k], b = P->pois_b[cur][k];
-    real g = st->gbase * (b - a);
-    real i = g * (st->erev - v);
-    real an, bn;
-    if (st->kind == EDEN_SYN_EXPONE) {
-        g = a;
-        i = g * (st->erev - v);
-        if (!init) {
-            an = a - dt * (a / st->tau_decay);
-            if (fired) an = a + st->gbase;
-        } else {
-            an = a;
-        }
-        bn = b;
-    } else if (init) {
-        an = R(0.0); bn = R(0.0);
-    } else {
-        an = a + dt * (-a / st->tau_rise);
-        bn = b + dt * (-b / st->tau_decay);
-        if (fired) {
-            an = a + st->weight_prop * st->waveform_factor;
-            bn = b + st->weight_prop * st->waveform_factor;
-        }
-    }
+    real g, i, an, bn;
+    syn_dyn(st, init, fired, dt, v, P->pois_a[cur][k], P->pois_b[cur][k], &an, &bn, &g, &i);
     P->pois_a[nxt][k] = an;
     P->pois_b[nxt][k] = bn;
     *iw = i * m->pois_weight[k];
@@ -279,30 +278,8 @@ static inline PORT_FN void timed_input_step(const Port *P, int cur, int64_t k, i
         }
     }
     const EdenGpuSynapseType *st = &m->syn_types[m->timed_type[k]];
-    real a = P->timed_a[cur][k], b = P->timed_b[cur][k];
-    real g = st->gbase * (b - a);
-    real i = g * (st->erev - v);
-    real an, bn;
-    if (st->kind == EDEN_SYN_EXPONE) {
-        g = a;
-        i = g * (st->erev - v);
-        if (!init) {
-            an = a - dt * (a / st->tau_decay);
-            if (fired) an = a + st->gbase;
-        } else {
-            an = a;
-        }
-        bn = b;
-    } else if (init) {
-        an = R(0.0); bn = R(0.0);
-    } else {
-        an = a + dt * (-a / st->tau_rise);
-        bn = b + dt * (-b / st->tau_decay);
-        if (fired) {
-            an = a + st->weight_prop * st->waveform_factor;
-            bn = b + st->weight_prop * st->waveform_factor;
-        }
-    }
+    real g, i, an, bn;
+    syn_dyn(st, init, fired, dt, v, P->timed_a[cur][k], P->timed_b[cur][k], &an, &bn, &g, &i);
     P->timed_a[nxt][k] = an;
     P->timed_b[nxt][k] = bn;
     *iw = i * m->timed_weight[k];

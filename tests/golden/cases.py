@@ -24,6 +24,7 @@ CASES = {
     "custom_setup": ("custom_setup", dict(), 1.0, None),
     "dl_inputs": ("dl_inputs", dict(), 1.0, None),
     "gap_junctions": ("gap_junctions", dict(), 1.0, None),
+    "alpha_synapses": ("alpha_synapses", dict(), 1.0, None),
 }
 
 

@@ -29,6 +29,7 @@ def _same(a, b):
     ("izh_net", dict(n_cells=20, in_degree=5, length_ms=5.0)),
     ("ball_and_stick", dict(n_inst=3, length_ms=5.0)),
     ("gap_junctions", dict(length_ms=5.0)),
+    ("alpha_synapses", dict(length_ms=5.0)),
 ])
 def test_write_read_round_trip(tmp_path, name, kw):
     spec = workloads.CONFIGS[name](**kw)
