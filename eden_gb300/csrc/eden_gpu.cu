@@ -800,7 +800,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         std::vector<char> is_src(nt, 0);
         for (int s = 0; s < m->n_src; s++)
             if (m->src_target[s] >= 0) is_src[u2i[m->src_target[s]]] = 1;
-        for (size_t f = 0; f < fo_t0.size(); f++) {
+        // (forests on the host's threads; each writes its own compartments)
+        parallel_for((int64_t)fo_t0.size(), [&](int64_t f) {
             const int a = fo_t0[f], b = fo_t1[f];
             for (int it = b - 1; it >= a; it--) {
                 const int k0 = c_child0[it], k1 = c_child0[it] + c_nchild[it];
@@ -819,7 +820,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
                 const uint32_t pp = c_parent[it] >= 0 ? (uint32_t)(c_parent[it] - a + 1) : 0u;
                 c_cep[it] = ce | (cb << kCepBeginShift) | (pp << kCepParentShift) | (nonflat[it] ? kCepNonFlat : 0u);
             }
-        }
+        }, 32);
     }
     // a flat compartment's pre-update increment, or a non-flat one's L
     std::vector<float> c_kl(nt, 0.f);
@@ -877,6 +878,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     auto sort_items = [&](int64_t n, const int32_t *tgt, const int32_t *type) {
         std::vector<int64_t> idx(n), tmp(n);
         std::iota(idx.begin(), idx.end(), 0);
+        // each item's internal target, looked up once (on the host's threads)
+        std::vector<int32_t> tkey(n);
+        parallel_for(n, [&](int64_t x) { tkey[x] = u2i[tgt[x]]; });
         auto pass = [&](int nkeys, auto key) {
             std::vector<int64_t> cnt((size_t)nkeys + 1, 0);
             for (int64_t k = 0; k < n; k++) cnt[key(idx[k]) + 1]++;
@@ -884,8 +888,11 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             for (int64_t k = 0; k < n; k++) tmp[cnt[key(idx[k])]++] = idx[k];
             idx.swap(tmp);
         };
-        if (type) pass(kMaxSynTypes, [&](int64_t x) { return (int)type[x]; });
-        pass(nt, [&](int64_t x) { return (int)u2i[tgt[x]]; });
+        // (the pass by type only where the items have more than one)
+        bool one_type = true;
+        for (int64_t x = 1; type && one_type && x < n; x++) one_type = type[x] == type[0];
+        if (type && !one_type) pass(kMaxSynTypes, [&](int64_t x) { return (int)type[x]; });
+        pass(nt, [&](int64_t x) { return (int)tkey[x]; });
         return idx;
     };
     auto offsets = [&](const std::vector<int64_t> &order, const int32_t *tgt) {
