@@ -12,13 +12,19 @@ values and units) and applies them to the instances' tables before the run
 
     set input <inputList> <input ids | all> <property> <value | multi> [<unit>]
 
+    set synapse <projection> <connection ids | all> post <property> <value | multi> [<unit>]
+
 Instance ids are comma-separated; a dimensional property needs its unit.
 Built here: `set cell` on point neurons (izhikevich2007Cell, iaf*Cell,
 adExIaFCell, izhikevichCell), whose LEMS parameters become per-instance
-values in the lowered model, and `set input` on the pulse, sine, ramp (and
-their DL forms) and voltage-clamp inputs of lists read from NeuroML.  Not
-built: properties of physical cells (segment states, channel gates) and
-`set synapse` statements; they are refused by name.
+values in the lowered model; `set input` on the pulse, sine, ramp (and
+their DL forms) and voltage-clamp inputs of lists read from NeuroML; and
+`set synapse` on the postsynaptic component of a projection's connections
+(the parameters of its expOne, expTwo, alpha or alphaCurrent synapse,
+eden/NeuroML.cpp:7853-7960), where each distinct set of overridden values
+becomes a synapse type of its own in the lowered model.  Not built:
+properties of physical cells (segment states, channel gates); they are
+refused by name.
 """
 from __future__ import annotations
 
@@ -29,7 +35,8 @@ import copy
 
 import numpy as np
 
-from .network import WAVE_SINE, AdExCell, IafCell, Izhikevich2007Cell, IzhikevichCell
+from .network import (SYN_ALPHA, SYN_ALPHA_CURRENT, SYN_EXPTWO, WAVE_SINE, AdExCell, IafCell, Izhikevich2007Cell,
+                      IzhikevichCell)
 
 # LEMS parameter -> (dataclass field, dimension of the unit table, factor to the field's unit)
 _IZH = {"v0": ("v0", "voltage", 1.0), "C": ("C", "capacitance", 1.0), "k": ("k", "cond_per_voltage", 1.0),
@@ -79,6 +86,42 @@ class SetInput:
     ids: Optional[List[int]]
     prop: str
     values: List[float]
+
+
+@dataclass
+class SetSynapse:
+    """One `set synapse` statement: `values` (field units) of the synapse
+    type field `prop` for the connections of NeuroML projection `proj` with
+    the given connection ids (None: all, by id)."""
+    proj: str
+    ids: Optional[List[int]]
+    prop: str
+    values: List[float]
+
+
+def _synapse_table(st):
+    """Settable parameters of a synapse type: NeuroML name -> (field, dimension, factor)."""
+    if st.kind == SYN_ALPHA_CURRENT:
+        return {"tau": ("tau_decay", "time", 1.0), "ibase": ("gbase", "current", 1.0)}
+    t = {"gbase": ("gbase", "conductance", 1.0), "erev": ("erev", "voltage", 1.0)}
+    if st.kind == SYN_ALPHA:
+        t["tau"] = ("tau_decay", "time", 1.0)
+    else:
+        t["tauDecay"] = ("tau_decay", "time", 1.0)
+    if st.kind == SYN_EXPTWO:
+        t["tauRise"] = ("tau_rise", "time", 1.0)
+    return t
+
+
+def _proj_members(spec, proj):
+    """[(connection id, (projection index, item index))] of NeuroML
+    projection `proj`, by connection id."""
+    members = []
+    for k, pr in enumerate(spec.projections):
+        for i, (pid, cid) in enumerate(pr.conn_ids or ()):
+            if pid == proj:
+                members.append((cid, (k, i)))
+    return sorted(members)
 
 
 def _input_table(obj):
@@ -149,9 +192,38 @@ def parse(text: str, spec) -> list:
                               len(known) if ids is None else len(ids))
             out.append(SetInput(lst, ids, field, vals))
             continue
+        if len(tok) >= 2 and tok[1] == "synapse":
+            if len(tok) < 7:
+                raise ValueError(f"custom setup line {i}: 'set synapse' needs projection, connections, location, "
+                                 f"property and value")
+            proj, ids_s, loc, prop, value = tok[2], tok[3], tok[4], tok[5], tok[6]
+            members = _proj_members(spec, proj)
+            if not members:
+                raise ValueError(f"custom setup line {i}: projection {proj} not found (or without connections)")
+            if loc != "post":
+                raise ValueError(f"custom setup line {i}: location {loc!r}: a spiking connection has its synaptic "
+                                 f"component on the 'post' side only")
+            known = [cid for cid, _ in members]
+            ids = None
+            if ids_s != "all":
+                ids = [int(x) for x in ids_s.split(",")]
+                if len(set(ids)) != len(ids):
+                    raise ValueError(f"custom setup line {i}: a connection is listed twice")
+                if any(x not in known for x in ids):
+                    raise ValueError(f"custom setup line {i}: connection not in projection {proj}")
+            k0, _ = members[0][1]
+            st = spec.synapse(spec.projections[k0].synapse)
+            table = _synapse_table(st)
+            if prop not in table:
+                raise ValueError(f"custom setup line {i}: synapse {st.name} has no settable property {prop!r}")
+            field, dim, factor = table[prop]
+            vals, i = _values(lines, i, value, tok[7] if len(tok) > 7 else None, dim, factor,
+                              len(known) if ids is None else len(ids))
+            out.append(SetSynapse(proj, ids, field, vals))
+            continue
         if len(tok) < 2 or tok[1] != "cell":
             raise ValueError(f"custom setup line {i}: 'set {tok[1] if len(tok) > 1 else ''}' is not supported "
-                             f"(only 'set cell' on point neurons and 'set input')")
+                             f"(only 'set cell' on point neurons, 'set input' and 'set synapse')")
         if len(tok) < 7:
             raise ValueError(f"custom setup line {i}: 'set cell' needs population, instances, segments, "
                              f"property and value")
@@ -226,6 +298,53 @@ def apply_inputs(spec):
     return out
 
 
+MAX_SYN_TYPES = 32   # synapse types per model the GPU library takes (eden_math.cuh kMaxSynTypes)
+
+
+def apply_synapses(spec):
+    """A copy of `spec` in which the connections that `set synapse`
+    statements name use synapse types of their own: one per (synapse type,
+    distinct set of overridden values), named `<type>:<n>`, with the
+    projections split accordingly (each part keeps its connections' order);
+    `spec` itself is unchanged."""
+    import dataclasses
+    stmts = [st for st in spec.custom_setup if isinstance(st, SetSynapse)]
+    if not stmts:
+        return spec
+    over = {}
+    for st in stmts:
+        members = _proj_members(spec, st.proj)
+        by_id = dict(members)
+        ids = [cid for cid, _ in members] if st.ids is None else st.ids
+        for cid, v in zip(ids, st.values):
+            over.setdefault(by_id[cid], {})[st.prop] = float(v)
+    out = copy.copy(spec)
+    out.synapses = list(spec.synapses)
+    out.projections = []
+    derived = {}
+    for k, pr in enumerate(spec.projections):
+        keys = [tuple(sorted(over.get((k, i), {}).items())) for i in range(len(pr.pre_cell))]
+        parts = {}
+        for i, key in enumerate(keys):
+            parts.setdefault(key, []).append(i)
+        for key, idx in parts.items():
+            syn = pr.synapse
+            if key:
+                if (syn, key) not in derived:
+                    derived[(syn, key)] = f"{syn}:{len(derived)}"
+                    out.synapses.append(dataclasses.replace(spec.synapse(syn), name=derived[(syn, key)], **dict(key)))
+                syn = derived[(syn, key)]
+            sel = np.array(idx, np.int64)
+            out.projections.append(dataclasses.replace(
+                pr, name=pr.name if not key else f"{pr.name}:{syn}", synapse=syn, pre_cell=pr.pre_cell[sel],
+                post_cell=pr.post_cell[sel], post_seg=pr.post_seg[sel], weight=pr.weight[sel], delay=pr.delay[sel],
+                conn_ids=[pr.conn_ids[i] for i in idx] if pr.conn_ids else None))
+    if len(out.synapses) > MAX_SYN_TYPES:
+        raise ValueError(f"set synapse: {len(out.synapses)} synapse types after the statements, more than the "
+                         f"{MAX_SYN_TYPES} a model may have (each distinct set of values is a type)")
+    return out
+
+
 def overrides(spec) -> dict:
     """(population, instance) -> {field: value} after every statement of
     `spec.custom_setup`, later statements overriding earlier ones."""
@@ -255,6 +374,14 @@ def write(spec, path: str) -> None:
                 f.write(f"set input {st.lst} {ids} {prop} multi{unit}\n")
                 f.write("values " + " ".join(_f(v) for v in st.values) + "\n")
                 continue
+            if isinstance(st, SetSynapse):
+                members = _proj_members(spec, st.proj)
+                syn = spec.synapse(spec.projections[members[0][1][0]].synapse)
+                prop, (field, dim, factor) = next((k, v) for k, v in _synapse_table(syn).items() if v[0] == st.prop)
+                ids = "all" if st.ids is None else ",".join(str(x) for x in st.ids)
+                f.write(f"set synapse {st.proj} {ids} post {prop} multi {unit_of[dim]}\n")
+                f.write("values " + " ".join(_f(v / factor) for v in st.values) + "\n")
+                continue
             ct = spec.cell_type({p.name: p for p in spec.populations}[st.pop].cell_type)
             prop, (field, dim, factor) = next((k, v) for k, v in _params_of(ct).items() if v[0] == st.prop)
             ids = "all" if st.ids is None else ",".join(str(x) for x in st.ids)
@@ -269,4 +396,5 @@ def apply_to(ct, fields: dict):
     return dataclasses.replace(ct, **fields)
 
 
-__all__ = ["SetCell", "SetInput", "parse", "overrides", "write", "apply_to", "apply_inputs"]
+__all__ = ["SetCell", "SetInput", "SetSynapse", "parse", "overrides", "write", "apply_to", "apply_inputs",
+           "apply_synapses"]

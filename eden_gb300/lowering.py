@@ -494,8 +494,8 @@ def joined(parts, dtype) -> np.ndarray:
 
 def lower(spec: NetworkSpec) -> LoweredModel:
     if spec.custom_setup:
-        from .custom_setup import apply_inputs
-        spec = apply_inputs(spec)
+        from .custom_setup import apply_inputs, apply_synapses
+        spec = apply_synapses(apply_inputs(spec))
     dt = _to_f32(spec.dt * 1000.0)
     gid_off = spec.pop_offsets()
     n_cells = spec.n_cells

@@ -292,6 +292,7 @@ class Projection:
     post_seg: np.ndarray     # int segment id on the post cell
     weight: np.ndarray       # float, dimensionless
     delay: np.ndarray        # float, ms
+    conn_ids: Optional[list] = None   # per connection, (projection id, connection id) as read from NeuroML
 
 
 @dataclass

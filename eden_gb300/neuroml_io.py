@@ -220,19 +220,23 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
                 f.write(repr(float(ts)) + "".join(f" {i}!{q}" for i, q in pairs) + "\n")
     pop_of, local_of = _gid_maps(spec)
     for pr in spec.projections:
-        # consecutive runs of one (pre, post) population pair, so the file's
-        # connection order -- the reference's instantiation order -- is the
-        # projection's own
+        # consecutive runs of one (pre, post) population pair -- and, where the
+        # connections carry the (projection id, connection id) they were read
+        # with, of one such projection, so `set synapse` statements still
+        # name them -- so the file's connection order, the reference's
+        # instantiation order, is the projection's own
+        ids = pr.conn_ids
         groups = []
         for i in range(len(pr.pre_cell)):
-            key = (pop_of[pr.pre_cell[i]], pop_of[pr.post_cell[i]])
+            key = (pop_of[pr.pre_cell[i]], pop_of[pr.post_cell[i]], ids[i][0] if ids else None)
             if not groups or groups[-1][0] != key:
                 groups.append((key, []))
             groups[-1][1].append(i)
-        for gi, ((pa, pb), idx) in enumerate(groups):
-            w(f' <projection id="{pr.name}_{gi}" presynapticPopulation="{pa}" '
+        for gi, ((pa, pb, pid), idx) in enumerate(groups):
+            w(f' <projection id="{pid if ids else f"{pr.name}_{gi}"}" presynapticPopulation="{pa}" '
               f'postsynapticPopulation="{pb}" synapse="{pr.synapse}">\n')
-            for n, i in enumerate(idx):
+            for n0, i in enumerate(idx):
+                n = ids[i][1] if ids else n0
                 if pa in readers:
                     inst, port = divmod(local_of[pr.pre_cell[i]], len(readers[pa].ports))
                     w(f'  <connectionWD id="{n}" preCellId="{inst}" preSegmentId="{readers[pa].ports[port]}" '
@@ -506,11 +510,17 @@ def _parse_rate(el):
                 _qty(el, "scale", "voltage"))
 
 
-def _parse_cell(el, channels_by_name):
+def _parse_cell(el, channels_by_name, top=None):
+    """A <cell>; its morphology and biophysicalProperties inline or, by the
+    cell's attributes of those names, top-level elements of `top` (id ->
+    element)."""
     name = el.get("id")
+    top = top or {}
     morph = _children(el, "morphology")
+    if not morph and el.get("morphology") in top:
+        morph = [top[el.get("morphology")]]
     if len(morph) != 1:
-        raise ValueError(f"cell {name}: exactly one inline <morphology> is supported")
+        raise ValueError(f"cell {name}: exactly one <morphology> is supported")
     segs = _children(morph[0], "segment")
     ids = [int(s.get("id")) for s in segs]
     index = {sid: i for i, sid in enumerate(ids)}
@@ -556,7 +566,12 @@ def _parse_cell(el, channels_by_name):
             raise ValueError(f"cell {name}: segment group properties (cable subdivision) are not supported")
         groups[g.get("id")] = mask
     groups.setdefault("all", np.ones(n, bool))
-    bio = _children(el, "biophysicalProperties")[0]
+    bio = _children(el, "biophysicalProperties")
+    if not bio and el.get("biophysicalProperties") in top:
+        bio = [top[el.get("biophysicalProperties")]]
+    if len(bio) != 1:
+        raise ValueError(f"cell {name}: exactly one <biophysicalProperties> is supported")
+    bio = bio[0]
     mem = _children(bio, "membraneProperties")[0]
     intra = _children(bio, "intracellularProperties")[0]
     dens = []
@@ -648,6 +663,8 @@ def read_lems(path: str) -> NetworkSpec:
     timed_def, wave_def, clamp_def, gap_def = {}, {}, {}, {}
     refused_inputs = {}
     net = None
+    # morphologies and biophysical properties a cell may name by id
+    top_parts = {e.get("id"): e for e in elems if _tag(e) in ("morphology", "biophysicalProperties")}
     for e in elems:
         t = _tag(e)
         if t == "ionChannelHH" or t == "ionChannel":
@@ -781,7 +798,7 @@ def read_lems(path: str) -> NetworkSpec:
             net = e
     for e in elems:
         if _tag(e) == "cell":
-            cells[e.get("id")] = _parse_cell(e, channels_by_name)
+            cells[e.get("id")] = _parse_cell(e, channels_by_name, top_parts)
     if net is None:
         raise ValueError(f"network {sim.get('target')} not found")
     if _tag(net) == "networkWithTemperature" or net.get("type") == "networkWithTemperature":
@@ -844,10 +861,11 @@ def read_lems(path: str) -> NetworkSpec:
         syn = pr.get("synapse")
         if syn not in synapses:
             raise ValueError(f"projection {pr.get('id')}: synapse {syn} not supported")
-        rows = by_syn.setdefault(syn, [[], [], [], [], []])
+        rows = by_syn.setdefault(syn, [[], [], [], [], [], []])
         for c in pr:
             if _tag(c) not in ("connectionWD", "connection"):
                 continue
+            rows[5].append((pr.get("id"), int(c.get("id"))))
             rows[0].append(pre_gid(c, pr))
             rows[1].append(gid(_cell_ref(c.get("postCellId"), pops, pr.get("postsynapticPopulation"))))
             rows[2].append(int(c.get("postSegmentId", "0")))
@@ -856,7 +874,7 @@ def read_lems(path: str) -> NetworkSpec:
     for syn, rows in by_syn.items():
         spec.projections.append(Projection(f"proj_{syn}", "*", "*", syn, np.array(rows[0], np.int64),
                                            np.array(rows[1], np.int64), np.array(rows[2], np.int64),
-                                           np.array(rows[3]), np.array(rows[4])))
+                                           np.array(rows[3]), np.array(rows[4]), conn_ids=rows[5]))
     # electrical projections: gap junctions, an instance on each end
     # (eden/NeuroML.cpp:6057-6125: electricalConnection with cell indices,
     # electricalConnectionInstance(W) with cell paths, W with a weight)

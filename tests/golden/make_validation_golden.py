@@ -1,9 +1,10 @@
 """Fixtures of the reference's own validation networks for the GPU.
 
-Reads five of the reference's validation networks
+Reads six of the reference's validation networks
 (testing/validation_tests/neuroml/LEMS_EdenTest_CoreInputs.xml,
 LEMS_EdenTest_PassiveCompartment.xml, LEMS_EdenTest1.xml,
-LEMS_EdenTest2.xml and LEMS_EdenTest_DomainDecomposition.xml) with this
+LEMS_EdenTest2.xml, LEMS_EdenTest_DomainDecomposition.xml and
+EdenTest_Extension_CustomSetup.nml with its custom setup file) with this
 package's NeuroML reader,
 writes each lowered network as a model file (eden_gb300/model_file.py) that
 the C++ host program runs through the C ABI, and stores the reference
@@ -35,6 +36,7 @@ NETWORKS = {
     "edentest1": ("LEMS_EdenTest1.xml", "results1.txt", 1),
     "edentest2": ("LEMS_EdenTest2.xml", "results1.txt", 1),
     "domain_decomposition": ("LEMS_EdenTest_DomainDecomposition.xml", "results.gen.txt", 4),
+    "custom_setup_ext": ("EdenTest_Extension_CustomSetup.nml", "results.gen.txt", 4),
 }
 
 

@@ -1,4 +1,4 @@
-"""Five of the reference's own validation networks on the GPU, run by the
+"""Six of the reference's own validation networks on the GPU, run by the
 C++ host program (eden_gb300/host/eden_gpu_host) through the C ABI:
 LEMS_EdenTest_CoreInputs (pulse, weighted pulse, sine, ramp and their DL
 forms, voltage clamps, timed input, spike array and generator),
@@ -7,7 +7,10 @@ cells with frustum dendrites, a gap junction, an expOne connection, a
 sodium gate's state recorded), LEMS_EdenTest2 (an HH cell with its m, h
 and n recorded) and LEMS_EdenTest_DomainDecomposition (14 spiking
 two-compartment cells, gap junctions, expOne connections; compared by the
-reference's box(0.1 ms, 0.5 mV) criterion), read by this package's NeuroML reader and lowered into
+reference's box(0.1 ms, 0.5 mV) criterion) and EdenTest_Extension_CustomSetup
+(izhikevichCell instances and pulse inputs customised per instance, expOne
+connections customised per connection, whose halves must be identical),
+read by this package's NeuroML reader and lowered into
 model files (tests/golden/make_validation_golden.py), against the
 reference simulator's own output on the same files: every recorded
 potential within the stated mV (0.01 for the networks without spikes; the
@@ -29,7 +32,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 @pytest.mark.parametrize("mode", ["batched", "plain"])
 @pytest.mark.parametrize("name,tol_mv", [("core_inputs", 0.01), ("passive_compartment", 0.01), ("edentest1", 0.05),
-                                         ("edentest2", 0.05), ("domain_decomposition", None)])
+                                         ("edentest2", 0.05), ("domain_decomposition", None),
+                                         ("custom_setup_ext", 0.1)])
 def test_validation_network_on_gpu_matches_reference(name, tol_mv, mode, tmp_path):
     z = np.load(os.path.join(HERE, "golden", f"validation_{name}.npz"))
     traj, ev = str(tmp_path / "traj.txt"), str(tmp_path / "ev.txt")
@@ -51,3 +55,9 @@ def test_validation_network_on_gpu_matches_reference(name, tol_mv, mode, tmp_pat
     err = np.abs(mine[:, 1:] - ref[:, 1:]) / scale  # engine units
     tol = np.where(scale == 1.0, tol_mv * 1e-2, tol_mv)
     assert (err <= tol).all(), err.max(0)
+    if name == "custom_setup_ext":
+        # the reference's half_vs_half criteria
+        # (testing/validation_tests/validation_tests.py:31-42): identical traces
+        full = np.loadtxt(traj, ndmin=2)[:, 1:]
+        for a, b in [(5, 0), (6, 1), (7, 2), (8, 3), (9, 4), (10, 12), (11, 13)]:
+            np.testing.assert_array_equal(full[:, a], full[:, b])

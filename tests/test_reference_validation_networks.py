@@ -30,6 +30,9 @@ from eden_gb300 import lowering, neuroml_io
     # 100 ms: spikes move by a step, so the reference's own criterion,
     # box(0.1 ms, 0.5 mV), is the measure (tol_mv None)
     ("LEMS_EdenTest_DomainDecomposition.xml", "results.gen.txt", None),
+    # izhikevichCell populations customised per instance by `set cell` and
+    # `set input`, and expOne connections by `set synapse`
+    ("EdenTest_Extension_CustomSetup.nml", "results.gen.txt", 0.1),
 ])
 def test_oracle_matches_the_reference_on_its_validation_network(name, outfile, tol_mv):
     path = reference_runner.validation_network(name)
@@ -58,3 +61,29 @@ def test_oracle_matches_the_reference_on_its_validation_network(name, outfile, t
         return
     tol = np.where(scale == 1.0, tol_mv * 1e-2, tol_mv)
     assert (np.abs(mine - ref_eng) <= tol).all(), np.abs(mine - ref_eng).max(0)
+
+
+# The reference's half_vs_half criteria for EdenTest_Extension_CustomSetup.nml
+# (testing/validation_tests/validation_tests.py:31-42), as pairs of output
+# columns whose traces must be identical: each customised instance of pop0
+# against the uncustomised cell it reproduces, and the two connections of
+# ToPopp_ExpWild customised into copies of ToPopp_ExpSlow and ToPopp_ExpFast.
+CUSTOM_SETUP_PAIRS = [(5, 0), (6, 1), (7, 2), (8, 3), (9, 4), (10, 12), (11, 13)]
+
+
+def test_custom_setup_network_halves_are_identical_on_the_oracle():
+    path = reference_runner.validation_network("EdenTest_Extension_CustomSetup.nml")
+    if path is None:
+        pytest.skip("reference tree not present")
+    spec = neuroml_io.read_lems(path)
+    low = lowering.lower(spec)
+    assert len(spec.synapses) == 3 and len(low.syn_types) == 5
+    tr = eden_port.run(low)["trace"]
+    for a, b in CUSTOM_SETUP_PAIRS:
+        np.testing.assert_array_equal(tr[:, a], tr[:, b])
+    # the customisation is what makes them equal
+    import copy
+    plain = copy.copy(spec)
+    plain.custom_setup = []
+    tr0 = eden_port.run(lowering.lower(plain))["trace"]
+    assert all(np.abs(tr0[:, a] - tr0[:, b]).max() > 1.0 for a, b in CUSTOM_SETUP_PAIRS)
