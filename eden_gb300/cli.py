@@ -130,7 +130,7 @@ def write_outputs(spec, low, rec, base_dir: str, n_steps: int) -> list:
 
 
 def run_lems(lems_file: str, seed: int | None = None, mode: str = "batched", verbose: bool = False,
-             out_dir: str | None = None) -> dict:
+             out_dir: str | None = None, cable_solver: str = "auto") -> dict:
     """Simulate a LEMS file on the GPU and write its output files next to it
     (or in out_dir).  Returns timing in seconds: config, setup, run."""
     from .engine import MODE_BATCHED, MODE_PLAIN, Simulation
@@ -138,6 +138,7 @@ def run_lems(lems_file: str, seed: int | None = None, mode: str = "batched", ver
     spec = neuroml_io.read_lems(lems_file)
     if seed is not None:
         spec.seed = seed
+    spec.cable_solver = cable_solver
     t1 = time.perf_counter()
     low = lowering.lower(spec)
     sim = Simulation(low, mode=MODE_PLAIN if mode == "plain" else MODE_BATCHED)
@@ -154,7 +155,7 @@ def run_lems(lems_file: str, seed: int | None = None, mode: str = "batched", ver
 
 def main(argv=None) -> int:
     argv = list(sys.argv[1:] if argv is None else argv)
-    lems, seed, verbose, mode = None, None, False, "batched"
+    lems, seed, verbose, mode, cable = None, None, False, "batched", "auto"
     i = 0
     while i < len(argv):
         tok = argv[i]
@@ -167,9 +168,16 @@ def main(argv=None) -> int:
             i += 2
             continue
         if tok == "cable_solver":
-            if argv[i + 1] not in ("auto", "bwd_euler"):
-                print(f"cable_solver {argv[i + 1]} is not available on the GPU path (backward Euler only)")
+            # eden/Eden.cpp:10485-10500
+            if i + 1 >= len(argv):
+                print(f"cmdline: {tok} type missing")
                 return 2
+            cable = argv[i + 1]
+            if cable not in ("auto", "bwd_euler", "fwd_euler"):
+                print(f"cmdline: unknown cable solver {cable}")
+                return 2
+            if cable == "fwd_euler":
+                print("Cable solver set to Forward Euler: make sure system is stable")
             i += 2
             continue
         if tok == "verbose":
@@ -188,7 +196,7 @@ def main(argv=None) -> int:
         return 2
     print("--- Extensible Dynamics Engine for Networks (GB300 step loop) ---")
     try:
-        t = run_lems(lems, seed=seed, mode=mode, verbose=verbose)
+        t = run_lems(lems, seed=seed, mode=mode, verbose=verbose, cable_solver=cable)
     except (ValueError, OSError) as e:
         print(f"cmdline: could not make sense of NeuroML file: {e}")
         return 1

@@ -216,6 +216,8 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
         return ctx->fail(EDEN_GPU_E_INVALID, "too many synapses");
     if (m->n_chan_types > kMaxChanTypes || m->n_syn_types > kMaxSynTypes)
         return ctx->fail(EDEN_GPU_E_INVALID, "too many channel or synapse types");
+    if (m->cable_solver != EDEN_CABLE_BWD_EULER && m->cable_solver != EDEN_CABLE_FWD_EULER)
+        return ctx->fail(EDEN_GPU_E_INVALID, "unknown cable solver %d", m->cable_solver);
     if (m->phys_comp_off[0] != 0 || m->phys_comp_off[m->n_phys] != m->n_comp)
         return ctx->fail(EDEN_GPU_E_INVALID, "phys_comp_off must span [0, n_comp]");
     for (int c = 0; c < m->n_phys; c++) {
@@ -487,8 +489,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     // times the event jump), so a cell can lose dominance only through a
     // negative channel density, synaptic gbase, expTwo jump or weight.  Such
     // cells are flagged: their elimination runs in double precision.
+    // (the forward-Euler update solves nothing: no cell is flagged)
     std::vector<char> cell_f64(n_phys, 0);
-    {
+    if (m->cable_solver == EDEN_CABLE_BWD_EULER) {
         auto syn_sign = [&](int type, float w) {
             const EdenGpuSynapseType &st = m->syn_types[type];
             float sg = st.gbase * w;
@@ -1266,7 +1269,9 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (auto &cl : ctx->classes) max_smem_class = std::max(max_smem_class, cl.smem);
     // (the windowed kernel packs forest-local indices in 10 bits: a single
     // cell of more than 1023 compartments runs the per-step kernels)
-    ctx->smem_window = max_smem_class <= (size_t)ctx->smem_optin && max_forest <= 1023;
+    // (the forward-Euler update runs the per-step kernels only)
+    ctx->smem_window = max_smem_class <= (size_t)ctx->smem_optin && max_forest <= 1023 &&
+                       m->cable_solver == EDEN_CABLE_BWD_EULER;
 
     phase("upload");
     // ---- upload
@@ -1283,6 +1288,19 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     TRY(upload_c(ctx, &d.c_cm, c_cm)); TRY(upload_c(ctx, &d.c_inv_rc, c_inv)); TRY(upload_c(ctx, &d.c_area, c_area));
     TRY(upload_c(ctx, &d.c_u, c_u)); TRY(upload_c(ctx, &d.c_l, c_l));
     TRY(upload_c(ctx, &d.c_cend, c_cend)); TRY(upload_c(ctx, &d.c_parent, c_parent));
+    d.fwd_euler = m->cable_solver == EDEN_CABLE_FWD_EULER ? 1 : 0;
+    if (d.fwd_euler) {
+        // each node's axial resistance to its parent and the start of its
+        // child range (empty ranges start at their end)
+        std::vector<float> c_rax(nt, 0.0f);
+        std::vector<int32_t> c_kb(nt, 0);
+        for (int it = 0; it < nt; it++) {
+            const int ut = i2u[it];
+            if (ut < n_comp && c_parent[it] >= 0) c_rax[it] = m->comp_r_axial[ut];
+            c_kb[it] = c_nchild[it] > 0 ? c_child0[it] : c_cend[it];
+        }
+        TRY(upload_c(ctx, &d.c_rax, c_rax)); TRY(upload_c(ctx, &d.c_kb, c_kb));
+    }
     TRY(upload_c(ctx, &d.c_kl, c_kl)); TRY(upload_c(ctx, &d.c_pv0, c_pv0));
     TRY(upload_c(ctx, &d.c_rt0, c_rt0)); TRY(upload_c(ctx, &d.c_cep, c_cep)); TRY(upload_c(ctx, &d.t_izh, t_izh));
     TRY(upload_c(ctx, &d.fo_t0, fo_t0)); TRY(upload_c(ctx, &d.fo_t1, fo_t1)); TRY(upload_c(ctx, &d.fo_l0, fo_l0));

@@ -755,6 +755,8 @@ int validate(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
                        "inputs and %lld gap-junction ends",
                        m->n_izh, (long long)m->n_pois, (long long)m->n_wave, (long long)m->n_clamp,
                        (long long)m->n_gap);
+    if (m->cable_solver != EDEN_CABLE_BWD_EULER)
+        return g->fail(EDEN_GPU_E_INVALID, "gradients follow the backward-Euler cable solve only");
     for (int k = 0; k < m->n_syn_types; k++) {
         const EdenGpuSynapseType &t = m->syn_types[k];
         if ((t.kind != EDEN_SYN_EXPONE && t.kind != EDEN_SYN_EXPTWO) || !std::isfinite(t.gbase) ||

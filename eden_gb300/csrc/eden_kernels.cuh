@@ -100,6 +100,11 @@ struct DevModel {
     const float *c_cm, *c_inv_rc, *c_area, *c_u, *c_l;  // U = -dt/(R C_i), L = -dt/(R C_parent)
     const int32_t *c_cend, *c_parent;  // end of each node's child range; parent (internal, -1 at roots)
     const int32_t *t_izh;                            // izhikevich index or -1
+    // forward-Euler cable update (fwd_euler != 0): each node's axial
+    // resistance to its parent and the start of its child range
+    int32_t fwd_euler;
+    const float *c_rax;
+    const int32_t *c_kb;
     // windowed-path constants of each physical compartment.  A "flat"
     // compartment has one gateless channel, no inputs, is no spike source and
     // has only flat compartments below it; everything else is "non-flat".
@@ -1046,8 +1051,22 @@ __device__ __forceinline__ bool point_update(int kind, const float *p, int ps, b
 // voltage pre-update of a compartment (eden/Eden.cpp:5013-6107), writing the
 // pre-updated V to *x and the Hines diagonal to *d, or the izhikevich2007
 // update (LEMS_CoreComponents.inc.xml:1140-1185), writing v' to *x.
+// Axial current into compartment t for the forward-Euler cable update
+// (eden/Eden.cpp:4969-4990): (V_adj - V) / R summed over the neighbours in
+// ascending compartment order -- the parent, then the children, which the
+// breadth-first numbering keeps in that order -- from the potentials at the
+// start of the step; R is the axial resistance of the edge's child end.
+__device__ __forceinline__ float axial_current(const DevModel &m, int t, float v, const float *vin) {
+    float I = 0.0f;
+    const int p = m.c_parent[t];
+    if (p >= 0) I += (vin[p] - v) / m.c_rax[t];
+    for (int k = m.c_kb[t]; k < m.c_cend[t]; k++) I += (vin[k] - v) / m.c_rax[k];
+    return I;
+}
+
 __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init, int64_t step, float tnow, float v,
-                                            float Iin, float Gin, float Isyn, float Gsyn, float *x, float *d, int wpar) {
+                                            float Iin, float Gin, float Isyn, float Gsyn, float *x, float *d, int wpar,
+                                            float Iax = 0.0f) {
     if (!init) {
         for (int k = m.t_trace0[t]; k < m.t_trace0[t + 1]; k++) {
             int64_t row = (step - 1) % m.trace_cap;
@@ -1079,7 +1098,9 @@ __device__ __forceinline__ void target_step(const DevModel &m, int t, bool init,
         float G = Gch + Gin + Gsyn;
         float C = m.c_cm[t];
         *d = 1.0f * (G / C) + m.c_inv_rc[t];
-        *x = init ? v : v + (m.dt * (I + (v * G))) / C;
+        // backward Euler: the pre-updated V the Hines solve starts from;
+        // forward Euler: V_next (eden/Eden.cpp:6092-6094)
+        *x = init ? v : m.fwd_euler ? v + (m.dt * (I + Iax)) / C : v + (m.dt * (I + (v * G))) / C;
     } else {
         float u = m.iz_u[iz], sv = m.iz_s[iz], vn;
         const bool spike = point_update(m.iz_kind[iz], m.iz_p + iz, m.n_izh, init, tnow, m.dt, v, Isyn + Iin, u, sv, vn);

@@ -66,7 +66,8 @@ __global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs 
             block_currents(m.Gp, m.t_blk0[i], m.t_blk0[i + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
                            Gsyn);
             if (EDEN_KIND_GAP) Isyn += gap_current(m, i, v, vin);
-            target_step(m, i, init, w.step0, tnow, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar);
+            const float Iax = (m.fwd_euler && !init && m.t_izh[i] < 0) ? axial_current(m, i, v, vin) : 0.0f;
+            target_step(m, i, init, w.step0, tnow, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar, Iax);
         }
     }
 }
@@ -89,7 +90,11 @@ __global__ void __launch_bounds__(kHinesThreads) k_hines_t(DevModel m, const Win
     for (int f = warp; f < m.n_forest; f += nwarps) {
         const int c0 = m.fo_t0[f], n = m.fo_t1[f] - c0, nlev = m.fo_nlev[f];
         const int32_t *lv = m.lvl + m.fo_l0[f];
-        if (m.fo_f64[f]) {
+        if (m.fwd_euler) {
+            // V_next is final already: only the threshold test
+            hines_forest(m, true, w.step0, w.t0, m.diag, x, m.c_u, m.c_l, m.c_cend, m.c_parent, lv, nlev, vin, 0,
+                         w.wpar, true);
+        } else if (m.fo_f64[f]) {
             hines_forest_f64(m, init, w.step0, w.t0, m.diag, x, m.c_u, m.c_l, m.c_cend, m.c_parent, lv, nlev, vin,
                              m.dscr, m.dscr + m.n_target, w.wpar);
         } else if (n <= cap && nlev < cap) {

@@ -130,6 +130,7 @@ void fill_model(const Reader &r, EdenGpuModel &m) {
     I64(n_clamp); PTR(clamp_target, int32_t); PTR(clamp_params, float); PTR(clamp_weight, float);
     I64(n_gap); PTR(gap_target, int32_t); PTR(gap_peer, int32_t); PTR(gap_conductance, float);
     PTR(gap_weight, float);
+    I32(cable_solver);
 #undef I32
 #undef I64
 #undef PTR

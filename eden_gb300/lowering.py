@@ -152,6 +152,8 @@ class LoweredModel:
     gap_peer: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     gap_conductance: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     gap_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    # cable solver of the physical cells: CABLE_BWD_EULER or CABLE_FWD_EULER
+    cable_solver: int = 0
 
     @property
     def n_comp(self) -> int:
@@ -490,6 +492,19 @@ def poisson_rng_bases(spec: NetworkSpec, gid_ctype: np.ndarray, gid_is_point: np
 
 def joined(parts, dtype) -> np.ndarray:
     return np.concatenate(parts).astype(dtype) if parts else np.zeros(0, dtype)
+
+
+CABLE_BWD_EULER = 0
+CABLE_FWD_EULER = 1
+
+
+def _cable_solver(spec) -> int:
+    """The model's cable solver: the reference's `cable_solver` setting,
+    where `auto` means backward Euler (eden/Eden.cpp:4699-4702)."""
+    name = getattr(spec, "cable_solver", "auto")
+    if name not in ("auto", "bwd_euler", "fwd_euler"):
+        raise ValueError(f"cable solver {name!r} unknown (auto, bwd_euler or fwd_euler)")
+    return CABLE_FWD_EULER if name == "fwd_euler" else CABLE_BWD_EULER
 
 
 def lower(spec: NetworkSpec) -> LoweredModel:
@@ -855,13 +870,14 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         pois_rng_base=prng, clamp_target=ct_, clamp_params=cpar, clamp_weight=cwt,
         gap_target=np.asarray(gj_t, np.int32), gap_peer=np.asarray(gj_p, np.int32),
         gap_conductance=np.asarray(gj_g, F32), gap_weight=np.asarray(gj_w, F32),
+        cable_solver=_cable_solver(spec),
     )
 
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 9
+ABI_VERSION = 10
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -894,7 +910,7 @@ class CModel(ctypes.Structure):
         ("pois_rng_base", _i32p),
         ("n_clamp", ctypes.c_int64), ("clamp_target", _i32p), ("clamp_params", _f32p), ("clamp_weight", _f32p),
         ("n_gap", ctypes.c_int64), ("gap_target", _i32p), ("gap_peer", _i32p), ("gap_conductance", _f32p),
-        ("gap_weight", _f32p),
+        ("gap_weight", _f32p), ("cable_solver", ctypes.c_int32),
     ]
 
 
@@ -989,4 +1005,5 @@ def to_cmodel(m: LoweredModel):
     cm.gap_peer = p(m.gap_peer, np.int32, _i32p)
     cm.gap_conductance = p(m.gap_conductance, F32, _f32p)
     cm.gap_weight = p(m.gap_weight, F32, _f32p)
+    cm.cable_solver = int(m.cable_solver)
     return cm, keep

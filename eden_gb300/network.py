@@ -440,6 +440,7 @@ class NetworkSpec:
     event_selections: List[EventSelection] = field(default_factory=list)
     event_file: str = "spikes.txt"
     event_format: str = "TIME_ID"
+    cable_solver: str = "auto"   # the reference's cable_solver setting: auto (= bwd_euler), bwd_euler, fwd_euler
 
     # -- lookups ---------------------------------------------------------
     def _index(self, attr: str, items) -> dict:

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 9
+#define EDEN_GPU_ABI_VERSION 10
 
 enum {
     EDEN_GPU_OK = 0,
@@ -122,6 +122,7 @@ typedef struct EdenGpuChannelType {
 } EdenGpuChannelType;
 
 enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1, EDEN_SYN_ALPHA = 2, EDEN_SYN_ALPHA_CURRENT = 3 };
+enum { EDEN_CABLE_BWD_EULER = 0, EDEN_CABLE_FWD_EULER = 1 };
 
 /* expOneSynapse (native, eden/Eden.cpp:3424-3466), expTwoSynapse,
  * alphaSynapse or alphaCurrentSynapse (LEMS, LEMS_CoreComponents.inc.xml:
@@ -272,6 +273,16 @@ typedef struct EdenGpuModel {
     const int32_t *gap_peer;        /* compartment at the other end */
     const float *gap_conductance;   /* uS */
     const float *gap_weight;
+
+    /* cable solver of the physical cells (the reference's command-line
+     * `cable_solver`, eden/Eden.cpp:10485-10500): EDEN_CABLE_BWD_EULER, its
+     * default, the backward-Euler Hines solve; or EDEN_CABLE_FWD_EULER, the
+     * explicit update V_next = V + dt (I + I_axial) / C with
+     * I_axial = sum of (V_adj - V) / R over the compartment's neighbours
+     * in ascending compartment order (parent, then children), from the
+     * potentials at the start of the step (4969-4990, 6092-6094).  A
+     * forward-Euler model runs the per-step kernels in either mode. */
+    int32_t cable_solver;
 } EdenGpuModel;
 
 /* Execution options. */

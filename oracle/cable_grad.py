@@ -72,8 +72,9 @@ class Cable:
     map: chan_param[ch] / cell_ra_param[c] give the parameter index or -1."""
 
     def __init__(self, low, chan_param, cell_ra_param=None, cell_ra=None, syn_param=None, timed_param=None):
-        if low.n_izh or len(low.pois_target) or len(low.gap_target):
-            raise ValueError("physical cells with HH channels, pulse inputs and fixed synaptic drive only")
+        if low.n_izh or len(low.pois_target) or len(low.gap_target) or low.cable_solver:
+            raise ValueError("physical cells with HH channels, pulse inputs and fixed synaptic drive only, "
+                             "backward-Euler cable solve")
         self.low = low
         self.syn_param = np.full(len(low.syn_target), -1) if syn_param is None else np.asarray(syn_param, np.int64)
         self.timed_param = (np.full(len(low.timed_target), -1) if timed_param is None

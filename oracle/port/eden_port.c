@@ -409,6 +409,22 @@ static PORT_FN void phys_cell_step(Port *P, int cur, int32_t cell, int init, rea
     int32_t c0 = m->phys_comp_off[cell], c1 = m->phys_comp_off[cell + 1];
     const real *V = P->v[cur];
     real *Vn = P->v[nxt];
+    const int fwd = m->cable_solver == EDEN_CABLE_FWD_EULER;
+    if (fwd && !init) {
+        /* forward Euler: each compartment's axial current (V_adj - V) / R
+         * summed over its neighbours in ascending order -- the parent, then
+         * the children (eden/Eden.cpp:4969-4990, R_Axial of the higher index
+         * of the pair) -- into diag.  Visiting the compartments in ascending
+         * order adds, for each one, its parent's term at its own visit and
+         * its children's at theirs, later and in ascending order. */
+        for (int32_t c = c0; c < c1; c++) P->diag[c] = R(0.0);
+        for (int32_t c = c0 + 1; c < c1; c++) {
+            int32_t j = c0 + m->comp_parent[c];
+            real Rr = m->comp_r_axial[c > j ? c : j];
+            P->diag[c] += (V[j] - V[c]) / Rr;
+            P->diag[j] += (V[c] - V[j]) / Rr;
+        }
+    }
     for (int32_t c = c0; c < c1; c++) {
         real A = m->comp_area[c], Vc = V[c];
         real Ich = R(0.0), Gch = R(0.0);
@@ -465,10 +481,15 @@ static PORT_FN void phys_cell_step(Port *P, int cur, int32_t cell, int init, rea
         target_currents(P, cur, c, init, t, dt, step, Vc, &Iin, &Gin, &Isyn, &Gsyn);
         real I = Ich + Iin + Isyn;
         real G = Gch + Gin + Gsyn;
+        if (fwd) {
+            /* V_next = V + dt (I + I_axial) / C (eden/Eden.cpp:6092-6094) */
+            Vn[c] = init ? Vc : Vc + (dt * (I + P->diag[c])) / m->comp_c[c];
+            continue;
+        }
         P->diag[c] = R(1.0) * (G / m->comp_c[c]) + m->comp_inv_rc[c];
         Vn[c] = init ? Vc : Vc + (dt * (I + (Vc * G))) / m->comp_c[c];
     }
-    if (!init) {
+    if (!init && !fwd) {
         int32_t n = c1 - c0;
         const int32_t *ord = P->order + c0;
         const int32_t *par = m->comp_parent + c0;

@@ -25,6 +25,13 @@ CASES = {
     "dl_inputs": ("dl_inputs", dict(), 1.0, None),
     "gap_junctions": ("gap_junctions", dict(), 1.0, None),
     "alpha_synapses": ("alpha_synapses", dict(), 1.0, None),
+    # the reference's `cable_solver fwd_euler` (an explicit cable update):
+    # HH ball-and-stick cells with five dendrite compartments, and the
+    # branched cells of the input-kinds case (stable at dt 0.025 ms, unlike
+    # the finer compartments of the other multicompartment cases)
+    "ball_and_stick_fwd": ("ball_and_stick", dict(n_inst=8, n_dend=5, length_ms=40.0, cable_solver="fwd_euler"),
+                           1.0, None),
+    "input_kinds_fwd": ("input_kinds", dict(cable_solver="fwd_euler"), 1.0, None),
 }
 
 
@@ -40,9 +47,16 @@ FULL_CASES = {
 
 
 def spec_of(name):
+    """The case's network; a `cable_solver` entry among its arguments is the
+    simulator setting (the reference's command-line option), not the
+    generator's."""
     from eden_gb300 import workloads
     gen, kw = (CASES[name][0], CASES[name][1]) if name in CASES else FULL_CASES[name][:2]
-    return workloads.CONFIGS[gen](**kw)
+    kw = dict(kw)
+    solver = kw.pop("cable_solver", "auto")
+    spec = workloads.CONFIGS[gen](**kw)
+    spec.cable_solver = solver
+    return spec
 
 
 # EDEN's extended loggers, added to the izh_net case's LEMS file: a trajectory

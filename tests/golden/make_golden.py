@@ -30,7 +30,8 @@ def make(name):
     stride = FULL_CASES[name][2] if name in FULL_CASES else 1
     with tempfile.TemporaryDirectory() as d:
         lems = neuroml_io.write_lems(spec, d)
-        out = reference_runner.run(lems, threads=8)
+        extra = () if spec.cable_solver == "auto" else ("cable_solver", spec.cable_solver)
+        out = reference_runner.run(lems, threads=8, extra=extra)
     traj = out["trajectory"].astype(np.float64)[::stride]
     ev = np.array(out.get("events", []), dtype=np.float64).reshape(-1, 2)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), time_s=traj[:, 0], values_si=traj[:, 1:].astype(np.float32),

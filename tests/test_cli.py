@@ -91,7 +91,8 @@ def test_step_times_accumulate_like_the_reference():
 def test_command_line_rejects_unknown_tokens(capsys):
     assert cli.main(["nml", "x.xml", "bogus_token"]) == 2
     assert cli.main([]) == 2
-    assert cli.main(["nml", "x.xml", "cable_solver", "fwd_euler"]) == 2
+    assert cli.main(["nml", "x.xml", "cable_solver", "rk4"]) == 2
+    assert cli.main(["nml", "x.xml", "cable_solver"]) == 2
 
 
 def test_extended_loggers_match_reference(tmp_path):

@@ -34,16 +34,20 @@ def _events(path, spec, low):
 
 
 @pytest.mark.parametrize("mode", ["batched", "plain"])
-@pytest.mark.parametrize("name", ["single_comp_hh", "izh_net", "multicomp_poisson", "input_kinds"])
+@pytest.mark.parametrize("name", ["single_comp_hh", "izh_net", "multicomp_poisson", "input_kinds", "input_kinds_fwd"])
 def test_command_line_matches_reference_files(name, mode, tmp_path):
-    lems = neuroml_io.write_lems(spec_of(name), str(tmp_path))
+    spec0 = spec_of(name)
+    lems = neuroml_io.write_lems(spec0, str(tmp_path))
+    # the cable solver is a command-line setting, as in the reference
     args = [sys.executable, "-m", "eden_gb300", "nml", os.path.basename(lems), "gcc"] + \
-        (["plain"] if mode == "plain" else [])
+        (["plain"] if mode == "plain" else []) + \
+        ([] if spec0.cable_solver == "auto" else ["cable_solver", spec0.cable_solver])
     p = subprocess.run(args, cwd=str(tmp_path), capture_output=True, text=True, timeout=600,
                        env=dict(os.environ, PYTHONPATH=ROOT))
     assert p.returncode == 0, p.stdout + p.stderr
     assert "Config:" in p.stdout and "Setup:" in p.stdout and "Run:" in p.stdout
     spec = neuroml_io.read_lems(lems)
+    spec.cable_solver = spec0.cable_solver
     low = lowering.lower(spec)
     z = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
     traj = open(os.path.join(str(tmp_path), spec.output_files[0]["path"])).read().splitlines()

@@ -147,6 +147,10 @@ def test_errors():
         CableGradient(low, per_cell_density_map(low, [0], ra=False))
     assert e.value.code == -1 and "fixed in advance" in str(e.value)
     _, low, pm, rec = _case(n_inst=2, n_dend=5, length_ms=2.0)
+    import dataclasses
+    with pytest.raises(engine.EdenGpuError) as e:   # the adjoint follows the backward-Euler solve
+        CableGradient(dataclasses.replace(low, cable_solver=lowering.CABLE_FWD_EULER), pm, rec_comp=rec)
+    assert "backward-Euler" in str(e.value)
     g = CableGradient(low, pm, rec_comp=rec)
     try:
         with pytest.raises(engine.EdenGpuError) as e:
