@@ -121,7 +121,8 @@ inline std::string channel_routines(const EdenGpuChannelType *types, const std::
 // compiles only their code (the EDEN_KIND_* switches of eden_kernels.cuh).
 struct Kinds {
     bool pulse = false, sine = false, ramp = false, pois = false, timed = false, syn = false, expone = false,
-         exptwo = false, forest = false, izh = false, gateforms = false, clamp = false, gap = false, alpha = false;
+         exptwo = false, forest = false, izh = false, gateforms = false, clamp = false, gap = false, alpha = false,
+         current = false;
 };
 
 inline std::string kind_defines(const Kinds &k) {
@@ -141,6 +142,7 @@ inline std::string kind_defines(const Kinds &k) {
     def("EDEN_KIND_IZH", k.izh);
     def("EDEN_KIND_GAP", k.gap);
     def("EDEN_KIND_ALPHA", k.alpha);
+    def("EDEN_KIND_CURRENT", k.current);
     return s;
 }
 

@@ -205,6 +205,10 @@ int upload_c(EdenGpuCtx *ctx, const T **dst, const std::vector<T> &v) {
 
 bool finite_pos(float x) { return std::isfinite(x) && x > 0.0f; }
 
+// synapse kinds whose state is a current (blocks flagged BK_CURRENT)
+bool current_kind(int kind) { return kind == EDEN_SYN_ALPHA_CURRENT || kind == EDEN_SYN_EXPONE_CURRENT; }
+
+
 int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
     if (m->abi_version != EDEN_GPU_ABI_VERSION)
         return ctx->fail(EDEN_GPU_E_INVALID, "ABI version %d, library is %d", m->abi_version, EDEN_GPU_ABI_VERSION);
@@ -300,7 +304,7 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
     }
     for (int k = 0; k < m->n_syn_types; k++) {
         const EdenGpuSynapseType &t = m->syn_types[k];
-        if (t.kind < EDEN_SYN_EXPONE || t.kind > EDEN_SYN_ALPHA_CURRENT)
+        if (t.kind < EDEN_SYN_EXPONE || t.kind > EDEN_SYN_EXPONE_CURRENT)
             return ctx->fail(EDEN_GPU_E_INVALID, "synapse type kind");
         if (!finite_pos(t.tau_decay) || (t.kind == EDEN_SYN_EXPTWO && !finite_pos(t.tau_rise)))
             return ctx->fail(EDEN_GPU_E_INVALID, "synapse type %d: time constants", k);
@@ -494,6 +498,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     if (m->cable_solver == EDEN_CABLE_BWD_EULER) {
         auto syn_sign = [&](int type, float w) {
             const EdenGpuSynapseType &st = m->syn_types[type];
+            if (current_kind(st.kind)) return 1.0f;  // a current: no conductance on the diagonal
             float sg = st.gbase * w;
             if (st.kind == EDEN_SYN_EXPTWO) sg *= st.waveform_factor * st.weight_prop;
             return sg;
@@ -1026,7 +1031,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = poff[t]; k < poff[t + 1];) {
             int64_t k1 = k;
             while (k1 < poff[t + 1] && po_type[k1] == po_type[k]) k1++;
-            bk_kind.push_back(BK_POIS | (m->syn_types[po_type[k]].kind == EDEN_SYN_ALPHA_CURRENT ? BK_CURRENT : 0));
+            bk_kind.push_back(BK_POIS | (current_kind(m->syn_types[po_type[k]].kind) ? BK_CURRENT : 0));
             bk_erev.push_back(m->syn_types[po_type[k]].erev); bk_type.push_back(po_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
@@ -1034,7 +1039,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = toff[t]; k < toff[t + 1];) {
             int64_t k1 = k;
             while (k1 < toff[t + 1] && tm_type[k1] == tm_type[k]) k1++;
-            bk_kind.push_back(BK_TIMED | (m->syn_types[tm_type[k]].kind == EDEN_SYN_ALPHA_CURRENT ? BK_CURRENT : 0));
+            bk_kind.push_back(BK_TIMED | (current_kind(m->syn_types[tm_type[k]].kind) ? BK_CURRENT : 0));
             bk_erev.push_back(m->syn_types[tm_type[k]].erev); bk_type.push_back(tm_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
@@ -1042,7 +1047,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = soff[t]; k < soff[t + 1];) {
             int64_t k1 = k;
             while (k1 < soff[t + 1] && sy_type[k1] == sy_type[k]) k1++;
-            bk_kind.push_back(BK_SYN | (m->syn_types[sy_type[k]].kind == EDEN_SYN_ALPHA_CURRENT ? BK_CURRENT : 0));
+            bk_kind.push_back(BK_SYN | (current_kind(m->syn_types[sy_type[k]].kind) ? BK_CURRENT : 0));
             bk_erev.push_back(m->syn_types[sy_type[k]].erev); bk_type.push_back(sy_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
@@ -1452,7 +1457,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         st[k].f_decay = 1.0f - dt / s.tau_decay;
         st[k].f_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f - dt / s.tau_rise : 1.0f;
         // an alpha kind's coupling e dt / tau: g' = f g + c A per step
-        st[k].c_alpha = s.kind >= EDEN_SYN_ALPHA ? (float)(2.7182818284590451 * (double)dt / (double)s.tau_decay) : 0.0f;
+        st[k].c_alpha = (s.kind == EDEN_SYN_ALPHA || s.kind == EDEN_SYN_ALPHA_CURRENT)
+                            ? (float)(2.7182818284590451 * (double)dt / (double)s.tau_decay) : 0.0f;
     }
     {
         const ChanTypeDev *pc = nullptr;
@@ -1520,9 +1526,11 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             kinds.syn |= kb == BK_SYN;
             if (kb != BK_PULSE && kb != BK_CLAMPV) {
                 const int sk = m->syn_types[bk_type[b]].kind;
-                kinds.expone |= sk == EDEN_SYN_EXPONE || sk >= EDEN_SYN_ALPHA;  // alpha items step like expOne's
+                // alpha and current-based expOne items step like expOne's
+                kinds.expone |= sk != EDEN_SYN_EXPTWO;
                 kinds.exptwo |= sk == EDEN_SYN_EXPTWO;
-                kinds.alpha |= sk >= EDEN_SYN_ALPHA;
+                kinds.alpha |= sk == EDEN_SYN_ALPHA || sk == EDEN_SYN_ALPHA_CURRENT;
+                kinds.current |= current_kind(sk);
             }
         }
         kinds.forest = d.n_forest > 0;

@@ -571,6 +571,7 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
 #define EDEN_KIND_IZH 1
 #define EDEN_KIND_GAP 1
 #define EDEN_KIND_ALPHA 1
+#define EDEN_KIND_CURRENT 1
 #endif
 
 // A timedSynapticInput item over the window: its synapse fires in each
@@ -790,7 +791,7 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     const unsigned rows = __ballot_sync(0xffffffffu, used);
     __syncwarp();
     float gj = 0.0f;
-    if (EDEN_KIND_ALPHA && st.kind >= EDEN_SYN_ALPHA) {
+    if (EDEN_KIND_ALPHA && (st.kind == EDEN_SYN_ALPHA || st.kind == EDEN_SYN_ALPHA_CURRENT)) {
         alpha_chunk_window(m, c, type, st, w, rows, A, B, tileA);
         return;
     }
@@ -856,7 +857,7 @@ __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1,
         float g = 0.0f;
         for (int c = BC0[bk]; c < BC0[bk + 1]; c++) g += Gpk[c + chk0];
         const int kind = BK_K[bk] & BK_KIND_MASK;
-        const bool current = EDEN_KIND_ALPHA && (BK_K[bk] & BK_CURRENT);
+        const bool current = EDEN_KIND_CURRENT && (BK_K[bk] & BK_CURRENT);
         if (kind == BK_PULSE) {
             Iin += g;
         } else if (EDEN_KIND_CLAMP && kind == BK_CLAMPV) {

@@ -35,7 +35,7 @@ import copy
 
 import numpy as np
 
-from .network import (SYN_ALPHA, SYN_ALPHA_CURRENT, SYN_EXPTWO, WAVE_SINE, AdExCell, IafCell, Izhikevich2007Cell,
+from .network import (SYN_ALPHA, SYN_ALPHA_CURRENT, SYN_EXPTHREE, SYN_EXPTWO, WAVE_SINE, AdExCell, IafCell, Izhikevich2007Cell,
                       IzhikevichCell)
 
 # LEMS parameter -> (dataclass field, dimension of the unit table, factor to the field's unit)
@@ -101,6 +101,15 @@ class SetSynapse:
 
 def _synapse_table(st):
     """Settable parameters of a synapse type: NeuroML name -> (field, dimension, factor)."""
+    if st.form:
+        t = {"tau_syn": ("tau_decay", None, 1.0)}
+        if st.form.endswith("CondSynapse"):
+            t["e_rev"] = ("erev", None, 1.0)
+        return t
+    if st.kind == SYN_EXPTHREE:
+        return {"gbase1": ("gbase", "conductance", 1.0), "gbase2": ("gbase2", "conductance", 1.0),
+                "erev": ("erev", "voltage", 1.0), "tauRise": ("tau_rise", "time", 1.0),
+                "tauDecay1": ("tau_decay", "time", 1.0), "tauDecay2": ("tau_decay2", "time", 1.0)}
     if st.kind == SYN_ALPHA_CURRENT:
         return {"tau": ("tau_decay", "time", 1.0), "ibase": ("gbase", "current", 1.0)}
     t = {"gbase": ("gbase", "conductance", 1.0), "erev": ("erev", "voltage", 1.0)}
@@ -379,7 +388,7 @@ def write(spec, path: str) -> None:
                 syn = spec.synapse(spec.projections[members[0][1][0]].synapse)
                 prop, (field, dim, factor) = next((k, v) for k, v in _synapse_table(syn).items() if v[0] == st.prop)
                 ids = "all" if st.ids is None else ",".join(str(x) for x in st.ids)
-                f.write(f"set synapse {st.proj} {ids} post {prop} multi {unit_of[dim]}\n")
+                f.write(f"set synapse {st.proj} {ids} post {prop} multi" + (f" {unit_of[dim]}" if dim else "") + "\n")
                 f.write("values " + " ".join(_f(v / factor) for v in st.values) + "\n")
                 continue
             ct = spec.cell_type({p.name: p for p in spec.populations}[st.pop].cell_type)

@@ -32,7 +32,7 @@ from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, FitzHugh
                       NetworkSpec,
                       PhysicalCell, SpikeArrayCell, SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       WAVE_RAMP, WAVE_SINE,
-                      SYN_EXPTWO, SYN_ALPHA_CURRENT)
+                      SYN_EXPTWO, SYN_ALPHA_CURRENT, SYN_EXPONE_CURRENT, SYN_EXPTHREE, SynapseType)
 
 F32 = np.float32
 MAX_GATES = 4
@@ -494,6 +494,50 @@ def joined(parts, dtype) -> np.ndarray:
     return np.concatenate(parts).astype(dtype) if parts else np.zeros(0, dtype)
 
 
+def _split_exp_three(spec):
+    """A copy of `spec` in which each expThreeSynapse is two expTwo
+    components in its place, `<name>:1` (gbase1, tauRise, tauDecay1) and
+    `<name>:2` (gbase2, tauRise, tauDecay2), and each of its connections and
+    timed inputs one of each.  Its conductance gbase1 (B - A) + gbase2 (C - A)
+    with A jumping by (gbase1 wf1 + gbase2 wf2) / (gbase1 + gbase2)
+    (LEMS_CoreComponents.inc.xml:182-224) is, A's decay being linear, the
+    sum of the two expTwo conductances gbase_k (B_k - A_k) whose A_k jump by
+    wf_k: the same waveform factors, the shared rise time and erev.  A
+    Poisson input draws one spike train, so it cannot be split; it is
+    refused on an expThreeSynapse."""
+    import copy
+    import dataclasses
+    three = {s.name: s for s in spec.synapses if s.kind == SYN_EXPTHREE}
+    if not three:
+        return spec
+    for po in spec.poissons:
+        if po.synapse in three:
+            raise ValueError(f"Poisson input on expThreeSynapse {po.synapse}: not supported")
+    out = copy.copy(spec)
+    out.synapses = []
+    for s in spec.synapses:
+        if s.kind != SYN_EXPTHREE:
+            out.synapses.append(s)
+            continue
+        for k, (g, td) in enumerate(((s.gbase, s.tau_decay), (s.gbase2, s.tau_decay2)), 1):
+            out.synapses.append(SynapseType(f"{s.name}:{k}", SYN_EXPTWO, g, s.erev, td, s.tau_rise))
+    out.projections = []
+    for pr in spec.projections:
+        if pr.synapse not in three:
+            out.projections.append(pr)
+            continue
+        for k in (1, 2):
+            out.projections.append(dataclasses.replace(pr, name=f"{pr.name}:{k}", synapse=f"{pr.synapse}:{k}"))
+    out.timed = []
+    for ti in spec.timed:
+        if ti.synapse not in three:
+            out.timed.append(ti)
+            continue
+        for k in (1, 2):
+            out.timed.append(dataclasses.replace(ti, synapse=f"{ti.synapse}:{k}"))
+    return out
+
+
 CABLE_BWD_EULER = 0
 CABLE_FWD_EULER = 1
 
@@ -511,6 +555,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     if spec.custom_setup:
         from .custom_setup import apply_inputs, apply_synapses
         spec = apply_synapses(apply_inputs(spec))
+    spec = _split_exp_three(spec)
     dt = _to_f32(spec.dt * 1000.0)
     gid_off = spec.pop_offsets()
     n_cells = spec.n_cells
@@ -662,8 +707,9 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         syn_index[s.name] = k
         st = syn_types[k]
         st["kind"] = s.kind
-        # nS -> uS; an alphaCurrentSynapse's ibase stays in nA
-        st["gbase"] = _to_f32(s.gbase) if s.kind == SYN_ALPHA_CURRENT else _to_f32(s.gbase * 1e-3)
+        # nS -> uS; the current-based kinds' jumps stay in nA
+        st["gbase"] = (_to_f32(s.gbase) if s.kind in (SYN_ALPHA_CURRENT, SYN_EXPONE_CURRENT)
+                       else _to_f32(s.gbase * 1e-3))
         st["erev"] = _to_f32(s.erev)
         st["tau_decay"] = _to_f32(s.tau_decay * 1000.0)
         st["tau_rise"] = _to_f32(s.tau_rise * 1000.0) if s.kind == SYN_EXPTWO else 0.0

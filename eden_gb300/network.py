@@ -256,19 +256,29 @@ SYN_EXPONE = 0
 SYN_EXPTWO = 1
 SYN_ALPHA = 2           # alphaSynapse: conductance, rise and decay both tau
 SYN_ALPHA_CURRENT = 3   # alphaCurrentSynapse: current ibase, rise and decay both tau
+SYN_EXPONE_CURRENT = 4  # expCurrSynapse (PyNN): current-based, instantaneous rise, single decay
+SYN_EXPTHREE = 5        # expThreeSynapse: two expTwo components sharing a rise time
 
 
 @dataclass
 class SynapseType:
     """A core synapse: expOneSynapse, expTwoSynapse, alphaSynapse (tau_decay
-    holds its tau) or alphaCurrentSynapse (tau_decay holds its tau, gbase
-    its ibase in nA, erev unused)."""
+    holds its tau), alphaCurrentSynapse (tau_decay holds its tau, gbase
+    its ibase in nA, erev unused), expThreeSynapse (gbase / tau_decay the
+    first component's gbase1 / tauDecay1, gbase2 / tau_decay2 the second's),
+    or a PyNN synapse (`form`: expCondSynapse and alphaCondSynapse as
+    SYN_EXPONE and SYN_ALPHA with gbase 1 uS, erev e_rev; expCurrSynapse as
+    SYN_EXPONE_CURRENT and alphaCurrSynapse as SYN_ALPHA_CURRENT with
+    1 nA; tau_decay their tau_syn)."""
     name: str
     kind: int
-    gbase: float          # nS (alphaCurrentSynapse: ibase, nA)
+    gbase: float          # nS (alphaCurrentSynapse, expCurrSynapse: nA)
     erev: float           # mV
     tau_decay: float      # ms
-    tau_rise: float = 0.0  # ms (expTwo only)
+    tau_rise: float = 0.0  # ms (expTwo and expThree)
+    gbase2: float = 0.0    # nS (expThree)
+    tau_decay2: float = 0.0  # ms (expThree)
+    form: str = ""         # the NeuroML element a PyNN synapse was read from
 
 
 @dataclass

@@ -26,7 +26,8 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       EventSetReaderCell,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
                       ClampInputs, FitzHughNagumoCell, IzhikevichCell, TimedInputs, WaveInputs,
-                      ElectricalProjection, GapJunctionType, SYN_ALPHA, SYN_ALPHA_CURRENT)
+                      ElectricalProjection, GapJunctionType, SYN_ALPHA, SYN_ALPHA_CURRENT,
+                      SYN_EXPONE_CURRENT, SYN_EXPTHREE)
 
 
 def _f(x: float) -> str:
@@ -77,7 +78,18 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w(f' </{tag}>\n')
         w('</ionChannelHH>\n')
     for s in spec.synapses:
-        if s.kind == SYN_EXPONE:
+        if s.form:
+            cond = _PYNN_SYNAPSES[s.form][1]
+            w(f'<{s.form} id="{s.name}" tau_syn="{_f(s.tau_decay)}"' + (f' e_rev="{_f(s.erev)}"' if cond else '')
+              + '/>\n')
+        elif s.kind == SYN_EXPTHREE:
+            w(f'<expThreeSynapse id="{s.name}" gbase1="{_f(s.gbase)}nS" gbase2="{_f(s.gbase2)}nS" '
+              f'erev="{_f(s.erev)}mV" tauRise="{_f(s.tau_rise)}ms" tauDecay1="{_f(s.tau_decay)}ms" '
+              f'tauDecay2="{_f(s.tau_decay2)}ms"/>\n')
+        elif s.kind == SYN_EXPONE_CURRENT:
+            raise ValueError(f"synapse {s.name}: a current-based single-exponential synapse is written as "
+                             f"expCurrSynapse (form), whose jump is 1 nA")
+        elif s.kind == SYN_EXPONE:
             w(f'<expOneSynapse id="{s.name}" gbase="{_f(s.gbase)}nS" erev="{_f(s.erev)}mV" '
               f'tauDecay="{_f(s.tau_decay)}ms"/>\n')
         elif s.kind == SYN_ALPHA:
@@ -436,6 +448,11 @@ _UNITS = {
 _QTY = re.compile(r"^\s*([-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?)\s*([A-Za-z_0-9]*)\s*$")
 
 
+# PyNN synapse element -> (kind, conductance-based)
+_PYNN_SYNAPSES = {"expCondSynapse": (SYN_EXPONE, True), "alphaCondSynapse": (SYN_ALPHA, True),
+                  "expCurrSynapse": (SYN_EXPONE_CURRENT, False), "alphaCurrSynapse": (SYN_ALPHA_CURRENT, False)}
+
+
 def _qty(el, attr, dim, default=None):
     text = el.get(attr)
     if text is None:
@@ -712,6 +729,19 @@ def read_lems(path: str) -> NetworkSpec:
         elif t == "alphaCurrentSynapse":
             synapses[e.get("id")] = SynapseType(e.get("id"), SYN_ALPHA_CURRENT, _qty(e, "ibase", "current"), 0.0,
                                                 _qty(e, "tau", "time"))
+        elif t == "expThreeSynapse":
+            synapses[e.get("id")] = SynapseType(e.get("id"), SYN_EXPTHREE, _qty(e, "gbase1", "conductance"),
+                                                _qty(e, "erev", "voltage"), _qty(e, "tauDecay1", "time"),
+                                                _qty(e, "tauRise", "time"), _qty(e, "gbase2", "conductance"),
+                                                _qty(e, "tauDecay2", "time"))
+        elif t in _PYNN_SYNAPSES:
+            # PyNN synapses (LEMS_CoreComponents.inc.xml:1834-1940): tau_syn in
+            # ms and e_rev in mV, without units; the state jumps by the
+            # weight property (1) and is a conductance in uS or a current in nA
+            kind, cond = _PYNN_SYNAPSES[t]
+            synapses[e.get("id")] = SynapseType(e.get("id"), kind, 1000.0 if cond else 1.0,
+                                                _qty(e, "e_rev", None) if cond else 0.0, _qty(e, "tau_syn", None),
+                                                form=t)
         elif t == "gapJunction":
             gap_def[e.get("id")] = GapJunctionType(e.get("id"), _qty(e, "conductance", "conductance"))
         elif t in ("pulseGenerator", "pulseGeneratorDL"):

@@ -914,6 +914,70 @@ def alpha_synapses(n_hh: int = 6, n_izh: int = 6, n_branch: int = 3, length_ms: 
     return spec
 
 
+def pynn_synapses(n_hh: int = 6, n_branch: int = 3, n_izh: int = 4, length_ms: float = 80.0, dt_ms: float = 0.025,
+                  seed: int = 4321) -> NetworkSpec:
+    """The PyNN synapses (expCondSynapse, alphaCondSynapse, expCurrSynapse,
+    alphaCurrSynapse) and expThreeSynapse on single-compartment HH cells,
+    the dendrites of branching cells and izhikevich2007 cells: recurrent
+    connections of each kind, Poisson inputs of three PyNN kinds and timed
+    inputs of four kinds (some in the same steps as other events)."""
+    from .network import SYN_ALPHA, SYN_ALPHA_CURRENT, SYN_EXPONE_CURRENT, SYN_EXPTHREE
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("pynn_synapses", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.synapses += [
+        SynapseType("syn_expcond", SYN_EXPONE, 1000.0, 0.0, 2.0, form="expCondSynapse"),
+        SynapseType("syn_alphacond", SYN_ALPHA, 1000.0, -10.0, 1.5, form="alphaCondSynapse"),
+        SynapseType("syn_expcurr", SYN_EXPONE_CURRENT, 1.0, 0.0, 3.0, form="expCurrSynapse"),
+        SynapseType("syn_alphacurr", SYN_ALPHA_CURRENT, 1.0, 0.0, 2.5, form="alphaCurrSynapse"),
+        SynapseType("syn_e3", SYN_EXPTHREE, 1.5, 0.0, 1.5, tau_rise=0.5, gbase2=0.8, tau_decay2=5.0),
+    ]
+    # PyNN weights are the state's jump: uS for the conductance kinds, nA
+    # for the current kinds
+    wscale = {"syn_expcond": 0.002, "syn_alphacond": 0.002, "syn_expcurr": 0.1, "syn_alphacurr": 0.05, "syn_e3": 1.0}
+    spec.cells.append(PhysicalCell("hhcell", np.array([-1]), np.array([0.0]), np.array([17.8]),
+                                   _hh_densities(1, np.ones(1, bool)), cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0))
+    parent = np.array([-1, 0, 1, 1])
+    soma = parent < 0
+    spec.cells.append(PhysicalCell("branch", parent, np.array([20.0, 60.0, 50.0, 40.0]),
+                                   np.array([20.0, 2.0, 1.5, 1.2]), _hh_densities(4, soma), cm=1.0, ra=150.0,
+                                   v0=-65.0, spike_thresh=-20.0, seg_groups={"soma_group": soma, "dend_group": ~soma}))
+    spec.cells.append(Izhikevich2007Cell("izRS", a=0.03, d=100.0, c=-50.0))
+    spec.populations.append(Population("hh", "hhcell", n_hh))
+    spec.populations.append(Population("branch", "branch", n_branch))
+    spec.populations.append(Population("iz", "izRS", n_izh))
+    hh = np.arange(n_hh)
+    br = n_hh + np.arange(n_branch)
+    iz = n_hh + n_branch + np.arange(n_izh)
+    n = n_hh + n_branch + n_izh
+    drv = np.arange(0, n, 3)
+    spec.pulses.append(PulseInputs("*", drv, np.zeros(len(drv), int), np.full(len(drv), 2.0),
+                                   np.full(len(drv), length_ms), np.round(0.12 * rng.uniform(0.8, 1.6, len(drv)), 4)))
+    for syn in ("syn_expcond", "syn_alphacond", "syn_expcurr", "syn_alphacurr", "syn_e3"):
+        post = np.repeat(np.arange(n), 2)
+        pre = rng.integers(0, n, size=post.size)
+        pre = np.where(pre == post, (pre + 1) % n, pre)
+        seg = np.where((post >= n_hh) & (post < n_hh + n_branch), rng.integers(0, 4, size=post.size), 0)
+        spec.projections.append(_flat_projection(spec, f"proj_{syn}", pre, post, syn,
+                                                 np.round(wscale[syn] * rng.uniform(0.5, 1.5, post.size), 5),
+                                                 _round_us(rng.uniform(0.5, 3.0, size=post.size)), post_seg=seg))
+    # (a Poisson input's weight is 1: on an expCondSynapse that is a 1 uS
+    # jump, left out)
+    for syn, rate in (("syn_alphacond", 40.0), ("syn_expcurr", 80.0), ("syn_alphacurr", 50.0)):
+        cells = np.concatenate([hh, br, iz])
+        segs = np.concatenate([np.zeros(n_hh, int), np.full(n_branch, 3), np.zeros(n_izh, int)])
+        spec.poissons.append(PoissonInputs("*", syn, rate, cells, segs))
+    for syn in ("syn_expcond", "syn_expcurr", "syn_alphacurr", "syn_e3"):
+        cells = np.concatenate([hh[::2], iz[::2]])
+        times = [np.round(np.sort(rng.uniform(0.0, length_ms, rng.integers(3, 9))), 4) for _ in cells]
+        times[0] = np.concatenate([times[0], [10.0, 10.0001, 20.025]])
+        spec.timed.append(TimedInputs(syn, cells, np.zeros(len(cells), np.int64), times,
+                                      np.round(wscale[syn] * rng.uniform(0.5, 1.5, len(cells)), 5)))
+    cols = [(g, 0) for g in range(n)] + [(int(b), 3) for b in br]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), seg) for g, seg in cols]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, g), 0) for g in range(n)]
+    return spec
+
+
 def gap_junctions(n_hh: int = 10, n_branch: int = 4, n_izh: int = 2, length_ms: float = 80.0,
                   dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
     """Gap junctions (two gapJunction types, 1 and 4 nS, weights 0.5-1.5)
@@ -990,6 +1054,7 @@ CONFIGS = {
     "voltage_clamps": voltage_clamps,
     "gap_junctions": gap_junctions,
     "alpha_synapses": alpha_synapses,
+    "pynn_synapses": pynn_synapses,
     "routing_probe": routing_probe,
     "random_sources": random_sources,
     "custom_setup": custom_setup,

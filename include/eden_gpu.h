@@ -121,7 +121,8 @@ typedef struct EdenGpuChannelType {
     float inf_rate[EDEN_MAX_GATES], inf_mid[EDEN_MAX_GATES], inf_scale[EDEN_MAX_GATES];
 } EdenGpuChannelType;
 
-enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1, EDEN_SYN_ALPHA = 2, EDEN_SYN_ALPHA_CURRENT = 3 };
+enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1, EDEN_SYN_ALPHA = 2, EDEN_SYN_ALPHA_CURRENT = 3,
+       EDEN_SYN_EXPONE_CURRENT = 4 };
 enum { EDEN_CABLE_BWD_EULER = 0, EDEN_CABLE_FWD_EULER = 1 };
 
 /* expOneSynapse (native, eden/Eden.cpp:3424-3466), expTwoSynapse,
@@ -130,7 +131,13 @@ enum { EDEN_CABLE_BWD_EULER = 0, EDEN_CABLE_FWD_EULER = 1 };
  * derived 1/(-exp(-tp/tr)+exp(-tp/td)) and `weight_prop` its LEMS `weight`
  * property (default 1).  The alpha kinds have one time constant, in
  * tau_decay; an alphaCurrentSynapse carries its ibase (nA) in gbase and
- * contributes current only (erev unused). */
+ * contributes current only (erev unused).  EDEN_SYN_EXPONE_CURRENT is
+ * PyNN's expCurrSynapse (LEMS_CoreComponents.inc.xml:1858-1877): expOne's
+ * state, jumping by gbase (nA) and decaying with tau_decay, taken as a
+ * current.  PyNN's expCondSynapse, alphaCondSynapse and alphaCurrSynapse
+ * are EDEN_SYN_EXPONE, EDEN_SYN_ALPHA and EDEN_SYN_ALPHA_CURRENT with
+ * gbase 1 (uS or nA), and an expThreeSynapse is two EDEN_SYN_EXPTWO types
+ * on the same connection. */
 typedef struct EdenGpuSynapseType {
     int32_t kind;
     float gbase, erev, tau_decay, tau_rise, waveform_factor, weight_prop;

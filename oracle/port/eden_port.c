@@ -173,6 +173,14 @@ static inline PORT_FN void syn_dyn(const EdenGpuSynapseType *st, int init, int f
         *an = init ? a : (fired ? a + st->gbase : a - dt * (a / st->tau_decay));
         *bn = b;
         return;
+    case EDEN_SYN_EXPONE_CURRENT:
+        /* expCurrSynapse: I' = -I / tau_syn, I += weight on an event, the
+         * current I (LEMS_CoreComponents.inc.xml:1858-1877) */
+        *g = R(0.0);
+        *i = a;
+        *an = init ? a : (fired ? a + st->gbase : a + dt * (-a / st->tau_decay));
+        *bn = b;
+        return;
     case EDEN_SYN_ALPHA:
     case EDEN_SYN_ALPHA_CURRENT:
         if (st->kind == EDEN_SYN_ALPHA) {

@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 from eden_gb300 import lowering, neuroml_io, workloads
+from golden.cases import spec_of
 
 
 def _same(a, b):
@@ -95,3 +96,27 @@ def test_gap_junctions_on_point_neurons_fail_loudly():
                                                 np.array([0]), np.array([1.0])))
     with pytest.raises(ValueError, match="physical cells"):
         lowering.lower(spec)
+
+
+def test_pynn_and_exp_three_synapses_round_trip(tmp_path):
+    """expCondSynapse, alphaCondSynapse, expCurrSynapse, alphaCurrSynapse and
+    expThreeSynapse are written back as themselves and lower to the same
+    tables; an expThreeSynapse lowers to two expTwo types on every one of
+    its connections and timed inputs."""
+    spec = spec_of("pynn_synapses")
+    low = lowering.lower(spec)
+    back = neuroml_io.read_lems(neuroml_io.write_lems(spec, str(tmp_path)))
+    assert [(s.kind, s.form) for s in back.synapses] == [(s.kind, s.form) for s in spec.synapses]
+    low2 = lowering.lower(back)
+    np.testing.assert_array_equal(low2.syn_types, low.syn_types)
+    np.testing.assert_array_equal(low2.syn_target, low.syn_target)
+    np.testing.assert_array_equal(low2.syn_type, low.syn_type)
+    n3 = len(next(p for p in spec.projections if p.synapse == "syn_e3").pre_cell)
+    n_conn = sum(len(p.pre_cell) for p in spec.projections)
+    assert len(low.syn_target) == n_conn + n3
+    # a Poisson input draws one train: it cannot drive an expThreeSynapse's two parts
+    import copy
+    bad = copy.deepcopy(spec)
+    bad.poissons[0].synapse = "syn_e3"
+    with pytest.raises(ValueError, match="expThreeSynapse"):
+        lowering.lower(bad)
