@@ -22,9 +22,11 @@ their DL forms) and voltage-clamp inputs of lists read from NeuroML; and
 `set synapse` on the postsynaptic component of a projection's connections
 (the parameters of its expOne, expTwo, alpha or alphaCurrent synapse,
 eden/NeuroML.cpp:7853-7960), where each distinct set of overridden values
-becomes a synapse type of its own in the lowered model.  Not built:
-properties of physical cells (segment states, channel gates); they are
-refused by name.
+becomes a synapse type of its own in the lowered model.  Properties of
+physical cells (segment voltage, gate states, calcium) are refused by
+name, as the reference refuses them when it applies the setup (its
+`set cell` application takes artificial-cell parameters only,
+eden/Eden.cpp:9501-9553).
 """
 from __future__ import annotations
 
