@@ -373,6 +373,20 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
         if (!std::isfinite(m->gap_conductance[k]) || !std::isfinite(m->gap_weight[k]))
             return ctx->fail(EDEN_GPU_E_INVALID, "gap junction %lld: non-finite conductance or weight", (long long)k);
     }
+    if (m->n_graded < 0) return ctx->fail(EDEN_GPU_E_INVALID, "n_graded must be >= 0");
+    if (m->n_graded > 0 && (!m->graded_target || !m->graded_peer || !m->graded_params || !m->graded_weight))
+        return ctx->fail(EDEN_GPU_E_INVALID, "graded synapses: null array");
+    for (int64_t k = 0; k < m->n_graded; k++) {
+        if (m->graded_target[k] < 0 || m->graded_target[k] >= m->n_comp || m->graded_peer[k] < 0 ||
+            m->graded_peer[k] >= m->n_comp)
+            return ctx->fail(EDEN_GPU_E_INVALID, "graded synapse %lld: ends must be compartments of physical cells",
+                             (long long)k);
+        const float *p = m->graded_params + (size_t)EDEN_GRADED_PARAMS * k;
+        for (int j = 0; j < EDEN_GRADED_PARAMS; j++)
+            if (!std::isfinite(p[j])) return ctx->fail(EDEN_GPU_E_INVALID, "graded synapse %lld: non-finite parameter", (long long)k);
+        if (p[1] == 0.0f || !(p[2] > 0.0f) || !std::isfinite(m->graded_weight[k]))
+            return ctx->fail(EDEN_GPU_E_INVALID, "graded synapse %lld: delta must be non-zero, k positive", (long long)k);
+    }
     return 0;
 }
 
@@ -467,6 +481,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     for (int64_t k = 0; k < m->n_wave; k++) n_in_user[m->wave_target[k]]++;
     for (int64_t k = 0; k < m->n_clamp; k++) n_in_user[m->clamp_target[k]] += 2;
     for (int64_t k = 0; k < m->n_gap; k++) n_in_user[m->gap_target[k]]++;
+    for (int64_t k = 0; k < m->n_graded; k++) n_in_user[m->graded_target[k]]++;
     std::vector<double> cost(n_cells, 0.0);
     double total = 0;
     int max_cell = 1;
@@ -779,6 +794,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = 0; k < m->n_wave; k++) has_input[u2i[m->wave_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_clamp; k++) has_input[u2i[m->clamp_target[k]]] = 1;
         for (int64_t k = 0; k < m->n_gap; k++) has_input[u2i[m->gap_target[k]]] = 1;
+        for (int64_t k = 0; k < m->n_graded; k++) has_input[u2i[m->graded_target[k]]] = 1;
         parallel_for(nt, [&](int64_t it) {
             if (t_izh[it] >= 0 || has_input[it]) return;
             if (c_chan0[it + 1] - c_chan0[it] != 1) return;
@@ -1082,7 +1098,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     }
     // gap junctions couple cells within a step: one-step windows, each
     // reading its peers' potentials from the buffer the previous one wrote
-    if (m->n_gap > 0) kmax = 1;
+    if (m->n_gap > 0 || m->n_graded > 0) kmax = 1;
     ctx->mode = opt ? opt->mode : EDEN_MODE_PLAIN;
     ctx->kernel_timing = opt && opt->kernel_timing;
     int kreq = (opt && opt->steps_per_launch > 0) ? opt->steps_per_launch : kmax;
@@ -1335,6 +1351,26 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         TRY(upload_c(ctx, &d.t_gap0, t_gap0)); TRY(upload_c(ctx, &d.gap_peer, gj_peer));
         TRY(upload_c(ctx, &d.gap_g, gj_g)); TRY(upload_c(ctx, &d.gap_w, gj_w));
     }
+    {
+        // gradedSynapse ends per internal target, in the model's order; their
+        // state starts at 0
+        const int64_t ng = m->n_graded;
+        std::vector<int32_t> t_gr0(nt + 1, 0), gr_peer(ng);
+        std::vector<float> gr_par((size_t)EDEN_GRADED_PARAMS * ng), gr_w(ng), gr_s(std::max<int64_t>(ng, 1), 0.0f);
+        for (int64_t k = 0; k < ng; k++) t_gr0[u2i[m->graded_target[k]] + 1]++;
+        for (int t = 0; t < nt; t++) t_gr0[t + 1] += t_gr0[t];
+        std::vector<int32_t> fill(t_gr0.begin(), t_gr0.end() - 1);
+        for (int64_t k = 0; k < ng; k++) {
+            const int32_t o = fill[u2i[m->graded_target[k]]]++;
+            gr_peer[o] = u2i[m->graded_peer[k]];
+            for (int j = 0; j < EDEN_GRADED_PARAMS; j++)
+                gr_par[(size_t)EDEN_GRADED_PARAMS * o + j] = m->graded_params[(size_t)EDEN_GRADED_PARAMS * k + j];
+            gr_w[o] = m->graded_weight[k];
+        }
+        TRY(upload_c(ctx, &d.t_gr0, t_gr0)); TRY(upload_c(ctx, &d.gr_peer, gr_peer));
+        TRY(upload_c(ctx, &d.gr_par, gr_par)); TRY(upload_c(ctx, &d.gr_w, gr_w));
+        TRY(upload_vec(ctx, &d.gr_s, gr_s));
+    }
     TRY(upload_c(ctx, &d.in_tgt, in_tgt));
     TRY(upload_c(ctx, &d.t_blk0, t_blk0)); TRY(upload_c(ctx, &d.bk_kind, bk_kind));
     TRY(upload_c(ctx, &d.bk_type, bk_type)); TRY(upload_c(ctx, &d.bk_erev, bk_erev));
@@ -1536,7 +1572,7 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         kinds.forest = d.n_forest > 0;
         kinds.gateforms = gate_forms;
         kinds.izh = n_izh > 0;
-        kinds.gap = m->n_gap > 0;
+        kinds.gap = m->n_gap > 0 || m->n_graded > 0;
         ctx->codegen_source = eden_codegen::program_source(eden_codegen::kind_defines(kinds) +
                                                            eden_codegen::channel_routines(m->chan_types, chan_sets));
         eden_codegen::Kernels kk;

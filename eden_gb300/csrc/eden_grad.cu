@@ -748,13 +748,13 @@ int validate(EdenGpuGrad *g, const EdenGpuModel *m, const EdenGpuGradSpec *s) {
     if (m->abi_version != EDEN_GPU_ABI_VERSION)
         return g->fail(EDEN_GPU_E_INVALID, "ABI version %d, library is %d", m->abi_version, EDEN_GPU_ABI_VERSION);
     if (!finite_pos(m->dt)) return g->fail(EDEN_GPU_E_INVALID, "dt must be positive");
-    if (m->n_izh != 0 || m->n_pois != 0 || m->n_wave != 0 || m->n_clamp != 0 || m->n_gap != 0)
+    if (m->n_izh != 0 || m->n_pois != 0 || m->n_wave != 0 || m->n_clamp != 0 || m->n_gap != 0 || m->n_graded != 0)
         return g->fail(EDEN_GPU_E_INVALID,
                        "gradients cover independent physical cells with HH channels, pulse inputs and synaptic drive "
                        "with fixed events: the model has %d point neurons, %lld Poisson, %lld waveform and %lld clamp "
-                       "inputs and %lld gap-junction ends",
+                       "inputs and %lld gap-junction and graded-synapse ends",
                        m->n_izh, (long long)m->n_pois, (long long)m->n_wave, (long long)m->n_clamp,
-                       (long long)m->n_gap);
+                       (long long)(m->n_gap + m->n_graded));
     if (m->cable_solver != EDEN_CABLE_BWD_EULER)
         return g->fail(EDEN_GPU_E_INVALID, "gradients follow the backward-Euler cable solve only");
     for (int k = 0; k < m->n_syn_types; k++) {

@@ -243,15 +243,38 @@ struct DevModel {
     // (internal target), conductance (uS) and weight
     const int32_t *t_gap0, *gap_peer;
     const float *gap_g, *gap_w;
+    // gradedSynapse ends of each target [t_gr0[t], t_gr0[t+1]): the peer,
+    // EDEN_GRADED_PARAMS parameters, weight and state s
+    const int32_t *t_gr0, *gr_peer;
+    const float *gr_par, *gr_w;
+    float *gr_s;
 };
 
 // The gap-junction current into target t at potential v, its peers read
 // from the step's starting potentials vnow: each end contributes
 // (g (V_peer - v)) w, as the reference sums a synapse's exposure times its
 // weight (eden/Eden.cpp:3407-3422, 3708-3710); no conductance term.
-__device__ __forceinline__ float gap_current(const DevModel &m, int t, float v, const float *vnow) {
+__device__ __forceinline__ float gap_current(const DevModel &m, int t, float v, const float *vnow, bool init) {
     float i = 0.0f;
     for (int k = m.t_gap0[t]; k < m.t_gap0[t + 1]; k++) i += (m.gap_g[k] * (vnow[m.gap_peer[k]] - v)) * m.gap_w[k];
+    // gradedSynapse ends (LEMS_CoreComponents.inc.xml:38-80, as the
+    // reference's LEMS code steps it: the derived values and the current
+    // from the step's starting state, s by forward Euler, the OnCondition
+    // overriding; s = 0 in the initialisation steps).  Each end's state is
+    // read and written by its own target's thread, once per step.
+    for (int k = m.t_gr0[t]; k < m.t_gr0[t + 1]; k++) {
+        const float *p = m.gr_par + (size_t)EDEN_GRADED_PARAMS * k;  // conductance, delta, k, Vth, erev
+        const float s = m.gr_s[k];
+        const float inf = 1.0f / (1.0f + expf((p[3] - vnow[m.gr_peer[k]]) / p[1]));
+        const float tau = (1.0f - inf) / p[2];
+        i += ((p[0] * s) * (p[4] - v)) * m.gr_w[k];
+        float sn = 0.0f;
+        if (!init) {
+            sn = s + m.dt * ((1.0f - inf) > 1e-4f ? (inf - s) / tau : 0.0f);
+            if ((1.0f - inf) < 1e-4f) sn = inf;
+        }
+        m.gr_s[k] = sn;
+    }
     return i;
 }
 

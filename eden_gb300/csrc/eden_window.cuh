@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs 
             float v = vin[i], Iin, Gin, Isyn, Gsyn;
             block_currents(m.Gp, m.t_blk0[i], m.t_blk0[i + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
                            Gsyn);
-            if (EDEN_KIND_GAP) Isyn += gap_current(m, i, v, vin);
+            if (EDEN_KIND_GAP) Isyn += gap_current(m, i, v, vin, init);
             const float Iax = (m.fwd_euler && !init && m.t_izh[i] < 0) ? axial_current(m, i, v, vin) : 0.0f;
             target_step(m, i, init, w.step0, tnow, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar, Iax);
         }
@@ -282,7 +282,7 @@ __device__ __forceinline__ void forest_window(const DevModel &m, const WindowArg
             block_currents(Gk, NB0[j], NB1[j], BKK, BKE, BKC, 0, v, Iin, Gin, Isyn, Gsyn);
             // (a model with gap junctions runs one-step windows: vsrc holds
             // every target's potential at this step's start)
-            if (EDEN_KIND_GAP) Isyn += gap_current(m, t0 + ti, v, vsrc);
+            if (EDEN_KIND_GAP) Isyn += gap_current(m, t0 + ti, v, vsrc, init);
             const float A = NA[j];
             float Ich = 0.f, Gch = 0.f;
 #ifdef EDEN_RTC_CHANNELS

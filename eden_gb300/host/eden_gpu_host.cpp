@@ -131,6 +131,8 @@ void fill_model(const Reader &r, EdenGpuModel &m) {
     I64(n_gap); PTR(gap_target, int32_t); PTR(gap_peer, int32_t); PTR(gap_conductance, float);
     PTR(gap_weight, float);
     I32(cable_solver);
+    I64(n_graded); PTR(graded_target, int32_t); PTR(graded_peer, int32_t); PTR(graded_params, float);
+    PTR(graded_weight, float);
 #undef I32
 #undef I64
 #undef PTR

@@ -154,6 +154,12 @@ class LoweredModel:
     gap_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     # cable solver of the physical cells: CABLE_BWD_EULER or CABLE_FWD_EULER
     cable_solver: int = 0
+    # gradedSynapse ends: the compartment, the peer compartment, [n, 5]
+    # (conductance uS, delta mV, k 1/us, Vth mV, erev mV), weight
+    graded_target: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    graded_peer: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    graded_params: np.ndarray = field(default_factory=lambda: np.zeros((0, 5), np.float32))
+    graded_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
 
     @property
     def n_comp(self) -> int:
@@ -720,22 +726,44 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     # ---- gap junctions: each electrical connection puts an instance on both
     # ends, each taking weight * conductance * (V_peer - V_own) as synaptic
     # current (eden/Eden.cpp:9233-9251, 3407-3422); physical compartments only
+    # A continuous connection puts its postComponent on the post end, then
+    # its preComponent on the pre end (eden/Eden.cpp:9254-9270): a
+    # linearGradedSynapse end is a gap-junction end, a gradedSynapse end
+    # has its own state (graded_*), a silentSynapse end is nothing.
     gap_of = {g.name: g for g in spec.gap_types}
     gj_t, gj_p, gj_g, gj_w = [], [], [], []
-    for ep in spec.electrical:
-        pre = np.asarray(ep.pre_cell, np.int64)
-        post = np.asarray(ep.post_cell, np.int64)
+    gr_t, gr_p, gr_par, gr_w = [], [], [], []
+
+    def put_end(comp, at, peer, w):
+        gt = gap_of[comp]
+        if gt.kind == "silentSynapse":
+            return
+        if gt.kind == "gradedSynapse":
+            gr_t.append(at); gr_p.append(peer); gr_w.append(w)
+            gr_par.append([_to_f32(gt.conductance * 1e-3), _to_f32(gt.delta), _to_f32(gt.k * 1e-3),
+                           _to_f32(gt.vth), _to_f32(gt.erev)])   # uS, mV, 1/us, mV, mV
+            return
+        gj_t.append(at); gj_p.append(peer); gj_w.append(w)
+        gj_g.append(_to_f32(gt.conductance * 1e-3))   # nS -> uS
+
+    def ends_of(name, pre_cell, pre_seg, post_cell, post_seg, weight):
+        pre = np.asarray(pre_cell, np.int64)
+        post = np.asarray(post_cell, np.int64)
         if len(pre) and (gid_is_izh[pre].any() or gid_is_izh[post].any()):
-            raise ValueError(f"{ep.name}: gap junctions join compartments of physical cells")
-        a = target_of(pre, ep.pre_seg, current=False)
-        b = target_of(post, ep.post_seg, current=False)
-        g = _to_f32(gap_of[ep.synapse].conductance * 1e-3)   # nS -> uS
-        w = np.asarray(ep.weight, np.float64).astype(F32)
-        for i in range(len(pre)):
-            gj_t += [a[i], b[i]]
-            gj_p += [b[i], a[i]]
-            gj_g += [g, g]
-            gj_w += [w[i], w[i]]
+            raise ValueError(f"{name}: electrical and continuous connections join compartments of physical cells")
+        return (target_of(pre, pre_seg, current=False), target_of(post, post_seg, current=False),
+                np.asarray(weight, np.float64).astype(F32))
+
+    for ep in spec.electrical:
+        a, b, w = ends_of(ep.name, ep.pre_cell, ep.pre_seg, ep.post_cell, ep.post_seg, ep.weight)
+        for i in range(len(a)):
+            put_end(ep.synapse, a[i], b[i], w[i])
+            put_end(ep.synapse, b[i], a[i], w[i])
+    for cp in spec.continuous:
+        a, b, w = ends_of(cp.name, cp.pre_cell, cp.pre_seg, cp.post_cell, cp.post_seg, cp.weight)
+        for i in range(len(a)):
+            put_end(cp.post_component, b[i], a[i], w[i])
+            put_end(cp.pre_component, a[i], b[i], w[i])
 
     # ---- connection synapses: grouped per target, type order, then connection order
     tgt, typ, src, wgt, dly, order_key = [], [], [], [], [], []
@@ -917,13 +945,15 @@ def lower(spec: NetworkSpec) -> LoweredModel:
         gap_target=np.asarray(gj_t, np.int32), gap_peer=np.asarray(gj_p, np.int32),
         gap_conductance=np.asarray(gj_g, F32), gap_weight=np.asarray(gj_w, F32),
         cable_solver=_cable_solver(spec),
+        graded_target=np.asarray(gr_t, np.int32), graded_peer=np.asarray(gr_p, np.int32),
+        graded_params=np.asarray(gr_par, F32).reshape(-1, 5), graded_weight=np.asarray(gr_w, F32),
     )
 
 
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 10
+ABI_VERSION = 11
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -957,6 +987,8 @@ class CModel(ctypes.Structure):
         ("n_clamp", ctypes.c_int64), ("clamp_target", _i32p), ("clamp_params", _f32p), ("clamp_weight", _f32p),
         ("n_gap", ctypes.c_int64), ("gap_target", _i32p), ("gap_peer", _i32p), ("gap_conductance", _f32p),
         ("gap_weight", _f32p), ("cable_solver", ctypes.c_int32),
+        ("n_graded", ctypes.c_int64), ("graded_target", _i32p), ("graded_peer", _i32p), ("graded_params", _f32p),
+        ("graded_weight", _f32p),
     ]
 
 
@@ -1052,4 +1084,9 @@ def to_cmodel(m: LoweredModel):
     cm.gap_conductance = p(m.gap_conductance, F32, _f32p)
     cm.gap_weight = p(m.gap_weight, F32, _f32p)
     cm.cable_solver = int(m.cable_solver)
+    cm.n_graded = len(m.graded_target)
+    cm.graded_target = p(m.graded_target, np.int32, _i32p)
+    cm.graded_peer = p(m.graded_peer, np.int32, _i32p)
+    cm.graded_params = p(m.graded_params, F32, _f32p)
+    cm.graded_weight = p(m.graded_weight, F32, _f32p)
     return cm, keep

@@ -307,9 +307,17 @@ class Projection:
 
 @dataclass
 class GapJunctionType:
-    """gapJunction: a linear electrical synapse of `conductance` (nS)."""
+    """A synaptic component for the ends of electrical and continuous
+    connections: gapJunction and linearGradedSynapse (a current
+    conductance * (vpeer - v), conductance in nS), silentSynapse (nothing),
+    or gradedSynapse (conductance nS, delta mV, k per ms, vth mV, erev mV)."""
     name: str
     conductance: float
+    kind: str = "gapJunction"
+    delta: float = 0.0
+    k: float = 0.0
+    vth: float = 0.0
+    erev: float = 0.0
 
 
 @dataclass
@@ -321,6 +329,21 @@ class ElectricalProjection:
     conductance term (eden/Eden.cpp:3407-3422, 9233-9251)."""
     name: str
     synapse: str
+    pre_cell: np.ndarray
+    pre_seg: np.ndarray
+    post_cell: np.ndarray
+    post_seg: np.ndarray
+    weight: np.ndarray
+
+
+@dataclass
+class ContinuousProjection:
+    """continuousConnection(Instance)(W) list: each connection puts
+    `pre_component` on the pre end and `post_component` on the post end
+    (GapJunctionType names), each end reading the other end's potential."""
+    name: str
+    pre_component: str
+    post_component: str
     pre_cell: np.ndarray
     pre_seg: np.ndarray
     post_cell: np.ndarray
@@ -438,6 +461,7 @@ class NetworkSpec:
     projections: List[Projection] = field(default_factory=list)
     gap_types: List[GapJunctionType] = field(default_factory=list)
     electrical: List[ElectricalProjection] = field(default_factory=list)
+    continuous: List[ContinuousProjection] = field(default_factory=list)
     pulses: List[PulseInputs] = field(default_factory=list)
     poissons: List[PoissonInputs] = field(default_factory=list)
     timed: List[TimedInputs] = field(default_factory=list)

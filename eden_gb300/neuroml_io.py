@@ -27,7 +27,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
                       ClampInputs, FitzHughNagumoCell, IzhikevichCell, TimedInputs, WaveInputs,
                       ElectricalProjection, GapJunctionType, SYN_ALPHA, SYN_ALPHA_CURRENT,
-                      SYN_EXPONE_CURRENT, SYN_EXPTHREE)
+                      SYN_EXPONE_CURRENT, SYN_EXPTHREE, ContinuousProjection)
 
 
 def _f(x: float) -> str:
@@ -101,7 +101,13 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             w(f'<expTwoSynapse id="{s.name}" gbase="{_f(s.gbase)}nS" erev="{_f(s.erev)}mV" '
               f'tauRise="{_f(s.tau_rise)}ms" tauDecay="{_f(s.tau_decay)}ms"/>\n')
     for gt in spec.gap_types:
-        w(f'<gapJunction id="{gt.name}" conductance="{_f(gt.conductance)}nS"/>\n')
+        if gt.kind == "silentSynapse":
+            w(f'<silentSynapse id="{gt.name}"/>\n')
+        elif gt.kind == "gradedSynapse":
+            w(f'<gradedSynapse id="{gt.name}" conductance="{_f(gt.conductance)}nS" delta="{_f(gt.delta)}mV" '
+              f'k="{_f(gt.k)}per_ms" Vth="{_f(gt.vth)}mV" erev="{_f(gt.erev)}mV"/>\n')
+        else:
+            w(f'<{gt.kind} id="{gt.name}" conductance="{_f(gt.conductance)}nS"/>\n')
     used_types = {p.cell_type for p in spec.populations}
     for c in spec.cells:
         if c.name not in used_types:
@@ -276,6 +282,24 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
                   f'postCell="../{pb}/{local_of[ep.post_cell[i]]}/{spec.population(pb).cell_type}" '
                   f'postSegment="{ep.post_seg[i]}" synapse="{ep.synapse}" weight="{_f(ep.weight[i])}"/>\n')
             w(' </electricalProjection>\n')
+    for cp in spec.continuous:
+        # one continuousProjection per (pre population, post population) run
+        groups = []
+        for i in range(len(cp.pre_cell)):
+            key = (pop_of[cp.pre_cell[i]], pop_of[cp.post_cell[i]])
+            if not groups or groups[-1][0] != key:
+                groups.append((key, []))
+            groups[-1][1].append(i)
+        for gi, ((pa, pb), idx) in enumerate(groups):
+            w(f' <continuousProjection id="{cp.name}_{gi}" presynapticPopulation="{pa}" '
+              f'postsynapticPopulation="{pb}">\n')
+            for n, i in enumerate(idx):
+                w(f'  <continuousConnectionInstanceW id="{n}" preCell="../{pa}/{local_of[cp.pre_cell[i]]}/'
+                  f'{spec.population(pa).cell_type}" preSegment="{cp.pre_seg[i]}" '
+                  f'postCell="../{pb}/{local_of[cp.post_cell[i]]}/{spec.population(pb).cell_type}" '
+                  f'postSegment="{cp.post_seg[i]}" preComponent="{cp.pre_component}" '
+                  f'postComponent="{cp.post_component}" weight="{_f(cp.weight[i])}"/>\n')
+            w(' </continuousProjection>\n')
     n_list = 0
 
     def input_lists(obj, comp_of, weighted):
@@ -742,8 +766,15 @@ def read_lems(path: str) -> NetworkSpec:
             synapses[e.get("id")] = SynapseType(e.get("id"), kind, 1000.0 if cond else 1.0,
                                                 _qty(e, "e_rev", None) if cond else 0.0, _qty(e, "tau_syn", None),
                                                 form=t)
-        elif t == "gapJunction":
-            gap_def[e.get("id")] = GapJunctionType(e.get("id"), _qty(e, "conductance", "conductance"))
+        elif t in ("gapJunction", "linearGradedSynapse"):
+            gap_def[e.get("id")] = GapJunctionType(e.get("id"), _qty(e, "conductance", "conductance"), kind=t)
+        elif t == "silentSynapse":
+            gap_def[e.get("id")] = GapJunctionType(e.get("id"), 0.0, kind=t)
+        elif t == "gradedSynapse":
+            # LEMS_CoreComponents.inc.xml:38-80
+            gap_def[e.get("id")] = GapJunctionType(e.get("id"), _qty(e, "conductance", "conductance"), kind=t,
+                                                   delta=_qty(e, "delta", "voltage"), k=_qty(e, "k", "rate_per_ms"),
+                                                   vth=_qty(e, "Vth", "voltage"), erev=_qty(e, "erev", "voltage"))
         elif t in ("pulseGenerator", "pulseGeneratorDL"):
             dl = t.endswith("DL")
             pulses_def[e.get("id")] = (_qty(e, "delay", "time"), _qty(e, "duration", "time"),
@@ -839,7 +870,7 @@ def read_lems(path: str) -> NetworkSpec:
     # network elements that carry dynamics and are not read fail loudly
     # rather than drop out of the simulation
     for el in net:
-        if _tag(el) in ("continuousProjection", "EdenTimeSeriesReader", "cellSet", "synapticConnection"):
+        if _tag(el) in ("EdenTimeSeriesReader", "cellSet", "synapticConnection"):
             raise ValueError(f"<{_tag(el)} id={el.get('id')}> is not supported")
     # populations (declaration order = gid order)
     pops = {}
@@ -917,7 +948,8 @@ def read_lems(path: str) -> NetworkSpec:
                 continue
             syn = c.get("synapse")
             if syn not in gap_def:
-                raise ValueError(f"electricalProjection {pr.get('id')}: synapse {syn} is not a gapJunction")
+                raise ValueError(f"electricalProjection {pr.get('id')}: synapse {syn} is not a gapJunction, "
+                                 f"linearGradedSynapse, gradedSynapse or silentSynapse")
             rows = by_gap.setdefault(syn, [[], [], [], [], []])
             rows[0].append(gid(_cell_ref(c.get("preCell"), pops, pa)))
             rows[1].append(int(c.get("preSegment", "0")))
@@ -927,6 +959,31 @@ def read_lems(path: str) -> NetworkSpec:
     for syn, rows in by_gap.items():
         spec.electrical.append(ElectricalProjection(f"gap_{syn}", syn, *(np.array(r, np.int64) for r in rows[:4]),
                                                     np.array(rows[4])))
+    # continuous projections: preComponent on the pre end, postComponent on
+    # the post end (eden/NeuroML.cpp:6126-6128 the connection forms,
+    # 6243-6260 the components; eden/Eden.cpp:9254-9270 both ends)
+    for pr in _children(net, "continuousProjection"):
+        pa, pb = pr.get("presynapticPopulation"), pr.get("postsynapticPopulation")
+        by_pair = {}
+        for c in pr:
+            tag = _tag(c)
+            if tag not in ("continuousConnection", "continuousConnectionInstance", "continuousConnectionInstanceW"):
+                continue
+            key = (c.get("preComponent"), c.get("postComponent"))
+            for comp in key:
+                if comp not in gap_def:
+                    raise ValueError(f"continuousProjection {pr.get('id')}: component {comp} is not a "
+                                     f"linearGradedSynapse, gradedSynapse, silentSynapse or gapJunction")
+            rows = by_pair.setdefault(key, [[], [], [], [], []])
+            rows[0].append(gid(_cell_ref(c.get("preCell"), pops, pa)))
+            rows[1].append(int(c.get("preSegment", "0")))
+            rows[2].append(gid(_cell_ref(c.get("postCell"), pops, pb)))
+            rows[3].append(int(c.get("postSegment", "0")))
+            rows[4].append(float(c.get("weight", "1")) if tag.endswith("W") else 1.0)
+        for (ca, cb), rows in by_pair.items():
+            spec.continuous.append(ContinuousProjection(pr.get("id"), ca, cb,
+                                                        *(np.array(r, np.int64) for r in rows[:4]),
+                                                        np.array(rows[4])))
     # inputs
     pcell, pseg, pdel, pdur, pamp, pwt, pdl, plist = [], [], [], [], [], [], [], []
     pois_rows, wave_rows, clamp_rows = {}, {}, {}

@@ -978,6 +978,54 @@ def pynn_synapses(n_hh: int = 6, n_branch: int = 3, n_izh: int = 4, length_ms: f
     return spec
 
 
+def continuous_synapses(n_pairs: int = 6, length_ms: float = 60.0, dt_ms: float = 0.01,
+                        seed: int = 1234) -> NetworkSpec:
+    """Continuous connections between HH cells (spiking under DC pulses)
+    and the somata or dendrites of branching cells: linearGradedSynapse on
+    either end with silentSynapse on the other, silentSynapse to
+    gradedSynapse, gradedSynapse on both ends, a linearGradedSynapse on an
+    electrical connection, and a gapJunction on a continuous connection;
+    weights 0.5-1.5.  (dt 0.01 ms: forward Euler on a graded synapse's s
+    is stable while dt k / (1 - inf) < 2, which the reference's own test
+    network keeps with dt 0.002 ms and k 0.025 per ms.)"""
+    from .network import ContinuousProjection
+    rng = np.random.default_rng(seed)
+    spec = NetworkSpec("continuous_synapses", dt_ms, length_ms, seed, channels=hh_channels())
+    spec.gap_types += [GapJunctionType("lin", 2.0, kind="linearGradedSynapse"),
+                       GapJunctionType("silent", 0.0, kind="silentSynapse"),
+                       GapJunctionType("graded", 5.0, kind="gradedSynapse", delta=5.0, k=0.025, vth=-35.0, erev=0.0),
+                       GapJunctionType("graded_inh", 3.0, kind="gradedSynapse", delta=4.0, k=0.02, vth=-40.0,
+                                       erev=-80.0),
+                       GapJunctionType("gap", 1.0)]
+    spec.cells.append(PhysicalCell("hhcell", np.array([-1]), np.array([0.0]), np.array([17.8]),
+                                   _hh_densities(1, np.ones(1, bool)), cm=1.0, ra=30.0, v0=-65.0, spike_thresh=-20.0))
+    parent = np.array([-1, 0, 1])
+    soma = parent < 0
+    spec.cells.append(PhysicalCell("branch", parent, np.array([20.0, 60.0, 50.0]), np.array([20.0, 2.0, 1.5]),
+                                   _hh_densities(3, soma), cm=1.0, ra=150.0, v0=-65.0, spike_thresh=-20.0,
+                                   seg_groups={"soma_group": soma, "dend_group": ~soma}))
+    spec.populations.append(Population("pre", "hhcell", n_pairs))
+    spec.populations.append(Population("post", "branch", n_pairs))
+    pre = np.arange(n_pairs)
+    post = n_pairs + np.arange(n_pairs)
+    spec.pulses.append(PulseInputs("*", pre, np.zeros(n_pairs, int), np.round(rng.uniform(2.0, 8.0, n_pairs), 3),
+                                   np.full(n_pairs, 40.0), np.round(rng.uniform(0.1, 0.3, n_pairs), 4)))
+    w = lambda n: np.round(rng.uniform(0.5, 1.5, n), 4)
+    z = lambda n: np.zeros(n, np.int64)
+    forms = [("lin", "silent"), ("silent", "lin"), ("silent", "graded"), ("graded", "graded_inh"),
+             ("gap", "silent"), ("silent", "graded_inh")]
+    for k, (ca, cb) in enumerate(forms):
+        i = np.array([k % n_pairs, (k + 2) % n_pairs])
+        seg = np.array([0, 2])
+        spec.continuous.append(ContinuousProjection(f"cont_{k}", ca, cb, pre[i], z(2), post[i], seg, w(2)))
+    spec.electrical.append(ElectricalProjection("lin_el", "lin", pre[[1, 4]], z(2), post[[3, 5]], np.array([1, 2]),
+                                                w(2)))
+    cols = [(int(g), 0) for g in pre] + [(int(g), seg) for g in post for seg in (0, 2)]
+    spec.trace_columns = [OutputColumn(*_gid_to_pop(spec, g), seg) for g, seg in cols]
+    spec.event_selections = [EventSelection(*_gid_to_pop(spec, int(g)), 0) for g in np.concatenate([pre, post])]
+    return spec
+
+
 def gap_junctions(n_hh: int = 10, n_branch: int = 4, n_izh: int = 2, length_ms: float = 80.0,
                   dt_ms: float = 0.025, seed: int = 1234) -> NetworkSpec:
     """Gap junctions (two gapJunction types, 1 and 4 nS, weights 0.5-1.5)
@@ -1055,6 +1103,7 @@ CONFIGS = {
     "gap_junctions": gap_junctions,
     "alpha_synapses": alpha_synapses,
     "pynn_synapses": pynn_synapses,
+    "continuous_synapses": continuous_synapses,
     "routing_probe": routing_probe,
     "random_sources": random_sources,
     "custom_setup": custom_setup,

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 10
+#define EDEN_GPU_ABI_VERSION 11
 
 enum {
     EDEN_GPU_OK = 0,
@@ -124,6 +124,7 @@ typedef struct EdenGpuChannelType {
 enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1, EDEN_SYN_ALPHA = 2, EDEN_SYN_ALPHA_CURRENT = 3,
        EDEN_SYN_EXPONE_CURRENT = 4 };
 enum { EDEN_CABLE_BWD_EULER = 0, EDEN_CABLE_FWD_EULER = 1 };
+#define EDEN_GRADED_PARAMS 5
 
 /* expOneSynapse (native, eden/Eden.cpp:3424-3466), expTwoSynapse,
  * alphaSynapse or alphaCurrentSynapse (LEMS, LEMS_CoreComponents.inc.xml:
@@ -290,6 +291,23 @@ typedef struct EdenGpuModel {
      * potentials at the start of the step (4969-4990, 6092-6094).  A
      * forward-Euler model runs the per-step kernels in either mode. */
     int32_t cable_solver;
+
+    /* gradedSynapse ends (continuous connections, LEMS_CoreComponents.inc.xml:
+     * 38-80; instantiated on each end like gap junctions, eden/Eden.cpp:
+     * 9254-9270): on compartment `graded_target`, with the potential of
+     * `graded_peer` at the step's start as vpeer,
+     *   inf = 1 / (1 + exp((Vth - vpeer) / delta)),  tau = (1 - inf) / k,
+     *   i = weight * conductance * s * (erev - V)   (current only),
+     *   s' = (inf - s) / tau while 1 - inf > 1e-4, else s = inf; s = 0 at start.
+     * graded_params per end: conductance (uS), delta (mV), k (1/us), Vth
+     * (mV), erev (mV).  A linearGradedSynapse end is a gap-junction end
+     * above; a silentSynapse end is nothing.  Like gap junctions they run
+     * one-step windows. */
+    int64_t n_graded;
+    const int32_t *graded_target;
+    const int32_t *graded_peer;
+    const float *graded_params;     /* [n_graded * EDEN_GRADED_PARAMS] */
+    const float *graded_weight;
 } EdenGpuModel;
 
 /* Execution options. */

@@ -154,6 +154,10 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         dm.gap_peer = g.copy(m->gap_peer, (size_t)m->n_gap);
         dm.gap_conductance = g.copy(m->gap_conductance, (size_t)m->n_gap);
         dm.gap_weight = g.copy(m->gap_weight, (size_t)m->n_gap);
+        dm.graded_target = g.copy(m->graded_target, (size_t)m->n_graded);
+        dm.graded_peer = g.copy(m->graded_peer, (size_t)m->n_graded);
+        dm.graded_params = g.copy(m->graded_params, (size_t)m->n_graded * EDEN_GRADED_PARAMS);
+        dm.graded_weight = g.copy(m->graded_weight, (size_t)m->n_graded);
         dm.pois_rng_base = m->pois_rng_base ? g.copy(m->pois_rng_base, (size_t)np) : nullptr;
         // the loop's state, set up on the host
         Port D = H;
@@ -174,6 +178,7 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
             D.spiked[b] = g.copy(H.spiked[b], (size_t)m->n_src + 1);
             D.timed_a[b] = g.copy(H.timed_a[b], (size_t)m->n_timed + 1);
             D.timed_b[b] = g.copy(H.timed_b[b], (size_t)m->n_timed + 1);
+            D.gr_s[b] = g.copy(H.gr_s[b], (size_t)m->n_graded + 1);
         }
         D.diag = g.copy(H.diag, (size_t)m->n_comp + 1);
         D.gate_off = g.copy(H.gate_off, (size_t)n_chan + 1);
@@ -192,6 +197,8 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
         D.timed_order = g.copy(H.timed_order, (size_t)m->n_timed + 1);
         D.gap_off = g.copy(H.gap_off, (size_t)nt + 1);
         D.gap_order = g.copy(H.gap_order, (size_t)m->n_gap + 1);
+        D.gr_off = g.copy(H.gr_off, (size_t)nt + 1);
+        D.gr_order = g.copy(H.gr_order, (size_t)m->n_graded + 1);
         int32_t *d_tt = g.copy(trace_target, (size_t)n_trace);
         double *d_trace = g.zeros<double>((size_t)n_steps * (size_t)(n_trace > 0 ? n_trace : 1));
         int32_t *d_lsrc = g.zeros<int32_t>((size_t)spike_cap);

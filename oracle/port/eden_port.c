@@ -113,6 +113,8 @@ typedef struct {
     int64_t *timed_tgt_off;             /* [n_target + 1] timed inputs by target */
     int64_t *timed_order;               /* inputs in target order */
     int64_t *gap_off, *gap_order;       /* gap-junction ends by target, model order within one */
+    int64_t *gr_off, *gr_order;         /* gradedSynapse ends likewise */
+    real *gr_s[2];                      /* their state s */
     unsigned char *spiked[2];           /* event-logger slot per source */
     real *diag;
     int64_t *gate_off;                  /* [n_chan + 1] */
@@ -389,11 +391,29 @@ static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, rea
     /* gap junctions: each end adds (g (V_peer - V)) w with the peer's
      * potential at the step's start, and no conductance term
      * (eden/Eden.cpp:3407-3422 exposure, 3689-3704 Vpeer, 3708-3710 sum) */
-    if (P->gap_off[tgt] < P->gap_off[tgt + 1]) {
+    if (P->gap_off[tgt] < P->gap_off[tgt + 1] || P->gr_off[tgt] < P->gr_off[tgt + 1]) {
         real Ia = R(0.0);
         for (int64_t q = P->gap_off[tgt]; q < P->gap_off[tgt + 1]; q++) {
             const int64_t k = P->gap_order[q];
             Ia += ((real)m->gap_conductance[k] * (P->v[cur][m->gap_peer[k]] - v)) * (real)m->gap_weight[k];
+        }
+        /* gradedSynapse ends (LEMS_CoreComponents.inc.xml:38-80): inf and tau
+         * from the peer's potential, i = conductance s (erev - V) from the
+         * step's s, s' = (inf - s) / tau by forward Euler while 1 - inf >
+         * 1e-4, else s = inf; s = 0 at the initialisation steps */
+        for (int64_t q = P->gr_off[tgt]; q < P->gr_off[tgt + 1]; q++) {
+            const int64_t k = P->gr_order[q];
+            const float *p = m->graded_params + (int64_t)EDEN_GRADED_PARAMS * k;
+            const real s = P->gr_s[cur][k];
+            const real inf = R(1.0) / (R(1.0) + EXP(((real)p[3] - P->v[cur][m->graded_peer[k]]) / (real)p[1]));
+            const real tau = (R(1.0) - inf) / (real)p[2];
+            Ia += (((real)p[0] * s) * ((real)p[4] - v)) * (real)m->graded_weight[k];
+            real sn = R(0.0);
+            if (!init) {
+                sn = s + dt * ((R(1.0) - inf) > (real)1e-4 ? (inf - s) / tau : R(0.0));
+                if ((R(1.0) - inf) < (real)1e-4) sn = inf;
+            }
+            P->gr_s[cur ^ 1][k] = sn;
         }
         Isyn += Ia;
     }
@@ -742,6 +762,17 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
     P.wave_off = csr_by_key(m->wave_target, m->n_wave, nt);
     P.clamp_off = csr_by_key(m->clamp_target, m->n_clamp, nt);
     P.fan_off = csr_by_key(m->syn_src, ns, m->n_src);
+    P.gr_off = csr_by_key(m->graded_target, m->n_graded, nt);
+    P.gr_order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m->n_graded + 1));
+    {
+        int64_t *fill = (int64_t *)calloc((size_t)nt + 1, sizeof(int64_t));
+        for (int64_t k = 0; k < m->n_graded; k++) {
+            int32_t t = m->graded_target[k];
+            P.gr_order[P.gr_off[t] + fill[t]++] = k;
+        }
+        free(fill);
+    }
+    for (int b = 0; b < 2; b++) P.gr_s[b] = (real *)calloc((size_t)m->n_graded + 1, sizeof(real));
     P.gap_off = csr_by_key(m->gap_target, m->n_gap, nt);
     P.gap_order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m->n_gap + 1));
     {
@@ -782,6 +813,7 @@ static void port_free(Port *P) {
     free(P->diag); free(P->syn_fire_count); free(P->gate_off); free(P->syn_off); free(P->pois_off);
     free(P->pulse_off); free(P->wave_off); free(P->clamp_off); free(P->fan_off); free(P->fan_syn); free(P->order); free(P->src_of_target);
     free(P->timed_cur); free(P->timed_tgt_off); free(P->timed_order); free(P->gap_off); free(P->gap_order);
+    free(P->gr_off); free(P->gr_order); free(P->gr_s[0]); free(P->gr_s[1]);
 }
 
 /* Wall-clock marks for timing a stretch of a run (the CPU timings beside

@@ -26,6 +26,7 @@ CASES = {
     "gap_junctions": ("gap_junctions", dict(), 1.0, None),
     "alpha_synapses": ("alpha_synapses", dict(), 1.0, None),
     "pynn_synapses": ("pynn_synapses", dict(), 1.0, None),
+    "continuous_synapses": ("continuous_synapses", dict(), 1.0, None),
     # the reference's `cable_solver fwd_euler` (an explicit cable update):
     # HH ball-and-stick cells with five dendrite compartments, and the
     # branched cells of the input-kinds case (stable at dt 0.025 ms, unlike

@@ -120,3 +120,18 @@ def test_pynn_and_exp_three_synapses_round_trip(tmp_path):
     bad.poissons[0].synapse = "syn_e3"
     with pytest.raises(ValueError, match="expThreeSynapse"):
         lowering.lower(bad)
+
+
+def test_continuous_projections_round_trip(tmp_path):
+    """continuousConnectionInstanceW with linearGraded, graded, silent and
+    gapJunction components on either end, and a linearGradedSynapse on an
+    electrical connection: written and read back to the same lowered ends."""
+    spec = spec_of("continuous_synapses")
+    low = lowering.lower(spec)
+    assert len(low.graded_target) == 2 + 2 * 2 + 2 and len(low.gap_target) == 2 + 2 + 2 + 2 * 2
+    back = neuroml_io.read_lems(neuroml_io.write_lems(spec, str(tmp_path)))
+    assert [(g.name, g.kind) for g in back.gap_types] == [(g.name, g.kind) for g in spec.gap_types]
+    low2 = lowering.lower(back)
+    for f in ("gap_target", "gap_peer", "gap_conductance", "gap_weight", "graded_target", "graded_peer",
+              "graded_params", "graded_weight"):
+        np.testing.assert_array_equal(getattr(low2, f), getattr(low, f), err_msg=f)
