@@ -304,9 +304,15 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
     }
     for (int k = 0; k < m->n_syn_types; k++) {
         const EdenGpuSynapseType &t = m->syn_types[k];
-        if (t.kind < EDEN_SYN_EXPONE || t.kind > EDEN_SYN_EXPONE_CURRENT)
+        if (t.kind < EDEN_SYN_EXPONE || t.kind > EDEN_SYN_BLOCKING_PLASTIC)
             return ctx->fail(EDEN_GPU_E_INVALID, "synapse type kind");
-        if (!finite_pos(t.tau_decay) || (t.kind == EDEN_SYN_EXPTWO && !finite_pos(t.tau_rise)))
+        if (t.kind == EDEN_SYN_BLOCKING_PLASTIC &&
+            (!std::isfinite(t.release_prob) || !(t.tau_rec >= 0.0f) || !(t.tau_fac >= 0.0f) ||
+             !std::isfinite(t.block_ratio) || !std::isfinite(t.block_volt) || !std::isfinite(t.tau_rec) ||
+             !std::isfinite(t.tau_fac)))
+            return ctx->fail(EDEN_GPU_E_INVALID, "synapse type %d: plasticity or block parameters", k);
+        const bool two = t.kind == EDEN_SYN_EXPTWO || t.kind == EDEN_SYN_BLOCKING_PLASTIC;
+        if (!finite_pos(t.tau_decay) || (two && !finite_pos(t.tau_rise)))
             return ctx->fail(EDEN_GPU_E_INVALID, "synapse type %d: time constants", k);
     }
     for (int64_t s = 0; s < m->n_syn; s++) {
@@ -373,6 +379,14 @@ int validate(EdenGpuCtx *ctx, const EdenGpuModel *m) {
         if (!std::isfinite(m->gap_conductance[k]) || !std::isfinite(m->gap_weight[k]))
             return ctx->fail(EDEN_GPU_E_INVALID, "gap junction %lld: non-finite conductance or weight", (long long)k);
     }
+    for (int64_t k = 0; k < m->n_pois; k++)
+        if (m->syn_types[m->pois_type[k]].kind == EDEN_SYN_BLOCKING_PLASTIC)
+            return ctx->fail(EDEN_GPU_E_INVALID, "Poisson input %lld: blocking-plastic synapses on connections only",
+                             (long long)k);
+    for (int64_t k = 0; k < m->n_timed; k++)
+        if (m->syn_types[m->timed_type[k]].kind == EDEN_SYN_BLOCKING_PLASTIC)
+            return ctx->fail(EDEN_GPU_E_INVALID, "timed input %lld: blocking-plastic synapses on connections only",
+                             (long long)k);
     if (m->n_graded < 0) return ctx->fail(EDEN_GPU_E_INVALID, "n_graded must be >= 0");
     if (m->n_graded > 0 && (!m->graded_target || !m->graded_peer || !m->graded_params || !m->graded_weight))
         return ctx->fail(EDEN_GPU_E_INVALID, "graded synapses: null array");
@@ -515,7 +529,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             const EdenGpuSynapseType &st = m->syn_types[type];
             if (current_kind(st.kind)) return 1.0f;  // a current: no conductance on the diagonal
             float sg = st.gbase * w;
-            if (st.kind == EDEN_SYN_EXPTWO) sg *= st.waveform_factor * st.weight_prop;
+            if (st.kind == EDEN_SYN_EXPTWO || st.kind == EDEN_SYN_BLOCKING_PLASTIC)
+                sg *= st.waveform_factor * st.weight_prop;
             return sg;
         };
         auto flag_comp = [&](int32_t t) { if (t >= 0 && t < n_comp) cell_f64[comp_cell[t]] = 1; };
@@ -1063,8 +1078,10 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         for (int64_t k = soff[t]; k < soff[t + 1];) {
             int64_t k1 = k;
             while (k1 < soff[t + 1] && sy_type[k1] == sy_type[k]) k1++;
-            bk_kind.push_back(BK_SYN | (current_kind(m->syn_types[sy_type[k]].kind) ? BK_CURRENT : 0));
-            bk_erev.push_back(m->syn_types[sy_type[k]].erev); bk_type.push_back(sy_type[k]);
+            const EdenGpuSynapseType &sk = m->syn_types[sy_type[k]];
+            const bool blocked = sk.kind == EDEN_SYN_BLOCKING_PLASTIC && sk.block_volt != 0.0f;
+            bk_kind.push_back(BK_SYN | (current_kind(sk.kind) ? BK_CURRENT : 0) | (blocked ? BK_BLOCK : 0));
+            bk_erev.push_back(sk.erev); bk_type.push_back(sy_type[k]);
             bk_i0.push_back(k); bk_i1.push_back(k1);
             k = k1;
         }
@@ -1291,8 +1308,12 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
     // (the windowed kernel packs forest-local indices in 10 bits: a single
     // cell of more than 1023 compartments runs the per-step kernels)
     // (the forward-Euler update runs the per-step kernels only)
+    // (and a model with blockingPlasticSynapses, whose voltage block the
+    // per-step kernels apply)
+    bool plastic_syn = false;
+    for (int k = 0; k < m->n_syn_types; k++) plastic_syn |= m->syn_types[k].kind == EDEN_SYN_BLOCKING_PLASTIC;
     ctx->smem_window = max_smem_class <= (size_t)ctx->smem_optin && max_forest <= 1023 &&
-                       m->cable_solver == EDEN_CABLE_BWD_EULER;
+                       m->cable_solver == EDEN_CABLE_BWD_EULER && !plastic_syn;
 
     phase("upload");
     // ---- upload
@@ -1414,6 +1435,23 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             CUDA_TRY(ctx, cudaMemcpy(d.tm_cur, cur.data(), sizeof(int64_t) * cur.size(), cudaMemcpyHostToDevice));
     }
     TRY(upload(ctx, &d.sy_a, (const float *)nullptr, (size_t)ns));
+    {
+        // blockingPlasticSynapse: plasticity state R = 1, U = p at start, and
+        // each input block's voltage-block parameters
+        bool any = false;
+        for (int k = 0; k < m->n_syn_types; k++) any |= m->syn_types[k].kind == EDEN_SYN_BLOCKING_PLASTIC;
+        std::vector<float> R(any ? ns : 1, 1.0f), U(any ? ns : 1, 1.0f);
+        if (any)
+            for (int64_t q = 0; q < ns; q++) U[q] = m->syn_types[sy_type[q]].release_prob;
+        TRY(upload_vec(ctx, &d.sy_R, R)); TRY(upload_vec(ctx, &d.sy_U, U));
+        std::vector<float2> bb(std::max<size_t>(bk_kind.size(), 1), make_float2(0.0f, 1.0f));
+        for (size_t b = 0; b < bk_kind.size(); b++)
+            if (bk_kind[b] & BK_BLOCK) {
+                const EdenGpuSynapseType &sk = m->syn_types[bk_type[b]];
+                bb[b] = make_float2(sk.block_ratio, sk.block_volt);
+            }
+        TRY(upload_c(ctx, &d.bk_block, bb));
+    }
     TRY(upload(ctx, &d.sy_b, (const float *)nullptr, (size_t)ns));
     TRY(upload(ctx, &d.sy_last, (const int32_t *)nullptr, (size_t)ns));
     TRY(upload_vec(ctx, &d.sy_pend, sy_pend));
@@ -1489,9 +1527,14 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
         st[k].tau_decay = s.tau_decay; st[k].tau_rise = s.tau_rise;
         st[k].wf_w = s.weight_prop * s.waveform_factor;
         st[k].r_decay = 1.0f / s.tau_decay;
-        st[k].r_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f / s.tau_rise : 1.0f;
+        const bool two = s.kind == EDEN_SYN_EXPTWO || s.kind == EDEN_SYN_BLOCKING_PLASTIC;
+        st[k].r_rise = two ? 1.0f / s.tau_rise : 1.0f;
         st[k].f_decay = 1.0f - dt / s.tau_decay;
-        st[k].f_rise = s.kind == EDEN_SYN_EXPTWO ? 1.0f - dt / s.tau_rise : 1.0f;
+        st[k].f_rise = two ? 1.0f - dt / s.tau_rise : 1.0f;
+        st[k].plastic = s.kind == EDEN_SYN_BLOCKING_PLASTIC && s.tau_rec > 0.0f;
+        st[k].rel_p = s.release_prob;
+        st[k].f_rec = s.tau_rec > 0.0f ? 1.0f - dt / s.tau_rec : 1.0f;
+        st[k].f_fac = s.tau_fac > 0.0f ? 1.0f - dt / s.tau_fac : 1.0f;
         // an alpha kind's coupling e dt / tau: g' = f g + c A per step
         st[k].c_alpha = (s.kind == EDEN_SYN_ALPHA || s.kind == EDEN_SYN_ALPHA_CURRENT)
                             ? (float)(2.7182818284590451 * (double)dt / (double)s.tau_decay) : 0.0f;
@@ -1563,8 +1606,8 @@ static int build_and_upload(EdenGpuCtx *ctx, const EdenGpuModel *m, const EdenGp
             if (kb != BK_PULSE && kb != BK_CLAMPV) {
                 const int sk = m->syn_types[bk_type[b]].kind;
                 // alpha and current-based expOne items step like expOne's
-                kinds.expone |= sk != EDEN_SYN_EXPTWO;
-                kinds.exptwo |= sk == EDEN_SYN_EXPTWO;
+                kinds.expone |= sk != EDEN_SYN_EXPTWO && sk != EDEN_SYN_BLOCKING_PLASTIC;
+                kinds.exptwo |= sk == EDEN_SYN_EXPTWO || sk == EDEN_SYN_BLOCKING_PLASTIC;
                 kinds.alpha |= sk == EDEN_SYN_ALPHA || sk == EDEN_SYN_ALPHA_CURRENT;
                 kinds.current |= current_kind(sk);
             }
@@ -2019,7 +2062,7 @@ extern "C" int edenGpuReadSynapses(EdenGpuCtx *ctx, float *pending_us, float *st
         const int64_t k = ctx->syn_internal_of_user[u];
         const SynTypeDev &st = ctx->h_syn_types[ctx->h_sy_type[k]];
         const int64_t steps = std::max<int64_t>(0, ctx->next_step - (int64_t)last[k] - 1);
-        const bool two = st.kind == EDEN_SYN_EXPTWO;
+        const bool two = st.kind == EDEN_SYN_EXPTWO || st.kind == EDEN_SYN_BLOCKING_PLASTIC;
         if (pending_us) pending_us[u] = pend[k];
         if (state_a) state_a[u] = steps > 0 ? a[k] * powf(two ? st.f_rise : st.f_decay, (float)steps) : a[k];
         if (state_b) state_b[u] = two ? (steps > 0 ? b[k] * powf(st.f_decay, (float)steps) : b[k]) : 0.0f;

@@ -48,6 +48,11 @@ struct SynTypeDev {
     float r_decay, r_rise;                          // correctly rounded 1 / tau
     float f_decay, f_rise;                          // 1 - dt / tau, one step's decay factor
     float c_alpha;                                  // alpha kinds: e dt / tau, g' = f g + c A
+    // blockingPlasticSynapse: plasticity (plastic != 0) with release
+    // probability p and one step's factors 1 - dt/tau_rec, 1 - dt/tau_fac
+    // (f_fac 1: U stays p)
+    int plastic;
+    float rel_p, f_rec, f_fac;
 };
 
 // x / tau, correctly rounded, from r = RN(1/tau): q = RN(x*r) is within an
@@ -77,7 +82,7 @@ enum : int { BK_PULSE = 0, BK_POIS = 1, BK_SYN = 2, BK_TIMED = 3 };
 enum : int { BK_CLAMPV = 4 };
 // a synapse block of a current-based kind (alphaCurrentSynapse) carries this
 // flag beside its kind: its exposure is a current, with no conductance
-enum : int { BK_KIND_MASK = 7, BK_CURRENT = 8 };
+enum : int { BK_KIND_MASK = 7, BK_CURRENT = 8, BK_BLOCK = 16 };
 // pulse-block types: 0 pulses, then the waveform shapes, then the two halves of a clamp
 enum : int { kPulseSine = 1 + EDEN_WAVE_SINE, kPulseRamp = 1 + EDEN_WAVE_RAMP, kClampA = 3, kClampB = 4 };
 constexpr int kMaxWindow = 31;  // trigger bits 1..K of a 32-bit mask
@@ -174,6 +179,8 @@ struct DevModel {
     int64_t *tm_cur;
     // connection synapses
     float *sy_a, *sy_b, *sy_pend;     // sy_a/sy_b: state just after the synapse's last event
+    float *sy_R, *sy_U;               // blockingPlasticSynapse: plasticity state after the last event
+    const float2 *bk_block;           // per input block: the voltage block's ratio and scaling voltage
     int32_t *sy_last;                 // step of that event
     uint32_t *sy_mask;
     const float *sy_w, *sy_delay;
@@ -425,14 +432,16 @@ __device__ __forceinline__ float decayed(float a, float f, const float *fpow, in
 // aggregate, and the synapse's own state after it.
 template <int KIND>
 __device__ __forceinline__ void input_event(const SynTypeDev &st, const float *pw, float dt, float w, int64_t s,
-                                            float &a, float &b, int32_t &last, float &dA, float &dB) {
+                                            float &a, float &b, int32_t &last, float &dA, float &dB, float js = 1.0f) {
     const int n = (int)(s - (int64_t)last) - 1;
     if (KIND == EDEN_SYN_EXPTWO) {
+        // (js: a blockingPlasticSynapse's plasticity factor for this event)
+        const float jump = st.wf_w * js;
         const float ai = decayed(a, st.f_rise, pw, n), bi = decayed(b, st.f_decay, pw + kPowLen, n);
-        dA = w * (dt * div_by_tau(ai, st.tau_rise, st.r_rise) + st.wf_w);
-        dB = w * (dt * div_by_tau(bi, st.tau_decay, st.r_decay) + st.wf_w);
-        a = ai + st.wf_w;
-        b = bi + st.wf_w;
+        dA = w * (dt * div_by_tau(ai, st.tau_rise, st.r_rise) + jump);
+        dB = w * (dt * div_by_tau(bi, st.tau_decay, st.r_decay) + jump);
+        a = ai + jump;
+        b = bi + jump;
     } else {
         const float gi = decayed(a, st.f_decay, pw + kPowLen, n);
         dA = w * (dt * div_by_tau(gi, st.tau_decay, st.r_decay) + st.gbase);
@@ -563,16 +572,36 @@ __device__ __forceinline__ void syn_window(const DevModel &m, int64_t it, const 
     const float wt = m.sy_w[it];
     float dA, dB;
     const float *pw = m.syn_pow + (size_t)m.sy_type[it] * 2 * kPowLen;
+    // a blockingPlasticSynapse's Tsodyks-Markram state (LEMS_CoreComponents.inc.xml:
+    // 263-312): forward Euler from the last event, 1 - R and U - p shrinking
+    // by their factor each step; the event's jump scaled by R U before the
+    // event, which then sets R = R (1 - U), U = U + p (1 - U)
+    const bool plastic = KIND == EDEN_SYN_EXPTWO && st.plastic;
+    float R = plastic ? m.sy_R[it] : 1.0f, U = plastic ? m.sy_U[it] : 1.0f;
+    auto factor = [&](int64_t s) {
+        if (!plastic) return 1.0f;
+        const float n = (float)(s - (int64_t)last - 1);
+        R = 1.0f - (1.0f - R) * powf(st.f_rec, n);
+        U = st.rel_p + (U - st.rel_p) * powf(st.f_fac, n);
+        const float f = R * U;
+        R = R * (1.0f - U);
+        U = U + st.rel_p * (1.0f - U);
+        if (st.f_fac == 1.0f) U = st.rel_p;
+        return f;
+    };
     if (now && jf != 0) {
-        input_event<KIND>(st, pw, dt, wt, w.step0, a, b, last, dA, dB);
+        const float js = factor(w.step0);
+        input_event<KIND>(st, pw, dt, wt, w.step0, a, b, last, dA, dB, js);
         put_event(rowA, rowB, used, w.K, 0, dA, dB);
     }
     if (jf >= 0) {
-        input_event<KIND>(st, pw, dt, wt, w.step0 + jf, a, b, last, dA, dB);
+        const float js = factor(w.step0 + jf);
+        input_event<KIND>(st, pw, dt, wt, w.step0 + jf, a, b, last, dA, dB, js);
         put_event(rowA, rowB, used, w.K, jf, dA, dB);
     }
     m.sy_a[it] = a;
     if (KIND == EDEN_SYN_EXPTWO) m.sy_b[it] = b;
+    if (plastic) { m.sy_R[it] = R; m.sy_U[it] = U; }
     m.sy_last[it] = last;
 }
 
@@ -773,7 +802,7 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
     }
     const int type = (info >> 2) & 63;
     const SynTypeDev st = m.syn_types[type];
-    const bool two = st.kind == EDEN_SYN_EXPTWO;
+    const bool two = st.kind == EDEN_SYN_EXPTWO || st.kind == EDEN_SYN_BLOCKING_PLASTIC;
     bool used = false;
     // the chunk's aggregate and its items' per-window state, loaded up front
     // so the loads overlap
@@ -874,11 +903,16 @@ __device__ __forceinline__ void chunk_window(const DevModel &m, int c, int32_t i
 // (indexed from blk0 and chk0, which may point into shared memory).
 __device__ __forceinline__ void block_currents(const float *Gpk, int b0, int b1, const int32_t *BK_K,
                                                const float *BK_E, const int32_t *BC0, int chk0, float v, float &Iin,
-                                               float &Gin, float &Isyn, float &Gsyn) {
+                                               float &Gin, float &Isyn, float &Gsyn,
+                                               const float2 *BK_B = nullptr) {
     Iin = 0.0f; Gin = 0.0f; Isyn = 0.0f; Gsyn = 0.0f;
     for (int bk = b0; bk < b1; bk++) {
         float g = 0.0f;
         for (int c = BC0[bk]; c < BC0[bk + 1]; c++) g += Gpk[c + chk0];
+        // a blockingPlasticSynapse's voltage block (voltageConcDepBlockMechanism,
+        // LEMS_CoreComponents.inc.xml:231-245) scales its conductance, so both
+        // the current and the conductance term (per-step kernels only)
+        if (BK_B && (BK_K[bk] & BK_BLOCK)) g = (1.0f / (1.0f + BK_B[bk].x * expf(-1.0f * (v / BK_B[bk].y)))) * g;
         const int kind = BK_K[bk] & BK_KIND_MASK;
         const bool current = EDEN_KIND_CURRENT && (BK_K[bk] & BK_CURRENT);
         if (kind == BK_PULSE) {

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(256) k_targets_t(DevModel m, const WindowArgs 
         if (i < n) {
             float v = vin[i], Iin, Gin, Isyn, Gsyn;
             block_currents(m.Gp, m.t_blk0[i], m.t_blk0[i + 1], m.bk_kind, m.bk_erev, m.bk_c0, 0, v, Iin, Gin, Isyn,
-                           Gsyn);
+                           Gsyn, m.bk_block);
             if (EDEN_KIND_GAP) Isyn += gap_current(m, i, v, vin, init);
             const float Iax = (m.fwd_euler && !init && m.t_izh[i] < 0) ? axial_current(m, i, v, vin) : 0.0f;
             target_step(m, i, init, w.step0, tnow, v, Iin, Gin, Isyn, Gsyn, &vout[i], &m.diag[i], w.wpar, Iax);

@@ -32,7 +32,7 @@ from .network import (SPIKE_SOURCE_TYPES, AdExCell, EventSetReaderCell, FitzHugh
                       NetworkSpec,
                       PhysicalCell, SpikeArrayCell, SpikeGeneratorPoissonCell, SpikeGeneratorRandomCell,
                       WAVE_RAMP, WAVE_SINE,
-                      SYN_EXPTWO, SYN_ALPHA_CURRENT, SYN_EXPONE_CURRENT, SYN_EXPTHREE, SynapseType)
+                      SYN_EXPTWO, SYN_ALPHA_CURRENT, SYN_EXPONE_CURRENT, SYN_EXPTHREE, SYN_BLOCKING_PLASTIC, SynapseType)
 
 F32 = np.float32
 MAX_GATES = 4
@@ -196,6 +196,8 @@ SYN_DTYPE = np.dtype([
     ("kind", np.int32), ("gbase", np.float32), ("erev", np.float32),
     ("tau_decay", np.float32), ("tau_rise", np.float32),
     ("waveform_factor", np.float32), ("weight_prop", np.float32),
+    ("release_prob", np.float32), ("tau_rec", np.float32), ("tau_fac", np.float32),
+    ("block_ratio", np.float32), ("block_volt", np.float32),
 ], align=True)
 
 
@@ -513,6 +515,10 @@ def _split_exp_three(spec):
     refused on an expThreeSynapse."""
     import copy
     import dataclasses
+    plastic = {s.name for s in spec.synapses if s.kind == SYN_BLOCKING_PLASTIC}
+    for inp in list(spec.poissons) + list(spec.timed):
+        if inp.synapse in plastic:
+            raise ValueError(f"blockingPlasticSynapse {inp.synapse} on an input: connections only")
     three = {s.name: s for s in spec.synapses if s.kind == SYN_EXPTHREE}
     if not three:
         return spec
@@ -543,6 +549,8 @@ def _split_exp_three(spec):
             out.timed.append(dataclasses.replace(ti, synapse=f"{ti.synapse}:{k}"))
     return out
 
+
+EDEN_SYN_BLOCKING_PLASTIC = 5   # the library's kind number of a blockingPlasticSynapse
 
 CABLE_BWD_EULER = 0
 CABLE_FWD_EULER = 1
@@ -712,16 +720,24 @@ def lower(spec: NetworkSpec) -> LoweredModel:
     for k, s in enumerate(spec.synapses):
         syn_index[s.name] = k
         st = syn_types[k]
-        st["kind"] = s.kind
+        st["kind"] = EDEN_SYN_BLOCKING_PLASTIC if s.kind == SYN_BLOCKING_PLASTIC else s.kind
         # nS -> uS; the current-based kinds' jumps stay in nA
         st["gbase"] = (_to_f32(s.gbase) if s.kind in (SYN_ALPHA_CURRENT, SYN_EXPONE_CURRENT)
                        else _to_f32(s.gbase * 1e-3))
         st["erev"] = _to_f32(s.erev)
         st["tau_decay"] = _to_f32(s.tau_decay * 1000.0)
-        st["tau_rise"] = _to_f32(s.tau_rise * 1000.0) if s.kind == SYN_EXPTWO else 0.0
-        st["waveform_factor"] = (exptwo_waveform_factor(st["tau_rise"], st["tau_decay"])
-                                 if s.kind == SYN_EXPTWO else 1.0)
+        two = s.kind in (SYN_EXPTWO, SYN_BLOCKING_PLASTIC)
+        st["tau_rise"] = _to_f32(s.tau_rise * 1000.0) if two else 0.0
+        st["waveform_factor"] = exptwo_waveform_factor(st["tau_rise"], st["tau_decay"]) if two else 1.0
         st["weight_prop"] = 1.0
+        if s.kind == SYN_BLOCKING_PLASTIC:
+            if s.plasticity:
+                st["release_prob"] = _to_f32(s.plasticity["initReleaseProb"])
+                st["tau_rec"] = _to_f32(s.plasticity["tauRec"] * 1000.0)
+                st["tau_fac"] = _to_f32(s.plasticity.get("tauFac", 0.0) * 1000.0)
+            if s.block:
+                st["block_ratio"] = _to_f32(s.block["blockConcentration"] / s.block["scalingConc"])
+                st["block_volt"] = _to_f32(s.block["scalingVolt"])
 
     # ---- gap junctions: each electrical connection puts an instance on both
     # ends, each taking weight * conductance * (V_peer - V_own) as synaptic
@@ -953,7 +969,7 @@ def lower(spec: NetworkSpec) -> LoweredModel:
 # ---------------------------------------------------------------------------
 # ctypes mirror of include/eden_gpu.h
 # ---------------------------------------------------------------------------
-ABI_VERSION = 11
+ABI_VERSION = 12
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)

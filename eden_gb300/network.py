@@ -258,6 +258,7 @@ SYN_ALPHA = 2           # alphaSynapse: conductance, rise and decay both tau
 SYN_ALPHA_CURRENT = 3   # alphaCurrentSynapse: current ibase, rise and decay both tau
 SYN_EXPONE_CURRENT = 4  # expCurrSynapse (PyNN): current-based, instantaneous rise, single decay
 SYN_EXPTHREE = 5        # expThreeSynapse: two expTwo components sharing a rise time
+SYN_BLOCKING_PLASTIC = 6  # blockingPlasticSynapse: expTwo with a voltage block and short-term plasticity
 
 
 @dataclass
@@ -279,6 +280,10 @@ class SynapseType:
     gbase2: float = 0.0    # nS (expThree)
     tau_decay2: float = 0.0  # ms (expThree)
     form: str = ""         # the NeuroML element a PyNN synapse was read from
+    # blockingPlasticSynapse: its mechanisms' type and parameters (mM, mV,
+    # ms, dimensionless), or None
+    block: Optional[dict] = None
+    plasticity: Optional[dict] = None
 
 
 @dataclass

@@ -27,7 +27,7 @@ from .network import (Channel, ChannelDensity, EventSelection, Gate,
                       RATE_TYPE_NAMES, SYN_EXPONE, SYN_EXPTWO, WAVE_SINE, WAVE_RAMP, AdExCell, IafCell,
                       ClampInputs, FitzHughNagumoCell, IzhikevichCell, TimedInputs, WaveInputs,
                       ElectricalProjection, GapJunctionType, SYN_ALPHA, SYN_ALPHA_CURRENT,
-                      SYN_EXPONE_CURRENT, SYN_EXPTHREE, ContinuousProjection)
+                      SYN_EXPONE_CURRENT, SYN_EXPTHREE, ContinuousProjection, SYN_BLOCKING_PLASTIC)
 
 
 def _f(x: float) -> str:
@@ -82,6 +82,20 @@ def write_lems(spec: NetworkSpec, dirname: str) -> str:
             cond = _PYNN_SYNAPSES[s.form][1]
             w(f'<{s.form} id="{s.name}" tau_syn="{_f(s.tau_decay)}"' + (f' e_rev="{_f(s.erev)}"' if cond else '')
               + '/>\n')
+        elif s.kind == SYN_BLOCKING_PLASTIC:
+            w(f'<blockingPlasticSynapse id="{s.name}" gbase="{_f(s.gbase)}nS" erev="{_f(s.erev)}mV" '
+              f'tauRise="{_f(s.tau_rise)}ms" tauDecay="{_f(s.tau_decay)}ms">\n')
+            if s.block:
+                b = s.block
+                w(f' <blockMechanism type="voltageConcDepBlockMechanism" species="{b.get("species") or "mg"}" '
+                  f'blockConcentration="{_f(b["blockConcentration"])}mM" scalingConc="{_f(b["scalingConc"])}mM" '
+                  f'scalingVolt="{_f(b["scalingVolt"])}mV"/>\n')
+            if s.plasticity:
+                pl = s.plasticity
+                w(f' <plasticityMechanism type="{pl["type"]}" initReleaseProb="{_f(pl["initReleaseProb"])}" '
+                  f'tauRec="{_f(pl["tauRec"])}ms"' + (f' tauFac="{_f(pl["tauFac"])}ms"' if "tauFac" in pl else "")
+                  + '/>\n')
+            w('</blockingPlasticSynapse>\n')
         elif s.kind == SYN_EXPTHREE:
             w(f'<expThreeSynapse id="{s.name}" gbase1="{_f(s.gbase)}nS" gbase2="{_f(s.gbase2)}nS" '
               f'erev="{_f(s.erev)}mV" tauRise="{_f(s.tau_rise)}ms" tauDecay1="{_f(s.tau_decay)}ms" '
@@ -466,6 +480,7 @@ _UNITS = {
     "resistivity": {"ohm_cm": 1.0, "kohm_cm": 1e3, "ohm_m": 100.0},
     "frequency_hz": {"Hz": 1.0, "per_s": 1.0, "per_ms": 1e3, "kHz": 1e3, "per_us": 1e6, "MHz": 1e6},
     "rate_per_ms": {"per_ms": 1.0, "kHz": 1.0, "per_s": 1e-3, "Hz": 1e-3, "per_us": 1e3, "MHz": 1e3},
+    "concentration": {"mM": 1.0, "mol_per_cm3": 1e6, "M": 1e3, "uM": 1e-3},
     "resistance": {"ohm": 1e-6, "kohm": 1e-3, "Mohm": 1.0, "Gohm": 1e3},
     "cond_per_voltage": {"nS_per_mV": 1.0, "S_per_V": 1e9 / 1e3, "uS_per_mV": 1e3, "pS_per_mV": 1e-3},
 }
@@ -753,6 +768,30 @@ def read_lems(path: str) -> NetworkSpec:
         elif t == "alphaCurrentSynapse":
             synapses[e.get("id")] = SynapseType(e.get("id"), SYN_ALPHA_CURRENT, _qty(e, "ibase", "current"), 0.0,
                                                 _qty(e, "tau", "time"))
+        elif t == "blockingPlasticSynapse":
+            # LEMS_CoreComponents.inc.xml:315-352, with at most one block
+            # mechanism (voltageConcDepBlockMechanism, 231-245) and one
+            # plasticity mechanism (tsodyksMarkram(DepFac)Mechanism, 247-312)
+            block = plast = None
+            for ch in e:
+                ct = _tag(ch)
+                if ct == "blockMechanism":
+                    if ch.get("type") != "voltageConcDepBlockMechanism":
+                        raise ValueError(f"{e.get('id')}: block mechanism {ch.get('type')!r} not supported")
+                    block = {"blockConcentration": _qty(ch, "blockConcentration", "concentration"),
+                             "scalingConc": _qty(ch, "scalingConc", "concentration"),
+                             "scalingVolt": _qty(ch, "scalingVolt", "voltage"), "species": ch.get("species", "")}
+                elif ct == "plasticityMechanism":
+                    kind = ch.get("type")
+                    if kind not in ("tsodyksMarkramDepMechanism", "tsodyksMarkramDepFacMechanism"):
+                        raise ValueError(f"{e.get('id')}: plasticity mechanism {kind!r} not supported")
+                    plast = {"type": kind, "initReleaseProb": _qty(ch, "initReleaseProb", None),
+                             "tauRec": _qty(ch, "tauRec", "time")}
+                    if kind.endswith("DepFacMechanism"):
+                        plast["tauFac"] = _qty(ch, "tauFac", "time")
+            synapses[e.get("id")] = SynapseType(e.get("id"), SYN_BLOCKING_PLASTIC, _qty(e, "gbase", "conductance"),
+                                                _qty(e, "erev", "voltage"), _qty(e, "tauDecay", "time"),
+                                                _qty(e, "tauRise", "time"), block=block, plasticity=plast)
         elif t == "expThreeSynapse":
             synapses[e.get("id")] = SynapseType(e.get("id"), SYN_EXPTHREE, _qty(e, "gbase1", "conductance"),
                                                 _qty(e, "erev", "voltage"), _qty(e, "tauDecay1", "time"),

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EDEN_GPU_ABI_VERSION 11
+#define EDEN_GPU_ABI_VERSION 12
 
 enum {
     EDEN_GPU_OK = 0,
@@ -122,7 +122,7 @@ typedef struct EdenGpuChannelType {
 } EdenGpuChannelType;
 
 enum { EDEN_SYN_EXPONE = 0, EDEN_SYN_EXPTWO = 1, EDEN_SYN_ALPHA = 2, EDEN_SYN_ALPHA_CURRENT = 3,
-       EDEN_SYN_EXPONE_CURRENT = 4 };
+       EDEN_SYN_EXPONE_CURRENT = 4, EDEN_SYN_BLOCKING_PLASTIC = 5 };
 enum { EDEN_CABLE_BWD_EULER = 0, EDEN_CABLE_FWD_EULER = 1 };
 #define EDEN_GRADED_PARAMS 5
 
@@ -142,6 +142,19 @@ enum { EDEN_CABLE_BWD_EULER = 0, EDEN_CABLE_FWD_EULER = 1 };
 typedef struct EdenGpuSynapseType {
     int32_t kind;
     float gbase, erev, tau_decay, tau_rise, waveform_factor, weight_prop;
+    /* EDEN_SYN_BLOCKING_PLASTIC (blockingPlasticSynapse,
+     * LEMS_CoreComponents.inc.xml:231-352): expTwo's A and B with each
+     * event's jump scaled by the plasticity factor R U before the event;
+     * tsodyksMarkram(DepFac)Mechanism: R' = (1 - R) / tau_rec,
+     * U' = (release_prob - U) / tau_fac (tau_fac 0: U = release_prob, the
+     * depression-only mechanism), on an event R = R (1 - U),
+     * U = U + release_prob (1 - U); R = 1, U = release_prob at start
+     * (tau_rec 0: no plasticity, factor 1).  voltageConcDepBlockMechanism:
+     * g = B(V) gbase (B - A) with B(V) = 1 / (1 + block_ratio exp(-V /
+     * block_volt)), block_ratio = blockConcentration / scalingConc
+     * (block_volt 0: no block).  Connections only; such a model runs the
+     * per-step kernels. */
+    float release_prob, tau_rec, tau_fac, block_ratio, block_volt;
 } EdenGpuSynapseType;
 
 /*

@@ -179,6 +179,8 @@ extern "C" int eden_port_gpu_run(const EdenGpuModel *m, int64_t n_steps, int32_t
             D.timed_a[b] = g.copy(H.timed_a[b], (size_t)m->n_timed + 1);
             D.timed_b[b] = g.copy(H.timed_b[b], (size_t)m->n_timed + 1);
             D.gr_s[b] = g.copy(H.gr_s[b], (size_t)m->n_graded + 1);
+            D.syn_R[b] = g.copy(H.syn_R[b], (size_t)ns + 1);
+            D.syn_U[b] = g.copy(H.syn_U[b], (size_t)ns + 1);
         }
         D.diag = g.copy(H.diag, (size_t)m->n_comp + 1);
         D.gate_off = g.copy(H.gate_off, (size_t)n_chan + 1);

@@ -106,6 +106,7 @@ typedef struct {
     /* double-buffered state */
     real *v[2], *gate[2], *izh_u[2], *izh_s[2];
     real *syn_a[2], *syn_b[2], *syn_pend[2];
+    real *syn_R[2], *syn_U[2];          /* blockingPlasticSynapse plasticity state */
     unsigned char *trig[2];
     real *pois_ts[2], *pois_isi[2], *pois_a[2], *pois_b[2];
     real *timed_a[2], *timed_b[2];      /* timedSynapticInput synapse states */
@@ -166,7 +167,7 @@ static void dfs_postorder(const int32_t *parent, int n, int32_t *order) {
  * (LEMS_CoreComponents.inc.xml:85-180): expTwo (a = A, b = B), alpha
  * (a = A, b = g) and alphaCurrent (a = J, b = I). */
 static inline PORT_FN void syn_dyn(const EdenGpuSynapseType *st, int init, int fired, real dt, real v, real a,
-                                   real b, real *an, real *bn, real *g, real *i) {
+                                   real b, real *an, real *bn, real *g, real *i, real js) {
     const real e = (real)2.7182818284590451;
     switch (st->kind) {
     case EDEN_SYN_EXPONE:
@@ -200,13 +201,20 @@ static inline PORT_FN void syn_dyn(const EdenGpuSynapseType *st, int init, int f
         }
         return;
     default:
-        *g = st->gbase * (b - a);
+        /* expTwo; a blockingPlasticSynapse scales its conductance by the
+         * voltage block 1 / (1 + ratio exp(-V / volt)) and each event's jump
+         * by the plasticity factor js (LEMS_CoreComponents.inc.xml:231-352) */
+        if (st->kind == EDEN_SYN_BLOCKING_PLASTIC && st->block_volt != 0.0f)
+            *g = ((R(1.0) / (R(1.0) + (real)st->block_ratio * EXP(R(-1.0) * (v / (real)st->block_volt)))) * st->gbase) *
+                 (b - a);
+        else
+            *g = st->gbase * (b - a);
         *i = *g * (st->erev - v);
         if (init) {
             *an = R(0.0); *bn = R(0.0);
         } else if (fired) {
-            *an = a + st->weight_prop * st->waveform_factor;
-            *bn = b + st->weight_prop * st->waveform_factor;
+            *an = a + st->weight_prop * js * st->waveform_factor;
+            *bn = b + st->weight_prop * js * st->waveform_factor;
         } else {
             *an = a + dt * (-a / st->tau_rise);
             *bn = b + dt * (-b / st->tau_decay);
@@ -220,7 +228,7 @@ static inline PORT_FN void syn_dyn(const EdenGpuSynapseType *st, int init, int f
 static inline PORT_FN void synapse_step(const EdenGpuSynapseType *st, int init, real t, real dt,
                                 int spike_in_raw, real delay, real pend, real *pend_next,
                                 real a, real b, real *a_next, real *b_next, real v, real w,
-                                real *iw, real *gw, int *fired) {
+                                real *iw, real *gw, int *fired, real pr, real pu, real *pr_next, real *pu_next) {
     int spike_now = 0;
     real next_next = pend;
     if (!init) {
@@ -233,8 +241,25 @@ static inline PORT_FN void synapse_step(const EdenGpuSynapseType *st, int init, 
     }
     *pend_next = next_next;
     *fired = spike_now;
+    /* a blockingPlasticSynapse's Tsodyks-Markram state, forward Euler, the
+     * event assignments from the step's values overriding
+     * (LEMS_CoreComponents.inc.xml:263-312) */
+    real js = R(1.0);
+    if (st->kind == EDEN_SYN_BLOCKING_PLASTIC && st->tau_rec > 0.0f) {
+        const real p = st->release_prob;
+        if (init) {
+            *pr_next = R(1.0); *pu_next = p;
+        } else if (spike_now) {
+            js = pr * pu;
+            *pr_next = pr * (R(1.0) - pu);
+            *pu_next = st->tau_fac > 0.0f ? pu + p * (R(1.0) - pu) : p;
+        } else {
+            *pr_next = pr + dt * ((R(1.0) - pr) / (real)st->tau_rec);
+            *pu_next = st->tau_fac > 0.0f ? pu + dt * ((p - pu) / (real)st->tau_fac) : p;
+        }
+    }
     real g, i;
-    syn_dyn(st, init, spike_now, dt, v, a, b, a_next, b_next, &g, &i);
+    syn_dyn(st, init, spike_now, dt, v, a, b, a_next, b_next, &g, &i, js);
     *iw = i * w;
     *gw = g * w;
 }
@@ -265,7 +290,7 @@ static inline PORT_FN void poisson_step(const Port *P, int cur, int64_t k, int i
     }
     const EdenGpuSynapseType *st = &m->syn_types[m->pois_type[k]];
     real g, i, an, bn;
-    syn_dyn(st, init, fired, dt, v, P->pois_a[cur][k], P->pois_b[cur][k], &an, &bn, &g, &i);
+    syn_dyn(st, init, fired, dt, v, P->pois_a[cur][k], P->pois_b[cur][k], &an, &bn, &g, &i, R(1.0));
     P->pois_a[nxt][k] = an;
     P->pois_b[nxt][k] = bn;
     *iw = i * m->pois_weight[k];
@@ -289,7 +314,7 @@ static inline PORT_FN void timed_input_step(const Port *P, int cur, int64_t k, i
     }
     const EdenGpuSynapseType *st = &m->syn_types[m->timed_type[k]];
     real g, i, an, bn;
-    syn_dyn(st, init, fired, dt, v, P->timed_a[cur][k], P->timed_b[cur][k], &an, &bn, &g, &i);
+    syn_dyn(st, init, fired, dt, v, P->timed_a[cur][k], P->timed_b[cur][k], &an, &bn, &g, &i, R(1.0));
     P->timed_a[nxt][k] = an;
     P->timed_b[nxt][k] = bn;
     *iw = i * m->timed_weight[k];
@@ -382,7 +407,8 @@ static PORT_FN void target_currents(Port *P, int cur, int64_t tgt, int init, rea
             int fired;
             synapse_step(st, init, t, dt, in, m->syn_delay[s], P->syn_pend[cur][s], &P->syn_pend[nxt][s],
                          P->syn_a[cur][s], P->syn_b[cur][s], &P->syn_a[nxt][s], &P->syn_b[nxt][s],
-                         v, m->syn_weight[s], &iw, &gw, &fired);
+                         v, m->syn_weight[s], &iw, &gw, &fired, P->syn_R[cur][s], P->syn_U[cur][s],
+                         &P->syn_R[nxt][s], &P->syn_U[nxt][s]);
             if (fired) P->syn_fire_count[s]++;
             Ia += iw; Ga += gw;
         }
@@ -706,6 +732,12 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
         P.syn_a[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
         P.syn_b[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
         P.syn_pend[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
+        P.syn_R[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
+        P.syn_U[b] = (real *)calloc((size_t)ns + 1, sizeof(real));
+        for (int64_t q = 0; q < ns; q++) {
+            P.syn_R[b][q] = R(1.0);
+            P.syn_U[b][q] = m->syn_types[m->syn_type[q]].release_prob;
+        }
         P.trig[b] = (unsigned char *)calloc((size_t)ns + 1, 1);
         P.pois_ts[b] = (real *)calloc((size_t)np + 1, sizeof(real));
         P.pois_isi[b] = (real *)calloc((size_t)np + 1, sizeof(real));
@@ -807,7 +839,7 @@ static void port_setup(Port *PP, const EdenGpuModel *m) {
 static void port_free(Port *P) {
     for (int b = 0; b < 2; b++) {
         free(P->v[b]); free(P->gate[b]); free(P->izh_u[b]); free(P->izh_s[b]); free(P->syn_a[b]); free(P->syn_b[b]);
-        free(P->syn_pend[b]); free(P->trig[b]); free(P->pois_ts[b]); free(P->pois_isi[b]);
+        free(P->syn_pend[b]); free(P->syn_R[b]); free(P->syn_U[b]); free(P->trig[b]); free(P->pois_ts[b]); free(P->pois_isi[b]);
         free(P->pois_a[b]); free(P->pois_b[b]); free(P->spiked[b]); free(P->timed_a[b]); free(P->timed_b[b]);
     }
     free(P->diag); free(P->syn_fire_count); free(P->gate_off); free(P->syn_off); free(P->pois_off);

@@ -1,9 +1,10 @@
 """Fixtures of the reference's own validation networks for the GPU.
 
-Reads six of the reference's validation networks
+Reads seven of the reference's validation networks
 (testing/validation_tests/neuroml/LEMS_EdenTest_CoreInputs.xml,
 LEMS_EdenTest_PassiveCompartment.xml, LEMS_EdenTest1.xml,
-LEMS_EdenTest2.xml, LEMS_EdenTest_DomainDecomposition.xml and
+LEMS_EdenTest2.xml, LEMS_EdenTest_DomainDecomposition.xml,
+LEMS_EdenTest_CoreSynapses.xml and
 EdenTest_Extension_CustomSetup.nml with its custom setup file) with this
 package's NeuroML reader,
 writes each lowered network as a model file (eden_gb300/model_file.py) that
@@ -37,6 +38,7 @@ NETWORKS = {
     "edentest2": ("LEMS_EdenTest2.xml", "results1.txt", 1),
     "domain_decomposition": ("LEMS_EdenTest_DomainDecomposition.xml", "results.gen.txt", 4),
     "custom_setup_ext": ("EdenTest_Extension_CustomSetup.nml", "results.gen.txt", 4),
+    "core_synapses": ("LEMS_EdenTest_CoreSynapses.xml", "results.gen.txt", 5),
 }
 
 

@@ -1,4 +1,4 @@
-"""Six of the reference's own validation networks on the GPU, run by the
+"""Seven of the reference's own validation networks on the GPU, run by the
 C++ host program (eden_gb300/host/eden_gpu_host) through the C ABI:
 LEMS_EdenTest_CoreInputs (pulse, weighted pulse, sine, ramp and their DL
 forms, voltage clamps, timed input, spike array and generator),
@@ -9,7 +9,9 @@ and n recorded) and LEMS_EdenTest_DomainDecomposition (14 spiking
 two-compartment cells, gap junctions, expOne connections; compared by the
 reference's box(0.1 ms, 0.5 mV) criterion) and EdenTest_Extension_CustomSetup
 (izhikevichCell instances and pulse inputs customised per instance, expOne
-connections customised per connection, whose halves must be identical),
+connections customised per connection, whose halves must be identical)
+and LEMS_EdenTest_CoreSynapses (every core chemical and continuous
+synapse, the blocking-plastic one with its block and plasticity),
 read by this package's NeuroML reader and lowered into
 model files (tests/golden/make_validation_golden.py), against the
 reference simulator's own output on the same files: every recorded
@@ -33,7 +35,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 @pytest.mark.parametrize("mode", ["batched", "plain"])
 @pytest.mark.parametrize("name,tol_mv", [("core_inputs", 0.01), ("passive_compartment", 0.01), ("edentest1", 0.05),
                                          ("edentest2", 0.05), ("domain_decomposition", None),
-                                         ("custom_setup_ext", 0.1)])
+                                         ("custom_setup_ext", 0.1), ("core_synapses", 0.05)])
 def test_validation_network_on_gpu_matches_reference(name, tol_mv, mode, tmp_path):
     z = np.load(os.path.join(HERE, "golden", f"validation_{name}.npz"))
     traj, ev = str(tmp_path / "traj.txt"), str(tmp_path / "ev.txt")

@@ -33,6 +33,11 @@ from eden_gb300 import lowering, neuroml_io
     # izhikevichCell populations customised per instance by `set cell` and
     # `set input`, and expOne connections by `set synapse`
     ("EdenTest_Extension_CustomSetup.nml", "results.gen.txt", 0.1),
+    # every core synapse on passive cells driven by one HH cell: the chemical
+    # ones (expOne, expTwo, expThree, alpha, alphaCurrent, blockingPlastic
+    # with its voltage block and Tsodyks-Markram plasticity, the PyNN ones)
+    # and the continuous ones (linearGraded, graded, silent, a gap junction)
+    ("LEMS_EdenTest_CoreSynapses.xml", "results.gen.txt", 0.05),
 ])
 def test_oracle_matches_the_reference_on_its_validation_network(name, outfile, tol_mv):
     path = reference_runner.validation_network(name)
