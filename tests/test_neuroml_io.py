@@ -135,3 +135,29 @@ def test_continuous_projections_round_trip(tmp_path):
     for f in ("gap_target", "gap_peer", "gap_conductance", "gap_weight", "graded_target", "graded_peer",
               "graded_params", "graded_weight"):
         np.testing.assert_array_equal(getattr(low2, f), getattr(low, f), err_msg=f)
+
+
+def test_blocking_plastic_synapse_round_trip(tmp_path):
+    """The reference's CoreSynapses network (every core synapse): the
+    blockingPlasticSynapse keeps its block and plasticity mechanisms through
+    a write and a read, and the lowered tables are the same."""
+    import reference_runner
+    path = reference_runner.validation_network("LEMS_EdenTest_CoreSynapses.xml")
+    if path is None:
+        pytest.skip("reference tree not present")
+    spec = neuroml_io.read_lems(path)
+    bp = next(s for s in spec.synapses if s.block)
+    assert bp.plasticity["type"] == "tsodyksMarkramDepFacMechanism" and bp.block["scalingVolt"] == 150.0
+    low = lowering.lower(spec)
+    back = neuroml_io.read_lems(neuroml_io.write_lems(spec, str(tmp_path)))
+    low2 = lowering.lower(back)
+    np.testing.assert_array_equal(low2.syn_types, low.syn_types)
+    for f in ("syn_target", "syn_type", "gap_target", "gap_peer", "graded_target", "graded_params"):
+        np.testing.assert_array_equal(getattr(low2, f), getattr(low, f), err_msg=f)
+    # connections only: a Poisson input on it is refused
+    import copy
+    bad = copy.deepcopy(spec)
+    from eden_gb300.network import PoissonInputs
+    bad.poissons.append(PoissonInputs("*", bp.name, 10.0, np.array([1]), np.array([0])))
+    with pytest.raises(ValueError, match="connections only"):
+        lowering.lower(bad)
